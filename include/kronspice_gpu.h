@@ -1,0 +1,273 @@
+/*
+ * kronspice_gpu.h — C ABI of the GB300 batched circuit-solve engine.
+ *
+ * The engine replaces, for a whole batch of circuits in one call, the
+ * per-circuit hot path of kronspice's analysis package:
+ *
+ *   analysis.OP            analysis/op.go:331        -> ks_op
+ *   (*Sim).dcSolve         analysis/newton.go:95     -> ks_op (fallback chain on device)
+ *   analysis.Tran          analysis/tran.go:70       -> ks_tran
+ *   analysis.DC            analysis/dc.go:51         -> ks_op with per-point source overrides
+ *   analysis.Options       analysis/op.go:22-62      -> ks_options
+ *   analysis.TranSpec/TranOptions analysis/tran.go:26-40 -> ks_tran_spec
+ *   solver sentinels       solver/matrix.go:15-20,
+ *   analysis sentinels     analysis/newton.go:20, analysis/tran.go:18-22 -> ks_status
+ *
+ * A Go caller binds these through cgo; a Python caller
+ * through ctypes (kronspice_gb300/_lib.py).  Every pointer argument is plain
+ * host memory unless the name ends in _dev (device memory).  No function keeps
+ * a caller pointer after it returns.  Every function returns a ks_rc.
+ *
+ * Circuits enter as a topology (element kinds and node connections, shared by
+ * every circuit of a batch) plus one value vector per circuit (element values
+ * and model parameters).  This is the "one call x N circuits" boundary: the
+ * symbolic work (unknown layout, stamp map, matrix pattern, ordering) is done
+ * once per topology on the host, the numeric work for all circuits on the GPU.
+ */
+#ifndef KRONSPICE_GPU_H
+#define KRONSPICE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes of the API calls ------------------------------------- */
+typedef enum {
+  KS_OK = 0,
+  KS_EINVAL = -1,   /* bad argument, bad topology or value vector            */
+  KS_ENOMEM = -2,   /* device or host allocation failed                      */
+  KS_ECUDA = -3,    /* a CUDA call failed (message in ks_last_error)         */
+  KS_EUNSUPPORTED = -4, /* element or analysis not built into this engine    */
+  KS_EVALIDATE = -5 /* structural validation failed (ks_validate's message)  */
+} ks_rc;
+
+/* ---- per-circuit status: 1:1 with the Go sentinels --------------------- */
+typedef enum {
+  KS_STATUS_OK = 0,
+  KS_STATUS_SINGULAR = 1,          /* solver.ErrSingularMatrix     solver/matrix.go:17 */
+  KS_STATUS_NONFINITE = 2,         /* solver.ErrNonFinite          solver/matrix.go:19 */
+  KS_STATUS_NO_CONVERGENCE = 3,    /* analysis.ErrNoConvergence    analysis/newton.go:20 */
+  KS_STATUS_TIMESTEP_TOO_SMALL = 4,/* analysis.ErrTimestepTooSmall analysis/tran.go:19 */
+  KS_STATUS_TOO_MANY_STEPS = 5,    /* analysis.ErrTooManySteps     analysis/tran.go:20 */
+  KS_STATUS_INTERRUPTED = 6,       /* context deadline / cancel    analysis/op.go:81-89 */
+  KS_STATUS_NOT_RUN = 7            /* circuit was not solved (earlier error)          */
+} ks_status;
+
+/* ---- element kinds (circuit/circuit.go:41-99) --------------------------- */
+typedef enum {
+  KS_ELEM_R = 1,  /* resistor          device/passive.go:32   */
+  KS_ELEM_C = 2,  /* capacitor         device/reactive.go:24  */
+  KS_ELEM_L = 3,  /* inductor          device/reactive.go:198 */
+  KS_ELEM_V = 4,  /* voltage source    device/source.go:77    */
+  KS_ELEM_I = 5,  /* current source    device/source.go:133   */
+  KS_ELEM_D = 6,  /* junction diode    device/diode.go:61     */
+  KS_ELEM_Q = 7,  /* Gummel-Poon BJT   device/bjt.go:78       */
+  KS_ELEM_M = 8   /* MOSFET level 1-3  device/mosfet.go:43    */
+} ks_elem_kind;
+
+/* source waveforms (circuit/circuit.go WaveKind; device/waveform.go) */
+typedef enum {
+  KS_WAVE_NONE = 0,
+  KS_WAVE_PULSE = 1,
+  KS_WAVE_SIN = 2,
+  KS_WAVE_EXP = 3,
+  KS_WAVE_PWL = 4
+} ks_wave_kind;
+
+/* element flags */
+enum {
+  KS_F_HAS_DC = 1 << 0,   /* source: DC value given explicitly (Element.HasDC) */
+  KS_F_HAS_IC = 1 << 1,   /* C, L: initial condition given (Element.HasIC)      */
+  KS_F_HAS_BV = 1 << 2,   /* diode: BV given (DiodeParams.HasBV)                */
+  KS_F_PTYPE = 1 << 3,    /* BJT: PNP; MOSFET: PMOS                             */
+  KS_F_INT_A = 1 << 4,    /* diode: internal anode node (RS > 0)                */
+  KS_F_INT_C = 1 << 5,    /* BJT: internal collector (RC > 0)                   */
+  KS_F_INT_B = 1 << 6,    /* BJT: internal base (RB > 0)                        */
+  KS_F_INT_E = 1 << 7,    /* BJT: internal emitter (RE > 0)                     */
+  KS_F_INT_D = 1 << 8,    /* MOSFET: internal drain (conductance 1/RD > 0)      */
+  KS_F_INT_S = 1 << 9     /* MOSFET: internal source (conductance 1/RS > 0)     */
+};
+
+/*
+ * One circuit element.  node[] holds circuit node indices (0 = ground):
+ *   R C L V I D : node[0] = n+ (anode), node[1] = n- (cathode)
+ *   Q (BJT)     : node[0] = collector, node[1] = emitter, node[2] = base,
+ *                 node[3] = substrate (0 = ground when absent)
+ *                 -- Element.Nodes/Extra of circuit/builder.go:101
+ *   M (MOSFET)  : node[0] = drain, node[1] = source, node[2] = gate,
+ *                 node[3] = bulk    -- circuit/builder.go:108
+ * param is the offset of the element's block in the per-circuit value vector;
+ * the block layouts are the KS_*_P_* enums below.
+ */
+typedef struct {
+  int32_t kind;
+  int32_t node[4];
+  int32_t flags;
+  int32_t level;     /* MOSFET level 1..3                                    */
+  int32_t wave;      /* source waveform kind                                 */
+  int32_t nargs;     /* source waveform arguments given (PULSE 2..7, SIN 2..6, EXP 2..6, PWL even) */
+  int32_t param;     /* offset of the element's value block                  */
+  uint64_t given;    /* MOSFET: bit KS_M_P_x set when model parameter x was given */
+} ks_element;
+
+typedef struct {
+  int32_t n_nodes;   /* circuit nodes including ground                      */
+  int32_t n_elem;
+  int32_t n_values;  /* length of each circuit's value vector               */
+  int32_t reserved;
+  const ks_element* elem;
+} ks_topology;
+
+/* value blocks -------------------------------------------------------------*/
+/* R: [R]   C: [C, IC]   L: [L, IC] */
+enum { KS_RCL_P_VALUE = 0, KS_RCL_P_IC = 1, KS_RCL_NP = 2 };
+/* V, I: [dc, ac_mag, ac_phase_deg, arg0 .. arg(nargs-1)] */
+enum { KS_SRC_P_DC = 0, KS_SRC_P_ACMAG = 1, KS_SRC_P_ACPHASE = 2, KS_SRC_P_ARGS = 3 };
+/* D: DiodeParams of device/diode.go:23 after defaults and area scaling */
+enum {
+  KS_D_P_IS, KS_D_P_N, KS_D_P_RS, KS_D_P_CJO, KS_D_P_VJ, KS_D_P_M, KS_D_P_TT,
+  KS_D_P_BV, KS_D_P_IBV, KS_D_P_FC, KS_D_NP
+};
+/* Q: BJTParams of device/bjt.go:17 after defaults, RBM <= RB, SUBS and area */
+enum {
+  KS_Q_P_IS, KS_Q_P_BF, KS_Q_P_NF, KS_Q_P_VAF, KS_Q_P_IKF, KS_Q_P_ISE, KS_Q_P_NE,
+  KS_Q_P_BR, KS_Q_P_NR, KS_Q_P_VAR, KS_Q_P_IKR, KS_Q_P_ISC, KS_Q_P_NC,
+  KS_Q_P_RB, KS_Q_P_IRB, KS_Q_P_RBM, KS_Q_P_RE, KS_Q_P_RC,
+  KS_Q_P_CJE, KS_Q_P_VJE, KS_Q_P_MJE, KS_Q_P_TF, KS_Q_P_XTF, KS_Q_P_VTF,
+  KS_Q_P_ITF, KS_Q_P_CJC, KS_Q_P_VJC, KS_Q_P_MJC, KS_Q_P_XCJC, KS_Q_P_TR,
+  KS_Q_P_CJS, KS_Q_P_VJS, KS_Q_P_MJS, KS_Q_P_FC, KS_Q_P_ISS, KS_Q_P_NS,
+  KS_Q_P_SUBS, KS_Q_NP
+};
+/* M: mosParams of device/mosfet.go:97 (model defaults of :140-149 applied)
+ * followed by the instance parameters */
+enum {
+  KS_M_P_VTO, KS_M_P_KP, KS_M_P_GAMMA, KS_M_P_PHI, KS_M_P_LAMBDA, KS_M_P_RD,
+  KS_M_P_RS, KS_M_P_CBD, KS_M_P_CBS, KS_M_P_IS, KS_M_P_PB, KS_M_P_CGSO,
+  KS_M_P_CGDO, KS_M_P_CGBO, KS_M_P_RSH, KS_M_P_CJ, KS_M_P_MJ, KS_M_P_CJSW,
+  KS_M_P_MJSW, KS_M_P_JS, KS_M_P_TOX, KS_M_P_NSUB, KS_M_P_NSS, KS_M_P_NFS,
+  KS_M_P_TPG, KS_M_P_XJ, KS_M_P_LD, KS_M_P_UO, KS_M_P_UCRIT, KS_M_P_UEXP,
+  KS_M_P_UTRA, KS_M_P_VMAX, KS_M_P_NEFF, KS_M_P_FC, KS_M_P_DELTA,
+  KS_M_P_THETA, KS_M_P_ETA, KS_M_P_KAPPA, KS_M_P_WD,
+  KS_M_P_L, KS_M_P_W, KS_M_P_AD, KS_M_P_AS, KS_M_P_PD, KS_M_P_PS,
+  KS_M_P_NRD, KS_M_P_NRS, KS_M_P_MULT, KS_M_NP
+};
+
+/* ---- analysis options (analysis/op.go:22-62, defaults :91-110) ---------- */
+enum { KS_PREC_FP64 = 0, KS_PREC_MIXED = 1 };
+enum { KS_BACKEND_AUTO = 0, KS_BACKEND_DENSE = 1, KS_BACKEND_SPARSE = 2 };
+
+typedef struct {
+  double reltol;   /* <= 0: 1e-3  */
+  double abstol;   /* <= 0: 1e-12 */
+  double vntol;    /* <= 0: 1e-6  */
+  double gmin;     /* <= 0: 1e-12 */
+  int32_t itl1;    /* <= 0: 100   */
+  int32_t itl4;    /* <= 0: 10    */
+  int32_t no_gmin_stepping;
+  int32_t no_source_stepping;
+  int32_t no_pseudo_transient;
+  int32_t precision;      /* KS_PREC_FP64 (plain) or KS_PREC_MIXED          */
+  int32_t backend;        /* linear solver of the CPU oracle               */
+  int32_t max_iter_total; /* device-side bound on all Newton iterations of one
+                             circuit, fallbacks included (0: unbounded by it) */
+  double deadline_s;      /* > 0: per-call wall-clock limit, the context
+                             deadline of Options.Context (KS_STATUS_INTERRUPTED) */
+} ks_options;
+
+/* ---- transient request (analysis/tran.go:26-59) ------------------------- */
+enum { KS_METHOD_BE = 1, KS_METHOD_TRAP = 2 };
+
+typedef struct {
+  double step, stop, start, max_step; /* TranSpec                              */
+  int32_t uic;
+  int32_t method;     /* 0: trapezoidal                                       */
+  int32_t fixed_step; /* 1: steps of exactly `step`, no LTE control, no
+                         breakpoint landing (the batch mode of the configs)   */
+  int32_t max_steps;  /* <= 0: 1,000,000                                      */
+  double chgtol;      /* <= 0: 1e-14 */
+  double trtol;       /* <= 0: 7     */
+  double min_step;    /* <= 0: 1e-12 * stop */
+} ks_tran_spec;
+
+/* ---- library ------------------------------------------------------------ */
+const char* ks_version(void);
+/* Message of the last failed call on this host thread ("" if none). */
+const char* ks_last_error(void);
+
+/*
+ * Structural check of one circuit, the equivalent of circuit.Validate
+ * (circuit/circuit.go:368, checkPaths :704-804) for the element kinds above.
+ * Returns KS_OK or KS_EVALIDATE with the reason (ErrFloatingNode, ErrBadValue,
+ * ErrSelfConnected, ...) in ks_last_error.  transient != 0 gives
+ * ValidateTransient (capacitors count as paths, for UIC).
+ */
+int ks_validate(const ks_topology* topo, const double* values, int transient);
+
+/* Number of MNA unknowns of the topology (node voltages, branch currents,
+ * internal nodes: the layout of device/device.go:36-100) and, if is_voltage is
+ * not NULL, whether each unknown is a voltage (1) or a current (0). */
+int ks_unknowns(const ks_topology* topo, int32_t* n_unknowns, int32_t* is_voltage);
+
+/* ---- plans and batches --------------------------------------------------- */
+typedef struct ks_plan ks_plan;   /* one topology, symbolic analysis done   */
+typedef struct ks_batch ks_batch; /* n circuits of one plan, values on device */
+
+/* Analyse a topology: unknown layout, stamp map, matrix pattern.  The plan
+ * owns copies of everything it needs. */
+int ks_plan_create(const ks_topology* topo, ks_plan** out);
+void ks_plan_destroy(ks_plan* plan);
+int ks_plan_info(const ks_plan* plan, int32_t* n_unknowns, int32_t* n_values, int32_t* n_state);
+
+/* Allocate device storage for n_circ circuits of a plan and upload their
+ * value vectors (row-major [n_circ][n_values], host memory). */
+int ks_batch_create(ks_plan* plan, int32_t n_circ, const double* values, ks_batch** out);
+/* Replace the value vectors of an existing batch (same n_circ); host memory,
+ * or device memory when values_are_device != 0 (then `values` is a device
+ * pointer to [n_circ][n_values] doubles). */
+int ks_batch_set_values(ks_batch* b, const double* values, int values_are_device, void* stream);
+void ks_batch_destroy(ks_batch* b);
+
+/*
+ * DC operating point of every circuit of the batch (analysis.OP for each):
+ * Newton with the SPICE3 convergence test, then gmin stepping, source
+ * stepping and pseudo-transient continuation on the circuits that fail.
+ *   x0        NULL (cold start: InitJct) or [n_circ][n_unknowns] starting
+ *             points (Options.NodeSet semantics: device limiting state is
+ *             seeded from the guess, analysis/newton.go:221-243)
+ *   out_x     [n_circ][n_unknowns] solutions
+ *   out_status[n_circ] ks_status, out_iters[n_circ] Newton iterations used
+ * All host buffers; the call returns when the results are in them.
+ */
+int ks_op(ks_batch* b, const ks_options* opt, const double* x0, double* out_x,
+          int32_t* out_status, int32_t* out_iters, void* stream);
+
+/* Same, on device buffers, asynchronous on `stream` (NULL: the batch's own
+ * stream).  x0_dev may be NULL. */
+int ks_op_async(ks_batch* b, const ks_options* opt, const double* x0_dev, double* out_x_dev,
+                int32_t* out_status_dev, int32_t* out_iters_dev, void* stream);
+
+/*
+ * Transient analysis of every circuit of the batch (analysis.Tran for each).
+ * Fixed-step mode (spec->fixed_step) records n_points = round((stop)/step)+1
+ * points t_k = k*step for every circuit:
+ *   out_wave  [n_points][n_circ][n_unknowns]  (NULL: not recorded)
+ * Adaptive mode records up to `capacity` accepted points per circuit:
+ *   out_time  [n_circ][capacity], out_wave [n_circ][capacity][n_unknowns],
+ *   out_npts  [n_circ]
+ * out_status[n_circ], out_steps[n_circ] accepted steps, out_iters[n_circ]
+ * total Newton iterations.
+ */
+int ks_tran(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt,
+            int32_t capacity, double* out_time, double* out_wave, int32_t* out_npts,
+            int32_t* out_status, int32_t* out_steps, int32_t* out_iters, void* stream);
+
+/* Number of points a fixed-step transient records. */
+int ks_tran_points(const ks_tran_spec* spec, int32_t* n_points);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KRONSPICE_GPU_H */

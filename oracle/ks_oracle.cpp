@@ -1,0 +1,541 @@
+// ks_oracle.cpp — CPU FP64 oracle: simulation driver and C API (test infrastructure).
+//
+// Restates the reference's analysis package for the hot path:
+//   (*Sim).solve            analysis/op.go:289-322
+//   (*Sim).newton/converged analysis/newton.go:36-82
+//   dcSolve + fallbacks     analysis/newton.go:95-311
+//   (*Sim).OP               analysis/op.go:340-357
+//   DC                      analysis/dc.go:51-130
+//   (*Sim).tran             analysis/tran.go:95-243 (and the fixed-step mode of
+//                           ks_tran_spec: steps of exactly `step`, no LTE control,
+//                           no breakpoint landing, h/8 retry on Newton failure)
+// Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
+#include "ks_oracle.h"
+#include "oracle_devices.hpp"
+#include "oracle_bjt.hpp"
+#include "oracle_mos.hpp"
+
+#include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <memory>
+#include <thread>
+
+namespace kso {
+
+enum Err { E_OK = 0, E_SINGULAR = KS_STATUS_SINGULAR, E_NONFINITE = KS_STATUS_NONFINITE,
+           E_NOCONV = KS_STATUS_NO_CONVERGENCE, E_TSTEP = KS_STATUS_TIMESTEP_TOO_SMALL,
+           E_TOOMANY = KS_STATUS_TOO_MANY_STEPS, E_INTR = KS_STATUS_INTERRUPTED, E_BAD = 100 };
+
+struct Opts {  // analysis.Options with defaults, analysis/op.go:91-110
+  double reltol, abstol, vntol, gmin;
+  int itl1, itl4;
+  bool noGmin, noSource, noPT;
+  int backend;
+  double deadline;  // absolute steady-clock seconds, 0 = none
+  explicit Opts(const ks_options* o) {
+    reltol = o && o->reltol > 0 ? o->reltol : 1e-3;
+    abstol = o && o->abstol > 0 ? o->abstol : 1e-12;
+    vntol = o && o->vntol > 0 ? o->vntol : 1e-6;
+    gmin = o && o->gmin > 0 ? o->gmin : 1e-12;
+    itl1 = o && o->itl1 > 0 ? o->itl1 : 100;
+    itl4 = o && o->itl4 > 0 ? o->itl4 : 10;
+    noGmin = o && o->no_gmin_stepping; noSource = o && o->no_source_stepping; noPT = o && o->no_pseudo_transient;
+    backend = o ? o->backend : 0;
+    deadline = 0;
+    if (o && o->deadline_s > 0) deadline = now() + o->deadline_s;
+  }
+  static double now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+  }
+  bool interrupted() const { return deadline > 0 && now() > deadline; }
+};
+
+struct Sim {
+  std::vector<std::unique_ptr<Device>> devs;
+  std::vector<int> reactive, nonlin, breakp;
+  std::vector<char> isV;
+  int n = 0, numNodes = 0;
+  std::vector<double> x, xOld, rhs, ptPrev;
+  double diagGmin = 0, ptG = 0;
+  bool warm = false;
+  std::unique_ptr<Matrix> M;
+  LoadCtx lc;
+  int iters = 0;  // total Newton iterations (solves)
+  std::string msg;
+
+  // newSim, analysis/op.go:160-208
+  int build(const ks_topology* t, const double* v, double step, double stop, int backend) {
+    numNodes = t->n_nodes;
+    for (int e = 0; e < t->n_elem; e++) {
+      const ks_element& el = t->elem[e];
+      const double* p = v + el.param;
+      Device* d = nullptr;
+      switch (el.kind) {
+        case KS_ELEM_R: { auto* r = new Resistor(p[0]); r->nodes[0] = el.node[0]; r->nodes[1] = el.node[1]; d = r; break; }
+        case KS_ELEM_C: { auto* c = new Capacitor(p[0], p[1], el.flags & KS_F_HAS_IC); c->nodes[0] = el.node[0]; c->nodes[1] = el.node[1]; d = c; break; }
+        case KS_ELEM_L: { auto* l = new Inductor(p[0], p[1], el.flags & KS_F_HAS_IC); l->nodes[0] = el.node[0]; l->nodes[1] = el.node[1]; d = l; break; }
+        case KS_ELEM_V: case KS_ELEM_I: {
+          SourceValue sv;
+          sv.dc = p[KS_SRC_P_DC]; sv.hasDC = el.flags & KS_F_HAS_DC; sv.wkind = el.wave;
+          sv.args.assign(p + KS_SRC_P_ARGS, p + KS_SRC_P_ARGS + el.nargs);
+          if (el.kind == KS_ELEM_V) { auto* s = new VSource(); s->src = sv; s->nodes[0] = el.node[0]; s->nodes[1] = el.node[1]; d = s; }
+          else { auto* s = new ISource(); s->src = sv; s->nodes[0] = el.node[0]; s->nodes[1] = el.node[1]; d = s; }
+          break;
+        }
+        case KS_ELEM_D: { auto* dd = new Diode(p, el.flags & KS_F_HAS_BV); dd->nodes[0] = el.node[0]; dd->nodes[1] = el.node[1]; d = dd; break; }
+        case KS_ELEM_Q: d = new BJT(p, el.flags & KS_F_PTYPE, el.node[0], el.node[1], el.node[2], el.node[3]); break;
+        case KS_ELEM_M: {
+          auto* m = new MOSFET(p, el.given, el.level, el.flags & KS_F_PTYPE, el.node[0], el.node[1], el.node[2], el.node[3]);
+          if (m->bad) { delete m; msg = "device: unsupported element kind: MOSFET parameters"; return E_BAD; }
+          d = m; break;
+        }
+        default: msg = "device: unsupported element kind"; return E_BAD;
+      }
+      devs.emplace_back(d);
+    }
+    SetupCtx sc;
+    sc.numNodes = numNodes; sc.step = step; sc.stop = stop;
+    for (size_t i = 0; i < devs.size(); i++) {
+      devs[i]->setup(sc);
+      if (devs[i]->reactive()) reactive.push_back((int)i);
+      if (devs[i]->nonlinear()) nonlin.push_back((int)i);
+      if (devs[i]->breakpointer()) breakp.push_back((int)i);
+    }
+    n = sc.size();
+    for (auto& d : devs) d->n = n;
+    int be = backend == KS_BACKEND_AUTO ? (n < 30 ? KS_BACKEND_DENSE : KS_BACKEND_SPARSE) : backend;
+    if (be == KS_BACKEND_SPARSE) M.reset(new Sparse(n)); else M.reset(new Dense(n));
+    x.assign(n, 0); xOld.assign(n, 0); rhs.assign(n, 0);
+    isV.assign(n, 0);
+    for (int i = 0; i < numNodes - 1; i++) isV[i] = 1;
+    for (int i : sc.internal) isV[i] = 1;
+    lc.M = M.get(); lc.rhs = rhs.data(); lc.n = n; lc.X = xOld.data(); lc.gmin = 1e-12;
+    return E_OK;
+  }
+
+  int solve() {  // analysis/op.go:289-322
+    iters++;
+    xOld = x;
+    lc.X = xOld.data();
+    M->clear();
+    std::fill(rhs.begin(), rhs.end(), 0.0);
+    for (auto& d : devs) d->load(lc);
+    if (ptG > 0) {
+      double g = ptG;
+      for (int i = 0; i < n; i++) {
+        if (isV[i]) { M->add(i, i, g); rhs[i] += g * ptPrev[i]; }
+        else { M->add(i, i, -g); rhs[i] -= g * ptPrev[i]; }
+      }
+    }
+    if (diagGmin > 0) for (int i = 0; i < n; i++) if (isV[i]) M->add(i, i, diagGmin);
+    std::string m;
+    int e = M->solve(rhs.data(), x.data(), &m);
+    if (e == SOLVE_SINGULAR) { msg = "solver: singular matrix" + m; return E_SINGULAR; }
+    if (e == SOLVE_NONFINITE) { msg = "solver: non-finite value in system"; return E_NONFINITE; }
+    return E_OK;
+  }
+  void accept(double t, int mode) { for (auto& d : devs) d->accept(x.data(), t, mode); }
+
+  bool converged(const Opts& o) {  // analysis/newton.go:59-82
+    for (int i : nonlin) if (devs[i]->limited()) return false;
+    for (int i = 0; i < n; i++) {
+      double tol = isV[i] ? o.vntol : o.abstol;
+      tol += o.reltol * std::max(std::fabs(x[i]), std::fabs(xOld[i]));
+      if (std::fabs(x[i] - xOld[i]) > tol) return false;
+    }
+    for (int i : nonlin) if (!devs[i]->convTest(x.data(), o.reltol, o.abstol)) return false;
+    return true;
+  }
+  static bool retryable(int e) { return e == E_NOCONV || e == E_NONFINITE || e == E_SINGULAR; }
+
+  int newton(int maxIter, const Opts& o) {  // analysis/newton.go:36-57
+    lc.gmin = o.gmin;
+    for (int it = 0; it < maxIter; it++) {
+      if (o.interrupted()) { msg = "analysis interrupted: context deadline exceeded"; return E_INTR; }
+      int e = solve();
+      if (e) return e;
+      if (nonlin.empty()) return E_OK;
+      if (lc.initJct) { lc.initJct = false; continue; }
+      if (converged(o)) return E_OK;
+    }
+    char buf[96]; snprintf(buf, sizeof buf, "analysis: no convergence after %d iterations", maxIter);
+    msg = buf;
+    return E_NOCONV;
+  }
+
+  int dcSolve(const Opts& o, const double* nodeset) {  // analysis/newton.go:95-128
+    lc.initJct = !warm;
+    if (!warm && nodeset) {  // applyNodeSet, analysis/newton.go:221-243
+      std::fill(x.begin(), x.end(), 0.0);
+      for (int i = 0; i < numNodes - 1; i++) x[i] = nodeset[i];
+      for (int i : nonlin) devs[i]->accept(x.data(), 0, ModeOP);
+      lc.initJct = false;
+    }
+    int err = newton(o.itl1, o);
+    if (err == E_OK || nonlin.empty() || !retryable(err)) {
+      warm = warm || err == E_OK;
+      return err;
+    }
+    std::string first = msg;
+    int firstErr = err;
+    if (!o.noGmin) { err = gminStepping(o); if (err == E_OK) { warm = true; return E_OK; } }
+    if (!o.noSource) { err = sourceStepping(o); if (err == E_OK) { warm = true; return E_OK; } }
+    if (!o.noPT) { err = pseudoTransient(o); if (err == E_OK) { warm = true; return E_OK; } }
+    msg = first + " (fallbacks failed: " + msg + ")";
+    return firstErr;
+  }
+
+  int gminStepping(const Opts& o) {  // analysis/newton.go:134-176
+    struct Reset { Sim* s; ~Reset() { s->diagGmin = 0; } } reset{this};
+    std::vector<double> save(n, 0.0);
+    std::fill(x.begin(), x.end(), 0.0);
+    lc.initJct = true;
+    double g = 1e-2, factor = 10.0;
+    bool ok = false;
+    for (int k = 0; k < 200; k++) {
+      diagGmin = g;
+      int err = newton(o.itl1, o);
+      if (err == E_OK) {
+        save = x;
+        if (g == 0) return E_OK;
+        ok = true;
+        factor = std::min(factor * std::sqrt(factor), 10.0);
+        if (g / factor < o.gmin) g = 0; else g /= factor;
+        continue;
+      } else if (!retryable(err)) return err;
+      if (!ok) { msg = "analysis: no convergence: gmin stepping failed at its first step"; return E_NOCONV; }
+      x = save;
+      double prev = g * factor;
+      if (g == 0) prev = o.gmin;
+      factor = std::sqrt(factor);
+      if (factor < 1.00005) {
+        char buf[128]; snprintf(buf, sizeof buf, "analysis: no convergence: gmin stepping stalled at %g S", prev);
+        msg = buf; return E_NOCONV;
+      }
+      g = prev / factor;
+    }
+    msg = "analysis: no convergence: gmin stepping exceeded 200 steps";
+    return E_NOCONV;
+  }
+
+  int sourceStepping(const Opts& o) {  // analysis/newton.go:180-214
+    struct Reset { Sim* s; ~Reset() { s->lc.srcStepping = false; s->lc.srcFact = 0; } } reset{this};
+    std::vector<double> save(n, 0.0);
+    std::fill(x.begin(), x.end(), 0.0);
+    lc.srcStepping = true;
+    double done = 0.0, step = 0.1;
+    lc.srcFact = 0;
+    int err = newton(o.itl1, o);
+    if (err) return err;
+    save = x;
+    for (int k = 0; k < 1000; k++) {
+      double f = std::min(done + step, 1.0);
+      lc.srcFact = f;
+      err = newton(o.itl1, o);
+      if (err == E_OK) {
+        if (f == 1) return E_OK;
+        save = x;
+        done = f; step = std::min(step * 1.5, 0.5);
+        continue;
+      } else if (!retryable(err)) return err;
+      x = save;
+      step /= 2;
+      if (step < 1e-3) {
+        char buf[128]; snprintf(buf, sizeof buf, "analysis: no convergence: source stepping stalled at %.4g of full value", done);
+        msg = buf; return E_NOCONV;
+      }
+    }
+    msg = "analysis: no convergence: source stepping exceeded 1000 steps";
+    return E_NOCONV;
+  }
+
+  int pseudoTransient(const Opts& o) {  // analysis/newton.go:260-311
+    struct Reset { Sim* s; ~Reset() { s->ptG = 0; } } reset{this};
+    ptPrev.assign(n, 0.0);
+    std::fill(x.begin(), x.end(), 0.0);
+    lc.initJct = true;
+    double h = 1e-6;
+    int quiet = 0;
+    for (int k = 0; k < 2000; k++) {
+      ptG = 1 / h;
+      int err = newton(o.itl1, o);
+      if (err) {
+        if (!retryable(err)) return err;
+        x = ptPrev;
+        h /= 4;
+        if (h < 1e-15) { msg = "analysis: no convergence: pseudo-transient step too small"; return E_NOCONV; }
+        continue;
+      }
+      bool moved = false;
+      for (int i = 0; i < n; i++) {
+        double tol = isV[i] ? o.vntol : o.abstol;
+        if (std::fabs(x[i] - ptPrev[i]) > o.reltol * std::fabs(x[i]) + tol) { moved = true; break; }
+      }
+      ptPrev = x;
+      if (!moved) quiet++; else quiet = 0;
+      if (quiet >= 3 && h >= 1e6) { ptG = 0; return newton(o.itl1, o); }
+      h = std::min(h * 2, 1e12);
+    }
+    msg = "analysis: no convergence: pseudo-transient exceeded 2000 steps";
+    return E_NOCONV;
+  }
+
+  int op(const Opts& o, const double* nodeset) {  // analysis/op.go:340-357 (ledger not built)
+    lc.mode = ModeOP; lc.time = 0;
+    int e = dcSolve(o, nodeset);
+    if (e) return e;
+    accept(0, ModeOP);
+    return E_OK;
+  }
+
+  double nextBreakpoint(double t) {  // analysis/tran.go:233-243
+    double nb = kInf;
+    for (int i : breakp) nb = std::min(nb, devs[i]->nextBreakpoint(t));
+    return nb;
+  }
+
+  struct Rec {
+    int cap = 0, npts = 0;
+    double *t = nullptr, *x = nullptr, *i = nullptr;
+    int n = 0, ne = 0;
+    double start = 0;
+  };
+  void record(Rec& r, double t) {
+    if (t < r.start) return;
+    if (r.npts >= r.cap) { r.npts++; return; }
+    int k = r.npts++;
+    if (r.t) r.t[k] = t;
+    if (r.x) for (int j = 0; j < n; j++) r.x[(size_t)k * n + j] = x[j];
+    if (r.i) for (int j = 0; j < (int)devs.size(); j++) r.i[(size_t)k * devs.size() + j] = devs[j]->current(x.data());
+  }
+
+  // analysis/tran.go:95-231 (adaptive) and the fixed-step mode.
+  int tran(const ks_tran_spec& sp, const Opts& o, Rec& rec, int* stepsOut) {
+    int method = sp.method == KS_METHOD_BE ? BE : TRAP;
+    double chgtol = sp.chgtol > 0 ? sp.chgtol : 1e-14, trtol = sp.trtol > 0 ? sp.trtol : 7;
+    double minStep = sp.min_step > 0 ? sp.min_step : 1e-12 * sp.stop;
+    int maxSteps = sp.max_steps > 0 ? sp.max_steps : 1000000;
+    bool fixed = sp.fixed_step != 0;
+    double maxStep = sp.max_step;
+    if (maxStep == 0) maxStep = std::min(sp.step, (sp.stop - sp.start) / 50);
+    if (fixed) maxStep = sp.step;
+    rec.start = sp.start;
+    if (sp.uic) {
+      for (auto& d : devs) d->setInitialCondition();
+      lc.mode = ModeUICInit; lc.time = 0; lc.initJct = true;
+      int e = newton(o.itl1, o);
+      if (e) { msg = "initial conditions: " + msg; return e; }
+      accept(0, ModeUICInit);
+    } else {
+      lc.mode = ModeTranOP; lc.time = 0;
+      int e = dcSolve(o, nullptr);
+      if (e) { msg = "transient operating point: " + msg; return e; }
+      accept(0, ModeTranOP);
+    }
+    record(rec, 0);
+    TruncCtx tc{0, 0, BE, o.reltol, o.abstol, o.vntol, chgtol, trtol};
+    double t = 0;
+    double h = fixed ? sp.step : std::min(maxStep, std::min(sp.step, sp.stop / 100)) / 10;
+    int order = BE;
+    int accepted = 0;
+    double eps = 1e-12 * sp.stop;
+    std::vector<double> xAcc = x;
+    long kgrid = 1;
+    long ngrid = fixed ? std::lround(sp.stop / sp.step) : 0;
+    auto reject = [&](double hNew) -> int {
+      x = xAcc;
+      if (hNew < minStep) {
+        char buf[128]; snprintf(buf, sizeof buf, "analysis: timestep too small: %.3g s at t = %g s", hNew, t);
+        msg = buf; return E_TSTEP;
+      }
+      return E_OK;
+    };
+    while (fixed ? kgrid <= ngrid : t < sp.stop - eps) {
+      if (o.interrupted()) { msg = "analysis interrupted: context deadline exceeded"; *stepsOut = accepted; return E_INTR; }
+      if (accepted >= maxSteps) {
+        char buf[128]; snprintf(buf, sizeof buf, "analysis: too many time steps: %d accepted steps at t = %g s", accepted, t);
+        msg = buf; *stepsOut = accepted; return E_TOOMANY;
+      }
+      double tn;
+      bool hitBreak = false, onGrid = false;
+      if (fixed) {
+        double target = double(kgrid) * sp.step;
+        tn = t + h;
+        if (tn >= target - eps) { tn = target; onGrid = true; }
+      } else {
+        double nb = nextBreakpoint(t);
+        tn = t + h;
+        if (tn >= nb - eps) { tn = nb; hitBreak = true; }
+        if (tn >= sp.stop - eps) { tn = sp.stop; hitBreak = false; }
+      }
+      h = tn - t;
+      lc.mode = ModeTran; lc.time = tn; lc.h = h; lc.method = order;
+      int e = newton(o.itl4, o);
+      if (e) {
+        if (!retryable(e) || nonlin.empty()) {
+          char buf[64]; snprintf(buf, sizeof buf, "t = %g s: ", tn);
+          msg = buf + msg; *stepsOut = accepted; return e;
+        }
+        h /= 8;
+        int r = reject(h);
+        if (r) { msg += " (Newton did not converge: analysis: no convergence)"; *stepsOut = accepted; return r; }
+        order = BE;
+        continue;
+      }
+      double proposal = kInf;
+      if (!fixed) {
+        tc.time = tn; tc.h = h; tc.method = order;
+        for (int i : reactive) proposal = std::min(proposal, devs[i]->truncate(x.data(), tc));
+        if (proposal < 0.9 * h) {
+          h = std::max(proposal, h / 8);
+          int r = reject(h);
+          if (r) { *stepsOut = accepted; return r; }
+          continue;
+        }
+      }
+      accept(tn, ModeTran);
+      if (!fixed || onGrid) record(rec, tn);
+      xAcc = x;
+      accepted++;
+      t = tn;
+      if (fixed) {
+        if (onGrid) kgrid++;
+        order = method;
+        h = std::max(std::min(2 * h, maxStep), minStep);
+        continue;
+      }
+      double next = std::min(proposal, 2 * h);
+      next = std::min(next, maxStep);
+      order = method;
+      if (hitBreak) {
+        order = BE;
+        double nb2 = nextBreakpoint(t);
+        next = std::min(next, 0.1 * std::min(maxStep, nb2 - t));
+      }
+      h = std::max(next, minStep);
+    }
+    *stepsOut = accepted;
+    return E_OK;
+  }
+};
+
+static void copyMsg(const std::string& m, char* err, int errlen) {
+  if (!err || errlen <= 0) return;
+  snprintf(err, errlen, "%s", m.c_str());
+}
+
+}  // namespace kso
+
+using namespace kso;
+
+extern "C" int kso_unknowns(const ks_topology* t, const double* values, int32_t* n, int32_t* is_v) {
+  Sim s;
+  if (s.build(t, values, 0, 0, 0)) return KS_EINVAL;
+  *n = s.n;
+  if (is_v) for (int i = 0; i < s.n; i++) is_v[i] = s.isV[i];
+  return KS_OK;
+}
+
+extern "C" int kso_op(const ks_topology* t, const double* values, const ks_options* o, const double* x0,
+                      double* x_out, double* i_out, int32_t* iters, char* err, int errlen) {
+  Sim s;
+  Opts opt(o);
+  if (s.build(t, values, 0, 0, opt.backend)) { copyMsg(s.msg, err, errlen); return KS_STATUS_NOT_RUN; }
+  int e = s.op(opt, x0);
+  if (iters) *iters = s.iters;
+  if (x_out) for (int i = 0; i < s.n; i++) x_out[i] = s.x[i];
+  if (i_out && e == E_OK) for (size_t i = 0; i < s.devs.size(); i++) i_out[i] = s.devs[i]->current(s.x.data());
+  copyMsg(e ? s.msg : std::string(), err, errlen);
+  return e;
+}
+
+extern "C" int kso_dc(const ks_topology* t, const double* values, const ks_options* o, int src,
+                      const double* vals, int npts, double* x_out, double* i_out, char* err, int errlen) {
+  Sim s;
+  Opts opt(o);
+  if (s.build(t, values, 0, 0, opt.backend)) { copyMsg(s.msg, err, errlen); return KS_STATUS_NOT_RUN; }
+  if (src < 0 || src >= (int)s.devs.size()) { copyMsg("analysis: swept source not found", err, errlen); return KS_STATUS_NOT_RUN; }
+  for (int k = 0; k < npts; k++) {  // analysis/dc.go:104-128: one OP per point, warm-started
+    s.devs[src]->setDCOverride(vals[k]);
+    int e = s.op(opt, nullptr);
+    if (e) {
+      char buf[64]; snprintf(buf, sizeof buf, "sweep = %g: ", vals[k]);
+      copyMsg(buf + s.msg, err, errlen);
+      return e;
+    }
+    if (x_out) for (int i = 0; i < s.n; i++) x_out[(size_t)k * s.n + i] = s.x[i];
+    if (i_out) for (size_t i = 0; i < s.devs.size(); i++) i_out[(size_t)k * s.devs.size() + i] = s.devs[i]->current(s.x.data());
+  }
+  s.devs[src]->clearDCOverride();
+  return E_OK;
+}
+
+extern "C" int kso_tran(const ks_topology* t, const double* values, const ks_tran_spec* spec,
+                        const ks_options* o, int capacity, double* t_out, double* x_out, double* i_out,
+                        int32_t* npts, int32_t* steps, int32_t* iters, char* err, int errlen) {
+  Sim s;
+  Opts opt(o);
+  if (s.build(t, values, spec->step, spec->stop, opt.backend)) { copyMsg(s.msg, err, errlen); return KS_STATUS_NOT_RUN; }
+  Sim::Rec rec;
+  rec.cap = capacity; rec.t = t_out; rec.x = x_out; rec.i = i_out; rec.n = s.n; rec.ne = (int)s.devs.size();
+  int st = 0;
+  int e = s.tran(*spec, opt, rec, &st);
+  if (npts) *npts = std::min(rec.npts, capacity);
+  if (steps) *steps = st;
+  if (iters) *iters = s.iters;
+  copyMsg(e ? s.msg : std::string(), err, errlen);
+  return e;
+}
+
+template <class F>
+static void parallelFor(int nc, int nthreads, F f) {
+  if (nthreads <= 0) nthreads = (int)std::thread::hardware_concurrency();
+  if (nthreads < 1) nthreads = 1;
+  std::atomic<int> next(0);
+  auto worker = [&]() {
+    for (;;) {
+      int c = next.fetch_add(1);
+      if (c >= nc) break;
+      f(c);
+    }
+  };
+  std::vector<std::thread> th;
+  for (int i = 1; i < nthreads; i++) th.emplace_back(worker);
+  worker();
+  for (auto& x : th) x.join();
+}
+
+extern "C" int kso_batch_op(const ks_topology* t, const double* values, int nc, const ks_options* o,
+                            const double* x0, int nthreads, double* x_out, int32_t* status, int32_t* iters) {
+  int32_t n = 0;
+  if (kso_unknowns(t, values, &n, nullptr)) return KS_EINVAL;
+  parallelFor(nc, nthreads, [&](int c) {
+    int32_t it = 0;
+    status[c] = kso_op(t, values + (size_t)c * t->n_values, o, x0 ? x0 + (size_t)c * n : nullptr,
+                       x_out ? x_out + (size_t)c * n : nullptr, nullptr, &it, nullptr, 0);
+    if (iters) iters[c] = it;
+  });
+  return KS_OK;
+}
+
+extern "C" int kso_batch_tran(const ks_topology* t, const double* values, int nc, const ks_tran_spec* spec,
+                              const ks_options* o, int nthreads, double* x_out, int32_t* status,
+                              int32_t* steps, int32_t* iters) {
+  int32_t n = 0;
+  if (kso_unknowns(t, values, &n, nullptr)) return KS_EINVAL;
+  if (!spec->fixed_step) return KS_EINVAL;
+  int npts = (int)std::lround(spec->stop / spec->step) + 1;
+  parallelFor(nc, nthreads, [&](int c) {
+    std::vector<double> xs(x_out ? (size_t)npts * n : 0);
+    int32_t np = 0, st = 0, it = 0;
+    status[c] = kso_tran(t, values + (size_t)c * t->n_values, spec, o, x_out ? npts : 0, nullptr,
+                         x_out ? xs.data() : nullptr, nullptr, &np, &st, &it, nullptr, 0);
+    if (x_out)
+      for (int k = 0; k < np; k++)
+        for (int i = 0; i < n; i++) x_out[((size_t)k * nc + c) * n + i] = xs[(size_t)k * n + i];
+    if (steps) steps[c] = st;
+    if (iters) iters[c] = it;
+  });
+  return KS_OK;
+}

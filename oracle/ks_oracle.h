@@ -1,0 +1,55 @@
+/*
+ * ks_oracle.h — CPU FP64 oracle of the batched circuit-solve engine.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a line-by-line C++ restatement of the
+ * reference's (fdamador/kronspice, pure Go) hot path for the element kinds of
+ * include/kronspice_gpu.h: device Setup/Load/Accept/ConvTest/Truncate, the
+ * dense and sparse LU backends, Newton with the SPICE3 convergence test, the
+ * DC fallback chain and the transient loop.  Only tests/, __graft_entry__.smoke()
+ * and bench.py's CPU-baseline leg may load it; the engine never does.
+ *
+ * Parity pin: tests/test_oracle_golden.py checks it against the reference's
+ * golden vectors (the testdata/golden CSV files, committed as fixtures under
+ * tests/golden/) with the reference's tolerances (internal/golden/golden.go:22-27).
+ */
+#ifndef KS_ORACLE_H
+#define KS_ORACLE_H
+#include "../include/kronspice_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* One operating point (analysis.OP).  x0 (nullable) gives NodeSet voltages for
+ * unknowns 0..n_nodes-2.  Returns a ks_status; err gets the Go error text. */
+int kso_op(const ks_topology* t, const double* values, const ks_options* o, const double* x0,
+           double* x_out, double* i_out, int32_t* iters, char* err, int errlen);
+
+/* DC sweep of source element `src` over vals[npts] (analysis.DC, one sweep).
+ * x_out [npts][n], i_out [npts][n_elem] (nullable).  Returns a ks_status. */
+int kso_dc(const ks_topology* t, const double* values, const ks_options* o, int src,
+           const double* vals, int npts, double* x_out, double* i_out, char* err, int errlen);
+
+/* Transient (analysis.Tran, or the fixed-step mode of ks_tran_spec).  Up to
+ * `capacity` recorded points: t_out[cap], x_out[cap][n], i_out[cap][n_elem]
+ * (nullable).  npts gets the number recorded. */
+int kso_tran(const ks_topology* t, const double* values, const ks_tran_spec* spec,
+             const ks_options* o, int capacity, double* t_out, double* x_out, double* i_out,
+             int32_t* npts, int32_t* steps, int32_t* iters, char* err, int errlen);
+
+/* Batches over host threads (the timed CPU baseline).  values [nc][n_values];
+ * x0 nullable [nc][n]; x_out [nc][n]. */
+int kso_batch_op(const ks_topology* t, const double* values, int nc, const ks_options* o,
+                 const double* x0, int nthreads, double* x_out, int32_t* status, int32_t* iters);
+/* Fixed-step transients of a batch: x_out [npts][nc][n] (nullable). */
+int kso_batch_tran(const ks_topology* t, const double* values, int nc, const ks_tran_spec* spec,
+                   const ks_options* o, int nthreads, double* x_out, int32_t* status,
+                   int32_t* steps, int32_t* iters);
+
+/* Unknown count and layout of one circuit (device Setup), for the tests. */
+int kso_unknowns(const ks_topology* t, const double* values, int32_t* n, int32_t* is_v);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

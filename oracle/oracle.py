@@ -1,0 +1,170 @@
+"""ctypes binding of the CPU FP64 oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module; the engine (kronspice_gb300) never does.  build() compiles the
+oracle from oracle/*.cpp with g++ into oracle/_build/.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libks_oracle.so")
+SOURCES = ["ks_oracle.cpp"]
+HEADERS = ["ks_oracle.h", "oracle_solver.hpp", "oracle_devices.hpp", "oracle_bjt.hpp", "oracle_mos.hpp"]
+
+
+def build(force=False):
+    srcs = [os.path.join(HERE, s) for s in SOURCES + HEADERS] + [os.path.join(HERE, "..", "include", "kronspice_gpu.h")]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(s) for s in srcs):
+        return LIB
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-o", tmp,
+                           os.path.join(HERE, "ks_oracle.cpp"), "-lpthread"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class Topology(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_int32), ("n_elem", ctypes.c_int32), ("n_values", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("elem", ctypes.c_void_p)]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("reltol", ctypes.c_double), ("abstol", ctypes.c_double), ("vntol", ctypes.c_double),
+                ("gmin", ctypes.c_double), ("itl1", ctypes.c_int32), ("itl4", ctypes.c_int32),
+                ("no_gmin_stepping", ctypes.c_int32), ("no_source_stepping", ctypes.c_int32),
+                ("no_pseudo_transient", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("backend", ctypes.c_int32), ("max_iter_total", ctypes.c_int32),
+                ("deadline_s", ctypes.c_double)]
+
+
+class TranSpec(ctypes.Structure):
+    _fields_ = [("step", ctypes.c_double), ("stop", ctypes.c_double), ("start", ctypes.c_double),
+                ("max_step", ctypes.c_double), ("uic", ctypes.c_int32), ("method", ctypes.c_int32),
+                ("fixed_step", ctypes.c_int32), ("max_steps", ctypes.c_int32), ("chgtol", ctypes.c_double),
+                ("trtol", ctypes.c_double), ("min_step", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        P = ctypes.c_void_p
+        L.kso_op.argtypes = [P, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
+        L.kso_dc.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, P, P, ctypes.c_char_p, ctypes.c_int]
+        L.kso_tran.argtypes = [P, P, P, P, ctypes.c_int, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
+        L.kso_batch_op.argtypes = [P, P, ctypes.c_int, P, P, ctypes.c_int, P, P, P]
+        L.kso_batch_tran.argtypes = [P, P, ctypes.c_int, P, P, ctypes.c_int, P, P, P, P]
+        L.kso_unknowns.argtypes = [P, P, P, P]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class Packed:
+    """A topology plus value vectors, kept alive for the C calls."""
+
+    def __init__(self, elements, n_nodes, values):
+        self.elements = np.ascontiguousarray(elements)
+        self.values = np.ascontiguousarray(values, dtype=np.float64)
+        nv = self.values.shape[-1]
+        self.topo = Topology(n_nodes, len(self.elements), nv, 0, self.elements.ctypes.data)
+
+    @classmethod
+    def of(cls, circuit):
+        el, vals, _ = circuit.pack()
+        return cls(el, circuit.n_nodes, vals)
+
+    def tref(self):
+        return ctypes.byref(self.topo)
+
+
+def options(reltol=0.0, abstol=0.0, vntol=0.0, gmin=0.0, itl1=0, itl4=0, backend=0,
+            no_gmin=False, no_source=False, no_pt=False, deadline_s=0.0):
+    return Options(reltol, abstol, vntol, gmin, itl1, itl4, int(no_gmin), int(no_source), int(no_pt),
+                   0, backend, 0, deadline_s)
+
+
+def unknowns(pk):
+    n = ctypes.c_int32()
+    isv = np.zeros(4096, dtype=np.int32)
+    rc = lib().kso_unknowns(pk.tref(), _ptr(pk.values), ctypes.byref(n), _ptr(isv))
+    if rc:
+        raise ValueError("kso_unknowns failed")
+    return n.value, isv[:n.value].astype(bool)
+
+
+def op(pk, opt=None, x0=None):
+    """(status, x, element currents, iterations, message)."""
+    n, _ = unknowns(pk)
+    x = np.zeros(n)
+    cur = np.zeros(max(1, len(pk.elements)))
+    it = ctypes.c_int32()
+    err = ctypes.create_string_buffer(512)
+    o = opt or options()
+    x0a = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
+    st = lib().kso_op(pk.tref(), _ptr(pk.values), ctypes.byref(o), _ptr(x0a), _ptr(x), _ptr(cur),
+                      ctypes.byref(it), err, 512)
+    return st, x, cur[:len(pk.elements)], it.value, err.value.decode()
+
+
+def dc(pk, src, vals, opt=None):
+    n, _ = unknowns(pk)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    x = np.zeros((len(vals), n))
+    cur = np.zeros((len(vals), len(pk.elements)))
+    err = ctypes.create_string_buffer(512)
+    o = opt or options()
+    st = lib().kso_dc(pk.tref(), _ptr(pk.values), ctypes.byref(o), src, _ptr(vals), len(vals), _ptr(x),
+                      _ptr(cur), err, 512)
+    return st, x, cur, err.value.decode()
+
+
+def tran(pk, spec, opt=None, capacity=200000, currents=True):
+    n, _ = unknowns(pk)
+    t = np.zeros(capacity)
+    x = np.zeros((capacity, n))
+    cur = np.zeros((capacity, len(pk.elements))) if currents else None
+    npts, steps, it = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    err = ctypes.create_string_buffer(512)
+    o = opt or options()
+    st = lib().kso_tran(pk.tref(), _ptr(pk.values), ctypes.byref(spec), ctypes.byref(o), capacity, _ptr(t),
+                        _ptr(x), _ptr(cur), ctypes.byref(npts), ctypes.byref(steps), ctypes.byref(it), err, 512)
+    k = npts.value
+    return (st, t[:k], x[:k], None if cur is None else cur[:k], steps.value, it.value, err.value.decode())
+
+
+def batch_op(pk, nc, opt=None, x0=None, nthreads=0):
+    n, _ = unknowns(Packed(pk.elements, pk.topo.n_nodes, pk.values[0]))
+    x = np.zeros((nc, n))
+    st = np.zeros(nc, dtype=np.int32)
+    it = np.zeros(nc, dtype=np.int32)
+    o = opt or options()
+    x0a = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
+    lib().kso_batch_op(pk.tref(), _ptr(pk.values), nc, ctypes.byref(o), _ptr(x0a), nthreads, _ptr(x),
+                       _ptr(st), _ptr(it))
+    return st, x, it
+
+
+def batch_tran(pk, nc, spec, opt=None, nthreads=0, record=True):
+    n, _ = unknowns(Packed(pk.elements, pk.topo.n_nodes, pk.values[0]))
+    npts = int(round(spec.stop / spec.step)) + 1
+    x = np.zeros((npts, nc, n)) if record else None
+    st = np.zeros(nc, dtype=np.int32)
+    steps = np.zeros(nc, dtype=np.int32)
+    it = np.zeros(nc, dtype=np.int32)
+    o = opt or options()
+    lib().kso_batch_tran(pk.tref(), _ptr(pk.values), nc, ctypes.byref(spec), ctypes.byref(o), nthreads,
+                         _ptr(x), _ptr(st), _ptr(steps), _ptr(it))
+    return st, x, steps, it

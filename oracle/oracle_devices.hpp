@@ -1,0 +1,539 @@
+// oracle_devices.hpp — CPU FP64 device models of the oracle (test infrastructure).
+//
+// Each device restates the reference's Go device of the same name; the file:line
+// of the reference function follows every method.  Element values arrive in the
+// value-block layouts of include/kronspice_gpu.h (defaults and area scaling
+// already applied, as NewDiode/NewBJT/NewMOSFET do when they read a model card).
+#pragma once
+#include "oracle_solver.hpp"
+#include "../include/kronspice_gpu.h"
+
+namespace kso {
+
+constexpr double kChargeQ = 1.602176634e-19;  // device/diode.go:15
+constexpr double kBoltzmann = 1.380649e-23;   // device/diode.go:16
+constexpr double kTNom = 300.15;              // device/diode.go:18
+constexpr double kInf = std::numeric_limits<double>::infinity();
+constexpr double kE = 2.718281828459045235360287;
+constexpr double kSqrt2 = 1.41421356237309504880168872;
+constexpr double kPi = 3.14159265358979323846264338;
+
+enum Mode { ModeOP = 0, ModeTranOP = 1, ModeUICInit = 2, ModeTran = 3 };  // device/device.go:103-116
+enum Method { BE = 1, TRAP = 2 };                                         // device/device.go:119-124
+
+struct LoadCtx {  // device/device.go:127-148
+  Matrix* M = nullptr;
+  double* rhs = nullptr;
+  int n = 0;
+  int mode = ModeOP;
+  double time = 0, h = 0;
+  int method = BE;
+  const double* X = nullptr;
+  bool initJct = false;
+  double gmin = 1e-12;
+  bool srcStepping = false;
+  double srcFact = 0;
+  void addRHS(int i, double v) { if (i >= 0 && i < n) rhs[i] += v; }
+};
+
+struct TruncCtx { double time, h; int method; double reltol, abstol, vntol, chgtol, trtol; };  // device/lte.go:10-19
+
+struct History {  // device/lte.go:23-37
+  double t[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+  int n = 0;
+  void push(double tt, double qq) {
+    t[2] = t[1]; t[1] = t[0]; t[0] = tt;
+    q[2] = q[1]; q[1] = q[0]; q[0] = qq;
+    if (n < 3) n++;
+  }
+  void reset() { n = 0; }
+};
+
+// lteStep, device/lte.go:50-85.
+static double lteStep(const History& hist, double qn, double in, double inPrev, double absTol, const TruncCtx& tc) {
+  int k = tc.method;
+  if (k < 1 || k > 2 || hist.n < k + 1) return kInf;
+  double ts[4] = {tc.time, hist.t[0], hist.t[1], hist.t[2]};
+  double qs[4] = {qn, hist.q[0], hist.q[1], hist.q[2]};
+  double dd[4] = {0, 0, 0, 0};
+  for (int i = 0; i < k + 2; i++) dd[i] = qs[i];
+  for (int order = 1; order <= k + 1; order++) {
+    for (int i = 0; i + order <= k + 1; i++) {
+      double den = ts[i] - ts[i + order];
+      if (den == 0) return kInf;
+      dd[i] = (dd[i] - dd[i + 1]) / den;
+    }
+  }
+  double deriv = dd[0];
+  double fact = 2.0, c = 0.5;
+  if (k == 2) { fact = 6; c = 1.0 / 12; }
+  double h = tc.h;
+  double errI = c * std::pow(h, double(k)) * std::fabs(deriv * fact);
+  if (errI == 0 || std::isnan(errI)) return kInf;
+  double qmax = std::max(std::fabs(qn), std::fabs(hist.q[0]));
+  double allowed = tc.trtol * std::max(tc.reltol * std::max(std::fabs(in), std::fabs(inPrev)) + absTol,
+                                       tc.reltol * std::max(qmax, tc.chgtol) / h);
+  return h * std::pow(allowed / errI, 1 / double(k));
+}
+
+static inline double at(const double* x, int n, int i) { return (i < 0 || i >= n) ? 0.0 : x[i]; }
+
+// pnjlim, device/diode.go:214-226.
+static double pnjlim(double vnew, double vold, double vt, double vcrit, bool* lim) {
+  if (vnew > vcrit && std::fabs(vnew - vold) > 2 * vt) {
+    *lim = true;
+    if (vold > 0) {
+      double arg = 1 + (vnew - vold) / vt;
+      if (arg > 0) return vold + vt * std::log(arg);
+      return vcrit;
+    }
+    return vt * std::log(vnew / vt);
+  }
+  *lim = false;
+  return vnew;
+}
+
+struct SetupCtx {  // device/device.go:36-100
+  int numNodes = 0, branches = 0;
+  std::vector<int> internal;
+  double step = 0, stop = 0;
+  int unknown(int node) const { return node - 1; }
+  int allocBranch() { return numNodes - 1 + branches++; }
+  int allocUnknown() { int i = allocBranch(); internal.push_back(i); return i; }
+  int size() const { return numNodes - 1 + branches; }
+};
+
+struct Device {
+  int n = 0;  // system size (set after setup)
+  virtual ~Device() {}
+  virtual void setup(SetupCtx& c) = 0;
+  virtual void load(LoadCtx& c) = 0;
+  virtual double current(const double* x) = 0;  // Operating(x).Current
+  virtual void accept(const double* x, double t, int mode) {}
+  virtual bool nonlinear() const { return false; }
+  virtual bool limited() const { return false; }
+  virtual bool convTest(const double* x, double reltol, double abstol) { return true; }
+  virtual bool reactive() const { return false; }
+  virtual double truncate(const double* x, const TruncCtx& tc) { return kInf; }
+  virtual bool breakpointer() const { return false; }
+  virtual double nextBreakpoint(double t) { return kInf; }
+  virtual void setInitialCondition() {}
+  virtual void setDCOverride(double v) {}
+  virtual void clearDCOverride() {}
+};
+
+struct TwoTerm : Device {
+  int nodes[2] = {0, 0}, u[2] = {-1, -1};
+  void setupNodes(SetupCtx& c) { u[0] = c.unknown(nodes[0]); u[1] = c.unknown(nodes[1]); }
+  double voltage(const double* x) const {  // device/device.go:310-319
+    double v = 0;
+    if (u[0] >= 0) v += x[u[0]];
+    if (u[1] >= 0) v -= x[u[1]];
+    return v;
+  }
+};
+
+// Resistor, device/passive.go:65-95 (no ECE terms).
+struct Resistor : TwoTerm {
+  double R, g = 0;
+  explicit Resistor(double r) : R(r) {}
+  void setup(SetupCtx& c) override { setupNodes(c); g = 1 / R; }
+  void load(LoadCtx& c) override {
+    int a = u[0], b = u[1];
+    c.M->add(a, a, g); c.M->add(b, b, g); c.M->add(a, b, -g); c.M->add(b, a, -g);
+  }
+  double current(const double* x) override { return voltage(x) * g; }
+};
+
+// Capacitor, device/reactive.go:43-181.
+struct Capacitor : TwoTerm {
+  double C, ic; bool hasIC;
+  double geq = 0, ihist = 0; bool tran = false;
+  double vPrev = 0, iPrev = 0;
+  History hist;
+  Capacitor(double c, double ic_, bool has) : C(c), ic(ic_), hasIC(has) {}
+  void setup(SetupCtx& c) override { setupNodes(c); }
+  bool reactive() const override { return true; }
+  void load(LoadCtx& c) override {
+    int a = u[0], b = u[1];
+    switch (c.mode) {
+      case ModeOP: case ModeTranOP: tran = false; geq = 0; ihist = 0; return;
+      case ModeUICInit: {
+        tran = false;
+        double g = 1e9;  // uicConductance, device/reactive.go:70
+        c.M->add(a, a, g); c.M->add(b, b, g); c.M->add(a, b, -g); c.M->add(b, a, -g);
+        c.addRHS(a, g * vPrev); c.addRHS(b, -g * vPrev);
+        geq = 0; ihist = 0;
+        return;
+      }
+    }
+    tran = true;
+    if (c.method == TRAP) { geq = 2 * C / c.h; ihist = -(geq * vPrev + iPrev); }
+    else { geq = C / c.h; ihist = -geq * vPrev; }
+    double g = geq;
+    c.M->add(a, a, g); c.M->add(b, b, g); c.M->add(a, b, -g); c.M->add(b, a, -g);
+    c.addRHS(a, -ihist); c.addRHS(b, ihist);
+  }
+  double current(const double* x) override { return tran ? geq * voltage(x) + ihist : 0.0; }
+  void accept(const double* x, double t, int mode) override {  // :144-161
+    if (mode == ModeUICInit) { iPrev = 0; hist.reset(); }
+    else if (mode == ModeOP || mode == ModeTranOP) { vPrev = voltage(x); iPrev = 0; hist.reset(); }
+    else { double v = voltage(x); double i = current(x); vPrev = v; iPrev = i; }
+    hist.push(t, C * vPrev);
+  }
+  void setInitialCondition() override { vPrev = 0; iPrev = 0; if (hasIC) vPrev = ic; }
+  double truncate(const double* x, const TruncCtx& tc) override {  // :178-181
+    double v = voltage(x), i = current(x);
+    return lteStep(hist, C * v, i, iPrev, tc.abstol, tc);
+  }
+};
+
+// Inductor, device/reactive.go:198-352.
+struct Inductor : TwoTerm {
+  double L, ic; bool hasIC;
+  int branch = -1;
+  double vPrev = 0, iPrev = 0;
+  History hist;
+  Inductor(double l, double ic_, bool has) : L(l), ic(ic_), hasIC(has) {}
+  void setup(SetupCtx& c) override { setupNodes(c); branch = c.allocBranch(); }
+  bool reactive() const override { return true; }
+  void load(LoadCtx& c) override {
+    int a = u[0], b = u[1], k = branch;
+    c.M->add(a, k, 1); c.M->add(b, k, -1);
+    switch (c.mode) {
+      case ModeOP: case ModeTranOP: c.M->add(k, a, 1); c.M->add(k, b, -1); return;
+      case ModeUICInit: c.M->add(k, k, 1); c.addRHS(k, iPrev); return;
+    }
+    double req = L / c.h, r = -req * iPrev;
+    if (c.method == TRAP) { req = 2 * L / c.h; r = -req * iPrev - vPrev; }
+    c.M->add(k, a, 1); c.M->add(k, b, -1); c.M->add(k, k, -req);
+    c.addRHS(k, r);
+  }
+  double current(const double* x) override { return x[branch]; }
+  void accept(const double* x, double t, int mode) override {  // :312-329
+    if (mode == ModeUICInit) { vPrev = 0; hist.reset(); }
+    else if (mode == ModeOP || mode == ModeTranOP) { vPrev = 0; iPrev = x[branch]; hist.reset(); }
+    else { vPrev = voltage(x); iPrev = x[branch]; }
+    hist.push(t, L * iPrev);
+  }
+  void setInitialCondition() override { vPrev = 0; iPrev = 0; if (hasIC) iPrev = ic; }
+  double truncate(const double* x, const TruncCtx& tc) override {  // :346-349
+    return lteStep(hist, L * x[branch], voltage(x), vPrev, tc.vntol, tc);
+  }
+};
+
+// Source waveform, device/waveform.go:10-239.
+struct Wave {
+  int kind = KS_WAVE_NONE;
+  double a[7] = {0, 0, 0, 0, 0, 0, 0};
+  std::vector<double> pwl;
+  void resolve(int k, const double* args, int nargs, double step, double stop) {  // :25-66
+    kind = k;
+    if (step <= 0) step = 1e-9;
+    if (stop <= 0) stop = 1e-6;
+    auto arg = [&](int i, double def) { return i < nargs ? args[i] : def; };
+    switch (k) {
+      case KS_WAVE_PULSE: {
+        double v[7] = {arg(0, 0), arg(1, 0), arg(2, 0), arg(3, step), arg(4, step), arg(5, stop), arg(6, stop)};
+        for (int i = 0; i < 7; i++) a[i] = v[i];
+        if (a[3] == 0) a[3] = step;
+        if (a[4] == 0) a[4] = step;
+        break;
+      }
+      case KS_WAVE_SIN: {
+        double v[7] = {arg(0, 0), arg(1, 0), arg(2, 1 / stop), arg(3, 0), arg(4, 0), arg(5, 0), 0};
+        for (int i = 0; i < 7; i++) a[i] = v[i];
+        break;
+      }
+      case KS_WAVE_EXP: {
+        double td1 = arg(2, 0);
+        double v[7] = {arg(0, 0), arg(1, 0), td1, arg(3, step), arg(4, td1 + step), arg(5, step), 0};
+        for (int i = 0; i < 7; i++) a[i] = v[i];
+        if (a[3] == 0) a[3] = step;
+        if (a[5] == 0) a[5] = step;
+        break;
+      }
+      case KS_WAVE_PWL: pwl.assign(args, args + nargs); break;
+    }
+  }
+  double value(double t) const {  // :69-126
+    switch (kind) {
+      case KS_WAVE_PULSE: {
+        double v1 = a[0], v2 = a[1], td = a[2], tr = a[3], tf = a[4], pw = a[5], per = a[6];
+        if (t < td) return v1;
+        double tt = t - td;
+        if (per > 0) tt = std::fmod(tt, per);
+        if (tt < tr) return v1 + (v2 - v1) * tt / tr;
+        if (tt < tr + pw) return v2;
+        if (tt < tr + pw + tf) return v2 + (v1 - v2) * (tt - tr - pw) / tf;
+        return v1;
+      }
+      case KS_WAVE_SIN: {
+        double vo = a[0], va = a[1], f = a[2], td = a[3], theta = a[4], ph = a[5] * kPi / 180;
+        if (t < td) return vo + va * std::sin(ph);
+        double tt = t - td;
+        return vo + va * std::exp(-tt * theta) * std::sin(2 * kPi * f * tt + ph);
+      }
+      case KS_WAVE_EXP: {
+        double v1 = a[0], v2 = a[1], td1 = a[2], tau1 = a[3], td2 = a[4], tau2 = a[5];
+        if (t < td1) return v1;
+        if (t < td2) return v1 + (v2 - v1) * (1 - std::exp(-(t - td1) / tau1));
+        return v1 + (v2 - v1) * (1 - std::exp(-(t - td1) / tau1)) + (v1 - v2) * (1 - std::exp(-(t - td2) / tau2));
+      }
+      case KS_WAVE_PWL: {
+        const std::vector<double>& p = pwl;
+        int n = (int)p.size() / 2;
+        if (t <= p[0]) return p[1];
+        if (t >= p[2 * (n - 1)]) return p[2 * n - 1];
+        int k = 0;
+        while (k < n && !(p[2 * k] > t)) k++;
+        double t0 = p[2 * (k - 1)], v0 = p[2 * (k - 1) + 1], t1 = p[2 * k], v1 = p[2 * k + 1];
+        if (t1 == t0) return v1;
+        return v0 + (v1 - v0) * (t - t0) / (t1 - t0);
+      }
+    }
+    return 0;
+  }
+  double nextBreakpoint(double t) const {  // :190-239
+    const double rel = 1e-12;
+    auto after = [&](double b) { return b > t + rel * std::max(std::fabs(t), 1e-15); };
+    switch (kind) {
+      case KS_WAVE_PULSE: {
+        double td = a[2], tr = a[3], tf = a[4], pw = a[5], per = a[6];
+        double edges[4] = {0, tr, tr + pw, tr + pw + tf};
+        if (per <= 0) {
+          for (double e : edges) if (after(td + e)) return td + e;
+          return kInf;
+        }
+        double k = std::floor((t - td) / per);
+        if (k < 0) k = 0;
+        for (double kk = k; kk <= k + 1; kk++) {
+          double base = td + kk * per;
+          for (double e : edges) if (after(base + e)) return base + e;
+        }
+        return td + (k + 2) * per;
+      }
+      case KS_WAVE_SIN: if (after(a[3])) return a[3]; break;
+      case KS_WAVE_EXP:
+        if (after(a[2])) return a[2];
+        if (after(a[4])) return a[4];
+        break;
+      case KS_WAVE_PWL: {
+        int n = (int)pwl.size() / 2;
+        for (int k = 0; k < n; k++) if (after(pwl[2 * k])) return pwl[2 * k];
+        break;
+      }
+    }
+    return kInf;
+  }
+};
+
+// sourceValue, device/source.go:21-73.
+struct SourceValue {
+  double dc; bool hasDC;
+  int wkind; std::vector<double> args;
+  Wave w;
+  double override_ = 0; bool overridden = false;
+  void setup(const SetupCtx& c) { w.resolve(wkind, args.data(), (int)args.size(), c.step, c.stop); }
+  double raw(const LoadCtx& c) const {
+    if (overridden && c.mode == ModeOP) return override_;
+    if (wkind == KS_WAVE_NONE) return dc;
+    if (c.mode == ModeOP && hasDC) return dc;
+    double t = c.mode == ModeTran ? c.time : 0;
+    return w.value(t);
+  }
+  double at(const LoadCtx& c) const {
+    double v = raw(c);
+    if (c.srcStepping && c.mode != ModeTran) v *= c.srcFact;
+    return v;
+  }
+  double nextBreakpoint(double t) const { return wkind == KS_WAVE_NONE ? kInf : w.nextBreakpoint(t); }
+};
+
+struct VSource : TwoTerm {  // device/source.go:75-121
+  SourceValue src; int branch = -1; double value = 0;
+  void setup(SetupCtx& c) override { setupNodes(c); branch = c.allocBranch(); src.setup(c); }
+  void load(LoadCtx& c) override {
+    int a = u[0], b = u[1], k = branch;
+    value = src.at(c);
+    c.M->add(a, k, 1); c.M->add(b, k, -1); c.M->add(k, a, 1); c.M->add(k, b, -1);
+    c.addRHS(k, value);
+  }
+  double current(const double* x) override { return x[branch]; }
+  bool breakpointer() const override { return true; }
+  double nextBreakpoint(double t) override { return src.nextBreakpoint(t); }
+  void setDCOverride(double v) override { src.override_ = v; src.overridden = true; }
+  void clearDCOverride() override { src.overridden = false; }
+};
+
+struct ISource : TwoTerm {  // device/source.go:131-177
+  SourceValue src; double value = 0;
+  void setup(SetupCtx& c) override { setupNodes(c); src.setup(c); }
+  void load(LoadCtx& c) override { value = src.at(c); c.addRHS(u[0], -value); c.addRHS(u[1], value); }
+  double current(const double*) override { return value; }
+  bool breakpointer() const override { return true; }
+  double nextBreakpoint(double t) override { return src.nextBreakpoint(t); }
+  void setDCOverride(double v) override { src.override_ = v; src.overridden = true; }
+  void clearDCOverride() override { src.overridden = false; }
+};
+
+// Diode, device/diode.go:61-397.
+struct Diode : TwoTerm {
+  double IS, N, RS, CJO, VJ, M, TT, BV, IBV, FC; bool hasBV;
+  double vte, vcrit, xbv = 0, grs = 0; int ai = -1;
+  double vd = 0, cd = 0, gd = 0, iq = 0, geq = 0; bool tran = false, lim = false, hasCharge;
+  double gmin = 1e-12, qPrev = 0, iqPrev = 0, vdAcc = 0;
+  History hist;
+  Diode(const double* p, bool hasBV_) {
+    IS = p[KS_D_P_IS]; N = p[KS_D_P_N]; RS = p[KS_D_P_RS]; CJO = p[KS_D_P_CJO]; VJ = p[KS_D_P_VJ];
+    M = p[KS_D_P_M]; TT = p[KS_D_P_TT]; BV = p[KS_D_P_BV]; IBV = p[KS_D_P_IBV]; FC = p[KS_D_P_FC];
+    hasBV = hasBV_;
+    vte = N * kBoltzmann * kTNom / kChargeQ;            // :116
+    vcrit = vte * std::log(vte / (kSqrt2 * IS));        // :117
+    if (RS > 0) grs = 1 / RS;
+    hasCharge = CJO > 0 || TT > 0;
+    if (hasBV) xbv = breakdownVoltage(IS, BV, IBV, kBoltzmann * kTNom / kChargeQ);
+  }
+  static double breakdownVoltage(double is, double bv, double ibv, double vt) {  // :166-187
+    if (ibv < is * bv / vt) return bv;
+    auto g = [&](double x) { return is * (std::exp(std::min((bv - x) / vt, 700.0)) - 1 + x / vt) - ibv; };
+    double lo = std::min(0.0, bv - vt * std::log1p(ibv / is)) - 10 * vt, hi = bv;
+    for (int i = 0; i < 200 && g(lo) <= 0; i++) lo -= 10 * vt;
+    for (int i = 0; i < 200; i++) {
+      double mid = 0.5 * (lo + hi);
+      if (mid == lo || mid == hi) break;
+      if (g(mid) > 0) lo = mid; else hi = mid;
+    }
+    return 0.5 * (lo + hi);
+  }
+  void setup(SetupCtx& c) override { setupNodes(c); ai = u[0]; if (grs > 0) ai = c.allocUnknown(); }
+  bool nonlinear() const override { return true; }
+  bool reactive() const override { return true; }
+  bool limited() const override { return lim; }
+  void curr(double v, double* id, double* g) const {  // :148-162
+    if (v >= -3 * vte) {
+      double e = std::exp(std::min(v / vte, 700.0));
+      *id = IS * (e - 1); *g = IS * e / vte; return;
+    }
+    if (!hasBV || v >= -xbv) {
+      double a = 3 * vte / (v * kE); a = a * a * a;
+      *id = -IS * (1 + a); *g = IS * 3 * a / v; return;
+    }
+    double e = std::exp(std::min(-(xbv + v) / vte, 700.0));
+    *id = -IS * e; *g = IS * e / vte;
+  }
+  void charge(double v, double id, double g, double* q, double* c) const {  // :191-211
+    *q = TT * id; *c = TT * g;
+    if (CJO == 0) return;
+    double fcv = FC * VJ;
+    if (v < fcv) {
+      double arg = 1 - v / VJ, sarg = std::pow(arg, -M);
+      *q += CJO * VJ * (1 - arg * sarg) / (1 - M);
+      *c += CJO * sarg;
+      return;
+    }
+    double f1 = VJ * (1 - std::pow(1 - FC, 1 - M)) / (1 - M);
+    double f2 = std::pow(1 - FC, 1 + M);
+    double f3 = 1 - FC * (1 + M);
+    *q += CJO * f1 + CJO / f2 * (f3 * (v - fcv) + M / (2 * VJ) * (v * v - fcv * fcv));
+    *c += CJO / f2 * (f3 + M * v / VJ);
+  }
+  void load(LoadCtx& c) override {  // :229-275
+    int a = u[0], k = u[1];
+    gmin = c.gmin;
+    double vraw = at(c.X, n, ai) - at(c.X, n, k);
+    if (c.initJct) { vd = vcrit; lim = true; }
+    else {
+      vd = pnjlim(vraw, vdAcc, vte, vcrit, &lim);
+      if (hasBV && vraw < std::min(0.0, -xbv + 10 * vte)) {
+        bool l2;
+        double vt = pnjlim(-(vraw + xbv), -(vdAcc + xbv), vte, vcrit, &l2);
+        vd = -(vt + xbv); lim = l2;
+      }
+    }
+    vdAcc = vd;
+    double id, g0;
+    curr(vd, &id, &g0);
+    cd = id + gmin * vd; gd = g0 + gmin;
+    tran = false; iq = 0; geq = 0;
+    if (c.mode == ModeTran && hasCharge) {
+      double q, cc;
+      charge(vd, id, g0, &q, &cc);
+      tran = true;
+      if (c.method == TRAP) { iq = 2 * (q - qPrev) / c.h - iqPrev; geq = 2 * cc / c.h; }
+      else { iq = (q - qPrev) / c.h; geq = cc / c.h; }
+    }
+    double g = gd + geq;
+    double ieq = cd + iq - g * vd;
+    c.M->add(ai, ai, g); c.M->add(k, k, g); c.M->add(ai, k, -g); c.M->add(k, ai, -g);
+    c.addRHS(ai, -ieq); c.addRHS(k, ieq);
+    if (grs > 0) { c.M->add(a, a, grs); c.M->add(ai, ai, grs); c.M->add(a, ai, -grs); c.M->add(ai, a, -grs); }
+  }
+  bool convTest(const double* x, double reltol, double abstol) override {  // :282-289
+    double v = at(x, n, ai) - at(x, n, u[1]);
+    double cdhat = cd + gd * (v - vd);
+    double id, g;
+    curr(v, &id, &g);
+    double cdn = id + gmin * v;
+    double tol = reltol * std::max(std::fabs(cdhat), std::fabs(cdn)) + abstol;
+    return std::fabs(cdhat - cdn) <= tol;
+  }
+  double current(const double* x) override {  // :293-301
+    double v = at(x, n, ai) - at(x, n, u[1]);
+    return (cd + gd * (v - vd)) + (iq + geq * (v - vd));
+  }
+  void accept(const double* x, double t, int mode) override {  // :304-322
+    double v = at(x, n, ai) - at(x, n, u[1]);
+    vdAcc = v;
+    double id, g, q, cc;
+    curr(v, &id, &g);
+    charge(v, id, g, &q, &cc);
+    if (mode == ModeTran) iqPrev = tran ? iq + geq * (v - vd) : 0;
+    else { iqPrev = 0; hist.reset(); }
+    qPrev = q;
+    hist.push(t, q);
+  }
+  double truncate(const double* x, const TruncCtx& tc) override {  // :388-397
+    if (!hasCharge) return kInf;
+    double v = at(x, n, ai) - at(x, n, u[1]);
+    double id, g, q, cc;
+    curr(v, &id, &g);
+    charge(v, id, g, &q, &cc);
+    double ic = iq + geq * (v - vd);
+    return lteStep(hist, q, ic, iqPrev, tc.abstol, tc);
+  }
+};
+
+static void deplF(double vj, double m, double fc, double* f1, double* f2, double* f3) {  // device/bjt.go:245-247
+  *f1 = vj * (1 - std::pow(1 - fc, 1 - m)) / (1 - m);
+  *f2 = std::pow(1 - fc, 1 + m);
+  *f3 = 1 - fc * (1 + m);
+}
+
+// junction, device/bjt.go:272-283.
+static void junction(double is, double v, double nvt, double* i, double* g) {
+  if (is == 0) { *i = 0; *g = 0; return; }
+  if (v >= -3 * nvt) {
+    double e = std::exp(std::min(v / nvt, 700.0));
+    *i = is * (e - 1); *g = is * e / nvt; return;
+  }
+  double a = 3 * nvt / (v * kE); a = a * a * a;
+  *i = -is * (1 + a); *g = is * 3 * a / v;
+}
+
+// depletion, device/bjt.go:358-370.
+static void depletion(double v, double cz, double vj, double m, double fc, double f1, double f2, double f3,
+                      double* q, double* c) {
+  if (cz == 0) { *q = 0; *c = 0; return; }
+  double fcv = fc * vj;
+  if (v < fcv) {
+    double arg = 1 - v / vj;
+    double sarg = std::exp(-m * std::log(arg));
+    *q = vj * cz * (1 - arg * sarg) / (1 - m); *c = cz * sarg; return;
+  }
+  double czf2 = cz / f2;
+  *q = cz * f1 + czf2 * (f3 * (v - fcv) + (m / (vj + vj)) * (v * v - fcv * fcv));
+  *c = czf2 * (f3 + m * v / vj);
+}
+
+}  // namespace kso
