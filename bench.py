@@ -1,0 +1,354 @@
+"""Benchmark: converged circuit solves/s of batched SPICE operating points on GB300.
+
+Workload (the headline configuration): DC operating points of 16,384 seeded
+single-stage BJT common-emitter amplifiers (IS log-U[1e-16, 1e-14] A, BF
+U[50, 300], R1 R2 RC RE log-U[100 ohm, 1 Mohm], Vcc U[5, 15] V) at SPICE reltol
+1e-6 / abstol 1e-12.  One step = one batched operating point of all circuits.
+
+  plain  : FP64 LU, standard Newton start (InitJct), the reference's algorithm
+  chosen : FP32 LU + FP64 Newton residual, with the learned Newton start when
+           the MLP is available (otherwise the standard start)
+
+value is the chosen path with inputs resident in HBM; e2e is the same through
+the C ABI with host buffers (values H2D, solutions D2H) inside the timed region.
+Between timed steps L2 is flushed (a 512 MB write); each step is timed with CUDA
+events on the launching stream.  --impl reference times the CPU restatement of
+the reference's Go path (the reference cannot be built here: no Go toolchain)
+over all host cores on a bounded sample of the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "converged circuit solves/s @ SPICE reltol, chosen vs plain GPU; Newton iters"
+UNIT = "solves/s"
+RELTOL = 1e-6
+ALGO_BYTES_PER_SOLVE = 96  # 7 parameters in + 5 unknowns out, 8 B each
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    p.add_argument("--n-circ", type=int, default=16384)
+    p.add_argument("--seed", type=int, default=0)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_baseline(el, nn, vals, min_wall=1.0, max_passes=20):
+    """Oracle (CPU restatement of the reference path) over all host threads."""
+    from oracle import oracle as orc
+    orc.build()
+    nthreads = os.cpu_count() or 1
+    pk = orc.Packed(el, nn, vals)
+    opt = orc.options(reltol=RELTOL)
+    orc.batch_op(pk, min(256, len(vals)), opt, nthreads=nthreads)  # warm-up
+    done, t0 = 0, time.perf_counter()
+    passes = 0
+    while True:
+        st, x, it = orc.batch_op(pk, len(vals), opt, nthreads=nthreads)
+        done += int((st == 0).sum())
+        passes += 1
+        wall = time.perf_counter() - t0
+        if wall >= min_wall or passes >= max_passes:
+            break
+    return {"value": done / wall, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": "%d passes over the %d-circuit batch (%.2f s wall, %.1f core-s), oracle/ks_oracle.cpp "
+                      "(C++ restatement of the Go path; no Go toolchain to build the reference)"
+                      % (passes, len(vals), wall, wall * nthreads),
+            "newton_iters_mean": float(it.mean())}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (clocks and throttle reasons)."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self, gpu_index):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [s.strip() for s in line.split(",")]
+                if len(p) < 9 or p[0] != str(gpu_index):
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    smax = float(p[2])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, p[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def traffic_from_profile():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from kronspice_gb300 import workloads
+    el, nn, vals = workloads.bjt_ce_batch(args.n_circ, args.seed)
+    from oracle import oracle as orc
+    orc.build()
+    nthreads = os.cpu_count() or 1
+    pk = orc.Packed(el, nn, vals)
+    opt = orc.options(reltol=RELTOL)
+    for _ in range(args.warmup):
+        orc.batch_op(pk, len(vals), opt, nthreads=nthreads)
+    t0 = time.perf_counter()
+    done = 0
+    its = []
+    for _ in range(args.steps):
+        st, x, it = orc.batch_op(pk, len(vals), opt, nthreads=nthreads)
+        done += int((st == 0).sum())
+        its.append(it)
+    wall = time.perf_counter() - t0
+    value = done / wall
+    it = np.concatenate(its)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Philox)",
+            "config": {"workload": "bjt_ce_op_%d" % args.n_circ, "n_circuits": args.n_circ, "reltol": RELTOL,
+                       "abstol": 1e-12, "host_threads": nthreads},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": "%d steps of the full %d-circuit batch on %d host threads; oracle/ks_oracle.cpp, "
+                                       "the C++ restatement of the reference's Go path (no Go toolchain here)"
+                                       % (args.steps, args.n_circ, nthreads)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "newton_iters_mean": float(it.mean()), "newton_iters_max": int(it.max())}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from kronspice_gb300 import analysis, build, workloads
+    build.build()
+    dev = torch.device("cuda", local)
+    el, nn, vals = workloads.bjt_ce_batch(args.n_circ, args.seed + rank)
+    B = vals.shape[0]
+    plan = analysis.Plan(el, nn, vals.shape[1])
+    batch = analysis.Batch(plan, vals)
+    n = plan.n
+    stream = torch.cuda.current_stream(dev)
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    x_dev = torch.empty((B, n), dtype=torch.float64, device=dev)
+    st_dev = torch.empty(B, dtype=torch.int32, device=dev)
+    it_dev = torch.empty(B, dtype=torch.int32, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    learned = None
+    try:
+        from kronspice_gb300 import learned_start
+        learned = learned_start.for_workload("bjt_ce", el, nn, vals, batch, dev)
+    except (ImportError, AttributeError):
+        learned = None
+
+    def step(opt, x0_dev=None):
+        batch.op_async(opt, None if x0_dev is None else x0_dev.data_ptr(), x_dev.data_ptr(), st_dev.data_ptr(),
+                       it_dev.data_ptr(), sh)
+
+    def timed(opt, with_start):
+        launches = 1 + (learned.launches_per_step if (with_start and learned) else 0)
+        for _ in range(args.warmup):
+            x0 = learned.predict(stream) if (with_start and learned) else None
+            step(opt, x0)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        times = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            x0 = learned.predict(stream) if (with_start and learned) else None
+            step(opt, x0)
+            e1.record(stream)
+            times.append((e0, e1))
+        torch.cuda.synchronize()
+        ms = [a.elapsed_time(b) for a, b in times]
+        total = sum(ms) / 1e3
+        if world > 1:
+            t = torch.tensor([total], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total = float(t.item())
+        st = st_dev.cpu().numpy()
+        it = it_dev.cpu().numpy()
+        return {"seconds": total, "ms_per_step": total / args.steps * 1e3, "ok": int((st == 0).sum()),
+                "iters_mean": float(it.mean()), "iters_max": int(it.max()), "launches": launches * args.steps,
+                "x": x_dev.cpu().numpy(), "status": st}
+
+    plain_opt = analysis.Options(reltol=RELTOL, precision="fp64")
+    chosen_opt = analysis.Options(reltol=RELTOL, precision="mixed")
+    clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp",
+                              "bench_clocks_%d.csv" % rank))
+    with clk:
+        plain = timed(plain_opt, False)
+        chosen = timed(chosen_opt, True)
+    clocks = clk.summary(local)
+
+    # end to end through the C ABI: pinned host values in, host solutions out
+    import torch as _t
+    vals_pin = _t.from_numpy(vals.copy()).pin_memory()
+    x_host = np.zeros((B, n))
+    s_host = np.zeros(B, dtype=np.int32)
+    i_host = np.zeros(B, dtype=np.int32)
+    L = __import__("kronspice_gb300._lib", fromlist=["x"]).load()
+    o = chosen_opt.c()
+
+    def e2e_step():
+        rc = L.ks_batch_set_values(batch.handle, ctypes.c_void_p(vals_pin.data_ptr()), 0, sh)
+        assert rc == 0
+        x0p = None
+        if learned:
+            x0 = learned.predict(stream)
+            x0p = x0.data_ptr()
+        if x0p is not None:
+            rc = L.ks_op_async(batch.handle, ctypes.byref(o), ctypes.c_void_p(x0p), x_dev.data_ptr(),
+                               st_dev.data_ptr(), it_dev.data_ptr(), sh)
+            assert rc == 0
+            x_host[:] = x_dev.cpu().numpy()
+            s_host[:] = st_dev.cpu().numpy()
+            i_host[:] = it_dev.cpu().numpy()
+        else:
+            rc = L.ks_op(batch.handle, ctypes.byref(o), None, x_host.ctypes.data, s_host.ctypes.data,
+                         i_host.ctypes.data, sh)
+            assert rc == 0
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_t = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        torch.cuda.synchronize()
+        e2e_t += time.perf_counter() - t0
+    e2e_value = world * B * args.steps / e2e_t if world == 1 else None
+    if world > 1:
+        t = torch.tensor([e2e_t], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_value = world * B * args.steps / float(t.item())
+
+    value = world * chosen["ok"] * args.steps / chosen["seconds"] if chosen["seconds"] > 0 else 0.0
+    plain_value = world * plain["ok"] * args.steps / plain["seconds"] if plain["seconds"] > 0 else 0.0
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return
+
+    # accuracy of the chosen path against the CPU oracle on a sample
+    from oracle import oracle as orc
+    samp = min(2048, B)
+    so, xo, io = orc.batch_op(orc.Packed(el, nn, vals[:samp]), samp, orc.options(reltol=RELTOL))
+    okm = (so == 0) & (chosen["status"][:samp] == 0)
+    max_err = float(np.max(np.abs(chosen["x"][:samp][okm, :nn - 1] - xo[okm, :nn - 1]))) if okm.any() else None
+    cpu = cpu_baseline(el, nn, vals)
+
+    per_launch_s = chosen["seconds"] / args.steps
+    achieved = ALGO_BYTES_PER_SOLVE * B / per_launch_s / 1e9
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    prof = traffic_from_profile().get("k_op_bjt_ce", {})
+    traffic = prof.get("dram_bytes_per_circuit")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": chosen["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 device eval + residual, f32 LU", "data": "synthetic (seeded Philox)",
+        "config": {"workload": "bjt_ce_op_%d" % B, "n_circuits_per_gpu": B, "n_unknowns": n, "reltol": RELTOL,
+                   "abstol": 1e-12, "l2": "flushed between timed steps (512 MB write)",
+                   "learned_start": learned is not None},
+        "plain": {"value": plain_value, "ms_per_step": plain["ms_per_step"], "newton_iters_mean": plain["iters_mean"],
+                  "newton_iters_max": plain["iters_max"], "precision": "fp64", "start": "InitJct"},
+        "chosen": {"value": value, "newton_iters_mean": chosen["iters_mean"], "newton_iters_max": chosen["iters_max"],
+                   "precision": "fp32 LU + fp64 residual",
+                   "start": "learned (MLP)" if learned is not None else "InitJct"},
+        "chosen_vs_plain": value / plain_value if plain_value else None,
+        "max_node_voltage_err_vs_oracle": max_err,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(vals.nbytes),
+                "d2h_bytes_per_step": int(x_host.nbytes + s_host.nbytes + i_host.nbytes)},
+        "gpu_launches": chosen["launches"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak,
+                     "traffic": None if traffic is None else traffic * B,
+                     "note": "k_op is FP64-issue and latency bound, not HBM bound: achieved counts the 96 B/solve "
+                             "of compulsory traffic, peak is the measured copy bandwidth"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.barrier()
+
+
+if __name__ == "__main__":
+    main()

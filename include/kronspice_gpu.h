@@ -88,7 +88,8 @@ enum {
   KS_F_INT_B = 1 << 6,    /* BJT: internal base (RB > 0)                        */
   KS_F_INT_E = 1 << 7,    /* BJT: internal emitter (RE > 0)                     */
   KS_F_INT_D = 1 << 8,    /* MOSFET: internal drain (conductance 1/RD > 0)      */
-  KS_F_INT_S = 1 << 9     /* MOSFET: internal source (conductance 1/RS > 0)     */
+  KS_F_INT_S = 1 << 9,    /* MOSFET: internal source (conductance 1/RS > 0)     */
+  KS_F_LATERAL = 1 << 10  /* BJT: SUBS < 0, substrate junction to the base      */
 };
 
 /*

@@ -1,0 +1,81 @@
+"""ctypes binding of libkronspice_gpu.so (include/kronspice_gpu.h).
+
+The library is built in-tree by kronspice_gb300.build (nvcc, sm_103a).  Loading
+fails loudly when it is missing: the engine has no CPU fallback.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libkronspice_gpu.so")
+
+
+class KsTopology(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_int32), ("n_elem", ctypes.c_int32), ("n_values", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("elem", ctypes.c_void_p)]
+
+
+class KsOptions(ctypes.Structure):
+    _fields_ = [("reltol", ctypes.c_double), ("abstol", ctypes.c_double), ("vntol", ctypes.c_double),
+                ("gmin", ctypes.c_double), ("itl1", ctypes.c_int32), ("itl4", ctypes.c_int32),
+                ("no_gmin_stepping", ctypes.c_int32), ("no_source_stepping", ctypes.c_int32),
+                ("no_pseudo_transient", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("backend", ctypes.c_int32), ("max_iter_total", ctypes.c_int32),
+                ("deadline_s", ctypes.c_double)]
+
+
+class KsTranSpec(ctypes.Structure):
+    _fields_ = [("step", ctypes.c_double), ("stop", ctypes.c_double), ("start", ctypes.c_double),
+                ("max_step", ctypes.c_double), ("uic", ctypes.c_int32), ("method", ctypes.c_int32),
+                ("fixed_step", ctypes.c_int32), ("max_steps", ctypes.c_int32), ("chgtol", ctypes.c_double),
+                ("trtol", ctypes.c_double), ("min_step", ctypes.c_double)]
+
+
+# every symbol include/kronspice_gpu.h declares
+EXPORTS = ["ks_version", "ks_last_error", "ks_validate", "ks_unknowns", "ks_plan_create", "ks_plan_destroy",
+           "ks_plan_info", "ks_batch_create", "ks_batch_set_values", "ks_batch_destroy", "ks_op", "ks_op_async",
+           "ks_tran", "ks_tran_points"]
+
+_lib = None
+
+
+class EngineMissing(RuntimeError):
+    pass
+
+
+def load(build_if_missing=False):
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if build_if_missing:
+            from . import build
+            build.build()
+        else:
+            raise EngineMissing("kronspice_gb300: %s is not built (run kronspice_gb300/build.py); "
+                                "the engine has no CPU fallback" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    L.ks_version.restype = ctypes.c_char_p
+    L.ks_last_error.restype = ctypes.c_char_p
+    L.ks_validate.argtypes = [P, P, ctypes.c_int]
+    L.ks_unknowns.argtypes = [P, P, P]
+    L.ks_plan_create.argtypes = [P, ctypes.POINTER(ctypes.c_void_p)]
+    L.ks_plan_destroy.argtypes = [P]
+    L.ks_plan_destroy.restype = None
+    L.ks_plan_info.argtypes = [P, P, P, P]
+    L.ks_batch_create.argtypes = [P, ctypes.c_int32, P, ctypes.POINTER(ctypes.c_void_p)]
+    L.ks_batch_set_values.argtypes = [P, P, ctypes.c_int, P]
+    L.ks_batch_destroy.argtypes = [P]
+    L.ks_batch_destroy.restype = None
+    L.ks_op.argtypes = [P, P, P, P, P, P, P]
+    L.ks_op_async.argtypes = [P, P, P, P, P, P, P]
+    if hasattr(L, "ks_tran"):
+        L.ks_tran.argtypes = [P, P, P, ctypes.c_int32, P, P, P, P, P, P, P]
+    L.ks_tran_points.argtypes = [P, P]
+    _lib = L
+    return L
+
+
+def last_error():
+    return load().ks_last_error().decode()

@@ -1,0 +1,226 @@
+"""Batched analyses on the GB300 engine: the host-side mirror of kronspice's analysis package.
+
+``op_batch(circuits, opt)`` is analysis.OP (analysis/op.go:331) for many
+circuits in one call; ``tran_batch`` is analysis.Tran (analysis/tran.go:70).
+Circuits are grouped by topology, each group is one plan and one batch on the
+GPU.  Each circuit gets back its solution or its typed error, with the same
+sentinels as the reference (solver/matrix.go:15-20, analysis/newton.go:20,
+analysis/tran.go:18-22, circuit/circuit.go:21-31), so callers such as a GA
+fitness function can classify failures unchanged.
+"""
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .circuit import ELEMENT_DTYPE
+
+
+class KronspiceError(Exception):
+    """Base of the engine's typed errors."""
+
+
+class ErrSingularMatrix(KronspiceError):
+    """solver.ErrSingularMatrix (solver/matrix.go:17)."""
+
+
+class ErrNonFinite(KronspiceError):
+    """solver.ErrNonFinite (solver/matrix.go:19)."""
+
+
+class ErrNoConvergence(KronspiceError):
+    """analysis.ErrNoConvergence (analysis/newton.go:20)."""
+
+
+class ErrTimestepTooSmall(KronspiceError):
+    """analysis.ErrTimestepTooSmall (analysis/tran.go:19)."""
+
+
+class ErrTooManySteps(KronspiceError):
+    """analysis.ErrTooManySteps (analysis/tran.go:20)."""
+
+
+class ErrInterrupted(KronspiceError):
+    """context deadline or cancel (analysis/op.go:81-89)."""
+
+
+class ErrValidation(KronspiceError):
+    """circuit.Validate failures (ErrFloatingNode, ErrBadValue, ... circuit/circuit.go:21-31)."""
+
+
+class ErrFloatingNode(ErrValidation):
+    """circuit.ErrFloatingNode (circuit/circuit.go:23)."""
+
+
+STATUS_ERRORS = {1: (ErrSingularMatrix, "solver: singular matrix"),
+                 2: (ErrNonFinite, "solver: non-finite value in system"),
+                 3: (ErrNoConvergence, "analysis: no convergence"),
+                 4: (ErrTimestepTooSmall, "analysis: timestep too small"),
+                 5: (ErrTooManySteps, "analysis: too many time steps"),
+                 6: (ErrInterrupted, "analysis interrupted: context deadline exceeded"),
+                 7: (KronspiceError, "not run")}
+
+PREC = {"fp64": 0, "mixed": 1}
+
+
+@dataclass
+class Options:
+    """analysis.Options (analysis/op.go:22-62) plus the engine's precision mode."""
+    reltol: float = 0.0
+    abstol: float = 0.0
+    vntol: float = 0.0
+    gmin: float = 0.0
+    itl1: int = 0
+    itl4: int = 0
+    no_gmin_stepping: bool = False
+    no_source_stepping: bool = False
+    no_pseudo_transient: bool = False
+    precision: str = "fp64"
+    max_iter_total: int = 0
+    deadline_s: float = 0.0
+
+    def c(self):
+        return _lib.KsOptions(self.reltol, self.abstol, self.vntol, self.gmin, self.itl1, self.itl4,
+                              int(self.no_gmin_stepping), int(self.no_source_stepping),
+                              int(self.no_pseudo_transient), PREC[self.precision], 0, self.max_iter_total,
+                              self.deadline_s)
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError("%s failed (%d): %s" % (what, rc, _lib.last_error()))
+
+
+def status_error(status):
+    if status == 0:
+        return None
+    cls, msg = STATUS_ERRORS.get(int(status), (KronspiceError, "status %d" % status))
+    return cls(msg)
+
+
+class Plan:
+    """One topology after the host symbolic pass (ks_plan_create)."""
+
+    def __init__(self, elements, n_nodes, n_values):
+        L = _lib.load()
+        self.elements = np.ascontiguousarray(elements, dtype=ELEMENT_DTYPE)
+        self.n_nodes = int(n_nodes)
+        self.topo = _lib.KsTopology(self.n_nodes, len(self.elements), int(n_values), 0, self.elements.ctypes.data)
+        h = ctypes.c_void_p()
+        _check(L.ks_plan_create(ctypes.byref(self.topo), ctypes.byref(h)), "ks_plan_create")
+        self.handle = h
+        n = ctypes.c_int32()
+        _check(L.ks_plan_info(h, ctypes.byref(n), None, None), "ks_plan_info")
+        self.n = n.value
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib._lib is not None:
+            _lib._lib.ks_plan_destroy(self.handle)
+            self.handle = None
+
+
+class Batch:
+    """n circuits of one plan with their values resident on the GPU (ks_batch_create)."""
+
+    def __init__(self, plan, values):
+        L = _lib.load()
+        self.plan = plan
+        self.values = np.ascontiguousarray(values, dtype=np.float64)
+        self.n_circ = self.values.shape[0]
+        h = ctypes.c_void_p()
+        _check(L.ks_batch_create(plan.handle, self.n_circ, self.values.ctypes.data, ctypes.byref(h)),
+               "ks_batch_create")
+        self.handle = h
+
+    def set_values(self, values):
+        self.values = np.ascontiguousarray(values, dtype=np.float64)
+        _check(_lib.load().ks_batch_set_values(self.handle, self.values.ctypes.data, 0, None), "ks_batch_set_values")
+
+    def op(self, opt=None, x0=None, stream=None):
+        """(x [n_circ][n], status [n_circ], iterations [n_circ]) through ks_op (host buffers)."""
+        o = (opt or Options()).c()
+        x = np.zeros((self.n_circ, self.plan.n))
+        st = np.zeros(self.n_circ, dtype=np.int32)
+        it = np.zeros(self.n_circ, dtype=np.int32)
+        x0a = None
+        if x0 is not None:
+            x0a = np.ascontiguousarray(x0, dtype=np.float64)
+            assert x0a.shape == (self.n_circ, self.plan.n)
+        _check(_lib.load().ks_op(self.handle, ctypes.byref(o), None if x0a is None else x0a.ctypes.data,
+                                 x.ctypes.data, st.ctypes.data, it.ctypes.data, stream), "ks_op")
+        return x, st, it
+
+    def op_async(self, opt, x0_dev, x_dev, status_dev, iters_dev, stream):
+        """ks_op_async on device pointers (ints) on a CUDA stream handle."""
+        o = (opt or Options()).c()
+        _check(_lib.load().ks_op_async(self.handle, ctypes.byref(o), x0_dev, x_dev, status_dev, iters_dev, stream),
+               "ks_op_async")
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib._lib is not None:
+            _lib._lib.ks_batch_destroy(self.handle)
+            self.handle = None
+
+
+def validate(circuit, transient=False):
+    """circuit.Validate: None or the typed validation error."""
+    el, vals, _ = circuit.pack()
+    topo = _lib.KsTopology(circuit.n_nodes, len(el), len(vals), 0, el.ctypes.data)
+    rc = _lib.load().ks_validate(ctypes.byref(topo), vals.ctypes.data, int(transient))
+    if rc == 0:
+        return None
+    msg = _lib.last_error()
+    if "no path to ground" in msg:
+        return ErrFloatingNode(msg)
+    return ErrValidation(msg)
+
+
+@dataclass
+class Result:
+    """The parts of output.Result (output/result.go:112-119) the engine computes."""
+    node_names: list
+    node_voltages: np.ndarray          # [n_nodes], ground first
+    x: np.ndarray                      # all MNA unknowns
+    iterations: int = 0
+    extra: dict = field(default_factory=dict)
+
+
+def op_batch(circuits, opt=None, nodeset=None):
+    """analysis.OP for every circuit: (results, errors), one entry per circuit."""
+    opt = opt or Options()
+    results, errors = [None] * len(circuits), [None] * len(circuits)
+    groups = {}
+    packed = []
+    for i, c in enumerate(circuits):
+        err = validate(c)
+        if err is not None:
+            errors[i] = err
+            packed.append(None)
+            continue
+        el, vals, key = c.pack()
+        packed.append((el, vals))
+        groups.setdefault(key, []).append(i)
+    for key, idx in groups.items():
+        el = packed[idx[0]][0]
+        nv = len(packed[idx[0]][1])
+        plan = Plan(el, circuits[idx[0]].n_nodes, nv)
+        vals = np.stack([packed[i][1] for i in idx])
+        b = Batch(plan, vals)
+        x0 = None
+        if nodeset is not None:
+            x0 = np.zeros((len(idx), plan.n))
+            for r, i in enumerate(idx):
+                ns = nodeset[i]
+                if ns is not None:
+                    x0[r, :len(ns)] = ns
+        x, st, it = b.op(opt, x0)
+        for r, i in enumerate(idx):
+            if st[r] != 0:
+                errors[i] = status_error(st[r])
+                continue
+            c = circuits[i]
+            nv_ = np.zeros(c.n_nodes)
+            nv_[1:] = x[r, :c.n_nodes - 1]
+            results[i] = Result(list(c.node_names), nv_, x[r].copy(), int(it[r]))
+    return results, errors

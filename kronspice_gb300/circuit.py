@@ -19,7 +19,7 @@ KIND = {"R": 1, "C": 2, "L": 3, "V": 4, "I": 5, "D": 6, "Q": 7, "M": 8}
 WAVE = {None: 0, "pulse": 1, "sin": 2, "exp": 3, "pwl": 4}
 
 F_HAS_DC, F_HAS_IC, F_HAS_BV, F_PTYPE = 1, 2, 4, 8
-F_INT_A, F_INT_C, F_INT_B, F_INT_E, F_INT_D, F_INT_S = 16, 32, 64, 128, 256, 512
+F_INT_A, F_INT_C, F_INT_B, F_INT_E, F_INT_D, F_INT_S, F_LATERAL = 16, 32, 64, 128, 256, 512, 1024
 
 # ks_element of include/kronspice_gpu.h (48 bytes)
 ELEMENT_DTYPE = np.dtype({
@@ -189,6 +189,8 @@ class Circuit:
                     flags |= F_INT_B
                 if p[Q_KEYS.index("re")] > 0:
                     flags |= F_INT_E
+                if p[Q_KEYS.index("subs")] < 0:
+                    flags |= F_LATERAL
                 vals += p
             elif e.kind == "M":
                 p, given, level, pmos, intd, ints = self._mos(e)

@@ -1,0 +1,225 @@
+// ks_api.cu — C ABI of the GB300 engine (include/kronspice_gpu.h): plans, batches,
+// operating points.  Plans own device copies of the compiled element program; a
+// batch owns the SoA value, derived-constant, state and work arrays of its
+// circuits and one CUDA stream.  Host buffers are staged through pinned memory.
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include "ks_internal.h"
+
+using ksh::set_error;
+
+struct ks_plan {
+  ksh::HostPlan hp;
+  KElem* d_elem = nullptr;
+  int8_t* d_isv = nullptr;
+  KPlan view() const {
+    KPlan p;
+    p.n = hp.n; p.n_elem = hp.n_elem; p.n_values = hp.n_values; p.n_derived = hp.n_derived;
+    p.n_state = hp.n_state; p.n_nodes = hp.n_nodes; p.n_nonlin = hp.n_nonlin; p.n_reactive = hp.n_reactive;
+    p.elem = d_elem; p.is_v = d_isv;
+    return p;
+  }
+};
+
+struct ks_batch {
+  ks_plan* plan = nullptr;
+  int64_t B = 0;
+  KsDeviceBatch dev{};
+  double* d_rows = nullptr;  // staging for row-major uploads [B][n_values]
+  cudaStream_t stream = nullptr;
+  // output staging
+  double* d_x = nullptr;
+  double* d_x0 = nullptr;
+  int32_t* d_status = nullptr;
+  int32_t* d_iters = nullptr;
+  double* h_pin = nullptr;
+  size_t h_pin_bytes = 0;
+  double setup_step = -1, setup_stop = -1;  // analysis the derived constants were made for
+};
+
+// Derived constants for an analysis with print step / stop time (0, 0 outside a transient).
+static int batch_setup(ks_batch* b, double step, double stop, cudaStream_t st) {
+  if (b->setup_step == step && b->setup_stop == stop) return KS_OK;
+  if (ks_launch_setup(b->dev, step, stop, st)) { set_error("setup kernel launch failed"); return KS_ECUDA; }
+  b->setup_step = step;
+  b->setup_stop = stop;
+  return KS_OK;
+}
+
+#define CK(call)                                                                            \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess) {                                                                \
+      set_error(std::string("CUDA: ") + cudaGetErrorString(e_) + " at " #call);            \
+      return KS_ECUDA;                                                                      \
+    }                                                                                       \
+  } while (0)
+
+static KOpts make_opts(const ks_options* o) {  // analysis/op.go:91-110
+  KOpts k{};
+  k.reltol = o && o->reltol > 0 ? o->reltol : 1e-3;
+  k.abstol = o && o->abstol > 0 ? o->abstol : 1e-12;
+  k.vntol = o && o->vntol > 0 ? o->vntol : 1e-6;
+  k.gmin = o && o->gmin > 0 ? o->gmin : 1e-12;
+  k.itl1 = o && o->itl1 > 0 ? o->itl1 : 100;
+  k.itl4 = o && o->itl4 > 0 ? o->itl4 : 10;
+  k.no_gmin = o ? o->no_gmin_stepping : 0;
+  k.no_source = o ? o->no_source_stepping : 0;
+  k.no_pt = o ? o->no_pseudo_transient : 0;
+  k.mixed = o ? (o->precision == KS_PREC_MIXED) : 0;
+  k.max_iter_total = o ? o->max_iter_total : 0;
+  return k;
+}
+
+extern "C" int ks_plan_create(const ks_topology* topo, ks_plan** out) {
+  if (!topo || !out) { set_error("ks_plan_create: null argument"); return KS_EINVAL; }
+  ks_plan* p = new ks_plan();
+  std::string err;
+  int rc = ksh::plan_layout(topo, &p->hp, &err);
+  if (rc) { set_error(err); delete p; return rc; }
+  if (p->hp.n > KS_MAX_DENSE) {
+    set_error("ks_plan_create: " + std::to_string(p->hp.n) + " unknowns; the thread-per-circuit kernels take up to " +
+              std::to_string(KS_MAX_DENSE));
+    delete p;
+    return KS_EUNSUPPORTED;
+  }
+  if (cudaMalloc(&p->d_elem, sizeof(KElem) * p->hp.n_elem) != cudaSuccess ||
+      cudaMalloc(&p->d_isv, p->hp.n + 8) != cudaSuccess) {
+    set_error("ks_plan_create: device allocation failed");
+    cudaFree(p->d_elem);
+    delete p;
+    return KS_ENOMEM;
+  }
+  cudaMemcpy(p->d_elem, p->hp.elem.data(), sizeof(KElem) * p->hp.n_elem, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->d_isv, p->hp.is_v.data(), p->hp.n, cudaMemcpyHostToDevice);
+  *out = p;
+  return KS_OK;
+}
+
+extern "C" void ks_plan_destroy(ks_plan* p) {
+  if (!p) return;
+  cudaFree(p->d_elem);
+  cudaFree(p->d_isv);
+  delete p;
+}
+
+extern "C" int ks_plan_info(const ks_plan* p, int32_t* n_unknowns, int32_t* n_values, int32_t* n_state) {
+  if (!p) return KS_EINVAL;
+  if (n_unknowns) *n_unknowns = p->hp.n;
+  if (n_values) *n_values = p->hp.n_values;
+  if (n_state) *n_state = p->hp.n_state;
+  return KS_OK;
+}
+
+static int batch_stage(ks_batch* b, size_t bytes) {
+  if (b->h_pin_bytes >= bytes) return KS_OK;
+  if (b->h_pin) cudaFreeHost(b->h_pin);
+  b->h_pin = nullptr;
+  b->h_pin_bytes = 0;
+  CK(cudaMallocHost(&b->h_pin, bytes));
+  b->h_pin_bytes = bytes;
+  return KS_OK;
+}
+
+extern "C" int ks_batch_create(ks_plan* plan, int32_t n_circ, const double* values, ks_batch** out) {
+  if (!plan || n_circ <= 0 || !out) { set_error("ks_batch_create: bad argument"); return KS_EINVAL; }
+  ks_batch* b = new ks_batch();
+  b->plan = plan;
+  b->B = n_circ;
+  const ksh::HostPlan& hp = plan->hp;
+  size_t B = (size_t)n_circ;
+  auto fail = [&](int rc) { ks_batch_destroy(b); return rc; };
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(KS_ECUDA);
+  if (cudaMalloc(&b->dev.values, sizeof(double) * hp.n_values * B) != cudaSuccess ||
+      cudaMalloc(&b->dev.derived, sizeof(double) * (hp.n_derived + 1) * B) != cudaSuccess ||
+      cudaMalloc(&b->dev.state, sizeof(double) * (hp.n_state + 1) * B) != cudaSuccess ||
+      cudaMalloc(&b->dev.work, sizeof(double) * (3 * hp.n + 1) * B) != cudaSuccess ||
+      cudaMalloc(&b->d_rows, sizeof(double) * hp.n_values * B) != cudaSuccess ||
+      cudaMalloc(&b->d_x, sizeof(double) * hp.n * B) != cudaSuccess ||
+      cudaMalloc(&b->d_x0, sizeof(double) * hp.n * B) != cudaSuccess ||
+      cudaMalloc(&b->d_status, sizeof(int32_t) * B) != cudaSuccess ||
+      cudaMalloc(&b->d_iters, sizeof(int32_t) * B) != cudaSuccess) {
+    set_error("ks_batch_create: device allocation failed");
+    return fail(KS_ENOMEM);
+  }
+  b->dev.plan = plan->view();
+  b->dev.B = n_circ;
+  if (values) {
+    int rc = ks_batch_set_values(b, values, 0, nullptr);
+    if (rc) return fail(rc);
+  }
+  *out = b;
+  return KS_OK;
+}
+
+extern "C" int ks_batch_set_values(ks_batch* b, const double* values, int values_are_device, void* stream) {
+  if (!b || !values) return KS_EINVAL;
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+  size_t nv = b->plan->hp.n_values;
+  size_t bytes = sizeof(double) * nv * b->B;
+  const double* rows = values;
+  if (!values_are_device) {
+    CK(cudaMemcpyAsync(b->d_rows, values, bytes, cudaMemcpyHostToDevice, st));
+    rows = b->d_rows;
+  }
+  if (ks_launch_transpose(rows, b->dev.values, b->B, (int64_t)nv, st)) { set_error("transpose launch failed"); return KS_ECUDA; }
+  b->setup_step = b->setup_stop = -1;
+  int rc = batch_setup(b, 0.0, 0.0, st);
+  if (rc) return rc;
+  if (!stream) CK(cudaStreamSynchronize(st));
+  return KS_OK;
+}
+
+extern "C" void ks_batch_destroy(ks_batch* b) {
+  if (!b) return;
+  cudaFree(b->dev.values); cudaFree(b->dev.derived); cudaFree(b->dev.state); cudaFree(b->dev.work);
+  cudaFree(b->d_rows); cudaFree(b->d_x); cudaFree(b->d_x0); cudaFree(b->d_status); cudaFree(b->d_iters);
+  if (b->h_pin) cudaFreeHost(b->h_pin);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+extern "C" int ks_op_async(ks_batch* b, const ks_options* opt, const double* x0_dev, double* out_x_dev,
+                           int32_t* out_status_dev, int32_t* out_iters_dev, void* stream) {
+  if (!b) return KS_EINVAL;
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+  const ksh::HostPlan& hp = b->plan->hp;
+  KOpts o = make_opts(opt);
+  (void)hp;
+  int rc = batch_setup(b, 0.0, 0.0, st);
+  if (rc) return rc;
+  rc = ks_launch_op(b->dev, o, x0_dev, out_x_dev, out_status_dev, out_iters_dev, opt ? opt->deadline_s : 0.0, st);
+  if (rc == -2) { set_error("ks_op: system too large for the dense kernels"); return KS_EUNSUPPORTED; }
+  if (rc) { set_error(std::string("op kernel launch failed: ") + cudaGetErrorString(cudaGetLastError())); return KS_ECUDA; }
+  return KS_OK;
+}
+
+extern "C" int ks_op(ks_batch* b, const ks_options* opt, const double* x0, double* out_x, int32_t* out_status,
+                     int32_t* out_iters, void* stream) {
+  if (!b) return KS_EINVAL;
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+  const ksh::HostPlan& hp = b->plan->hp;
+  size_t B = b->B, n = hp.n;
+  size_t xbytes = sizeof(double) * n * B;
+  int rc = batch_stage(b, xbytes + 2 * sizeof(int32_t) * B + 64);
+  if (rc) return rc;
+  if (x0) {
+    std::memcpy(b->h_pin, x0, xbytes);
+    CK(cudaMemcpyAsync(b->d_x0, b->h_pin, xbytes, cudaMemcpyHostToDevice, st));
+  }
+  rc = ks_op_async(b, opt, x0 ? b->d_x0 : nullptr, b->d_x, b->d_status, b->d_iters, st);
+  if (rc) return rc;
+  char* hp_bytes = reinterpret_cast<char*>(b->h_pin);
+  CK(cudaMemcpyAsync(hp_bytes, b->d_x, xbytes, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hp_bytes + xbytes, b->d_status, sizeof(int32_t) * B, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hp_bytes + xbytes + sizeof(int32_t) * B, b->d_iters, sizeof(int32_t) * B, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (out_x) std::memcpy(out_x, hp_bytes, xbytes);
+  if (out_status) std::memcpy(out_status, hp_bytes + xbytes, sizeof(int32_t) * B);
+  if (out_iters) std::memcpy(out_iters, hp_bytes + xbytes + sizeof(int32_t) * B, sizeof(int32_t) * B);
+  return KS_OK;
+}

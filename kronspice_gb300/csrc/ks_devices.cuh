@@ -1,0 +1,563 @@
+// ks_devices.cuh — device models of the GB300 engine, evaluated in FP64.
+//
+// One thread evaluates one circuit; every thread of a warp runs the same
+// element program (same topology), so the kind switch is warp-uniform and the
+// per-circuit operands are coalesced columns of the SoA arrays.  The model
+// equations are those of the reference's devices, cited per function.
+// Stamps go into a per-thread dense matrix in shared memory (stride TPB).
+#pragma once
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+#include "ks_engine.h"
+#include "../../include/kronspice_gpu.h"
+
+namespace ksg {
+
+constexpr double kQ = 1.602176634e-19;     // device/diode.go:15
+constexpr double kK = 1.380649e-23;        // device/diode.go:16
+constexpr double kTNom = 300.15;           // device/diode.go:18
+constexpr double kE = 2.718281828459045235360287;
+constexpr double kSqrt2 = 1.41421356237309504880168872;
+constexpr double kPi = 3.14159265358979323846264338;
+constexpr double kEpsOx = 3.9 * 8.854214871e-12;   // device/mosfet.go:117
+constexpr double kEpsSi = 11.7 * 8.854214871e-12;  // device/mosfet.go:118
+constexpr double kNiSi = 1.45e16;                  // device/mosfet.go:119
+
+enum { ModeOP = 0, ModeTranOP = 1, ModeUICInit = 2, ModeTran = 3 };
+enum { BE = 1, TRAP = 2 };
+
+// One circuit's column of a SoA array: element k at p[k * B].
+struct Col {
+  double* p;
+  int64_t B;
+  __device__ __forceinline__ double& operator[](int k) const { return p[(int64_t)k * B]; }
+};
+
+// Per-thread dense system in shared memory, element (i, j) at a[(i*n + j) * T].
+template <int T>
+struct SysRef {
+  double* a;    // matrix  (n*n)
+  double* rhs;  // right-hand side (n)
+  const double* x;  // linearization point X (n)
+  int n;
+  __device__ __forceinline__ void add(int i, int j, double v) const {
+    if (i >= 0 && j >= 0) a[(i * n + j) * T] += v;
+  }
+  __device__ __forceinline__ void addRHS(int i, double v) const {
+    if (i >= 0) rhs[i * T] += v;
+  }
+  __device__ __forceinline__ double X(int i) const { return i >= 0 ? x[i * T] : 0.0; }
+};
+
+struct LoadParams {  // device/device.go:127-148
+  int mode, method;
+  double time, h;
+  bool initJct;
+  double gmin;
+  bool srcStepping;
+  double srcFact;
+};
+
+struct TruncParams { double time, h; int method; double reltol, abstol, vntol, chgtol, trtol; };
+
+__device__ __forceinline__ double xat(const double* x, int i, int T) { return i >= 0 ? x[i * T] : 0.0; }
+
+// ---------------------------------------------------------------- history / LTE
+__device__ inline void hist_push(const Col& S, int h, double t, double q) {  // device/lte.go:23-31
+  S[h + H_T2] = S[h + H_T1]; S[h + H_T1] = S[h + H_T0]; S[h + H_T0] = t;
+  S[h + H_Q2] = S[h + H_Q1]; S[h + H_Q1] = S[h + H_Q0]; S[h + H_Q0] = q;
+  if (S[h + H_N] < 3) S[h + H_N] += 1;
+}
+__device__ inline void hist_reset(const Col& S, int h) { S[h + H_N] = 0; }
+
+// lteStep, device/lte.go:50-85.
+__device__ inline double lte_step(const Col& S, int h, double qn, double in, double inPrev, double absTol,
+                                  const TruncParams& tc) {
+  int k = tc.method;
+  if (k < 1 || k > 2 || S[h + H_N] < k + 1) return CUDART_INF;
+  double ts[4] = {tc.time, S[h + H_T0], S[h + H_T1], S[h + H_T2]};
+  double dd[4] = {qn, S[h + H_Q0], S[h + H_Q1], S[h + H_Q2]};
+  for (int order = 1; order <= k + 1; order++) {
+    for (int i = 0; i + order <= k + 1; i++) {
+      double den = ts[i] - ts[i + order];
+      if (den == 0) return CUDART_INF;
+      dd[i] = (dd[i] - dd[i + 1]) / den;
+    }
+  }
+  double fact = k == 2 ? 6.0 : 2.0, c = k == 2 ? 1.0 / 12 : 0.5;
+  double hh = tc.h;
+  double errI = c * (k == 2 ? hh * hh : hh) * fabs(dd[0] * fact);
+  if (errI == 0 || isnan(errI)) return CUDART_INF;
+  double qmax = fmax(fabs(qn), fabs(S[h + H_Q0]));
+  double allowed = tc.trtol * fmax(tc.reltol * fmax(fabs(in), fabs(inPrev)) + absTol, tc.reltol * fmax(qmax, tc.chgtol) / hh);
+  return k == 2 ? hh * sqrt(allowed / errI) : hh * (allowed / errI);
+}
+
+// pnjlim, device/diode.go:214-226.
+__device__ __forceinline__ double pnjlim(double vnew, double vold, double vt, double vcrit, bool* lim) {
+  if (vnew > vcrit && fabs(vnew - vold) > 2 * vt) {
+    *lim = true;
+    if (vold > 0) {
+      double arg = 1 + (vnew - vold) / vt;
+      return arg > 0 ? vold + vt * log(arg) : vcrit;
+    }
+    return vt * log(vnew / vt);
+  }
+  *lim = false;
+  return vnew;
+}
+
+// ---------------------------------------------------------------- waveforms
+// resolveWave, device/waveform.go:25-66: into the derived block a[0..6].
+__device__ inline void wave_resolve(int kind, const Col& V, int args, int nargs, const Col& D, int d,
+                                    double step, double stop) {
+  if (step <= 0) step = 1e-9;
+  if (stop <= 0) stop = 1e-6;
+  auto arg = [&](int i, double def) { return i < nargs ? V[args + i] : def; };
+  double a[7] = {0, 0, 0, 0, 0, 0, 0};
+  if (kind == KS_WAVE_PULSE) {
+    a[0] = arg(0, 0); a[1] = arg(1, 0); a[2] = arg(2, 0); a[3] = arg(3, step); a[4] = arg(4, step);
+    a[5] = arg(5, stop); a[6] = arg(6, stop);
+    if (a[3] == 0) a[3] = step;
+    if (a[4] == 0) a[4] = step;
+  } else if (kind == KS_WAVE_SIN) {
+    a[0] = arg(0, 0); a[1] = arg(1, 0); a[2] = arg(2, 1 / stop); a[3] = arg(3, 0); a[4] = arg(4, 0); a[5] = arg(5, 0);
+  } else if (kind == KS_WAVE_EXP) {
+    double td1 = arg(2, 0);
+    a[0] = arg(0, 0); a[1] = arg(1, 0); a[2] = td1; a[3] = arg(3, step); a[4] = arg(4, td1 + step); a[5] = arg(5, step);
+    if (a[3] == 0) a[3] = step;
+    if (a[5] == 0) a[5] = step;
+  }
+  for (int i = 0; i < 7; i++) D[d + i] = a[i];
+}
+
+// wave.value, device/waveform.go:69-126.
+__device__ inline double wave_value(int kind, const Col& D, int d, const Col& V, int args, int nargs, double t) {
+  if (kind == KS_WAVE_PULSE) {
+    double v1 = D[d], v2 = D[d + 1], td = D[d + 2], tr = D[d + 3], tf = D[d + 4], pw = D[d + 5], per = D[d + 6];
+    if (t < td) return v1;
+    double tt = t - td;
+    if (per > 0) tt = fmod(tt, per);
+    if (tt < tr) return v1 + (v2 - v1) * tt / tr;
+    if (tt < tr + pw) return v2;
+    if (tt < tr + pw + tf) return v2 + (v1 - v2) * (tt - tr - pw) / tf;
+    return v1;
+  }
+  if (kind == KS_WAVE_SIN) {
+    double vo = D[d], va = D[d + 1], f = D[d + 2], td = D[d + 3], theta = D[d + 4], ph = D[d + 5] * kPi / 180;
+    if (t < td) return vo + va * sin(ph);
+    double tt = t - td;
+    return vo + va * exp(-tt * theta) * sin(2 * kPi * f * tt + ph);
+  }
+  if (kind == KS_WAVE_EXP) {
+    double v1 = D[d], v2 = D[d + 1], td1 = D[d + 2], tau1 = D[d + 3], td2 = D[d + 4], tau2 = D[d + 5];
+    if (t < td1) return v1;
+    if (t < td2) return v1 + (v2 - v1) * (1 - exp(-(t - td1) / tau1));
+    return v1 + (v2 - v1) * (1 - exp(-(t - td1) / tau1)) + (v1 - v2) * (1 - exp(-(t - td2) / tau2));
+  }
+  if (kind == KS_WAVE_PWL) {
+    int n = nargs / 2;
+    if (t <= V[args]) return V[args + 1];
+    if (t >= V[args + 2 * (n - 1)]) return V[args + 2 * n - 1];
+    int k = 1;
+    while (k < n && !(V[args + 2 * k] > t)) k++;
+    double t0 = V[args + 2 * (k - 1)], v0 = V[args + 2 * (k - 1) + 1], t1 = V[args + 2 * k], v1 = V[args + 2 * k + 1];
+    if (t1 == t0) return v1;
+    return v0 + (v1 - v0) * (t - t0) / (t1 - t0);
+  }
+  return 0;
+}
+
+// wave.nextBreakpoint, device/waveform.go:190-239.
+__device__ inline double wave_next_breakpoint(int kind, const Col& D, int d, const Col& V, int args, int nargs, double t) {
+  const double rel = 1e-12;
+  double lim = t + rel * fmax(fabs(t), 1e-15);
+  if (kind == KS_WAVE_PULSE) {
+    double td = D[d + 2], tr = D[d + 3], tf = D[d + 4], pw = D[d + 5], per = D[d + 6];
+    double edges[4] = {0, tr, tr + pw, tr + pw + tf};
+    if (per <= 0) {
+      for (int i = 0; i < 4; i++) if (td + edges[i] > lim) return td + edges[i];
+      return CUDART_INF;
+    }
+    double k = floor((t - td) / per);
+    if (k < 0) k = 0;
+    for (double kk = k; kk <= k + 1; kk++) {
+      double base = td + kk * per;
+      for (int i = 0; i < 4; i++) if (base + edges[i] > lim) return base + edges[i];
+    }
+    return td + (k + 2) * per;
+  }
+  if (kind == KS_WAVE_SIN) { if (D[d + 3] > lim) return D[d + 3]; }
+  else if (kind == KS_WAVE_EXP) {
+    if (D[d + 2] > lim) return D[d + 2];
+    if (D[d + 4] > lim) return D[d + 4];
+  } else if (kind == KS_WAVE_PWL) {
+    for (int k = 0; k < nargs / 2; k++) if (V[args + 2 * k] > lim) return V[args + 2 * k];
+  }
+  return CUDART_INF;
+}
+
+// sourceValue.at, device/source.go:43-66 (SV_OVR/SV_OVRON: the .DC override).
+__device__ inline double source_at(const KElem& e, const Col& V, const Col& D, const Col& S, const LoadParams& lp) {
+  double v;
+  if (S[SV_OVRON] != 0 && lp.mode == ModeOP) v = S[SV_OVR];
+  else if (e.wave == KS_WAVE_NONE) v = V[e.param + KS_SRC_P_DC];
+  else if (lp.mode == ModeOP && (e.flags & KS_F_HAS_DC)) v = V[e.param + KS_SRC_P_DC];
+  else v = wave_value(e.wave, D, e.derived, V, e.param + KS_SRC_P_ARGS, e.nargs, lp.mode == ModeTran ? lp.time : 0.0);
+  if (lp.srcStepping && lp.mode != ModeTran) v *= lp.srcFact;
+  return v;
+}
+
+// ---------------------------------------------------------------- diode
+// current, device/diode.go:148-162 (dd: derived block of the diode).
+__device__ inline void diode_iv(const Col& V, const Col& Dv, int p, int dd, bool hasBV, double v, double* id, double* g) {
+  double IS = V[p + KS_D_P_IS], vte = Dv[dd + DD_VTE];
+  if (v >= -3 * vte) {
+    double e = exp(fmin(v / vte, 700.0));
+    *id = IS * (e - 1); *g = IS * e / vte; return;
+  }
+  double xbv = Dv[dd + DD_XBV];
+  if (!hasBV || v >= -xbv) {
+    double a = 3 * vte / (v * kE); a = a * a * a;
+    *id = -IS * (1 + a); *g = IS * 3 * a / v; return;
+  }
+  double e = exp(fmin(-(xbv + v) / vte, 700.0));
+  *id = -IS * e; *g = IS * e / vte;
+}
+
+// charge, device/diode.go:191-211.
+__device__ inline void diode_charge(const Col& V, int p, double v, double id, double g, double* q, double* c) {
+  double TT = V[p + KS_D_P_TT], CJO = V[p + KS_D_P_CJO], VJ = V[p + KS_D_P_VJ], M = V[p + KS_D_P_M], FC = V[p + KS_D_P_FC];
+  *q = TT * id; *c = TT * g;
+  if (CJO == 0) return;
+  double fcv = FC * VJ;
+  if (v < fcv) {
+    double arg = 1 - v / VJ, sarg = pow(arg, -M);
+    *q += CJO * VJ * (1 - arg * sarg) / (1 - M);
+    *c += CJO * sarg;
+    return;
+  }
+  double f1 = VJ * (1 - pow(1 - FC, 1 - M)) / (1 - M), f2 = pow(1 - FC, 1 + M), f3 = 1 - FC * (1 + M);
+  *q += CJO * f1 + CJO / f2 * (f3 * (v - fcv) + M / (2 * VJ) * (v * v - fcv * fcv));
+  *c += CJO / f2 * (f3 + M * v / VJ);
+}
+
+// Load, device/diode.go:229-275.
+template <int T>
+__device__ inline void diode_load(const KElem& e, const Col& V, const Col& Dv, const Col& S, const SysRef<T>& sys,
+                                  const LoadParams& lp) {
+  int p = e.param, dd = e.derived;
+  int a = e.u[0], k = e.u[1], ai = e.u[2];
+  bool hasBV = e.flags & KS_F_HAS_BV;
+  double vte = Dv[dd + DD_VTE], vcrit = Dv[dd + DD_VCRIT], xbv = Dv[dd + DD_XBV];
+  double vraw = sys.X(ai) - sys.X(k);
+  double vd;
+  bool lim;
+  if (lp.initJct) { vd = vcrit; lim = true; }
+  else {
+    double vacc = S[SD_VDACC];
+    vd = pnjlim(vraw, vacc, vte, vcrit, &lim);
+    if (hasBV && vraw < fmin(0.0, -xbv + 10 * vte)) {
+      bool l2;
+      double vt = pnjlim(-(vraw + xbv), -(vacc + xbv), vte, vcrit, &l2);
+      vd = -(vt + xbv); lim = l2;
+    }
+  }
+  S[SD_VDACC] = vd;
+  double id, g0;
+  diode_iv(V, Dv, p, dd, hasBV, vd, &id, &g0);
+  double cd = id + lp.gmin * vd, gd = g0 + lp.gmin;
+  double iq = 0, geq = 0;
+  bool tran = false;
+  if (lp.mode == ModeTran && (V[p + KS_D_P_CJO] > 0 || V[p + KS_D_P_TT] > 0)) {
+    double q, c;
+    diode_charge(V, p, vd, id, g0, &q, &c);
+    tran = true;
+    if (lp.method == TRAP) { iq = 2 * (q - S[SD_QPREV]) / lp.h - S[SD_IQPREV]; geq = 2 * c / lp.h; }
+    else { iq = (q - S[SD_QPREV]) / lp.h; geq = c / lp.h; }
+  }
+  S[SD_VD] = vd; S[SD_CD] = cd; S[SD_GD] = gd; S[SD_IQ] = iq; S[SD_GEQ] = geq;
+  S[SD_LIM] = lim ? 1.0 : 0.0; S[SD_TRAN] = tran ? 1.0 : 0.0;
+  double gg = gd + geq, ieq = cd + iq - gg * vd;
+  sys.add(ai, ai, gg); sys.add(k, k, gg); sys.add(ai, k, -gg); sys.add(k, ai, -gg);
+  sys.addRHS(ai, -ieq); sys.addRHS(k, ieq);
+  double grs = Dv[dd + DD_GRS];
+  if (grs > 0) { sys.add(a, a, grs); sys.add(ai, ai, grs); sys.add(a, ai, -grs); sys.add(ai, a, -grs); }
+}
+
+// ConvTest, device/diode.go:282-289.
+template <int T>
+__device__ inline bool diode_conv(const KElem& e, const Col& V, const Col& Dv, const Col& S, const double* x,
+                                  double reltol, double abstol, double gmin) {
+  double v = xat(x, e.u[2], T) - xat(x, e.u[1], T);
+  double cdhat = S[SD_CD] + S[SD_GD] * (v - S[SD_VD]);
+  double id, g;
+  diode_iv(V, Dv, e.param, e.derived, e.flags & KS_F_HAS_BV, v, &id, &g);
+  double cdn = id + gmin * v;
+  return fabs(cdhat - cdn) <= reltol * fmax(fabs(cdhat), fabs(cdn)) + abstol;
+}
+
+// Accept, device/diode.go:304-322.
+template <int T>
+__device__ inline void diode_accept(const KElem& e, const Col& V, const Col& Dv, const Col& S, const double* x,
+                                    double t, int mode) {
+  double v = xat(x, e.u[2], T) - xat(x, e.u[1], T);
+  S[SD_VDACC] = v;
+  double id, g, q, c;
+  diode_iv(V, Dv, e.param, e.derived, e.flags & KS_F_HAS_BV, v, &id, &g);
+  diode_charge(V, e.param, v, id, g, &q, &c);
+  if (mode == ModeTran) S[SD_IQPREV] = S[SD_TRAN] != 0 ? S[SD_IQ] + S[SD_GEQ] * (v - S[SD_VD]) : 0.0;
+  else { S[SD_IQPREV] = 0; hist_reset(S, SD_HIST); }
+  S[SD_QPREV] = q;
+  hist_push(S, SD_HIST, t, q);
+}
+
+// ---------------------------------------------------------------- BJT
+// junction, device/bjt.go:272-283.
+__device__ __forceinline__ void junction(double is, double v, double nvt, double* i, double* g) {
+  if (is == 0) { *i = 0; *g = 0; return; }
+  if (v >= -3 * nvt) {
+    double e = exp(fmin(v / nvt, 700.0));
+    *i = is * (e - 1); *g = is * e / nvt; return;
+  }
+  double a = 3 * nvt / (v * kE); a = a * a * a;
+  *i = -is * (1 + a); *g = is * 3 * a / v;
+}
+
+struct BjtDC { double cbe, gbe, cbc, gbc, it, itBE, itBC, ibe, gpi, ibc, gmu, qb, dqbdve, dqbdvc, gx; };
+
+// evalDC, device/bjt.go:294-354.
+__device__ inline BjtDC bjt_eval_dc(const Col& V, const Col& Dv, int p, int dd, double vbe, double vbc, double gmin) {
+  BjtDC d;
+  double vt = Dv[dd + DQ_VT];
+  junction(V[p + KS_Q_P_IS], vbe, V[p + KS_Q_P_NF] * vt, &d.cbe, &d.gbe);
+  double cben, gben;
+  junction(V[p + KS_Q_P_ISE], vbe, V[p + KS_Q_P_NE] * vt, &cben, &gben);
+  cben += gmin * vbe; gben += gmin;
+  junction(V[p + KS_Q_P_IS], vbc, V[p + KS_Q_P_NR] * vt, &d.cbc, &d.gbc);
+  double cbcn, gbcn;
+  junction(V[p + KS_Q_P_ISC], vbc, V[p + KS_Q_P_NC] * vt, &cbcn, &gbcn);
+  cbcn += gmin * vbc; gbcn += gmin;
+  double VAF = V[p + KS_Q_P_VAF], VAR = V[p + KS_Q_P_VAR], IKF = V[p + KS_Q_P_IKF], IKR = V[p + KS_Q_P_IKR];
+  double ivaf = VAF > 0 ? 1 / VAF : 0, ivar = VAR > 0 ? 1 / VAR : 0;
+  double oik = IKF > 0 ? 1 / IKF : 0, oikr = IKR > 0 ? 1 / IKR : 0;
+  double q1 = 1 / (1 - ivaf * vbc - ivar * vbe);
+  if (oik == 0 && oikr == 0) {
+    d.qb = q1; d.dqbdve = q1 * d.qb * ivar; d.dqbdvc = q1 * d.qb * ivaf;
+  } else {
+    double q2 = oik * d.cbe + oikr * d.cbc;
+    double arg = fmax(0.0, 1 + 4 * q2);
+    double sq = arg != 0 ? sqrt(arg) : 1.0;
+    d.qb = q1 * (1 + sq) / 2;
+    d.dqbdve = q1 * (d.qb * ivar + oik * d.gbe / sq);
+    d.dqbdvc = q1 * (d.qb * ivaf + oikr * d.gbc / sq);
+  }
+  d.it = (d.cbe - d.cbc) / d.qb;
+  d.itBE = (d.gbe - d.it * d.dqbdve) / d.qb;
+  d.itBC = (-d.gbc - d.it * d.dqbdvc) / d.qb;
+  double BF = V[p + KS_Q_P_BF], BR = V[p + KS_Q_P_BR];
+  d.ibe = d.cbe / BF + cben; d.gpi = d.gbe / BF + gben;
+  d.ibc = d.cbc / BR + cbcn; d.gmu = d.gbc / BR + gbcn;
+  double rbpr = Dv[dd + DQ_RBPR], rbpi = Dv[dd + DQ_RBPI];
+  double gx = rbpr + rbpi / d.qb;
+  double IRB = V[p + KS_Q_P_IRB];
+  if (IRB > 0 && rbpi != 0) {
+    double cb = d.ibe + d.ibc;
+    double a1 = fmax(cb / IRB, 1e-9);
+    double z = (-1 + sqrt(1 + 14.59025 * a1)) / 2.4317 / sqrt(a1);
+    double tz = tan(z);
+    gx = rbpr + 3 * rbpi * (tz - z) / z / tz / tz;
+  }
+  d.gx = gx != 0 ? 1 / gx : 0;
+  return d;
+}
+
+// depletion, device/bjt.go:358-370.
+__device__ inline void depletion(double v, double cz, double vj, double m, double fc, double f1, double f2, double f3,
+                                 double* q, double* c) {
+  if (cz == 0) { *q = 0; *c = 0; return; }
+  double fcv = fc * vj;
+  if (v < fcv) {
+    double arg = 1 - v / vj, sarg = exp(-m * log(arg));
+    *q = vj * cz * (1 - arg * sarg) / (1 - m); *c = cz * sarg; return;
+  }
+  double czf2 = cz / f2;
+  *q = cz * f1 + czf2 * (f3 * (v - fcv) + (m / (vj + vj)) * (v * v - fcv * fcv));
+  *c = czf2 * (f3 + m * v / vj);
+}
+
+struct BjtCh { double q[4], c[4], dqbeDvbc; };
+
+// charges, device/bjt.go:373-412.
+__device__ inline BjtCh bjt_charges(const Col& V, const Col& Dv, int p, int dd, double vbe, double vbc, double vbx,
+                                    double vcs, const BjtDC& d) {
+  BjtCh ch;
+  ch.dqbeDvbc = 0;
+  double cbe = d.cbe, gbe = d.gbe;
+  double TF = V[p + KS_Q_P_TF], XTF = V[p + KS_Q_P_XTF], ITF = V[p + KS_Q_P_ITF], ovtf = Dv[dd + DQ_OVTF];
+  if (TF != 0 && vbe > 0) {
+    double argtf = 0, arg2 = 0, arg3 = 0;
+    if (XTF != 0) {
+      argtf = XTF;
+      if (ovtf != 0) argtf *= exp(vbc * ovtf);
+      arg2 = argtf;
+      if (ITF != 0) {
+        double t = cbe / (cbe + ITF);
+        argtf *= t * t;
+        arg2 = argtf * (3 - t - t);
+      }
+      arg3 = cbe * argtf * ovtf;
+    }
+    cbe = cbe * (1 + argtf) / d.qb;
+    gbe = (gbe * (1 + arg2) - cbe * d.dqbdve) / d.qb;
+    ch.dqbeDvbc = TF * (arg3 - cbe * d.dqbdvc) / d.qb;
+  }
+  double qd, cd;
+  double FC = V[p + KS_Q_P_FC];
+  depletion(vbe, V[p + KS_Q_P_CJE], V[p + KS_Q_P_VJE], V[p + KS_Q_P_MJE], FC, Dv[dd + DQ_F1E], Dv[dd + DQ_F2E],
+            Dv[dd + DQ_F3E], &qd, &cd);
+  ch.q[0] = TF * cbe + qd; ch.c[0] = TF * gbe + cd;
+  double CJC = V[p + KS_Q_P_CJC], czbc = CJC * V[p + KS_Q_P_XCJC];
+  double VJC = V[p + KS_Q_P_VJC], MJC = V[p + KS_Q_P_MJC];
+  depletion(vbc, czbc, VJC, MJC, FC, Dv[dd + DQ_F1C], Dv[dd + DQ_F2C], Dv[dd + DQ_F3C], &qd, &cd);
+  double TR = V[p + KS_Q_P_TR];
+  ch.q[1] = TR * d.cbc + qd; ch.c[1] = TR * d.gbc + cd;
+  depletion(vbx, CJC - czbc, VJC, MJC, FC, Dv[dd + DQ_F1C], Dv[dd + DQ_F2C], Dv[dd + DQ_F3C], &ch.q[2], &ch.c[2]);
+  ch.q[3] = 0; ch.c[3] = 0;
+  double CJS = V[p + KS_Q_P_CJS];
+  if (CJS != 0) {
+    double VJS = V[p + KS_Q_P_VJS], MJS = V[p + KS_Q_P_MJS];
+    if (vcs < 0) {
+      double arg = 1 - vcs / VJS, sarg = exp(-MJS * log(arg));
+      ch.q[3] = VJS * CJS * (1 - arg * sarg) / (1 - MJS); ch.c[3] = CJS * sarg;
+    } else {
+      ch.q[3] = vcs * CJS * (1 + MJS * vcs / (2 * VJS)); ch.c[3] = CJS * (1 + MJS * vcs / VJS);
+    }
+  }
+  return ch;
+}
+
+template <int T>
+__device__ inline void bjt_voltages(const KElem& e, const Col& V, const double* x, double* vbe, double* vbc,
+                                    double* vbx, double* vcs) {  // device/bjt.go:415-419
+  double t = (e.flags & KS_F_PTYPE) ? -1.0 : 1.0;
+  double vb = xat(x, e.u[2], T), vbp = xat(x, e.u[5], T), vcp = xat(x, e.u[4], T), vep = xat(x, e.u[6], T);
+  *vbe = t * (vbp - vep); *vbc = t * (vbp - vcp); *vbx = t * (vb - vcp);
+  *vcs = t * (xat(x, e.u[7], T) - xat(x, e.u[8], T));
+}
+
+template <int T>
+__device__ __forceinline__ void bjt_branch(const SysRef<T>& s, double typ, int a, int b, double i0, double g1, int p1,
+                                           int n1, double v10, double g2, int p2, int n2, double v20) {  // :463-480
+  if (g1 != 0) { s.add(a, p1, g1); s.add(a, n1, -g1); s.add(b, p1, -g1); s.add(b, n1, g1); }
+  if (g2 != 0) { s.add(a, p2, g2); s.add(a, n2, -g2); s.add(b, p2, -g2); s.add(b, n2, g2); }
+  double ieq = typ * (i0 - g1 * v10 - g2 * v20);
+  s.addRHS(a, -ieq); s.addRHS(b, ieq);
+}
+
+template <int T>
+__device__ __forceinline__ void stamp_g(const SysRef<T>& s, int a, int b, double g) {  // device/bjt.go:482-490
+  if (g == 0) return;
+  s.add(a, a, g); s.add(b, b, g); s.add(a, b, -g); s.add(b, a, -g);
+}
+
+// Load + stamp, device/bjt.go:422-515.
+template <int T>
+__device__ inline void bjt_load(const KElem& e, const Col& V, const Col& Dv, const Col& S, const SysRef<T>& sys,
+                                const LoadParams& lp) {
+  int p = e.param, dd = e.derived;
+  double vt = Dv[dd + DQ_VT], vcrit = Dv[dd + DQ_VCRIT];
+  double vbe, vbc, vbx, vcs;
+  bjt_voltages<T>(e, V, sys.x, &vbe, &vbc, &vbx, &vcs);
+  bool lim;
+  if (lp.initJct) { vbe = vcrit; vbc = 0; lim = true; vbx = 0; vcs = 0; }
+  else {
+    bool l1, l2;
+    vbe = pnjlim(vbe, S[SQ_VBEACC], vt, vcrit, &l1);
+    vbc = pnjlim(vbc, S[SQ_VBCACC], vt, vcrit, &l2);
+    lim = l1 || l2;
+  }
+  S[SQ_VBEACC] = vbe; S[SQ_VBCACC] = vbc;
+  S[SQ_VBE] = vbe; S[SQ_VBC] = vbc; S[SQ_VBX] = vbx; S[SQ_VCS] = vcs;
+  BjtDC d = bjt_eval_dc(V, Dv, p, dd, vbe, vbc, lp.gmin);
+  double isub, gsub;
+  junction(V[p + KS_Q_P_ISS], vcs, V[p + KS_Q_P_NS] * vt, &isub, &gsub);
+  isub += lp.gmin * vcs; gsub += lp.gmin;
+  S[SQ_CBE] = d.cbe; S[SQ_GBE] = d.gbe; S[SQ_CBC] = d.cbc; S[SQ_GBC] = d.gbc; S[SQ_IT] = d.it;
+  S[SQ_ITBE] = d.itBE; S[SQ_ITBC] = d.itBC; S[SQ_IBE] = d.ibe; S[SQ_GPI] = d.gpi; S[SQ_IBC] = d.ibc;
+  S[SQ_GMU] = d.gmu; S[SQ_QB] = d.qb; S[SQ_DQBDVE] = d.dqbdve; S[SQ_DQBDVC] = d.dqbdvc; S[SQ_GX] = d.gx;
+  S[SQ_ISUB] = isub; S[SQ_GSUB] = gsub; S[SQ_LIM] = lim ? 1.0 : 0.0;
+  bool hasCharge = V[p + KS_Q_P_CJE] > 0 || V[p + KS_Q_P_CJC] > 0 || V[p + KS_Q_P_CJS] > 0 ||
+                   V[p + KS_Q_P_TF] > 0 || V[p + KS_Q_P_TR] > 0;
+  bool tran = lp.mode == ModeTran && hasCharge;
+  double ag = 0, iq[4] = {0, 0, 0, 0};
+  BjtCh ch;
+  if (tran) {
+    ch = bjt_charges(V, Dv, p, dd, vbe, vbc, vbx, vcs, d);
+    ag = lp.method == TRAP ? 2 / lp.h : 1 / lp.h;
+    for (int k = 0; k < 4; k++) {
+      iq[k] = ag * (ch.q[k] - S[SQ_QPREV0 + k]);
+      if (lp.method == TRAP) iq[k] -= S[SQ_IQPREV0 + k];
+      S[SQ_C0 + k] = ch.c[k];
+    }
+    S[SQ_DQBEDVBC] = ch.dqbeDvbc;
+  }
+  S[SQ_TRAN] = tran ? 1.0 : 0.0; S[SQ_AG] = ag;
+  for (int k = 0; k < 4; k++) S[SQ_IQ0 + k] = iq[k];
+  double typ = (e.flags & KS_F_PTYPE) ? -1.0 : 1.0;
+  int b = e.u[2], cp = e.u[4], bp = e.u[5], ep = e.u[6], sa = e.u[7], sb = e.u[8];
+  bjt_branch<T>(sys, typ, cp, ep, d.it, d.itBE, bp, ep, vbe, d.itBC, bp, cp, vbc);
+  bjt_branch<T>(sys, typ, bp, ep, d.ibe, d.gpi, bp, ep, vbe, 0, 0, 0, 0);
+  bjt_branch<T>(sys, typ, bp, cp, d.ibc, d.gmu, bp, cp, vbc, 0, 0, 0, 0);
+  bjt_branch<T>(sys, typ, sa, sb, isub, gsub, sa, sb, vcs, 0, 0, 0, 0);
+  if (tran) {
+    bjt_branch<T>(sys, typ, bp, ep, iq[0], ag * ch.c[0], bp, ep, vbe, ag * ch.dqbeDvbc, bp, cp, vbc);
+    bjt_branch<T>(sys, typ, bp, cp, iq[1], ag * ch.c[1], bp, cp, vbc, 0, 0, 0, 0);
+    bjt_branch<T>(sys, typ, b, cp, iq[2], ag * ch.c[2], b, cp, vbx, 0, 0, 0, 0);
+    bjt_branch<T>(sys, typ, sa, sb, iq[3], ag * ch.c[3], sa, sb, vcs, 0, 0, 0, 0);
+  }
+  if (bp != b) stamp_g<T>(sys, b, bp, d.gx);
+  if (cp != e.u[0]) stamp_g<T>(sys, e.u[0], cp, Dv[dd + DQ_GCPR]);
+  if (ep != e.u[1]) stamp_g<T>(sys, e.u[1], ep, Dv[dd + DQ_GEPR]);
+}
+
+// ConvTest, device/bjt.go:522-532.
+template <int T>
+__device__ inline bool bjt_conv(const KElem& e, const Col& V, const Col& Dv, const Col& S, const double* x,
+                                double reltol, double abstol, double gmin) {
+  double vbe, vbc, vbx, vcs;
+  bjt_voltages<T>(e, V, x, &vbe, &vbc, &vbx, &vcs);
+  double dbe = vbe - S[SQ_VBE], dbc = vbc - S[SQ_VBC];
+  double ichat = S[SQ_IT] - S[SQ_IBC] + S[SQ_ITBE] * dbe + (S[SQ_ITBC] - S[SQ_GMU]) * dbc;
+  double ibhat = S[SQ_IBE] + S[SQ_IBC] + S[SQ_GPI] * dbe + S[SQ_GMU] * dbc;
+  BjtDC n = bjt_eval_dc(V, Dv, e.param, e.derived, vbe, vbc, gmin);
+  double ic = n.it - n.ibc, ib = n.ibe + n.ibc;
+  return fabs(ichat - ic) <= reltol * fmax(fabs(ichat), fabs(ic)) + abstol &&
+         fabs(ibhat - ib) <= reltol * fmax(fabs(ibhat), fabs(ib)) + abstol;
+}
+
+// Accept, device/bjt.go:579-601.
+template <int T>
+__device__ inline void bjt_accept(const KElem& e, const Col& V, const Col& Dv, const Col& S, const double* x,
+                                  double t, int mode, double gmin) {
+  double vbe, vbc, vbx, vcs;
+  bjt_voltages<T>(e, V, x, &vbe, &vbc, &vbx, &vcs);
+  S[SQ_VBEACC] = vbe; S[SQ_VBCACC] = vbc;
+  BjtDC d = bjt_eval_dc(V, Dv, e.param, e.derived, vbe, vbc, gmin);
+  BjtCh ch = bjt_charges(V, Dv, e.param, e.derived, vbe, vbc, vbx, vcs, d);
+  double dv[4] = {vbe - S[SQ_VBE], vbc - S[SQ_VBC], vbx - S[SQ_VBX], vcs - S[SQ_VCS]};
+  bool tran = S[SQ_TRAN] != 0;
+  for (int k = 0; k < 4; k++) {
+    if (mode == ModeTran && tran) {
+      double i = S[SQ_IQ0 + k] + S[SQ_AG] * S[SQ_C0 + k] * dv[k];
+      if (k == 0) i += S[SQ_AG] * S[SQ_DQBEDVBC] * dv[1];
+      S[SQ_IQPREV0 + k] = i;
+    } else S[SQ_IQPREV0 + k] = 0;
+    if (mode != ModeTran) hist_reset(S, SQ_HIST + k * H_SIZE);
+    S[SQ_QPREV0 + k] = ch.q[k];
+    hist_push(S, SQ_HIST + k * H_SIZE, t, ch.q[k]);
+  }
+}
+
+}  // namespace ksg

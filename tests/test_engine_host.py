@@ -1,0 +1,119 @@
+"""CPU-only checks of the engine's C ABI: the library loads, exports every symbol
+include/kronspice_gpu.h declares, and its host symbolic pass (unknown layout,
+validation) agrees with the oracle and the reference's Validate semantics.
+No compute call is made (no GPU here)."""
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+from kronspice_gb300 import _lib, analysis, build
+from kronspice_gb300 import circuit as kc
+from oracle import oracle as orc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def header_symbols():
+    with open(os.path.join(ROOT, "include", "kronspice_gpu.h")) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ks_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    syms = header_symbols()
+    assert len(syms) >= 12
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(syms) == set(_lib.EXPORTS) | (set(syms) - set(_lib.EXPORTS)) and set(_lib.EXPORTS) <= set(syms)
+
+
+def test_version(lib):
+    assert b"sm_103a" in lib.ks_version()
+
+
+with open(os.path.join(ROOT, "tests", "golden", "reference_cases.json")) as f:
+    CASES = [c for c in json.load(f)["cases"] if not c["skip"]]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_unknown_layout_matches_oracle(lib, case):
+    ckt = kc.from_dict(case["circuit"])
+    el, vals, _ = ckt.pack()
+    n = np.zeros(1, dtype=np.int32)
+    isv = np.zeros(1024, dtype=np.int32)
+    topo = _lib.KsTopology(ckt.n_nodes, len(el), len(vals), 0, el.ctypes.data)
+    import ctypes
+    assert lib.ks_unknowns(ctypes.byref(topo), n.ctypes.data, isv.ctypes.data) == 0
+    no, isvo = orc.unknowns(orc.Packed.of(ckt))
+    assert n[0] == no
+    assert np.array_equal(isv[:no].astype(bool), isvo)
+    assert analysis.validate(ckt) is None
+
+
+def _rv(extra):
+    b = kc.Builder("v")
+    b.voltage_source("V1", "a", "0", 1.0)
+    extra(b)
+    return b.build()
+
+
+def test_validate_floating_node(lib):
+    # TestFloatingNodeRejected, analysis/op_test.go:100-111
+    b = kc.Builder("f")
+    b.resistor("R1", "a", "0", 1.0)
+    b.current_source("I1", "b", "0", 1.0)
+    err = analysis.validate(b.build())
+    assert isinstance(err, analysis.ErrFloatingNode)
+    # a capacitor is a path only for a transient without operating point (ValidateTransient)
+    b = kc.Builder("c")
+    b.voltage_source("V1", "a", "0", 1.0)
+    b.resistor("R1", "a", "b", 1.0)
+    b.capacitor("C1", "b", "c", 1e-9)
+    b.resistor("R2", "c", "d", 1.0)
+    c = b.build()
+    assert isinstance(analysis.validate(c), analysis.ErrFloatingNode)
+    assert analysis.validate(c, transient=True) is None
+
+
+def test_validate_bad_values(lib):
+    c = _rv(lambda b: b.resistor("R1", "a", "0", 0.0))
+    assert isinstance(analysis.validate(c), analysis.ErrValidation)
+    c = _rv(lambda b: b.capacitor("C1", "a", "0", -1e-9))
+    assert isinstance(analysis.validate(c), analysis.ErrValidation)
+    c = _rv(lambda b: b.resistor("R1", "a", "a", 1.0))
+    assert "itself" in str(analysis.validate(c))
+    c = _rv(lambda b: b.resistor("R1", "a", "0", float("nan")))
+    assert isinstance(analysis.validate(c), analysis.ErrValidation)
+    # negative resistance is allowed (device/passive.go:21-31)
+    c = _rv(lambda b: b.resistor("R1", "a", "0", -5.0))
+    assert analysis.validate(c) is None
+
+
+def test_validate_waveforms(lib):
+    b = kc.Builder("w")
+    b.voltage_wave("V1", "a", "0", "pulse", [0, 1, -1e-9])
+    b.resistor("R1", "a", "0", 1.0)
+    assert "PULSE" in str(analysis.validate(b.build()))
+    b = kc.Builder("w")
+    b.voltage_wave("V1", "a", "0", "pwl", [0, 0, 2e-9, 1, 1e-9, 0])
+    b.resistor("R1", "a", "0", 1.0)
+    assert "PWL" in str(analysis.validate(b.build()))
+
+
+def test_workload_batches_are_seeded():
+    from kronspice_gb300 import workloads as w
+    el, nn, v1 = w.bjt_ce_batch(64, 3)
+    _, _, v2 = w.bjt_ce_batch(64, 3)
+    _, _, v3 = w.bjt_ce_batch(64, 4)
+    assert np.array_equal(v1, v2) and not np.array_equal(v1, v3)
+    assert v1.shape == (64, len(w.bjt_ce_template().pack()[1]))
