@@ -54,7 +54,7 @@ def dist_env():
     return rank, world, local
 
 
-def cpu_baseline(el, nn, vals, min_wall=1.0, max_passes=20):
+def cpu_baseline(el, nn, vals, min_wall=1.0, max_passes=400):
     """Oracle (CPU restatement of the reference path) over all host threads."""
     from oracle import oracle as orc
     orc.build()
@@ -193,7 +193,8 @@ def main():
     plan = analysis.Plan(el, nn, vals.shape[1])
     batch = analysis.Batch(plan, vals)
     n = plan.n
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)  # a real stream: kernels and events on the same one
+    torch.cuda.set_stream(stream)
     sh = ctypes.c_void_p(stream.cuda_stream)
     x_dev = torch.empty((B, n), dtype=torch.float64, device=dev)
     st_dev = torch.empty(B, dtype=torch.int32, device=dev)
