@@ -265,6 +265,12 @@ int ks_tran(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt,
             int32_t capacity, double* out_time, double* out_wave, int32_t* out_npts,
             int32_t* out_status, int32_t* out_steps, int32_t* out_iters, void* stream);
 
+/* Same, on device buffers, asynchronous on `stream` (NULL: the batch's own
+ * stream); any output pointer may be NULL. */
+int ks_tran_async(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
+                  double* out_time_dev, double* out_wave_dev, int32_t* out_npts_dev,
+                  int32_t* out_status_dev, int32_t* out_steps_dev, int32_t* out_iters_dev, void* stream);
+
 /* Number of points a fixed-step transient records. */
 int ks_tran_points(const ks_tran_spec* spec, int32_t* n_points);
 

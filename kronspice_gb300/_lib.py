@@ -34,7 +34,7 @@ class KsTranSpec(ctypes.Structure):
 # every symbol include/kronspice_gpu.h declares
 EXPORTS = ["ks_version", "ks_last_error", "ks_validate", "ks_unknowns", "ks_plan_create", "ks_plan_destroy",
            "ks_plan_info", "ks_batch_create", "ks_batch_set_values", "ks_batch_destroy", "ks_op", "ks_op_async",
-           "ks_tran", "ks_tran_points"]
+           "ks_tran", "ks_tran_async", "ks_tran_points"]
 
 _lib = None
 
@@ -70,8 +70,8 @@ def load(build_if_missing=False):
     L.ks_batch_destroy.restype = None
     L.ks_op.argtypes = [P, P, P, P, P, P, P]
     L.ks_op_async.argtypes = [P, P, P, P, P, P, P]
-    if hasattr(L, "ks_tran"):
-        L.ks_tran.argtypes = [P, P, P, ctypes.c_int32, P, P, P, P, P, P, P]
+    L.ks_tran.argtypes = [P, P, P, ctypes.c_int32, P, P, P, P, P, P, P]
+    L.ks_tran_async.argtypes = [P, P, P, ctypes.c_int32, P, P, P, P, P, P, P]
     L.ks_tran_points.argtypes = [P, P]
     _lib = L
     return L

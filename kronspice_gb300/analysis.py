@@ -151,6 +151,31 @@ class Batch:
                                  x.ctypes.data, st.ctypes.data, it.ctypes.data, stream), "ks_op")
         return x, st, it
 
+    def tran(self, spec, opt=None, capacity=0, record=True, stream=None):
+        """analysis.Tran for every circuit (ks_tran).  Fixed-step specs return
+        (wave [n_points][n_circ][n], None, npts, status, steps, iters); adaptive specs
+        return (wave [n_circ][capacity][n], time [n_circ][capacity], npts, ...)."""
+        L = _lib.load()
+        o = (opt or Options()).c()
+        sp = spec.c() if hasattr(spec, "c") else spec
+        B, n = self.n_circ, self.plan.n
+        if sp.fixed_step:
+            npts = int(round(sp.stop / sp.step)) + 1
+            wave = np.zeros((npts, B, n)) if record else None
+            tim = None
+        else:
+            wave = np.zeros((B, capacity, n)) if record else None
+            tim = np.zeros((B, capacity)) if record else None
+        np_ = np.zeros(B, dtype=np.int32)
+        st = np.zeros(B, dtype=np.int32)
+        steps = np.zeros(B, dtype=np.int32)
+        it = np.zeros(B, dtype=np.int32)
+        rc = L.ks_tran(self.handle, ctypes.byref(sp), ctypes.byref(o), int(capacity),
+                       None if tim is None else tim.ctypes.data, None if wave is None else wave.ctypes.data,
+                       np_.ctypes.data, st.ctypes.data, steps.ctypes.data, it.ctypes.data, stream)
+        _check(rc, "ks_tran")
+        return wave, tim, np_, st, steps, it
+
     def op_async(self, opt, x0_dev, x_dev, status_dev, iters_dev, stream):
         """ks_op_async on device pointers (ints) on a CUDA stream handle."""
         o = (opt or Options()).c()
@@ -174,6 +199,27 @@ def validate(circuit, transient=False):
     if "no path to ground" in msg:
         return ErrFloatingNode(msg)
     return ErrValidation(msg)
+
+
+@dataclass
+class TranSpec:
+    """analysis.TranSpec + TranOptions (analysis/tran.go:26-40) plus the fixed-step batch mode."""
+    step: float
+    stop: float
+    start: float = 0.0
+    max_step: float = 0.0
+    uic: bool = False
+    method: str = "trap"
+    fixed_step: bool = False
+    max_steps: int = 0
+    chgtol: float = 0.0
+    trtol: float = 0.0
+    min_step: float = 0.0
+
+    def c(self):
+        return _lib.KsTranSpec(self.step, self.stop, self.start, self.max_step, int(self.uic),
+                               1 if self.method == "be" else 2, int(self.fixed_step), self.max_steps, self.chgtol,
+                               self.trtol, self.min_step)
 
 
 @dataclass

@@ -8,6 +8,8 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
+#include <algorithm>
 #include "ks_internal.h"
 
 using ksh::set_error;
@@ -221,5 +223,68 @@ extern "C" int ks_op(ks_batch* b, const ks_options* opt, const double* x0, doubl
   if (out_x) std::memcpy(out_x, hp_bytes, xbytes);
   if (out_status) std::memcpy(out_status, hp_bytes + xbytes, sizeof(int32_t) * B);
   if (out_iters) std::memcpy(out_iters, hp_bytes + xbytes + sizeof(int32_t) * B, sizeof(int32_t) * B);
+  return KS_OK;
+}
+
+// TranSpec check of analysis.Tran (analysis/tran.go:71-74): ErrBadTranSpec.
+static bool tran_spec_ok(const ks_tran_spec* sp) {
+  if (!sp) return false;
+  double sum = sp->step + sp->stop + sp->start + sp->max_step;
+  return sp->step > 0 && sp->stop > 0 && sp->start >= 0 && sp->start < sp->stop && sp->max_step >= 0 &&
+         !std::isnan(sum) && !std::isinf(sp->stop);
+}
+
+extern "C" int ks_tran_async(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
+                             double* out_time_dev, double* out_wave_dev, int32_t* out_npts_dev,
+                             int32_t* out_status_dev, int32_t* out_steps_dev, int32_t* out_iters_dev, void* stream) {
+  if (!b) return KS_EINVAL;
+  if (!tran_spec_ok(spec)) { set_error("analysis: invalid transient specification"); return KS_EINVAL; }
+  if (!spec->fixed_step && capacity <= 0 && (out_time_dev || out_wave_dev)) { set_error("ks_tran: capacity"); return KS_EINVAL; }
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+  KOpts o = make_opts(opt);
+  int rc = batch_setup(b, spec->step, spec->stop, st);
+  if (rc) return rc;
+  rc = ks_launch_tran(b->dev, o, *spec, capacity, out_time_dev, out_wave_dev, out_npts_dev, out_status_dev,
+                      out_steps_dev, out_iters_dev, opt ? opt->deadline_s : 0.0, st);
+  if (rc == -2) { set_error("ks_tran: system too large for the dense kernels"); return KS_EUNSUPPORTED; }
+  if (rc) { set_error(std::string("tran kernel launch failed: ") + cudaGetErrorString(cudaGetLastError())); return KS_ECUDA; }
+  return KS_OK;
+}
+
+extern "C" int ks_tran(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
+                       double* out_time, double* out_wave, int32_t* out_npts, int32_t* out_status, int32_t* out_steps,
+                       int32_t* out_iters, void* stream) {
+  if (!b) return KS_EINVAL;
+  if (!tran_spec_ok(spec)) { set_error("analysis: invalid transient specification"); return KS_EINVAL; }
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+  size_t B = b->B, n = b->plan->hp.n;
+  size_t npts = spec->fixed_step ? (size_t)llround(spec->stop / spec->step) + 1 : 0;
+  size_t wave_elems = spec->fixed_step ? npts * B * n : (size_t)std::max(capacity, 0) * B * n;
+  size_t time_elems = spec->fixed_step ? 0 : (size_t)std::max(capacity, 0) * B;
+  double* d_wave = nullptr;
+  double* d_time = nullptr;
+  int32_t* d_ints = nullptr;
+  auto cleanup = [&]() { cudaFree(d_wave); cudaFree(d_time); cudaFree(d_ints); };
+  if (out_wave && wave_elems && cudaMalloc(&d_wave, wave_elems * sizeof(double)) != cudaSuccess) {
+    cleanup(); set_error("ks_tran: device allocation for the waveforms failed"); return KS_ENOMEM;
+  }
+  if (out_time && time_elems && cudaMalloc(&d_time, time_elems * sizeof(double)) != cudaSuccess) {
+    cleanup(); set_error("ks_tran: device allocation failed"); return KS_ENOMEM;
+  }
+  if (cudaMalloc(&d_ints, 4 * B * sizeof(int32_t)) != cudaSuccess) { cleanup(); set_error("ks_tran: allocation failed"); return KS_ENOMEM; }
+  int rc = ks_tran_async(b, spec, opt, capacity, d_time, d_wave, d_ints, d_ints + B, d_ints + 2 * B, d_ints + 3 * B, st);
+  if (rc) { cleanup(); return rc; }
+  cudaError_t e = cudaSuccess;
+  if (out_wave && d_wave) e = cudaMemcpyAsync(out_wave, d_wave, wave_elems * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && out_time && d_time) e = cudaMemcpyAsync(out_time, d_time, time_elems * sizeof(double), cudaMemcpyDeviceToHost, st);
+  std::vector<int32_t> ints(4 * B);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ints.data(), d_ints, 4 * B * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cleanup();
+  if (e != cudaSuccess) { set_error(std::string("ks_tran: ") + cudaGetErrorString(e)); return KS_ECUDA; }
+  if (out_npts) std::memcpy(out_npts, ints.data(), B * sizeof(int32_t));
+  if (out_status) std::memcpy(out_status, ints.data() + B, B * sizeof(int32_t));
+  if (out_steps) std::memcpy(out_steps, ints.data() + 2 * B, B * sizeof(int32_t));
+  if (out_iters) std::memcpy(out_iters, ints.data() + 3 * B, B * sizeof(int32_t));
   return KS_OK;
 }

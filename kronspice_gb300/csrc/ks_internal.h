@@ -38,5 +38,8 @@ struct KsDeviceBatch {
 
 int ks_launch_transpose(const double* src_rows, double* dst_cols, int64_t rows, int64_t cols, void* stream);
 int ks_launch_setup(const KsDeviceBatch& b, double step, double stop, void* stream);
+int ks_launch_tran(const KsDeviceBatch& b, const KOpts& o, const ks_tran_spec& spec, int cap, double* out_time,
+                   double* out_wave, int32_t* out_npts, int32_t* out_status, int32_t* out_steps, int32_t* out_iters,
+                   double deadline_s, void* stream);
 int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, double* out_x, int32_t* out_status,
                  int32_t* out_iters, double deadline_s, void* stream);

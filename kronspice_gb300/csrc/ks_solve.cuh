@@ -148,12 +148,35 @@ __device__ inline int lu_solve_fp64(const ThreadSys<T>& s, const double* b, doub
   return SOLVE_OK;
 }
 
-// Mixed precision: x = xold + LU32^-1 (rhs - A*xold), the FP64 Newton residual
-// with an FP32 factorization.  Returns SOLVE_FP32_FAIL when a pivot is below
-// the FP32 threshold (the caller then solves in FP64).
+// FP32 forward/back substitution with the factor in L32: y (FP64 in/out, in place).
+template <int T>
+__device__ inline void lu32_apply(const ThreadSys<T>& s, double* y) {
+  const int n = s.n;
+  for (int k = 0; k < n; k++) {
+    int p = s.piv[k * T];
+    if (p != k) { double t = y[k * T]; y[k * T] = y[p * T]; y[p * T] = t; }
+  }
+  for (int i = 0; i < n; i++) {
+    float acc = (float)y[i * T];
+    for (int j = 0; j < i; j++) acc = fmaf(-s.l(i, j), (float)y[j * T], acc);
+    y[i * T] = acc;
+  }
+  for (int i = n - 1; i >= 0; i--) {
+    float acc = (float)y[i * T];
+    for (int j = i + 1; j < n; j++) acc = fmaf(-s.l(i, j), (float)y[j * T], acc);
+    y[i * T] = acc / s.l(i, i);
+  }
+}
+
+// Mixed precision: FP32 LU with partial pivoting of the FP64 matrix, then
+// x = xold + LU32^-1 (rhs - A*xold) and iterative refinement with the FP64
+// residual rhs - A*x until the correction is at FP64 round-off (at most 6
+// passes).  A and rhs are left intact.  Returns SOLVE_FP32_FAIL when a pivot is
+// below the FP32 threshold or refinement does not contract (the caller then
+// solves in FP64).
 template <int T>
 __device__ inline int lu_solve_mixed(const ThreadSys<T>& s) {
-  int n = s.n;
+  const int n = s.n;
   double scale = 0;
   for (int i = 0; i < n * n; i++) {
     double v = s.A[i * T];
@@ -161,12 +184,6 @@ __device__ inline int lu_solve_mixed(const ThreadSys<T>& s) {
     scale = fmax(scale, fabs(v));
   }
   if (scale == 0) return SOLVE_SINGULAR;
-  // FP64 residual r = rhs - A*xold, kept in rhs.
-  for (int i = 0; i < n; i++) {
-    double r = s.rhs[i * T];
-    for (int j = 0; j < n; j++) r -= s.a(i, j) * s.xold[j * T];
-    s.rhs[i * T] = r;
-  }
   for (int j = 0; j < n; j++) {
     double m = 0;
     for (int i = 0; i < n; i++) m = fmax(m, fabs(s.a(i, j)));
@@ -192,26 +209,30 @@ __device__ inline int lu_solve_mixed(const ThreadSys<T>& s) {
       for (int j = k + 1; j < n; j++) s.l(i, j) = fmaf(-f, s.l(k, j), s.l(i, j));
     }
   }
-  // dx in x (as FP32 values), then x = xold + dx
-  for (int i = 0; i < n; i++) s.x[i * T] = s.rhs[i * T];
-  for (int k = 0; k < n; k++) {
-    int p = s.piv[k * T];
-    if (p != k) { double t = s.x[k * T]; s.x[k * T] = s.x[p * T]; s.x[p * T] = t; }
-  }
-  for (int i = 0; i < n; i++) {
-    float acc = (float)s.x[i * T];
-    for (int j = 0; j < i; j++) acc = fmaf(-s.l(i, j), (float)s.x[j * T], acc);
-    s.x[i * T] = acc;
-  }
-  for (int i = n - 1; i >= 0; i--) {
-    float acc = (float)s.x[i * T];
-    for (int j = i + 1; j < n; j++) acc = fmaf(-s.l(i, j), (float)s.x[j * T], acc);
-    s.x[i * T] = acc / s.l(i, i);
-  }
-  for (int i = 0; i < n; i++) {
-    double v = s.xold[i * T] + s.x[i * T];
-    if (!isfinite(v)) return SOLVE_NONFINITE;
-    s.x[i * T] = v;
+  // x starts at the linearization point; each pass adds LU32^-1 of the FP64 residual.
+  for (int i = 0; i < n; i++) s.x[i * T] = s.xold[i * T];
+  double prev = CUDART_INF;
+  for (int pass = 0; pass < 6; pass++) {
+    for (int i = 0; i < n; i++) {  // residual in col (the column maxima are no longer needed)
+      double r = s.rhs[i * T];
+      for (int j = 0; j < n; j++) r -= s.a(i, j) * s.x[j * T];
+      s.col[i * T] = r;
+    }
+    lu32_apply<T>(s, s.col);
+    double dmax = 0, xmax = 0;
+    for (int i = 0; i < n; i++) {
+      double v = s.x[i * T] + s.col[i * T];
+      if (!isfinite(v)) return SOLVE_NONFINITE;
+      s.x[i * T] = v;
+      dmax = fmax(dmax, fabs(s.col[i * T]));
+      xmax = fmax(xmax, fabs(v));
+    }
+    if (dmax <= 4e-16 * xmax || dmax == 0) break;
+    if (pass > 0 && dmax > 0.5 * prev) {  // refinement stopped contracting
+      if (dmax <= 1e-11 * xmax) break;      // at the round-off floor of this system
+      return SOLVE_FP32_FAIL;
+    }
+    prev = dmax;
   }
   return SOLVE_OK;
 }
