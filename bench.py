@@ -334,6 +334,7 @@ def main():
                    "precision": "fp32 LU + fp64 residual",
                    "start": "learned (MLP)" if learned is not None else "InitJct"},
         "chosen_vs_plain": value / plain_value if plain_value else None,
+        "learned_start": None if learned is None else learned.info,
         "max_node_voltage_err_vs_oracle": max_err,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(vals.nbytes),
                 "d2h_bytes_per_step": int(x_host.nbytes + s_host.nbytes + i_host.nbytes)},

@@ -274,6 +274,37 @@ int ks_tran_async(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, 
 /* Number of points a fixed-step transient records. */
 int ks_tran_points(const ks_tran_spec* spec, int32_t* n_points);
 
+/* ---- learned Newton start ------------------------------------------------
+ * A BF16 MLP in -> H -> H -> H -> out (ReLU) on the GPU's tensor cores that
+ * predicts each circuit's Newton starting point from its parameter vector.
+ * It plays the role of Options.NodeSet (analysis/op.go:39-43, applied by
+ * analysis/newton.go:221-243): plain Newton corrects the prediction, and the
+ * gmin/source-stepping chain takes over when Newton from it fails. */
+typedef struct ks_mlp ks_mlp;
+
+int ks_mlp_create(int32_t in_dim, int32_t hidden, int32_t out_dim, uint64_t seed, ks_mlp** out);
+void ks_mlp_destroy(ks_mlp* m);
+int ks_mlp_num_params(const ks_mlp* m, int64_t* n);
+/* FP32 parameters, layout per layer l: W_l [out][in] row-major, then b_l [out]. */
+int ks_mlp_get_params(const ks_mlp* m, float* host);
+int ks_mlp_set_params(ks_mlp* m, const float* host);
+/* Features: value-vector columns `cols[in_dim]`, log-transformed where bit j of
+ * logmask is set, standardized by fmean/fstd; targets: unknowns 0..out_dim-1
+ * divided by value column scale_col (-1: not divided), standardized by
+ * tmean/tstd. */
+int ks_mlp_set_io(ks_mlp* m, const int32_t* cols, uint64_t logmask, const float* fmean, const float* fstd,
+                  const float* tmean, const float* tstd, int32_t scale_col);
+/* One forward and backward pass on host data (standardized X [rows][in],
+ * T [rows][out]); FP32 gradients in the parameter layout and the MSE loss. */
+int ks_mlp_grad(ks_mlp* m, const float* X, const float* T, int32_t rows, float* grads, float* loss);
+/* Adam training on the circuits idx_dev[0..n_train) of a batch, with solutions
+ * x_dev [n_circ][n] (device memory), `epochs` passes of minibatches of `mb`
+ * rows (a multiple of 64). */
+int ks_mlp_train(ks_mlp* m, ks_batch* b, const double* x_dev, const int32_t* idx_dev, int32_t n_train,
+                 int32_t epochs, int32_t mb, float lr, float* last_loss, void* stream);
+/* Predicted starting points x0_dev [n_circ][n] (device memory) for ks_op_async. */
+int ks_mlp_predict(ks_mlp* m, ks_batch* b, double* x0_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

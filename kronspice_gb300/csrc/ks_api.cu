@@ -144,7 +144,8 @@ extern "C" int ks_batch_create(ks_plan* plan, int32_t n_circ, const double* valu
       cudaMalloc(&b->d_x, sizeof(double) * hp.n * B) != cudaSuccess ||
       cudaMalloc(&b->d_x0, sizeof(double) * hp.n * B) != cudaSuccess ||
       cudaMalloc(&b->d_status, sizeof(int32_t) * B) != cudaSuccess ||
-      cudaMalloc(&b->d_iters, sizeof(int32_t) * B) != cudaSuccess) {
+      cudaMalloc(&b->d_iters, sizeof(int32_t) * B) != cudaSuccess ||
+      cudaMalloc(&b->dev.queue, 64) != cudaSuccess) {
     set_error("ks_batch_create: device allocation failed");
     return fail(KS_ENOMEM);
   }
@@ -179,6 +180,7 @@ extern "C" int ks_batch_set_values(ks_batch* b, const double* values, int values
 extern "C" void ks_batch_destroy(ks_batch* b) {
   if (!b) return;
   cudaFree(b->dev.values); cudaFree(b->dev.derived); cudaFree(b->dev.state); cudaFree(b->dev.work);
+  cudaFree(b->dev.queue);
   cudaFree(b->d_rows); cudaFree(b->d_x); cudaFree(b->d_x0); cudaFree(b->d_status); cudaFree(b->d_iters);
   if (b->h_pin) cudaFreeHost(b->h_pin);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -286,5 +288,14 @@ extern "C" int ks_tran(ks_batch* b, const ks_tran_spec* spec, const ks_options* 
   if (out_status) std::memcpy(out_status, ints.data() + B, B * sizeof(int32_t));
   if (out_steps) std::memcpy(out_steps, ints.data() + 2 * B, B * sizeof(int32_t));
   if (out_iters) std::memcpy(out_iters, ints.data() + 3 * B, B * sizeof(int32_t));
+  return KS_OK;
+}
+
+// The batch's SoA values [n_values][B], circuit count and unknown count (for the
+// learned-start kernels, which read their features from the values in place).
+int ks_batch_values_view(ks_batch* b, const double** vals, int64_t* B, int* n) {
+  *vals = b->dev.values;
+  *B = b->B;
+  *n = b->plan->hp.n;
   return KS_OK;
 }

@@ -33,7 +33,8 @@ struct KsDeviceBatch {
   double* values;      // [n_values][B]
   double* derived;     // [n_derived][B]
   double* state;       // [n_state][B]
-  double* work;        // [3*n][B]: x, save, ptPrev
+  double* work;        // [3*n][B]: save, ptPrev, xacc
+  unsigned long long* queue;  // next-circuit counter of the persistent kernels
 };
 
 int ks_launch_transpose(const double* src_rows, double* dst_cols, int64_t rows, int64_t cols, void* stream);

@@ -110,36 +110,65 @@ int ks_launch_setup(const KsDeviceBatch& b, double step, double stop, void* stre
 
 // ---------------------------------------------------------------- operating point
 // analysis.OP for every circuit: dcSolve (Newton, then the fallback chain) at
-// ModeOP, then Accept.  One thread per circuit.
+// ModeOP, then Accept.  Persistent: each thread takes the next circuit from the
+// queue counter as soon as its circuit is done, so a warp's lanes stay busy
+// while circuits need different numbers of Newton iterations.
 template <int T>
 __global__ void __launch_bounds__(T) k_op(KPlan plan, KOpts o, const double* __restrict__ values,
                                           const double* __restrict__ derived, double* state, double* work,
                                           int64_t B, const double* __restrict__ x0, double* out_x,
-                                          int32_t* out_status, int32_t* out_iters, uint64_t deadline_ns) {
+                                          int32_t* out_status, int32_t* out_iters, uint64_t deadline_ns,
+                                          unsigned long long* queue) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int64_t c = (int64_t)blockIdx.x * T + threadIdx.x;
   Thr<T> t;
-  thr_init<T>(t, plan, o, smem, values, derived, state, work, B, c < B ? c : 0);
+  thr_init<T>(t, plan, o, smem, values, derived, state, work, B, 0);
   __syncthreads();
-  if (c >= B) return;
   const uint64_t t0 = deadline_ns ? globaltimer_ns() : 0;
   const int maxTotal = o.max_iter_total > 0 ? o.max_iter_total : 3300 * o.itl1 + 16;
-  init_state(t.el, t.ne, t.n_state, t.D, t.Sb);
-  OpState st;
-  dc_start<T>(t, st, x0, c, ModeOP);
+  const int n = t.n;
   LoadParams lp;
   lp.mode = ModeOP; lp.method = BE; lp.time = 0; lp.h = 0;
-  while (st.phase != PH_DONE) {
-    if (deadline_ns && globaltimer_ns() - t0 > deadline_ns) { st.status = KS_STATUS_INTERRUPTED; break; }
-    if (st.total >= maxTotal) { st.status = KS_STATUS_NO_CONVERGENCE; break; }
-    int res = newton_step<T>(t, st, lp);
-    if (res >= 0) dc_advance<T>(t, st, res);
+  OpState st;
+  int64_t c = (int64_t)atomicAdd(queue, 1ull);
+  if (c < B) {
+    thr_bind<T>(t, values, derived, state, work, B, c);
+    init_state(t.el, t.ne, t.n_state, t.D, t.Sb);
+    dc_start<T>(t, st, x0, c, ModeOP);
   }
-  if (st.status == KS_STATUS_OK) accept_all<T>(t.el, t.ne, t.V, t.D, t.Sb, t.s.x, 0.0, ModeOP, o.gmin, false);
-  const int n = t.n;
-  if (out_x) for (int i = 0; i < n; i++) out_x[c * n + i] = t.s.x[i * T];
-  if (out_status) out_status[c] = st.status;
-  if (out_iters) out_iters[c] = st.total;
+  while (c < B) {
+    bool done = false;
+    if (deadline_ns && globaltimer_ns() - t0 > deadline_ns) { st.status = KS_STATUS_INTERRUPTED; done = true; }
+    else if (st.total >= maxTotal) { st.status = KS_STATUS_NO_CONVERGENCE; done = true; }
+    else {
+      int res = newton_step<T>(t, st, lp);
+      if (res >= 0) dc_advance<T>(t, st, res);
+      done = st.phase == PH_DONE;
+    }
+    if (!done) continue;
+    if (st.status == KS_STATUS_OK) accept_all<T>(t.el, t.ne, t.V, t.D, t.Sb, t.s.x, 0.0, ModeOP, o.gmin, false);
+    if (out_x) for (int i = 0; i < n; i++) out_x[c * n + i] = t.s.x[i * T];
+    if (out_status) out_status[c] = st.status;
+    if (out_iters) out_iters[c] = st.total;
+    c = (int64_t)atomicAdd(queue, 1ull);
+    if (c < B) {
+      thr_bind<T>(t, values, derived, state, work, B, c);
+      init_state(t.el, t.ne, t.n_state, t.D, t.Sb);
+      dc_start<T>(t, st, x0, c, ModeOP);
+    }
+  }
+}
+
+// Blocks of T threads that keep every SM full (persistent grid), capped by the work.
+template <typename K>
+static unsigned persistent_grid(K kernel, int T, size_t smem, int64_t B) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, T, smem);
+  if (per < 1) per = 1;
+  int64_t need = (B + T - 1) / T;
+  int64_t g = (int64_t)sms * per;
+  return (unsigned)(need < g ? need : g);
 }
 
 int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, double* out_x, int32_t* out_status,
@@ -154,16 +183,18 @@ int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, doubl
   size_t sm = thr_smem(n, ne, 64);
   if (sm > (size_t)maxSmem) { T = 32; sm = thr_smem(n, ne, 32); }
   if (sm > (size_t)maxSmem) return -2;
-  unsigned grid = (unsigned)((b.B + T - 1) / T);
   cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemsetAsync(b.queue, 0, sizeof(unsigned long long), st) != cudaSuccess) return -1;
   if (T == 64) {
     cudaFuncSetAttribute(k_op<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    unsigned grid = persistent_grid(k_op<64>, 64, sm, b.B);
     k_op<64><<<grid, 64, sm, st>>>(b.plan, o, b.values, b.derived, b.state, b.work, b.B, x0, out_x, out_status,
-                                   out_iters, dl);
+                                   out_iters, dl, b.queue);
   } else {
     cudaFuncSetAttribute(k_op<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    unsigned grid = persistent_grid(k_op<32>, 32, sm, b.B);
     k_op<32><<<grid, 32, sm, st>>>(b.plan, o, b.values, b.derived, b.state, b.work, b.B, x0, out_x, out_status,
-                                   out_iters, dl);
+                                   out_iters, dl, b.queue);
   }
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

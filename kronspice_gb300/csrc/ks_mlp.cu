@@ -1,0 +1,527 @@
+// ks_mlp.cu — the learned Newton start: a BF16 MLP trained and run on the GB300's
+// tensor cores by hand-written kernels.
+//
+// Network: in -> H -> H -> H -> out, ReLU on the hidden layers, linear output,
+// on standardized features and targets.  Weights are FP32 masters (Adam) with
+// BF16 copies W[out][in] and W^T[in][out] for the GEMMs; activations are BF16,
+// accumulation FP32.  One GEMM kernel serves every product through layout
+// flags: ldmatrix (.trans where an operand is stored the other way round)
+// feeds mma.sync m16n8k16 BF16 with FP32 accumulators; the epilogue fuses bias,
+// ReLU, the ReLU-backward mask, or split-K atomic accumulation of weight
+// gradients.  Dimensions are padded: batch to 64, feature and output widths to
+// 64, so every tile is full and every 16-byte access aligned.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "ks_internal.h"
+
+using ksh::set_error;
+
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
+
+enum Epi { EPI_RELU_BF16 = 0, EPI_LINEAR_F32 = 1, EPI_MASK_BF16 = 2, EPI_ATOMIC_F32 = 3 };
+
+__device__ __forceinline__ void ldsm_x4(uint32_t* r, const void* p) {
+  uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t* r, const void* p) {
+  uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+}
+__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, uint32_t b0, uint32_t b1) {
+  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+               "{%0,%1,%2,%3};\n"
+               : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// C[M][N] = A * B over K.
+//   A_T = false: A stored [M][K] (lda = row stride);  A_T = true: A stored [K][M]
+//   B_T = false: B stored [N][K] (the weight layout); B_T = true: B stored [K][N]
+// Grid: (N/BN, M/BM, splits); blockIdx.z takes K range [z*kchunk, (z+1)*kchunk).
+template <bool A_T, bool B_T, int EPI>
+__global__ void __launch_bounds__(128) k_gemm(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__ Bm,
+                                              void* C, const float* __restrict__ bias,
+                                              const __nv_bfloat16* __restrict__ mask, int M, int N, int K, int lda,
+                                              int ldb, int ldc, int kchunk) {
+  constexpr int AR = A_T ? BK : BM, AC = A_T ? BM : BK;  // smem tile rows x cols as stored
+  constexpr int BR = B_T ? BK : BN, BC = B_T ? BN : BK;
+  __shared__ __align__(16) __nv_bfloat16 As[AR][AC + PAD];
+  __shared__ __align__(16) __nv_bfloat16 Bs[BR][BC + PAD];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int kbeg = blockIdx.z * kchunk, kend = min(K, kbeg + kchunk);
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) acc[i][j][e] = 0.f;
+
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    // global -> shared, 16-byte vectors (AR*AC/8 = 256 vectors per tile)
+#pragma unroll
+    for (int v = tid; v < AR * AC / 8; v += 128) {
+      int r = v / (AC / 8), cc = (v % (AC / 8)) * 8;
+      const __nv_bfloat16* src = A_T ? A + (size_t)(k0 + r) * lda + m0 + cc : A + (size_t)(m0 + r) * lda + k0 + cc;
+      *reinterpret_cast<uint4*>(&As[r][cc]) = *reinterpret_cast<const uint4*>(src);
+    }
+#pragma unroll
+    for (int v = tid; v < BR * BC / 8; v += 128) {
+      int r = v / (BC / 8), cc = (v % (BC / 8)) * 8;
+      const __nv_bfloat16* src = B_T ? Bm + (size_t)(k0 + r) * ldb + n0 + cc : Bm + (size_t)(n0 + r) * ldb + k0 + cc;
+      *reinterpret_cast<uint4*>(&Bs[r][cc]) = *reinterpret_cast<const uint4*>(src);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; kk += 16) {
+      uint32_t af[2][4], bf[2][4];
+      const int j = lane >> 3, r = lane & 7;
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        int mb = wm + i * 16;
+        if (!A_T) ldsm_x4(af[i], &As[mb + (lane & 15)][kk + (lane >> 4) * 8]);
+        else ldsm_x4_t(af[i], &As[kk + (j >> 1) * 8 + r][mb + (j & 1) * 8]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; i++) {  // two n16 groups -> b fragments of 4 n8 blocks
+        int nb = wn + i * 16;
+        if (!B_T) ldsm_x4(bf[i], &Bs[nb + (j >> 1) * 8 + r][kk + (j & 1) * 8]);
+        else ldsm_x4_t(bf[i], &Bs[kk + (j & 1) * 8 + r][nb + (j >> 1) * 8]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int jn = 0; jn < 4; jn++) mma_bf16(acc[i][jn], af[i], bf[jn >> 1][(jn & 1) * 2], bf[jn >> 1][(jn & 1) * 2 + 1]);
+    }
+    __syncthreads();
+  }
+  const int g = lane >> 2, t4 = lane & 3;
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int jn = 0; jn < 4; jn++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        int row = m0 + wm + i * 16 + g + h * 8;
+        int col = n0 + wn + jn * 8 + t4 * 2;
+        float v0 = acc[i][jn][h * 2], v1 = acc[i][jn][h * 2 + 1];
+        if (row >= M || col >= N) continue;  // N even except for the atomic (unpadded) case below
+        if (EPI == EPI_RELU_BF16) {
+          v0 = fmaxf(v0 + bias[col], 0.f); v1 = fmaxf(v1 + bias[col + 1], 0.f);
+          *reinterpret_cast<__nv_bfloat162*>((__nv_bfloat16*)C + (size_t)row * ldc + col) = __floats2bfloat162_rn(v0, v1);
+        } else if (EPI == EPI_LINEAR_F32) {
+          float* o = (float*)C + (size_t)row * ldc + col;
+          o[0] = v0 + bias[col]; o[1] = v1 + bias[col + 1];
+        } else if (EPI == EPI_MASK_BF16) {  // dX of a ReLU layer: zero where the forward activation was 0
+          const __nv_bfloat16* mk = mask + (size_t)row * ldc + col;
+          if (!(__bfloat162float(mk[0]) > 0.f)) v0 = 0.f;
+          if (!(__bfloat162float(mk[1]) > 0.f)) v1 = 0.f;
+          *reinterpret_cast<__nv_bfloat162*>((__nv_bfloat16*)C + (size_t)row * ldc + col) = __floats2bfloat162_rn(v0, v1);
+        } else {
+          float* o = (float*)C + (size_t)row * ldc + col;
+          atomicAdd(o, v0);
+          if (col + 1 < N) atomicAdd(o + 1, v1);
+        }
+      }
+}
+
+inline int pad64(int x) { return (x + 63) / 64 * 64; }
+
+// Gather standardized features: X[r][j] = bf16((f(values[col_j][idx[r]]) - mean_j) / std_j),
+// f = log when logmask bit j is set; rows beyond rows_valid and columns beyond d are 0.
+__global__ void k_features(const double* __restrict__ vals_soa, int64_t B, const int32_t* __restrict__ idx,
+                           const int32_t* __restrict__ cols, uint64_t logmask, const float* __restrict__ mean,
+                           const float* __restrict__ stdv, int d, int dp, int rows_valid, __nv_bfloat16* X, int rows) {
+  int r = blockIdx.x * blockDim.y + threadIdx.y;
+  int j = threadIdx.x;
+  if (r >= rows) return;
+  for (int jj = j; jj < dp; jj += blockDim.x) {
+    float v = 0.f;
+    if (r < rows_valid && jj < d) {
+      int64_t c = idx ? idx[r] : r;
+      double x = vals_soa[(int64_t)cols[jj] * B + c];
+      if ((logmask >> jj) & 1) x = log(x);
+      v = (float)((x - mean[jj]) / stdv[jj]);
+    }
+    X[(size_t)r * dp + jj] = __float2bfloat16(v);
+  }
+}
+
+// Standardized targets T[r][j] (FP32) from solutions x [B][n] (node voltages).
+__global__ void k_targets(const double* __restrict__ x, int n, const int32_t* __restrict__ idx, const float* __restrict__ mean,
+                          const float* __restrict__ stdv, int dout, int dop, int rows_valid, float* T, int rows,
+                          const double* __restrict__ vals_soa, int64_t B, int scale_col) {
+  int r = blockIdx.x * blockDim.y + threadIdx.y;
+  if (r >= rows) return;
+  double sc = 1.0;
+  if (scale_col >= 0 && r < rows_valid) sc = vals_soa[(int64_t)scale_col * B + idx[r]];
+  for (int j = threadIdx.x; j < dop; j += blockDim.x) {
+    float v = 0.f;
+    if (r < rows_valid && j < dout) v = (float)((x[(int64_t)idx[r] * n + j] / sc - mean[j]) / stdv[j]);
+    T[(size_t)r * dop + j] = v;
+  }
+}
+
+// MSE gradient dY = 2 (Y - T) / rows_valid on the valid block, bf16; loss partials.
+__global__ void k_loss_grad(const float* __restrict__ Y, const float* __restrict__ T, int dout, int dop, int rows_valid,
+                            __nv_bfloat16* dY, int rows, float* loss) {
+  int r = blockIdx.x * blockDim.y + threadIdx.y;
+  if (r >= rows) return;
+  float l = 0.f;
+  for (int j = threadIdx.x; j < dop; j += blockDim.x) {
+    float g = 0.f;
+    if (r < rows_valid && j < dout) {
+      float e = Y[(size_t)r * dop + j] - T[(size_t)r * dop + j];
+      l += e * e;
+      g = 2.f * e / rows_valid;
+    }
+    dY[(size_t)r * dop + j] = __float2bfloat16(g);
+  }
+  if (loss) atomicAdd(loss, l / (rows_valid * (float)dout));
+}
+
+// Column sums of dY (bias gradients): db[j] += sum_r dY[r][j].
+__global__ void k_colsum(const __nv_bfloat16* __restrict__ dY, int rows, int cols, int ld, float* db) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= cols) return;
+  float s = 0.f;
+  for (int r = blockIdx.y; r < rows; r += gridDim.y) s += __bfloat162float(dY[(size_t)r * ld + j]);
+  atomicAdd(&db[j], s);
+}
+
+// Adam step on FP32 masters, then BF16 copies W[o][i] (ld ip) and W^T[i][o] (ld op).
+__global__ void k_adam(float* w, const float* __restrict__ g, float* m, float* v, int nparam, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nparam) return;
+  float gi = g[i];
+  float mi = b1 * m[i] + (1 - b1) * gi, vi = b2 * v[i] + (1 - b2) * gi * gi;
+  m[i] = mi; v[i] = vi;
+  w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+__global__ void k_quantize(const float* __restrict__ w, int out, int in, __nv_bfloat16* W, int ldw, __nv_bfloat16* WT,
+                           int ldt) {
+  int o = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= out || i >= in) return;
+  __nv_bfloat16 q = __float2bfloat16(w[(size_t)o * in + i]);
+  W[(size_t)o * ldw + i] = q;
+  WT[(size_t)i * ldt + o] = q;
+}
+
+// Decode standardized outputs into Newton starting points x0[c][0..dout) (doubles).
+__global__ void k_decode(const float* __restrict__ Y, int dop, int dout, const float* __restrict__ mean,
+                         const float* __restrict__ stdv, double* x0, int n, int rows, const double* __restrict__ vals_soa,
+                         int64_t B, int scale_col) {
+  int r = blockIdx.x * blockDim.y + threadIdx.y;
+  if (r >= rows) return;
+  double sc = scale_col >= 0 ? vals_soa[(int64_t)scale_col * B + r] : 1.0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x)
+    x0[(size_t)r * n + j] = j < dout ? ((double)Y[(size_t)r * dop + j] * stdv[j] + mean[j]) * sc : 0.0;
+}
+
+}  // namespace
+
+struct ks_mlp {
+  int din, h, dout, dip, dop;  // dims and padded dims
+  int nlayers = 4;
+  int in_[4], out_[4], ldi[4], ldo[4];   // per layer fan-in/out (unpadded) and padded
+  std::vector<size_t> woff, boff;        // offsets in the flat parameter vector
+  size_t nparam = 0;
+  float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;  // FP32 masters, grads, Adam moments
+  __nv_bfloat16* Wq[4] = {};  // [out_pad][in_pad]
+  __nv_bfloat16* WTq[4] = {}; // [in_pad][out_pad]
+  float* bias_pad[4] = {};    // padded bias views (copies)
+  // normalization
+  float *fmean = nullptr, *fstd = nullptr, *tmean = nullptr, *tstd = nullptr;
+  int32_t* fcols = nullptr;
+  uint64_t logmask = 0;
+  int scale_col = -1;  // targets are unknowns divided by this value column (-1: none)
+  int adam_t = 0;
+  // activations for a batch of up to cap rows
+  int cap = 0;
+  __nv_bfloat16 *X = nullptr, *H[3] = {}, *dH[3] = {}, *dYb = nullptr;
+  float *Y = nullptr, *T = nullptr, *loss = nullptr;
+  int32_t* idx = nullptr;
+};
+
+static int mlp_alloc_batch(ks_mlp* p, int rows) {
+  int R = pad64(rows);
+  if (R <= p->cap) return KS_OK;
+  cudaFree(p->X); cudaFree(p->Y); cudaFree(p->T); cudaFree(p->dYb); cudaFree(p->idx);
+  for (int i = 0; i < 3; i++) { cudaFree(p->H[i]); cudaFree(p->dH[i]); }
+  bool ok = cudaMalloc(&p->X, (size_t)R * p->dip * 2) == cudaSuccess &&
+            cudaMalloc(&p->Y, (size_t)R * p->dop * 4) == cudaSuccess &&
+            cudaMalloc(&p->T, (size_t)R * p->dop * 4) == cudaSuccess &&
+            cudaMalloc(&p->dYb, (size_t)R * p->dop * 2) == cudaSuccess &&
+            cudaMalloc(&p->idx, (size_t)R * 4) == cudaSuccess;
+  for (int i = 0; i < 3 && ok; i++)
+    ok = cudaMalloc(&p->H[i], (size_t)R * p->h * 2) == cudaSuccess && cudaMalloc(&p->dH[i], (size_t)R * p->h * 2) == cudaSuccess;
+  if (!ok) { set_error("ks_mlp: device allocation failed"); p->cap = 0; return KS_ENOMEM; }
+  p->cap = R;
+  return KS_OK;
+}
+
+template <bool AT, bool BT, int EPI>
+static void gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, void* C, const float* bias, const __nv_bfloat16* mask,
+                 int M, int N, int K, int lda, int ldb, int ldc, int splits, cudaStream_t st) {
+  int kchunk = (K + splits - 1) / splits;
+  kchunk = (kchunk + BK - 1) / BK * BK;
+  splits = (K + kchunk - 1) / kchunk;
+  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, splits);  // M, N: logical bounds; tiles read padded storage
+  k_gemm<AT, BT, EPI><<<grid, 128, 0, st>>>(A, B, C, bias, mask, M, N, K, lda, ldb, ldc, kchunk);
+}
+
+static void sync_weights(ks_mlp* p, cudaStream_t st) {
+  for (int l = 0; l < p->nlayers; l++) {
+    dim3 grid((p->in_[l] + 127) / 128, p->out_[l]);
+    k_quantize<<<grid, 128, 0, st>>>(p->w + p->woff[l], p->out_[l], p->in_[l], p->Wq[l], p->ldi[l], p->WTq[l], p->ldo[l]);
+    cudaMemcpyAsync(p->bias_pad[l], p->w + p->boff[l], sizeof(float) * p->out_[l], cudaMemcpyDeviceToDevice, st);
+  }
+}
+
+// forward on p->X (rows R) -> p->H[*], p->Y
+static void mlp_forward(ks_mlp* p, int R, cudaStream_t st) {
+  gemm<false, false, EPI_RELU_BF16>(p->X, p->Wq[0], p->H[0], p->bias_pad[0], nullptr, R, p->ldo[0], p->ldi[0], p->dip,
+                                    p->ldi[0], p->h, 1, st);
+  gemm<false, false, EPI_RELU_BF16>(p->H[0], p->Wq[1], p->H[1], p->bias_pad[1], nullptr, R, p->h, p->h, p->h, p->h, p->h, 1, st);
+  gemm<false, false, EPI_RELU_BF16>(p->H[1], p->Wq[2], p->H[2], p->bias_pad[2], nullptr, R, p->h, p->h, p->h, p->h, p->h, 1, st);
+  gemm<false, false, EPI_LINEAR_F32>(p->H[2], p->Wq[3], p->Y, p->bias_pad[3], nullptr, R, p->dop, p->h, p->h, p->h, p->dop, 1, st);
+}
+
+// backward from p->dYb; accumulates into p->g (zeroed by the caller)
+static void mlp_backward(ks_mlp* p, int R, cudaStream_t st) {
+  int splits = R / 512 > 1 ? R / 512 : 1;
+  const __nv_bfloat16* acts[4] = {p->X, p->H[0], p->H[1], p->H[2]};
+  const __nv_bfloat16* dout = p->dYb;
+  int ldd = p->dop;
+  for (int l = 3; l >= 0; l--) {
+    // dW_l[o][i] += sum_r dout[r][o] * act[r][i]:  A = dout^T (stored [R][o]), B = act (stored [R][i])
+    gemm<true, true, EPI_ATOMIC_F32>(dout, acts[l], p->g + p->woff[l], nullptr, nullptr, p->out_[l], p->in_[l], R, ldd,
+                                     p->ldi[l], p->in_[l], splits, st);
+    dim3 cg((p->out_[l] + 127) / 128, 64);
+    k_colsum<<<cg, 128, 0, st>>>(dout, R, p->out_[l], ldd, p->g + p->boff[l]);
+    if (l == 0) break;
+    // dact[r][i] = sum_o dout[r][o] W[o][i], masked by the ReLU of layer l-1
+    gemm<false, false, EPI_MASK_BF16>(dout, p->WTq[l], p->dH[l - 1], nullptr, acts[l], R, p->ldi[l], p->ldo[l], ldd,
+                                      p->ldo[l], p->ldi[l], 1, st);
+    dout = p->dH[l - 1];
+    ldd = p->h;
+  }
+}
+
+extern "C" int ks_mlp_create(int32_t in_dim, int32_t hidden, int32_t out_dim, uint64_t seed, ks_mlp** out) {
+  if (in_dim <= 0 || in_dim > 64 || out_dim <= 0 || out_dim > 64 || hidden <= 0 || hidden % 64 || !out) {
+    set_error("ks_mlp_create: dimensions (in <= 64, out <= 64, hidden a multiple of 64)");
+    return KS_EINVAL;
+  }
+  ks_mlp* p = new ks_mlp();
+  p->din = in_dim; p->h = hidden; p->dout = out_dim; p->dip = pad64(in_dim); p->dop = pad64(out_dim);
+  int ins[4] = {in_dim, hidden, hidden, hidden}, outs[4] = {hidden, hidden, hidden, out_dim};
+  int insp[4] = {p->dip, hidden, hidden, hidden}, outsp[4] = {hidden, hidden, hidden, p->dop};
+  size_t off = 0;
+  for (int l = 0; l < 4; l++) {
+    p->in_[l] = ins[l]; p->out_[l] = outs[l]; p->ldi[l] = insp[l]; p->ldo[l] = outsp[l];
+    p->woff.push_back(off); off += (size_t)outs[l] * ins[l];
+    p->boff.push_back(off); off += outs[l];
+  }
+  p->nparam = off;
+  // He-uniform initial weights from a fixed-seed generator, zero biases
+  std::vector<float> w(off, 0.f);
+  uint64_t s = seed * 6364136223846793005ULL + 1442695040888963407ULL;
+  auto rnd = [&]() { s = s * 6364136223846793005ULL + 1442695040888963407ULL; return ((s >> 11) * (1.0 / 9007199254740992.0)) * 2 - 1; };
+  for (int l = 0; l < 4; l++) {
+    float a = sqrtf(6.f / ins[l]) * (l == 3 ? 0.5f : 1.f);
+    for (size_t i = 0; i < (size_t)outs[l] * ins[l]; i++) w[p->woff[l] + i] = (float)(a * rnd());
+  }
+  bool ok = cudaMalloc(&p->w, off * 4) == cudaSuccess && cudaMalloc(&p->g, off * 4) == cudaSuccess &&
+            cudaMalloc(&p->m, off * 4) == cudaSuccess && cudaMalloc(&p->v, off * 4) == cudaSuccess &&
+            cudaMalloc(&p->fmean, 64 * 4) == cudaSuccess && cudaMalloc(&p->fstd, 64 * 4) == cudaSuccess &&
+            cudaMalloc(&p->tmean, 64 * 4) == cudaSuccess && cudaMalloc(&p->tstd, 64 * 4) == cudaSuccess &&
+            cudaMalloc(&p->fcols, 64 * 4) == cudaSuccess;
+  for (int l = 0; l < 4 && ok; l++)
+    ok = cudaMalloc(&p->Wq[l], (size_t)p->ldo[l] * p->ldi[l] * 2) == cudaSuccess &&
+         cudaMalloc(&p->WTq[l], (size_t)p->ldo[l] * p->ldi[l] * 2) == cudaSuccess &&
+         cudaMalloc(&p->bias_pad[l], (size_t)p->ldo[l] * 4) == cudaSuccess;
+  if (!ok) { set_error("ks_mlp_create: device allocation failed"); return KS_ENOMEM; }
+  for (int l = 0; l < 4; l++) {
+    cudaMemset(p->Wq[l], 0, (size_t)p->ldo[l] * p->ldi[l] * 2);
+    cudaMemset(p->WTq[l], 0, (size_t)p->ldo[l] * p->ldi[l] * 2);
+    cudaMemset(p->bias_pad[l], 0, (size_t)p->ldo[l] * 4);
+  }
+  cudaMemcpy(p->w, w.data(), off * 4, cudaMemcpyHostToDevice);
+  cudaMemset(p->m, 0, off * 4);
+  cudaMemset(p->v, 0, off * 4);
+  std::vector<float> one(64, 1.f), zero(64, 0.f);
+  cudaMemcpy(p->fmean, zero.data(), 256, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->tmean, zero.data(), 256, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->fstd, one.data(), 256, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->tstd, one.data(), 256, cudaMemcpyHostToDevice);
+  sync_weights(p, nullptr);
+  if (cudaDeviceSynchronize() != cudaSuccess) { set_error("ks_mlp_create: CUDA error"); return KS_ECUDA; }
+  *out = p;
+  return KS_OK;
+}
+
+extern "C" void ks_mlp_destroy(ks_mlp* p) {
+  if (!p) return;
+  cudaFree(p->w); cudaFree(p->g); cudaFree(p->m); cudaFree(p->v);
+  cudaFree(p->fmean); cudaFree(p->fstd); cudaFree(p->tmean); cudaFree(p->tstd); cudaFree(p->fcols);
+  for (int l = 0; l < 4; l++) { cudaFree(p->Wq[l]); cudaFree(p->WTq[l]); cudaFree(p->bias_pad[l]); }
+  cudaFree(p->X); cudaFree(p->Y); cudaFree(p->T); cudaFree(p->dYb); cudaFree(p->idx); cudaFree(p->loss);
+  for (int i = 0; i < 3; i++) { cudaFree(p->H[i]); cudaFree(p->dH[i]); }
+  delete p;
+}
+
+extern "C" int ks_mlp_num_params(const ks_mlp* p, int64_t* n) {
+  if (!p || !n) return KS_EINVAL;
+  *n = (int64_t)p->nparam;
+  return KS_OK;
+}
+
+extern "C" int ks_mlp_get_params(const ks_mlp* p, float* host) {
+  if (!p || !host) return KS_EINVAL;
+  return cudaMemcpy(host, p->w, p->nparam * 4, cudaMemcpyDeviceToHost) == cudaSuccess ? KS_OK : KS_ECUDA;
+}
+
+extern "C" int ks_mlp_set_params(ks_mlp* p, const float* host) {
+  if (!p || !host) return KS_EINVAL;
+  if (cudaMemcpy(p->w, host, p->nparam * 4, cudaMemcpyHostToDevice) != cudaSuccess) return KS_ECUDA;
+  sync_weights(p, nullptr);
+  return cudaDeviceSynchronize() == cudaSuccess ? KS_OK : KS_ECUDA;
+}
+
+// Features: value columns `cols` (log-transformed where logmask has the bit),
+// standardized by fmean/fstd; targets: the first out_dim unknowns, by tmean/tstd.
+extern "C" int ks_mlp_set_io(ks_mlp* p, const int32_t* cols, uint64_t logmask, const float* fmean, const float* fstd,
+                             const float* tmean, const float* tstd, int32_t scale_col) {
+  if (!p || !cols || !fmean || !fstd || !tmean || !tstd) return KS_EINVAL;
+  p->scale_col = scale_col;
+  cudaMemcpy(p->fcols, cols, p->din * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->fmean, fmean, p->din * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->fstd, fstd, p->din * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->tmean, tmean, p->dout * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->tstd, tstd, p->dout * 4, cudaMemcpyHostToDevice);
+  p->logmask = logmask;
+  return cudaDeviceSynchronize() == cudaSuccess ? KS_OK : KS_ECUDA;
+}
+
+// One forward + backward on host data (standardized X [rows][in], T [rows][out]);
+// grads (FP32, parameter layout) and the loss come back to the host.  For the
+// gradient check against the CPU oracle network.
+extern "C" int ks_mlp_grad(ks_mlp* p, const float* X, const float* T, int32_t rows, float* grads, float* loss) {
+  if (!p || !X || !T || rows <= 0) return KS_EINVAL;
+  int rc = mlp_alloc_batch(p, rows);
+  if (rc) return rc;
+  int R = pad64(rows);
+  std::vector<__nv_bfloat16> xb((size_t)R * p->dip, __float2bfloat16(0.f));
+  std::vector<float> tb((size_t)R * p->dop, 0.f);
+  for (int r = 0; r < rows; r++) {
+    for (int j = 0; j < p->din; j++) xb[(size_t)r * p->dip + j] = __float2bfloat16(X[(size_t)r * p->din + j]);
+    for (int j = 0; j < p->dout; j++) tb[(size_t)r * p->dop + j] = T[(size_t)r * p->dout + j];
+  }
+  cudaMemcpy(p->X, xb.data(), xb.size() * 2, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->T, tb.data(), tb.size() * 4, cudaMemcpyHostToDevice);
+  if (!p->loss && cudaMalloc(&p->loss, 4) != cudaSuccess) return KS_ENOMEM;
+  cudaMemset(p->loss, 0, 4);
+  cudaMemset(p->g, 0, p->nparam * 4);
+  mlp_forward(p, R, nullptr);
+  dim3 blk(64, 4);
+  k_loss_grad<<<(R + 3) / 4, blk>>>(p->Y, p->T, p->dout, p->dop, rows, p->dYb, R, p->loss);
+  mlp_backward(p, R, nullptr);
+  if (cudaDeviceSynchronize() != cudaSuccess) { set_error("ks_mlp_grad: CUDA error"); return KS_ECUDA; }
+  if (grads) cudaMemcpy(grads, p->g, p->nparam * 4, cudaMemcpyDeviceToHost);
+  if (loss) cudaMemcpy(loss, p->loss, 4, cudaMemcpyDeviceToHost);
+  return KS_OK;
+}
+
+// Train on the circuits of a batch: features from the batch's values, targets from
+// solutions x_dev [B][n] (device), rows with status_dev != 0 skipped by the caller's
+// index list idx_dev (device, n_train entries).  `epochs` passes of minibatches of
+// `mb` rows in the order of idx (the caller shuffles).  Returns the last epoch's mean loss.
+extern "C" int ks_mlp_train(ks_mlp* p, ks_batch* b, const double* x_dev, const int32_t* idx_dev, int32_t n_train,
+                            int32_t epochs, int32_t mb, float lr, float* last_loss, void* stream);
+
+// Predict Newton starting points x0_dev [B][n] for every circuit of a batch.
+extern "C" int ks_mlp_predict(ks_mlp* p, ks_batch* b, double* x0_dev, void* stream);
+
+// The batch's SoA value array and shape (for the two calls above).
+int ks_batch_values_view(ks_batch* b, const double** vals, int64_t* B, int* n);
+
+extern "C" int ks_mlp_train(ks_mlp* p, ks_batch* b, const double* x_dev, const int32_t* idx_dev, int32_t n_train,
+                            int32_t epochs, int32_t mb, float lr, float* last_loss, void* stream) {
+  if (!p || !b || !x_dev || !idx_dev || n_train <= 0 || epochs <= 0 || mb <= 0 || mb % 64) return KS_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  const double* vals;
+  int64_t B;
+  int n;
+  ks_batch_values_view(b, &vals, &B, &n);
+  if (p->dout > n) { set_error("ks_mlp_train: more outputs than unknowns"); return KS_EINVAL; }
+  int rc = mlp_alloc_batch(p, mb);
+  if (rc) return rc;
+  if (!p->loss && cudaMalloc(&p->loss, 4) != cudaSuccess) return KS_ENOMEM;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  float lsum = 0.f;
+  int nb = 0;
+  for (int ep = 0; ep < epochs; ep++) {
+    lsum = 0.f; nb = 0;
+    for (int r0 = 0; r0 + mb <= n_train; r0 += mb) {
+      cudaMemcpyAsync(p->idx, idx_dev + r0, mb * 4, cudaMemcpyDeviceToDevice, st);
+      dim3 blk(64, 4);
+      k_features<<<(mb + 3) / 4, blk, 0, st>>>(vals, B, p->idx, p->fcols, p->logmask, p->fmean, p->fstd, p->din, p->dip,
+                                               mb, p->X, mb);
+      k_targets<<<(mb + 3) / 4, blk, 0, st>>>(x_dev, n, p->idx, p->tmean, p->tstd, p->dout, p->dop, mb, p->T, mb, vals,
+                                              B, p->scale_col);
+      cudaMemsetAsync(p->loss, 0, 4, st);
+      cudaMemsetAsync(p->g, 0, p->nparam * 4, st);
+      mlp_forward(p, mb, st);
+      k_loss_grad<<<(mb + 3) / 4, blk, 0, st>>>(p->Y, p->T, p->dout, p->dop, mb, p->dYb, mb, p->loss);
+      mlp_backward(p, mb, st);
+      p->adam_t++;
+      float c1 = 1.f - powf(b1, (float)p->adam_t), c2 = 1.f - powf(b2, (float)p->adam_t);
+      k_adam<<<(unsigned)((p->nparam + 255) / 256), 256, 0, st>>>(p->w, p->g, p->m, p->v, (int)p->nparam, lr, b1, b2, eps, c1, c2);
+      sync_weights(p, st);
+      if (ep == epochs - 1) {
+        float l = 0.f;
+        cudaMemcpyAsync(&l, p->loss, 4, cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        lsum += l; nb++;
+      }
+    }
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess) { set_error("ks_mlp_train: CUDA error"); return KS_ECUDA; }
+  if (last_loss) *last_loss = nb ? lsum / nb : 0.f;
+  return KS_OK;
+}
+
+extern "C" int ks_mlp_predict(ks_mlp* p, ks_batch* b, double* x0_dev, void* stream) {
+  if (!p || !b || !x0_dev) return KS_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  const double* vals;
+  int64_t B;
+  int n;
+  ks_batch_values_view(b, &vals, &B, &n);
+  int rc = mlp_alloc_batch(p, (int)B);
+  if (rc) return rc;
+  int R = pad64((int)B);
+  dim3 blk(64, 4);
+  k_features<<<(R + 3) / 4, blk, 0, st>>>(vals, B, nullptr, p->fcols, p->logmask, p->fmean, p->fstd, p->din, p->dip,
+                                          (int)B, p->X, R);
+  mlp_forward(p, R, st);
+  dim3 blk2(32, 8);
+  k_decode<<<(unsigned)((B + 7) / 8), blk2, 0, st>>>(p->Y, p->dop, p->dout, p->tmean, p->tstd, x0_dev, n, (int)B, vals,
+                                                     B, p->scale_col);
+  return cudaGetLastError() == cudaSuccess ? KS_OK : KS_ECUDA;
+}

@@ -71,6 +71,20 @@ __device__ inline void thr_init(Thr<T>& t, const KPlan& plan, const KOpts& o, un
   t.o = o;
 }
 
+// Point a thread's SoA columns at circuit c (persistent kernels move a thread
+// from circuit to circuit).
+template <int T>
+__device__ inline void thr_bind(Thr<T>& t, const double* values, const double* derived, double* state, double* work,
+                                int64_t B, int64_t c) {
+  const int n = t.n;
+  t.V = Col{const_cast<double*>(values) + c, B};
+  t.D = Col{const_cast<double*>(derived) + c, B};
+  t.Sb = Col{state + c, B};
+  t.save = Col{work + c, B};
+  t.ptPrev = Col{work + (int64_t)n * B + c, B};
+  t.xacc = Col{work + (int64_t)2 * n * B + c, B};
+}
+
 // Bytes of dynamic shared memory thr_init lays out.
 inline size_t thr_smem(int n, int ne, int T) {
   size_t off = (size_t)ne * sizeof(KElem) + ((n + 15) / 16) * 16;

@@ -142,41 +142,45 @@ template <int T>
 __global__ void __launch_bounds__(T) k_tran(KPlan plan, KOpts o, TranSpecK sp, const double* __restrict__ values,
                                             const double* __restrict__ derived, double* state, double* work, int64_t B,
                                             double* out_time, double* out_wave, int32_t* out_npts, int32_t* out_status,
-                                            int32_t* out_steps, int32_t* out_iters, uint64_t deadline_ns) {
+                                            int32_t* out_steps, int32_t* out_iters, uint64_t deadline_ns,
+                                            unsigned long long* queue) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int64_t c = (int64_t)blockIdx.x * T + threadIdx.x;
   Thr<T> t;
-  thr_init<T>(t, plan, o, smem, values, derived, state, work, B, c < B ? c : 0);
+  thr_init<T>(t, plan, o, smem, values, derived, state, work, B, 0);
   __syncthreads();
-  if (c >= B) return;
   const int n = t.n;
   const uint64_t t0 = deadline_ns ? globaltimer_ns() : 0;
-  init_state(t.el, t.ne, t.n_state, t.D, t.Sb);
+  const double eps = 1e-12 * sp.stop;
+  const int maxTotal = o.max_iter_total > 0 ? o.max_iter_total : 0x7fffffff;
+  TruncParams tc{0, 0, BE, o.reltol, o.abstol, o.vntol, sp.chgtol, sp.trtol};
   OpState st;
   LoadParams lp;
-  lp.method = BE; lp.time = 0; lp.h = 0;
-  int phase = TR_START, status = KS_STATUS_OK, accepted = 0, npts = 0, kgrid = 1, order = BE;
+  int phase = TR_DONE, status = KS_STATUS_OK, accepted = 0, npts = 0, kgrid = 1, order = BE;
   bool hitBreak = false, onGrid = false;
   double tnow = 0, h = 0, tn = 0;
-  const double eps = 1e-12 * sp.stop;
-  if (sp.uic) {  // analysis/tran.go:104-116
-    set_initial_conditions<T>(t);
-    op_state_reset<T>(st, o);
-    for (int i = 0; i < n; i++) t.s.x[i * T] = 0.0;
-    lp.mode = ModeUICInit;
-    st.phase = PH_PT_FINAL;  // a plain newton(ITL1): its result ends the start phase
-    st.firstErr = KS_STATUS_NO_CONVERGENCE;
-  } else {
-    dc_start<T>(t, st, nullptr, c, ModeTranOP);
-    lp.mode = ModeTranOP;
-  }
-  TruncParams tc{0, 0, BE, o.reltol, o.abstol, o.vntol, sp.chgtol, sp.trtol};
-  const int maxTotal = o.max_iter_total > 0 ? o.max_iter_total : 0x7fffffff;
+  int64_t c = B;
 
-  // Set up the next time step (the head of the loop at analysis/tran.go:145-163).
-  auto begin_step = [&]() -> bool {
-    if (sp.fixed ? (kgrid > sp.npts - 1) : !(tnow < sp.stop - eps)) { phase = TR_DONE; status = KS_STATUS_OK; return false; }
-    if (accepted >= sp.maxSteps) { phase = TR_DONE; status = KS_STATUS_TOO_MANY_STEPS; return false; }
+  // Starting point of circuit c: analysis/tran.go:103-126.
+  auto start = [&]() {
+    thr_bind<T>(t, values, derived, state, work, B, c);
+    init_state(t.el, t.ne, t.n_state, t.D, t.Sb);
+    lp.method = BE; lp.time = 0; lp.h = 0;
+    phase = TR_START; status = KS_STATUS_OK; accepted = 0; npts = 0; kgrid = 1; order = BE;
+    tnow = 0; h = 0; tn = 0;
+    if (sp.uic) {
+      set_initial_conditions<T>(t);
+      op_state_reset<T>(st, o);
+      for (int i = 0; i < n; i++) t.s.x[i * T] = 0.0;
+      lp.mode = ModeUICInit;
+    } else {
+      dc_start<T>(t, st, nullptr, c, ModeTranOP);
+      lp.mode = ModeTranOP;
+    }
+  };
+  // The head of the time loop, analysis/tran.go:145-163.
+  auto begin_step = [&]() {
+    if (sp.fixed ? (kgrid > sp.npts - 1) : !(tnow < sp.stop - eps)) { phase = TR_DONE; status = KS_STATUS_OK; return; }
+    if (accepted >= sp.maxSteps) { phase = TR_DONE; status = KS_STATUS_TOO_MANY_STEPS; return; }
     hitBreak = false; onGrid = false;
     if (sp.fixed) {
       double target = (double)kgrid * sp.step;
@@ -191,7 +195,6 @@ __global__ void __launch_bounds__(T) k_tran(KPlan plan, KOpts o, TranSpecK sp, c
     h = tn - tnow;
     lp.mode = ModeTran; lp.time = tn; lp.h = h; lp.method = order;
     st.it = 0; st.maxIter = o.itl4;
-    return true;
   };
   auto reject = [&](double hNew) -> bool {  // analysis/tran.go:136-143
     for (int i = 0; i < n; i++) t.s.x[i * T] = t.xacc[i];
@@ -199,72 +202,83 @@ __global__ void __launch_bounds__(T) k_tran(KPlan plan, KOpts o, TranSpecK sp, c
     return true;
   };
 
-  while (phase != TR_DONE) {
-    if (deadline_ns && globaltimer_ns() - t0 > deadline_ns) { status = KS_STATUS_INTERRUPTED; break; }
-    if (st.total >= maxTotal) { status = KS_STATUS_NO_CONVERGENCE; break; }
-    int res = newton_step<T>(t, st, lp);
-    if (res < 0) continue;
-    if (phase == TR_START) {
-      if (!sp.uic) {
-        dc_advance<T>(t, st, res);
-        if (st.phase != PH_DONE) continue;
-        res = st.status;
+  c = (int64_t)atomicAdd(queue, 1ull);
+  if (c < B) start();
+  while (c < B) {
+    if (phase != TR_DONE) {
+      if (deadline_ns && globaltimer_ns() - t0 > deadline_ns) { status = KS_STATUS_INTERRUPTED; phase = TR_DONE; }
+      else if (st.total >= maxTotal) { status = KS_STATUS_NO_CONVERGENCE; phase = TR_DONE; }
+    }
+    if (phase != TR_DONE) {
+      int res = newton_step<T>(t, st, lp);
+      if (res < 0) continue;
+      if (phase == TR_START) {
+        if (!sp.uic) {
+          dc_advance<T>(t, st, res);
+          if (st.phase != PH_DONE) continue;
+          res = st.status;
+        }
+        if (res != KS_STATUS_OK) { status = res; phase = TR_DONE; }
+        else {
+          accept_all<T>(t.el, t.ne, t.V, t.D, t.Sb, t.s.x, 0.0, sp.uic ? ModeUICInit : ModeTranOP, o.gmin, false);
+          record<T>(t, sp, c, B, 0.0, 0, &npts, out_time, out_wave);
+          for (int i = 0; i < n; i++) t.xacc[i] = t.s.x[i * T];
+          phase = TR_STEP;
+          st.initJct = false;
+          h = sp.fixed ? sp.step : fmin(sp.maxStep, fmin(sp.step, sp.stop / 100)) / 10;
+          order = BE;
+          begin_step();
+        }
+      } else if (res != KS_STATUS_OK) {  // a time step's newton failed
+        if (!retryable(res) || t.nonlinEmpty) { status = res; phase = TR_DONE; }
+        else {
+          h /= 8;  // analysis/tran.go:168-175
+          if (reject(h)) { order = BE; begin_step(); }
+        }
+      } else {
+        double proposal = CUDART_INF;
+        bool rejected = false;
+        if (!sp.fixed) {  // analysis/tran.go:178-197
+          tc.time = tn; tc.h = h; tc.method = order;
+          proposal = truncate_all<T>(t, tc);
+          if (proposal < 0.9 * h) {
+            h = fmax(proposal, h / 8);
+            rejected = true;
+            if (reject(h)) begin_step();
+          }
+        }
+        if (!rejected) {
+          accept_all<T>(t.el, t.ne, t.V, t.D, t.Sb, t.s.x, tn, ModeTran, o.gmin, false);  // :200-208
+          if (!sp.fixed || onGrid) record<T>(t, sp, c, B, tn, kgrid, &npts, out_time, out_wave);
+          for (int i = 0; i < n; i++) t.xacc[i] = t.s.x[i * T];
+          accepted++;
+          tnow = tn;
+          order = sp.method;
+          if (sp.fixed) {
+            if (onGrid) kgrid++;
+            h = fmax(fmin(2 * h, sp.maxStep), sp.minStep);
+          } else {  // :211-225
+            double next = fmin(fmin(proposal, 2 * h), sp.maxStep);
+            if (hitBreak) {
+              order = BE;
+              double nb2 = next_breakpoint<T>(t, tnow);
+              next = fmin(next, 0.1 * fmin(sp.maxStep, nb2 - tnow));
+            }
+            h = fmax(next, sp.minStep);
+          }
+          begin_step();
+        }
       }
-      if (res != KS_STATUS_OK) { status = res; phase = TR_DONE; break; }
-      accept_all<T>(t.el, t.ne, t.V, t.D, t.Sb, t.s.x, 0.0, sp.uic ? ModeUICInit : ModeTranOP, o.gmin, false);
-      record<T>(t, sp, c, B, 0.0, 0, &npts, out_time, out_wave);
-      for (int i = 0; i < n; i++) t.xacc[i] = t.s.x[i * T];
-      phase = TR_STEP;
-      st.initJct = false;
-      h = sp.fixed ? sp.step : fmin(sp.maxStep, fmin(sp.step, sp.stop / 100)) / 10;
-      order = BE;
-      begin_step();
-      continue;
+      if (phase != TR_DONE) continue;
     }
-    // a time step's newton finished
-    if (res != KS_STATUS_OK) {
-      if (!retryable(res) || t.nonlinEmpty) { status = res; phase = TR_DONE; break; }
-      h /= 8;  // analysis/tran.go:168-175
-      if (!reject(h)) break;
-      order = BE;
-      begin_step();
-      continue;
-    }
-    double proposal = CUDART_INF;
-    if (!sp.fixed) {  // analysis/tran.go:178-197
-      tc.time = tn; tc.h = h; tc.method = order;
-      proposal = truncate_all<T>(t, tc);
-      if (proposal < 0.9 * h) {
-        h = fmax(proposal, h / 8);
-        if (!reject(h)) break;
-        begin_step();
-        continue;
-      }
-    }
-    accept_all<T>(t.el, t.ne, t.V, t.D, t.Sb, t.s.x, tn, ModeTran, o.gmin, false);  // :200-208
-    if (!sp.fixed || onGrid) record<T>(t, sp, c, B, tn, kgrid, &npts, out_time, out_wave);
-    for (int i = 0; i < n; i++) t.xacc[i] = t.s.x[i * T];
-    accepted++;
-    tnow = tn;
-    order = sp.method;
-    if (sp.fixed) {
-      if (onGrid) kgrid++;
-      h = fmax(fmin(2 * h, sp.maxStep), sp.minStep);
-    } else {  // :211-225
-      double next = fmin(fmin(proposal, 2 * h), sp.maxStep);
-      if (hitBreak) {
-        order = BE;
-        double nb2 = next_breakpoint<T>(t, tnow);
-        next = fmin(next, 0.1 * fmin(sp.maxStep, nb2 - tnow));
-      }
-      h = fmax(next, sp.minStep);
-    }
-    begin_step();
+    // circuit c finished: write its results and take the next one
+    if (out_status) out_status[c] = status;
+    if (out_steps) out_steps[c] = accepted;
+    if (out_iters) out_iters[c] = st.total;
+    if (out_npts) out_npts[c] = sp.fixed ? kgrid : (npts < sp.cap ? npts : sp.cap);
+    c = (int64_t)atomicAdd(queue, 1ull);
+    if (c < B) start();
   }
-  if (out_status) out_status[c] = status;
-  if (out_steps) out_steps[c] = accepted;
-  if (out_iters) out_iters[c] = st.total;
-  if (out_npts) out_npts[c] = sp.fixed ? kgrid : (npts < sp.cap ? npts : sp.cap);
 }
 
 int ks_launch_tran(const KsDeviceBatch& b, const KOpts& o, const ks_tran_spec& spec, int cap, double* out_time,
@@ -294,16 +308,24 @@ int ks_launch_tran(const KsDeviceBatch& b, const KOpts& o, const ks_tran_spec& s
   size_t sm = thr_smem(n, ne, 64);
   if (sm > (size_t)maxSmem) { T = 32; sm = thr_smem(n, ne, 32); }
   if (sm > (size_t)maxSmem) return -2;
-  unsigned grid = (unsigned)((b.B + T - 1) / T);
   cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemsetAsync(b.queue, 0, sizeof(unsigned long long), st) != cudaSuccess) return -1;
+  int sms = 0, per = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (T == 64) {
     cudaFuncSetAttribute(k_tran<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_tran<64><<<grid, 64, sm, st>>>(b.plan, o, sp, b.values, b.derived, b.state, b.work, b.B, out_time, out_wave,
-                                     out_npts, out_status, out_steps, out_iters, dl);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tran<64>, 64, sm);
   } else {
     cudaFuncSetAttribute(k_tran<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_tran<32><<<grid, 32, sm, st>>>(b.plan, o, sp, b.values, b.derived, b.state, b.work, b.B, out_time, out_wave,
-                                     out_npts, out_status, out_steps, out_iters, dl);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tran<32>, 32, sm);
   }
+  int64_t need = (b.B + T - 1) / T, cap_blocks = (int64_t)sms * (per > 0 ? per : 1);
+  unsigned grid = (unsigned)(need < cap_blocks ? need : cap_blocks);
+  if (T == 64)
+    k_tran<64><<<grid, 64, sm, st>>>(b.plan, o, sp, b.values, b.derived, b.state, b.work, b.B, out_time, out_wave,
+                                     out_npts, out_status, out_steps, out_iters, dl, b.queue);
+  else
+    k_tran<32><<<grid, 32, sm, st>>>(b.plan, o, sp, b.values, b.derived, b.state, b.work, b.B, out_time, out_wave,
+                                     out_npts, out_status, out_steps, out_iters, dl, b.queue);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
