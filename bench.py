@@ -33,7 +33,13 @@ sys.path.insert(0, ROOT)
 METRIC = "converged circuit solves/s @ SPICE reltol, chosen vs plain GPU; Newton iters"
 UNIT = "solves/s"
 RELTOL = 1e-6
-ALGO_BYTES_PER_SOLVE = 96  # 7 parameters in + 5 unknowns out, 8 B each
+# workload -> (default circuits, compulsory bytes per solve: parameters in + node voltages out, 8 B each)
+WORKLOADS = {"bjt_ce": (16384, (7 + 5) * 8), "cmos_opamp": (65536, (24 + 7) * 8)}
+
+
+def generator(name):
+    from kronspice_gb300 import workloads
+    return {"bjt_ce": workloads.bjt_ce_batch, "cmos_opamp": workloads.cmos_opamp_batch}[name]
 
 
 def parse():
@@ -42,7 +48,8 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    p.add_argument("--n-circ", type=int, default=16384)
+    p.add_argument("--n-circ", type=int, default=0)
+    p.add_argument("--workload", default="bjt_ce", choices=sorted(WORKLOADS))
     p.add_argument("--seed", type=int, default=0)
     return p.parse_args()
 
@@ -140,8 +147,7 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from kronspice_gb300 import workloads
-    el, nn, vals = workloads.bjt_ce_batch(args.n_circ, args.seed)
+    el, nn, vals = generator(args.workload)(args.n_circ, args.seed)
     from oracle import oracle as orc
     orc.build()
     nthreads = os.cpu_count() or 1
@@ -163,7 +169,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Philox)",
-            "config": {"workload": "bjt_ce_op_%d" % args.n_circ, "n_circuits": args.n_circ, "reltol": RELTOL,
+            "config": {"workload": "%s_op_%d" % (args.workload, args.n_circ), "n_circuits": args.n_circ, "reltol": RELTOL,
                        "abstol": 1e-12, "host_threads": nthreads},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": "%d steps of the full %d-circuit batch on %d host threads; oracle/ks_oracle.cpp, "
@@ -176,6 +182,8 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.n_circ <= 0:
+        args.n_circ = WORKLOADS[args.workload][0]
     if args.impl == "reference":
         run_reference(args)
         return
@@ -188,7 +196,7 @@ def main():
     from kronspice_gb300 import analysis, build, workloads
     build.build()
     dev = torch.device("cuda", local)
-    el, nn, vals = workloads.bjt_ce_batch(args.n_circ, args.seed + rank)
+    el, nn, vals = generator(args.workload)(args.n_circ, args.seed + rank)
     B = vals.shape[0]
     plan = analysis.Plan(el, nn, vals.shape[1])
     batch = analysis.Batch(plan, vals)
@@ -204,7 +212,7 @@ def main():
     learned = None
     try:
         from kronspice_gb300 import learned_start
-        learned = learned_start.for_workload("bjt_ce", el, nn, vals, batch, dev)
+        learned = learned_start.for_workload(args.workload, el, nn, vals, batch, dev)
     except (ImportError, AttributeError):
         learned = None
 
@@ -311,7 +319,7 @@ def main():
     cpu = cpu_baseline(el, nn, vals)
 
     per_launch_s = chosen["seconds"] / args.steps
-    achieved = ALGO_BYTES_PER_SOLVE * B / per_launch_s / 1e9
+    achieved = WORKLOADS[args.workload][1] * B / per_launch_s / 1e9
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -319,13 +327,13 @@ def main():
     except OSError:
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
-    prof = traffic_from_profile().get("k_op_bjt_ce", {})
+    prof = traffic_from_profile().get("k_op_%s" % args.workload, {})
     traffic = prof.get("dram_bytes_per_circuit")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": chosen["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64 device eval + residual, f32 LU", "data": "synthetic (seeded Philox)",
-        "config": {"workload": "bjt_ce_op_%d" % B, "n_circuits_per_gpu": B, "n_unknowns": n, "reltol": RELTOL,
+        "config": {"workload": "%s_op_%d" % (args.workload, B), "n_circuits_per_gpu": B, "n_unknowns": n, "reltol": RELTOL,
                    "abstol": 1e-12, "l2": "flushed between timed steps (512 MB write)",
                    "learned_start": learned is not None},
         "plain": {"value": plain_value, "ms_per_step": plain["ms_per_step"], "newton_iters_mean": plain["iters_mean"],
@@ -342,8 +350,9 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "traffic": None if traffic is None else traffic * B,
-                     "note": "k_op is FP64-issue and latency bound, not HBM bound: achieved counts the 96 B/solve "
-                             "of compulsory traffic, peak is the measured copy bandwidth"},
+                     "note": "k_op is latency bound (FP64 dependency chains, one circuit per thread), not HBM bound: "
+                             "achieved counts the compulsory %d B/solve, peak is the measured copy bandwidth"
+                             % WORKLOADS[args.workload][1]},
         "cpu_baseline": cpu,
         "clocks": clocks,
     }

@@ -27,8 +27,10 @@
 #ifndef KRONSPICE_GPU_H
 #define KRONSPICE_GPU_H
 
+#ifndef __CUDACC_RTC__
 #include <stddef.h>
 #include <stdint.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {

@@ -6,13 +6,16 @@
 // equations are those of the reference's devices, cited per function.
 // Stamps go into a per-thread dense matrix in shared memory (stride TPB).
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cuda_runtime.h>
-#include <math_constants.h>
 #include <stdint.h>
+#endif
 #include "ks_engine.h"
 #include "../../include/kronspice_gpu.h"
 
 namespace ksg {
+
+#define KS_INF __longlong_as_double(0x7ff0000000000000LL)
 
 constexpr double kQ = 1.602176634e-19;     // device/diode.go:15
 constexpr double kK = 1.380649e-23;        // device/diode.go:16
@@ -34,21 +37,21 @@ struct Col {
   __device__ __forceinline__ double& operator[](int k) const { return p[(int64_t)k * B]; }
 };
 
-// Per-thread dense system in shared memory, element (i, j) at a[(i*n + j) * T].
-template <int T>
-struct SysRef {
-  double* a;    // matrix  (n*n)
-  double* rhs;  // right-hand side (n)
-  const double* x;  // linearization point X (n)
-  int n;
-  __device__ __forceinline__ void add(int i, int j, double v) const {
-    if (i >= 0 && j >= 0) a[(i * n + j) * T] += v;
-  }
-  __device__ __forceinline__ void addRHS(int i, double v) const {
-    if (i >= 0) rhs[i * T] += v;
-  }
-  __device__ __forceinline__ double X(int i) const { return i >= 0 ? x[i * T] : 0.0; }
-};
+// Stamping into a thread's system S (shared-memory or register storage, see
+// ks_solve.cuh): S provides a(i, j), rhs(i), xo(i) (the linearization point X of
+// the current load) and xn(i) (the new iterate).  Ground (-1) is dropped.
+template <class S>
+__device__ __forceinline__ void sadd(S& s, int i, int j, double v) {
+  if (i >= 0 && j >= 0) s.a(i, j) += v;
+}
+template <class S>
+__device__ __forceinline__ void srhs(S& s, int i, double v) {
+  if (i >= 0) s.rhs(i) += v;
+}
+template <class S>
+__device__ __forceinline__ double xo_(S& s, int i) { return i >= 0 ? s.xo(i) : 0.0; }
+template <class S>
+__device__ __forceinline__ double xn_(S& s, int i) { return i >= 0 ? s.xn(i) : 0.0; }
 
 struct LoadParams {  // device/device.go:127-148
   int mode, method;
@@ -60,8 +63,6 @@ struct LoadParams {  // device/device.go:127-148
 };
 
 struct TruncParams { double time, h; int method; double reltol, abstol, vntol, chgtol, trtol; };
-
-__device__ __forceinline__ double xat(const double* x, int i, int T) { return i >= 0 ? x[i * T] : 0.0; }
 
 // ---------------------------------------------------------------- history / LTE
 __device__ inline void hist_push(const Col& S, int h, double t, double q) {  // device/lte.go:23-31
@@ -75,20 +76,20 @@ __device__ inline void hist_reset(const Col& S, int h) { S[h + H_N] = 0; }
 __device__ inline double lte_step(const Col& S, int h, double qn, double in, double inPrev, double absTol,
                                   const TruncParams& tc) {
   int k = tc.method;
-  if (k < 1 || k > 2 || S[h + H_N] < k + 1) return CUDART_INF;
+  if (k < 1 || k > 2 || S[h + H_N] < k + 1) return KS_INF;
   double ts[4] = {tc.time, S[h + H_T0], S[h + H_T1], S[h + H_T2]};
   double dd[4] = {qn, S[h + H_Q0], S[h + H_Q1], S[h + H_Q2]};
   for (int order = 1; order <= k + 1; order++) {
     for (int i = 0; i + order <= k + 1; i++) {
       double den = ts[i] - ts[i + order];
-      if (den == 0) return CUDART_INF;
+      if (den == 0) return KS_INF;
       dd[i] = (dd[i] - dd[i + 1]) / den;
     }
   }
   double fact = k == 2 ? 6.0 : 2.0, c = k == 2 ? 1.0 / 12 : 0.5;
   double hh = tc.h;
   double errI = c * (k == 2 ? hh * hh : hh) * fabs(dd[0] * fact);
-  if (errI == 0 || isnan(errI)) return CUDART_INF;
+  if (errI == 0 || isnan(errI)) return KS_INF;
   double qmax = fmax(fabs(qn), fabs(S[h + H_Q0]));
   double allowed = tc.trtol * fmax(tc.reltol * fmax(fabs(in), fabs(inPrev)) + absTol, tc.reltol * fmax(qmax, tc.chgtol) / hh);
   return k == 2 ? hh * sqrt(allowed / errI) : hh * (allowed / errI);
@@ -178,7 +179,7 @@ __device__ inline double wave_next_breakpoint(int kind, const Col& D, int d, con
     double edges[4] = {0, tr, tr + pw, tr + pw + tf};
     if (per <= 0) {
       for (int i = 0; i < 4; i++) if (td + edges[i] > lim) return td + edges[i];
-      return CUDART_INF;
+      return KS_INF;
     }
     double k = floor((t - td) / per);
     if (k < 0) k = 0;
@@ -195,7 +196,7 @@ __device__ inline double wave_next_breakpoint(int kind, const Col& D, int d, con
   } else if (kind == KS_WAVE_PWL) {
     for (int k = 0; k < nargs / 2; k++) if (V[args + 2 * k] > lim) return V[args + 2 * k];
   }
-  return CUDART_INF;
+  return KS_INF;
 }
 
 // sourceValue.at, device/source.go:43-66 (SV_OVR/SV_OVRON: the .DC override).
@@ -244,14 +245,14 @@ __device__ inline void diode_charge(const Col& V, int p, double v, double id, do
 }
 
 // Load, device/diode.go:229-275.
-template <int T>
-__device__ inline void diode_load(const KElem& e, const Col& V, const Col& Dv, const Col& S, const SysRef<T>& sys,
+template <class SY>
+__device__ inline void diode_load(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
                                   const LoadParams& lp) {
   int p = e.param, dd = e.derived;
   int a = e.u[0], k = e.u[1], ai = e.u[2];
   bool hasBV = e.flags & KS_F_HAS_BV;
   double vte = Dv[dd + DD_VTE], vcrit = Dv[dd + DD_VCRIT], xbv = Dv[dd + DD_XBV];
-  double vraw = sys.X(ai) - sys.X(k);
+  double vraw = xo_(sys, ai) - xo_(sys, k);
   double vd;
   bool lim;
   if (lp.initJct) { vd = vcrit; lim = true; }
@@ -280,17 +281,17 @@ __device__ inline void diode_load(const KElem& e, const Col& V, const Col& Dv, c
   S[SD_VD] = vd; S[SD_CD] = cd; S[SD_GD] = gd; S[SD_IQ] = iq; S[SD_GEQ] = geq;
   S[SD_LIM] = lim ? 1.0 : 0.0; S[SD_TRAN] = tran ? 1.0 : 0.0;
   double gg = gd + geq, ieq = cd + iq - gg * vd;
-  sys.add(ai, ai, gg); sys.add(k, k, gg); sys.add(ai, k, -gg); sys.add(k, ai, -gg);
-  sys.addRHS(ai, -ieq); sys.addRHS(k, ieq);
+  sadd(sys, ai, ai, gg); sadd(sys, k, k, gg); sadd(sys, ai, k, -gg); sadd(sys, k, ai, -gg);
+  srhs(sys, ai, -ieq); srhs(sys, k, ieq);
   double grs = Dv[dd + DD_GRS];
-  if (grs > 0) { sys.add(a, a, grs); sys.add(ai, ai, grs); sys.add(a, ai, -grs); sys.add(ai, a, -grs); }
+  if (grs > 0) { sadd(sys, a, a, grs); sadd(sys, ai, ai, grs); sadd(sys, a, ai, -grs); sadd(sys, ai, a, -grs); }
 }
 
 // ConvTest, device/diode.go:282-289.
-template <int T>
-__device__ inline bool diode_conv(const KElem& e, const Col& V, const Col& Dv, const Col& S, const double* x,
+template <class SY>
+__device__ inline bool diode_conv(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
                                   double reltol, double abstol, double gmin) {
-  double v = xat(x, e.u[2], T) - xat(x, e.u[1], T);
+  double v = xn_(sys, e.u[2]) - xn_(sys, e.u[1]);
   double cdhat = S[SD_CD] + S[SD_GD] * (v - S[SD_VD]);
   double id, g;
   diode_iv(V, Dv, e.param, e.derived, e.flags & KS_F_HAS_BV, v, &id, &g);
@@ -299,10 +300,10 @@ __device__ inline bool diode_conv(const KElem& e, const Col& V, const Col& Dv, c
 }
 
 // Accept, device/diode.go:304-322.
-template <int T>
-__device__ inline void diode_accept(const KElem& e, const Col& V, const Col& Dv, const Col& S, const double* x,
+template <class SY>
+__device__ inline void diode_accept(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
                                     double t, int mode) {
-  double v = xat(x, e.u[2], T) - xat(x, e.u[1], T);
+  double v = xn_(sys, e.u[2]) - xn_(sys, e.u[1]);
   S[SD_VDACC] = v;
   double id, g, q, c;
   diode_iv(V, Dv, e.param, e.derived, e.flags & KS_F_HAS_BV, v, &id, &g);
@@ -438,38 +439,39 @@ __device__ inline BjtCh bjt_charges(const Col& V, const Col& Dv, int p, int dd, 
   return ch;
 }
 
-template <int T>
-__device__ inline void bjt_voltages(const KElem& e, const Col& V, const double* x, double* vbe, double* vbc,
-                                    double* vbx, double* vcs) {  // device/bjt.go:415-419
+template <bool NEW, class SY>
+__device__ inline void bjt_voltages(const KElem& e, SY& s, double* vbe, double* vbc, double* vbx,
+                                    double* vcs) {  // device/bjt.go:415-419 (NEW: at the new iterate, else at X)
+  auto X = [&](int i) { return NEW ? xn_(s, i) : xo_(s, i); };
   double t = (e.flags & KS_F_PTYPE) ? -1.0 : 1.0;
-  double vb = xat(x, e.u[2], T), vbp = xat(x, e.u[5], T), vcp = xat(x, e.u[4], T), vep = xat(x, e.u[6], T);
+  double vb = X(e.u[2]), vbp = X(e.u[5]), vcp = X(e.u[4]), vep = X(e.u[6]);
   *vbe = t * (vbp - vep); *vbc = t * (vbp - vcp); *vbx = t * (vb - vcp);
-  *vcs = t * (xat(x, e.u[7], T) - xat(x, e.u[8], T));
+  *vcs = t * (X(e.u[7]) - X(e.u[8]));
 }
 
-template <int T>
-__device__ __forceinline__ void bjt_branch(const SysRef<T>& s, double typ, int a, int b, double i0, double g1, int p1,
+template <class SY>
+__device__ __forceinline__ void bjt_branch(SY& s, double typ, int a, int b, double i0, double g1, int p1,
                                            int n1, double v10, double g2, int p2, int n2, double v20) {  // :463-480
-  if (g1 != 0) { s.add(a, p1, g1); s.add(a, n1, -g1); s.add(b, p1, -g1); s.add(b, n1, g1); }
-  if (g2 != 0) { s.add(a, p2, g2); s.add(a, n2, -g2); s.add(b, p2, -g2); s.add(b, n2, g2); }
+  if (g1 != 0) { sadd(s, a, p1, g1); sadd(s, a, n1, -g1); sadd(s, b, p1, -g1); sadd(s, b, n1, g1); }
+  if (g2 != 0) { sadd(s, a, p2, g2); sadd(s, a, n2, -g2); sadd(s, b, p2, -g2); sadd(s, b, n2, g2); }
   double ieq = typ * (i0 - g1 * v10 - g2 * v20);
-  s.addRHS(a, -ieq); s.addRHS(b, ieq);
+  srhs(s, a, -ieq); srhs(s, b, ieq);
 }
 
-template <int T>
-__device__ __forceinline__ void stamp_g(const SysRef<T>& s, int a, int b, double g) {  // device/bjt.go:482-490
+template <class SY>
+__device__ __forceinline__ void stamp_g(SY& s, int a, int b, double g) {  // device/bjt.go:482-490
   if (g == 0) return;
-  s.add(a, a, g); s.add(b, b, g); s.add(a, b, -g); s.add(b, a, -g);
+  sadd(s, a, a, g); sadd(s, b, b, g); sadd(s, a, b, -g); sadd(s, b, a, -g);
 }
 
 // Load + stamp, device/bjt.go:422-515.
-template <int T>
-__device__ inline void bjt_load(const KElem& e, const Col& V, const Col& Dv, const Col& S, const SysRef<T>& sys,
+template <class SY>
+__device__ inline void bjt_load(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
                                 const LoadParams& lp) {
   int p = e.param, dd = e.derived;
   double vt = Dv[dd + DQ_VT], vcrit = Dv[dd + DQ_VCRIT];
   double vbe, vbc, vbx, vcs;
-  bjt_voltages<T>(e, V, sys.x, &vbe, &vbc, &vbx, &vcs);
+  bjt_voltages<false>(e, sys, &vbe, &vbc, &vbx, &vcs);
   bool lim;
   if (lp.initJct) { vbe = vcrit; vbc = 0; lim = true; vbx = 0; vcs = 0; }
   else {
@@ -507,27 +509,27 @@ __device__ inline void bjt_load(const KElem& e, const Col& V, const Col& Dv, con
   for (int k = 0; k < 4; k++) S[SQ_IQ0 + k] = iq[k];
   double typ = (e.flags & KS_F_PTYPE) ? -1.0 : 1.0;
   int b = e.u[2], cp = e.u[4], bp = e.u[5], ep = e.u[6], sa = e.u[7], sb = e.u[8];
-  bjt_branch<T>(sys, typ, cp, ep, d.it, d.itBE, bp, ep, vbe, d.itBC, bp, cp, vbc);
-  bjt_branch<T>(sys, typ, bp, ep, d.ibe, d.gpi, bp, ep, vbe, 0, 0, 0, 0);
-  bjt_branch<T>(sys, typ, bp, cp, d.ibc, d.gmu, bp, cp, vbc, 0, 0, 0, 0);
-  bjt_branch<T>(sys, typ, sa, sb, isub, gsub, sa, sb, vcs, 0, 0, 0, 0);
+  bjt_branch(sys, typ, cp, ep, d.it, d.itBE, bp, ep, vbe, d.itBC, bp, cp, vbc);
+  bjt_branch(sys, typ, bp, ep, d.ibe, d.gpi, bp, ep, vbe, 0, 0, 0, 0);
+  bjt_branch(sys, typ, bp, cp, d.ibc, d.gmu, bp, cp, vbc, 0, 0, 0, 0);
+  bjt_branch(sys, typ, sa, sb, isub, gsub, sa, sb, vcs, 0, 0, 0, 0);
   if (tran) {
-    bjt_branch<T>(sys, typ, bp, ep, iq[0], ag * ch.c[0], bp, ep, vbe, ag * ch.dqbeDvbc, bp, cp, vbc);
-    bjt_branch<T>(sys, typ, bp, cp, iq[1], ag * ch.c[1], bp, cp, vbc, 0, 0, 0, 0);
-    bjt_branch<T>(sys, typ, b, cp, iq[2], ag * ch.c[2], b, cp, vbx, 0, 0, 0, 0);
-    bjt_branch<T>(sys, typ, sa, sb, iq[3], ag * ch.c[3], sa, sb, vcs, 0, 0, 0, 0);
+    bjt_branch(sys, typ, bp, ep, iq[0], ag * ch.c[0], bp, ep, vbe, ag * ch.dqbeDvbc, bp, cp, vbc);
+    bjt_branch(sys, typ, bp, cp, iq[1], ag * ch.c[1], bp, cp, vbc, 0, 0, 0, 0);
+    bjt_branch(sys, typ, b, cp, iq[2], ag * ch.c[2], b, cp, vbx, 0, 0, 0, 0);
+    bjt_branch(sys, typ, sa, sb, iq[3], ag * ch.c[3], sa, sb, vcs, 0, 0, 0, 0);
   }
-  if (bp != b) stamp_g<T>(sys, b, bp, d.gx);
-  if (cp != e.u[0]) stamp_g<T>(sys, e.u[0], cp, Dv[dd + DQ_GCPR]);
-  if (ep != e.u[1]) stamp_g<T>(sys, e.u[1], ep, Dv[dd + DQ_GEPR]);
+  if (bp != b) stamp_g(sys, b, bp, d.gx);
+  if (cp != e.u[0]) stamp_g(sys, e.u[0], cp, Dv[dd + DQ_GCPR]);
+  if (ep != e.u[1]) stamp_g(sys, e.u[1], ep, Dv[dd + DQ_GEPR]);
 }
 
 // ConvTest, device/bjt.go:522-532.
-template <int T>
-__device__ inline bool bjt_conv(const KElem& e, const Col& V, const Col& Dv, const Col& S, const double* x,
+template <class SY>
+__device__ inline bool bjt_conv(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
                                 double reltol, double abstol, double gmin) {
   double vbe, vbc, vbx, vcs;
-  bjt_voltages<T>(e, V, x, &vbe, &vbc, &vbx, &vcs);
+  bjt_voltages<true>(e, sys, &vbe, &vbc, &vbx, &vcs);
   double dbe = vbe - S[SQ_VBE], dbc = vbc - S[SQ_VBC];
   double ichat = S[SQ_IT] - S[SQ_IBC] + S[SQ_ITBE] * dbe + (S[SQ_ITBC] - S[SQ_GMU]) * dbc;
   double ibhat = S[SQ_IBE] + S[SQ_IBC] + S[SQ_GPI] * dbe + S[SQ_GMU] * dbc;
@@ -538,11 +540,11 @@ __device__ inline bool bjt_conv(const KElem& e, const Col& V, const Col& Dv, con
 }
 
 // Accept, device/bjt.go:579-601.
-template <int T>
-__device__ inline void bjt_accept(const KElem& e, const Col& V, const Col& Dv, const Col& S, const double* x,
+template <class SY>
+__device__ inline void bjt_accept(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
                                   double t, int mode, double gmin) {
   double vbe, vbc, vbx, vcs;
-  bjt_voltages<T>(e, V, x, &vbe, &vbc, &vbx, &vcs);
+  bjt_voltages<true>(e, sys, &vbe, &vbc, &vbx, &vcs);
   S[SQ_VBEACC] = vbe; S[SQ_VBCACC] = vbc;
   BjtDC d = bjt_eval_dc(V, Dv, e.param, e.derived, vbe, vbc, gmin);
   BjtCh ch = bjt_charges(V, Dv, e.param, e.derived, vbe, vbc, vbx, vcs, d);

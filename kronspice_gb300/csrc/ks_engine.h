@@ -12,7 +12,15 @@
 //   derived [n_derived][B] per-circuit constants (setup kernel)
 //   state   [n_state][B]   device linearization and accepted state
 #pragma once
+#ifdef __CUDACC_RTC__
+typedef signed char int8_t;
+typedef int int32_t;
+typedef long long int64_t;
+typedef unsigned int uint32_t;
+typedef unsigned long long uint64_t;
+#else
 #include <stdint.h>
+#endif
 
 #define KS_MAX_DENSE 32  // largest system of the thread-per-circuit kernels
 

@@ -120,42 +120,11 @@ __global__ void __launch_bounds__(T) k_op(KPlan plan, KOpts o, const double* __r
                                           int32_t* out_status, int32_t* out_iters, uint64_t deadline_ns,
                                           unsigned long long* queue) {
   extern __shared__ __align__(16) unsigned char smem[];
-  Thr<T> t;
-  thr_init<T>(t, plan, o, smem, values, derived, state, work, B, 0);
+  Thr<SmemSys<T>, RtProg> t;
+  smem_layout<T>(t, plan, smem);
+  t.o = o;
   __syncthreads();
-  const uint64_t t0 = deadline_ns ? globaltimer_ns() : 0;
-  const int maxTotal = o.max_iter_total > 0 ? o.max_iter_total : 3300 * o.itl1 + 16;
-  const int n = t.n;
-  LoadParams lp;
-  lp.mode = ModeOP; lp.method = BE; lp.time = 0; lp.h = 0;
-  OpState st;
-  int64_t c = (int64_t)atomicAdd(queue, 1ull);
-  if (c < B) {
-    thr_bind<T>(t, values, derived, state, work, B, c);
-    init_state(t.el, t.ne, t.n_state, t.D, t.Sb);
-    dc_start<T>(t, st, x0, c, ModeOP);
-  }
-  while (c < B) {
-    bool done = false;
-    if (deadline_ns && globaltimer_ns() - t0 > deadline_ns) { st.status = KS_STATUS_INTERRUPTED; done = true; }
-    else if (st.total >= maxTotal) { st.status = KS_STATUS_NO_CONVERGENCE; done = true; }
-    else {
-      int res = newton_step<T>(t, st, lp);
-      if (res >= 0) dc_advance<T>(t, st, res);
-      done = st.phase == PH_DONE;
-    }
-    if (!done) continue;
-    if (st.status == KS_STATUS_OK) accept_all<T>(t.el, t.ne, t.V, t.D, t.Sb, t.s.x, 0.0, ModeOP, o.gmin, false);
-    if (out_x) for (int i = 0; i < n; i++) out_x[c * n + i] = t.s.x[i * T];
-    if (out_status) out_status[c] = st.status;
-    if (out_iters) out_iters[c] = st.total;
-    c = (int64_t)atomicAdd(queue, 1ull);
-    if (c < B) {
-      thr_bind<T>(t, values, derived, state, work, B, c);
-      init_state(t.el, t.ne, t.n_state, t.D, t.Sb);
-      dc_start<T>(t, st, x0, c, ModeOP);
-    }
-  }
+  op_persistent(t, values, derived, state, work, B, x0, out_x, out_status, out_iters, deadline_ns, queue);
 }
 
 // Blocks of T threads that keep every SM full (persistent grid), capped by the work.

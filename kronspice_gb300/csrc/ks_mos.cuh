@@ -495,33 +495,34 @@ __device__ inline void mos_bulk_charge(const Col& V, int p, const Col& D, int d,
   *q = q1 + q2; *c = c1 + c2;
 }
 
-template <int T>
-__device__ inline void mos_voltages(const KElem& e, const double* x, double* vgs, double* vds, double* vbs, double* vgb) {
+template <bool NEW, class SY>
+__device__ inline void mos_voltages(const KElem& e, SY& s, double* vgs, double* vds, double* vbs, double* vgb) {
+  auto X = [&](int i) { return NEW ? xn_(s, i) : xo_(s, i); };
   double t = (e.flags & KS_F_PTYPE) ? -1.0 : 1.0;  // device/mosfet.go:340-344
-  double vg = xat(x, e.u[2], T), vb = xat(x, e.u[3], T), vdp = xat(x, e.u[4], T), vsp = xat(x, e.u[5], T);
+  double vg = X(e.u[2]), vb = X(e.u[3]), vdp = X(e.u[4]), vsp = X(e.u[5]);
   *vgs = t * (vg - vsp); *vds = t * (vdp - vsp); *vbs = t * (vb - vsp); *vgb = t * (vg - vb);
 }
 
-template <int T>
-__device__ __forceinline__ void mos_branch1(const SysRef<T>& s, double typ, int a, int b, double i0, double g, int pk,
+template <class SY>
+__device__ __forceinline__ void mos_branch1(SY& s, double typ, int a, int b, double i0, double g, int pk,
                                             int mk, double v0) {  // device/mosfet.go:563-578, one control
   double ieq = i0;
   if (g != 0) {
-    s.add(a, pk, g); s.add(a, mk, -g); s.add(b, pk, -g); s.add(b, mk, g);
+    sadd(s, a, pk, g); sadd(s, a, mk, -g); sadd(s, b, pk, -g); sadd(s, b, mk, g);
     ieq -= g * v0;
   }
   ieq *= typ;
-  s.addRHS(a, -ieq); s.addRHS(b, ieq);
+  srhs(s, a, -ieq); srhs(s, b, ieq);
 }
 
 // Load + stamp, device/mosfet.go:476-611.
-template <int T>
-__device__ inline void mos_load(const KElem& e, const Col& V, const Col& D, const Col& S, const SysRef<T>& sys,
+template <class SY>
+__device__ inline void mos_load(const KElem& e, const Col& V, const Col& D, const Col& S, SY& sys,
                                 const LoadParams& lp) {
   int d = e.derived, p = e.param;
   double vt = D[d + DM_VT];
   double vgs, vds, vbs, vgb0;
-  mos_voltages<T>(e, sys.x, &vgs, &vds, &vbs, &vgb0);
+  mos_voltages<false>(e, sys, &vgs, &vds, &vbs, &vgb0);
   bool lim = false;
   if (lp.initJct) { vbs = -1; vgs = D[d + DM_VTO]; vds = 0; lim = true; }
   else {
@@ -585,29 +586,29 @@ __device__ inline void mos_load(const KElem& e, const Col& V, const Col& D, cons
   if (o[0] <= 0) { i0 = -o[1]; g0 = -o[2]; g1 = o[2] + o[3] + o[4]; g2 = -o[4]; }
   {  // channel branch dp -> sp controlled by vgs, vds, vbs
     double ieq = i0;
-    if (g0 != 0) { sys.add(dp, g, g0); sys.add(dp, sp, -g0); sys.add(sp, g, -g0); sys.add(sp, sp, g0); ieq -= g0 * vgs; }
-    if (g1 != 0) { sys.add(dp, dp, g1); sys.add(dp, sp, -g1); sys.add(sp, dp, -g1); sys.add(sp, sp, g1); ieq -= g1 * vds; }
-    if (g2 != 0) { sys.add(dp, b, g2); sys.add(dp, sp, -g2); sys.add(sp, b, -g2); sys.add(sp, sp, g2); ieq -= g2 * vbs; }
+    if (g0 != 0) { sadd(sys, dp, g, g0); sadd(sys, dp, sp, -g0); sadd(sys, sp, g, -g0); sadd(sys, sp, sp, g0); ieq -= g0 * vgs; }
+    if (g1 != 0) { sadd(sys, dp, dp, g1); sadd(sys, dp, sp, -g1); sadd(sys, sp, dp, -g1); sadd(sys, sp, sp, g1); ieq -= g1 * vds; }
+    if (g2 != 0) { sadd(sys, dp, b, g2); sadd(sys, dp, sp, -g2); sadd(sys, sp, b, -g2); sadd(sys, sp, sp, g2); ieq -= g2 * vbs; }
     ieq *= typ;
-    sys.addRHS(dp, -ieq); sys.addRHS(sp, ieq);
+    srhs(sys, dp, -ieq); srhs(sys, sp, ieq);
   }
-  mos_branch1<T>(sys, typ, b, sp, cbs, gbs, b, sp, vbs);
-  mos_branch1<T>(sys, typ, b, dp, cbd, gbd, b, dp, vbd);
+  mos_branch1(sys, typ, b, sp, cbs, gbs, b, sp, vbs);
+  mos_branch1(sys, typ, b, dp, cbd, gbd, b, dp, vbd);
   if (tran) {
     const int ea[5] = {g, g, g, b, b}, eb[5] = {sp, dp, b, sp, dp};
-    for (int k = 0; k < 5; k++) mos_branch1<T>(sys, typ, ea[k], eb[k], iq[k], ag * cap[k], ea[k], eb[k], dv[k]);
+    for (int k = 0; k < 5; k++) mos_branch1(sys, typ, ea[k], eb[k], iq[k], ag * cap[k], ea[k], eb[k], dv[k]);
   }
-  if (dp != e.u[0]) stamp_g<T>(sys, e.u[0], dp, D[d + DM_GDPR]);
-  if (sp != e.u[1]) stamp_g<T>(sys, e.u[1], sp, D[d + DM_GSPR]);
+  if (dp != e.u[0]) stamp_g(sys, e.u[0], dp, D[d + DM_GDPR]);
+  if (sp != e.u[1]) stamp_g(sys, e.u[1], sp, D[d + DM_GSPR]);
 }
 
 // ConvTest, device/mosfet.go:618-631.
-template <int T>
-__device__ inline bool mos_conv(const KElem& e, const Col& V, const Col& D, const Col& S, const double* x,
+template <class SY>
+__device__ inline bool mos_conv(const KElem& e, const Col& V, const Col& D, const Col& S, SY& sys,
                                 double reltol, double abstol, double gmin) {
   int d = e.derived;
   double vgs, vds, vbs, vgb;
-  mos_voltages<T>(e, x, &vgs, &vds, &vbs, &vgb);
+  mos_voltages<true>(e, sys, &vgs, &vds, &vbs, &vgb);
   double vbd = vbs - vds;
   double i0 = S[SM_CDRAIN], g0 = S[SM_GM], g1 = S[SM_GDS], g2 = S[SM_GMBS];
   if (S[SM_MODE] <= 0) { double gm = g0; i0 = -i0; g0 = -gm; g1 = gm + g1 + g2; g2 = -g2; }
@@ -627,12 +628,12 @@ __device__ inline bool mos_conv(const KElem& e, const Col& V, const Col& D, cons
 }
 
 // Accept, device/mosfet.go:668-705.
-template <int T>
-__device__ inline void mos_accept(const KElem& e, const Col& V, const Col& D, const Col& S, const double* x,
+template <class SY>
+__device__ inline void mos_accept(const KElem& e, const Col& V, const Col& D, const Col& S, SY& sys,
                                   double t, int mode) {
   int d = e.derived, p = e.param;
   double vgs, vds, vbs, vgb;
-  mos_voltages<T>(e, x, &vgs, &vds, &vbs, &vgb);
+  mos_voltages<true>(e, sys, &vgs, &vds, &vbs, &vgb);
   double vgd = vgs - vds, vbd = vbs - vds;
   double o[7];
   mos_channel(e, V, D, vgs, vds, vbs, o);

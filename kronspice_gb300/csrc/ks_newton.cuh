@@ -1,5 +1,5 @@
 // ks_newton.cuh — per-thread Newton and DC-solve state machine of the GB300 engine,
-// shared by the operating-point and transient kernels.
+// shared by the operating-point and transient kernels (generic and per-topology).
 //
 // One pass of the kernels' loop is one (*Sim).solve (analysis/op.go:289-322); the
 // scalar control code here decides what the next solve is, restating
@@ -24,25 +24,36 @@ __device__ __forceinline__ bool retryable(int e) {  // analysis/newton.go:86-89
   return e == KS_STATUS_NO_CONVERGENCE || e == KS_STATUS_NONFINITE || e == KS_STATUS_SINGULAR;
 }
 
-// Everything one thread needs: its shared-memory system, its SoA columns, the
-// element program and the options.
-template <int T>
+// Everything one thread needs: its system, the element program, its SoA columns
+// and the options.
+template <class SY, class P>
 struct Thr {
-  ThreadSys<T> s;
-  const KElem* el;
-  const int8_t* isv;
-  int ne, n, n_nodes, n_state;
-  bool nonlinEmpty;
+  SY s;
+  P prog;
   Col V, D, Sb;
   Col save, ptPrev, xacc;  // work columns (n each)
   KOpts o;
+  __device__ __forceinline__ int n() const { return s.size(); }
 };
 
-// Shared-memory layout of a block: element table, is_voltage flags, then the
-// per-thread arrays with stride T.  Returns the per-thread views.
+// Point a thread's SoA columns at circuit c (persistent kernels move a thread
+// from circuit to circuit).
+template <class SY, class P>
+__device__ inline void thr_bind(Thr<SY, P>& t, const double* values, const double* derived, double* state, double* work,
+                                int64_t B, int64_t c) {
+  const int n = t.n();
+  t.V = Col{const_cast<double*>(values) + c, B};
+  t.D = Col{const_cast<double*>(derived) + c, B};
+  t.Sb = Col{state + c, B};
+  t.save = Col{work + c, B};
+  t.ptPrev = Col{work + (int64_t)n * B + c, B};
+  t.xacc = Col{work + (int64_t)2 * n * B + c, B};
+}
+
+// Generic kernels: element table and is_voltage flags copied to shared memory,
+// then each thread's system in shared memory with stride T.
 template <int T>
-__device__ inline void thr_init(Thr<T>& t, const KPlan& plan, const KOpts& o, unsigned char* smem, const double* values,
-                                const double* derived, double* state, double* work, int64_t B, int64_t c) {
+__device__ inline void smem_layout(Thr<SmemSys<T>, RtProg>& t, const KPlan& plan, unsigned char* smem) {
   const int n = plan.n, ne = plan.n_elem;
   KElem* el = reinterpret_cast<KElem*>(smem);
   for (int i = threadIdx.x; i < ne * (int)(sizeof(KElem) / 4); i += T)
@@ -52,48 +63,44 @@ __device__ inline void thr_init(Thr<T>& t, const KPlan& plan, const KOpts& o, un
   size_t off = ne * sizeof(KElem) + ((n + 15) / 16) * 16;
   double* base = reinterpret_cast<double*>(smem + off);
   const int tid = threadIdx.x;
-  t.s.n = n;
-  t.s.A = base + tid;
-  t.s.rhs = base + (size_t)n * n * T + tid;
-  t.s.x = t.s.rhs + (size_t)n * T;
-  t.s.xold = t.s.x + (size_t)n * T;
-  t.s.col = t.s.xold + (size_t)n * T;
-  t.s.piv = reinterpret_cast<int*>(base + (size_t)(n * n + 4 * n) * T) + tid;
-  t.s.L32 = reinterpret_cast<float*>(base + (size_t)(n * n + 4 * n) * T + ((size_t)n * T + 1) / 2) + tid;
-  t.el = el; t.isv = isv; t.ne = ne; t.n = n; t.n_nodes = plan.n_nodes; t.n_state = plan.n_state;
-  t.nonlinEmpty = plan.n_nonlin == 0;
-  t.V = Col{const_cast<double*>(values) + c, B};
-  t.D = Col{const_cast<double*>(derived) + c, B};
-  t.Sb = Col{state + c, B};
-  t.save = Col{work + c, B};
-  t.ptPrev = Col{work + (int64_t)n * B + c, B};
-  t.xacc = Col{work + (int64_t)2 * n * B + c, B};
-  t.o = o;
+  t.s.n_ = n;
+  t.s.A_ = base + tid;
+  t.s.rhs_ = base + (size_t)n * n * T + tid;
+  t.s.x_ = t.s.rhs_ + (size_t)n * T;
+  t.s.xold_ = t.s.x_ + (size_t)n * T;
+  t.s.col_ = t.s.xold_ + (size_t)n * T;
+  t.s.piv_ = reinterpret_cast<int*>(base + (size_t)(n * n + 4 * n) * T) + tid;
+  t.s.L_ = reinterpret_cast<float*>(base + (size_t)(n * n + 4 * n) * T + ((size_t)n * T + 1) / 2) + tid;
+  t.prog.el = el; t.prog.isv = isv; t.prog.ne = ne; t.prog.n_nodes = plan.n_nodes; t.prog.n_state = plan.n_state;
+  t.prog.nonlin_empty = plan.n_nonlin == 0;
 }
 
-// Point a thread's SoA columns at circuit c (persistent kernels move a thread
-// from circuit to circuit).
-template <int T>
-__device__ inline void thr_bind(Thr<T>& t, const double* values, const double* derived, double* state, double* work,
-                                int64_t B, int64_t c) {
-  const int n = t.n;
-  t.V = Col{const_cast<double*>(values) + c, B};
-  t.D = Col{const_cast<double*>(derived) + c, B};
-  t.Sb = Col{state + c, B};
-  t.save = Col{work + c, B};
-  t.ptPrev = Col{work + (int64_t)n * B + c, B};
-  t.xacc = Col{work + (int64_t)2 * n * B + c, B};
+// Per-topology kernels with a shared-memory system of compile-time size N: the
+// same per-thread layout without the element table.
+template <int T, int N>
+__device__ inline void smem_layout_static(SmemSys<T, N>& s, unsigned char* smem) {
+  double* base = reinterpret_cast<double*>(smem);
+  const int tid = threadIdx.x;
+  s.n_ = N;
+  s.A_ = base + tid;
+  s.rhs_ = base + N * N * T + tid;
+  s.x_ = s.rhs_ + N * T;
+  s.xold_ = s.x_ + N * T;
+  s.col_ = s.xold_ + N * T;
+  s.piv_ = reinterpret_cast<int*>(base + (N * N + 4 * N) * T) + tid;
+  s.L_ = reinterpret_cast<float*>(base + (N * N + 4 * N) * T + (N * T + 1) / 2) + tid;
 }
 
-// Bytes of dynamic shared memory thr_init lays out.
+#ifndef __CUDACC_RTC__
+// Bytes of dynamic shared memory smem_layout lays out (ne = 0: smem_layout_static).
 inline size_t thr_smem(int n, int ne, int T) {
-  size_t off = (size_t)ne * sizeof(KElem) + ((n + 15) / 16) * 16;
+  size_t off = ne ? (size_t)ne * sizeof(KElem) + ((n + 15) / 16) * 16 : 0;
   size_t per = (size_t)(n * n + 4 * n) * 8 + (size_t)n * 4 + 8 + (size_t)n * n * 4 + 8;
   return off + per * T;
 }
+#endif
 
-template <int T>
-__device__ inline void op_state_reset(OpState& st, const KOpts& o) {
+__device__ __forceinline__ void op_state_reset(OpState& st, const KOpts& o) {
   st.phase = PH_MAIN; st.it = 0; st.maxIter = o.itl1; st.total = 0; st.firstErr = 0; st.status = KS_STATUS_NOT_RUN;
   st.nsteps = 0; st.quiet = 0; st.ok = false; st.srcStepping = false; st.fp64 = !o.mixed; st.initJct = true;
   st.diagGmin = 0; st.g = 0; st.factor = 0; st.srcFact = 0; st.done = 0; st.step = 0; st.ptG = 0; st.h = 0;
@@ -101,33 +108,38 @@ __device__ inline void op_state_reset(OpState& st, const KOpts& o) {
 
 // One (*Sim).solve: stamp at x (copied to xold), add the gmin-stepping and
 // pseudo-transient diagonals, solve.  Returns 0 or the solver error.
-template <int T>
-__device__ inline int solve_once(Thr<T>& t, OpState& st, LoadParams lp) {
-  ThreadSys<T>& s = t.s;
-  const int n = t.n;
-  for (int i = 0; i < n; i++) s.xold[i * T] = s.x[i * T];
+template <class SY, class P>
+__device__ inline int solve_once(Thr<SY, P>& t, OpState& st, LoadParams lp) {
+  SY& s = t.s;
+  const int n = t.n();
+#pragma unroll
+  for (int i = 0; i < n; i++) s.xo(i) = s.xn(i);
   lp.initJct = st.initJct;
   lp.gmin = t.o.gmin;
   lp.srcStepping = st.srcStepping;
   lp.srcFact = st.srcFact;
-  load_all<T>(t.el, t.ne, t.V, t.D, t.Sb, s, lp);
+  load_all(t.prog, t.V, t.D, t.Sb, s, lp);
   if (st.ptG > 0) {
+#pragma unroll
     for (int i = 0; i < n; i++) {
       double pv = t.ptPrev[i];
-      if (t.isv[i]) { s.a(i, i) += st.ptG; s.rhs[i * T] += st.ptG * pv; }
-      else { s.a(i, i) -= st.ptG; s.rhs[i * T] -= st.ptG * pv; }
+      if (t.prog.is_v(i)) { s.a(i, i) += st.ptG; s.rhs(i) += st.ptG * pv; }
+      else { s.a(i, i) -= st.ptG; s.rhs(i) -= st.ptG * pv; }
     }
   }
-  if (st.diagGmin > 0) for (int i = 0; i < n; i++) if (t.isv[i]) s.a(i, i) += st.diagGmin;
+  if (st.diagGmin > 0) {
+#pragma unroll
+    for (int i = 0; i < n; i++) if (t.prog.is_v(i)) s.a(i, i) += st.diagGmin;
+  }
   int err;
   if (!st.fp64) {
-    err = lu_solve_mixed<T>(s);
+    err = lu_solve_mixed(s);
     if (err == SOLVE_FP32_FAIL) {  // the FP64 path takes over this circuit
       st.fp64 = true;
-      err = lu_solve_fp64<T>(s, s.rhs, s.x);
+      err = lu_solve_fp64(s);
     }
   } else {
-    err = lu_solve_fp64<T>(s, s.rhs, s.x);
+    err = lu_solve_fp64(s);
   }
   st.total++;
   return err;
@@ -135,14 +147,14 @@ __device__ inline int solve_once(Thr<T>& t, OpState& st, LoadParams lp) {
 
 // One Newton iteration: a solve plus the bookkeeping of analysis/newton.go:36-57.
 // Returns -1 while the current newton() call goes on, else its result.
-template <int T>
-__device__ inline int newton_step(Thr<T>& t, OpState& st, const LoadParams& lp) {
-  int err = solve_once<T>(t, st, lp);
+template <class SY, class P>
+__device__ inline int newton_step(Thr<SY, P>& t, OpState& st, const LoadParams& lp) {
+  int err = solve_once(t, st, lp);
   int res = -1;
   if (err) res = err;
-  else if (t.nonlinEmpty) res = KS_STATUS_OK;
+  else if (t.prog.nonlin_empty) res = KS_STATUS_OK;
   else if (st.initJct) st.initJct = false;
-  else if (converged<T>(t.el, t.ne, t.isv, t.V, t.D, t.Sb, t.s, t.o, t.o.gmin)) res = KS_STATUS_OK;
+  else if (converged(t.prog, t.V, t.D, t.Sb, t.s, t.o, t.o.gmin)) res = KS_STATUS_OK;
   if (res < 0) {
     st.it++;
     if (st.it < st.maxIter) return -1;
@@ -152,37 +164,55 @@ __device__ inline int newton_step(Thr<T>& t, OpState& st, const LoadParams& lp) 
   return res;
 }
 
+template <class SY, class P>
+__device__ __forceinline__ void x_from_col(Thr<SY, P>& t, const Col& c) {
+#pragma unroll
+  for (int i = 0; i < t.n(); i++) t.s.xn(i) = c[i];
+}
+template <class SY, class P>
+__device__ __forceinline__ void x_to_col(Thr<SY, P>& t, const Col& c) {
+#pragma unroll
+  for (int i = 0; i < t.n(); i++) c[i] = t.s.xn(i);
+}
+template <class SY, class P>
+__device__ __forceinline__ void x_zero(Thr<SY, P>& t, const Col& also) {
+#pragma unroll
+  for (int i = 0; i < t.n(); i++) { t.s.xn(i) = 0.0; also[i] = 0.0; }
+}
+
 // dcSolve start, analysis/newton.go:96-102, with applyNodeSet (:221-243) when x0
 // holds a starting point (node voltages; other unknowns start at 0).
-template <int T>
-__device__ inline void dc_start(Thr<T>& t, OpState& st, const double* x0, int64_t c, int mode) {
-  op_state_reset<T>(st, t.o);
-  for (int i = 0; i < t.n; i++) t.s.x[i * T] = 0.0;
+template <class SY, class P>
+__device__ inline void dc_start(Thr<SY, P>& t, OpState& st, const double* x0, int64_t c) {
+  op_state_reset(st, t.o);
+  const int n = t.n();
+#pragma unroll
+  for (int i = 0; i < n; i++) t.s.xn(i) = 0.0;
   if (x0) {
-    for (int i = 0; i < t.n_nodes - 1; i++) t.s.x[i * T] = x0[c * t.n + i];
-    accept_all<T>(t.el, t.ne, t.V, t.D, t.Sb, t.s.x, 0.0, ModeOP, t.o.gmin, true);
+#pragma unroll
+    for (int i = 0; i < n; i++)
+      if (i < t.prog.n_nodes - 1) t.s.xn(i) = x0[c * n + i];
+    accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, ModeOP, t.o.gmin, true);
     st.initJct = false;
   }
-  (void)mode;
 }
 
 // Advance dcSolve with the result of a finished newton() call.  Sets st.phase to
 // PH_DONE and st.status when the DC solve is over.
-template <int T>
-__device__ inline void dc_advance(Thr<T>& t, OpState& st, int res) {
+template <class SY, class P>
+__device__ inline void dc_advance(Thr<SY, P>& t, OpState& st, int res) {
   const KOpts& o = t.o;
-  ThreadSys<T>& s = t.s;
-  const int n = t.n;
+  const int n = t.n();
   bool advance = true;
   while (advance) {
     advance = false;
     switch (st.phase) {
       case PH_MAIN:
-        if (res == KS_STATUS_OK || t.nonlinEmpty || !retryable(res)) { st.status = res; st.phase = PH_DONE; break; }
+        if (res == KS_STATUS_OK || t.prog.nonlin_empty || !retryable(res)) { st.status = res; st.phase = PH_DONE; break; }
         st.firstErr = res;
         st.phase = PH_GMIN;
         if (!o.no_gmin) {  // gminStepping start, :134-142
-          for (int i = 0; i < n; i++) { s.x[i * T] = 0.0; t.save[i] = 0.0; }
+          x_zero(t, t.save);
           st.initJct = true; st.g = 1e-2; st.factor = 10.0; st.ok = false; st.nsteps = 0;
           st.diagGmin = st.g;
         } else { st.nsteps = -1; res = KS_STATUS_NO_CONVERGENCE; advance = true; }
@@ -191,7 +221,7 @@ __device__ inline void dc_advance(Thr<T>& t, OpState& st, int res) {
         bool fail = false;
         if (st.nsteps < 0) fail = true;
         else if (res == KS_STATUS_OK) {
-          for (int i = 0; i < n; i++) t.save[i] = s.x[i * T];
+          x_to_col(t, t.save);
           if (st.g == 0) { st.diagGmin = 0; st.status = KS_STATUS_OK; st.phase = PH_DONE; break; }
           st.ok = true;
           st.factor = fmin(st.factor * sqrt(st.factor), 10.0);
@@ -200,7 +230,7 @@ __device__ inline void dc_advance(Thr<T>& t, OpState& st, int res) {
         } else if (!retryable(res) || !st.ok) {
           fail = true;
         } else {
-          for (int i = 0; i < n; i++) s.x[i * T] = t.save[i];
+          x_from_col(t, t.save);
           double prev = st.g == 0 ? o.gmin : st.g * st.factor;
           st.factor = sqrt(st.factor);
           if (st.factor < 1.00005) fail = true;
@@ -211,7 +241,7 @@ __device__ inline void dc_advance(Thr<T>& t, OpState& st, int res) {
           st.diagGmin = 0;
           if (!o.no_source) {  // sourceStepping start, :180-192
             st.phase = PH_SRC_INIT;
-            for (int i = 0; i < n; i++) { s.x[i * T] = 0.0; t.save[i] = 0.0; }
+            x_zero(t, t.save);
             st.srcStepping = true; st.done = 0; st.step = 0.1; st.srcFact = 0; st.nsteps = 0;
           } else { st.phase = PH_SRC; st.nsteps = -1; res = KS_STATUS_NO_CONVERGENCE; advance = true; }
         }
@@ -219,7 +249,7 @@ __device__ inline void dc_advance(Thr<T>& t, OpState& st, int res) {
       }
       case PH_SRC_INIT:
         if (res != KS_STATUS_OK) { st.phase = PH_SRC; st.nsteps = -1; advance = true; break; }
-        for (int i = 0; i < n; i++) t.save[i] = s.x[i * T];
+        x_to_col(t, t.save);
         st.phase = PH_SRC;
         st.srcFact = fmin(st.done + st.step, 1.0);
         break;
@@ -228,12 +258,12 @@ __device__ inline void dc_advance(Thr<T>& t, OpState& st, int res) {
         if (st.nsteps < 0) fail = true;
         else if (res == KS_STATUS_OK) {
           if (st.srcFact == 1) { st.srcStepping = false; st.srcFact = 0; st.status = KS_STATUS_OK; st.phase = PH_DONE; break; }
-          for (int i = 0; i < n; i++) t.save[i] = s.x[i * T];
+          x_to_col(t, t.save);
           st.done = st.srcFact; st.step = fmin(st.step * 1.5, 0.5);
           if (++st.nsteps >= 1000) fail = true;
         } else if (!retryable(res)) fail = true;
         else {
-          for (int i = 0; i < n; i++) s.x[i * T] = t.save[i];
+          x_from_col(t, t.save);
           st.step /= 2;
           if (st.step < 1e-3) fail = true;
           else if (++st.nsteps >= 1000) fail = true;
@@ -242,7 +272,7 @@ __device__ inline void dc_advance(Thr<T>& t, OpState& st, int res) {
           st.srcStepping = false; st.srcFact = 0;
           if (!o.no_pt) {  // pseudoTransient start, :260-273
             st.phase = PH_PT;
-            for (int i = 0; i < n; i++) { s.x[i * T] = 0.0; t.ptPrev[i] = 0.0; }
+            x_zero(t, t.ptPrev);
             st.initJct = true; st.h = 1e-6; st.quiet = 0; st.nsteps = 0; st.ptG = 1 / st.h;
           } else { st.status = st.firstErr; st.phase = PH_DONE; }
         } else st.srcFact = fmin(st.done + st.step, 1.0);
@@ -253,18 +283,19 @@ __device__ inline void dc_advance(Thr<T>& t, OpState& st, int res) {
         if (res != KS_STATUS_OK) {
           if (!retryable(res)) fail = true;
           else {
-            for (int i = 0; i < n; i++) s.x[i * T] = t.ptPrev[i];
+            x_from_col(t, t.ptPrev);
             st.h /= 4;
             if (st.h < 1e-15) fail = true;
           }
         } else {
           bool moved = false;
+#pragma unroll
           for (int i = 0; i < n; i++) {
-            double xv = s.x[i * T];
-            double tol = t.isv[i] ? o.vntol : o.abstol;
-            if (fabs(xv - t.ptPrev[i]) > o.reltol * fabs(xv) + tol) { moved = true; break; }
+            double xv = t.s.xn(i);
+            double tol = t.prog.is_v(i) ? o.vntol : o.abstol;
+            moved |= fabs(xv - t.ptPrev[i]) > o.reltol * fabs(xv) + tol;
           }
-          for (int i = 0; i < n; i++) t.ptPrev[i] = s.x[i * T];
+          x_to_col(t, t.ptPrev);
           st.quiet = moved ? 0 : st.quiet + 1;
           if (st.quiet >= 3 && st.h >= 1e6) { st.ptG = 0; st.phase = PH_PT_FINAL; break; }
           st.h = fmin(st.h * 2, 1e12);
@@ -279,6 +310,51 @@ __device__ inline void dc_advance(Thr<T>& t, OpState& st, int res) {
         st.phase = PH_DONE;
         break;
       default: break;
+    }
+  }
+}
+
+// The operating point of one circuit after another, pulled from the queue.
+template <class SY, class P>
+__device__ inline void op_persistent(Thr<SY, P>& t, const double* values, const double* derived, double* state,
+                                     double* work, int64_t B, const double* x0, double* out_x, int32_t* out_status,
+                                     int32_t* out_iters, uint64_t deadline_ns, unsigned long long* queue) {
+  const uint64_t t0 = deadline_ns ? globaltimer_ns() : 0;
+  const KOpts& o = t.o;
+  const int maxTotal = o.max_iter_total > 0 ? o.max_iter_total : 3300 * o.itl1 + 16;
+  const int n = t.n();
+  LoadParams lp;
+  lp.mode = ModeOP; lp.method = BE; lp.time = 0; lp.h = 0; lp.initJct = false; lp.gmin = o.gmin;
+  lp.srcStepping = false; lp.srcFact = 0;
+  OpState st;
+  int64_t c = (int64_t)atomicAdd(queue, 1ull);
+  if (c < B) {
+    thr_bind(t, values, derived, state, work, B, c);
+    init_state(t.prog, t.D, t.Sb);
+    dc_start(t, st, x0, c);
+  }
+  while (c < B) {
+    bool done = false;
+    if (deadline_ns && globaltimer_ns() - t0 > deadline_ns) { st.status = KS_STATUS_INTERRUPTED; done = true; }
+    else if (st.total >= maxTotal) { st.status = KS_STATUS_NO_CONVERGENCE; done = true; }
+    else {
+      int res = newton_step(t, st, lp);
+      if (res >= 0) dc_advance(t, st, res);
+      done = st.phase == PH_DONE;
+    }
+    if (!done) continue;
+    if (st.status == KS_STATUS_OK) accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, ModeOP, o.gmin, false);
+    if (out_x) {
+#pragma unroll
+      for (int i = 0; i < n; i++) out_x[c * n + i] = t.s.xn(i);
+    }
+    if (out_status) out_status[c] = st.status;
+    if (out_iters) out_iters[c] = st.total;
+    c = (int64_t)atomicAdd(queue, 1ull);
+    if (c < B) {
+      thr_bind(t, values, derived, state, work, B, c);
+      init_state(t.prog, t.D, t.Sb);
+      dc_start(t, st, x0, c);
     }
   }
 }

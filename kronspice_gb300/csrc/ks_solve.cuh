@@ -1,5 +1,12 @@
-// ks_solve.cuh — per-thread element program, dense LU and Newton bookkeeping shared by
-// the operating-point and transient kernels of the GB300 engine.
+// ks_solve.cuh — the per-thread linear system, element dispatch and dense LU of the
+// GB300 engine, shared by the generic kernels and the per-topology kernels.
+//
+// A thread's system S lives either in shared memory (SmemSys: one column per
+// thread, stride T; runtime or compile-time size) or in registers (RegSys:
+// compile-time size, every index a constant after unrolling).  The element
+// program P is either the runtime table of a plan (RtProg, interpreted) or a
+// generated list of constant elements (per-topology kernels), so the same device
+// code becomes straight-line code with constant matrix positions.
 #pragma once
 #include "ks_devices.cuh"
 #include "ks_mos.cuh"
@@ -8,163 +15,267 @@ namespace ksg {
 
 enum { SOLVE_OK = 0, SOLVE_SINGULAR = KS_STATUS_SINGULAR, SOLVE_NONFINITE = KS_STATUS_NONFINITE, SOLVE_FP32_FAIL = 99 };
 
-// Per-thread views into the block's shared memory (stride T between entries).
-template <int T>
-struct ThreadSys {
-  double* A;     // n*n   stamped matrix (FP64)
-  double* rhs;   // n
-  double* x;     // n     new iterate
-  double* xold;  // n     linearization point
-  double* col;   // n     column maxima
-  int* piv;      // n
-  float* L32;    // n*n   FP32 factor (mixed precision only)
-  int n;
-  __device__ __forceinline__ double& a(int i, int j) const { return A[(i * n + j) * T]; }
-  __device__ __forceinline__ float& l(int i, int j) const { return L32[(i * n + j) * T]; }
+// Shared-memory system with stride T; N = 0: size known at run time.
+template <int T, int N = 0>
+struct SmemSys {
+  static constexpr bool kStatic = N > 0;
+  static constexpr int kN = N;
+  double *A_, *rhs_, *x_, *xold_, *col_;
+  int* piv_;
+  float* L_;
+  int n_;
+  __device__ __forceinline__ int size() const { return N > 0 ? N : n_; }
+  __device__ __forceinline__ double& a(int i, int j) { return A_[(i * size() + j) * T]; }
+  __device__ __forceinline__ double& rhs(int i) { return rhs_[i * T]; }
+  __device__ __forceinline__ double& xn(int i) { return x_[i * T]; }
+  __device__ __forceinline__ double& xo(int i) { return xold_[i * T]; }
+  __device__ __forceinline__ double& col(int i) { return col_[i * T]; }
+  __device__ __forceinline__ int& piv(int i) { return piv_[i * T]; }
+  __device__ __forceinline__ float& l(int i, int j) { return L_[(i * size() + j) * T]; }
 };
 
-// Stamp every element at xold (analysis/op.go:289-322 without the solve).
-template <int T>
-__device__ inline void load_all(const KElem* el, int n_elem, const Col& Vb, const Col& Db, const Col& Sb,
-                                const ThreadSys<T>& s, const LoadParams& lp) {
-  int n = s.n;
-  for (int i = 0; i < n * n; i++) s.A[i * T] = 0.0;
-  for (int i = 0; i < n; i++) s.rhs[i * T] = 0.0;
-  SysRef<T> sys{s.A, s.rhs, s.xold, n};
-  for (int k = 0; k < n_elem; k++) {
-    const KElem& e = el[k];
-    Col S{Sb.p + (int64_t)e.state * Sb.B, Sb.B};
-    switch (e.kind) {
-      case KS_ELEM_R: {  // device/passive.go:72-84
-        double g = Db[e.derived + DR_G];
-        int a = e.u[0], b = e.u[1];
-        sys.add(a, a, g); sys.add(b, b, g); sys.add(a, b, -g); sys.add(b, a, -g);
+// Register system of compile-time size N.
+template <int N>
+struct RegSys {
+  static constexpr bool kStatic = true;
+  static constexpr int kN = N;
+  double A_[N * N], rhs_[N], x_[N], xold_[N], col_[N];
+  int piv_[N];
+  float L_[N * N];
+  __device__ __forceinline__ static constexpr int size() { return N; }
+  __device__ __forceinline__ double& a(int i, int j) { return A_[i * N + j]; }
+  __device__ __forceinline__ double& rhs(int i) { return rhs_[i]; }
+  __device__ __forceinline__ double& xn(int i) { return x_[i]; }
+  __device__ __forceinline__ double& xo(int i) { return xold_[i]; }
+  __device__ __forceinline__ double& col(int i) { return col_[i]; }
+  __device__ __forceinline__ int& piv(int i) { return piv_[i]; }
+  __device__ __forceinline__ float& l(int i, int j) { return L_[i * N + j]; }
+};
+
+// The runtime element program of a plan (element table in shared memory).
+struct RtProg {
+  const KElem* el;
+  const int8_t* isv;
+  int ne, n_nodes, n_state;
+  bool nonlin_empty;
+  template <class F>
+  __device__ __forceinline__ void each(F&& f) const { for (int k = 0; k < ne; k++) f(el[k]); }
+  __device__ __forceinline__ bool is_v(int i) const { return isv[i] != 0; }
+};
+
+__device__ __forceinline__ Col state_col(const Col& Sb, const KElem& e) { return Col{Sb.p + (int64_t)e.state * Sb.B, Sb.B}; }
+
+__device__ __forceinline__ int lim_slot(int kind) {
+  return kind == KS_ELEM_D ? SD_LIM : kind == KS_ELEM_Q ? SQ_LIM : kind == KS_ELEM_M ? SM_LIM : -1;
+}
+
+// Stamp one element at the linearization point (the element's Load).
+template <class SY>
+__device__ __forceinline__ void elem_load(const KElem& e, const Col& Vb, const Col& Db, const Col& Sb, SY& sys,
+                                          const LoadParams& lp) {
+  Col S = state_col(Sb, e);
+  switch (e.kind) {
+    case KS_ELEM_R: {  // device/passive.go:72-84
+      double g = Db[e.derived + DR_G];
+      int a = e.u[0], b = e.u[1];
+      sadd(sys, a, a, g); sadd(sys, b, b, g); sadd(sys, a, b, -g); sadd(sys, b, a, -g);
+      break;
+    }
+    case KS_ELEM_C: {  // device/reactive.go:60-106
+      int a = e.u[0], b = e.u[1];
+      if (lp.mode == ModeOP || lp.mode == ModeTranOP) { S[SC_TRAN] = 0; S[SC_GEQ] = 0; S[SC_IHIST] = 0; break; }
+      if (lp.mode == ModeUICInit) {
+        double g = 1e9, vp = S[SC_VPREV];
+        sadd(sys, a, a, g); sadd(sys, b, b, g); sadd(sys, a, b, -g); sadd(sys, b, a, -g);
+        srhs(sys, a, g * vp); srhs(sys, b, -g * vp);
+        S[SC_TRAN] = 0; S[SC_GEQ] = 0; S[SC_IHIST] = 0;
         break;
       }
-      case KS_ELEM_C: {  // device/reactive.go:60-106
-        int a = e.u[0], b = e.u[1];
-        if (lp.mode == ModeOP || lp.mode == ModeTranOP) { S[SC_TRAN] = 0; S[SC_GEQ] = 0; S[SC_IHIST] = 0; break; }
-        if (lp.mode == ModeUICInit) {
-          double g = 1e9, vp = S[SC_VPREV];
-          sys.add(a, a, g); sys.add(b, b, g); sys.add(a, b, -g); sys.add(b, a, -g);
-          sys.addRHS(a, g * vp); sys.addRHS(b, -g * vp);
-          S[SC_TRAN] = 0; S[SC_GEQ] = 0; S[SC_IHIST] = 0;
-          break;
-        }
-        double C = Vb[e.param + KS_RCL_P_VALUE], geq, ih;
-        if (lp.method == TRAP) { geq = 2 * C / lp.h; ih = -(geq * S[SC_VPREV] + S[SC_IPREV]); }
-        else { geq = C / lp.h; ih = -geq * S[SC_VPREV]; }
-        S[SC_TRAN] = 1; S[SC_GEQ] = geq; S[SC_IHIST] = ih;
-        sys.add(a, a, geq); sys.add(b, b, geq); sys.add(a, b, -geq); sys.add(b, a, -geq);
-        sys.addRHS(a, -ih); sys.addRHS(b, ih);
-        break;
-      }
-      case KS_ELEM_L: {  // device/reactive.go:230-259
-        int a = e.u[0], b = e.u[1], kk = e.u[2];
-        sys.add(a, kk, 1); sys.add(b, kk, -1);
-        if (lp.mode == ModeOP || lp.mode == ModeTranOP) { sys.add(kk, a, 1); sys.add(kk, b, -1); break; }
-        if (lp.mode == ModeUICInit) { sys.add(kk, kk, 1); sys.addRHS(kk, S[SL_IPREV]); break; }
-        double L = Vb[e.param + KS_RCL_P_VALUE];
-        double req = L / lp.h, r = -req * S[SL_IPREV];
-        if (lp.method == TRAP) { req = 2 * L / lp.h; r = -req * S[SL_IPREV] - S[SL_VPREV]; }
-        sys.add(kk, a, 1); sys.add(kk, b, -1); sys.add(kk, kk, -req);
-        sys.addRHS(kk, r);
-        break;
-      }
-      case KS_ELEM_V: {  // device/source.go:102-112
-        Col D{Db.p, Db.B};
-        double v = source_at(e, Vb, D, S, lp);
-        S[SV_VALUE] = v;
-        int a = e.u[0], b = e.u[1], kk = e.u[2];
-        sys.add(a, kk, 1); sys.add(b, kk, -1); sys.add(kk, a, 1); sys.add(kk, b, -1);
-        sys.addRHS(kk, v);
-        break;
-      }
-      case KS_ELEM_I: {  // device/source.go:155-160
-        double v = source_at(e, Vb, Db, S, lp);
-        S[SV_VALUE] = v;
-        sys.addRHS(e.u[0], -v); sys.addRHS(e.u[1], v);
-        break;
-      }
-      case KS_ELEM_D: diode_load<T>(e, Vb, Db, S, sys, lp); break;
-      case KS_ELEM_Q: bjt_load<T>(e, Vb, Db, S, sys, lp); break;
-      case KS_ELEM_M: mos_load<T>(e, Vb, Db, S, sys, lp); break;
+      double C = Vb[e.param + KS_RCL_P_VALUE], geq, ih;
+      if (lp.method == TRAP) { geq = 2 * C / lp.h; ih = -(geq * S[SC_VPREV] + S[SC_IPREV]); }
+      else { geq = C / lp.h; ih = -geq * S[SC_VPREV]; }
+      S[SC_TRAN] = 1; S[SC_GEQ] = geq; S[SC_IHIST] = ih;
+      sadd(sys, a, a, geq); sadd(sys, b, b, geq); sadd(sys, a, b, -geq); sadd(sys, b, a, -geq);
+      srhs(sys, a, -ih); srhs(sys, b, ih);
+      break;
+    }
+    case KS_ELEM_L: {  // device/reactive.go:230-259
+      int a = e.u[0], b = e.u[1], kk = e.u[2];
+      sadd(sys, a, kk, 1); sadd(sys, b, kk, -1);
+      if (lp.mode == ModeOP || lp.mode == ModeTranOP) { sadd(sys, kk, a, 1); sadd(sys, kk, b, -1); break; }
+      if (lp.mode == ModeUICInit) { sadd(sys, kk, kk, 1); srhs(sys, kk, S[SL_IPREV]); break; }
+      double L = Vb[e.param + KS_RCL_P_VALUE];
+      double req = L / lp.h, r = -req * S[SL_IPREV];
+      if (lp.method == TRAP) { req = 2 * L / lp.h; r = -req * S[SL_IPREV] - S[SL_VPREV]; }
+      sadd(sys, kk, a, 1); sadd(sys, kk, b, -1); sadd(sys, kk, kk, -req);
+      srhs(sys, kk, r);
+      break;
+    }
+    case KS_ELEM_V: {  // device/source.go:102-112
+      double v = source_at(e, Vb, Db, S, lp);
+      S[SV_VALUE] = v;
+      int a = e.u[0], b = e.u[1], kk = e.u[2];
+      sadd(sys, a, kk, 1); sadd(sys, b, kk, -1); sadd(sys, kk, a, 1); sadd(sys, kk, b, -1);
+      srhs(sys, kk, v);
+      break;
+    }
+    case KS_ELEM_I: {  // device/source.go:155-160
+      double v = source_at(e, Vb, Db, S, lp);
+      S[SV_VALUE] = v;
+      srhs(sys, e.u[0], -v); srhs(sys, e.u[1], v);
+      break;
+    }
+    case KS_ELEM_D: diode_load(e, Vb, Db, S, sys, lp); break;
+    case KS_ELEM_Q: bjt_load(e, Vb, Db, S, sys, lp); break;
+    case KS_ELEM_M: mos_load(e, Vb, Db, S, sys, lp); break;
+  }
+}
+
+// Stamp every element (analysis/op.go:289-322 without the solve).
+template <class SY, class P>
+__device__ __forceinline__ void load_all(const P& prog, const Col& Vb, const Col& Db, const Col& Sb, SY& s,
+                                         const LoadParams& lp) {
+  const int n = s.size();
+#pragma unroll
+  for (int i = 0; i < n; i++) {
+#pragma unroll
+    for (int j = 0; j < n; j++) s.a(i, j) = 0.0;
+    s.rhs(i) = 0.0;
+  }
+  prog.each([&](const KElem& e) { elem_load(e, Vb, Db, Sb, s, lp); });
+}
+
+// Swap rows k and p (static systems compare p against every later row, so every
+// register index stays a constant).
+template <class SY>
+__device__ __forceinline__ void swap_rows(SY& s, int k, int p) {
+  const int n = s.size();
+  if constexpr (SY::kStatic) {
+#pragma unroll
+    for (int i = 0; i < n; i++)
+      if (i > k && i == p)
+#pragma unroll
+        for (int j = 0; j < n; j++) { double t = s.a(k, j); s.a(k, j) = s.a(i, j); s.a(i, j) = t; }
+  } else if (p != k) {
+    for (int j = 0; j < n; j++) { double t = s.a(k, j); s.a(k, j) = s.a(p, j); s.a(p, j) = t; }
+  }
+}
+template <class SY>
+__device__ __forceinline__ void swap_rows32(SY& s, int k, int p) {
+  const int n = s.size();
+  if constexpr (SY::kStatic) {
+#pragma unroll
+    for (int i = 0; i < n; i++)
+      if (i > k && i == p)
+#pragma unroll
+        for (int j = 0; j < n; j++) { float t = s.l(k, j); s.l(k, j) = s.l(i, j); s.l(i, j) = t; }
+  } else if (p != k) {
+    for (int j = 0; j < n; j++) { float t = s.l(k, j); s.l(k, j) = s.l(p, j); s.l(p, j) = t; }
+  }
+}
+// y <- P y with the recorded pivots (y given as an accessor).
+template <class SY, class Y>
+__device__ __forceinline__ void permute(SY& s, Y&& y) {
+  const int n = s.size();
+#pragma unroll
+  for (int k = 0; k < n; k++) {
+    int p = s.piv(k);
+    if constexpr (SY::kStatic) {
+#pragma unroll
+      for (int i = 0; i < n; i++)
+        if (i > k && i == p) { double t = y(k); y(k) = y(i); y(i) = t; }
+    } else if (p != k) {
+      double t = y(k); y(k) = y(p); y(p) = t;
     }
   }
 }
 
-// Dense LU with partial pivoting in FP64, solver/dense.go:80-177; A is factored in place.
-template <int T>
-__device__ inline int lu_solve_fp64(const ThreadSys<T>& s, const double* b, double* out) {
-  int n = s.n;
+// Dense LU with partial pivoting in FP64, solver/dense.go:80-177; A is factored in
+// place and x = A^-1 rhs.
+template <class SY>
+__device__ inline int lu_solve_fp64(SY& s) {
+  const int n = s.size();
   double scale = 0;
-  for (int i = 0; i < n * n; i++) {
-    double v = s.A[i * T];
-    if (!isfinite(v)) return SOLVE_NONFINITE;
-    scale = fmax(scale, fabs(v));
-  }
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < n; i++)
+#pragma unroll
+    for (int j = 0; j < n; j++) {
+      double v = s.a(i, j);
+      bad |= !isfinite(v);
+      scale = fmax(scale, fabs(v));
+    }
+  if (bad) return SOLVE_NONFINITE;
   if (scale == 0) return SOLVE_SINGULAR;
+#pragma unroll
   for (int j = 0; j < n; j++) {
     double m = 0;
+#pragma unroll
     for (int i = 0; i < n; i++) m = fmax(m, fabs(s.a(i, j)));
-    s.col[j * T] = m;
+    s.col(j) = m;
   }
+#pragma unroll
   for (int k = 0; k < n; k++) {
     int p = k;
     double maxv = fabs(s.a(k, k));
+#pragma unroll
     for (int i = k + 1; i < n; i++) {
       double v = fabs(s.a(i, k));
       if (v > maxv) { maxv = v; p = i; }
     }
-    if (maxv <= s.col[k * T] * double(n) * 1e-14) return SOLVE_SINGULAR;
-    s.piv[k * T] = p;
-    if (p != k)
-      for (int j = 0; j < n; j++) { double t = s.a(k, j); s.a(k, j) = s.a(p, j); s.a(p, j) = t; }
+    if (maxv <= s.col(k) * double(n) * 1e-14) return SOLVE_SINGULAR;
+    s.piv(k) = p;
+    swap_rows(s, k, p);
     double pivot = s.a(k, k);
+#pragma unroll
     for (int i = k + 1; i < n; i++) {
       double f = s.a(i, k) / pivot;
       s.a(i, k) = f;
-      if (f == 0) continue;
+#pragma unroll
       for (int j = k + 1; j < n; j++) s.a(i, j) -= f * s.a(k, j);
     }
   }
-  // y = P b in `out`, then forward (unit lower) and back substitution.
-  for (int i = 0; i < n; i++) out[i * T] = b[i * T];
-  for (int k = 0; k < n; k++) {
-    int p = s.piv[k * T];
-    if (p != k) { double t = out[k * T]; out[k * T] = out[p * T]; out[p * T] = t; }
-  }
+#pragma unroll
+  for (int i = 0; i < n; i++) s.xn(i) = s.rhs(i);
+  permute(s, [&](int i) -> double& { return s.xn(i); });
+#pragma unroll
   for (int i = 0; i < n; i++) {
-    double acc = out[i * T];
-    for (int j = 0; j < i; j++) acc -= s.a(i, j) * out[j * T];
-    out[i * T] = acc;
+    double acc = s.xn(i);
+#pragma unroll
+    for (int j = 0; j < i; j++) acc -= s.a(i, j) * s.xn(j);
+    s.xn(i) = acc;
   }
+#pragma unroll
   for (int i = n - 1; i >= 0; i--) {
-    double acc = out[i * T];
-    for (int j = i + 1; j < n; j++) acc -= s.a(i, j) * out[j * T];
-    out[i * T] = acc / s.a(i, i);
+    double acc = s.xn(i);
+#pragma unroll
+    for (int j = i + 1; j < n; j++) acc -= s.a(i, j) * s.xn(j);
+    s.xn(i) = acc / s.a(i, i);
   }
-  for (int i = 0; i < n; i++) if (!isfinite(out[i * T])) return SOLVE_NONFINITE;
-  return SOLVE_OK;
+  bool nf = false;
+#pragma unroll
+  for (int i = 0; i < n; i++) nf |= !isfinite(s.xn(i));
+  return nf ? SOLVE_NONFINITE : SOLVE_OK;
 }
 
-// FP32 forward/back substitution with the factor in L32: y (FP64 in/out, in place).
-template <int T>
-__device__ inline void lu32_apply(const ThreadSys<T>& s, double* y) {
-  const int n = s.n;
-  for (int k = 0; k < n; k++) {
-    int p = s.piv[k * T];
-    if (p != k) { double t = y[k * T]; y[k * T] = y[p * T]; y[p * T] = t; }
-  }
+// FP32 forward/back substitution with the factor in L32, in place on col().
+template <class SY>
+__device__ __forceinline__ void lu32_apply_col(SY& s) {
+  const int n = s.size();
+  permute(s, [&](int i) -> double& { return s.col(i); });
+#pragma unroll
   for (int i = 0; i < n; i++) {
-    float acc = (float)y[i * T];
-    for (int j = 0; j < i; j++) acc = fmaf(-s.l(i, j), (float)y[j * T], acc);
-    y[i * T] = acc;
+    float acc = (float)s.col(i);
+#pragma unroll
+    for (int j = 0; j < i; j++) acc = fmaf(-s.l(i, j), (float)s.col(j), acc);
+    s.col(i) = acc;
   }
+#pragma unroll
   for (int i = n - 1; i >= 0; i--) {
-    float acc = (float)y[i * T];
-    for (int j = i + 1; j < n; j++) acc = fmaf(-s.l(i, j), (float)y[j * T], acc);
-    y[i * T] = acc / s.l(i, i);
+    float acc = (float)s.col(i);
+#pragma unroll
+    for (int j = i + 1; j < n; j++) acc = fmaf(-s.l(i, j), (float)s.col(j), acc);
+    s.col(i) = acc / s.l(i, i);
   }
 }
 
@@ -172,61 +283,75 @@ __device__ inline void lu32_apply(const ThreadSys<T>& s, double* y) {
 // x = xold + LU32^-1 (rhs - A*xold) and iterative refinement with the FP64
 // residual rhs - A*x until the correction is at FP64 round-off (at most 6
 // passes).  A and rhs are left intact.  Returns SOLVE_FP32_FAIL when a pivot is
-// below the FP32 threshold or refinement does not contract (the caller then
-// solves in FP64).
-template <int T>
-__device__ inline int lu_solve_mixed(const ThreadSys<T>& s) {
-  const int n = s.n;
+// below the FP32 threshold or refinement stops contracting above round-off (the
+// caller then solves in FP64).
+template <class SY>
+__device__ inline int lu_solve_mixed(SY& s) {
+  const int n = s.size();
   double scale = 0;
-  for (int i = 0; i < n * n; i++) {
-    double v = s.A[i * T];
-    if (!isfinite(v)) return SOLVE_NONFINITE;
-    scale = fmax(scale, fabs(v));
-  }
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < n; i++)
+#pragma unroll
+    for (int j = 0; j < n; j++) {
+      double v = s.a(i, j);
+      bad |= !isfinite(v);
+      scale = fmax(scale, fabs(v));
+      s.l(i, j) = (float)v;
+    }
+  if (bad) return SOLVE_NONFINITE;
   if (scale == 0) return SOLVE_SINGULAR;
+#pragma unroll
   for (int j = 0; j < n; j++) {
     double m = 0;
+#pragma unroll
     for (int i = 0; i < n; i++) m = fmax(m, fabs(s.a(i, j)));
-    s.col[j * T] = m;
+    s.col(j) = m;
   }
-  for (int i = 0; i < n * n; i++) s.L32[i * T] = (float)s.A[i * T];
+#pragma unroll
   for (int k = 0; k < n; k++) {
     int p = k;
     float maxv = fabsf(s.l(k, k));
+#pragma unroll
     for (int i = k + 1; i < n; i++) {
       float v = fabsf(s.l(i, k));
       if (v > maxv) { maxv = v; p = i; }
     }
-    if ((double)maxv <= s.col[k * T] * double(n) * 1e-6) return SOLVE_FP32_FAIL;
-    s.piv[k * T] = p;
-    if (p != k)
-      for (int j = 0; j < n; j++) { float t = s.l(k, j); s.l(k, j) = s.l(p, j); s.l(p, j) = t; }
+    if ((double)maxv <= s.col(k) * double(n) * 1e-6) return SOLVE_FP32_FAIL;
+    s.piv(k) = p;
+    swap_rows32(s, k, p);
     float rp = 1.0f / s.l(k, k);
+#pragma unroll
     for (int i = k + 1; i < n; i++) {
       float f = s.l(i, k) * rp;
       s.l(i, k) = f;
-      if (f == 0.0f) continue;
+#pragma unroll
       for (int j = k + 1; j < n; j++) s.l(i, j) = fmaf(-f, s.l(k, j), s.l(i, j));
     }
   }
-  // x starts at the linearization point; each pass adds LU32^-1 of the FP64 residual.
-  for (int i = 0; i < n; i++) s.x[i * T] = s.xold[i * T];
-  double prev = CUDART_INF;
+#pragma unroll
+  for (int i = 0; i < n; i++) s.xn(i) = s.xo(i);
+  double prev = KS_INF;
   for (int pass = 0; pass < 6; pass++) {
-    for (int i = 0; i < n; i++) {  // residual in col (the column maxima are no longer needed)
-      double r = s.rhs[i * T];
-      for (int j = 0; j < n; j++) r -= s.a(i, j) * s.x[j * T];
-      s.col[i * T] = r;
+#pragma unroll
+    for (int i = 0; i < n; i++) {  // FP64 residual in col()
+      double r = s.rhs(i);
+#pragma unroll
+      for (int j = 0; j < n; j++) r -= s.a(i, j) * s.xn(j);
+      s.col(i) = r;
     }
-    lu32_apply<T>(s, s.col);
+    lu32_apply_col(s);
     double dmax = 0, xmax = 0;
+    bool nf = false;
+#pragma unroll
     for (int i = 0; i < n; i++) {
-      double v = s.x[i * T] + s.col[i * T];
-      if (!isfinite(v)) return SOLVE_NONFINITE;
-      s.x[i * T] = v;
-      dmax = fmax(dmax, fabs(s.col[i * T]));
+      double v = s.xn(i) + s.col(i);
+      nf |= !isfinite(v);
+      s.xn(i) = v;
+      dmax = fmax(dmax, fabs(s.col(i)));
       xmax = fmax(xmax, fabs(v));
     }
+    if (nf) return SOLVE_NONFINITE;
     if (dmax <= 4e-16 * xmax || dmax == 0) break;
     if (pass > 0 && dmax > 0.5 * prev) {  // refinement stopped contracting
       if (dmax <= 1e-11 * xmax) break;      // at the round-off floor of this system
@@ -238,40 +363,45 @@ __device__ inline int lu_solve_mixed(const ThreadSys<T>& s) {
 }
 
 // converged, analysis/newton.go:59-82.
-template <int T>
-__device__ inline bool converged(const KElem* el, int n_elem, const int8_t* isv, const Col& Vb, const Col& Db,
-                                 const Col& Sb, const ThreadSys<T>& s, const KOpts& o, double gmin) {
-  for (int k = 0; k < n_elem; k++) {
-    const KElem& e = el[k];
-    int lim = e.kind == KS_ELEM_D ? SD_LIM : e.kind == KS_ELEM_Q ? SQ_LIM : e.kind == KS_ELEM_M ? SM_LIM : -1;
-    if (lim >= 0 && Sb.p[(int64_t)(e.state + lim) * Sb.B] != 0) return false;
+template <class SY, class P>
+__device__ inline bool converged(const P& prog, const Col& Vb, const Col& Db, const Col& Sb, SY& s, const KOpts& o,
+                                 double gmin) {
+  bool lim = false;
+  prog.each([&](const KElem& e) {
+    int ls = lim_slot(e.kind);
+    if (ls >= 0 && Sb[e.state + ls] != 0) lim = true;
+  });
+  if (lim) return false;
+  const int n = s.size();
+  bool moved = false;
+#pragma unroll
+  for (int i = 0; i < n; i++) {
+    double x = s.xn(i), old = s.xo(i);
+    double tol = (prog.is_v(i) ? o.vntol : o.abstol) + o.reltol * fmax(fabs(x), fabs(old));
+    moved |= fabs(x - old) > tol;
   }
-  for (int i = 0; i < s.n; i++) {
-    double x = s.x[i * T], old = s.xold[i * T];
-    double tol = (isv[i] ? o.vntol : o.abstol) + o.reltol * fmax(fabs(x), fabs(old));
-    if (fabs(x - old) > tol) return false;
-  }
-  for (int k = 0; k < n_elem; k++) {
-    const KElem& e = el[k];
-    Col S{Sb.p + (int64_t)e.state * Sb.B, Sb.B};
-    if (e.kind == KS_ELEM_D) { if (!diode_conv<T>(e, Vb, Db, S, s.x, o.reltol, o.abstol, gmin)) return false; }
-    else if (e.kind == KS_ELEM_Q) { if (!bjt_conv<T>(e, Vb, Db, S, s.x, o.reltol, o.abstol, gmin)) return false; }
-    else if (e.kind == KS_ELEM_M) { if (!mos_conv<T>(e, Vb, Db, S, s.x, o.reltol, o.abstol, gmin)) return false; }
-  }
-  return true;
+  if (moved) return false;
+  bool ok = true;
+  prog.each([&](const KElem& e) {
+    if (!ok) return;
+    Col S = state_col(Sb, e);
+    if (e.kind == KS_ELEM_D) ok = diode_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
+    else if (e.kind == KS_ELEM_Q) ok = bjt_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
+    else if (e.kind == KS_ELEM_M) ok = mos_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
+  });
+  return ok;
 }
 
-// Accept every element at x (analysis/op.go:324-328).
-template <int T>
-__device__ inline void accept_all(const KElem* el, int n_elem, const Col& Vb, const Col& Db, const Col& Sb,
-                                  const double* x, double t, int mode, double gmin, bool nonlinOnly) {
-  for (int k = 0; k < n_elem; k++) {
-    const KElem& e = el[k];
-    Col S{Sb.p + (int64_t)e.state * Sb.B, Sb.B};
+// Accept every element at the new iterate (analysis/op.go:324-328).
+template <class SY, class P>
+__device__ inline void accept_all(const P& prog, const Col& Vb, const Col& Db, const Col& Sb, SY& s, double t,
+                                  int mode, double gmin, bool nonlinOnly) {
+  prog.each([&](const KElem& e) {
+    Col S = state_col(Sb, e);
     switch (e.kind) {
       case KS_ELEM_C: {  // device/reactive.go:144-161
         if (nonlinOnly) break;
-        double v = xat(x, e.u[0], T) - xat(x, e.u[1], T);
+        double v = xn_(s, e.u[0]) - xn_(s, e.u[1]);
         if (mode == ModeUICInit) { S[SC_IPREV] = 0; hist_reset(S, SC_HIST); }
         else if (mode == ModeOP || mode == ModeTranOP) { S[SC_VPREV] = v; S[SC_IPREV] = 0; hist_reset(S, SC_HIST); }
         else { double i = S[SC_TRAN] != 0 ? S[SC_GEQ] * v + S[SC_IHIST] : 0.0; S[SC_VPREV] = v; S[SC_IPREV] = i; }
@@ -280,26 +410,28 @@ __device__ inline void accept_all(const KElem* el, int n_elem, const Col& Vb, co
       }
       case KS_ELEM_L: {  // device/reactive.go:312-329
         if (nonlinOnly) break;
-        double v = xat(x, e.u[0], T) - xat(x, e.u[1], T), i = x[e.u[2] * T];
+        double v = xn_(s, e.u[0]) - xn_(s, e.u[1]), i = xn_(s, e.u[2]);
         if (mode == ModeUICInit) { S[SL_VPREV] = 0; hist_reset(S, SL_HIST); }
         else if (mode == ModeOP || mode == ModeTranOP) { S[SL_VPREV] = 0; S[SL_IPREV] = i; hist_reset(S, SL_HIST); }
         else { S[SL_VPREV] = v; S[SL_IPREV] = i; }
         hist_push(S, SL_HIST, t, Vb[e.param] * S[SL_IPREV]);
         break;
       }
-      case KS_ELEM_D: diode_accept<T>(e, Vb, Db, S, x, t, mode); break;
-      case KS_ELEM_Q: bjt_accept<T>(e, Vb, Db, S, x, t, mode, gmin); break;
-      case KS_ELEM_M: mos_accept<T>(e, Vb, Db, S, x, t, mode); break;
+      case KS_ELEM_D: diode_accept(e, Vb, Db, S, s, t, mode); break;
+      case KS_ELEM_Q: bjt_accept(e, Vb, Db, S, s, t, mode, gmin); break;
+      case KS_ELEM_M: mos_accept(e, Vb, Db, S, s, t, mode); break;
     }
-  }
+  });
 }
 
 // Fresh device state of one circuit (the zero state of newly built devices, with
 // each MOSFET's limiting threshold at VTO, device/mosfet.go:321).
-__device__ inline void init_state(const KElem* el, int n_elem, int n_state, const Col& Db, const Col& Sb) {
-  for (int k = 0; k < n_state; k++) Sb[k] = 0.0;
-  for (int k = 0; k < n_elem; k++)
-    if (el[k].kind == KS_ELEM_M) Sb[el[k].state + SM_AVON] = Db[el[k].derived + DM_VTO];
+template <class P>
+__device__ inline void init_state(const P& prog, const Col& Db, const Col& Sb) {
+  for (int k = 0; k < prog.n_state; k++) Sb[k] = 0.0;
+  prog.each([&](const KElem& e) {
+    if (e.kind == KS_ELEM_M) Sb[e.state + SM_AVON] = Db[e.derived + DM_VTO];
+  });
 }
 
 __device__ __forceinline__ uint64_t globaltimer_ns() {

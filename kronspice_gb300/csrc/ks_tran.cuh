@@ -1,0 +1,282 @@
+// ks_tran.cuh — batched transient analysis of the GB300 engine (shared by the generic
+// and the per-topology kernels).
+//
+// One thread runs (*Sim).tran (analysis/tran.go:95-231) for one circuit after another
+// as a state machine on top of the shared Newton/dcSolve machine: starting point
+// (dcSolve at ModeTranOP, or the UIC solve), then time steps with BE/trapezoidal
+// companion models, the h/8 retry on Newton failure, LTE step control
+// (device/lte.go:50-85) and landing on source breakpoints (device/waveform.go:190),
+// or the fixed-step mode of ks_tran_spec.  Circuits advance through time
+// independently; every loop is bounded by the reference's limits.
+#pragma once
+#include "ks_newton.cuh"
+
+namespace ksg {
+
+// Truncate of every reactive element at the candidate solution x
+// (device/reactive.go:178-181, :346-349; device/diode.go:388-397; BJT and
+// MOSFET Truncate in device/bjt.go and device/mosfet.go:734-757).
+template <class SY, class P>
+__device__ double truncate_all(Thr<SY, P>& t, const TruncParams& tc) {
+  double prop = KS_INF;
+  SY& x = t.s;
+  t.prog.each([&](const KElem& e) {
+    Col S = state_col(t.Sb, e);
+    switch (e.kind) {
+      case KS_ELEM_C: {
+        double v = xn_(x, e.u[0]) - xn_(x, e.u[1]);
+        double i = S[SC_TRAN] != 0 ? S[SC_GEQ] * v + S[SC_IHIST] : 0.0;
+        prop = fmin(prop, lte_step(S, SC_HIST, t.V[e.param] * v, i, S[SC_IPREV], tc.abstol, tc));
+        break;
+      }
+      case KS_ELEM_L: {
+        double v = xn_(x, e.u[0]) - xn_(x, e.u[1]);
+        prop = fmin(prop, lte_step(S, SL_HIST, t.V[e.param] * xn_(x, e.u[2]), v, S[SL_VPREV], tc.vntol, tc));
+        break;
+      }
+      case KS_ELEM_D: {
+        int p = e.param;
+        if (!(t.V[p + KS_D_P_CJO] > 0 || t.V[p + KS_D_P_TT] > 0)) break;
+        double v = xn_(x, e.u[2]) - xn_(x, e.u[1]);
+        double id, g, q, c;
+        diode_iv(t.V, t.D, p, e.derived, e.flags & KS_F_HAS_BV, v, &id, &g);
+        diode_charge(t.V, p, v, id, g, &q, &c);
+        double ic = S[SD_IQ] + S[SD_GEQ] * (v - S[SD_VD]);
+        prop = fmin(prop, lte_step(S, SD_HIST, q, ic, S[SD_IQPREV], tc.abstol, tc));
+        break;
+      }
+      case KS_ELEM_Q: {
+        if (S[SQ_TRAN] == 0) break;
+        double vbe, vbc, vbx, vcs;
+        bjt_voltages<true>(e, x, &vbe, &vbc, &vbx, &vcs);
+        BjtDC d = bjt_eval_dc(t.V, t.D, e.param, e.derived, vbe, vbc, t.o.gmin);
+        BjtCh ch = bjt_charges(t.V, t.D, e.param, e.derived, vbe, vbc, vbx, vcs, d);
+        double dv[4] = {vbe - S[SQ_VBE], vbc - S[SQ_VBC], vbx - S[SQ_VBX], vcs - S[SQ_VCS]};
+        for (int j = 0; j < 4; j++) {
+          if (ch.q[j] == 0 && S[SQ_QPREV0 + j] == 0) continue;
+          double i = S[SQ_IQ0 + j] + S[SQ_AG] * S[SQ_C0 + j] * dv[j];
+          if (j == 0) i += S[SQ_AG] * S[SQ_DQBEDVBC] * dv[1];
+          prop = fmin(prop, lte_step(S, SQ_HIST + j * H_SIZE, ch.q[j], i, S[SQ_IQPREV0 + j], tc.abstol, tc));
+        }
+        break;
+      }
+      case KS_ELEM_M: {
+        if (S[SM_TRAN] == 0) break;
+        double vgs, vds, vbs, vgb;
+        mos_voltages<true>(e, x, &vgs, &vds, &vbs, &vgb);
+        double v[5] = {vgs, vgs - vds, vgb, vbs, vbs - vds};
+        for (int j = 0; j < 5; j++) {
+          double qk, cap, tmp;
+          if (j < 3) { cap = S[SM_CAPG0 + j]; qk = S[SM_QPREV0 + j] + cap * (v[j] - S[SM_VPREV0 + j]); }
+          else {
+            cap = S[SM_CAPB0 + j - 3];
+            if (j == 3) mos_bulk_charge(t.V, e.param, t.D, e.derived, v[j], t.D[e.derived + DM_CZBS], t.D[e.derived + DM_CZBSSW], &qk, &tmp);
+            else mos_bulk_charge(t.V, e.param, t.D, e.derived, v[j], t.D[e.derived + DM_CZBD], t.D[e.derived + DM_CZBDSW], &qk, &tmp);
+          }
+          if (qk == 0 && S[SM_QPREV0 + j] == 0) continue;
+          double i = S[SM_IQ0 + j] + S[SM_AG] * cap * (v[j] - S[SM_DV0 + j]);
+          prop = fmin(prop, lte_step(S, SM_HIST + j * H_SIZE, qk, i, S[SM_IQPREV0 + j], tc.abstol, tc));
+        }
+        break;
+      }
+      default: break;
+    }
+  });
+  return prop;
+}
+
+// (*Sim).nextBreakpoint, analysis/tran.go:233-243.
+template <class SY, class P>
+__device__ double next_breakpoint(Thr<SY, P>& t, double tnow) {
+  double nb = KS_INF;
+  t.prog.each([&](const KElem& e) {
+    if ((e.kind == KS_ELEM_V || e.kind == KS_ELEM_I) && e.wave != KS_WAVE_NONE)
+      nb = fmin(nb, wave_next_breakpoint(e.wave, t.D, e.derived, t.V, e.param + KS_SRC_P_ARGS, e.nargs, tnow));
+  });
+  return nb;
+}
+
+// C and L initial conditions for UIC (device/reactive.go:298-303, :466-471).
+template <class SY, class P>
+__device__ void set_initial_conditions(Thr<SY, P>& t) {
+  t.prog.each([&](const KElem& e) {
+    Col S = state_col(t.Sb, e);
+    bool has = e.flags & KS_F_HAS_IC;
+    if (e.kind == KS_ELEM_C) { S[SC_VPREV] = has ? t.V[e.param + KS_RCL_P_IC] : 0.0; S[SC_IPREV] = 0; }
+    if (e.kind == KS_ELEM_L) { S[SL_VPREV] = 0; S[SL_IPREV] = has ? t.V[e.param + KS_RCL_P_IC] : 0.0; }
+  });
+}
+
+enum { TR_START = 0, TR_STEP, TR_DONE };
+
+struct TranSpecK {
+  double step, stop, start, maxStep, minStep, chgtol, trtol;
+  int uic, method, fixed, maxSteps, cap, npts;
+};
+
+template <class SY, class P>
+__device__ inline void record(Thr<SY, P>& t, const TranSpecK& sp, int64_t c, int64_t B, double tnow, int kgrid, int* npts,
+                              double* out_time, double* out_wave) {
+  const int n = t.n();
+  if (sp.fixed) {
+    if (out_wave && kgrid < sp.npts) {
+#pragma unroll
+      for (int i = 0; i < n; i++) out_wave[((int64_t)kgrid * B + c) * n + i] = t.s.xn(i);
+    }
+    return;
+  }
+  if (tnow < sp.start) return;
+  if (*npts < sp.cap) {
+    if (out_time) out_time[c * sp.cap + *npts] = tnow;
+    if (out_wave) {
+#pragma unroll
+      for (int i = 0; i < n; i++) out_wave[(c * sp.cap + *npts) * n + i] = t.s.xn(i);
+    }
+  }
+  (*npts)++;
+}
+
+
+// analysis.Tran of one circuit after another, pulled from the queue.
+template <class SY, class P>
+__device__ inline void tran_persistent(Thr<SY, P>& t, const TranSpecK& sp, const double* values, const double* derived,
+                                       double* state, double* work, int64_t B, double* out_time, double* out_wave,
+                                       int32_t* out_npts, int32_t* out_status, int32_t* out_steps, int32_t* out_iters,
+                                       uint64_t deadline_ns, unsigned long long* queue) {
+  const KOpts& o = t.o;
+  const int n = t.n();
+  const uint64_t t0 = deadline_ns ? globaltimer_ns() : 0;
+  const double eps = 1e-12 * sp.stop;
+  const int maxTotal = o.max_iter_total > 0 ? o.max_iter_total : 0x7fffffff;
+  TruncParams tc{0, 0, BE, o.reltol, o.abstol, o.vntol, sp.chgtol, sp.trtol};
+  OpState st;
+  LoadParams lp;
+  int phase = TR_DONE, status = KS_STATUS_OK, accepted = 0, npts = 0, kgrid = 1, order = BE;
+  bool hitBreak = false, onGrid = false;
+  double tnow = 0, h = 0, tn = 0;
+  int64_t c = B;
+
+  // Starting point of circuit c: analysis/tran.go:103-126.
+  auto start = [&]() {
+    thr_bind(t, values, derived, state, work, B, c);
+    init_state(t.prog, t.D, t.Sb);
+    lp.method = BE; lp.time = 0; lp.h = 0;
+    phase = TR_START; status = KS_STATUS_OK; accepted = 0; npts = 0; kgrid = 1; order = BE;
+    tnow = 0; h = 0; tn = 0;
+    if (sp.uic) {
+      set_initial_conditions(t);
+      op_state_reset(st, o);
+#pragma unroll
+      for (int i = 0; i < n; i++) t.s.xn(i) = 0.0;
+      lp.mode = ModeUICInit;
+    } else {
+      dc_start(t, st, nullptr, c);
+      lp.mode = ModeTranOP;
+    }
+  };
+  // The head of the time loop, analysis/tran.go:145-163.
+  auto begin_step = [&]() {
+    if (sp.fixed ? (kgrid > sp.npts - 1) : !(tnow < sp.stop - eps)) { phase = TR_DONE; status = KS_STATUS_OK; return; }
+    if (accepted >= sp.maxSteps) { phase = TR_DONE; status = KS_STATUS_TOO_MANY_STEPS; return; }
+    hitBreak = false; onGrid = false;
+    if (sp.fixed) {
+      double target = (double)kgrid * sp.step;
+      tn = tnow + h;
+      if (tn >= target - eps) { tn = target; onGrid = true; }
+    } else {
+      double nb = next_breakpoint(t, tnow);
+      tn = tnow + h;
+      if (tn >= nb - eps) { tn = nb; hitBreak = true; }
+      if (tn >= sp.stop - eps) { tn = sp.stop; hitBreak = false; }
+    }
+    h = tn - tnow;
+    lp.mode = ModeTran; lp.time = tn; lp.h = h; lp.method = order;
+    st.it = 0; st.maxIter = o.itl4;
+  };
+  auto reject = [&](double hNew) -> bool {  // analysis/tran.go:136-143
+    x_from_col(t, t.xacc);
+    if (hNew < sp.minStep) { phase = TR_DONE; status = KS_STATUS_TIMESTEP_TOO_SMALL; return false; }
+    return true;
+  };
+
+  c = (int64_t)atomicAdd(queue, 1ull);
+  if (c < B) start();
+  while (c < B) {
+    if (phase != TR_DONE) {
+      if (deadline_ns && globaltimer_ns() - t0 > deadline_ns) { status = KS_STATUS_INTERRUPTED; phase = TR_DONE; }
+      else if (st.total >= maxTotal) { status = KS_STATUS_NO_CONVERGENCE; phase = TR_DONE; }
+    }
+    if (phase != TR_DONE) {
+      int res = newton_step(t, st, lp);
+      if (res < 0) continue;
+      if (phase == TR_START) {
+        if (!sp.uic) {
+          dc_advance(t, st, res);
+          if (st.phase != PH_DONE) continue;
+          res = st.status;
+        }
+        if (res != KS_STATUS_OK) { status = res; phase = TR_DONE; }
+        else {
+          accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, sp.uic ? ModeUICInit : ModeTranOP, o.gmin, false);
+          record(t, sp, c, B, 0.0, 0, &npts, out_time, out_wave);
+          x_to_col(t, t.xacc);
+          phase = TR_STEP;
+          st.initJct = false;
+          h = sp.fixed ? sp.step : fmin(sp.maxStep, fmin(sp.step, sp.stop / 100)) / 10;
+          order = BE;
+          begin_step();
+        }
+      } else if (res != KS_STATUS_OK) {  // a time step's newton failed
+        if (!retryable(res) || t.prog.nonlin_empty) { status = res; phase = TR_DONE; }
+        else {
+          h /= 8;  // analysis/tran.go:168-175
+          if (reject(h)) { order = BE; begin_step(); }
+        }
+      } else {
+        double proposal = KS_INF;
+        bool rejected = false;
+        if (!sp.fixed) {  // analysis/tran.go:178-197
+          tc.time = tn; tc.h = h; tc.method = order;
+          proposal = truncate_all(t, tc);
+          if (proposal < 0.9 * h) {
+            h = fmax(proposal, h / 8);
+            rejected = true;
+            if (reject(h)) begin_step();
+          }
+        }
+        if (!rejected) {
+          accept_all(t.prog, t.V, t.D, t.Sb, t.s, tn, ModeTran, o.gmin, false);  // :200-208
+          if (!sp.fixed || onGrid) record(t, sp, c, B, tn, kgrid, &npts, out_time, out_wave);
+          x_to_col(t, t.xacc);
+          accepted++;
+          tnow = tn;
+          order = sp.method;
+          if (sp.fixed) {
+            if (onGrid) kgrid++;
+            h = fmax(fmin(2 * h, sp.maxStep), sp.minStep);
+          } else {  // :211-225
+            double next = fmin(fmin(proposal, 2 * h), sp.maxStep);
+            if (hitBreak) {
+              order = BE;
+              double nb2 = next_breakpoint(t, tnow);
+              next = fmin(next, 0.1 * fmin(sp.maxStep, nb2 - tnow));
+            }
+            h = fmax(next, sp.minStep);
+          }
+          begin_step();
+        }
+      }
+      if (phase != TR_DONE) continue;
+    }
+    // circuit c finished: write its results and take the next one
+    if (out_status) out_status[c] = status;
+    if (out_steps) out_steps[c] = accepted;
+    if (out_iters) out_iters[c] = st.total;
+    if (out_npts) out_npts[c] = sp.fixed ? kgrid : (npts < sp.cap ? npts : sp.cap);
+    c = (int64_t)atomicAdd(queue, 1ull);
+    if (c < B) start();
+  }
+}
+
+
+}  // namespace ksg

@@ -102,6 +102,9 @@ def feature_spec(name, el):
                [int(el[0]["param"])]
         logmask = 0b0111101
         return cols, logmask, int(el[0]["param"])
+    if name == "cmos_opamp":
+        cols, logs, scale = workloads.cmos_opamp_feature_columns(el)
+        return cols, sum(1 << j for j, lg in enumerate(logs) if lg), scale
     raise KeyError(name)
 
 
@@ -131,7 +134,7 @@ def train_for(name, el, nn, vals, batch, device, n_train=131072, epochs=40, mb=2
     topology solved by the plain FP64 GPU solver, then bind it to `batch`."""
     import torch
     t0 = time.perf_counter()
-    gen = {"bjt_ce": workloads.bjt_ce_batch}[name]
+    gen = {"bjt_ce": workloads.bjt_ce_batch, "cmos_opamp": workloads.cmos_opamp_batch}[name]
     _, _, tv = gen(n_train, seed)
     plan = analysis.Plan(el, nn, tv.shape[1])
     tb = analysis.Batch(plan, tv)
@@ -178,5 +181,6 @@ def train_for(name, el, nn, vals, batch, device, n_train=131072, epochs=40, mb=2
 
 
 def for_workload(name, el, nn, vals, batch, device):
-    """The bench's learned start: 1,048,576 plain-solver operating points, 60 epochs."""
-    return train_for(name, el, nn, vals, batch, device, n_train=1 << 20, epochs=60, mb=4096, lr=2e-3)
+    """The bench's learned start: 1,048,576 plain-solver operating points."""
+    return train_for(name, el, nn, vals, batch, device, n_train=1 << 20, epochs=60 if name == "bjt_ce" else 40,
+                     mb=4096, lr=2e-3)

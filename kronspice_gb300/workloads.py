@@ -87,3 +87,92 @@ def rc_ladder_batch(n_circ, seed=0, sections=10):
         vals[:, off["R%d" % k]] = log_uniform(g, 1e2, 1e5, n_circ)
         vals[:, off["C%d" % k]] = log_uniform(g, 1e-12, 1e-6, n_circ)
     return el, c.n_nodes, vals
+
+
+# ------------------------------------------------------------------ two-stage CMOS op-amp operating point
+OPAMP_DEVICES = ["M1", "M2", "M3", "M4", "M5", "M6", "M7", "M8"]
+OPAMP_NMOS = ["M1", "M2", "M5", "M7", "M8"]
+
+
+def cmos_opamp_template():
+    """Two-stage Miller op-amp in unity-gain feedback (level-1 MOSFETs): NMOS input
+    pair M1/M2 with PMOS mirror load M3/M4 and tail M5, PMOS common-source second
+    stage M6 with NMOS current-source load M7, bias mirror M8 fed by RB, Miller
+    capacitor CC and load CL.  The output drives the inverting input, so the
+    operating point is defined: v(out) follows the common-mode input VCM."""
+    b = Builder("two-stage cmos op-amp")
+    b.voltage_source("VDD", "vdd", "0", 5.0)
+    b.voltage_source("VCM", "inp", "0", 2.5)
+    b.resistor("RB", "vdd", "nb", 100e3)
+    b.model("nch", "nmos", {"level": 1, "vto": 0.6, "kp": 100e-6, "lambda": 0.04, "gamma": 0.4, "phi": 0.7})
+    b.model("pch", "pmos", {"level": 1, "vto": -0.6, "kp": 40e-6, "lambda": 0.05, "gamma": 0.45, "phi": 0.7})
+    L = 1e-6
+    b.mosfet("M1", "n1", "inp", "tail", "0", "nch", {"l": L, "w": 10 * L})
+    b.mosfet("M2", "n2", "out", "tail", "0", "nch", {"l": L, "w": 10 * L})
+    b.mosfet("M3", "n1", "n1", "vdd", "vdd", "pch", {"l": L, "w": 20 * L})
+    b.mosfet("M4", "n2", "n1", "vdd", "vdd", "pch", {"l": L, "w": 20 * L})
+    b.mosfet("M5", "tail", "nb", "0", "0", "nch", {"l": L, "w": 20 * L})
+    b.mosfet("M6", "out", "n2", "vdd", "vdd", "pch", {"l": L, "w": 80 * L})
+    b.mosfet("M7", "out", "nb", "0", "0", "nch", {"l": L, "w": 40 * L})
+    b.mosfet("M8", "nb", "nb", "0", "0", "nch", {"l": L, "w": 10 * L})
+    b.capacitor("CC", "n2", "out", 2e-12)
+    b.capacitor("CL", "out", "0", 10e-12)
+    return b.build()
+
+
+OPAMP_FEATURES = (["w/l %s" % m for m in OPAMP_DEVICES] +
+                  ["vto n", "vto p", "kp n", "kp p", "lambda n", "lambda p", "gamma n", "gamma p", "phi n", "phi p",
+                   "rb", "cc", "cl", "vdd", "vcm", "l"])
+
+
+def cmos_opamp_batch(n_circ, seed=0):
+    """24-D parameter vector per variant: W/L of the 8 devices log-U[1, 100]; VTO
+    U[0.4, 0.8] V (PMOS negative); KP log-U[20, 200] uA/V^2; LAMBDA U[0.01, 0.1];
+    GAMMA U[0.3, 0.6]; PHI U[0.6, 0.8]; RB log-U[10 k, 1 M]; CC log-U[0.1, 10] pF;
+    CL log-U[1, 100] pF; VDD U[3, 5] V; VCM U[0.4, 0.6] VDD; L log-U[0.5, 5] um."""
+    c = cmos_opamp_template()
+    el, v0, off = _offsets(c)
+    g = rng(4, seed)
+    vals = np.tile(v0, (n_circ, 1))
+    k = M_KEYS.index
+    L = log_uniform(g, 0.5e-6, 5e-6, n_circ)
+    wl = {m: log_uniform(g, 1.0, 100.0, n_circ) for m in OPAMP_DEVICES}
+    vto = {"n": g.uniform(0.4, 0.8, n_circ), "p": -g.uniform(0.4, 0.8, n_circ)}
+    kp = {"n": log_uniform(g, 20e-6, 200e-6, n_circ), "p": log_uniform(g, 20e-6, 200e-6, n_circ)}
+    lam = {"n": g.uniform(0.01, 0.1, n_circ), "p": g.uniform(0.01, 0.1, n_circ)}
+    gam = {"n": g.uniform(0.3, 0.6, n_circ), "p": g.uniform(0.3, 0.6, n_circ)}
+    phi = {"n": g.uniform(0.6, 0.8, n_circ), "p": g.uniform(0.6, 0.8, n_circ)}
+    for m in OPAMP_DEVICES:
+        t = "n" if m in OPAMP_NMOS else "p"
+        p = off[m]
+        vals[:, p + k("l")] = L
+        vals[:, p + k("w")] = wl[m] * L
+        vals[:, p + k("vto")] = vto[t]
+        vals[:, p + k("kp")] = kp[t]
+        vals[:, p + k("lambda")] = lam[t]
+        vals[:, p + k("gamma")] = gam[t]
+        vals[:, p + k("phi")] = phi[t]
+    vals[:, off["RB"]] = log_uniform(g, 1e4, 1e6, n_circ)
+    vals[:, off["CC"]] = log_uniform(g, 0.1e-12, 10e-12, n_circ)
+    vals[:, off["CL"]] = log_uniform(g, 1e-12, 100e-12, n_circ)
+    vdd = g.uniform(3.0, 5.0, n_circ)
+    vals[:, off["VDD"]] = vdd
+    vals[:, off["VCM"]] = vdd * g.uniform(0.4, 0.6, n_circ)
+    return el, c.n_nodes, vals
+
+
+def cmos_opamp_feature_columns(el):
+    """Value columns of the 24-D parameter vector (and which are log-scaled)."""
+    c = cmos_opamp_template()
+    names = [e.name for e in c.elements]
+    off = {nm: int(el[i]["param"]) for i, nm in enumerate(names)}
+    k = M_KEYS.index
+    cols, logs = [], []
+    for m in OPAMP_DEVICES:   # W/L enters through W (L is its own feature)
+        cols.append(off[m] + k("w")); logs.append(True)
+    for key in ("vto", "kp", "lambda", "gamma", "phi"):
+        cols.append(off["M1"] + k(key)); logs.append(key == "kp")
+        cols.append(off["M3"] + k(key)); logs.append(key == "kp")
+    cols += [off["RB"], off["CC"], off["CL"], off["VDD"], off["VCM"], off["M1"] + k("l")]
+    logs += [True, True, True, False, False, True]
+    return cols, logs, off["VDD"]

@@ -156,3 +156,16 @@ def test_fallback_chain_matches_oracle():
         assert np.array_equal(sg, so)
         ok = so == 0
         assert np.all(np.abs(xg[ok] - xo[ok]) <= tol(xo[ok], isv, 1e-3))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cmos_opamp_batch_matches_oracle(precision):
+    """Level-1 two-stage op-amp variants (the 24-D parameter workload)."""
+    el, nn, vals = workloads.cmos_opamp_batch(2048, seed=13)
+    og = analysis.Options(reltol=RELTOL, precision=precision)
+    oc = orc.options(reltol=RELTOL)
+    (xg, sg, ig), (xo, so, io), isv = run_both(el, nn, vals, og, oc)
+    assert np.array_equal(sg, so), np.nonzero(sg != so)
+    ok = so == 0
+    assert ok.mean() > 0.98
+    assert np.all(np.abs(xg[ok] - xo[ok]) <= tol(xo[ok], isv, 1e-5))
