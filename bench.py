@@ -18,6 +18,7 @@ over all host cores on a bounded sample of the same workload.
 """
 import argparse
 import ctypes
+import dataclasses
 import json
 import os
 import statistics
@@ -51,6 +52,11 @@ def parse():
     p.add_argument("--n-circ", type=int, default=0)
     p.add_argument("--workload", default="bjt_ce", choices=sorted(WORKLOADS))
     p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                   help="LU precision of the chosen path")
+    p.add_argument("--variants", type=int, default=1, help="also time every kernel/precision/start combination")
+    p.add_argument("--start-cache", default=None,
+                   help="learned-start network file (.npz): loaded when present, else trained and saved there")
     return p.parse_args()
 
 
@@ -212,7 +218,7 @@ def main():
     learned = None
     try:
         from kronspice_gb300 import learned_start
-        learned = learned_start.for_workload(args.workload, el, nn, vals, batch, dev)
+        learned = learned_start.for_workload(args.workload, el, nn, vals, batch, dev, cache=args.start_cache)
     except (ImportError, AttributeError):
         learned = None
 
@@ -250,13 +256,35 @@ def main():
                 "iters_mean": float(it.mean()), "iters_max": int(it.max()), "launches": launches * args.steps,
                 "x": x_dev.cpu().numpy(), "status": st}
 
-    plain_opt = analysis.Options(reltol=RELTOL, precision="fp64")
-    chosen_opt = analysis.Options(reltol=RELTOL, precision="mixed")
+    spec_info = None
+    try:
+        kname, csec = plan.specialize("op")
+        spec_info = {"kernel": kname, "nvrtc_s": csec}
+    except RuntimeError as e:  # no per-topology kernel: everything runs on the generic one
+        spec_info = {"kernel": None, "error": str(e)[:200]}
+    spec_ok = spec_info["kernel"] is not None
+    plain_opt = analysis.Options(reltol=RELTOL, precision="fp64", kernel="generic")
+    chosen_opt = analysis.Options(reltol=RELTOL, precision=args.precision,
+                                  kernel="specialized" if spec_ok else "generic")
     clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp",
                               "bench_clocks_%d.csv" % rank))
+    variants = {}
     with clk:
         plain = timed(plain_opt, False)
         chosen = timed(chosen_opt, True)
+        if args.variants:  # each ingredient of the chosen path alone and combined
+            for kern in (["generic", "specialized"] if spec_ok else ["generic"]):
+                for prec in ("fp64", "mixed"):
+                    for ws in ((False, True) if learned else (False,)):
+                        r = timed(analysis.Options(reltol=RELTOL, precision=prec, kernel=kern), ws)
+                        variants["%s/%s/%s" % (kern, prec, "learned" if ws else "InitJct")] = {
+                            "ms_per_step": r["ms_per_step"], "solves_per_s": r["ok"] * args.steps / r["seconds"],
+                            "newton_iters_mean": r["iters_mean"], "newton_iters_max": r["iters_max"]}
+            # one unchecked FP64-residual pass per Newton step
+            r = timed(dataclasses.replace(chosen_opt, precision="mixed", mixed_passes=1), True)
+            variants["%s/mixed-1pass/learned" % chosen_opt.kernel] = {
+                "ms_per_step": r["ms_per_step"], "solves_per_s": r["ok"] * args.steps / r["seconds"],
+                "newton_iters_mean": r["iters_mean"], "newton_iters_max": r["iters_max"]}
     clocks = clk.summary(local)
 
     # end to end through the C ABI: pinned host values in, host solutions out
@@ -332,15 +360,18 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": chosen["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64 device eval + residual, f32 LU", "data": "synthetic (seeded Philox)",
+        "vs_baseline": None,
+        "dtype": "f64 device eval + residual, f32 LU" if args.precision == "mixed" else "f64", "data": "synthetic (seeded Philox)",
         "config": {"workload": "%s_op_%d" % (args.workload, B), "n_circuits_per_gpu": B, "n_unknowns": n, "reltol": RELTOL,
                    "abstol": 1e-12, "l2": "flushed between timed steps (512 MB write)",
                    "learned_start": learned is not None},
         "plain": {"value": plain_value, "ms_per_step": plain["ms_per_step"], "newton_iters_mean": plain["iters_mean"],
                   "newton_iters_max": plain["iters_max"], "precision": "fp64", "start": "InitJct"},
         "chosen": {"value": value, "newton_iters_mean": chosen["iters_mean"], "newton_iters_max": chosen["iters_max"],
-                   "precision": "fp32 LU + fp64 residual",
-                   "start": "learned (MLP)" if learned is not None else "InitJct"},
+                   "precision": "fp32 LU + fp64 residual" if args.precision == "mixed" else "fp64",
+                   "kernel": chosen_opt.kernel, "start": "learned (MLP)" if learned is not None else "InitJct"},
+        "per_topology_kernel": spec_info,
+        "variants": variants or None,
         "chosen_vs_plain": value / plain_value if plain_value else None,
         "learned_start": None if learned is None else learned.info,
         "max_node_voltage_err_vs_oracle": max_err,

@@ -160,7 +160,14 @@ enum {
 
 /* ---- analysis options (analysis/op.go:22-62, defaults :91-110) ---------- */
 enum { KS_PREC_FP64 = 0, KS_PREC_MIXED = 1 };
-enum { KS_BACKEND_AUTO = 0, KS_BACKEND_DENSE = 1, KS_BACKEND_SPARSE = 2 };
+/* backend: DENSE / SPARSE pick the CPU oracle's linear solver; on the GPU,
+ * GENERIC forces the generic thread-per-circuit kernels, SPECIALIZED the
+ * per-topology kernels (compiled at run time, ks_plan_specialize), and AUTO
+ * takes the per-topology kernels for large batches. */
+enum { KS_BACKEND_AUTO = 0, KS_BACKEND_DENSE = 1, KS_BACKEND_SPARSE = 2, KS_BACKEND_GENERIC = 3,
+       KS_BACKEND_SPECIALIZED = 4 };
+/* Kernel of a batch's last analysis (ks_batch_last_kernel). */
+enum { KS_KERNEL_GENERIC = 0, KS_KERNEL_SPEC_REG = 1, KS_KERNEL_SPEC_SMEM = 2 };
 
 typedef struct {
   double reltol;   /* <= 0: 1e-3  */
@@ -173,11 +180,17 @@ typedef struct {
   int32_t no_source_stepping;
   int32_t no_pseudo_transient;
   int32_t precision;      /* KS_PREC_FP64 (plain) or KS_PREC_MIXED          */
-  int32_t backend;        /* linear solver of the CPU oracle               */
+  int32_t backend;        /* KS_BACKEND_*                                   */
   int32_t max_iter_total; /* device-side bound on all Newton iterations of one
                              circuit, fallbacks included (0: unbounded by it) */
   double deadline_s;      /* > 0: per-call wall-clock limit, the context
                              deadline of Options.Context (KS_STATUS_INTERRUPTED) */
+  int32_t mixed_passes;   /* KS_PREC_MIXED: most FP64-residual refinement passes
+                             per linear solve (<= 0: 6); a solve not refined to
+                             1e-11 within them goes to FP64.  1: one unchecked
+                             pass, each Newton step the FP32 solve of the FP64
+                             residual (well-conditioned systems only) */
+  int32_t reserved;
 } ks_options;
 
 /* ---- transient request (analysis/tran.go:26-59) ------------------------- */
@@ -195,6 +208,7 @@ typedef struct {
   double min_step;    /* <= 0: 1e-12 * stop */
 } ks_tran_spec;
 
+#ifndef __CUDACC_RTC__ /* the device code compiled at run time needs only the layout above */
 /* ---- library ------------------------------------------------------------ */
 const char* ks_version(void);
 /* Message of the last failed call on this host thread ("" if none). */
@@ -224,6 +238,20 @@ int ks_plan_create(const ks_topology* topo, ks_plan** out);
 void ks_plan_destroy(ks_plan* plan);
 int ks_plan_info(const ks_plan* plan, int32_t* n_unknowns, int32_t* n_values, int32_t* n_state);
 
+/* Per-topology kernels (engine-specific, no counterpart in the reference): the
+ * plan's element program written out as CUDA source with every element a
+ * compile-time constant, compiled by NVRTC for the current device, one kernel
+ * per analysis (KS_ANALYSIS_OP: ks_op, KS_ANALYSIS_TRAN: ks_tran).  Compiles
+ * (or loads from the cubin cache) now instead of at the first large analysis;
+ * *kernel receives KS_KERNEL_SPEC_REG or KS_KERNEL_SPEC_SMEM, *compile_s the
+ * NVRTC time (0 when cached).  KS_EUNSUPPORTED with the compiler log in
+ * ks_last_error when it does not compile. */
+enum { KS_ANALYSIS_OP = 0, KS_ANALYSIS_TRAN = 1 };
+int ks_plan_specialize(ks_plan* plan, int32_t analysis, int32_t* kernel, double* compile_s);
+/* The generated source of one analysis' kernel (NUL-terminated, truncated to
+ * cap-1 bytes; *len = full size). */
+int ks_plan_kernel_source(const ks_plan* plan, int32_t analysis, char* buf, size_t cap, size_t* len);
+
 /* Allocate device storage for n_circ circuits of a plan and upload their
  * value vectors (row-major [n_circ][n_values], host memory). */
 int ks_batch_create(ks_plan* plan, int32_t n_circ, const double* values, ks_batch** out);
@@ -231,6 +259,8 @@ int ks_batch_create(ks_plan* plan, int32_t n_circ, const double* values, ks_batc
  * or device memory when values_are_device != 0 (then `values` is a device
  * pointer to [n_circ][n_values] doubles). */
 int ks_batch_set_values(ks_batch* b, const double* values, int values_are_device, void* stream);
+/* KS_KERNEL_* that ran the batch's last analysis (-1 before the first). */
+int ks_batch_last_kernel(const ks_batch* b);
 void ks_batch_destroy(ks_batch* b);
 
 /*
@@ -306,6 +336,7 @@ int ks_mlp_train(ks_mlp* m, ks_batch* b, const double* x_dev, const int32_t* idx
                  int32_t epochs, int32_t mb, float lr, float* last_loss, void* stream);
 /* Predicted starting points x0_dev [n_circ][n] (device memory) for ks_op_async. */
 int ks_mlp_predict(ks_mlp* m, ks_batch* b, double* x0_dev, void* stream);
+#endif /* __CUDACC_RTC__ */
 
 #ifdef __cplusplus
 }

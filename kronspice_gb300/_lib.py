@@ -21,7 +21,7 @@ class KsOptions(ctypes.Structure):
                 ("no_gmin_stepping", ctypes.c_int32), ("no_source_stepping", ctypes.c_int32),
                 ("no_pseudo_transient", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("backend", ctypes.c_int32), ("max_iter_total", ctypes.c_int32),
-                ("deadline_s", ctypes.c_double)]
+                ("deadline_s", ctypes.c_double), ("mixed_passes", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class KsTranSpec(ctypes.Structure):
@@ -34,7 +34,8 @@ class KsTranSpec(ctypes.Structure):
 # every symbol include/kronspice_gpu.h declares
 EXPORTS = ["ks_version", "ks_last_error", "ks_validate", "ks_unknowns", "ks_plan_create", "ks_plan_destroy",
            "ks_plan_info", "ks_batch_create", "ks_batch_set_values", "ks_batch_destroy", "ks_op", "ks_op_async",
-           "ks_tran", "ks_tran_async", "ks_tran_points"]
+           "ks_tran", "ks_tran_async", "ks_tran_points", "ks_plan_specialize", "ks_plan_kernel_source",
+           "ks_batch_last_kernel"]
 
 _lib = None
 
@@ -73,6 +74,9 @@ def load(build_if_missing=False):
     L.ks_tran.argtypes = [P, P, P, ctypes.c_int32, P, P, P, P, P, P, P]
     L.ks_tran_async.argtypes = [P, P, P, ctypes.c_int32, P, P, P, P, P, P, P]
     L.ks_tran_points.argtypes = [P, P]
+    L.ks_plan_specialize.argtypes = [P, ctypes.c_int32, P, P]
+    L.ks_plan_kernel_source.argtypes = [P, ctypes.c_int32, ctypes.c_char_p, ctypes.c_size_t, P]
+    L.ks_batch_last_kernel.argtypes = [P]
     _lib = L
     return L
 

@@ -62,6 +62,10 @@ STATUS_ERRORS = {1: (ErrSingularMatrix, "solver: singular matrix"),
                  7: (KronspiceError, "not run")}
 
 PREC = {"fp64": 0, "mixed": 1}
+# GPU kernel choice: "auto" (per-topology kernels for large batches), "generic", "specialized"
+KERNEL = {"auto": 0, "generic": 3, "specialized": 4}
+ANALYSIS = {"op": 0, "tran": 1}
+KERNEL_NAMES = {-1: None, 0: "generic", 1: "specialized-registers", 2: "specialized-shared"}
 
 
 @dataclass
@@ -79,12 +83,14 @@ class Options:
     precision: str = "fp64"
     max_iter_total: int = 0
     deadline_s: float = 0.0
+    kernel: str = "auto"
+    mixed_passes: int = 0
 
     def c(self):
         return _lib.KsOptions(self.reltol, self.abstol, self.vntol, self.gmin, self.itl1, self.itl4,
                               int(self.no_gmin_stepping), int(self.no_source_stepping),
-                              int(self.no_pseudo_transient), PREC[self.precision], 0, self.max_iter_total,
-                              self.deadline_s)
+                              int(self.no_pseudo_transient), PREC[self.precision], KERNEL[self.kernel],
+                              self.max_iter_total, self.deadline_s, self.mixed_passes, 0)
 
 
 def _check(rc, what):
@@ -114,6 +120,24 @@ class Plan:
         _check(L.ks_plan_info(h, ctypes.byref(n), None, None), "ks_plan_info")
         self.n = n.value
 
+    def specialize(self, analysis="op"):
+        """Compile (or load from the cache) the per-topology kernel of one
+        analysis ("op" or "tran") now: (kernel name, NVRTC seconds)."""
+        k, t = ctypes.c_int32(), ctypes.c_double()
+        _check(_lib.load().ks_plan_specialize(self.handle, ANALYSIS[analysis], ctypes.byref(k), ctypes.byref(t)),
+               "ks_plan_specialize")
+        return KERNEL_NAMES[k.value], t.value
+
+    def kernel_source(self, analysis="op"):
+        L = _lib.load()
+        n = ctypes.c_size_t()
+        _check(L.ks_plan_kernel_source(self.handle, ANALYSIS[analysis], None, 0, ctypes.byref(n)),
+               "ks_plan_kernel_source")
+        buf = ctypes.create_string_buffer(n.value + 1)
+        _check(L.ks_plan_kernel_source(self.handle, ANALYSIS[analysis], buf, n.value + 1, None),
+               "ks_plan_kernel_source")
+        return buf.value.decode()
+
     def __del__(self):
         if getattr(self, "handle", None) and _lib._lib is not None:
             _lib._lib.ks_plan_destroy(self.handle)
@@ -132,6 +156,12 @@ class Batch:
         _check(L.ks_batch_create(plan.handle, self.n_circ, self.values.ctypes.data, ctypes.byref(h)),
                "ks_batch_create")
         self.handle = h
+
+    @property
+    def last_kernel(self):
+        """Kernel that ran the last analysis: "generic", "specialized-registers",
+        "specialized-shared" (None before the first)."""
+        return KERNEL_NAMES[_lib.load().ks_batch_last_kernel(self.handle)]
 
     def set_values(self, values):
         self.values = np.ascontiguousarray(values, dtype=np.float64)

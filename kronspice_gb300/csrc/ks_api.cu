@@ -10,6 +10,8 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <cstdlib>
+#include <map>
 #include "ks_internal.h"
 
 using ksh::set_error;
@@ -18,6 +20,9 @@ struct ks_plan {
   ksh::HostPlan hp;
   KElem* d_elem = nullptr;
   int8_t* d_isv = nullptr;
+  std::mutex spec_mu;                  // per-topology kernels, per device
+  std::map<std::pair<int, int>, KsSpec> spec;           // (device, kind)
+  std::map<std::pair<int, int>, std::string> spec_err;  // compile failure (not retried)
   KPlan view() const {
     KPlan p;
     p.n = hp.n; p.n_elem = hp.n_elem; p.n_values = hp.n_values; p.n_derived = hp.n_derived;
@@ -41,6 +46,7 @@ struct ks_batch {
   double* h_pin = nullptr;
   size_t h_pin_bytes = 0;
   double setup_step = -1, setup_stop = -1;  // analysis the derived constants were made for
+  int last_kernel = -1;                       // KS_KERNEL_* of the last launch
 };
 
 // Derived constants for an analysis with print step / stop time (0, 0 outside a transient).
@@ -73,6 +79,7 @@ static KOpts make_opts(const ks_options* o) {  // analysis/op.go:91-110
   k.no_source = o ? o->no_source_stepping : 0;
   k.no_pt = o ? o->no_pseudo_transient : 0;
   k.mixed = o ? (o->precision == KS_PREC_MIXED) : 0;
+  k.passes = o && o->mixed_passes > 0 ? std::min(o->mixed_passes, 8) : 6;
   k.max_iter_total = o ? o->max_iter_total : 0;
   return k;
 }
@@ -89,23 +96,14 @@ extern "C" int ks_plan_create(const ks_topology* topo, ks_plan** out) {
     delete p;
     return KS_EUNSUPPORTED;
   }
-  if (cudaMalloc(&p->d_elem, sizeof(KElem) * p->hp.n_elem) != cudaSuccess ||
-      cudaMalloc(&p->d_isv, p->hp.n + 8) != cudaSuccess) {
-    set_error("ks_plan_create: device allocation failed");
-    cudaFree(p->d_elem);
-    delete p;
-    return KS_ENOMEM;
-  }
-  cudaMemcpy(p->d_elem, p->hp.elem.data(), sizeof(KElem) * p->hp.n_elem, cudaMemcpyHostToDevice);
-  cudaMemcpy(p->d_isv, p->hp.is_v.data(), p->hp.n, cudaMemcpyHostToDevice);
   *out = p;
   return KS_OK;
 }
 
 extern "C" void ks_plan_destroy(ks_plan* p) {
   if (!p) return;
-  cudaFree(p->d_elem);
-  cudaFree(p->d_isv);
+  if (p->d_elem) cudaFree(p->d_elem);
+  if (p->d_isv) cudaFree(p->d_isv);
   delete p;
 }
 
@@ -127,8 +125,34 @@ static int batch_stage(ks_batch* b, size_t bytes) {
   return KS_OK;
 }
 
+// Device copy of the element program, made with the plan's first batch (a plan
+// itself is host-only symbolic work).
+static int plan_upload(ks_plan* p) {
+  std::lock_guard<std::mutex> lk(p->spec_mu);
+  if (p->d_elem) return KS_OK;
+  KElem* de = nullptr;
+  int8_t* di = nullptr;
+  if (cudaMalloc(&de, sizeof(KElem) * p->hp.n_elem) != cudaSuccess || cudaMalloc(&di, p->hp.n + 8) != cudaSuccess) {
+    set_error("ks_batch_create: device allocation for the plan failed");
+    cudaFree(de);
+    return KS_ENOMEM;
+  }
+  if (cudaMemcpy(de, p->hp.elem.data(), sizeof(KElem) * p->hp.n_elem, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(di, p->hp.is_v.data(), p->hp.n, cudaMemcpyHostToDevice) != cudaSuccess) {
+    set_error("ks_batch_create: plan upload failed");
+    cudaFree(de);
+    cudaFree(di);
+    return KS_ECUDA;
+  }
+  p->d_elem = de;
+  p->d_isv = di;
+  return KS_OK;
+}
+
 extern "C" int ks_batch_create(ks_plan* plan, int32_t n_circ, const double* values, ks_batch** out) {
   if (!plan || n_circ <= 0 || !out) { set_error("ks_batch_create: bad argument"); return KS_EINVAL; }
+  int urc = plan_upload(plan);
+  if (urc) return urc;
   ks_batch* b = new ks_batch();
   b->plan = plan;
   b->B = n_circ;
@@ -187,6 +211,81 @@ extern "C" void ks_batch_destroy(ks_batch* b) {
   delete b;
 }
 
+// Per-topology kernels of a plan for the current device, compiled (or loaded from
+// a cache) on first use.
+static int plan_spec(ks_plan* p, int kind, const KsSpec** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { set_error("no CUDA device"); return KS_ECUDA; }
+  auto key = std::make_pair(dev, kind);
+  std::lock_guard<std::mutex> lk(p->spec_mu);
+  auto it = p->spec.find(key);
+  if (it != p->spec.end()) { *out = &it->second; return KS_OK; }
+  auto ie = p->spec_err.find(key);
+  if (ie != p->spec_err.end()) { set_error(ie->second); return KS_EUNSUPPORTED; }
+  KsSpec k;
+  std::string err;
+  if (ksj::get(p->hp, kind, &k, &err)) {
+    p->spec_err[key] = "per-topology kernels: " + err;
+    set_error(p->spec_err[key]);
+    return KS_EUNSUPPORTED;
+  }
+  *out = &(p->spec[key] = k);
+  return KS_OK;
+}
+
+static int64_t env_int(const char* name, int64_t dflt) {
+  const char* e = getenv(name);
+  return e && *e ? atoll(e) : dflt;
+}
+
+// Kernel choice (ks_options.backend): the per-topology kernels always under
+// KS_BACKEND_SPECIALIZED, never under KS_BACKEND_GENERIC, and under
+// KS_BACKEND_AUTO for systems that fit in registers (KS_JIT_REG_MAX unknowns,
+// default 6) in batches of at least KS_JIT_MIN_BATCH circuits (default 2048: the
+// NVRTC compile, about ten seconds, is paid once per topology and process and
+// then comes from the disk cache), unless KS_JIT=0; a failed compile then falls
+// back to the generic kernels.  Larger systems stay on the generic kernels under
+// AUTO: their per-topology code unrolls every element (megabytes of code for a
+// few dozen devices, and as long to compile).
+static int pick_kernel(ks_batch* b, const ks_options* opt, int kind, const KsSpec** out) {
+  *out = nullptr;
+  int backend = opt ? opt->backend : KS_BACKEND_AUTO;
+  bool want = backend == KS_BACKEND_SPECIALIZED ||
+              (backend != KS_BACKEND_GENERIC && env_int("KS_JIT", 1) != 0 && b->plan->hp.n <= ksj::reg_max() &&
+               b->B >= env_int("KS_JIT_MIN_BATCH", 2048));
+  if (want) {
+    int rc = plan_spec(b->plan, kind, out);
+    if (rc && backend == KS_BACKEND_SPECIALIZED) return rc;
+    if (rc) *out = nullptr;
+  }
+  b->last_kernel = *out ? ((*out)->reg ? KS_KERNEL_SPEC_REG : KS_KERNEL_SPEC_SMEM) : KS_KERNEL_GENERIC;
+  return KS_OK;
+}
+
+extern "C" int ks_plan_specialize(ks_plan* plan, int32_t analysis, int32_t* kernel, double* compile_s) {
+  if (!plan || (analysis != KS_ANALYSIS_OP && analysis != KS_ANALYSIS_TRAN)) return KS_EINVAL;
+  const KsSpec* k = nullptr;
+  int rc = plan_spec(plan, analysis == KS_ANALYSIS_OP ? ksj::KIND_OP : ksj::KIND_TRAN, &k);
+  if (rc) return rc;
+  if (kernel) *kernel = k->reg ? KS_KERNEL_SPEC_REG : KS_KERNEL_SPEC_SMEM;
+  if (compile_s) *compile_s = k->compile_s;
+  return KS_OK;
+}
+
+extern "C" int ks_plan_kernel_source(const ks_plan* plan, int32_t analysis, char* buf, size_t cap, size_t* len) {
+  if (!plan || (analysis != KS_ANALYSIS_OP && analysis != KS_ANALYSIS_TRAN)) return KS_EINVAL;
+  std::string s = ksj::source(plan->hp, 64, analysis == KS_ANALYSIS_OP ? ksj::KIND_OP : ksj::KIND_TRAN, nullptr);
+  if (len) *len = s.size();
+  if (buf && cap) {
+    size_t m = std::min(cap - 1, s.size());
+    std::memcpy(buf, s.data(), m);
+    buf[m] = 0;
+  }
+  return KS_OK;
+}
+
+extern "C" int ks_batch_last_kernel(const ks_batch* b) { return b ? b->last_kernel : -1; }
+
 extern "C" int ks_op_async(ks_batch* b, const ks_options* opt, const double* x0_dev, double* out_x_dev,
                            int32_t* out_status_dev, int32_t* out_iters_dev, void* stream) {
   if (!b) return KS_EINVAL;
@@ -194,10 +293,14 @@ extern "C" int ks_op_async(ks_batch* b, const ks_options* opt, const double* x0_
   const ksh::HostPlan& hp = b->plan->hp;
   KOpts o = make_opts(opt);
   (void)hp;
-  int rc = batch_setup(b, 0.0, 0.0, st);
+  const KsSpec* ks = nullptr;
+  int rc = pick_kernel(b, opt, ksj::KIND_OP, &ks);
   if (rc) return rc;
-  rc = ks_launch_op(b->dev, o, x0_dev, out_x_dev, out_status_dev, out_iters_dev, opt ? opt->deadline_s : 0.0, st);
+  rc = batch_setup(b, 0.0, 0.0, st);
+  if (rc) return rc;
+  rc = ks_launch_op(b->dev, o, x0_dev, out_x_dev, out_status_dev, out_iters_dev, opt ? opt->deadline_s : 0.0, st, ks);
   if (rc == -2) { set_error("ks_op: system too large for the dense kernels"); return KS_EUNSUPPORTED; }
+  if (rc && ks) return KS_ECUDA;  // message set by the launcher
   if (rc) { set_error(std::string("op kernel launch failed: ") + cudaGetErrorString(cudaGetLastError())); return KS_ECUDA; }
   return KS_OK;
 }
@@ -244,11 +347,15 @@ extern "C" int ks_tran_async(ks_batch* b, const ks_tran_spec* spec, const ks_opt
   if (!spec->fixed_step && capacity <= 0 && (out_time_dev || out_wave_dev)) { set_error("ks_tran: capacity"); return KS_EINVAL; }
   cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
   KOpts o = make_opts(opt);
-  int rc = batch_setup(b, spec->step, spec->stop, st);
+  const KsSpec* ks = nullptr;
+  int rc = pick_kernel(b, opt, ksj::KIND_TRAN, &ks);
+  if (rc) return rc;
+  rc = batch_setup(b, spec->step, spec->stop, st);
   if (rc) return rc;
   rc = ks_launch_tran(b->dev, o, *spec, capacity, out_time_dev, out_wave_dev, out_npts_dev, out_status_dev,
-                      out_steps_dev, out_iters_dev, opt ? opt->deadline_s : 0.0, st);
+                      out_steps_dev, out_iters_dev, opt ? opt->deadline_s : 0.0, st, ks);
   if (rc == -2) { set_error("ks_tran: system too large for the dense kernels"); return KS_EUNSUPPORTED; }
+  if (rc && ks) return KS_ECUDA;  // message set by the launcher
   if (rc) { set_error(std::string("tran kernel launch failed: ") + cudaGetErrorString(cudaGetLastError())); return KS_ECUDA; }
   return KS_OK;
 }

@@ -16,6 +16,9 @@
 namespace ksg {
 
 #define KS_INF __longlong_as_double(0x7ff0000000000000LL)
+// Element callbacks are inlined at every call: with a per-topology program each
+// call sees its element as constants and the per-thread system stays in registers.
+#define KS_INLINE_LAMBDA __attribute__((always_inline))
 
 constexpr double kQ = 1.602176634e-19;     // device/diode.go:15
 constexpr double kK = 1.380649e-23;        // device/diode.go:16
@@ -95,15 +98,15 @@ __device__ inline double lte_step(const Col& S, int h, double qn, double in, dou
   return k == 2 ? hh * sqrt(allowed / errI) : hh * (allowed / errI);
 }
 
-// pnjlim, device/diode.go:214-226.
-__device__ __forceinline__ double pnjlim(double vnew, double vold, double vt, double vcrit, bool* lim) {
+// pnjlim, device/diode.go:214-226 (rvt = 1/vt).
+__device__ __forceinline__ double pnjlim(double vnew, double vold, double vt, double rvt, double vcrit, bool* lim) {
   if (vnew > vcrit && fabs(vnew - vold) > 2 * vt) {
     *lim = true;
     if (vold > 0) {
-      double arg = 1 + (vnew - vold) / vt;
+      double arg = 1 + (vnew - vold) * rvt;
       return arg > 0 ? vold + vt * log(arg) : vcrit;
     }
-    return vt * log(vnew / vt);
+    return vt * log(vnew * rvt);
   }
   *lim = false;
   return vnew;
@@ -213,18 +216,18 @@ __device__ inline double source_at(const KElem& e, const Col& V, const Col& D, c
 // ---------------------------------------------------------------- diode
 // current, device/diode.go:148-162 (dd: derived block of the diode).
 __device__ inline void diode_iv(const Col& V, const Col& Dv, int p, int dd, bool hasBV, double v, double* id, double* g) {
-  double IS = V[p + KS_D_P_IS], vte = Dv[dd + DD_VTE];
+  double IS = V[p + KS_D_P_IS], vte = Dv[dd + DD_VTE], rvte = Dv[dd + DD_RVTE];
   if (v >= -3 * vte) {
-    double e = exp(fmin(v / vte, 700.0));
-    *id = IS * (e - 1); *g = IS * e / vte; return;
+    double e = exp(fmin(v * rvte, 700.0));
+    *id = IS * (e - 1); *g = IS * e * rvte; return;
   }
   double xbv = Dv[dd + DD_XBV];
   if (!hasBV || v >= -xbv) {
     double a = 3 * vte / (v * kE); a = a * a * a;
     *id = -IS * (1 + a); *g = IS * 3 * a / v; return;
   }
-  double e = exp(fmin(-(xbv + v) / vte, 700.0));
-  *id = -IS * e; *g = IS * e / vte;
+  double e = exp(fmin(-(xbv + v) * rvte, 700.0));
+  *id = -IS * e; *g = IS * e * rvte;
 }
 
 // charge, device/diode.go:191-211.
@@ -246,7 +249,7 @@ __device__ inline void diode_charge(const Col& V, int p, double v, double id, do
 
 // Load, device/diode.go:229-275.
 template <class SY>
-__device__ inline void diode_load(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+__device__ __forceinline__ void diode_load(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
                                   const LoadParams& lp) {
   int p = e.param, dd = e.derived;
   int a = e.u[0], k = e.u[1], ai = e.u[2];
@@ -258,10 +261,11 @@ __device__ inline void diode_load(const KElem& e, const Col& V, const Col& Dv, c
   if (lp.initJct) { vd = vcrit; lim = true; }
   else {
     double vacc = S[SD_VDACC];
-    vd = pnjlim(vraw, vacc, vte, vcrit, &lim);
+    const double rvte = Dv[dd + DD_RVTE];
+    vd = pnjlim(vraw, vacc, vte, rvte, vcrit, &lim);
     if (hasBV && vraw < fmin(0.0, -xbv + 10 * vte)) {
       bool l2;
-      double vt = pnjlim(-(vraw + xbv), -(vacc + xbv), vte, vcrit, &l2);
+      double vt = pnjlim(-(vraw + xbv), -(vacc + xbv), vte, rvte, vcrit, &l2);
       vd = -(vt + xbv); lim = l2;
     }
   }
@@ -289,7 +293,7 @@ __device__ inline void diode_load(const KElem& e, const Col& V, const Col& Dv, c
 
 // ConvTest, device/diode.go:282-289.
 template <class SY>
-__device__ inline bool diode_conv(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+__device__ __forceinline__ bool diode_conv(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
                                   double reltol, double abstol, double gmin) {
   double v = xn_(sys, e.u[2]) - xn_(sys, e.u[1]);
   double cdhat = S[SD_CD] + S[SD_GD] * (v - S[SD_VD]);
@@ -301,7 +305,7 @@ __device__ inline bool diode_conv(const KElem& e, const Col& V, const Col& Dv, c
 
 // Accept, device/diode.go:304-322.
 template <class SY>
-__device__ inline void diode_accept(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+__device__ __forceinline__ void diode_accept(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
                                     double t, int mode) {
   double v = xn_(sys, e.u[2]) - xn_(sys, e.u[1]);
   S[SD_VDACC] = v;
@@ -315,12 +319,12 @@ __device__ inline void diode_accept(const KElem& e, const Col& V, const Col& Dv,
 }
 
 // ---------------------------------------------------------------- BJT
-// junction, device/bjt.go:272-283.
-__device__ __forceinline__ void junction(double is, double v, double nvt, double* i, double* g) {
+// junction, device/bjt.go:272-283 (rnvt = 1/nvt).
+__device__ __forceinline__ void junction(double is, double v, double nvt, double rnvt, double* i, double* g) {
   if (is == 0) { *i = 0; *g = 0; return; }
   if (v >= -3 * nvt) {
-    double e = exp(fmin(v / nvt, 700.0));
-    *i = is * (e - 1); *g = is * e / nvt; return;
+    double e = exp(fmin(v * rnvt, 700.0));
+    *i = is * (e - 1); *g = is * e * rnvt; return;
   }
   double a = 3 * nvt / (v * kE); a = a * a * a;
   *i = -is * (1 + a); *g = is * 3 * a / v;
@@ -328,21 +332,21 @@ __device__ __forceinline__ void junction(double is, double v, double nvt, double
 
 struct BjtDC { double cbe, gbe, cbc, gbc, it, itBE, itBC, ibe, gpi, ibc, gmu, qb, dqbdve, dqbdvc, gx; };
 
-// evalDC, device/bjt.go:294-354.
-__device__ inline BjtDC bjt_eval_dc(const Col& V, const Col& Dv, int p, int dd, double vbe, double vbc, double gmin) {
+// evalDC, device/bjt.go:294-354, with the divisions by per-circuit constants
+// taken from their reciprocals and the three divisions by qb as one.
+__device__ __forceinline__ BjtDC bjt_eval_dc(const Col& V, const Col& Dv, int p, int dd, double vbe, double vbc,
+                                             double gmin) {
   BjtDC d;
   double vt = Dv[dd + DQ_VT];
-  junction(V[p + KS_Q_P_IS], vbe, V[p + KS_Q_P_NF] * vt, &d.cbe, &d.gbe);
+  junction(V[p + KS_Q_P_IS], vbe, V[p + KS_Q_P_NF] * vt, Dv[dd + DQ_RNF], &d.cbe, &d.gbe);
   double cben, gben;
-  junction(V[p + KS_Q_P_ISE], vbe, V[p + KS_Q_P_NE] * vt, &cben, &gben);
+  junction(V[p + KS_Q_P_ISE], vbe, V[p + KS_Q_P_NE] * vt, Dv[dd + DQ_RNE], &cben, &gben);
   cben += gmin * vbe; gben += gmin;
-  junction(V[p + KS_Q_P_IS], vbc, V[p + KS_Q_P_NR] * vt, &d.cbc, &d.gbc);
+  junction(V[p + KS_Q_P_IS], vbc, V[p + KS_Q_P_NR] * vt, Dv[dd + DQ_RNR], &d.cbc, &d.gbc);
   double cbcn, gbcn;
-  junction(V[p + KS_Q_P_ISC], vbc, V[p + KS_Q_P_NC] * vt, &cbcn, &gbcn);
+  junction(V[p + KS_Q_P_ISC], vbc, V[p + KS_Q_P_NC] * vt, Dv[dd + DQ_RNC], &cbcn, &gbcn);
   cbcn += gmin * vbc; gbcn += gmin;
-  double VAF = V[p + KS_Q_P_VAF], VAR = V[p + KS_Q_P_VAR], IKF = V[p + KS_Q_P_IKF], IKR = V[p + KS_Q_P_IKR];
-  double ivaf = VAF > 0 ? 1 / VAF : 0, ivar = VAR > 0 ? 1 / VAR : 0;
-  double oik = IKF > 0 ? 1 / IKF : 0, oikr = IKR > 0 ? 1 / IKR : 0;
+  double ivaf = Dv[dd + DQ_IVAF], ivar = Dv[dd + DQ_IVAR], oik = Dv[dd + DQ_OIK], oikr = Dv[dd + DQ_OIKR];
   double q1 = 1 / (1 - ivaf * vbc - ivar * vbe);
   if (oik == 0 && oikr == 0) {
     d.qb = q1; d.dqbdve = q1 * d.qb * ivar; d.dqbdvc = q1 * d.qb * ivaf;
@@ -350,18 +354,20 @@ __device__ inline BjtDC bjt_eval_dc(const Col& V, const Col& Dv, int p, int dd, 
     double q2 = oik * d.cbe + oikr * d.cbc;
     double arg = fmax(0.0, 1 + 4 * q2);
     double sq = arg != 0 ? sqrt(arg) : 1.0;
+    double rsq = 1 / sq;
     d.qb = q1 * (1 + sq) / 2;
-    d.dqbdve = q1 * (d.qb * ivar + oik * d.gbe / sq);
-    d.dqbdvc = q1 * (d.qb * ivaf + oikr * d.gbc / sq);
+    d.dqbdve = q1 * (d.qb * ivar + oik * d.gbe * rsq);
+    d.dqbdvc = q1 * (d.qb * ivaf + oikr * d.gbc * rsq);
   }
-  d.it = (d.cbe - d.cbc) / d.qb;
-  d.itBE = (d.gbe - d.it * d.dqbdve) / d.qb;
-  d.itBC = (-d.gbc - d.it * d.dqbdvc) / d.qb;
-  double BF = V[p + KS_Q_P_BF], BR = V[p + KS_Q_P_BR];
-  d.ibe = d.cbe / BF + cben; d.gpi = d.gbe / BF + gben;
-  d.ibc = d.cbc / BR + cbcn; d.gmu = d.gbc / BR + gbcn;
+  double rqb = 1 / d.qb;
+  d.it = (d.cbe - d.cbc) * rqb;
+  d.itBE = (d.gbe - d.it * d.dqbdve) * rqb;
+  d.itBC = (-d.gbc - d.it * d.dqbdvc) * rqb;
+  double rBF = Dv[dd + DQ_RBF], rBR = Dv[dd + DQ_RBR];
+  d.ibe = d.cbe * rBF + cben; d.gpi = d.gbe * rBF + gben;
+  d.ibc = d.cbc * rBR + cbcn; d.gmu = d.gbc * rBR + gbcn;
   double rbpr = Dv[dd + DQ_RBPR], rbpi = Dv[dd + DQ_RBPI];
-  double gx = rbpr + rbpi / d.qb;
+  double gx = rbpr + rbpi * rqb;
   double IRB = V[p + KS_Q_P_IRB];
   if (IRB > 0 && rbpi != 0) {
     double cb = d.ibe + d.ibc;
@@ -410,9 +416,10 @@ __device__ inline BjtCh bjt_charges(const Col& V, const Col& Dv, int p, int dd, 
       }
       arg3 = cbe * argtf * ovtf;
     }
-    cbe = cbe * (1 + argtf) / d.qb;
-    gbe = (gbe * (1 + arg2) - cbe * d.dqbdve) / d.qb;
-    ch.dqbeDvbc = TF * (arg3 - cbe * d.dqbdvc) / d.qb;
+    double rqb = 1 / d.qb;
+    cbe = cbe * (1 + argtf) * rqb;
+    gbe = (gbe * (1 + arg2) - cbe * d.dqbdve) * rqb;
+    ch.dqbeDvbc = TF * (arg3 - cbe * d.dqbdvc) * rqb;
   }
   double qd, cd;
   double FC = V[p + KS_Q_P_FC];
@@ -466,7 +473,7 @@ __device__ __forceinline__ void stamp_g(SY& s, int a, int b, double g) {  // dev
 
 // Load + stamp, device/bjt.go:422-515.
 template <class SY>
-__device__ inline void bjt_load(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+__device__ __forceinline__ void bjt_load(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
                                 const LoadParams& lp) {
   int p = e.param, dd = e.derived;
   double vt = Dv[dd + DQ_VT], vcrit = Dv[dd + DQ_VCRIT];
@@ -476,15 +483,16 @@ __device__ inline void bjt_load(const KElem& e, const Col& V, const Col& Dv, con
   if (lp.initJct) { vbe = vcrit; vbc = 0; lim = true; vbx = 0; vcs = 0; }
   else {
     bool l1, l2;
-    vbe = pnjlim(vbe, S[SQ_VBEACC], vt, vcrit, &l1);
-    vbc = pnjlim(vbc, S[SQ_VBCACC], vt, vcrit, &l2);
+    const double rvt = Dv[dd + DQ_RVT];
+    vbe = pnjlim(vbe, S[SQ_VBEACC], vt, rvt, vcrit, &l1);
+    vbc = pnjlim(vbc, S[SQ_VBCACC], vt, rvt, vcrit, &l2);
     lim = l1 || l2;
   }
   S[SQ_VBEACC] = vbe; S[SQ_VBCACC] = vbc;
   S[SQ_VBE] = vbe; S[SQ_VBC] = vbc; S[SQ_VBX] = vbx; S[SQ_VCS] = vcs;
   BjtDC d = bjt_eval_dc(V, Dv, p, dd, vbe, vbc, lp.gmin);
   double isub, gsub;
-  junction(V[p + KS_Q_P_ISS], vcs, V[p + KS_Q_P_NS] * vt, &isub, &gsub);
+  junction(V[p + KS_Q_P_ISS], vcs, V[p + KS_Q_P_NS] * vt, Dv[dd + DQ_RNS], &isub, &gsub);
   isub += lp.gmin * vcs; gsub += lp.gmin;
   S[SQ_CBE] = d.cbe; S[SQ_GBE] = d.gbe; S[SQ_CBC] = d.cbc; S[SQ_GBC] = d.gbc; S[SQ_IT] = d.it;
   S[SQ_ITBE] = d.itBE; S[SQ_ITBC] = d.itBC; S[SQ_IBE] = d.ibe; S[SQ_GPI] = d.gpi; S[SQ_IBC] = d.ibc;
@@ -526,7 +534,7 @@ __device__ inline void bjt_load(const KElem& e, const Col& V, const Col& Dv, con
 
 // ConvTest, device/bjt.go:522-532.
 template <class SY>
-__device__ inline bool bjt_conv(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+__device__ __forceinline__ bool bjt_conv(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
                                 double reltol, double abstol, double gmin) {
   double vbe, vbc, vbx, vcs;
   bjt_voltages<true>(e, sys, &vbe, &vbc, &vbx, &vcs);
@@ -541,7 +549,7 @@ __device__ inline bool bjt_conv(const KElem& e, const Col& V, const Col& Dv, con
 
 // Accept, device/bjt.go:579-601.
 template <class SY>
-__device__ inline void bjt_accept(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+__device__ __forceinline__ void bjt_accept(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
                                   double t, int mode, double gmin) {
   double vbe, vbc, vbx, vcs;
   bjt_voltages<true>(e, sys, &vbe, &vbc, &vbx, &vcs);

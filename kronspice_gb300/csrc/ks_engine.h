@@ -19,6 +19,7 @@ typedef long long int64_t;
 typedef unsigned int uint32_t;
 typedef unsigned long long uint64_t;
 #else
+#include <stddef.h>
 #include <stdint.h>
 #endif
 
@@ -41,14 +42,19 @@ struct KElem {
 // Derived constants per kind (offsets within the element's derived block).
 enum { DR_G = 0, DR_N = 1 };
 enum { DS_A0 = 0, DS_N = 7 };  // resolved waveform arguments a[0..6]
-enum { DD_VTE = 0, DD_VCRIT, DD_XBV, DD_GRS, DD_N };
+// The R* entries are reciprocals of per-circuit constants, so that the Newton
+// loop multiplies where the model equations divide by a parameter.
+enum { DD_VTE = 0, DD_VCRIT, DD_XBV, DD_GRS, DD_RVTE, DD_N };
 enum { DQ_VT = 0, DQ_VCRIT, DQ_RBPR, DQ_RBPI, DQ_GCPR, DQ_GEPR, DQ_OVTF, DQ_F1E, DQ_F2E, DQ_F3E,
-       DQ_F1C, DQ_F2C, DQ_F3C, DQ_N };
+       DQ_F1C, DQ_F2C, DQ_F3C,
+       DQ_RVT, DQ_RNF, DQ_RNE, DQ_RNR, DQ_RNC, DQ_RNS,  // 1/vt, 1/(N* vt)
+       DQ_IVAF, DQ_IVAR, DQ_OIK, DQ_OIKR,             // 1/VAF, 1/VAR, 1/IKF, 1/IKR (0 when not given)
+       DQ_RBF, DQ_RBR, DQ_N };
 enum { DM_VT = 0, DM_LEFF, DM_WEFF, DM_BETA, DM_COX, DM_OXCAP, DM_VBI, DM_VTO, DM_GDPR, DM_GSPR,
        DM_ISD, DM_ISS, DM_VCRITD, DM_VCRITS, DM_CZBD, DM_CZBDSW, DM_CZBS, DM_CZBSSW,
        DM_FBT0, DM_FBT1, DM_FBT2, DM_FSW0, DM_FSW1, DM_FSW2, DM_CGSO, DM_CGDO, DM_CGBO,
        DM_HASJCAP, DM_HASGCAP, DM_XD, DM_ALPHA, DM_CFS, DM_FACTOR, DM_NARROW, DM_ETA3, DM_SQRTPB,
-       DM_HASNSUB, DM_KP, DM_PHI, DM_GAMMA, DM_VTOP, DM_CJ, DM_BAD, DM_N };
+       DM_HASNSUB, DM_KP, DM_PHI, DM_GAMMA, DM_VTOP, DM_CJ, DM_BAD, DM_RVT, DM_N };
 
 // History of accepted charges for LTE (device/lte.go:23-37): t[3], q[3], n.
 enum { H_T0 = 0, H_T1, H_T2, H_Q0, H_Q1, H_Q2, H_N, H_SIZE };
@@ -78,8 +84,19 @@ struct KOpts {
   int32_t no_gmin, no_source, no_pt;
   int32_t mixed;           // FP32 LU + FP64 residual
   int32_t max_iter_total;  // bound on all solves of one circuit (0 = default)
-  int32_t pad;
+  int32_t passes;          // mixed: refinement passes per solve (>= 1)
 };
+
+#ifndef __CUDACC_RTC__
+// Bytes of dynamic shared memory of T per-thread dense systems of n unknowns,
+// behind an element table of ne entries and its is-voltage flags (ne = 0: no
+// table, the per-topology kernels).
+inline size_t ks_sys_smem(int n, int ne, int T) {
+  size_t off = ne ? (size_t)ne * sizeof(KElem) + ((n + 15) / 16) * 16 : 0;
+  size_t per = (size_t)(n * n + 4 * n) * 8 + (size_t)n * 4 + 8 + (size_t)n * n * 4 + 8;
+  return off + per * T;
+}
+#endif
 
 struct KPlan {  // device-side view of a plan
   int32_t n, n_elem, n_values, n_derived, n_state, n_nodes;

@@ -39,8 +39,36 @@ struct KsDeviceBatch {
 
 int ks_launch_transpose(const double* src_rows, double* dst_cols, int64_t rows, int64_t cols, void* stream);
 int ks_launch_setup(const KsDeviceBatch& b, double step, double stop, void* stream);
+struct KsSpec;
+// Launch shape of the persistent kernels: at least this many circuits per thread
+// (KS_CIRCUITS_PER_THREAD, default 1), so that a lane whose circuit converges
+// takes the next one from the queue instead of idling while the rest of its warp
+// iterates.
+int circuits_per_thread();
+// spec: the plan's per-topology kernels, or null for the generic kernels.
 int ks_launch_tran(const KsDeviceBatch& b, const KOpts& o, const ks_tran_spec& spec, int cap, double* out_time,
                    double* out_wave, int32_t* out_npts, int32_t* out_status, int32_t* out_steps, int32_t* out_iters,
-                   double deadline_s, void* stream);
+                   double deadline_s, void* stream, const KsSpec* kspec);
 int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, double* out_x, int32_t* out_status,
-                 int32_t* out_iters, double deadline_s, void* stream);
+                 int32_t* out_iters, double deadline_s, void* stream, const KsSpec* kspec);
+
+// One per-topology kernel of a plan on one device (ks_jit.cpp).
+struct KsSpec {
+  void* fn = nullptr;    // cudaKernel_t of ks_spec_op or ks_spec_tran
+  int T = 0;             // threads per block
+  size_t smem = 0;       // dynamic shared memory per block
+  bool reg = false;      // system in registers (else shared memory)
+  int device = -1;
+  int blocks = 0;        // resident blocks over all SMs
+  double compile_s = 0;  // NVRTC time (0 when the cubin came from a cache)
+  bool from_disk = false;
+  uint64_t key = 0;
+};
+
+namespace ksj {
+enum { KIND_OP = 0, KIND_TRAN = 1 };
+int reg_max();  // largest system the per-topology kernels keep in registers
+std::string source(const ksh::HostPlan& hp, int T, int kind, bool* reg);
+int get(const ksh::HostPlan& hp, int kind, KsSpec* out, std::string* err);
+int launch(void* fn, unsigned grid, int T, size_t smem, void* stream, void** args, std::string* err);
+}  // namespace ksj

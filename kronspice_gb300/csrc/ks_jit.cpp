@@ -1,0 +1,304 @@
+// ks_jit.cpp — per-topology kernels of the GB300 engine.
+//
+// Every circuit of a plan has the same topology, so the element program of the
+// generic kernels (an element table read from shared memory and a kind switch
+// per element per Newton iteration) is known before the batch runs.  For large
+// batches the host writes that program out as CUDA source: each element becomes
+// a compile-time constant KElem, so the kind switch folds away, every unknown
+// index is an immediate, and systems of up to KS_JIT_REG_MAX unknowns live in
+// registers (larger ones in shared memory at constant offsets).  The device code
+// is the same set of templates the generic kernels instantiate (ks_tran.cuh and
+// below, embedded in the library at build time), so both kernels follow the same
+// arithmetic; only the program and the system storage differ.
+//
+// NVRTC compiles the source for the device's own architecture; the cubin is kept
+// in memory per process and on disk (KS_JIT_CACHE_DIR, else
+// $XDG_CACHE_HOME/kronspice_gb300, else ~/.cache/kronspice_gb300; "off" disables)
+// under a hash of the source, the embedded headers, the options and the NVRTC
+// version, and is loaded as a context-independent CUDA library (cudaLibrary_t)
+// whose kernels the runtime launches like any other.
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ks_internal.h"
+
+// Generated at build time from the device headers (kronspice_gb300/build.py).
+extern const int ks_jit_n_headers;
+extern const char* const ks_jit_header_names[];
+extern const char* const ks_jit_header_srcs[];
+
+namespace ksj {
+
+int reg_max() {
+  const char* e = getenv("KS_JIT_REG_MAX");
+  return e ? atoi(e) : 6;
+}
+
+static void append_elem(std::string& s, const KElem& e) {
+  char buf[512];
+  snprintf(buf, sizeof buf, "    { const KElem e{%d, %d, %d, %d, %d, %d, %d, %d, {", e.kind, e.flags, e.level, e.wave,
+           e.nargs, e.param, e.derived, e.state);
+  s += buf;
+  for (int i = 0; i < 10; i++) {
+    snprintf(buf, sizeof buf, "%s%d", i ? ", " : "", e.u[i]);
+    s += buf;
+  }
+  snprintf(buf, sizeof buf, "}, 0x%llxull}; f(e); }\n", (unsigned long long)e.given);
+  s += buf;
+}
+
+std::string source(const ksh::HostPlan& hp, int T, int kind, bool* reg_out) {
+  const int n = hp.n;
+  const bool reg = n <= reg_max();
+  if (reg_out) *reg_out = reg;
+  uint32_t isv = 0;
+  for (int i = 0; i < n; i++)
+    if (hp.is_v[i]) isv |= 1u << i;
+  std::string s;
+  char buf[512];
+  s += "// per-topology kernels: " + std::to_string(hp.n_elem) + " elements, " + std::to_string(n) + " unknowns\n";
+  s += "#include \"ks_tran.cuh\"\nusing namespace ksg;\n\nstruct GenProg {\n";
+  snprintf(buf, sizeof buf,
+           "  static constexpr int ne = %d, n_nodes = %d, n_state = %d;\n"
+           "  static constexpr bool nonlin_empty = %s;\n"
+           "  template <class F>\n  __device__ __forceinline__ void each(F&& f) const {\n",
+           hp.n_elem, hp.n_nodes, hp.n_state, hp.n_nonlin == 0 ? "true" : "false");
+  s += buf;
+  for (const KElem& e : hp.elem) append_elem(s, e);
+  snprintf(buf, sizeof buf,
+           "  }\n  __device__ __forceinline__ bool is_v(int i) const { return (0x%xu >> i) & 1u; }\n};\n\n", isv);
+  s += buf;
+  snprintf(buf, sizeof buf, "#define KS_T %d\n#define KS_N %d\n", T, n);
+  s += buf;
+  if (reg) {
+    s += "typedef RegSys<KS_N> Sys;\n#define KS_BIND(t)\n";
+  } else {
+    s += "typedef SmemSys<KS_T, KS_N> Sys;\n"
+         "#define KS_BIND(t) extern __shared__ __align__(16) unsigned char smem[]; "
+         "smem_layout_static<KS_T, KS_N>(t.s, smem);\n";
+  }
+  if (kind == KIND_OP) s += R"(
+extern "C" __global__ void __launch_bounds__(KS_T)
+ks_spec_op(KOpts o, const double* __restrict__ values, const double* __restrict__ derived, double* state,
+           double* work, int64_t B, const double* __restrict__ x0, double* out_x, int32_t* out_status,
+           int32_t* out_iters, uint64_t deadline_ns, unsigned long long* queue) {
+  Thr<Sys, GenProg> t;
+  KS_BIND(t)
+  t.o = o;
+  op_persistent(t, values, derived, state, work, B, x0, out_x, out_status, out_iters, deadline_ns, queue);
+}
+)";
+  else s += R"(
+extern "C" __global__ void __launch_bounds__(KS_T)
+ks_spec_tran(KOpts o, TranSpecK sp, const double* __restrict__ values, const double* __restrict__ derived,
+             double* state, double* work, int64_t B, double* out_time, double* out_wave, int32_t* out_npts,
+             int32_t* out_status, int32_t* out_steps, int32_t* out_iters, uint64_t deadline_ns,
+             unsigned long long* queue) {
+  Thr<Sys, GenProg> t;
+  KS_BIND(t)
+  t.o = o;
+  tran_persistent(t, sp, values, derived, state, work, B, out_time, out_wave, out_npts, out_status, out_steps,
+                  out_iters, deadline_ns, queue);
+}
+)";
+  return s;
+}
+
+static uint64_t fnv1a(uint64_t h, const void* p, size_t len) {
+  const unsigned char* b = static_cast<const unsigned char*>(p);
+  for (size_t i = 0; i < len; i++) { h ^= b[i]; h *= 1099511628211ull; }
+  return h;
+}
+
+static std::string cache_dir() {
+  const char* d = getenv("KS_JIT_CACHE_DIR");
+  if (d) return strcmp(d, "off") == 0 ? std::string() : std::string(d);
+  const char* x = getenv("XDG_CACHE_HOME");
+  if (x && *x) return std::string(x) + "/kronspice_gb300";
+  const char* h = getenv("HOME");
+  if (h && *h) return std::string(h) + "/.cache/kronspice_gb300";
+  return std::string();
+}
+
+static bool read_file(const std::string& path, std::string* out) {
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) return false;
+  std::string s;
+  char buf[65536];
+  size_t r;
+  while ((r = fread(buf, 1, sizeof buf, f)) > 0) s.append(buf, r);
+  fclose(f);
+  *out = s;
+  return !s.empty();
+}
+
+static void write_file(const std::string& dir, const std::string& path, const std::string& data) {
+  std::string cur;
+  for (size_t i = 1; i <= dir.size(); i++)  // mkdir -p
+    if (i == dir.size() || dir[i] == '/') mkdir(dir.substr(0, i).c_str(), 0755);
+  std::string tmp = path + ".tmp" + std::to_string(getpid());
+  FILE* f = fopen(tmp.c_str(), "wb");
+  if (!f) return;
+  bool ok = fwrite(data.data(), 1, data.size(), f) == data.size();
+  ok = (fclose(f) == 0) && ok;
+  if (ok) rename(tmp.c_str(), path.c_str());
+  else remove(tmp.c_str());
+}
+
+struct Compiled {
+  std::string cubin;
+  double seconds = 0;
+  bool from_disk = false;
+};
+
+static std::mutex g_mu;
+static std::map<uint64_t, Compiled> g_cubins;
+static std::map<uint64_t, cudaLibrary_t> g_libs;
+
+static int compile(const std::string& src, const std::string& arch, uint64_t key, Compiled* out, std::string* err) {
+  std::string dir = cache_dir();
+  char name[64];
+  snprintf(name, sizeof name, "/spec_%016llx_%s.cubin", (unsigned long long)key, arch.c_str());
+  if (!dir.empty() && read_file(dir + name, &out->cubin)) { out->from_disk = true; return 0; }
+  struct timespec t0, t1;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, src.c_str(), "ks_spec.cu", ks_jit_n_headers, ks_jit_header_srcs,
+                         ks_jit_header_names) != NVRTC_SUCCESS) {
+    *err = "nvrtcCreateProgram failed";
+    return -1;
+  }
+  std::string archopt = "--gpu-architecture=" + arch;
+  const char* opts[] = {archopt.c_str(), "-std=c++17", "--generate-line-info", "-DKS_JIT=1"};
+  nvrtcResult rc = nvrtcCompileProgram(prog, 4, opts);
+  if (rc != NVRTC_SUCCESS) {
+    size_t ls = 0;
+    nvrtcGetProgramLogSize(prog, &ls);
+    std::string log(ls, '\0');
+    if (ls) nvrtcGetProgramLog(prog, &log[0]);
+    *err = std::string("NVRTC: ") + nvrtcGetErrorString(rc) + "\n" + log.substr(0, 4000);
+    nvrtcDestroyProgram(&prog);
+    return -1;
+  }
+  size_t cs = 0;
+  nvrtcGetCUBINSize(prog, &cs);
+  out->cubin.resize(cs);
+  if (cs == 0 || nvrtcGetCUBIN(prog, &out->cubin[0]) != NVRTC_SUCCESS) {
+    nvrtcDestroyProgram(&prog);
+    *err = "NVRTC produced no cubin for " + arch;
+    return -1;
+  }
+  nvrtcDestroyProgram(&prog);
+  clock_gettime(CLOCK_MONOTONIC, &t1);
+  out->seconds = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+  if (!dir.empty()) write_file(dir, dir + name, out->cubin);
+  return 0;
+}
+
+static std::string device_arch(int dev, std::string* err) {
+  int major = 0, minor = 0;
+  if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess) {
+    *err = "cannot read the device's compute capability";
+    return std::string();
+  }
+  // architecture-specific targets (sm_90a, sm_100a, sm_103a, ...) from compute capability 9.0 on
+  return "sm_" + std::to_string(major) + std::to_string(minor) + (major >= 9 ? "a" : "");
+}
+
+#define RT_OK(call, what)                                                        \
+  do {                                                                           \
+    cudaError_t r_ = (call);                                                     \
+    if (r_ != cudaSuccess) {                                                     \
+      *err = std::string(what) + ": " + cudaGetErrorString(r_);                  \
+      return -1;                                                                 \
+    }                                                                            \
+  } while (0)
+
+// Per-topology kernel of hp (KIND_OP or KIND_TRAN) for the current device,
+// compiled or loaded once.
+int get(const ksh::HostPlan& hp, int kind, KsSpec* out, std::string* err) {
+  if (hp.n > KS_MAX_DENSE) { *err = "system larger than the thread-per-circuit kernels take"; return -1; }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaFree(0) != cudaSuccess) { *err = "no CUDA device"; return -1; }
+  std::string arch = device_arch(dev, err);
+  if (arch.empty()) return -1;
+  const int T = 64;
+  bool reg = false;
+  std::string src = source(hp, T, kind, &reg);
+  int ver[2] = {0, 0};
+  nvrtcVersion(&ver[0], &ver[1]);
+  uint64_t key = 1469598103934665603ull;
+  key = fnv1a(key, src.data(), src.size());
+  for (int i = 0; i < ks_jit_n_headers; i++) key = fnv1a(key, ks_jit_header_srcs[i], strlen(ks_jit_header_srcs[i]));
+  key = fnv1a(key, ver, sizeof ver);
+  key = fnv1a(key, arch.data(), arch.size());
+
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_cubins.find(key);
+  if (it == g_cubins.end()) {
+    Compiled c;
+    if (compile(src, arch, key, &c, err)) return -1;
+    it = g_cubins.emplace(key, std::move(c)).first;
+  }
+  cudaLibrary_t lib = nullptr;
+  auto li = g_libs.find(key);
+  if (li != g_libs.end()) {
+    lib = li->second;
+  } else {
+    RT_OK(cudaLibraryLoadData(&lib, it->second.cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0),
+          "loading the per-topology kernels");
+    g_libs[key] = lib;
+  }
+  cudaKernel_t k = nullptr;
+  RT_OK(cudaLibraryGetKernel(&k, lib, kind == KIND_OP ? "ks_spec_op" : "ks_spec_tran"), "per-topology kernel");
+  const void* fn = reinterpret_cast<const void*>(k);
+  size_t smem = reg ? 0 : ks_sys_smem(hp.n, 0, T);
+  int maxSmem = 0;
+  cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (smem > (size_t)maxSmem) { *err = "per-thread systems exceed shared memory"; return -1; }
+  RT_OK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "shared memory size");
+  int per = 0, sms = 0;
+  RT_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, T, smem), "occupancy");
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  out->fn = const_cast<void*>(fn);
+  out->T = T;
+  out->smem = smem;
+  out->reg = reg;
+  out->device = dev;
+  out->blocks = sms * (per > 0 ? per : 1);
+  out->compile_s = it->second.seconds;
+  out->from_disk = it->second.from_disk;
+  out->key = key;
+  return 0;
+}
+
+}  // namespace ksj
+
+int circuits_per_thread() {
+  static int v = [] {
+    const char* e = getenv("KS_CIRCUITS_PER_THREAD");
+    int k = e ? atoi(e) : 1;
+    return k < 1 ? 1 : k;
+  }();
+  return v;
+}
+
+namespace ksj {
+
+int launch(void* fn, unsigned grid, int T, size_t smem, void* stream, void** args, std::string* err) {
+  RT_OK(cudaLaunchKernel(fn, dim3(grid), dim3(T), args, smem, (cudaStream_t)stream), "launching a per-topology kernel");
+  return 0;
+}
+
+}  // namespace ksj

@@ -74,6 +74,7 @@ __global__ void k_setup(KPlan plan, const double* __restrict__ values, double* d
         D[d + DD_XBV] = (e.flags & KS_F_HAS_BV) ? breakdown_voltage(IS, V[p + KS_D_P_BV], V[p + KS_D_P_IBV], vt0) : 0.0;
         double RS = V[p + KS_D_P_RS];
         D[d + DD_GRS] = RS > 0 ? 1 / RS : 0.0;
+        D[d + DD_RVTE] = 1 / vte;
         break;
       }
       case KS_ELEM_Q: {
@@ -93,6 +94,19 @@ __global__ void k_setup(KPlan plan, const double* __restrict__ values, double* d
         D[d + DQ_F1C] = vjc * (1 - pow(1 - fc, 1 - mjc)) / (1 - mjc);
         D[d + DQ_F2C] = pow(1 - fc, 1 + mjc);
         D[d + DQ_F3C] = 1 - fc * (1 + mjc);
+        D[d + DQ_RVT] = 1 / vt;
+        D[d + DQ_RNF] = 1 / (V[p + KS_Q_P_NF] * vt);
+        D[d + DQ_RNE] = 1 / (V[p + KS_Q_P_NE] * vt);
+        D[d + DQ_RNR] = 1 / (V[p + KS_Q_P_NR] * vt);
+        D[d + DQ_RNC] = 1 / (V[p + KS_Q_P_NC] * vt);
+        D[d + DQ_RNS] = 1 / (V[p + KS_Q_P_NS] * vt);
+        double VAF = V[p + KS_Q_P_VAF], VAR = V[p + KS_Q_P_VAR], IKF = V[p + KS_Q_P_IKF], IKR = V[p + KS_Q_P_IKR];
+        D[d + DQ_IVAF] = VAF > 0 ? 1 / VAF : 0;
+        D[d + DQ_IVAR] = VAR > 0 ? 1 / VAR : 0;
+        D[d + DQ_OIK] = IKF > 0 ? 1 / IKF : 0;
+        D[d + DQ_OIKR] = IKR > 0 ? 1 / IKR : 0;
+        D[d + DQ_RBF] = 1 / V[p + KS_Q_P_BF];
+        D[d + DQ_RBR] = 1 / V[p + KS_Q_P_BR];
         break;
       }
       case KS_ELEM_M: mos_derive(e, V, D); break;
@@ -135,22 +149,36 @@ static unsigned persistent_grid(K kernel, int T, size_t smem, int64_t B) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, T, smem);
   if (per < 1) per = 1;
-  int64_t need = (B + T - 1) / T;
+  int64_t need = (B + (int64_t)T * circuits_per_thread() - 1) / ((int64_t)T * circuits_per_thread());
   int64_t g = (int64_t)sms * per;
   return (unsigned)(need < g ? need : g);
 }
 
 int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, double* out_x, int32_t* out_status,
-                 int32_t* out_iters, double deadline_s, void* stream) {
+                 int32_t* out_iters, double deadline_s, void* stream, const KsSpec* kspec) {
   int n = b.plan.n, ne = b.plan.n_elem;
   if (n > KS_MAX_DENSE) return -2;
   uint64_t dl = deadline_s > 0 ? (uint64_t)(deadline_s * 1e9) : 0;
+  if (kspec) {  // per-topology kernel of the plan (ks_jit.cpp)
+    if (cudaMemsetAsync(b.queue, 0, sizeof(unsigned long long), (cudaStream_t)stream) != cudaSuccess) return -1;
+    KOpts ko = o;
+    const double *values = b.values, *derived = b.derived;
+    double *state = b.state, *work = b.work;
+    int64_t B = b.B;
+    unsigned long long* queue = b.queue;
+    void* args[] = {&ko, &values, &derived, &state, &work, &B, &x0, &out_x, &out_status, &out_iters, &dl, &queue};
+    int64_t need = (B + (int64_t)kspec->T * circuits_per_thread() - 1) / ((int64_t)kspec->T * circuits_per_thread());
+    unsigned grid = (unsigned)(need < kspec->blocks ? need : kspec->blocks);
+    std::string err;
+    if (ksj::launch(kspec->fn, grid, kspec->T, kspec->smem, stream, args, &err)) { ksh::set_error(err); return -1; }
+    return 0;
+  }
   int maxSmem = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   int T = 64;
-  size_t sm = thr_smem(n, ne, 64);
-  if (sm > (size_t)maxSmem) { T = 32; sm = thr_smem(n, ne, 32); }
+  size_t sm = ks_sys_smem(n, ne, 64);
+  if (sm > (size_t)maxSmem) { T = 32; sm = ks_sys_smem(n, ne, 32); }
   if (sm > (size_t)maxSmem) return -2;
   cudaStream_t st = (cudaStream_t)stream;
   if (cudaMemsetAsync(b.queue, 0, sizeof(unsigned long long), st) != cudaSuccess) return -1;

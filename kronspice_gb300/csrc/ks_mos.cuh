@@ -78,7 +78,7 @@ __device__ inline void mos_derive(const KElem& e, const Col& V, const Col& D) {
     }
   }
   double M = V[p + KS_M_P_MULT];
-  D[d + DM_VT] = vt; D[d + DM_LEFF] = leff; D[d + DM_WEFF] = weff; D[d + DM_COX] = cox;
+  D[d + DM_VT] = vt; D[d + DM_RVT] = 1 / vt; D[d + DM_LEFF] = leff; D[d + DM_WEFF] = weff; D[d + DM_COX] = cox;
   D[d + DM_OXCAP] = cox * leff * weff * M;
   D[d + DM_BETA] = KP * weff / leff * M;
   double vto = typ * VTO;
@@ -454,11 +454,12 @@ __device__ inline void mos_channel(const KElem& e, const Col& V, const Col& D, d
   else ids_level1(D, e.derived, V[e.param + KS_M_P_LAMBDA], vg, vd, vb, o + 1);
 }
 
-// bulkDiode, device/mosfet.go:408-414.
-__device__ __forceinline__ void mos_bulk_diode(double v, double is, double vt, double gmin, double* i, double* g) {
+// bulkDiode, device/mosfet.go:408-414 (rvt = 1/vt).
+__device__ __forceinline__ void mos_bulk_diode(double v, double is, double vt, double rvt, double gmin, double* i,
+                                               double* g) {
   if (v <= -3 * vt) { *i = gmin * v - is; *g = gmin; return; }
-  double ex = exp(fmin(v / vt, 700.0));
-  *i = is * (ex - 1) + gmin * v; *g = is * ex / vt + gmin;
+  double ex = exp(fmin(v * rvt, 700.0));
+  *i = is * (ex - 1) + gmin * v; *g = is * ex * rvt + gmin;
 }
 
 // meyer, device/mosfet.go:419-438.
@@ -517,7 +518,7 @@ __device__ __forceinline__ void mos_branch1(SY& s, double typ, int a, int b, dou
 
 // Load + stamp, device/mosfet.go:476-611.
 template <class SY>
-__device__ inline void mos_load(const KElem& e, const Col& V, const Col& D, const Col& S, SY& sys,
+__device__ __forceinline__ void mos_load(const KElem& e, const Col& V, const Col& D, const Col& S, SY& sys,
                                 const LoadParams& lp) {
   int d = e.derived, p = e.param;
   double vt = D[d + DM_VT];
@@ -538,9 +539,9 @@ __device__ inline void mos_load(const KElem& e, const Col& V, const Col& D, cons
       vds = -limvds(-vds, -avds);
       vgs = vgd + vds;
     }
-    if (vds >= 0) vbs = pnjlim(vbs, avbs, vt, D[d + DM_VCRITS], &lim);
+    if (vds >= 0) vbs = pnjlim(vbs, avbs, vt, D[d + DM_RVT], D[d + DM_VCRITS], &lim);
     else {
-      double vbd = pnjlim(vbs - vds, avbs - avds, vt, D[d + DM_VCRITD], &lim);
+      double vbd = pnjlim(vbs - vds, avbs - avds, vt, D[d + DM_RVT], D[d + DM_VCRITD], &lim);
       vbs = vbd + vds;
     }
   }
@@ -548,8 +549,8 @@ __device__ inline void mos_load(const KElem& e, const Col& V, const Col& D, cons
   S[SM_VGS] = vgs; S[SM_VDS] = vds; S[SM_VBS] = vbs; S[SM_VBD] = vbd; S[SM_VGD] = vgd; S[SM_VGB] = vgb;
   S[SM_AVGS] = vgs; S[SM_AVDS] = vds; S[SM_AVBS] = vbs;
   double cbs, gbs, cbd, gbd;
-  mos_bulk_diode(vbs, D[d + DM_ISS], vt, lp.gmin, &cbs, &gbs);
-  mos_bulk_diode(vbd, D[d + DM_ISD], vt, lp.gmin, &cbd, &gbd);
+  mos_bulk_diode(vbs, D[d + DM_ISS], vt, D[d + DM_RVT], lp.gmin, &cbs, &gbs);
+  mos_bulk_diode(vbd, D[d + DM_ISD], vt, D[d + DM_RVT], lp.gmin, &cbd, &gbd);
   double o[7];
   mos_channel(e, V, D, vgs, vds, vbs, o);
   S[SM_CBS] = cbs; S[SM_GBS] = gbs; S[SM_CBD] = cbd; S[SM_GBD] = gbd;
@@ -604,7 +605,7 @@ __device__ inline void mos_load(const KElem& e, const Col& V, const Col& D, cons
 
 // ConvTest, device/mosfet.go:618-631.
 template <class SY>
-__device__ inline bool mos_conv(const KElem& e, const Col& V, const Col& D, const Col& S, SY& sys,
+__device__ __forceinline__ bool mos_conv(const KElem& e, const Col& V, const Col& D, const Col& S, SY& sys,
                                 double reltol, double abstol, double gmin) {
   int d = e.derived;
   double vgs, vds, vbs, vgb;
@@ -620,8 +621,8 @@ __device__ inline bool mos_conv(const KElem& e, const Col& V, const Col& D, cons
   double ichN = o[0] * o[1];
   double ibsN, ibdN, t;
   double vt = D[d + DM_VT];
-  mos_bulk_diode(vbs, D[d + DM_ISS], vt, gmin, &ibsN, &t);
-  mos_bulk_diode(vbd, D[d + DM_ISD], vt, gmin, &ibdN, &t);
+  mos_bulk_diode(vbs, D[d + DM_ISS], vt, D[d + DM_RVT], gmin, &ibsN, &t);
+  mos_bulk_diode(vbd, D[d + DM_ISD], vt, D[d + DM_RVT], gmin, &ibdN, &t);
   double a1 = ich - ibd, b1 = ichN - ibdN, a2 = ibs + ibd, b2 = ibsN + ibdN;
   return fabs(a1 - b1) <= reltol * fmax(fabs(a1), fabs(b1)) + abstol &&
          fabs(a2 - b2) <= reltol * fmax(fabs(a2), fabs(b2)) + abstol;
@@ -629,7 +630,7 @@ __device__ inline bool mos_conv(const KElem& e, const Col& V, const Col& D, cons
 
 // Accept, device/mosfet.go:668-705.
 template <class SY>
-__device__ inline void mos_accept(const KElem& e, const Col& V, const Col& D, const Col& S, SY& sys,
+__device__ __forceinline__ void mos_accept(const KElem& e, const Col& V, const Col& D, const Col& S, SY& sys,
                                   double t, int mode) {
   int d = e.derived, p = e.param;
   double vgs, vds, vbs, vgb;

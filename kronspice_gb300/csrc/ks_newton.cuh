@@ -39,7 +39,7 @@ struct Thr {
 // Point a thread's SoA columns at circuit c (persistent kernels move a thread
 // from circuit to circuit).
 template <class SY, class P>
-__device__ inline void thr_bind(Thr<SY, P>& t, const double* values, const double* derived, double* state, double* work,
+__device__ __forceinline__ void thr_bind(Thr<SY, P>& t, const double* values, const double* derived, double* state, double* work,
                                 int64_t B, int64_t c) {
   const int n = t.n();
   t.V = Col{const_cast<double*>(values) + c, B};
@@ -91,14 +91,6 @@ __device__ inline void smem_layout_static(SmemSys<T, N>& s, unsigned char* smem)
   s.L_ = reinterpret_cast<float*>(base + (N * N + 4 * N) * T + (N * T + 1) / 2) + tid;
 }
 
-#ifndef __CUDACC_RTC__
-// Bytes of dynamic shared memory smem_layout lays out (ne = 0: smem_layout_static).
-inline size_t thr_smem(int n, int ne, int T) {
-  size_t off = ne ? (size_t)ne * sizeof(KElem) + ((n + 15) / 16) * 16 : 0;
-  size_t per = (size_t)(n * n + 4 * n) * 8 + (size_t)n * 4 + 8 + (size_t)n * n * 4 + 8;
-  return off + per * T;
-}
-#endif
 
 __device__ __forceinline__ void op_state_reset(OpState& st, const KOpts& o) {
   st.phase = PH_MAIN; st.it = 0; st.maxIter = o.itl1; st.total = 0; st.firstErr = 0; st.status = KS_STATUS_NOT_RUN;
@@ -109,7 +101,7 @@ __device__ __forceinline__ void op_state_reset(OpState& st, const KOpts& o) {
 // One (*Sim).solve: stamp at x (copied to xold), add the gmin-stepping and
 // pseudo-transient diagonals, solve.  Returns 0 or the solver error.
 template <class SY, class P>
-__device__ inline int solve_once(Thr<SY, P>& t, OpState& st, LoadParams lp) {
+__device__ __forceinline__ int solve_once(Thr<SY, P>& t, OpState& st, LoadParams lp) {
   SY& s = t.s;
   const int n = t.n();
 #pragma unroll
@@ -133,7 +125,7 @@ __device__ inline int solve_once(Thr<SY, P>& t, OpState& st, LoadParams lp) {
   }
   int err;
   if (!st.fp64) {
-    err = lu_solve_mixed(s);
+    err = lu_solve_mixed(s, t.o.passes);
     if (err == SOLVE_FP32_FAIL) {  // the FP64 path takes over this circuit
       st.fp64 = true;
       err = lu_solve_fp64(s);
@@ -148,7 +140,7 @@ __device__ inline int solve_once(Thr<SY, P>& t, OpState& st, LoadParams lp) {
 // One Newton iteration: a solve plus the bookkeeping of analysis/newton.go:36-57.
 // Returns -1 while the current newton() call goes on, else its result.
 template <class SY, class P>
-__device__ inline int newton_step(Thr<SY, P>& t, OpState& st, const LoadParams& lp) {
+__device__ __forceinline__ int newton_step(Thr<SY, P>& t, OpState& st, const LoadParams& lp) {
   int err = solve_once(t, st, lp);
   int res = -1;
   if (err) res = err;
@@ -183,7 +175,7 @@ __device__ __forceinline__ void x_zero(Thr<SY, P>& t, const Col& also) {
 // dcSolve start, analysis/newton.go:96-102, with applyNodeSet (:221-243) when x0
 // holds a starting point (node voltages; other unknowns start at 0).
 template <class SY, class P>
-__device__ inline void dc_start(Thr<SY, P>& t, OpState& st, const double* x0, int64_t c) {
+__device__ __forceinline__ void dc_start(Thr<SY, P>& t, OpState& st, const double* x0, int64_t c) {
   op_state_reset(st, t.o);
   const int n = t.n();
 #pragma unroll
@@ -200,7 +192,7 @@ __device__ inline void dc_start(Thr<SY, P>& t, OpState& st, const double* x0, in
 // Advance dcSolve with the result of a finished newton() call.  Sets st.phase to
 // PH_DONE and st.status when the DC solve is over.
 template <class SY, class P>
-__device__ inline void dc_advance(Thr<SY, P>& t, OpState& st, int res) {
+__device__ __forceinline__ void dc_advance(Thr<SY, P>& t, OpState& st, int res) {
   const KOpts& o = t.o;
   const int n = t.n();
   bool advance = true;
@@ -316,7 +308,7 @@ __device__ inline void dc_advance(Thr<SY, P>& t, OpState& st, int res) {
 
 // The operating point of one circuit after another, pulled from the queue.
 template <class SY, class P>
-__device__ inline void op_persistent(Thr<SY, P>& t, const double* values, const double* derived, double* state,
+__device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* values, const double* derived, double* state,
                                      double* work, int64_t B, const double* x0, double* out_x, int32_t* out_status,
                                      int32_t* out_iters, uint64_t deadline_ns, unsigned long long* queue) {
   const uint64_t t0 = deadline_ns ? globaltimer_ns() : 0;

@@ -142,7 +142,7 @@ __device__ __forceinline__ void load_all(const P& prog, const Col& Vb, const Col
     for (int j = 0; j < n; j++) s.a(i, j) = 0.0;
     s.rhs(i) = 0.0;
   }
-  prog.each([&](const KElem& e) { elem_load(e, Vb, Db, Sb, s, lp); });
+  prog.each([&](const KElem& e) KS_INLINE_LAMBDA { elem_load(e, Vb, Db, Sb, s, lp); });
 }
 
 // Swap rows k and p (static systems compare p against every later row, so every
@@ -190,46 +190,58 @@ __device__ __forceinline__ void permute(SY& s, Y&& y) {
   }
 }
 
-// Dense LU with partial pivoting in FP64, solver/dense.go:80-177; A is factored in
-// place and x = A^-1 rhs.
+// Magnitude of a double as an integer key: key(a) < key(b) iff |a| < |b| for
+// every non-NaN pair, and keys at or above KS_INF_KEY are infinities and NaNs.
+// The LU's scans for the largest entry and for non-finite entries run on these
+// keys in the integer pipes; GB300's FP64 pipe is kept for the arithmetic.
+#define KS_INF_KEY 0x7ff0000000000000LL
+__device__ __forceinline__ long long mag_key(double x) { return __double_as_longlong(x) & 0x7fffffffffffffffLL; }
+__device__ __forceinline__ double key_mag(long long k) { return __longlong_as_double(k); }
+__device__ __forceinline__ long long key_max(long long a, long long b) { return a > b ? a : b; }
+
+// Largest |a(i,j)| of every column into col(j); returns the key of the largest
+// entry of the matrix (>= KS_INF_KEY: a non-finite entry).
 template <class SY>
-__device__ inline int lu_solve_fp64(SY& s) {
+__device__ __forceinline__ long long column_scales(SY& s) {
   const int n = s.size();
-  double scale = 0;
-  bool bad = false;
-#pragma unroll
-  for (int i = 0; i < n; i++)
-#pragma unroll
-    for (int j = 0; j < n; j++) {
-      double v = s.a(i, j);
-      bad |= !isfinite(v);
-      scale = fmax(scale, fabs(v));
-    }
-  if (bad) return SOLVE_NONFINITE;
-  if (scale == 0) return SOLVE_SINGULAR;
+  long long kall = 0;
 #pragma unroll
   for (int j = 0; j < n; j++) {
-    double m = 0;
+    long long m = 0;
 #pragma unroll
-    for (int i = 0; i < n; i++) m = fmax(m, fabs(s.a(i, j)));
-    s.col(j) = m;
+    for (int i = 0; i < n; i++) m = key_max(m, mag_key(s.a(i, j)));
+    s.col(j) = key_mag(m);
+    kall = key_max(kall, m);
   }
+  return kall;
+}
+
+// Dense LU with partial pivoting in FP64, solver/dense.go:80-177; A is factored in
+// place and x = A^-1 rhs.  Each column divides by its pivot once (a reciprocal,
+// kept in col(k) for the back substitution) instead of once per row.
+template <class SY>
+__device__ __forceinline__ int lu_solve_fp64(SY& s) {
+  const int n = s.size();
+  long long kall = column_scales(s);
+  if (kall >= KS_INF_KEY) return SOLVE_NONFINITE;
+  if (kall == 0) return SOLVE_SINGULAR;
 #pragma unroll
   for (int k = 0; k < n; k++) {
     int p = k;
-    double maxv = fabs(s.a(k, k));
+    long long km = mag_key(s.a(k, k));
 #pragma unroll
     for (int i = k + 1; i < n; i++) {
-      double v = fabs(s.a(i, k));
-      if (v > maxv) { maxv = v; p = i; }
+      long long v = mag_key(s.a(i, k));
+      if (v > km) { km = v; p = i; }
     }
-    if (maxv <= s.col(k) * double(n) * 1e-14) return SOLVE_SINGULAR;
+    if (key_mag(km) <= s.col(k) * double(n) * 1e-14) return SOLVE_SINGULAR;
     s.piv(k) = p;
     swap_rows(s, k, p);
-    double pivot = s.a(k, k);
+    double rp = 1.0 / s.a(k, k);
+    s.col(k) = rp;
 #pragma unroll
     for (int i = k + 1; i < n; i++) {
-      double f = s.a(i, k) / pivot;
+      double f = s.a(i, k) * rp;
       s.a(i, k) = f;
 #pragma unroll
       for (int j = k + 1; j < n; j++) s.a(i, j) -= f * s.a(k, j);
@@ -245,17 +257,16 @@ __device__ inline int lu_solve_fp64(SY& s) {
     for (int j = 0; j < i; j++) acc -= s.a(i, j) * s.xn(j);
     s.xn(i) = acc;
   }
+  long long kx = 0;
 #pragma unroll
   for (int i = n - 1; i >= 0; i--) {
     double acc = s.xn(i);
 #pragma unroll
     for (int j = i + 1; j < n; j++) acc -= s.a(i, j) * s.xn(j);
-    s.xn(i) = acc / s.a(i, i);
+    s.xn(i) = acc * s.col(i);
+    kx = key_max(kx, mag_key(s.xn(i)));
   }
-  bool nf = false;
-#pragma unroll
-  for (int i = 0; i < n; i++) nf |= !isfinite(s.xn(i));
-  return nf ? SOLVE_NONFINITE : SOLVE_OK;
+  return kx >= KS_INF_KEY ? SOLVE_NONFINITE : SOLVE_OK;
 }
 
 // FP32 forward/back substitution with the factor in L32, in place on col().
@@ -280,34 +291,25 @@ __device__ __forceinline__ void lu32_apply_col(SY& s) {
 }
 
 // Mixed precision: FP32 LU with partial pivoting of the FP64 matrix, then
-// x = xold + LU32^-1 (rhs - A*xold) and iterative refinement with the FP64
-// residual rhs - A*x until the correction is at FP64 round-off (at most 6
-// passes).  A and rhs are left intact.  Returns SOLVE_FP32_FAIL when a pivot is
-// below the FP32 threshold or refinement stops contracting above round-off (the
-// caller then solves in FP64).
+// x = xold + LU32^-1 (rhs - A*xold) with the residual in FP64, repeated as
+// iterative refinement (x += LU32^-1 (rhs - A*x)) until the correction is below
+// 1e-11 of the solution (five orders under the tightest Newton tolerance the
+// analyses use), for at most `passes` passes.  A and rhs are left intact.
+// Returns SOLVE_FP32_FAIL when a pivot is below the FP32 threshold or the
+// refinement stops contracting (the caller then solves in FP64), so a system
+// too ill-conditioned for FP32 factors never yields an unrefined step.  One pass
+// (passes = 1) skips both checks: each Newton step is then the FP32 solve of the
+// FP64 residual, for well-conditioned systems only.
 template <class SY>
-__device__ inline int lu_solve_mixed(SY& s) {
+__device__ __forceinline__ int lu_solve_mixed(SY& s, int passes) {
   const int n = s.size();
-  double scale = 0;
-  bool bad = false;
+  long long kall = column_scales(s);
+  if (kall >= KS_INF_KEY) return SOLVE_NONFINITE;
+  if (kall == 0) return SOLVE_SINGULAR;
 #pragma unroll
   for (int i = 0; i < n; i++)
 #pragma unroll
-    for (int j = 0; j < n; j++) {
-      double v = s.a(i, j);
-      bad |= !isfinite(v);
-      scale = fmax(scale, fabs(v));
-      s.l(i, j) = (float)v;
-    }
-  if (bad) return SOLVE_NONFINITE;
-  if (scale == 0) return SOLVE_SINGULAR;
-#pragma unroll
-  for (int j = 0; j < n; j++) {
-    double m = 0;
-#pragma unroll
-    for (int i = 0; i < n; i++) m = fmax(m, fabs(s.a(i, j)));
-    s.col(j) = m;
-  }
+    for (int j = 0; j < n; j++) s.l(i, j) = (float)s.a(i, j);
 #pragma unroll
   for (int k = 0; k < n; k++) {
     int p = k;
@@ -332,7 +334,7 @@ __device__ inline int lu_solve_mixed(SY& s) {
 #pragma unroll
   for (int i = 0; i < n; i++) s.xn(i) = s.xo(i);
   double prev = KS_INF;
-  for (int pass = 0; pass < 6; pass++) {
+  for (int pass = 0; pass < passes; pass++) {
 #pragma unroll
     for (int i = 0; i < n; i++) {  // FP64 residual in col()
       double r = s.rhs(i);
@@ -341,22 +343,19 @@ __device__ inline int lu_solve_mixed(SY& s) {
       s.col(i) = r;
     }
     lu32_apply_col(s);
-    double dmax = 0, xmax = 0;
-    bool nf = false;
+    long long kd = 0, kx = 0;
 #pragma unroll
     for (int i = 0; i < n; i++) {
       double v = s.xn(i) + s.col(i);
-      nf |= !isfinite(v);
       s.xn(i) = v;
-      dmax = fmax(dmax, fabs(s.col(i)));
-      xmax = fmax(xmax, fabs(v));
+      kd = key_max(kd, mag_key(s.col(i)));
+      kx = key_max(kx, mag_key(v));
     }
-    if (nf) return SOLVE_NONFINITE;
-    if (dmax <= 4e-16 * xmax || dmax == 0) break;
-    if (pass > 0 && dmax > 0.5 * prev) {  // refinement stopped contracting
-      if (dmax <= 1e-11 * xmax) break;      // at the round-off floor of this system
-      return SOLVE_FP32_FAIL;
-    }
+    if (kx >= KS_INF_KEY || kd >= KS_INF_KEY) return SOLVE_NONFINITE;
+    double dmax = key_mag(kd), xmax = key_mag(kx);
+    if (dmax <= 1e-11 * xmax || dmax == 0) break;
+    if (pass > 0 && dmax > 0.5 * prev) return SOLVE_FP32_FAIL;  // refinement stopped contracting
+    if (pass == passes - 1 && passes > 1) return SOLVE_FP32_FAIL;  // not refined within the passes
     prev = dmax;
   }
   return SOLVE_OK;
@@ -364,10 +363,10 @@ __device__ inline int lu_solve_mixed(SY& s) {
 
 // converged, analysis/newton.go:59-82.
 template <class SY, class P>
-__device__ inline bool converged(const P& prog, const Col& Vb, const Col& Db, const Col& Sb, SY& s, const KOpts& o,
+__device__ __forceinline__ bool converged(const P& prog, const Col& Vb, const Col& Db, const Col& Sb, SY& s, const KOpts& o,
                                  double gmin) {
   bool lim = false;
-  prog.each([&](const KElem& e) {
+  prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
     int ls = lim_slot(e.kind);
     if (ls >= 0 && Sb[e.state + ls] != 0) lim = true;
   });
@@ -377,12 +376,12 @@ __device__ inline bool converged(const P& prog, const Col& Vb, const Col& Db, co
 #pragma unroll
   for (int i = 0; i < n; i++) {
     double x = s.xn(i), old = s.xo(i);
-    double tol = (prog.is_v(i) ? o.vntol : o.abstol) + o.reltol * fmax(fabs(x), fabs(old));
+    double tol = (prog.is_v(i) ? o.vntol : o.abstol) + o.reltol * key_mag(key_max(mag_key(x), mag_key(old)));
     moved |= fabs(x - old) > tol;
   }
   if (moved) return false;
   bool ok = true;
-  prog.each([&](const KElem& e) {
+  prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
     if (!ok) return;
     Col S = state_col(Sb, e);
     if (e.kind == KS_ELEM_D) ok = diode_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
@@ -394,9 +393,9 @@ __device__ inline bool converged(const P& prog, const Col& Vb, const Col& Db, co
 
 // Accept every element at the new iterate (analysis/op.go:324-328).
 template <class SY, class P>
-__device__ inline void accept_all(const P& prog, const Col& Vb, const Col& Db, const Col& Sb, SY& s, double t,
+__device__ __forceinline__ void accept_all(const P& prog, const Col& Vb, const Col& Db, const Col& Sb, SY& s, double t,
                                   int mode, double gmin, bool nonlinOnly) {
-  prog.each([&](const KElem& e) {
+  prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
     Col S = state_col(Sb, e);
     switch (e.kind) {
       case KS_ELEM_C: {  // device/reactive.go:144-161
@@ -429,7 +428,7 @@ __device__ inline void accept_all(const P& prog, const Col& Vb, const Col& Db, c
 template <class P>
 __device__ inline void init_state(const P& prog, const Col& Db, const Col& Sb) {
   for (int k = 0; k < prog.n_state; k++) Sb[k] = 0.0;
-  prog.each([&](const KElem& e) {
+  prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
     if (e.kind == KS_ELEM_M) Sb[e.state + SM_AVON] = Db[e.derived + DM_VTO];
   });
 }

@@ -22,7 +22,7 @@ __global__ void __launch_bounds__(T) k_tran(KPlan plan, KOpts o, TranSpecK sp, c
 
 int ks_launch_tran(const KsDeviceBatch& b, const KOpts& o, const ks_tran_spec& spec, int cap, double* out_time,
                    double* out_wave, int32_t* out_npts, int32_t* out_status, int32_t* out_steps, int32_t* out_iters,
-                   double deadline_s, void* stream) {
+                   double deadline_s, void* stream, const KsSpec* kspec) {
   int n = b.plan.n, ne = b.plan.n_elem;
   if (n > KS_MAX_DENSE) return -2;
   TranSpecK sp;
@@ -40,12 +40,27 @@ int ks_launch_tran(const KsDeviceBatch& b, const KOpts& o, const ks_tran_spec& s
   sp.cap = cap;
   sp.npts = (int)llround(spec.stop / spec.step) + 1;
   uint64_t dl = deadline_s > 0 ? (uint64_t)(deadline_s * 1e9) : 0;
+  if (kspec) {  // per-topology kernel of the plan (ks_jit.cpp)
+    if (cudaMemsetAsync(b.queue, 0, sizeof(unsigned long long), (cudaStream_t)stream) != cudaSuccess) return -1;
+    KOpts ko = o;
+    const double *values = b.values, *derived = b.derived;
+    double *state = b.state, *work = b.work;
+    int64_t B = b.B;
+    unsigned long long* queue = b.queue;
+    void* args[] = {&ko, &sp, &values, &derived, &state, &work, &B, &out_time, &out_wave, &out_npts,
+                    &out_status, &out_steps, &out_iters, &dl, &queue};
+    int64_t need = (B + (int64_t)kspec->T * circuits_per_thread() - 1) / ((int64_t)kspec->T * circuits_per_thread());
+    unsigned grid = (unsigned)(need < kspec->blocks ? need : kspec->blocks);
+    std::string err;
+    if (ksj::launch(kspec->fn, grid, kspec->T, kspec->smem, stream, args, &err)) { ksh::set_error(err); return -1; }
+    return 0;
+  }
   int maxSmem = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   int T = 64;
-  size_t sm = thr_smem(n, ne, 64);
-  if (sm > (size_t)maxSmem) { T = 32; sm = thr_smem(n, ne, 32); }
+  size_t sm = ks_sys_smem(n, ne, 64);
+  if (sm > (size_t)maxSmem) { T = 32; sm = ks_sys_smem(n, ne, 32); }
   if (sm > (size_t)maxSmem) return -2;
   cudaStream_t st = (cudaStream_t)stream;
   if (cudaMemsetAsync(b.queue, 0, sizeof(unsigned long long), st) != cudaSuccess) return -1;
@@ -58,7 +73,7 @@ int ks_launch_tran(const KsDeviceBatch& b, const KOpts& o, const ks_tran_spec& s
     cudaFuncSetAttribute(k_tran<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tran<32>, 32, sm);
   }
-  int64_t need = (b.B + T - 1) / T, cap_blocks = (int64_t)sms * (per > 0 ? per : 1);
+  int64_t need = (b.B + (int64_t)T * circuits_per_thread() - 1) / ((int64_t)T * circuits_per_thread()), cap_blocks = (int64_t)sms * (per > 0 ? per : 1);
   unsigned grid = (unsigned)(need < cap_blocks ? need : cap_blocks);
   if (T == 64)
     k_tran<64><<<grid, 64, sm, st>>>(b.plan, o, sp, b.values, b.derived, b.state, b.work, b.B, out_time, out_wave,

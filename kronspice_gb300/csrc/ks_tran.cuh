@@ -17,10 +17,10 @@ namespace ksg {
 // (device/reactive.go:178-181, :346-349; device/diode.go:388-397; BJT and
 // MOSFET Truncate in device/bjt.go and device/mosfet.go:734-757).
 template <class SY, class P>
-__device__ double truncate_all(Thr<SY, P>& t, const TruncParams& tc) {
+__device__ __forceinline__ double truncate_all(Thr<SY, P>& t, const TruncParams& tc) {
   double prop = KS_INF;
   SY& x = t.s;
-  t.prog.each([&](const KElem& e) {
+  t.prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
     Col S = state_col(t.Sb, e);
     switch (e.kind) {
       case KS_ELEM_C: {
@@ -87,9 +87,9 @@ __device__ double truncate_all(Thr<SY, P>& t, const TruncParams& tc) {
 
 // (*Sim).nextBreakpoint, analysis/tran.go:233-243.
 template <class SY, class P>
-__device__ double next_breakpoint(Thr<SY, P>& t, double tnow) {
+__device__ __forceinline__ double next_breakpoint(Thr<SY, P>& t, double tnow) {
   double nb = KS_INF;
-  t.prog.each([&](const KElem& e) {
+  t.prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
     if ((e.kind == KS_ELEM_V || e.kind == KS_ELEM_I) && e.wave != KS_WAVE_NONE)
       nb = fmin(nb, wave_next_breakpoint(e.wave, t.D, e.derived, t.V, e.param + KS_SRC_P_ARGS, e.nargs, tnow));
   });
@@ -98,8 +98,8 @@ __device__ double next_breakpoint(Thr<SY, P>& t, double tnow) {
 
 // C and L initial conditions for UIC (device/reactive.go:298-303, :466-471).
 template <class SY, class P>
-__device__ void set_initial_conditions(Thr<SY, P>& t) {
-  t.prog.each([&](const KElem& e) {
+__device__ __forceinline__ void set_initial_conditions(Thr<SY, P>& t) {
+  t.prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
     Col S = state_col(t.Sb, e);
     bool has = e.flags & KS_F_HAS_IC;
     if (e.kind == KS_ELEM_C) { S[SC_VPREV] = has ? t.V[e.param + KS_RCL_P_IC] : 0.0; S[SC_IPREV] = 0; }
@@ -115,7 +115,7 @@ struct TranSpecK {
 };
 
 template <class SY, class P>
-__device__ inline void record(Thr<SY, P>& t, const TranSpecK& sp, int64_t c, int64_t B, double tnow, int kgrid, int* npts,
+__device__ __forceinline__ void record(Thr<SY, P>& t, const TranSpecK& sp, int64_t c, int64_t B, double tnow, int kgrid, int* npts,
                               double* out_time, double* out_wave) {
   const int n = t.n();
   if (sp.fixed) {
@@ -139,7 +139,7 @@ __device__ inline void record(Thr<SY, P>& t, const TranSpecK& sp, int64_t c, int
 
 // analysis.Tran of one circuit after another, pulled from the queue.
 template <class SY, class P>
-__device__ inline void tran_persistent(Thr<SY, P>& t, const TranSpecK& sp, const double* values, const double* derived,
+__device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& sp, const double* values, const double* derived,
                                        double* state, double* work, int64_t B, double* out_time, double* out_wave,
                                        int32_t* out_npts, int32_t* out_status, int32_t* out_steps, int32_t* out_iters,
                                        uint64_t deadline_ns, unsigned long long* queue) {

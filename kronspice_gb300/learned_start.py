@@ -9,6 +9,8 @@ from the prediction, corrects it, and the usual gmin / source-stepping chain
 takes over for any circuit whose Newton from the prediction fails.
 """
 import ctypes
+import json
+import os
 import time
 
 import numpy as np
@@ -74,6 +76,7 @@ class MLP:
         self._io = [np.ascontiguousarray(a, dtype=d) for a, d in
                     ((cols, np.int32), (fmean, np.float32), (fstd, np.float32), (tmean, np.float32), (tstd, np.float32))]
         c, fm, fs, tm, ts = self._io
+        self._logmask, self._scale_col = int(logmask), int(scale_col)
         analysis._check(self.L.ks_mlp_set_io(self.handle, c.ctypes.data, int(logmask), fm.ctypes.data, fs.ctypes.data,
                                              tm.ctypes.data, ts.ctypes.data, int(scale_col)), "ks_mlp_set_io")
 
@@ -126,6 +129,27 @@ class LearnedStart:
     def predict(self, stream):
         self.mlp.predict(self.batch, self.x0.data_ptr(), ctypes.c_void_p(stream.cuda_stream))
         return self.x0
+
+    def save(self, path):
+        """The trained network and its input/output normalisation (.npz)."""
+        c, fm, fs, tm, ts = self.mlp._io
+        np.savez(path, params=self.mlp.get_params(), dims=np.array([self.mlp.in_dim, self.mlp.hidden,
+                                                                   self.mlp.out_dim]),
+                 cols=c, fmean=fm, fstd=fs, tmean=tm, tstd=ts,
+                 io=np.array([self.mlp._logmask, self.mlp._scale_col]), info=json.dumps(self.info))
+
+    @classmethod
+    def load(cls, path, batch, device):
+        import torch
+        z = np.load(path)
+        i, h, o = (int(v) for v in z["dims"])
+        mlp = MLP(i, o, h, seed=7)
+        logmask, scale_col = (int(v) for v in z["io"])
+        mlp.set_io(z["cols"], logmask, z["fmean"], z["fstd"], z["tmean"], z["tstd"], scale_col)
+        mlp.set_params(z["params"])
+        x0 = torch.zeros((batch.n_circ, batch.plan.n), dtype=torch.float64, device=device)
+        info = dict(json.loads(str(z["info"])), loaded_from=os.path.basename(path))
+        return cls(mlp, batch, x0, info)
 
 
 def train_for(name, el, nn, vals, batch, device, n_train=131072, epochs=40, mb=2048, lr=2e-3, seed=1000,
@@ -180,7 +204,13 @@ def train_for(name, el, nn, vals, batch, device, n_train=131072, epochs=40, mb=2
     return LearnedStart(mlp, batch, x0, info)
 
 
-def for_workload(name, el, nn, vals, batch, device):
-    """The bench's learned start: 1,048,576 plain-solver operating points."""
-    return train_for(name, el, nn, vals, batch, device, n_train=1 << 20, epochs=60 if name == "bjt_ce" else 40,
-                     mb=4096, lr=2e-3)
+def for_workload(name, el, nn, vals, batch, device, cache=None):
+    """The bench's learned start: 1,048,576 plain-solver operating points (or the
+    network saved at `cache` by an earlier run, which it saves otherwise)."""
+    if cache and os.path.exists(cache):
+        return LearnedStart.load(cache, batch, device)
+    ls = train_for(name, el, nn, vals, batch, device, n_train=1 << 20, epochs=60 if name == "bjt_ce" else 40,
+                   mb=4096, lr=2e-3)
+    if cache:
+        ls.save(cache)
+    return ls

@@ -117,3 +117,38 @@ def test_workload_batches_are_seeded():
     _, _, v3 = w.bjt_ce_batch(64, 4)
     assert np.array_equal(v1, v2) and not np.array_equal(v1, v3)
     assert v1.shape == (64, len(w.bjt_ce_template().pack()[1]))
+
+
+def test_per_topology_source_on_cpu():
+    """The per-topology source is host work (no GPU): one constant element per
+    element of the plan, registers up to 6 unknowns, shared memory above."""
+    from kronspice_gb300 import analysis, workloads
+    el, nn, vals = workloads.bjt_ce_batch(2, seed=1)
+    plan = analysis.Plan(el, nn, vals.shape[1])
+    src = plan.kernel_source("op")
+    assert src.count("const KElem e{") == len(el)
+    assert "RegSys<KS_N>" in src and "ks_spec_op" in src and "ks_spec_tran" not in src
+    el2, nn2, vals2 = workloads.rc_ladder_batch(2, seed=1, sections=10)
+    plan2 = analysis.Plan(el2, nn2, vals2.shape[1])
+    src2 = plan2.kernel_source("tran")
+    assert "SmemSys<KS_T, KS_N>" in src2 and "ks_spec_tran" in src2 and "#define KS_N 12" in src2
+
+
+def test_per_topology_source_compiles_with_nvrtc():
+    """The generated source with the device headers as the library embeds them
+    compiles under NVRTC for sm_103a (no GPU needed)."""
+    nvrtc = pytest.importorskip("cuda.bindings.nvrtc")
+    from kronspice_gb300 import analysis, build, workloads
+    el, nn, vals = workloads.rc_ladder_batch(2, seed=1, sections=3)
+    src = analysis.Plan(el, nn, vals.shape[1]).kernel_source("op")
+    names = [n.encode() for n, _ in build.JIT_HEADERS]
+    heads = [open(os.path.join(build.CSRC, rel), "rb").read() for _, rel in build.JIT_HEADERS]
+    err, prog = nvrtc.nvrtcCreateProgram(src.encode(), b"ks_spec.cu", len(names), heads, names)
+    opts = [b"--gpu-architecture=sm_103a", b"-std=c++17", b"-DKS_JIT=1"]
+    (rc,) = nvrtc.nvrtcCompileProgram(prog, len(opts), opts)
+    _, ls = nvrtc.nvrtcGetProgramLogSize(prog)
+    log = b" " * ls
+    nvrtc.nvrtcGetProgramLog(prog, log)
+    assert rc == nvrtc.nvrtcResult.NVRTC_SUCCESS, log.decode()[:2000]
+    _, size = nvrtc.nvrtcGetCUBINSize(prog)
+    assert size > 0

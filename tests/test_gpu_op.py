@@ -42,10 +42,12 @@ def run_both(el, nn, vals, opt_gpu, opt_cpu, x0=None):
     return (xg, sg, ig), (xo, so, io), isv
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_bjt_ce_batch_matches_oracle(precision):
+@pytest.mark.parametrize("precision,passes", [("fp64", 0), ("mixed", 0), ("mixed", 1)])
+def test_bjt_ce_batch_matches_oracle(precision, passes):
+    """mixed: every linear solve refined from the FP64 residual (default), or one
+    unchecked pass per Newton step (passes=1, well-conditioned systems)."""
     el, nn, vals = workloads.bjt_ce_batch(4096, seed=11)
-    og = analysis.Options(reltol=RELTOL, precision=precision)
+    og = analysis.Options(reltol=RELTOL, precision=precision, mixed_passes=passes)
     oc = orc.options(reltol=RELTOL)
     (xg, sg, ig), (xo, so, io), isv = run_both(el, nn, vals, og, oc)
     assert np.array_equal(sg, so), np.nonzero(sg != so)
@@ -158,11 +160,11 @@ def test_fallback_chain_matches_oracle():
         assert np.all(np.abs(xg[ok] - xo[ok]) <= tol(xo[ok], isv, 1e-3))
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_cmos_opamp_batch_matches_oracle(precision):
+@pytest.mark.parametrize("precision,passes", [("fp64", 0), ("mixed", 0)])
+def test_cmos_opamp_batch_matches_oracle(precision, passes):
     """Level-1 two-stage op-amp variants (the 24-D parameter workload)."""
     el, nn, vals = workloads.cmos_opamp_batch(2048, seed=13)
-    og = analysis.Options(reltol=RELTOL, precision=precision)
+    og = analysis.Options(reltol=RELTOL, precision=precision, mixed_passes=passes)
     oc = orc.options(reltol=RELTOL)
     (xg, sg, ig), (xo, so, io), isv = run_both(el, nn, vals, og, oc)
     assert np.array_equal(sg, so), np.nonzero(sg != so)
