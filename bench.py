@@ -237,14 +237,16 @@ def main():
         times = []
         for _ in range(args.steps):
             flush.fill_(1.0)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0, em, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
             e0.record(stream)
             x0 = learned.predict(stream) if (with_start and learned) else None
+            em.record(stream)
             step(opt, x0)
             e1.record(stream)
-            times.append((e0, e1))
+            times.append((e0, em, e1))
         torch.cuda.synchronize()
-        ms = [a.elapsed_time(b) for a, b in times]
+        ms = [a.elapsed_time(c) for a, b, c in times]
+        op_ms = [b.elapsed_time(c) for a, b, c in times]
         total = sum(ms) / 1e3
         if world > 1:
             t = torch.tensor([total], device=dev)
@@ -253,6 +255,7 @@ def main():
         st = st_dev.cpu().numpy()
         it = it_dev.cpu().numpy()
         return {"seconds": total, "ms_per_step": total / args.steps * 1e3, "ok": int((st == 0).sum()),
+                "op_kernel_s": sum(op_ms) / 1e3 / args.steps,
                 "iters_mean": float(it.mean()), "iters_max": int(it.max()), "launches": launches * args.steps,
                 "x": x_dev.cpu().numpy(), "status": st}
 
@@ -346,8 +349,11 @@ def main():
     max_err = float(np.max(np.abs(chosen["x"][:samp][okm, :nn - 1] - xo[okm, :nn - 1]))) if okm.any() else None
     cpu = cpu_baseline(el, nn, vals)
 
-    per_launch_s = chosen["seconds"] / args.steps
-    achieved = WORKLOADS[args.workload][1] * B / per_launch_s / 1e9
+    per_launch_s = chosen["op_kernel_s"]  # the operating-point kernel alone (events around its launch)
+    # algorithmic bytes of one solve: its value vector in, its solution, status and iteration count out
+    nv = vals.shape[1]
+    alg_bytes = (nv + n) * 8 + 8
+    achieved = alg_bytes * B / per_launch_s / 1e9
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -355,7 +361,8 @@ def main():
     except OSError:
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
-    prof = traffic_from_profile().get("k_op_%s" % args.workload, {})
+    prof = traffic_from_profile().get("%s_%s" % ("ks_spec_op" if chosen_opt.kernel == "specialized" else "k_op",
+                                                 args.workload), {})
     traffic = prof.get("dram_bytes_per_circuit")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -381,9 +388,12 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "traffic": None if traffic is None else traffic * B,
-                     "note": "k_op is latency bound (FP64 dependency chains, one circuit per thread), not HBM bound: "
-                             "achieved counts the compulsory %d B/solve, peak is the measured copy bandwidth"
-                             % WORKLOADS[args.workload][1]},
+                     "kernel": "ks_spec_op" if chosen_opt.kernel == "specialized" else "k_op",
+                     "algorithmic_bytes_per_solve": alg_bytes, "kernel_ms": per_launch_s * 1e3,
+                     "note": "the operating-point kernel is bound by FP64 issue (GB300: 2 FP64 lanes/clk/SM; one "
+                             "circuit per thread), not by HBM: achieved counts the value vector in and the "
+                             "solution out per solve over the launch's event time, peak is the measured copy "
+                             "bandwidth"},
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
