@@ -261,6 +261,25 @@ int ks_batch_create(ks_plan* plan, int32_t n_circ, const double* values, ks_batc
 int ks_batch_set_values(ks_batch* b, const double* values, int values_are_device, void* stream);
 /* KS_KERNEL_* that ran the batch's last analysis (-1 before the first). */
 int ks_batch_last_kernel(const ks_batch* b);
+
+/* ---- operating point without device allocation --------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they solve (a memory pool or arena that owns the device, a path
+ * where an allocation could synchronise the device or fail under pressure):
+ * ks_op for n_circ circuits of one topology with every intermediate array in a
+ * fixed scratch area of KS_NOALLOC_SCRATCH_BYTES that the library holds on each
+ * GPU that loads it, and no cudaMalloc / cudaFree.  values_dev: device memory
+ * [n_circ][n_values] row-major; out_x_dev [n_circ][n], out_status_dev and
+ * out_iters_dev [n_circ]: device memory.  Returns KS_EINVAL when the batch needs
+ * more scratch than that (ks_op_noalloc_scratch_bytes gives the need).  Runs the
+ * generic kernel, standard start.  All calls share the scratch: calls that
+ * overlap on the GPU race.  The first call on a device looks up the scratch
+ * address; make it before any stream capture.  It returns once the element
+ * table is on the device; the solve runs on `stream`. */
+#define KS_NOALLOC_SCRATCH_BYTES (64u << 20)
+int ks_op_noalloc(const ks_topology* topo, int32_t n_circ, const double* values_dev, const ks_options* opt,
+                  double* out_x_dev, int32_t* out_status_dev, int32_t* out_iters_dev, void* stream);
+int ks_op_noalloc_scratch_bytes(const ks_topology* topo, int32_t n_circ, size_t* bytes);
 void ks_batch_destroy(ks_batch* b);
 
 /*

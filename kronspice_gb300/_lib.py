@@ -35,7 +35,7 @@ class KsTranSpec(ctypes.Structure):
 EXPORTS = ["ks_version", "ks_last_error", "ks_validate", "ks_unknowns", "ks_plan_create", "ks_plan_destroy",
            "ks_plan_info", "ks_batch_create", "ks_batch_set_values", "ks_batch_destroy", "ks_op", "ks_op_async",
            "ks_tran", "ks_tran_async", "ks_tran_points", "ks_plan_specialize", "ks_plan_kernel_source",
-           "ks_batch_last_kernel"]
+           "ks_batch_last_kernel", "ks_op_noalloc", "ks_op_noalloc_scratch_bytes"]
 
 _lib = None
 
@@ -77,6 +77,8 @@ def load(build_if_missing=False):
     L.ks_plan_specialize.argtypes = [P, ctypes.c_int32, P, P]
     L.ks_plan_kernel_source.argtypes = [P, ctypes.c_int32, ctypes.c_char_p, ctypes.c_size_t, P]
     L.ks_batch_last_kernel.argtypes = [P]
+    L.ks_op_noalloc.argtypes = [P, ctypes.c_int32, P, P, P, P, P, P]
+    L.ks_op_noalloc_scratch_bytes.argtypes = [P, ctypes.c_int32, P]
     _lib = L
     return L
 

@@ -84,6 +84,9 @@ static KOpts make_opts(const ks_options* o) {  // analysis/op.go:91-110
   return k;
 }
 
+// The options as the kernels read them, for the other translation units.
+KOpts ks_kopts_from(const ks_options* o) { return make_opts(o); }
+
 extern "C" int ks_plan_create(const ks_topology* topo, ks_plan** out) {
   if (!topo || !out) { set_error("ks_plan_create: null argument"); return KS_EINVAL; }
   ks_plan* p = new ks_plan();
