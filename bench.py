@@ -35,12 +35,16 @@ METRIC = "converged circuit solves/s @ SPICE reltol, chosen vs plain GPU; Newton
 UNIT = "solves/s"
 RELTOL = 1e-6
 # workload -> (default circuits, compulsory bytes per solve: parameters in + node voltages out, 8 B each)
-WORKLOADS = {"bjt_ce": (16384, (7 + 5) * 8), "cmos_opamp": (65536, (24 + 7) * 8)}
+WORKLOADS = {"bjt_ce": (16384, (7 + 5) * 8), "cmos_opamp": (65536, (24 + 7) * 8), "rc_ladder": (4096, 0)}
+# transient workloads: unit of work = one accepted time point of one circuit
+TRAN_UNIT = "accepted time points/s"
+RC_LADDER_SPEC = dict(step=10e-9, stop=10e-6, fixed_step=True, method="trap")  # 1,000 TRAP steps of 10 ns
 
 
 def generator(name):
     from kronspice_gb300 import workloads
-    return {"bjt_ce": workloads.bjt_ce_batch, "cmos_opamp": workloads.cmos_opamp_batch}[name]
+    return {"bjt_ce": workloads.bjt_ce_batch, "cmos_opamp": workloads.cmos_opamp_batch,
+            "rc_ladder": workloads.rc_ladder_batch}[name]
 
 
 def parse():
@@ -149,9 +153,46 @@ def traffic_from_profile():
         return {}
 
 
+def run_reference_tran(args):
+    el, nn, vals = generator(args.workload)(args.n_circ, args.seed)
+    from oracle import oracle as orc
+    from kronspice_gb300 import analysis
+    orc.build()
+    nthreads = os.cpu_count() or 1
+    sp = analysis.TranSpec(**RC_LADDER_SPEC)
+    ospec = orc.TranSpec(sp.step, sp.stop, 0.0, 0.0, 0, 2, 1, 0, 0.0, 0.0, 0.0)
+    samp = min(len(vals), 512)  # a bounded sample of the batch per step
+    pk = orc.Packed(el, nn, vals[:samp])
+    opt = orc.options(reltol=RELTOL)
+    for _ in range(args.warmup):
+        orc.batch_tran(pk, samp, ospec, opt, nthreads=nthreads, record=False)
+    t0 = time.perf_counter()
+    pts = 0
+    for _ in range(args.steps):
+        st, _, steps, it = orc.batch_tran(pk, samp, ospec, opt, nthreads=nthreads, record=False)
+        pts += int(steps[st == 0].sum())
+    wall = time.perf_counter() - t0
+    value = pts / wall
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": TRAN_UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Philox)",
+            "config": {"workload": "rc_ladder_tran_%d" % args.n_circ, "n_circuits": args.n_circ,
+                       "steps_per_circuit": 1000, "method": "trap", "reltol": RELTOL, "host_threads": nthreads},
+            "cpu_baseline": {"value": value, "unit": TRAN_UNIT, "cores": nthreads, "kind": "port",
+                             "sample": "%d of the %d circuits per step, 1,000 TRAP steps each, on %d host threads; "
+                                       "oracle/ks_oracle.cpp (C++ restatement of the Go path)"
+                                       % (samp, args.n_circ, nthreads)},
+            "e2e": {"value": value, "unit": TRAN_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
+        return
+    if args.workload == "rc_ladder":
+        run_reference_tran(args)
         return
     el, nn, vals = generator(args.workload)(args.n_circ, args.seed)
     from oracle import oracle as orc
@@ -186,12 +227,205 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+
+def bench_tran(args):
+    """The RC-ladder transient: 4,096 seeded 10-section ladders, 1,000 fixed TRAP
+    steps of 10 ns each; unit of work = one accepted time point of one circuit."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from kronspice_gb300 import analysis, build
+    build.build()
+    dev = torch.device("cuda", local)
+    el, nn, vals = generator(args.workload)(args.n_circ, args.seed + rank)
+    B = vals.shape[0]
+    plan = analysis.Plan(el, nn, vals.shape[1])
+    batch = analysis.Batch(plan, vals)
+    n = plan.n
+    sp = analysis.TranSpec(**RC_LADDER_SPEC)
+    npts = int(round(sp.stop / sp.step)) + 1
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    wave = torch.empty((npts, B, n), dtype=torch.float64, device=dev)
+    ints = torch.empty((4, B), dtype=torch.int32, device=dev)  # npts, status, steps, iters
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    spec_info = None
+    try:
+        kname, csec = plan.specialize("tran")
+        spec_info = {"kernel": kname, "nvrtc_s": csec}
+    except RuntimeError as e:
+        spec_info = {"kernel": None, "error": str(e)[:200]}
+    spec_ok = spec_info["kernel"] is not None
+    plain_opt = analysis.Options(reltol=RELTOL, precision="fp64", kernel="generic")
+    chosen_opt = analysis.Options(reltol=RELTOL, precision=args.precision, kernel="specialized" if spec_ok else "generic")
+
+    def step(opt):
+        batch.tran_async(sp, opt, 0, None, wave.data_ptr(), ints[0].data_ptr(), ints[1].data_ptr(),
+                         ints[2].data_ptr(), ints[3].data_ptr(), sh)
+
+    def timed(opt):
+        for _ in range(args.warmup):
+            step(opt)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        evs = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step(opt)
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        total = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+        if world > 1:
+            t = torch.tensor([total], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total = float(t.item())
+        iv = ints.cpu().numpy()
+        ok = iv[1] == 0
+        pts = int(iv[2][ok].sum())
+        return {"seconds": total, "ms_per_step": total / args.steps * 1e3, "points": pts, "ok": int(ok.sum()),
+                "iters_per_point": float(iv[3][ok].sum() / max(pts, 1)), "status": iv[1].copy()}
+
+    clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp",
+                              "bench_clocks_%d.csv" % rank))
+    variants = {}
+    with clk:
+        plain = timed(plain_opt)
+        chosen = timed(chosen_opt)
+        chosen_wave = wave[:, :64].cpu().numpy()  # parity sample
+        if args.variants:
+            for kern in (["generic", "specialized"] if spec_ok else ["generic"]):
+                for prec in ("fp64", "mixed"):
+                    r = timed(analysis.Options(reltol=RELTOL, precision=prec, kernel=kern))
+                    variants["%s/%s" % (kern, prec)] = {"ms_per_step": r["ms_per_step"],
+                                                         "points_per_s": r["points"] * args.steps / r["seconds"]}
+    clocks = clk.summary(local)
+
+    # end to end through the C ABI: pinned host values in, host waveforms out
+    L = __import__("kronspice_gb300._lib", fromlist=["x"]).load()
+    vals_pin = torch.from_numpy(vals.copy()).pin_memory()
+    wave_host = torch.empty((npts, B, n), dtype=torch.float64).pin_memory()
+    ints_host = torch.empty((4, B), dtype=torch.int32).pin_memory()
+    o = chosen_opt.c()
+    spc = sp.c()
+
+    def e2e_step():  # ks_batch_set_values + ks_tran, both on host buffers
+        rc = L.ks_batch_set_values(batch.handle, ctypes.c_void_p(vals_pin.data_ptr()), 0, sh)
+        assert rc == 0
+        ip = ints_host.data_ptr()
+        rc = L.ks_tran(batch.handle, ctypes.byref(spc), ctypes.byref(o), 0, None, ctypes.c_void_p(wave_host.data_ptr()),
+                       ctypes.c_void_p(ip), ctypes.c_void_p(ip + 4 * B), ctypes.c_void_p(ip + 8 * B),
+                       ctypes.c_void_p(ip + 12 * B), sh)
+        assert rc == 0
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_t = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        torch.cuda.synchronize()
+        e2e_t += time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_t], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_value = world * chosen["points"] * args.steps / e2e_t
+    value = world * chosen["points"] * args.steps / chosen["seconds"]
+    plain_value = world * plain["points"] * args.steps / plain["seconds"]
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return
+
+    from oracle import oracle as orc
+    ospec = orc.TranSpec(sp.step, sp.stop, 0.0, 0.0, 0, 2, 1, 0, 0.0, 0.0, 0.0)
+    so, xo, _, _ = orc.batch_tran(orc.Packed(el, nn, vals[:64]), 64, ospec, orc.options(reltol=RELTOL))
+    okm = (so == 0) & (chosen["status"][:64] == 0)
+    max_err = float(np.max(np.abs(chosen_wave[:, okm, :nn - 1] - xo[:, okm, :nn - 1]))) if okm.any() else None
+
+    # CPU baseline: the oracle on a bounded sample of the same workload, all host threads
+    nthreads = os.cpu_count() or 1
+    samp = 256
+    pk = orc.Packed(el, nn, vals[:samp])
+    t0 = time.perf_counter()
+    cpts, reps = 0, 0
+    while True:
+        st_c, _, steps_c, _ = orc.batch_tran(pk, samp, ospec, orc.options(reltol=RELTOL), nthreads=nthreads,
+                                             record=False)
+        cpts += int(steps_c[st_c == 0].sum())
+        reps += 1
+        if time.perf_counter() - t0 > 1.0 or reps >= 50:
+            break
+    cwall = time.perf_counter() - t0
+    cpu = {"value": cpts / cwall, "unit": TRAN_UNIT, "cores": nthreads, "kind": "port",
+           "sample": "%d passes over %d of the circuits, 1,000 TRAP steps each (%.2f s wall); oracle/ks_oracle.cpp"
+                     % (reps, samp, cwall)}
+
+    per_launch_s = chosen["seconds"] / args.steps
+    alg_bytes = B * (npts * n * 8 + vals.shape[1] * 8)  # recorded waveform + each circuit's values once
+    achieved = alg_bytes / per_launch_s / 1e9
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    kname = "ks_spec_tran" if chosen_opt.kernel == "specialized" else "k_tran"
+    prof = traffic_from_profile().get("%s_rc_ladder" % kname, {})
+    traffic = prof.get("dram_bytes_per_circuit")
+    line = {
+        "metric": METRIC, "value": value, "unit": TRAN_UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": chosen["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 device eval + residual, f32 LU" if args.precision == "mixed" else "f64",
+        "data": "synthetic (seeded Philox)",
+        "config": {"workload": "rc_ladder_tran_%d" % B, "n_circuits_per_gpu": B, "n_unknowns": n,
+                   "steps_per_circuit": npts - 1, "step_s": sp.step, "method": "trap", "reltol": RELTOL,
+                   "l2": "flushed between timed steps (512 MB write); the 393 MB waveform output exceeds L2"},
+        "plain": {"value": plain_value, "ms_per_step": plain["ms_per_step"], "precision": "fp64",
+                  "kernel": "generic"},
+        "chosen": {"value": value, "precision": args.precision, "kernel": chosen_opt.kernel,
+                   "newton_iters_per_point": chosen["iters_per_point"]},
+        "chosen_vs_plain": value / plain_value if plain_value else None,
+        "per_topology_kernel": spec_info,
+        "variants": variants or None,
+        "max_node_voltage_err_vs_oracle": max_err,
+        "e2e": {"value": e2e_value, "unit": TRAN_UNIT, "h2d_bytes_per_step": int(vals.nbytes),
+                "d2h_bytes_per_step": int(wave_host.numel() * 8 + ints_host.numel() * 4)},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None if traffic is None else traffic * B, "kernel": kname,
+                     "algorithmic_bytes_per_point": n * 8 + vals.shape[1] * 8 / (npts - 1),
+                     "note": "the transient kernel is bound by FP64 issue per Newton step (one circuit per thread); "
+                             "achieved counts the recorded waveform plus each circuit's value vector"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.barrier()
+
+
 def main():
     args = parse()
     if args.n_circ <= 0:
         args.n_circ = WORKLOADS[args.workload][0]
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "rc_ladder":
+        bench_tran(args)
         return
     import torch
     rank, world, local = dist_env()

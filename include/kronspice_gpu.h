@@ -186,10 +186,13 @@ typedef struct {
   double deadline_s;      /* > 0: per-call wall-clock limit, the context
                              deadline of Options.Context (KS_STATUS_INTERRUPTED) */
   int32_t mixed_passes;   /* KS_PREC_MIXED: most FP64-residual refinement passes
-                             per linear solve (<= 0: 6); a solve not refined to
-                             1e-11 within them goes to FP64.  1: one unchecked
-                             pass, each Newton step the FP32 solve of the FP64
-                             residual (well-conditioned systems only) */
+                             per linear solve (<= 0: 6).  Refinement stops at a
+                             correction below 1e-3 reltol of the solution (1e-11
+                             for linear circuits); a solve that does not get
+                             there, or whose refinement stops contracting, goes
+                             to FP64.  1: one unchecked pass, each Newton step
+                             the FP32 solve of the FP64 residual
+                             (well-conditioned systems only). */
   int32_t reserved;
 } ks_options;
 

@@ -206,6 +206,15 @@ class Batch:
         _check(rc, "ks_tran")
         return wave, tim, np_, st, steps, it
 
+    def tran_async(self, spec, opt, capacity, time_dev, wave_dev, npts_dev, status_dev, steps_dev, iters_dev,
+                   stream):
+        """ks_tran_async on device pointers (ints; 0 or None where not wanted) on a CUDA stream handle."""
+        o = (opt or Options()).c()
+        sp = spec.c() if hasattr(spec, "c") else spec
+        _check(_lib.load().ks_tran_async(self.handle, ctypes.byref(sp), ctypes.byref(o), int(capacity), time_dev,
+                                         wave_dev, npts_dev, status_dev, steps_dev, iters_dev, stream),
+               "ks_tran_async")
+
     def op_async(self, opt, x0_dev, x_dev, status_dev, iters_dev, stream):
         """ks_op_async on device pointers (ints) on a CUDA stream handle."""
         o = (opt or Options()).c()

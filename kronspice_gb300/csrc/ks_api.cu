@@ -47,6 +47,12 @@ struct ks_batch {
   size_t h_pin_bytes = 0;
   double setup_step = -1, setup_stop = -1;  // analysis the derived constants were made for
   int last_kernel = -1;                       // KS_KERNEL_* of the last launch
+  // ks_tran's device staging, kept between calls (grow only)
+  double* d_wave = nullptr;
+  size_t d_wave_elems = 0;
+  double* d_time = nullptr;
+  size_t d_time_elems = 0;
+  int32_t* d_tints = nullptr;
 };
 
 // Derived constants for an analysis with print step / stop time (0, 0 outside a transient).
@@ -80,6 +86,9 @@ static KOpts make_opts(const ks_options* o) {  // analysis/op.go:91-110
   k.no_pt = o ? o->no_pseudo_transient : 0;
   k.mixed = o ? (o->precision == KS_PREC_MIXED) : 0;
   k.passes = o && o->mixed_passes > 0 ? std::min(o->mixed_passes, 8) : 6;
+  // refinement stops three orders under the Newton tolerance (nonlinear circuits;
+  // linear ones, whose single solve per point is final, refine to 1e-11)
+  k.refine_tol = std::min(1e-9, 1e-3 * k.reltol);
   k.max_iter_total = o ? o->max_iter_total : 0;
   return k;
 }
@@ -121,6 +130,9 @@ extern "C" int ks_plan_info(const ks_plan* p, int32_t* n_unknowns, int32_t* n_va
 static int batch_stage(ks_batch* b, size_t bytes) {
   if (b->h_pin_bytes >= bytes) return KS_OK;
   if (b->h_pin) cudaFreeHost(b->h_pin);
+  cudaFree(b->d_wave);
+  cudaFree(b->d_time);
+  cudaFree(b->d_tints);
   b->h_pin = nullptr;
   b->h_pin_bytes = 0;
   CK(cudaMallocHost(&b->h_pin, bytes));
@@ -210,6 +222,9 @@ extern "C" void ks_batch_destroy(ks_batch* b) {
   cudaFree(b->dev.queue);
   cudaFree(b->d_rows); cudaFree(b->d_x); cudaFree(b->d_x0); cudaFree(b->d_status); cudaFree(b->d_iters);
   if (b->h_pin) cudaFreeHost(b->h_pin);
+  cudaFree(b->d_wave);
+  cudaFree(b->d_time);
+  cudaFree(b->d_tints);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -373,17 +388,29 @@ extern "C" int ks_tran(ks_batch* b, const ks_tran_spec* spec, const ks_options* 
   size_t npts = spec->fixed_step ? (size_t)llround(spec->stop / spec->step) + 1 : 0;
   size_t wave_elems = spec->fixed_step ? npts * B * n : (size_t)std::max(capacity, 0) * B * n;
   size_t time_elems = spec->fixed_step ? 0 : (size_t)std::max(capacity, 0) * B;
-  double* d_wave = nullptr;
-  double* d_time = nullptr;
-  int32_t* d_ints = nullptr;
-  auto cleanup = [&]() { cudaFree(d_wave); cudaFree(d_time); cudaFree(d_ints); };
-  if (out_wave && wave_elems && cudaMalloc(&d_wave, wave_elems * sizeof(double)) != cudaSuccess) {
-    cleanup(); set_error("ks_tran: device allocation for the waveforms failed"); return KS_ENOMEM;
+  // device staging kept in the batch between calls
+  auto grow = [&](double** p, size_t* have, size_t need) {
+    if (need <= *have) return true;
+    cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+    if (cudaMalloc(p, need * sizeof(double)) != cudaSuccess) return false;
+    *have = need;
+    return true;
+  };
+  if (out_wave && wave_elems && !grow(&b->d_wave, &b->d_wave_elems, wave_elems)) {
+    set_error("ks_tran: device allocation for the waveforms failed"); return KS_ENOMEM;
   }
-  if (out_time && time_elems && cudaMalloc(&d_time, time_elems * sizeof(double)) != cudaSuccess) {
-    cleanup(); set_error("ks_tran: device allocation failed"); return KS_ENOMEM;
+  if (out_time && time_elems && !grow(&b->d_time, &b->d_time_elems, time_elems)) {
+    set_error("ks_tran: device allocation failed"); return KS_ENOMEM;
   }
-  if (cudaMalloc(&d_ints, 4 * B * sizeof(int32_t)) != cudaSuccess) { cleanup(); set_error("ks_tran: allocation failed"); return KS_ENOMEM; }
+  if (!b->d_tints && cudaMalloc(&b->d_tints, 4 * B * sizeof(int32_t)) != cudaSuccess) {
+    set_error("ks_tran: allocation failed"); return KS_ENOMEM;
+  }
+  double* d_wave = (out_wave && wave_elems) ? b->d_wave : nullptr;
+  double* d_time = (out_time && time_elems) ? b->d_time : nullptr;
+  int32_t* d_ints = b->d_tints;
+  auto cleanup = [&]() {};
   int rc = ks_tran_async(b, spec, opt, capacity, d_time, d_wave, d_ints, d_ints + B, d_ints + 2 * B, d_ints + 3 * B, st);
   if (rc) { cleanup(); return rc; }
   cudaError_t e = cudaSuccess;

@@ -59,6 +59,7 @@ __device__ __forceinline__ double xn_(S& s, int i) { return i >= 0 ? s.xn(i) : 0
 struct LoadParams {  // device/device.go:127-148
   int mode, method;
   double time, h;
+  double rh;  // 1/h, set with h: the companion models multiply instead of dividing per element
   bool initJct;
   double gmin;
   bool srcStepping;
@@ -279,8 +280,8 @@ __device__ __forceinline__ void diode_load(const KElem& e, const Col& V, const C
     double q, c;
     diode_charge(V, p, vd, id, g0, &q, &c);
     tran = true;
-    if (lp.method == TRAP) { iq = 2 * (q - S[SD_QPREV]) / lp.h - S[SD_IQPREV]; geq = 2 * c / lp.h; }
-    else { iq = (q - S[SD_QPREV]) / lp.h; geq = c / lp.h; }
+    if (lp.method == TRAP) { iq = 2 * (q - S[SD_QPREV]) * lp.rh - S[SD_IQPREV]; geq = 2 * c * lp.rh; }
+    else { iq = (q - S[SD_QPREV]) * lp.rh; geq = c * lp.rh; }
   }
   S[SD_VD] = vd; S[SD_CD] = cd; S[SD_GD] = gd; S[SD_IQ] = iq; S[SD_GEQ] = geq;
   S[SD_LIM] = lim ? 1.0 : 0.0; S[SD_TRAN] = tran ? 1.0 : 0.0;
@@ -505,7 +506,7 @@ __device__ __forceinline__ void bjt_load(const KElem& e, const Col& V, const Col
   BjtCh ch;
   if (tran) {
     ch = bjt_charges(V, Dv, p, dd, vbe, vbc, vbx, vcs, d);
-    ag = lp.method == TRAP ? 2 / lp.h : 1 / lp.h;
+    ag = lp.method == TRAP ? 2 * lp.rh : lp.rh;
     for (int k = 0; k < 4; k++) {
       iq[k] = ag * (ch.q[k] - S[SQ_QPREV0 + k]);
       if (lp.method == TRAP) iq[k] -= S[SQ_IQPREV0 + k];

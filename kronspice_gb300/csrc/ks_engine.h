@@ -84,7 +84,8 @@ struct KOpts {
   int32_t no_gmin, no_source, no_pt;
   int32_t mixed;           // FP32 LU + FP64 residual
   int32_t max_iter_total;  // bound on all solves of one circuit (0 = default)
-  int32_t passes;          // mixed: refinement passes per solve (>= 1)
+  int32_t passes;          // mixed: most refinement passes per solve
+  double refine_tol;       // mixed: refinement stops when the correction is below this fraction of x
 };
 
 #ifndef __CUDACC_RTC__

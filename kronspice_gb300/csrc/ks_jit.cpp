@@ -57,6 +57,237 @@ static void append_elem(std::string& s, const KElem& e) {
   s += buf;
 }
 
+
+// ---------------------------------------------------------------- fixed pivot sequence
+// A symbolic LU of the plan's MNA pattern, emitted as straight-line code over the
+// structurally non-zero entries only:
+//   1. the pattern: every entry any element stamps in any mode (devices as dense
+//      blocks over their terminals), and every diagonal (gmin and
+//      pseudo-transient stepping add to them);
+//   2. rows: the branch row of each voltage source / inductor trades places with
+//      the row of one of its nodes, so both pivots are the source's +-1
+//      incidence entries instead of the branch row's structural zero;
+//   3. columns: minimum degree on the pattern of B + B^T (ties to the lowest
+//      index), as solver/sparse.go's minimumDegree orders its columns;
+//   4. fill of the LU with diagonal pivots in that order.
+// At run time each pivot must pass a threshold (within 2^-10 of the largest
+// entry left in its column, and not below 2^-30 of the column's largest input
+// entry, both on exponent bits); a failed check returns SOLVE_STATIC_FAIL and
+// the solve falls back to partial pivoting, which also owns the singular test.
+namespace {
+
+struct Symbolic {
+  int n = 0;
+  std::vector<int> prow;          // prow[k]: A row pivoting in step k
+  std::vector<int> q;             // q[k]: A column eliminated in step k
+  std::vector<uint32_t> Amask;    // structural pattern of A, by A row (bit = A column)
+  std::vector<uint64_t> Cmask;    // pattern of the factors, by step (bit = step), fill included
+};
+
+void stamp_pattern(const ksh::HostPlan& hp, std::vector<uint32_t>& m) {
+  auto add = [&](int i, int j) { if (i >= 0 && j >= 0) m[i] |= 1u << j; };
+  auto block = [&](const int* u, int k) {
+    for (int a = 0; a < k; a++)
+      for (int b = 0; b < k; b++) add(u[a], u[b]);
+  };
+  for (const KElem& e : hp.elem) {
+    const int* u = e.u;
+    switch (e.kind) {
+      case KS_ELEM_R: case KS_ELEM_C: block(u, 2); break;
+      case KS_ELEM_V: case KS_ELEM_L:
+        add(u[0], u[2]); add(u[1], u[2]); add(u[2], u[0]); add(u[2], u[1]); add(u[2], u[2]); break;
+      case KS_ELEM_I: break;
+      case KS_ELEM_D: block(u, 3); break;
+      case KS_ELEM_Q: block(u, 9); break;
+      case KS_ELEM_M: block(u, 6); break;
+      default: break;
+    }
+  }
+  for (int i = 0; i < hp.n; i++) add(i, i);
+}
+
+bool symbolic(const ksh::HostPlan& hp, Symbolic* sy) {
+  const int n = hp.n;
+  if (n < 1 || n > 32) return false;
+  sy->n = n;
+  sy->Amask.assign(n, 0);
+  stamp_pattern(hp, sy->Amask);
+  auto has = [&](int r, int c) { return (sy->Amask[r] >> c) & 1u; };
+  // 2. row pairing: pivot row of each A column
+  std::vector<int> pr(n);
+  for (int i = 0; i < n; i++) pr[i] = i;
+  for (const KElem& e : hp.elem) {
+    if (e.kind != KS_ELEM_V && e.kind != KS_ELEM_L) continue;
+    int j = e.u[2];
+    for (int t = 0; t < 2; t++) {
+      int a = e.u[t];
+      if (a < 0 || pr[a] != a || pr[j] != j || a == j) continue;
+      if (!has(j, a) || !has(a, j)) continue;
+      pr[a] = j;
+      pr[j] = a;
+      break;
+    }
+  }
+  // B(k, c) = A(pr[k], c): minimum degree on the pattern of B + B^T
+  std::vector<uint32_t> G(n, 0);
+  for (int k = 0; k < n; k++)
+    for (int c = 0; c < n; c++)
+      if (k != c && has(pr[k], c)) { G[k] |= 1u << c; G[c] |= 1u << k; }
+  std::vector<int> q;
+  uint32_t left = n == 32 ? 0xffffffffu : ((1u << n) - 1);
+  while (left) {
+    int best = -1, bd = 1 << 30;
+    for (int v = 0; v < n; v++) {
+      if (!((left >> v) & 1u)) continue;
+      int d = __builtin_popcount(G[v] & left);
+      if (d < bd) { bd = d; best = v; }
+    }
+    uint32_t nb = G[best] & left & ~(1u << best);
+    for (int v = 0; v < n; v++)
+      if ((nb >> v) & 1u) G[v] |= nb & ~(1u << v);
+    left &= ~(1u << best);
+    q.push_back(best);
+  }
+  sy->q = q;
+  sy->prow.resize(n);
+  for (int k = 0; k < n; k++) sy->prow[k] = pr[q[k]];
+  // C(k, l) = A(prow[k], q[l]) and its fill
+  sy->Cmask.assign(n, 0);
+  for (int k = 0; k < n; k++)
+    for (int l = 0; l < n; l++)
+      if (has(sy->prow[k], q[l])) sy->Cmask[k] |= 1ull << l;
+  for (int k = 0; k < n; k++) {
+    if (!((sy->Cmask[k] >> k) & 1ull)) return false;  // structurally zero pivot
+    for (int i = k + 1; i < n; i++) {
+      if (!((sy->Cmask[i] >> k) & 1ull)) continue;
+      sy->Cmask[i] |= sy->Cmask[k] & ~((2ull << k) - 1);
+    }
+  }
+  return true;
+}
+
+// Straight-line factor + solve in type T ("double" or "float"), reading A from
+// the system; mixed = FP32 factor with FP64-residual refinement.
+std::string emit_lu(const Symbolic& sy, bool mixed) {
+  const int n = sy.n;
+  const char* T = mixed ? "float" : "double";
+  auto C = [&](int k, int l) { return (sy.Cmask[k] >> l) & 1ull; };
+  std::string o;
+  char b[512];
+  auto f = [&](int k, int l) { snprintf(b, sizeof b, "f%d_%d", k, l); return std::string(b); };
+  // load (fill entries start at zero) and the column scales of the input
+  for (int k = 0; k < n; k++)
+    for (int l = 0; l < n; l++) {
+      if (!C(k, l)) continue;
+      bool inA = (sy.Amask[sy.prow[k]] >> sy.q[l]) & 1u;
+      if (inA) snprintf(b, sizeof b, "    %s %s = (%s)s.a(%d, %d);\n", T, f(k, l).c_str(), T, sy.prow[k], sy.q[l]);
+      else snprintf(b, sizeof b, "    %s %s = 0;\n", T, f(k, l).c_str());
+      o += b;
+    }
+  // exponent field of |v| as an int (float or double)
+  const char* ex = mixed ? "ks_exp32" : "ks_exp64";
+  for (int l = 0; l < n; l++) {
+    snprintf(b, sizeof b, "    int cs%d = 0;", l);
+    o += b;
+    for (int k = 0; k < n; k++)
+      if (C(k, l) && ((sy.Amask[sy.prow[k]] >> sy.q[l]) & 1u)) {
+        snprintf(b, sizeof b, " cs%d = max(cs%d, %s(%s));", l, l, ex, f(k, l).c_str());
+        o += b;
+      }
+    o += "\n";
+  }
+  const int big = mixed ? 255 : 2047;  // exponent field of infinities and NaNs
+  for (int k = 0; k < n; k++) {
+    // threshold on exponents: pivot within 2^-10 of the column's largest remaining entry
+    snprintf(b, sizeof b, "    { int ep = %s(%s), em = ep;", ex, f(k, k).c_str());
+    o += b;
+    for (int i = k + 1; i < n; i++)
+      if (C(i, k)) { snprintf(b, sizeof b, " em = max(em, %s(%s));", ex, f(i, k).c_str()); o += b; }
+    snprintf(b, sizeof b,
+             "\n      if (em >= %d || ep == 0 || ep + 10 < em || ep + 30 < cs%d) return SOLVE_STATIC_FAIL;"
+             " }\n",
+             big, k);
+    o += b;
+    snprintf(b, sizeof b, "    const %s r%d = %s / %s;\n", T, k, mixed ? "1.0f" : "1.0", f(k, k).c_str());
+    o += b;
+    for (int i = k + 1; i < n; i++) {
+      if (!C(i, k)) continue;
+      snprintf(b, sizeof b, "    %s *= r%d;\n", f(i, k).c_str(), k);
+      o += b;
+      for (int l = k + 1; l < n; l++)
+        if (C(k, l)) {
+          snprintf(b, sizeof b, "    %s = %s(-%s, %s, %s);\n", f(i, l).c_str(), mixed ? "fmaf" : "fma",
+                   f(i, k).c_str(), f(k, l).c_str(), f(i, l).c_str());
+          o += b;
+        }
+    }
+  }
+  // y = C^-1 v for a right-hand side v given per A row: forward, then back substitution
+  auto solve = [&](const char* vin, const char* yout) {
+    std::string r;
+    for (int k = 0; k < n; k++) {
+      snprintf(b, sizeof b, "      %s y%d = (%s)(%s);\n", T, k, T,
+               (std::string(vin) + "(" + std::to_string(sy.prow[k]) + ")").c_str());
+      r += b;
+    }
+    for (int k = 0; k < n; k++)
+      for (int i = k + 1; i < n; i++)
+        if (C(i, k)) {
+          snprintf(b, sizeof b, "      y%d = %s(-%s, y%d, y%d);\n", i, mixed ? "fmaf" : "fma", f(i, k).c_str(), k, i);
+          r += b;
+        }
+    for (int k = n - 1; k >= 0; k--) {
+      for (int l = k + 1; l < n; l++)
+        if (C(k, l)) {
+          snprintf(b, sizeof b, "      y%d = %s(-%s, y%d, y%d);\n", k, mixed ? "fmaf" : "fma", f(k, l).c_str(), l, k);
+          r += b;
+        }
+      snprintf(b, sizeof b, "      y%d *= r%d;\n", k, k);
+      r += b;
+    }
+    for (int k = 0; k < n; k++) {
+      snprintf(b, sizeof b, "      %s(%d) = y%d;\n", yout, sy.q[k], k);
+      r += b;
+    }
+    return r;
+  };
+  if (!mixed) {
+    o += "    {\n" + solve("s.rhs", "s.xn") + "    }\n";
+    o += "    long long kx = 0;\n";
+    for (int i = 0; i < n; i++) { snprintf(b, sizeof b, "    kx = key_max(kx, mag_key(s.xn(%d)));\n", i); o += b; }
+    o += "    return kx >= KS_INF_KEY ? SOLVE_NONFINITE : SOLVE_OK;\n";
+    return o;
+  }
+  // refinement from x_old: r = rhs - A x in FP64 over A's pattern, d = C^-1 r in FP32
+  for (int i = 0; i < n; i++) { snprintf(b, sizeof b, "    s.xn(%d) = s.xo(%d);\n", i, i); o += b; }
+  o += "    double prev = KS_INF;\n    for (int pass = 0; pass < passes; pass++) {\n";
+  for (int i = 0; i < n; i++) {
+    snprintf(b, sizeof b, "      { double r = s.rhs(%d);", i);
+    o += b;
+    for (int j = 0; j < n; j++)
+      if ((sy.Amask[i] >> j) & 1u) { snprintf(b, sizeof b, " r = fma(-s.a(%d, %d), s.xn(%d), r);", i, j, j); o += b; }
+    snprintf(b, sizeof b, " s.col(%d) = r; }\n", i);
+    o += b;
+  }
+  o += "      {\n" + solve("s.col", "s.col") + "      }\n";
+  o += "      long long kd = 0, kx = 0;\n";
+  for (int i = 0; i < n; i++) {
+    snprintf(b, sizeof b,
+             "      { double v = s.xn(%d) + s.col(%d); s.xn(%d) = v; kd = key_max(kd, mag_key(s.col(%d))); "
+             "kx = key_max(kx, mag_key(v)); }\n", i, i, i, i);
+    o += b;
+  }
+  o += "      if (kx >= KS_INF_KEY || kd >= KS_INF_KEY) return SOLVE_NONFINITE;\n"
+       "      const double dmax = key_mag(kd), xmax = key_mag(kx);\n"
+       "      if (dmax <= rtol * xmax || dmax == 0) break;\n"
+       "      if (pass > 0 && dmax > 0.5 * prev) return SOLVE_FP32_FAIL;\n"
+       "      if (pass == passes - 1 && passes > 1) return SOLVE_FP32_FAIL;\n"
+       "      prev = dmax;\n    }\n    return SOLVE_OK;\n";
+  return o;
+}
+
+}  // namespace
+
 std::string source(const ksh::HostPlan& hp, int T, int kind, bool* reg_out) {
   const int n = hp.n;
   const bool reg = n <= reg_max();
@@ -75,9 +306,27 @@ std::string source(const ksh::HostPlan& hp, int T, int kind, bool* reg_out) {
            hp.n_elem, hp.n_nodes, hp.n_state, hp.n_nonlin == 0 ? "true" : "false");
   s += buf;
   for (const KElem& e : hp.elem) append_elem(s, e);
-  snprintf(buf, sizeof buf,
-           "  }\n  __device__ __forceinline__ bool is_v(int i) const { return (0x%xu >> i) & 1u; }\n};\n\n", isv);
+  snprintf(buf, sizeof buf, "  }\n  __device__ __forceinline__ bool is_v(int i) const { return (0x%xu >> i) & 1u; }\n",
+           isv);
   s += buf;
+  Symbolic sy;
+  if (getenv("KS_JIT_STATIC_LU") && atoi(getenv("KS_JIT_STATIC_LU")) == 0) {
+    s += "  static constexpr bool kStaticLU = false;\n";
+  } else if (symbolic(hp, &sy)) {
+    s += "  static constexpr bool kStaticLU = true;\n";
+    s += "  // factor and solve on the fixed pivot sequence (steps: A rows";
+    for (int k = 0; k < hp.n; k++) s += " " + std::to_string(sy.prow[k]);
+    s += "; A columns";
+    for (int k = 0; k < hp.n; k++) s += " " + std::to_string(sy.q[k]);
+    s += ")\n  template <class SY>\n  __device__ __forceinline__ int lu_fp64(SY& s) const {\n";
+    s += emit_lu(sy, false);
+    s += "  }\n  template <class SY>\n  __device__ __forceinline__ int lu_mixed(SY& s, int passes, double rtol) const {\n";
+    s += emit_lu(sy, true);
+    s += "  }\n";
+  } else {
+    s += "  static constexpr bool kStaticLU = false;  // a structurally zero pivot: partial pivoting\n";
+  }
+  s += "};\n\n";
   snprintf(buf, sizeof buf, "#define KS_T %d\n#define KS_N %d\n", T, n);
   s += buf;
   if (reg) {

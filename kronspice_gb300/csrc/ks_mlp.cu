@@ -151,9 +151,9 @@ __global__ void k_features(const double* __restrict__ vals_soa, int64_t B, const
     float v = 0.f;
     if (r < rows_valid && jj < d) {
       int64_t c = idx ? idx[r] : r;
-      double x = vals_soa[(int64_t)cols[jj] * B + c];
-      if ((logmask >> jj) & 1) x = log(x);
-      v = (float)((x - mean[jj]) / stdv[jj]);
+      float x = (float)vals_soa[(int64_t)cols[jj] * B + c];  // the network reads BF16: FP32 is ample here
+      if ((logmask >> jj) & 1) x = logf(x);
+      v = (x - mean[jj]) / stdv[jj];
     }
     X[(size_t)r * dp + jj] = __float2bfloat16(v);
   }
@@ -230,6 +230,136 @@ __global__ void k_decode(const float* __restrict__ Y, int dop, int dout, const f
   double sc = scale_col >= 0 ? vals_soa[(int64_t)scale_col * B + r] : 1.0;
   for (int j = threadIdx.x; j < n; j += blockDim.x)
     x0[(size_t)r * n + j] = j < dout ? ((double)Y[(size_t)r * dop + j] * stdv[j] + mean[j]) * sc : 0.0;
+}
+
+
+// Inference in one kernel: each block takes 128 circuits through the whole
+// network with the activations in shared memory.  Features are read in place
+// from the batch's SoA values; each layer's BF16 weights [N][K] are staged in
+// shared memory (read from L2, which holds them for every block); eight warps
+// each own a quarter of the layer's output columns for 64 of the rows (mma.sync
+// m16n8k16, FP32 accumulators); the bias + ReLU epilogue writes the next
+// activations over the previous ones; the output layer is decoded straight
+// into the Newton starting points (doubles).
+constexpr int IR = 128;  // rows per block: 8 warps, each 64 rows x a quarter of the columns
+
+template <int NT>  // n8 tiles per warp: 8 for 256-wide layers, 2 for the 64-wide output layer
+__device__ __forceinline__ void infer_layer(const __nv_bfloat16* As, int lda, const __nv_bfloat16* Ws, int ldw, int K,
+                                            float (&acc)[4][NT][4]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int j = lane >> 3, r = lane & 7;
+  const int n0 = (warp & 3) * NT * 8;
+  As += (size_t)(warp >> 2) * 64 * lda;
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int t = 0; t < NT; t++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) acc[i][t][e] = 0.f;
+  for (int kk = 0; kk < K; kk += 16) {
+    uint32_t af[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) ldsm_x4(af[i], As + (size_t)(i * 16 + (lane & 15)) * lda + kk + (lane >> 4) * 8);
+#pragma unroll
+    for (int g = 0; g < NT / 2; g++) {
+      uint32_t bf[4];
+      ldsm_x4(bf, Ws + (size_t)(n0 + g * 16 + (j >> 1) * 8 + r) * ldw + kk + (j & 1) * 8);
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        mma_bf16(acc[i][2 * g], af[i], bf[0], bf[1]);
+        mma_bf16(acc[i][2 * g + 1], af[i], bf[2], bf[3]);
+      }
+    }
+  }
+}
+
+// Copy a [rows][cols] BF16 matrix (global row stride ldg) into shared memory (row
+// stride lds) with asynchronous 16-byte copies, all in flight at once; the
+// caller waits (cp_async_wait_all) and synchronises the block.
+__device__ __forceinline__ void stage(__nv_bfloat16* dst, int lds, const __nv_bfloat16* __restrict__ src, int ldg,
+                                      int rows, int cols) {
+  const int vpr = cols / 8;
+  for (int v = threadIdx.x; v < rows * vpr; v += blockDim.x) {
+    int rr = v / vpr, cc = (v % vpr) * 8;
+    uint32_t d = (uint32_t)__cvta_generic_to_shared(dst + (size_t)rr * lds + cc);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src + (size_t)rr * ldg + cc));
+  }
+  asm volatile("cp.async.commit_group;\n" ::);
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+struct InferArgs {
+  const double* vals; int64_t B; int n;
+  const int32_t* cols; uint64_t logmask; const float *fmean, *fstd;
+  int din, dip, h, dout, dop;
+  const __nv_bfloat16* W[4]; const float* bias[4];
+  const float *tmean, *tstd; int scale_col;
+  double* x0;
+};
+
+__global__ void __launch_bounds__(256) k_mlp_infer(InferArgs a) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int ldh = a.h + PAD, ldx = a.dip + PAD;
+  __nv_bfloat16* Hs = reinterpret_cast<__nv_bfloat16*>(sm);              // [IR][h + PAD]
+  __nv_bfloat16* Xs = Hs + (size_t)IR * ldh;                              // [IR][dip + PAD]
+  __nv_bfloat16* Ws = Xs + (size_t)IR * ldx;                              // [h][h + PAD] (largest layer)
+  const int64_t r0 = (int64_t)blockIdx.x * IR;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t4 = lane & 3;
+  const int wrow = (warp >> 2) * 64, wcol = warp & 3;
+  // features
+  for (int v = threadIdx.x; v < IR * a.dip; v += blockDim.x) {
+    int rr = v / a.dip, jj = v % a.dip;
+    int64_t c = r0 + rr;
+    float f = 0.f;
+    if (c < a.B && jj < a.din) {
+      float x = (float)a.vals[(int64_t)a.cols[jj] * a.B + c];
+      if ((a.logmask >> jj) & 1) x = logf(x);
+      f = (x - a.fmean[jj]) / a.fstd[jj];
+    }
+    Xs[(size_t)rr * ldx + jj] = __float2bfloat16(f);
+  }
+  // hidden layers
+  float acc[4][8][4];
+  for (int l = 0; l < 3; l++) {
+    const int K = l == 0 ? a.dip : a.h, ldw = K + PAD;
+    stage(Ws, ldw, a.W[l], K, a.h, K);
+    cp_async_wait_all();
+    __syncthreads();
+    infer_layer<8>(l == 0 ? Xs : Hs, l == 0 ? ldx : ldh, Ws, ldw, K, acc);
+    __syncthreads();  // every warp is done reading Hs and Ws
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int t = 0; t < 8; t++)
+#pragma unroll
+        for (int hh = 0; hh < 2; hh++) {
+          int row = wrow + i * 16 + g + hh * 8, col = wcol * 64 + t * 8 + t4 * 2;
+          float v0 = fmaxf(acc[i][t][hh * 2] + a.bias[l][col], 0.f);
+          float v1 = fmaxf(acc[i][t][hh * 2 + 1] + a.bias[l][col + 1], 0.f);
+          *reinterpret_cast<__nv_bfloat162*>(Hs + (size_t)row * ldh + col) = __floats2bfloat162_rn(v0, v1);
+        }
+  }
+  // output layer (dop = 64 columns, 16 per warp) and decode
+  stage(Ws, ldh, a.W[3], a.h, a.dop, a.h);
+  cp_async_wait_all();
+  __syncthreads();
+  float out[4][2][4];
+  infer_layer<2>(Hs, ldh, Ws, ldh, a.h, out);
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int t = 0; t < 2; t++)
+#pragma unroll
+      for (int hh = 0; hh < 2; hh++)
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+          int row = wrow + i * 16 + g + hh * 8, col = wcol * 16 + t * 8 + t4 * 2 + e;
+          int64_t c = r0 + row;
+          if (c >= a.B || col >= a.n) continue;
+          double sc = a.scale_col >= 0 ? a.vals[(int64_t)a.scale_col * a.B + c] : 1.0;
+          double y = out[i][t][hh * 2 + e] + a.bias[3][col];
+          a.x0[(size_t)c * a.n + col] = col < a.dout ? (y * a.tstd[col] + a.tmean[col]) * sc : 0.0;
+        }
 }
 
 }  // namespace
@@ -516,6 +646,18 @@ extern "C" int ks_mlp_predict(ks_mlp* p, ks_batch* b, double* x0_dev, void* stre
   int rc = mlp_alloc_batch(p, (int)B);
   if (rc) return rc;
   int R = pad64((int)B);
+  if (p->h % 64 == 0 && p->h <= 256 && p->dip <= p->h && p->dop == 64 && n <= 64) {  // the fused kernel's shapes
+    InferArgs a;
+    a.vals = vals; a.B = B; a.n = n; a.cols = p->fcols; a.logmask = p->logmask; a.fmean = p->fmean; a.fstd = p->fstd;
+    a.din = p->din; a.dip = p->dip; a.h = p->h; a.dout = p->dout; a.dop = p->dop;
+    for (int l = 0; l < 4; l++) { a.W[l] = p->Wq[l]; a.bias[l] = p->bias_pad[l]; }
+    a.tmean = p->tmean; a.tstd = p->tstd; a.scale_col = p->scale_col; a.x0 = x0_dev;
+    size_t smem = sizeof(__nv_bfloat16) * ((size_t)IR * (p->h + PAD) + (size_t)IR * (p->dip + PAD) +
+                                           (size_t)p->h * (p->h + PAD));
+    cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_mlp_infer<<<(unsigned)((B + IR - 1) / IR), 256, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? KS_OK : KS_ECUDA;
+  }
   dim3 blk(64, 4);
   k_features<<<(R + 3) / 4, blk, 0, st>>>(vals, B, nullptr, p->fcols, p->logmask, p->fmean, p->fstd, p->din, p->dip,
                                           (int)B, p->X, R);

@@ -560,7 +560,7 @@ __device__ __forceinline__ void mos_load(const KElem& e, const Col& V, const Col
   double ag = 0, iq[5] = {0, 0, 0, 0, 0}, cap[5] = {0, 0, 0, 0, 0};
   double dv[5] = {vgs, vgd, vgb, vbs, vbd};
   if (tran) {
-    ag = lp.method == TRAP ? 2 / lp.h : 1 / lp.h;
+    ag = lp.method == TRAP ? 2 * lp.rh : lp.rh;
     double mc[3];
     meyer_caps(D, d, vgs, vgd, o[5], o[6], o[0], mc);
     double ov[3] = {D[d + DM_CGSO], D[d + DM_CGDO], D[d + DM_CGBO]};

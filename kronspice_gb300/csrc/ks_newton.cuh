@@ -123,15 +123,20 @@ __device__ __forceinline__ int solve_once(Thr<SY, P>& t, OpState& st, LoadParams
 #pragma unroll
     for (int i = 0; i < n; i++) if (t.prog.is_v(i)) s.a(i, i) += st.diagGmin;
   }
-  int err;
+  // a per-topology program factors on its fixed pivot sequence first; a pivot
+  // that fails its threshold hands the solve to partial pivoting
+  int err = SOLVE_STATIC_FAIL;
   if (!st.fp64) {
-    err = lu_solve_mixed(s, t.o.passes);
+    const double rtol = t.prog.nonlin_empty ? 1e-11 : t.o.refine_tol;
+    if constexpr (P::kStaticLU) err = t.prog.lu_mixed(s, t.o.passes, rtol);
+    if (err == SOLVE_STATIC_FAIL) err = lu_solve_mixed(s, t.o.passes, rtol);
     if (err == SOLVE_FP32_FAIL) {  // the FP64 path takes over this circuit
       st.fp64 = true;
       err = lu_solve_fp64(s);
     }
   } else {
-    err = lu_solve_fp64(s);
+    if constexpr (P::kStaticLU) err = t.prog.lu_fp64(s);
+    if (err == SOLVE_STATIC_FAIL) err = lu_solve_fp64(s);
   }
   st.total++;
   return err;
@@ -316,7 +321,7 @@ __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* value
   const int maxTotal = o.max_iter_total > 0 ? o.max_iter_total : 3300 * o.itl1 + 16;
   const int n = t.n();
   LoadParams lp;
-  lp.mode = ModeOP; lp.method = BE; lp.time = 0; lp.h = 0; lp.initJct = false; lp.gmin = o.gmin;
+  lp.mode = ModeOP; lp.method = BE; lp.time = 0; lp.h = 0; lp.rh = 0; lp.initJct = false; lp.gmin = o.gmin;
   lp.srcStepping = false; lp.srcFact = 0;
   OpState st;
   int64_t c = (int64_t)atomicAdd(queue, 1ull);

@@ -13,12 +13,17 @@
 
 namespace ksg {
 
-enum { SOLVE_OK = 0, SOLVE_SINGULAR = KS_STATUS_SINGULAR, SOLVE_NONFINITE = KS_STATUS_NONFINITE, SOLVE_FP32_FAIL = 99 };
+// SOLVE_STATIC_FAIL: a pivot of a per-topology program's fixed pivot sequence
+// failed its threshold; the caller factors with partial pivoting instead.
+enum { SOLVE_OK = 0, SOLVE_SINGULAR = KS_STATUS_SINGULAR, SOLVE_NONFINITE = KS_STATUS_NONFINITE, SOLVE_FP32_FAIL = 99,
+       SOLVE_STATIC_FAIL = 98 };
 
-// Shared-memory system with stride T; N = 0: size known at run time.
+// Shared-memory system with stride T; N = 0: size known at run time.  Rows are
+// swapped by run-time index (kStatic = false) whatever N is.
 template <int T, int N = 0>
 struct SmemSys {
-  static constexpr bool kStatic = N > 0;
+  static constexpr bool kStatic = false;
+  static constexpr int kUnroll = 1;  // LU loops stay loops (code size)
   static constexpr int kN = N;
   double *A_, *rhs_, *x_, *xold_, *col_;
   int* piv_;
@@ -38,6 +43,7 @@ struct SmemSys {
 template <int N>
 struct RegSys {
   static constexpr bool kStatic = true;
+  static constexpr int kUnroll = N;  // LU loops fully unrolled (trip counts are at most N): every register index a constant
   static constexpr int kN = N;
   double A_[N * N], rhs_[N], x_[N], xold_[N], col_[N];
   int piv_[N];
@@ -61,6 +67,7 @@ struct RtProg {
   template <class F>
   __device__ __forceinline__ void each(F&& f) const { for (int k = 0; k < ne; k++) f(el[k]); }
   __device__ __forceinline__ bool is_v(int i) const { return isv[i] != 0; }
+  static constexpr bool kStaticLU = false;  // no fixed pivot sequence: partial pivoting
 };
 
 __device__ __forceinline__ Col state_col(const Col& Sb, const KElem& e) { return Col{Sb.p + (int64_t)e.state * Sb.B, Sb.B}; }
@@ -92,8 +99,8 @@ __device__ __forceinline__ void elem_load(const KElem& e, const Col& Vb, const C
         break;
       }
       double C = Vb[e.param + KS_RCL_P_VALUE], geq, ih;
-      if (lp.method == TRAP) { geq = 2 * C / lp.h; ih = -(geq * S[SC_VPREV] + S[SC_IPREV]); }
-      else { geq = C / lp.h; ih = -geq * S[SC_VPREV]; }
+      if (lp.method == TRAP) { geq = 2 * C * lp.rh; ih = -(geq * S[SC_VPREV] + S[SC_IPREV]); }
+      else { geq = C * lp.rh; ih = -geq * S[SC_VPREV]; }
       S[SC_TRAN] = 1; S[SC_GEQ] = geq; S[SC_IHIST] = ih;
       sadd(sys, a, a, geq); sadd(sys, b, b, geq); sadd(sys, a, b, -geq); sadd(sys, b, a, -geq);
       srhs(sys, a, -ih); srhs(sys, b, ih);
@@ -105,8 +112,8 @@ __device__ __forceinline__ void elem_load(const KElem& e, const Col& Vb, const C
       if (lp.mode == ModeOP || lp.mode == ModeTranOP) { sadd(sys, kk, a, 1); sadd(sys, kk, b, -1); break; }
       if (lp.mode == ModeUICInit) { sadd(sys, kk, kk, 1); srhs(sys, kk, S[SL_IPREV]); break; }
       double L = Vb[e.param + KS_RCL_P_VALUE];
-      double req = L / lp.h, r = -req * S[SL_IPREV];
-      if (lp.method == TRAP) { req = 2 * L / lp.h; r = -req * S[SL_IPREV] - S[SL_VPREV]; }
+      double req = L * lp.rh, r = -req * S[SL_IPREV];
+      if (lp.method == TRAP) { req = 2 * L * lp.rh; r = -req * S[SL_IPREV] - S[SL_VPREV]; }
       sadd(sys, kk, a, 1); sadd(sys, kk, b, -1); sadd(sys, kk, kk, -req);
       srhs(sys, kk, r);
       break;
@@ -136,11 +143,14 @@ template <class SY, class P>
 __device__ __forceinline__ void load_all(const P& prog, const Col& Vb, const Col& Db, const Col& Sb, SY& s,
                                          const LoadParams& lp) {
   const int n = s.size();
+  // -0.0 is the identity of addition (x + -0.0 == x for every x), so in a
+  // register system the first stamp into an entry folds into a plain move
+  const double z = SY::kStatic ? -0.0 : 0.0;
 #pragma unroll
   for (int i = 0; i < n; i++) {
 #pragma unroll
-    for (int j = 0; j < n; j++) s.a(i, j) = 0.0;
-    s.rhs(i) = 0.0;
+    for (int j = 0; j < n; j++) s.a(i, j) = z;
+    s.rhs(i) = z;
   }
   prog.each([&](const KElem& e) KS_INLINE_LAMBDA { elem_load(e, Vb, Db, Sb, s, lp); });
 }
@@ -151,10 +161,10 @@ template <class SY>
 __device__ __forceinline__ void swap_rows(SY& s, int k, int p) {
   const int n = s.size();
   if constexpr (SY::kStatic) {
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int i = 0; i < n; i++)
       if (i > k && i == p)
-#pragma unroll
+#pragma unroll (SY::kUnroll)
         for (int j = 0; j < n; j++) { double t = s.a(k, j); s.a(k, j) = s.a(i, j); s.a(i, j) = t; }
   } else if (p != k) {
     for (int j = 0; j < n; j++) { double t = s.a(k, j); s.a(k, j) = s.a(p, j); s.a(p, j) = t; }
@@ -164,10 +174,10 @@ template <class SY>
 __device__ __forceinline__ void swap_rows32(SY& s, int k, int p) {
   const int n = s.size();
   if constexpr (SY::kStatic) {
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int i = 0; i < n; i++)
       if (i > k && i == p)
-#pragma unroll
+#pragma unroll (SY::kUnroll)
         for (int j = 0; j < n; j++) { float t = s.l(k, j); s.l(k, j) = s.l(i, j); s.l(i, j) = t; }
   } else if (p != k) {
     for (int j = 0; j < n; j++) { float t = s.l(k, j); s.l(k, j) = s.l(p, j); s.l(p, j) = t; }
@@ -177,11 +187,11 @@ __device__ __forceinline__ void swap_rows32(SY& s, int k, int p) {
 template <class SY, class Y>
 __device__ __forceinline__ void permute(SY& s, Y&& y) {
   const int n = s.size();
-#pragma unroll
+#pragma unroll (SY::kUnroll)
   for (int k = 0; k < n; k++) {
     int p = s.piv(k);
     if constexpr (SY::kStatic) {
-#pragma unroll
+#pragma unroll (SY::kUnroll)
       for (int i = 0; i < n; i++)
         if (i > k && i == p) { double t = y(k); y(k) = y(i); y(i) = t; }
     } else if (p != k) {
@@ -198,6 +208,10 @@ __device__ __forceinline__ void permute(SY& s, Y&& y) {
 __device__ __forceinline__ long long mag_key(double x) { return __double_as_longlong(x) & 0x7fffffffffffffffLL; }
 __device__ __forceinline__ double key_mag(long long k) { return __longlong_as_double(k); }
 __device__ __forceinline__ long long key_max(long long a, long long b) { return a > b ? a : b; }
+// Biased exponent field of a double / float (0: zero or subnormal; 2047 / 255:
+// infinity or NaN), for the pivot thresholds of the fixed pivot sequence.
+__device__ __forceinline__ int ks_exp64(double v) { return (int)((__double_as_longlong(v) >> 52) & 0x7ff); }
+__device__ __forceinline__ int ks_exp32(float v) { return (__float_as_int(v) >> 23) & 0xff; }
 
 // Largest |a(i,j)| of every column into col(j); returns the key of the largest
 // entry of the matrix (>= KS_INF_KEY: a non-finite entry).
@@ -205,10 +219,10 @@ template <class SY>
 __device__ __forceinline__ long long column_scales(SY& s) {
   const int n = s.size();
   long long kall = 0;
-#pragma unroll
+#pragma unroll (SY::kUnroll)
   for (int j = 0; j < n; j++) {
     long long m = 0;
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int i = 0; i < n; i++) m = key_max(m, mag_key(s.a(i, j)));
     s.col(j) = key_mag(m);
     kall = key_max(kall, m);
@@ -225,11 +239,11 @@ __device__ __forceinline__ int lu_solve_fp64(SY& s) {
   long long kall = column_scales(s);
   if (kall >= KS_INF_KEY) return SOLVE_NONFINITE;
   if (kall == 0) return SOLVE_SINGULAR;
-#pragma unroll
+#pragma unroll (SY::kUnroll)
   for (int k = 0; k < n; k++) {
     int p = k;
     long long km = mag_key(s.a(k, k));
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int i = k + 1; i < n; i++) {
       long long v = mag_key(s.a(i, k));
       if (v > km) { km = v; p = i; }
@@ -239,29 +253,29 @@ __device__ __forceinline__ int lu_solve_fp64(SY& s) {
     swap_rows(s, k, p);
     double rp = 1.0 / s.a(k, k);
     s.col(k) = rp;
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int i = k + 1; i < n; i++) {
       double f = s.a(i, k) * rp;
       s.a(i, k) = f;
-#pragma unroll
+#pragma unroll (SY::kUnroll)
       for (int j = k + 1; j < n; j++) s.a(i, j) -= f * s.a(k, j);
     }
   }
-#pragma unroll
+#pragma unroll (SY::kUnroll)
   for (int i = 0; i < n; i++) s.xn(i) = s.rhs(i);
   permute(s, [&](int i) -> double& { return s.xn(i); });
-#pragma unroll
+#pragma unroll (SY::kUnroll)
   for (int i = 0; i < n; i++) {
     double acc = s.xn(i);
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int j = 0; j < i; j++) acc -= s.a(i, j) * s.xn(j);
     s.xn(i) = acc;
   }
   long long kx = 0;
-#pragma unroll
+#pragma unroll (SY::kUnroll)
   for (int i = n - 1; i >= 0; i--) {
     double acc = s.xn(i);
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int j = i + 1; j < n; j++) acc -= s.a(i, j) * s.xn(j);
     s.xn(i) = acc * s.col(i);
     kx = key_max(kx, mag_key(s.xn(i)));
@@ -274,17 +288,17 @@ template <class SY>
 __device__ __forceinline__ void lu32_apply_col(SY& s) {
   const int n = s.size();
   permute(s, [&](int i) -> double& { return s.col(i); });
-#pragma unroll
+#pragma unroll (SY::kUnroll)
   for (int i = 0; i < n; i++) {
     float acc = (float)s.col(i);
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int j = 0; j < i; j++) acc = fmaf(-s.l(i, j), (float)s.col(j), acc);
     s.col(i) = acc;
   }
-#pragma unroll
+#pragma unroll (SY::kUnroll)
   for (int i = n - 1; i >= 0; i--) {
     float acc = (float)s.col(i);
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int j = i + 1; j < n; j++) acc = fmaf(-s.l(i, j), (float)s.col(j), acc);
     s.col(i) = acc / s.l(i, i);
   }
@@ -293,28 +307,30 @@ __device__ __forceinline__ void lu32_apply_col(SY& s) {
 // Mixed precision: FP32 LU with partial pivoting of the FP64 matrix, then
 // x = xold + LU32^-1 (rhs - A*xold) with the residual in FP64, repeated as
 // iterative refinement (x += LU32^-1 (rhs - A*x)) until the correction is below
-// 1e-11 of the solution (five orders under the tightest Newton tolerance the
-// analyses use), for at most `passes` passes.  A and rhs are left intact.
-// Returns SOLVE_FP32_FAIL when a pivot is below the FP32 threshold or the
-// refinement stops contracting (the caller then solves in FP64), so a system
-// too ill-conditioned for FP32 factors never yields an unrefined step.  One pass
-// (passes = 1) skips both checks: each Newton step is then the FP32 solve of the
-// FP64 residual, for well-conditioned systems only.
+// rtol of the solution, for at most `passes` passes.  The caller's rtol is three
+// orders under the Newton tolerance for nonlinear circuits (the Newton test
+// cannot tell the solve's error from zero) and 1e-11 for linear ones (one solve
+// per time point, errors would accumulate).  A and rhs are left intact.  Returns
+// SOLVE_FP32_FAIL when a pivot is below the FP32 threshold or the refinement
+// stops contracting or does not reach rtol (the caller then solves in FP64), so
+// a system too ill-conditioned for FP32 factors never yields an unrefined step.
+// One pass (passes = 1) skips those checks: each Newton step is then the FP32
+// solve of the FP64 residual, for well-conditioned systems only.
 template <class SY>
-__device__ __forceinline__ int lu_solve_mixed(SY& s, int passes) {
+__device__ __forceinline__ int lu_solve_mixed(SY& s, int passes, double rtol) {
   const int n = s.size();
   long long kall = column_scales(s);
   if (kall >= KS_INF_KEY) return SOLVE_NONFINITE;
   if (kall == 0) return SOLVE_SINGULAR;
-#pragma unroll
+#pragma unroll (SY::kUnroll)
   for (int i = 0; i < n; i++)
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int j = 0; j < n; j++) s.l(i, j) = (float)s.a(i, j);
-#pragma unroll
+#pragma unroll (SY::kUnroll)
   for (int k = 0; k < n; k++) {
     int p = k;
     float maxv = fabsf(s.l(k, k));
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int i = k + 1; i < n; i++) {
       float v = fabsf(s.l(i, k));
       if (v > maxv) { maxv = v; p = i; }
@@ -323,28 +339,28 @@ __device__ __forceinline__ int lu_solve_mixed(SY& s, int passes) {
     s.piv(k) = p;
     swap_rows32(s, k, p);
     float rp = 1.0f / s.l(k, k);
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int i = k + 1; i < n; i++) {
       float f = s.l(i, k) * rp;
       s.l(i, k) = f;
-#pragma unroll
+#pragma unroll (SY::kUnroll)
       for (int j = k + 1; j < n; j++) s.l(i, j) = fmaf(-f, s.l(k, j), s.l(i, j));
     }
   }
-#pragma unroll
+#pragma unroll (SY::kUnroll)
   for (int i = 0; i < n; i++) s.xn(i) = s.xo(i);
   double prev = KS_INF;
   for (int pass = 0; pass < passes; pass++) {
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int i = 0; i < n; i++) {  // FP64 residual in col()
       double r = s.rhs(i);
-#pragma unroll
+#pragma unroll (SY::kUnroll)
       for (int j = 0; j < n; j++) r -= s.a(i, j) * s.xn(j);
       s.col(i) = r;
     }
     lu32_apply_col(s);
     long long kd = 0, kx = 0;
-#pragma unroll
+#pragma unroll (SY::kUnroll)
     for (int i = 0; i < n; i++) {
       double v = s.xn(i) + s.col(i);
       s.xn(i) = v;
@@ -353,7 +369,7 @@ __device__ __forceinline__ int lu_solve_mixed(SY& s, int passes) {
     }
     if (kx >= KS_INF_KEY || kd >= KS_INF_KEY) return SOLVE_NONFINITE;
     double dmax = key_mag(kd), xmax = key_mag(kx);
-    if (dmax <= 1e-11 * xmax || dmax == 0) break;
+    if (dmax <= rtol * xmax || dmax == 0) break;
     if (pass > 0 && dmax > 0.5 * prev) return SOLVE_FP32_FAIL;  // refinement stopped contracting
     if (pass == passes - 1 && passes > 1) return SOLVE_FP32_FAIL;  // not refined within the passes
     prev = dmax;

@@ -160,7 +160,7 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
   auto start = [&]() {
     thr_bind(t, values, derived, state, work, B, c);
     init_state(t.prog, t.D, t.Sb);
-    lp.method = BE; lp.time = 0; lp.h = 0;
+    lp.method = BE; lp.time = 0; lp.h = 0; lp.rh = 0;
     phase = TR_START; status = KS_STATUS_OK; accepted = 0; npts = 0; kgrid = 1; order = BE;
     tnow = 0; h = 0; tn = 0;
     if (sp.uic) {
@@ -190,6 +190,7 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
       if (tn >= sp.stop - eps) { tn = sp.stop; hitBreak = false; }
     }
     h = tn - tnow;
+    if (h != lp.h) lp.rh = 1 / h;  // one division per new step size
     lp.mode = ModeTran; lp.time = tn; lp.h = h; lp.method = order;
     st.it = 0; st.maxIter = o.itl4;
   };

@@ -79,3 +79,42 @@ def test_learned_start_cuts_newton_iterations():
     err = np.abs(x0h[ok, :nn - 1] - xo[ok, :nn - 1]).mean()
     assert err < 0.1, err
     assert il.mean() < 0.7 * ip.mean(), (il.mean(), ip.mean())
+
+
+@pytest.mark.gpu
+def test_fused_inference_matches_cpu_network():
+    """ks_mlp_predict (features, three hidden layers, output and decode in one
+    kernel) against the CPU network on the same BF16-rounded weights and
+    activations, for a batch that is not a multiple of the kernel's 64-row tile."""
+    import torch
+    from kronspice_gb300 import analysis, build, workloads, learned_start as ls
+    build.build()
+    el, nn, vals = workloads.bjt_ce_batch(1000, seed=4)
+    plan = analysis.Plan(el, nn, vals.shape[1])
+    batch = analysis.Batch(plan, vals)
+    cols, logmask, scale_col = ls.feature_spec("bjt_ce", el)
+    m = ls.MLP(len(cols), nn - 1, hidden=256, seed=3)
+    shapes = m.layer_shapes()
+    p = mo.init(shapes, 5).astype(np.float32)
+    m.set_params(p)
+    F = ls.features_host(vals, cols, logmask)
+    fmean, fstd = F.mean(0), F.std(0) + 1e-12
+    tmean = np.linspace(0.1, 0.9, nn - 1)
+    tstd = np.full(nn - 1, 0.2)
+    m.set_io(cols, logmask, fmean, fstd, tmean, tstd, scale_col)
+    x0 = torch.zeros((1000, plan.n), dtype=torch.float64, device="cuda")
+    m.predict(batch, x0.data_ptr())
+    torch.cuda.synchronize()
+    got = x0.cpu().numpy()
+    # CPU: FP32 features, BF16 inputs, weights and hidden activations
+    f32 = vals[:, cols].astype(np.float32)
+    for j in range(len(cols)):
+        if (logmask >> j) & 1:
+            f32[:, j] = np.log(f32[:, j])
+    Xs = ((f32 - fmean.astype(np.float32)) / fstd.astype(np.float32)).astype(np.float64)
+    params = [(mo.to_bf16(W), b) for W, b in mo.unpack(p.astype(np.float64), shapes)]
+    Y, _ = mo.forward(params, mo.to_bf16(Xs), round_bf16=True)
+    sc = vals[:, scale_col]
+    y_gpu = (got[:, :nn - 1] / sc[:, None] - tmean) / tstd
+    assert np.all(np.abs(y_gpu - Y) <= 0.03 + 0.02 * np.abs(Y)), np.abs(y_gpu - Y).max()
+    assert np.all(got[:, nn - 1:] == 0.0)
