@@ -234,6 +234,7 @@ int ks_unknowns(const ks_topology* topo, int32_t* n_unknowns, int32_t* is_voltag
 /* ---- plans and batches --------------------------------------------------- */
 typedef struct ks_plan ks_plan;   /* one topology, symbolic analysis done   */
 typedef struct ks_batch ks_batch; /* n circuits of one plan, values on device */
+typedef struct ks_multi ks_multi; /* n circuits of different topologies       */
 
 /* Analyse a topology: unknown layout, stamp map, matrix pattern.  The plan
  * owns copies of everything it needs. */
@@ -264,6 +265,41 @@ int ks_batch_create(ks_plan* plan, int32_t n_circ, const double* values, ks_batc
 int ks_batch_set_values(ks_batch* b, const double* values, int values_are_device, void* stream);
 /* KS_KERNEL_* that ran the batch's last analysis (-1 before the first). */
 int ks_batch_last_kernel(const ks_batch* b);
+
+/* ---- batches of different topologies --------------------------------------
+ * analysis.OP / analysis.Tran for n_circ circuits that share nothing: each has
+ * its own topology and size (thousands of unknowns each at most by memory),
+ * the way a caller runs a pool of goroutines over unrelated circuits
+ * (evo/engine.go:519-543).  One warp per circuit on the GPU; the host computes
+ * each circuit's sparse pattern, fill and fixed pivot sequence once, at
+ * creation (solver/sparse.go:154-187, :412-452).  topos[c] / values +
+ * value_offsets[c] are circuit c's topology and value vector (host memory).
+ * Results are concatenated per circuit in circuit order: x [sum n_c], fixed-step
+ * waveforms [sum over c of n_points * n_c], each circuit's block [n_points][n_c]. */
+/* The host's analysis of one circuit (no GPU work; values: its value vector,
+ * which picks the pivot rows at DC when step = 0, else with the trapezoidal
+ * companions of that time step): unknowns, slots of L + U with fill,
+ * multiply-adds of one numeric factorization, the fixed pivot sequence (step k
+ * pivots A row prow[k] on A column pcol[k]; [n] each) and the pattern of L + U
+ * in step coordinates (rowptr [n + 1], cols [slots], columns ascending in each
+ * row).  Output pointers are optional. */
+int ks_sparse_analyze(const ks_topology* topo, const double* values, double step, int32_t* n, int64_t* slots, int64_t* lu_flops, int32_t* prow,
+                      int32_t* pcol, int32_t* rowptr, int32_t* cols);
+int ks_multi_create(int32_t n_circ, const ks_topology* topos, const double* values, const int64_t* value_offsets,
+                    ks_multi** out);
+void ks_multi_destroy(ks_multi* m);
+/* Totals, and each circuit's unknown count (n_per_circuit [n_circ], optional). */
+int ks_multi_info(const ks_multi* m, int64_t* total_unknowns, int64_t* factor_slots, int64_t* lu_flops,
+                  int32_t* n_per_circuit);
+int ks_multi_op(ks_multi* m, const ks_options* opt, double* out_x, int32_t* out_status, int32_t* out_iters);
+int ks_multi_op_async(ks_multi* m, const ks_options* opt, double* out_x_dev, int32_t* out_status_dev,
+                      int32_t* out_iters_dev, void* stream);
+/* Fixed-step transients only (spec->fixed_step = 1). */
+int ks_multi_tran(ks_multi* m, const ks_tran_spec* spec, const ks_options* opt, double* out_wave,
+                  int32_t* out_status, int32_t* out_steps, int32_t* out_iters);
+int ks_multi_tran_async(ks_multi* m, const ks_tran_spec* spec, const ks_options* opt, double* out_wave_dev,
+                        int32_t* out_npts_dev, int32_t* out_status_dev, int32_t* out_steps_dev,
+                        int32_t* out_iters_dev, void* stream);
 
 /* ---- operating point without device allocation --------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

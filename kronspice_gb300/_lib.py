@@ -35,7 +35,9 @@ class KsTranSpec(ctypes.Structure):
 EXPORTS = ["ks_version", "ks_last_error", "ks_validate", "ks_unknowns", "ks_plan_create", "ks_plan_destroy",
            "ks_plan_info", "ks_batch_create", "ks_batch_set_values", "ks_batch_destroy", "ks_op", "ks_op_async",
            "ks_tran", "ks_tran_async", "ks_tran_points", "ks_plan_specialize", "ks_plan_kernel_source",
-           "ks_batch_last_kernel", "ks_op_noalloc", "ks_op_noalloc_scratch_bytes"]
+           "ks_batch_last_kernel", "ks_op_noalloc", "ks_op_noalloc_scratch_bytes", "ks_multi_create",
+           "ks_multi_destroy", "ks_multi_info", "ks_multi_op", "ks_multi_op_async", "ks_multi_tran",
+           "ks_multi_tran_async", "ks_sparse_analyze"]
 
 _lib = None
 
@@ -79,6 +81,15 @@ def load(build_if_missing=False):
     L.ks_batch_last_kernel.argtypes = [P]
     L.ks_op_noalloc.argtypes = [P, ctypes.c_int32, P, P, P, P, P, P]
     L.ks_op_noalloc_scratch_bytes.argtypes = [P, ctypes.c_int32, P]
+    L.ks_multi_create.argtypes = [ctypes.c_int32, P, P, P, ctypes.POINTER(ctypes.c_void_p)]
+    L.ks_sparse_analyze.argtypes = [P, P, ctypes.c_double, P, P, P, P, P, P, P]
+    L.ks_multi_destroy.argtypes = [P]
+    L.ks_multi_destroy.restype = None
+    L.ks_multi_info.argtypes = [P, P, P, P, P]
+    L.ks_multi_op.argtypes = [P, P, P, P, P]
+    L.ks_multi_op_async.argtypes = [P, P, P, P, P, P]
+    L.ks_multi_tran.argtypes = [P, P, P, P, P, P, P]
+    L.ks_multi_tran_async.argtypes = [P, P, P, P, P, P, P, P, P]
     _lib = L
     return L
 

@@ -227,6 +227,78 @@ class Batch:
             self.handle = None
 
 
+class MultiBatch:
+    """Circuits of different topologies and sizes in one batch (ks_multi_create):
+    the GPU gives each circuit a warp and a sparse system with a fixed pivot
+    sequence from the host's symbolic analysis."""
+
+    def __init__(self, circuits):
+        L = _lib.load()
+        self._els, topos, vals, offs = [], [], [], []
+        nv = 0
+        for c in circuits:
+            if isinstance(c, tuple):
+                el, nn, v = c
+            else:
+                el, v, _ = c.pack()
+                nn = c.n_nodes
+            el = np.ascontiguousarray(el, dtype=ELEMENT_DTYPE)
+            self._els.append(el)
+            topos.append(_lib.KsTopology(int(nn), len(el), len(v), 0, el.ctypes.data))
+            vals.append(np.asarray(v, dtype=np.float64))
+            offs.append(nv)
+            nv += len(v)
+        self.n_circ = len(topos)
+        self._topos = (_lib.KsTopology * self.n_circ)(*topos)
+        self._vals = np.ascontiguousarray(np.concatenate(vals))
+        self._offs = np.asarray(offs, dtype=np.int64)
+        h = ctypes.c_void_p()
+        _check(L.ks_multi_create(self.n_circ, self._topos, self._vals.ctypes.data, self._offs.ctypes.data,
+                                 ctypes.byref(h)), "ks_multi_create")
+        self.handle = h
+        N, F, fl = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self.n = np.zeros(self.n_circ, dtype=np.int32)
+        _check(L.ks_multi_info(h, ctypes.byref(N), ctypes.byref(F), ctypes.byref(fl), self.n.ctypes.data),
+               "ks_multi_info")
+        self.total_unknowns, self.factor_slots, self.lu_flops = N.value, F.value, fl.value
+        self.x_off = np.concatenate([[0], np.cumsum(self.n)[:-1]]).astype(np.int64)
+
+    def op(self, opt=None):
+        """([x_c], status, iters) for every circuit."""
+        o = (opt or Options()).c()
+        x = np.zeros(self.total_unknowns)
+        st = np.zeros(self.n_circ, dtype=np.int32)
+        it = np.zeros(self.n_circ, dtype=np.int32)
+        _check(_lib.load().ks_multi_op(self.handle, ctypes.byref(o), x.ctypes.data, st.ctypes.data, it.ctypes.data),
+               "ks_multi_op")
+        return [x[a:a + n] for a, n in zip(self.x_off, self.n)], st, it
+
+    def tran(self, spec, opt=None):
+        """Fixed-step transient: ([wave_c [n_points][n_c]], status, steps, iters)."""
+        o = (opt or Options()).c()
+        sp = spec.c() if hasattr(spec, "c") else spec
+        npts = int(round(sp.stop / sp.step)) + 1
+        w = np.zeros(npts * self.total_unknowns)
+        st = np.zeros(self.n_circ, dtype=np.int32)
+        steps = np.zeros(self.n_circ, dtype=np.int32)
+        it = np.zeros(self.n_circ, dtype=np.int32)
+        _check(_lib.load().ks_multi_tran(self.handle, ctypes.byref(sp), ctypes.byref(o), w.ctypes.data,
+                                         st.ctypes.data, steps.ctypes.data, it.ctypes.data), "ks_multi_tran")
+        waves = [w[npts * a:npts * (a + n)].reshape(npts, n) for a, n in zip(self.x_off, self.n)]
+        return waves, st, steps, it
+
+    def tran_async(self, spec, opt, wave_dev, npts_dev, status_dev, steps_dev, iters_dev, stream):
+        o = (opt or Options()).c()
+        sp = spec.c() if hasattr(spec, "c") else spec
+        _check(_lib.load().ks_multi_tran_async(self.handle, ctypes.byref(sp), ctypes.byref(o), wave_dev, npts_dev,
+                                               status_dev, steps_dev, iters_dev, stream), "ks_multi_tran_async")
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib._lib is not None:
+            _lib._lib.ks_multi_destroy(self.handle)
+            self.handle = None
+
+
 def validate(circuit, transient=False):
     """circuit.Validate: None or the typed validation error."""
     el, vals, _ = circuit.pack()

@@ -43,13 +43,18 @@ struct Col {
 // Stamping into a thread's system S (shared-memory or register storage, see
 // ks_solve.cuh): S provides a(i, j), rhs(i), xo(i) (the linearization point X of
 // the current load) and xn(i) (the new iterate).  Ground (-1) is dropped.
+// Systems shared by the lanes of a warp (kAtomic) take the adds atomically.
 template <class S>
 __device__ __forceinline__ void sadd(S& s, int i, int j, double v) {
-  if (i >= 0 && j >= 0) s.a(i, j) += v;
+  if (i < 0 || j < 0) return;
+  if constexpr (S::kAtomic) s.add(i, j, v);
+  else s.a(i, j) += v;
 }
 template <class S>
 __device__ __forceinline__ void srhs(S& s, int i, double v) {
-  if (i >= 0) s.rhs(i) += v;
+  if (i < 0) return;
+  if constexpr (S::kAtomic) s.add_rhs(i, v);
+  else s.rhs(i) += v;
 }
 template <class S>
 __device__ __forceinline__ double xo_(S& s, int i) { return i >= 0 ? s.xo(i) : 0.0; }

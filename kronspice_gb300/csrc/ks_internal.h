@@ -24,6 +24,19 @@ int validate(const ks_topology* t, const double* values, bool transient, std::st
 
 void set_error(const std::string& s);
 
+// Symbolic sparse LU of one circuit (ks_sparse.cpp): fixed pivot sequence
+// (step k pivots A row prow[k] on A column q[k]) and the pattern of L + U in
+// step coordinates, rows in step order, columns ascending.
+struct SparseSym {
+  int n = 0;
+  std::vector<int> prow, q, pinv, qinv;  // step -> A row / col, A row / col -> step
+  std::vector<int> rp, ci, dg;           // row pointers [n+1], column (step) of each slot, slot of each diagonal
+  std::vector<uint8_t> in_a;             // slot is structurally in A (else fill)
+  int64_t flops = 0;                     // multiply-adds of one numeric factorization
+};
+// h = 0: pivot rows chosen at DC; h > 0: with the companion models of step h.
+int sparse_symbolic(const HostPlan& hp, const double* values, double h, SparseSym* sy, std::string* err);
+
 }  // namespace ksh
 
 // Kernel launchers (ks_kernels.cu).

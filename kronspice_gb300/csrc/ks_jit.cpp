@@ -309,6 +309,10 @@ std::string source(const ksh::HostPlan& hp, int T, int kind, bool* reg_out) {
   snprintf(buf, sizeof buf, "  }\n  __device__ __forceinline__ bool is_v(int i) const { return (0x%xu >> i) & 1u; }\n",
            isv);
   s += buf;
+  s += "  static constexpr bool kWarp = false;\n"
+       "  __device__ __forceinline__ static int64_t x_base(int64_t c, int n) { return c * n; }\n"
+       "  __device__ __forceinline__ static int64_t wave_base(int64_t c, int64_t B, int n, int k) {\n"
+       "    return ((int64_t)k * B + c) * n;\n  }\n";
   Symbolic sy;
   if (getenv("KS_JIT_STATIC_LU") && atoi(getenv("KS_JIT_STATIC_LU")) == 0) {
     s += "  static constexpr bool kStaticLU = false;\n";

@@ -38,81 +38,14 @@ int ks_launch_transpose(const double* src, double* dst, int64_t rows, int64_t co
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-// breakdownVoltage, device/diode.go:166-187.
-__device__ double breakdown_voltage(double is, double bv, double ibv, double vt) {
-  if (ibv < is * bv / vt) return bv;
-  auto g = [&](double x) { return is * (exp(fmin((bv - x) / vt, 700.0)) - 1 + x / vt) - ibv; };
-  double lo = fmin(0.0, bv - vt * log1p(ibv / is)) - 10 * vt, hi = bv;
-  for (int i = 0; i < 200 && g(lo) <= 0; i++) lo -= 10 * vt;
-  for (int i = 0; i < 200; i++) {
-    double mid = 0.5 * (lo + hi);
-    if (mid == lo || mid == hi) break;
-    if (g(mid) > 0) lo = mid; else hi = mid;
-  }
-  return 0.5 * (lo + hi);
-}
-
 // Per-circuit constants (NewDiode, NewBJT, NewMOSFET/derive, resolveWave with the
-// analysis's print step and stop time).
+// analysis's print step and stop time): setup_elem per element.
 __global__ void k_setup(KPlan plan, const double* __restrict__ values, double* derived, int64_t B,
                         double step, double stop) {
   int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= B) return;
   Col V{const_cast<double*>(values) + c, B}, D{derived + c, B};
-  for (int k = 0; k < plan.n_elem; k++) {
-    KElem e = plan.elem[k];
-    int p = e.param, d = e.derived;
-    switch (e.kind) {
-      case KS_ELEM_R: D[d + DR_G] = 1 / V[p]; break;
-      case KS_ELEM_V: case KS_ELEM_I:
-        wave_resolve(e.wave, V, p + KS_SRC_P_ARGS, e.nargs, D, d, step, stop);
-        break;
-      case KS_ELEM_D: {
-        double vt0 = kK * kTNom / kQ, vte = V[p + KS_D_P_N] * vt0, IS = V[p + KS_D_P_IS];
-        D[d + DD_VTE] = vte;
-        D[d + DD_VCRIT] = vte * log(vte / (kSqrt2 * IS));
-        D[d + DD_XBV] = (e.flags & KS_F_HAS_BV) ? breakdown_voltage(IS, V[p + KS_D_P_BV], V[p + KS_D_P_IBV], vt0) : 0.0;
-        double RS = V[p + KS_D_P_RS];
-        D[d + DD_GRS] = RS > 0 ? 1 / RS : 0.0;
-        D[d + DD_RVTE] = 1 / vte;
-        break;
-      }
-      case KS_ELEM_Q: {
-        double vt = kK * kTNom / kQ;
-        D[d + DQ_VT] = vt;
-        D[d + DQ_VCRIT] = vt * log(vt / (kSqrt2 * V[p + KS_Q_P_IS]));
-        D[d + DQ_RBPR] = V[p + KS_Q_P_RBM];
-        D[d + DQ_RBPI] = V[p + KS_Q_P_RB] - V[p + KS_Q_P_RBM];
-        D[d + DQ_GCPR] = V[p + KS_Q_P_RC] > 0 ? 1 / V[p + KS_Q_P_RC] : 0.0;
-        D[d + DQ_GEPR] = V[p + KS_Q_P_RE] > 0 ? 1 / V[p + KS_Q_P_RE] : 0.0;
-        D[d + DQ_OVTF] = V[p + KS_Q_P_VTF] > 0 ? 1 / (1.44 * V[p + KS_Q_P_VTF]) : 0.0;
-        double fc = V[p + KS_Q_P_FC];
-        double vje = V[p + KS_Q_P_VJE], mje = V[p + KS_Q_P_MJE], vjc = V[p + KS_Q_P_VJC], mjc = V[p + KS_Q_P_MJC];
-        D[d + DQ_F1E] = vje * (1 - pow(1 - fc, 1 - mje)) / (1 - mje);
-        D[d + DQ_F2E] = pow(1 - fc, 1 + mje);
-        D[d + DQ_F3E] = 1 - fc * (1 + mje);
-        D[d + DQ_F1C] = vjc * (1 - pow(1 - fc, 1 - mjc)) / (1 - mjc);
-        D[d + DQ_F2C] = pow(1 - fc, 1 + mjc);
-        D[d + DQ_F3C] = 1 - fc * (1 + mjc);
-        D[d + DQ_RVT] = 1 / vt;
-        D[d + DQ_RNF] = 1 / (V[p + KS_Q_P_NF] * vt);
-        D[d + DQ_RNE] = 1 / (V[p + KS_Q_P_NE] * vt);
-        D[d + DQ_RNR] = 1 / (V[p + KS_Q_P_NR] * vt);
-        D[d + DQ_RNC] = 1 / (V[p + KS_Q_P_NC] * vt);
-        D[d + DQ_RNS] = 1 / (V[p + KS_Q_P_NS] * vt);
-        double VAF = V[p + KS_Q_P_VAF], VAR = V[p + KS_Q_P_VAR], IKF = V[p + KS_Q_P_IKF], IKR = V[p + KS_Q_P_IKR];
-        D[d + DQ_IVAF] = VAF > 0 ? 1 / VAF : 0;
-        D[d + DQ_IVAR] = VAR > 0 ? 1 / VAR : 0;
-        D[d + DQ_OIK] = IKF > 0 ? 1 / IKF : 0;
-        D[d + DQ_OIKR] = IKR > 0 ? 1 / IKR : 0;
-        D[d + DQ_RBF] = 1 / V[p + KS_Q_P_BF];
-        D[d + DQ_RBR] = 1 / V[p + KS_Q_P_BR];
-        break;
-      }
-      case KS_ELEM_M: mos_derive(e, V, D); break;
-      default: break;
-    }
-  }
+  for (int k = 0; k < plan.n_elem; k++) setup_elem(plan.elem[k], V, D, step, stop);
 }
 
 int ks_launch_setup(const KsDeviceBatch& b, double step, double stop, void* stream) {

@@ -41,6 +41,10 @@ struct Thr {
 template <class SY, class P>
 __device__ __forceinline__ void thr_bind(Thr<SY, P>& t, const double* values, const double* derived, double* state, double* work,
                                 int64_t B, int64_t c) {
+  if constexpr (P::kWarp) {  // per-circuit layout of the multi-topology kernels
+    t.prog.bind(t, c);
+    return;
+  }
   const int n = t.n();
   t.V = Col{const_cast<double*>(values) + c, B};
   t.D = Col{const_cast<double*>(derived) + c, B};
@@ -110,10 +114,13 @@ __device__ __forceinline__ int solve_once(Thr<SY, P>& t, OpState& st, LoadParams
   lp.gmin = t.o.gmin;
   lp.srcStepping = st.srcStepping;
   lp.srcFact = st.srcFact;
+  // systems with one pivot sequence at DC and one for transient steps
+  if constexpr (SY::kModes) s.set_mode(lp.mode == ModeOP || lp.mode == ModeTranOP ? 0 : 1);
   load_all(t.prog, t.V, t.D, t.Sb, s, lp);
   if (st.ptG > 0) {
 #pragma unroll
     for (int i = 0; i < n; i++) {
+      if (!prog_owns(t.prog, i)) continue;
       double pv = t.ptPrev[i];
       if (t.prog.is_v(i)) { s.a(i, i) += st.ptG; s.rhs(i) += st.ptG * pv; }
       else { s.a(i, i) -= st.ptG; s.rhs(i) -= st.ptG * pv; }
@@ -121,8 +128,9 @@ __device__ __forceinline__ int solve_once(Thr<SY, P>& t, OpState& st, LoadParams
   }
   if (st.diagGmin > 0) {
 #pragma unroll
-    for (int i = 0; i < n; i++) if (t.prog.is_v(i)) s.a(i, i) += st.diagGmin;
+    for (int i = 0; i < n; i++) if (prog_owns(t.prog, i) && t.prog.is_v(i)) s.a(i, i) += st.diagGmin;
   }
+  prog_sync(t.prog);
   // a per-topology program factors on its fixed pivot sequence first; a pivot
   // that fails its threshold hands the solve to partial pivoting
   int err = SOLVE_STATIC_FAIL;
@@ -316,15 +324,14 @@ template <class SY, class P>
 __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* values, const double* derived, double* state,
                                      double* work, int64_t B, const double* x0, double* out_x, int32_t* out_status,
                                      int32_t* out_iters, uint64_t deadline_ns, unsigned long long* queue) {
-  const uint64_t t0 = deadline_ns ? globaltimer_ns() : 0;
+  const uint64_t t0 = deadline_ns ? prog_clock(t.prog) : 0;
   const KOpts& o = t.o;
   const int maxTotal = o.max_iter_total > 0 ? o.max_iter_total : 3300 * o.itl1 + 16;
-  const int n = t.n();
   LoadParams lp;
   lp.mode = ModeOP; lp.method = BE; lp.time = 0; lp.h = 0; lp.rh = 0; lp.initJct = false; lp.gmin = o.gmin;
   lp.srcStepping = false; lp.srcFact = 0;
   OpState st;
-  int64_t c = (int64_t)atomicAdd(queue, 1ull);
+  int64_t c = prog_next(t.prog, queue);
   if (c < B) {
     thr_bind(t, values, derived, state, work, B, c);
     init_state(t.prog, t.D, t.Sb);
@@ -332,7 +339,7 @@ __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* value
   }
   while (c < B) {
     bool done = false;
-    if (deadline_ns && globaltimer_ns() - t0 > deadline_ns) { st.status = KS_STATUS_INTERRUPTED; done = true; }
+    if (deadline_ns && prog_clock(t.prog) - t0 > deadline_ns) { st.status = KS_STATUS_INTERRUPTED; done = true; }
     else if (st.total >= maxTotal) { st.status = KS_STATUS_NO_CONVERGENCE; done = true; }
     else {
       int res = newton_step(t, st, lp);
@@ -342,12 +349,14 @@ __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* value
     if (!done) continue;
     if (st.status == KS_STATUS_OK) accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, ModeOP, o.gmin, false);
     if (out_x) {
+      const int n = t.n();  // per circuit for the multi-topology kernels
+      const int64_t base = t.prog.x_base(c, n);
 #pragma unroll
-      for (int i = 0; i < n; i++) out_x[c * n + i] = t.s.xn(i);
+      for (int i = 0; i < n; i++) out_x[base + i] = t.s.xn(i);
     }
     if (out_status) out_status[c] = st.status;
     if (out_iters) out_iters[c] = st.total;
-    c = (int64_t)atomicAdd(queue, 1ull);
+    c = prog_next(t.prog, queue);
     if (c < B) {
       thr_bind(t, values, derived, state, work, B, c);
       init_state(t.prog, t.D, t.Sb);

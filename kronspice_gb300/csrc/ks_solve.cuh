@@ -23,6 +23,8 @@ enum { SOLVE_OK = 0, SOLVE_SINGULAR = KS_STATUS_SINGULAR, SOLVE_NONFINITE = KS_S
 template <int T, int N = 0>
 struct SmemSys {
   static constexpr bool kStatic = false;
+  static constexpr bool kAtomic = false;
+  static constexpr bool kModes = false;
   static constexpr int kUnroll = 1;  // LU loops stay loops (code size)
   static constexpr int kN = N;
   double *A_, *rhs_, *x_, *xold_, *col_;
@@ -43,6 +45,8 @@ struct SmemSys {
 template <int N>
 struct RegSys {
   static constexpr bool kStatic = true;
+  static constexpr bool kAtomic = false;
+  static constexpr bool kModes = false;
   static constexpr int kUnroll = N;  // LU loops fully unrolled (trip counts are at most N): every register index a constant
   static constexpr int kN = N;
   double A_[N * N], rhs_[N], x_[N], xold_[N], col_[N];
@@ -58,6 +62,76 @@ struct RegSys {
   __device__ __forceinline__ float& l(int i, int j) { return L_[i * N + j]; }
 };
 
+// breakdownVoltage, device/diode.go:166-187.
+__device__ inline double breakdown_voltage(double is, double bv, double ibv, double vt) {
+  if (ibv < is * bv / vt) return bv;
+  auto g = [&](double x) { return is * (exp(fmin((bv - x) / vt, 700.0)) - 1 + x / vt) - ibv; };
+  double lo = fmin(0.0, bv - vt * log1p(ibv / is)) - 10 * vt, hi = bv;
+  for (int i = 0; i < 200 && g(lo) <= 0; i++) lo -= 10 * vt;
+  for (int i = 0; i < 200; i++) {
+    double mid = 0.5 * (lo + hi);
+    if (mid == lo || mid == hi) break;
+    if (g(mid) > 0) lo = mid; else hi = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+// Per-circuit constants of one element (NewDiode, NewBJT, NewMOSFET/derive,
+// resolveWave with the analysis's print step and stop time) into its derived block.
+__device__ inline void setup_elem(const KElem& e, const Col& V, const Col& D, double step, double stop) {
+  int p = e.param, d = e.derived;
+  switch (e.kind) {
+    case KS_ELEM_R: D[d + DR_G] = 1 / V[p]; break;
+    case KS_ELEM_V: case KS_ELEM_I:
+      wave_resolve(e.wave, V, p + KS_SRC_P_ARGS, e.nargs, D, d, step, stop);
+      break;
+    case KS_ELEM_D: {
+      double vt0 = kK * kTNom / kQ, vte = V[p + KS_D_P_N] * vt0, IS = V[p + KS_D_P_IS];
+      D[d + DD_VTE] = vte;
+      D[d + DD_VCRIT] = vte * log(vte / (kSqrt2 * IS));
+      D[d + DD_XBV] = (e.flags & KS_F_HAS_BV) ? breakdown_voltage(IS, V[p + KS_D_P_BV], V[p + KS_D_P_IBV], vt0) : 0.0;
+      double RS = V[p + KS_D_P_RS];
+      D[d + DD_GRS] = RS > 0 ? 1 / RS : 0.0;
+      D[d + DD_RVTE] = 1 / vte;
+      break;
+    }
+    case KS_ELEM_Q: {
+      double vt = kK * kTNom / kQ;
+      D[d + DQ_VT] = vt;
+      D[d + DQ_VCRIT] = vt * log(vt / (kSqrt2 * V[p + KS_Q_P_IS]));
+      D[d + DQ_RBPR] = V[p + KS_Q_P_RBM];
+      D[d + DQ_RBPI] = V[p + KS_Q_P_RB] - V[p + KS_Q_P_RBM];
+      D[d + DQ_GCPR] = V[p + KS_Q_P_RC] > 0 ? 1 / V[p + KS_Q_P_RC] : 0.0;
+      D[d + DQ_GEPR] = V[p + KS_Q_P_RE] > 0 ? 1 / V[p + KS_Q_P_RE] : 0.0;
+      D[d + DQ_OVTF] = V[p + KS_Q_P_VTF] > 0 ? 1 / (1.44 * V[p + KS_Q_P_VTF]) : 0.0;
+      double fc = V[p + KS_Q_P_FC];
+      double vje = V[p + KS_Q_P_VJE], mje = V[p + KS_Q_P_MJE], vjc = V[p + KS_Q_P_VJC], mjc = V[p + KS_Q_P_MJC];
+      D[d + DQ_F1E] = vje * (1 - pow(1 - fc, 1 - mje)) / (1 - mje);
+      D[d + DQ_F2E] = pow(1 - fc, 1 + mje);
+      D[d + DQ_F3E] = 1 - fc * (1 + mje);
+      D[d + DQ_F1C] = vjc * (1 - pow(1 - fc, 1 - mjc)) / (1 - mjc);
+      D[d + DQ_F2C] = pow(1 - fc, 1 + mjc);
+      D[d + DQ_F3C] = 1 - fc * (1 + mjc);
+      D[d + DQ_RVT] = 1 / vt;
+      D[d + DQ_RNF] = 1 / (V[p + KS_Q_P_NF] * vt);
+      D[d + DQ_RNE] = 1 / (V[p + KS_Q_P_NE] * vt);
+      D[d + DQ_RNR] = 1 / (V[p + KS_Q_P_NR] * vt);
+      D[d + DQ_RNC] = 1 / (V[p + KS_Q_P_NC] * vt);
+      D[d + DQ_RNS] = 1 / (V[p + KS_Q_P_NS] * vt);
+      double VAF = V[p + KS_Q_P_VAF], VAR = V[p + KS_Q_P_VAR], IKF = V[p + KS_Q_P_IKF], IKR = V[p + KS_Q_P_IKR];
+      D[d + DQ_IVAF] = VAF > 0 ? 1 / VAF : 0;
+      D[d + DQ_IVAR] = VAR > 0 ? 1 / VAR : 0;
+      D[d + DQ_OIK] = IKF > 0 ? 1 / IKF : 0;
+      D[d + DQ_OIKR] = IKR > 0 ? 1 / IKR : 0;
+      D[d + DQ_RBF] = 1 / V[p + KS_Q_P_BF];
+      D[d + DQ_RBR] = 1 / V[p + KS_Q_P_BR];
+      break;
+    }
+    case KS_ELEM_M: mos_derive(e, V, D); break;
+    default: break;
+  }
+}
+
 // The runtime element program of a plan (element table in shared memory).
 struct RtProg {
   const KElem* el;
@@ -68,7 +142,59 @@ struct RtProg {
   __device__ __forceinline__ void each(F&& f) const { for (int k = 0; k < ne; k++) f(el[k]); }
   __device__ __forceinline__ bool is_v(int i) const { return isv[i] != 0; }
   static constexpr bool kStaticLU = false;  // no fixed pivot sequence: partial pivoting
+  static constexpr bool kWarp = false;      // one thread per circuit
+  // result layouts of a batch of one topology: x [B][n], fixed-step waveforms [points][B][n]
+  __device__ __forceinline__ static int64_t x_base(int64_t c, int n) { return c * n; }
+  __device__ __forceinline__ static int64_t wave_base(int64_t c, int64_t B, int n, int k) {
+    return ((int64_t)k * B + c) * n;
+  }
 };
+
+// Programs whose circuit is shared by the 32 lanes of a warp (kWarp; the
+// multi-topology kernels) run the scalar control code redundantly on every lane
+// and split the element and matrix work between lanes: element loops are
+// lane-strided, so their results are combined (prog_any / prog_all / prog_min),
+// and read-modify-writes of shared per-circuit data are done by the owning lane
+// (prog_owns) with a warp barrier (prog_sync) before others read them.  For one
+// thread per circuit these are identities.
+template <class P>
+__device__ __forceinline__ void prog_sync(const P&) {
+  if constexpr (P::kWarp) __syncwarp();
+}
+template <class P>
+__device__ __forceinline__ bool prog_any(const P&, bool v) {
+  if constexpr (P::kWarp) return __any_sync(0xffffffffu, v);
+  else return v;
+}
+template <class P>
+__device__ __forceinline__ bool prog_all(const P&, bool v) {
+  if constexpr (P::kWarp) return __all_sync(0xffffffffu, v);
+  else return v;
+}
+template <class P>
+__device__ __forceinline__ double prog_min(const P&, double v) {
+  if constexpr (P::kWarp) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  return v;
+}
+template <class P>
+__device__ __forceinline__ bool prog_owns(const P&, int i) {
+  if constexpr (P::kWarp) return (i & 31) == (int)(threadIdx.x & 31);
+  else return true;
+}
+// The next circuit from the persistent kernels' queue (one ticket per warp for warp programs).
+template <class P>
+__device__ __forceinline__ int64_t prog_next(const P&, unsigned long long* queue) {
+  if constexpr (P::kWarp) {
+    unsigned long long c = 0;
+    if ((threadIdx.x & 31) == 0) c = atomicAdd(queue, 1ull);
+    return (int64_t)__shfl_sync(0xffffffffu, c, 0);
+  } else {
+    return (int64_t)atomicAdd(queue, 1ull);
+  }
+}
 
 __device__ __forceinline__ Col state_col(const Col& Sb, const KElem& e) { return Col{Sb.p + (int64_t)e.state * Sb.B, Sb.B}; }
 
@@ -146,13 +272,19 @@ __device__ __forceinline__ void load_all(const P& prog, const Col& Vb, const Col
   // -0.0 is the identity of addition (x + -0.0 == x for every x), so in a
   // register system the first stamp into an entry folds into a plain move
   const double z = SY::kStatic ? -0.0 : 0.0;
+  if constexpr (SY::kAtomic) {
+    s.zero();
+    prog_sync(prog);
+  } else {
 #pragma unroll
-  for (int i = 0; i < n; i++) {
+    for (int i = 0; i < n; i++) {
 #pragma unroll
-    for (int j = 0; j < n; j++) s.a(i, j) = z;
-    s.rhs(i) = z;
+      for (int j = 0; j < n; j++) s.a(i, j) = z;
+      s.rhs(i) = z;
+    }
   }
   prog.each([&](const KElem& e) KS_INLINE_LAMBDA { elem_load(e, Vb, Db, Sb, s, lp); });
+  prog_sync(prog);
 }
 
 // Swap rows k and p (static systems compare p against every later row, so every
@@ -386,7 +518,7 @@ __device__ __forceinline__ bool converged(const P& prog, const Col& Vb, const Co
     int ls = lim_slot(e.kind);
     if (ls >= 0 && Sb[e.state + ls] != 0) lim = true;
   });
-  if (lim) return false;
+  if (prog_any(prog, lim)) return false;
   const int n = s.size();
   bool moved = false;
 #pragma unroll
@@ -395,7 +527,7 @@ __device__ __forceinline__ bool converged(const P& prog, const Col& Vb, const Co
     double tol = (prog.is_v(i) ? o.vntol : o.abstol) + o.reltol * key_mag(key_max(mag_key(x), mag_key(old)));
     moved |= fabs(x - old) > tol;
   }
-  if (moved) return false;
+  if (prog_any(prog, moved)) return false;
   bool ok = true;
   prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
     if (!ok) return;
@@ -404,7 +536,7 @@ __device__ __forceinline__ bool converged(const P& prog, const Col& Vb, const Co
     else if (e.kind == KS_ELEM_Q) ok = bjt_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
     else if (e.kind == KS_ELEM_M) ok = mos_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
   });
-  return ok;
+  return prog_all(prog, ok);
 }
 
 // Accept every element at the new iterate (analysis/op.go:324-328).
@@ -437,6 +569,7 @@ __device__ __forceinline__ void accept_all(const P& prog, const Col& Vb, const C
       case KS_ELEM_M: mos_accept(e, Vb, Db, S, s, t, mode); break;
     }
   });
+  prog_sync(prog);
 }
 
 // Fresh device state of one circuit (the zero state of newly built devices, with
@@ -444,14 +577,25 @@ __device__ __forceinline__ void accept_all(const P& prog, const Col& Vb, const C
 template <class P>
 __device__ inline void init_state(const P& prog, const Col& Db, const Col& Sb) {
   for (int k = 0; k < prog.n_state; k++) Sb[k] = 0.0;
+  prog_sync(prog);
   prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
     if (e.kind == KS_ELEM_M) Sb[e.state + SM_AVON] = Db[e.derived + DM_VTO];
   });
+  prog_sync(prog);
 }
 
 __device__ __forceinline__ uint64_t globaltimer_ns() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// The wall clock as every lane of a warp program sees it (lane 0's reading), so a
+// deadline ends the circuit on all lanes together.
+template <class P>
+__device__ __forceinline__ uint64_t prog_clock(const P&) {
+  uint64_t t = globaltimer_ns();
+  if constexpr (P::kWarp) t = __shfl_sync(0xffffffffu, t, 0);
   return t;
 }
 

@@ -82,7 +82,7 @@ __device__ __forceinline__ double truncate_all(Thr<SY, P>& t, const TruncParams&
       default: break;
     }
   });
-  return prop;
+  return prog_min(t.prog, prop);
 }
 
 // (*Sim).nextBreakpoint, analysis/tran.go:233-243.
@@ -93,7 +93,7 @@ __device__ __forceinline__ double next_breakpoint(Thr<SY, P>& t, double tnow) {
     if ((e.kind == KS_ELEM_V || e.kind == KS_ELEM_I) && e.wave != KS_WAVE_NONE)
       nb = fmin(nb, wave_next_breakpoint(e.wave, t.D, e.derived, t.V, e.param + KS_SRC_P_ARGS, e.nargs, tnow));
   });
-  return nb;
+  return prog_min(t.prog, nb);
 }
 
 // C and L initial conditions for UIC (device/reactive.go:298-303, :466-471).
@@ -105,6 +105,7 @@ __device__ __forceinline__ void set_initial_conditions(Thr<SY, P>& t) {
     if (e.kind == KS_ELEM_C) { S[SC_VPREV] = has ? t.V[e.param + KS_RCL_P_IC] : 0.0; S[SC_IPREV] = 0; }
     if (e.kind == KS_ELEM_L) { S[SL_VPREV] = 0; S[SL_IPREV] = has ? t.V[e.param + KS_RCL_P_IC] : 0.0; }
   });
+  prog_sync(t.prog);
 }
 
 enum { TR_START = 0, TR_STEP, TR_DONE };
@@ -120,8 +121,9 @@ __device__ __forceinline__ void record(Thr<SY, P>& t, const TranSpecK& sp, int64
   const int n = t.n();
   if (sp.fixed) {
     if (out_wave && kgrid < sp.npts) {
+      const int64_t base = t.prog.wave_base(c, B, n, kgrid);
 #pragma unroll
-      for (int i = 0; i < n; i++) out_wave[((int64_t)kgrid * B + c) * n + i] = t.s.xn(i);
+      for (int i = 0; i < n; i++) out_wave[base + i] = t.s.xn(i);
     }
     return;
   }
@@ -144,8 +146,7 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
                                        int32_t* out_npts, int32_t* out_status, int32_t* out_steps, int32_t* out_iters,
                                        uint64_t deadline_ns, unsigned long long* queue) {
   const KOpts& o = t.o;
-  const int n = t.n();
-  const uint64_t t0 = deadline_ns ? globaltimer_ns() : 0;
+  const uint64_t t0 = deadline_ns ? prog_clock(t.prog) : 0;
   const double eps = 1e-12 * sp.stop;
   const int maxTotal = o.max_iter_total > 0 ? o.max_iter_total : 0x7fffffff;
   TruncParams tc{0, 0, BE, o.reltol, o.abstol, o.vntol, sp.chgtol, sp.trtol};
@@ -167,7 +168,7 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
       set_initial_conditions(t);
       op_state_reset(st, o);
 #pragma unroll
-      for (int i = 0; i < n; i++) t.s.xn(i) = 0.0;
+      for (int i = 0; i < t.n(); i++) t.s.xn(i) = 0.0;
       lp.mode = ModeUICInit;
     } else {
       dc_start(t, st, nullptr, c);
@@ -200,11 +201,11 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
     return true;
   };
 
-  c = (int64_t)atomicAdd(queue, 1ull);
+  c = prog_next(t.prog, queue);
   if (c < B) start();
   while (c < B) {
     if (phase != TR_DONE) {
-      if (deadline_ns && globaltimer_ns() - t0 > deadline_ns) { status = KS_STATUS_INTERRUPTED; phase = TR_DONE; }
+      if (deadline_ns && prog_clock(t.prog) - t0 > deadline_ns) { status = KS_STATUS_INTERRUPTED; phase = TR_DONE; }
       else if (st.total >= maxTotal) { status = KS_STATUS_NO_CONVERGENCE; phase = TR_DONE; }
     }
     if (phase != TR_DONE) {
@@ -274,7 +275,7 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
     if (out_steps) out_steps[c] = accepted;
     if (out_iters) out_iters[c] = st.total;
     if (out_npts) out_npts[c] = sp.fixed ? kgrid : (npts < sp.cap ? npts : sp.cap);
-    c = (int64_t)atomicAdd(queue, 1ull);
+    c = prog_next(t.prog, queue);
     if (c < B) start();
   }
 }

@@ -176,3 +176,61 @@ def cmos_opamp_feature_columns(el):
     cols += [off["RB"], off["CC"], off["CL"], off["VDD"], off["VCM"], off["M1"] + k("l")]
     logs += [True, True, True, False, False, True]
     return cols, logs, off["VDD"]
+
+
+# ------------------------------------------------------------------ random netlists
+def random_netlist(g, k, nodes=(10, 400)):
+    """One connected netlist: U{10..400} nodes, mean degree U[2, 6], a random
+    spanning tree of resistors and inductors (edges at ground resistive, so the
+    source and the inductors close no loop at DC) plus extra R / C / diode
+    edges, 10 % of all elements diodes (IS 1e-14, N U[1, 2]), one SIN source
+    (1 V, 1 kHz - 1 MHz) at node n1.  R log-U[1, 1e6] ohm, C log-U[1 pF, 1 uF],
+    L log-U[1 nH, 1 mH]."""
+    N = int(g.integers(nodes[0], nodes[1] + 1))
+    deg = g.uniform(2.0, 6.0)
+    E = max(N, int(round(deg * (N + 1) / 2)))
+    b = Builder("random %d" % k)
+    name = lambda v: "0" if v == 0 else "n%d" % v
+    b.voltage_wave("V1", "n1", "0", "sin", [0.0, 1.0, float(np.exp(g.uniform(np.log(1e3), np.log(1e6))))])
+    b.model("dm", "d", {"is": 1e-14, "n": 1.0})
+    order = g.permutation(np.arange(1, N + 1))
+    seen = [0]
+    edges = set()
+    counts = {"r": 0, "c": 0, "l": 0, "d": 0}
+    def add(kind, u, v):
+        i = sum(counts.values())
+        counts[kind] += 1
+        if kind == "r":
+            b.resistor("R%d" % i, name(u), name(v), float(np.exp(g.uniform(np.log(1.0), np.log(1e6)))))
+        elif kind == "c":
+            b.capacitor("C%d" % i, name(u), name(v), float(np.exp(g.uniform(np.log(1e-12), np.log(1e-6)))))
+        elif kind == "l":
+            b.inductor("L%d" % i, name(u), name(v), float(np.exp(g.uniform(np.log(1e-9), np.log(1e-3)))))
+        else:
+            n = float(g.uniform(1.0, 2.0))
+            b.model("dm%d" % i, "d", {"is": 1e-14, "n": n})
+            b.diode("D%d" % i, name(u), name(v), "dm%d" % i)
+        edges.add((min(u, v), max(u, v)))
+    for v in order:
+        u = int(seen[g.integers(0, len(seen))])
+        kind = "r" if (u == 0 or g.random() < 0.8) else "l"
+        add(kind, int(v), u)
+        seen.append(int(v))
+    extra = E - N
+    tries = 0
+    while extra > 0 and tries < 20 * E:
+        tries += 1
+        u, v = (int(a) for a in g.integers(0, N + 1, 2))
+        if u == v or (min(u, v), max(u, v)) in edges:
+            continue
+        r = g.random()
+        kind = "d" if r < 0.18 else ("r" if r < 0.58 else "c")
+        add(kind, u, v)
+        extra -= 1
+    return b.build()
+
+
+def random_netlists(n_circ, seed=0, nodes=(10, 400)):
+    """n_circ seeded random netlists of uneven size (the multi-topology workload)."""
+    g = rng(3, seed)
+    return [random_netlist(g, k, nodes) for k in range(n_circ)]
