@@ -35,7 +35,9 @@ METRIC = "converged circuit solves/s @ SPICE reltol, chosen vs plain GPU; Newton
 UNIT = "solves/s"
 RELTOL = 1e-6
 # workload -> (default circuits, compulsory bytes per solve: parameters in + node voltages out, 8 B each)
-WORKLOADS = {"bjt_ce": (16384, (7 + 5) * 8), "cmos_opamp": (65536, (24 + 7) * 8), "rc_ladder": (4096, 0)}
+WORKLOADS = {"bjt_ce": (16384, (7 + 5) * 8), "cmos_opamp": (65536, (24 + 7) * 8), "rc_ladder": (4096, 0),
+             "random_netlists": (8192, 0)}
+RANDOM_SPEC = dict(step=5e-9, stop=2000 * 5e-9, fixed_step=True, method="trap")  # 2,000 TRAP steps of 5 ns
 # transient workloads: unit of work = one accepted time point of one circuit
 TRAN_UNIT = "accepted time points/s"
 RC_LADDER_SPEC = dict(step=10e-9, stop=10e-6, fixed_step=True, method="trap")  # 1,000 TRAP steps of 10 ns
@@ -187,12 +189,51 @@ def run_reference_tran(args):
     print(json.dumps(line))
 
 
+def run_reference_multi(args):
+    from kronspice_gb300 import workloads, analysis
+    from oracle import oracle as orc
+    import concurrent.futures as cf
+    orc.build()
+    nthreads = os.cpu_count() or 1
+    circuits = workloads.random_netlists(args.n_circ, args.seed)
+    sp = analysis.TranSpec(**RANDOM_SPEC)
+    ospec = orc.TranSpec(sp.step, sp.stop, 0.0, 0.0, 0, 2, 1, 0, 0.0, 0.0, 0.0)
+    samp = circuits[:4 * nthreads]  # a bounded sample of the batch per step
+
+    def one(c):
+        el, vals, _ = c.pack()
+        so, _, ss, _ = orc.batch_tran(orc.Packed(el, c.n_nodes, vals[None, :]), 1, ospec, orc.options(reltol=RELTOL),
+                                      nthreads=1, record=False)
+        return int(ss[0]) if so[0] == 0 else 0
+    t0 = time.perf_counter()
+    pts = 0
+    with cf.ThreadPoolExecutor(max_workers=nthreads) as ex:
+        for _ in range(max(1, args.steps)):
+            pts += sum(ex.map(one, samp))
+    wall = time.perf_counter() - t0
+    value = pts / wall
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": TRAN_UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / max(1, args.steps) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Philox): random connected netlists",
+            "config": {"workload": "random_netlists_tran_%d" % args.n_circ, "n_circuits": args.n_circ,
+                       "steps_per_circuit": 2000, "method": "trap", "reltol": RELTOL, "host_threads": nthreads},
+            "cpu_baseline": {"value": value, "unit": TRAN_UNIT, "cores": nthreads, "kind": "port",
+                             "sample": "%d of the %d circuits per step, one per host thread; oracle/ks_oracle.cpp"
+                                       % (len(samp), args.n_circ)},
+            "e2e": {"value": value, "unit": TRAN_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
     if args.workload == "rc_ladder":
         run_reference_tran(args)
+        return
+    if args.workload == "random_netlists":
+        run_reference_multi(args)
         return
     el, nn, vals = generator(args.workload)(args.n_circ, args.seed)
     from oracle import oracle as orc
@@ -417,6 +458,154 @@ def bench_tran(args):
         torch.distributed.barrier()
 
 
+def bench_multi(args):
+    """8,192 seeded random netlists of 10-400 nodes (each its own topology), one
+    transient of 2,000 fixed TRAP steps each; unit = one accepted time point of
+    one circuit.  A step of the bench is the whole batch's transient."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from kronspice_gb300 import analysis, build, workloads
+    build.build()
+    dev = torch.device("cuda", local)
+    t0 = time.perf_counter()
+    circuits = workloads.random_netlists(args.n_circ, args.seed + rank)
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mb = analysis.MultiBatch(circuits)
+    t_create = time.perf_counter() - t0
+    sp = analysis.TranSpec(**RANDOM_SPEC)
+    npts = int(round(sp.stop / sp.step)) + 1
+    B, N = mb.n_circ, mb.total_unknowns
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    wave = torch.empty(npts * N, dtype=torch.float64, device=dev)
+    ints = torch.empty((4, B), dtype=torch.int32, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    plain_opt = analysis.Options(reltol=RELTOL, precision="fp64")
+    chosen_opt = analysis.Options(reltol=RELTOL, precision=args.precision)
+
+    def step(opt):
+        mb.tran_async(sp, opt, wave.data_ptr(), ints[0].data_ptr(), ints[1].data_ptr(), ints[2].data_ptr(),
+                      ints[3].data_ptr(), sh)
+
+    def timed(opt):
+        for _ in range(args.warmup):
+            step(opt)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        evs = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step(opt)
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        total = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+        if world > 1:
+            t = torch.tensor([total], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total = float(t.item())
+        iv = ints.cpu().numpy()
+        ok = iv[1] == 0
+        return {"seconds": total, "ms_per_step": total / args.steps * 1e3, "points": int(iv[2][ok].sum()),
+                "ok": int(ok.sum()), "iters_per_point": float(iv[3][ok].sum() / max(1, iv[2][ok].sum())),
+                "status": iv[1].copy()}
+
+    clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp",
+                              "bench_clocks_%d.csv" % rank))
+    with clk:
+        plain = timed(plain_opt)
+        chosen = timed(chosen_opt)
+        wave_h = wave.cpu().numpy()
+    clocks = clk.summary(local)
+    value = world * chosen["points"] * args.steps / chosen["seconds"]
+    plain_value = world * plain["points"] * args.steps / plain["seconds"]
+    # end to end through the C ABI with host buffers (ks_multi_tran)
+    L = __import__("kronspice_gb300._lib", fromlist=["x"]).load()
+    wave_host = torch.empty(npts * N, dtype=torch.float64).pin_memory()
+    ints_host = torch.empty((4, B), dtype=torch.int32).pin_memory()
+    o, spc = chosen_opt.c(), sp.c()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ip = ints_host.data_ptr()
+    rc = L.ks_multi_tran(mb.handle, ctypes.byref(spc), ctypes.byref(o), ctypes.c_void_p(wave_host.data_ptr()),
+                         ctypes.c_void_p(ip + 4 * B), ctypes.c_void_p(ip + 8 * B), ctypes.c_void_p(ip + 12 * B))
+    assert rc == 0
+    e2e_t = time.perf_counter() - t0
+    e2e_value = world * chosen["points"] / e2e_t
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return
+    # parity on a sample against the oracle, and the CPU baseline on a bounded sample
+    from oracle import oracle as orc
+    ospec = orc.TranSpec(sp.step, sp.stop, 0.0, 0.0, 0, 2, 1, 0, 0.0, 0.0, 0.0)
+    max_err, samp = 0.0, list(range(0, B, max(1, B // 16)))[:16]
+    for k in samp:
+        c = circuits[k]
+        el, vals, _ = c.pack()
+        so, xo, _, _ = orc.batch_tran(orc.Packed(el, c.n_nodes, vals[None, :]), 1, ospec, orc.options(reltol=RELTOL))
+        if so[0] == 0 and chosen["status"][k] == 0:
+            n = int(mb.n[k])
+            w = wave_h[npts * mb.x_off[k]:npts * (mb.x_off[k] + n)].reshape(npts, n)
+            nn = c.n_nodes - 1
+            max_err = max(max_err, float(np.max(np.abs(w[:, :nn] - xo[:, 0, :nn]))))
+    nthreads = os.cpu_count() or 1
+    csamp = circuits[:64]
+    t0 = time.perf_counter()
+    cpts = 0
+    import concurrent.futures as cf
+
+    def one(c):
+        el, vals, _ = c.pack()
+        so, _, ss, _ = orc.batch_tran(orc.Packed(el, c.n_nodes, vals[None, :]), 1, ospec, orc.options(reltol=RELTOL),
+                                      nthreads=1, record=False)
+        return int(ss[0]) if so[0] == 0 else 0
+    with cf.ThreadPoolExecutor(max_workers=nthreads) as ex:
+        cpts = sum(ex.map(one, csamp))
+    cwall = time.perf_counter() - t0
+    cpu = {"value": cpts / cwall, "unit": TRAN_UNIT, "cores": nthreads, "kind": "port",
+           "sample": "the first 64 of the circuits, 2,000 TRAP steps each, one circuit per host thread (%.1f s "
+                     "wall); oracle/ks_oracle.cpp with the reference's dense/sparse solver rule" % cwall}
+    line = {
+        "metric": METRIC, "value": value, "unit": TRAN_UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": chosen["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 device eval + residual, f32 LU" if args.precision == "mixed" else "f64",
+        "data": "synthetic (seeded Philox): random connected netlists",
+        "config": {"workload": "random_netlists_tran_%d" % B, "n_circuits_per_gpu": B, "nodes": "10-400",
+                   "unknowns_total": N, "steps_per_circuit": npts - 1, "step_s": sp.step, "method": "trap",
+                   "reltol": RELTOL, "lu_multiply_adds_per_factorization_of_all": mb.lu_flops,
+                   "l2": "flushed between timed steps (512 MB write)",
+                   "host_setup_s": {"generate": t_gen, "symbolic": t_create}},
+        "plain": {"value": plain_value, "ms_per_step": plain["ms_per_step"], "precision": "fp64",
+                  "ok": plain["ok"]},
+        "chosen": {"value": value, "precision": args.precision, "ok": chosen["ok"],
+                   "newton_iters_per_point": chosen["iters_per_point"]},
+        "chosen_vs_plain": value / plain_value if plain_value else None,
+        "max_node_voltage_err_vs_oracle": max_err,
+        "e2e": {"value": e2e_value, "unit": TRAN_UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(npts * N * 8 + 12 * B),
+                "note": "values are uploaded once at batch creation (ks_multi_create)"},
+        "gpu_launches": args.steps * 2,
+        "roofline": {"bound": "hbm", "achieved": None, "peak": None, "unit": "GB/s", "frac": None, "traffic": None,
+                     "note": "latency bound: one warp per circuit walks its sparse factorization row by row"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.barrier()
+
+
 def main():
     args = parse()
     if args.n_circ <= 0:
@@ -426,6 +615,9 @@ def main():
         return
     if args.workload == "rc_ladder":
         bench_tran(args)
+        return
+    if args.workload == "random_netlists":
+        bench_multi(args)
         return
     import torch
     rank, world, local = dist_env()

@@ -72,6 +72,7 @@ struct MultiArgs {
   long long* cmax;      // [total unknowns]: magnitude key of each step column's largest A entry
   MultiLayout lay[2];
   int npts;             // fixed-step points per circuit (waveform layout)
+  int wcap;             // doubles of shared memory per warp for the accumulator (0: use y)
 };
 
 namespace ksg {
@@ -117,6 +118,7 @@ struct WarpSys {
   float* f322;
   volatile double* rhs_;
   double *x_, *xo_, *col_, *y, *rpiv;
+  double* w;  // dense accumulator of the row being eliminated [n]: shared memory, or global for large n
   float *y32, *rpiv32;
   volatile long long* cmax;
   template <class T>
@@ -207,19 +209,15 @@ struct WarpProg {
     s.rpiv = a.rpiv + m.noff;
     s.rpiv32 = a.rpiv32 + m.noff;
     s.cmax = a.cmax + m.noff;
+    if (n <= a.wcap) {
+      extern __shared__ __align__(16) double ks_multi_smem[];
+      s.w = ks_multi_smem + (size_t)(threadIdx.x >> 5) * a.wcap;
+    } else {
+      s.w = s.y;
+    }
     __syncwarp();
   }
 };
-
-// slot of step column c in step row r (the column is in the row's pattern)
-__device__ __forceinline__ int row_find(const WarpSys& s, int lo, int hi, int c) {
-  hi -= 1;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (s.ci[mid] < c) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
 
 // Largest |A| of every step column (magnitude keys), for the singular test.
 __device__ __forceinline__ void column_keys(WarpSys& s) {
@@ -234,29 +232,33 @@ __device__ __forceinline__ void column_keys(WarpSys& s) {
 }
 
 // Numeric LU on the fixed pivot sequence, row by row in step order, into F
-// (T = double: fv, rpiv; T = float: f32, rpiv32).  A pivot at or below
-// colmax * n * 1e-14 (colmax: the largest |A| of its column) is singular, the
-// test of solver/sparse.go:240,271.
+// (T = double: fv, rpiv; T = float: f32, rpiv32), with the row being
+// eliminated expanded into a dense accumulator W [n] (row-by-row elimination:
+// the lanes update W at the columns of each U row directly, no search).  A
+// pivot at or below colmax * n * 1e-14 (colmax: the largest |A| of its
+// column) is singular, the test of solver/sparse.go:240,271.
 template <class T>
-__device__ __forceinline__ int warp_factor(WarpSys& s, T* F, T* rp_) {
+__device__ __forceinline__ int warp_factor(WarpSys& s, T* F, T* rp_, T* W) {
   const int n = s.n_, lane = lane_id();
   column_keys(s);
   for (int i = 0; i < n; i++) {
     const int r0 = s.rp[i], r1 = s.rp[i + 1], d = s.dg[i];
+    for (int p = r0 + lane; p < r1; p += 32) W[s.ci[p]] = (T)s.av[p];  // A row, fill at zero
+    __syncwarp();
     for (int p = r0; p < d; p++) {
       const int k = s.ci[p];
-      const T f = F[p] * rp_[k];
+      const T f = W[k] * rp_[k];
       const int k1 = s.rp[k + 1];
-      for (int qq = s.dg[k] + 1 + lane; qq < k1; qq += 32) {
-        const int tgt = row_find(s, p + 1, r1, s.ci[qq]);
-        F[tgt] -= f * F[qq];
-      }
-      if (lane == 0) F[p] = f;
+      for (int qq = s.dg[k] + 1 + lane; qq < k1; qq += 32) W[s.ci[qq]] -= f * F[qq];
+      __syncwarp();
+      if (lane == 0) W[k] = f;
       __syncwarp();
     }
-    const double dv = (double)F[d];
+    for (int p = r0 + lane; p < r1; p += 32) F[p] = W[s.ci[p]];
+    const double dv = (double)W[i];
+    __syncwarp();
     if (!(fabs(dv) > key_mag(s.cmax[i]) * (double)n * 1e-14) || !isfinite(dv)) return SOLVE_SINGULAR;
-    if (lane == 0) rp_[i] = (T)1 / F[d];
+    if (lane == 0) rp_[i] = (T)1 / (T)dv;
     __syncwarp();
   }
   return SOLVE_OK;
@@ -290,16 +292,11 @@ __device__ __forceinline__ void warp_lu_solve(WarpSys& s, const T* F, const T* r
 __device__ __noinline__ int lu_solve_fp64(WarpSys& s) {
   const int n = s.n_, nnz = s.rp[n], lane = lane_id();
   long long kall = 0;
-  for (int p = lane; p < nnz; p += 32) {
-    const double v = s.av[p];
-    s.fv[p] = v;
-    kall = key_max(kall, mag_key(v));
-  }
+  for (int p = lane; p < nnz; p += 32) kall = key_max(kall, mag_key(s.av[p]));
   kall = warp_max(kall);
-  __syncwarp();
   if (kall >= KS_INF_KEY) return SOLVE_NONFINITE;
   if (kall == 0) return SOLVE_SINGULAR;
-  int rc = warp_factor<double>(s, s.fv, s.rpiv);
+  int rc = warp_factor<double>(s, s.fv, s.rpiv, s.w);
   if (rc) return rc;
   warp_lu_solve<double>(s, s.fv, s.rpiv, s.y, [&](int r) { return s.rhs_[r]; },
                         [&](int c, double v) { s.x_[c] = v; });
@@ -313,16 +310,11 @@ __device__ __noinline__ int lu_solve_fp64(WarpSys& s) {
 __device__ __noinline__ int lu_solve_mixed(WarpSys& s, int passes, double rtol) {
   const int n = s.n_, nnz = s.rp[n], lane = lane_id();
   long long kall = 0;
-  for (int p = lane; p < nnz; p += 32) {
-    const double v = s.av[p];
-    s.f32[p] = (float)v;
-    kall = key_max(kall, mag_key(v));
-  }
+  for (int p = lane; p < nnz; p += 32) kall = key_max(kall, mag_key(s.av[p]));
   kall = warp_max(kall);
-  __syncwarp();
   if (kall >= KS_INF_KEY) return SOLVE_NONFINITE;
   if (kall == 0) return SOLVE_SINGULAR;
-  if (warp_factor<float>(s, s.f32, s.rpiv32)) return SOLVE_FP32_FAIL;
+  if (warp_factor<float>(s, s.f32, s.rpiv32, reinterpret_cast<float*>(s.w))) return SOLVE_FP32_FAIL;
   for (int i = lane; i < n; i += 32) s.x_[i] = s.xo_[i];
   __syncwarp();
   double prev = KS_INF;
@@ -611,11 +603,19 @@ extern "C" int ks_multi_info(const ks_multi* m, int64_t* total_unknowns, int64_t
   return KS_OK;
 }
 
-static unsigned multi_grid(const void* kernel, int64_t B) {
+// Shared memory for the warps' accumulators: room for the largest circuit when
+// four of them fit in 96 KB per block, else none (the accumulator is then global).
+static int multi_wcap(const ks_multi* m) {
+  int nmax = *std::max_element(m->n_of.begin(), m->n_of.end());
+  return nmax * 8 * 4 <= 96 * 1024 ? nmax : 0;
+}
+
+static unsigned multi_grid(const void* kernel, int64_t B, size_t smem) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 128, 0);
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 128, smem);
   int64_t need = (B + 3) / 4, cap = (int64_t)sms * (per > 0 ? per : 1);
   return (unsigned)(need < cap ? need : cap);
 }
@@ -638,8 +638,11 @@ extern "C" int ks_multi_op_async(ks_multi* m, const ks_options* opt, double* out
   KOpts o = ks_kopts_from(opt);
   uint64_t dl = opt && opt->deadline_s > 0 ? (uint64_t)(opt->deadline_s * 1e9) : 0;
   if (cudaMemsetAsync(m->queue, 0, 8, st) != cudaSuccess) { set_error("ks_multi_op: memset failed"); return KS_ECUDA; }
-  k_multi_op<<<multi_grid((const void*)k_multi_op, m->B), 128, 0, st>>>(m->a, o, m->B, out_x_dev, out_status_dev,
-                                                                        out_iters_dev, dl, m->queue);
+  MultiArgs a = m->a;
+  a.wcap = multi_wcap(m);
+  const size_t smem = (size_t)a.wcap * 8 * 4;
+  k_multi_op<<<multi_grid((const void*)k_multi_op, m->B, smem), 128, smem, st>>>(a, o, m->B, out_x_dev, out_status_dev,
+                                                                                 out_iters_dev, dl, m->queue);
   if (cudaGetLastError() != cudaSuccess) { set_error("ks_multi_op: launch failed"); return KS_ECUDA; }
   return KS_OK;
 }
@@ -677,6 +680,8 @@ extern "C" int ks_multi_tran_async(ks_multi* m, const ks_tran_spec* spec, const 
   sp.npts = (int)llround(spec->stop / spec->step) + 1;
   MultiArgs a = m->a;
   a.npts = sp.npts;
+  a.wcap = multi_wcap(m);
+  const size_t smem = (size_t)a.wcap * 8 * 4;
   std::vector<MultiCirc> circ = m->circ;  // waveform offsets: npts * (unknowns before the circuit)
   bool changed = false;
   for (auto& c : circ) {
@@ -694,7 +699,7 @@ extern "C" int ks_multi_tran_async(ks_multi* m, const ks_tran_spec* spec, const 
   }
   uint64_t dl = opt && opt->deadline_s > 0 ? (uint64_t)(opt->deadline_s * 1e9) : 0;
   if (cudaMemsetAsync(m->queue, 0, 8, st) != cudaSuccess) { set_error("ks_multi_tran: memset failed"); return KS_ECUDA; }
-  k_multi_tran<<<multi_grid((const void*)k_multi_tran, m->B), 128, 0, st>>>(
+  k_multi_tran<<<multi_grid((const void*)k_multi_tran, m->B, smem), 128, smem, st>>>(
       a, o, sp, m->B, out_wave_dev, out_npts_dev, out_status_dev, out_steps_dev, out_iters_dev, dl, m->queue);
   if (cudaGetLastError() != cudaSuccess) { set_error("ks_multi_tran: launch failed"); return KS_ECUDA; }
   return KS_OK;
