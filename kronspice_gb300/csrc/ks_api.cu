@@ -292,7 +292,7 @@ extern "C" int ks_plan_specialize(ks_plan* plan, int32_t analysis, int32_t* kern
 
 extern "C" int ks_plan_kernel_source(const ks_plan* plan, int32_t analysis, char* buf, size_t cap, size_t* len) {
   if (!plan || (analysis != KS_ANALYSIS_OP && analysis != KS_ANALYSIS_TRAN)) return KS_EINVAL;
-  std::string s = ksj::source(plan->hp, 64, analysis == KS_ANALYSIS_OP ? ksj::KIND_OP : ksj::KIND_TRAN, nullptr);
+  std::string s = ksj::source(plan->hp, plan->hp.n <= ksj::reg_max() ? 32 : 64, analysis == KS_ANALYSIS_OP ? ksj::KIND_OP : ksj::KIND_TRAN, nullptr);
   if (len) *len = s.size();
   if (buf && cap) {
     size_t m = std::min(cap - 1, s.size());

@@ -486,7 +486,9 @@ int get(const ksh::HostPlan& hp, int kind, KsSpec* out, std::string* err) {
   if (cudaGetDevice(&dev) != cudaSuccess || cudaFree(0) != cudaSuccess) { *err = "no CUDA device"; return -1; }
   std::string arch = device_arch(dev, err);
   if (arch.empty()) return -1;
-  const int T = 64;
+  // threads per block: 32 for register systems (a few thousand circuits then
+  // spread over every SM), 64 for shared-memory ones (measured faster)
+  const int T = hp.n <= reg_max() ? 32 : 64;
   bool reg = false;
   std::string src = source(hp, T, kind, &reg);
   int ver[2] = {0, 0};
