@@ -78,6 +78,7 @@ struct Sim {
         case KS_ELEM_V: case KS_ELEM_I: {
           SourceValue sv;
           sv.dc = p[KS_SRC_P_DC]; sv.hasDC = el.flags & KS_F_HAS_DC; sv.wkind = el.wave;
+          sv.ac = std::polar(p[KS_SRC_P_ACMAG], p[KS_SRC_P_ACPHASE] * M_PI / 180);  // device/source.go:34
           sv.args.assign(p + KS_SRC_P_ARGS, p + KS_SRC_P_ARGS + el.nargs);
           if (el.kind == KS_ELEM_V) { auto* s = new VSource(); s->src = sv; s->nodes[0] = el.node[0]; s->nodes[1] = el.node[1]; d = s; }
           else { auto* s = new ISource(); s->src = sv; s->nodes[0] = el.node[0]; s->nodes[1] = el.node[1]; d = s; }
@@ -281,6 +282,44 @@ struct Sim {
     return E_NOCONV;
   }
 
+  // polish, analysis/op.go:251-271: up to two more solves at the operating point.
+  int polish() {
+    if (nonlin.empty()) return E_OK;
+    for (int k = 0; k < 2; k++) {
+      int e = solve();
+      if (e) return e;
+      bool done = true;
+      for (int i = 0; i < n; i++)
+        if (std::fabs(x[i] - xOld[i]) > 1e-12 * std::max(1.0, std::fabs(x[i]))) done = false;
+      if (done) break;
+    }
+    accept(0, ModeOP);
+    return E_OK;
+  }
+
+  // AC, analysis/ac.go:76-150 (phasors only; the power ledger is not built):
+  // the operating point, polish, then one complex solve per frequency.
+  int ac(const Opts& o, const double* freqs, int nf, std::complex<double>* xout) {
+    int e = op(o, nullptr);
+    if (e) { msg = "AC operating point: " + msg; return e; }
+    e = polish();
+    if (e) { msg = "AC operating point: " + msg; return e; }
+    std::vector<std::complex<double>> A((size_t)n * n), rhs(n), xc(n);
+    ACCtx c;
+    c.n = n; c.A = &A; c.rhs = &rhs;
+    for (int k = 0; k < nf; k++) {
+      std::fill(A.begin(), A.end(), 0.0);
+      std::fill(rhs.begin(), rhs.end(), 0.0);
+      c.omega = 2 * M_PI * freqs[k];
+      for (auto& d : devs) d->loadAC(c);
+      int se = cdense_solve(n, A, rhs, xc);
+      if (se == SOLVE_SINGULAR) { msg = "solver: singular matrix"; return E_SINGULAR; }
+      if (se == SOLVE_NONFINITE) { msg = "solver: non-finite value in system"; return E_NONFINITE; }
+      for (int i = 0; i < n; i++) xout[(size_t)k * n + i] = xc[i];
+    }
+    return E_OK;
+  }
+
   int op(const Opts& o, const double* nodeset) {  // analysis/op.go:340-357 (ledger not built)
     lc.mode = ModeOP; lc.time = 0;
     int e = dcSolve(o, nodeset);
@@ -446,6 +485,19 @@ extern "C" int kso_op(const ks_topology* t, const double* values, const ks_optio
   if (iters) *iters = s.iters;
   if (x_out) for (int i = 0; i < s.n; i++) x_out[i] = s.x[i];
   if (i_out && e == E_OK) for (size_t i = 0; i < s.devs.size(); i++) i_out[i] = s.devs[i]->current(s.x.data());
+  copyMsg(e ? s.msg : std::string(), err, errlen);
+  return e;
+}
+
+extern "C" int kso_ac(const ks_topology* t, const double* values, const ks_options* o, const double* freqs, int nf,
+                      double* x_out, char* err, int errlen) {
+  Sim s;
+  Opts opt(o);
+  if (s.build(t, values, 0, 0, opt.backend)) { copyMsg(s.msg, err, errlen); return KS_STATUS_NOT_RUN; }
+  std::vector<std::complex<double>> xc((size_t)nf * s.n);
+  int e = s.ac(opt, freqs, nf, xc.data());
+  if (x_out)
+    for (size_t i = 0; i < xc.size(); i++) { x_out[2 * i] = xc[i].real(); x_out[2 * i + 1] = xc[i].imag(); }
   copyMsg(e ? s.msg : std::string(), err, errlen);
   return e;
 }

@@ -27,6 +27,9 @@ int kso_op(const ks_topology* t, const double* values, const ks_options* o, cons
 
 /* DC sweep of source element `src` over vals[npts] (analysis.DC, one sweep).
  * x_out [npts][n], i_out [npts][n_elem] (nullable).  Returns a ks_status. */
+/* AC small-signal sweep (analysis/ac.go): x_out [nf][n] complex, interleaved re/im. */
+int kso_ac(const ks_topology* t, const double* values, const ks_options* o, const double* freqs, int nf,
+           double* x_out, char* err, int errlen);
 int kso_dc(const ks_topology* t, const double* values, const ks_options* o, int src,
            const double* vals, int npts, double* x_out, double* i_out, char* err, int errlen);
 

@@ -145,6 +145,17 @@ def tran(pk, spec, opt=None, capacity=200000, currents=True):
     return (st, t[:k], x[:k], None if cur is None else cur[:k], steps.value, it.value, err.value.decode())
 
 
+def ac(pk, freqs, opt=None):
+    """AC sweep (analysis/ac.go): (status, x [nf][n] complex, message)."""
+    n, _ = unknowns(pk)
+    f = np.ascontiguousarray(freqs, dtype=np.float64)
+    x = np.zeros((len(f), n, 2))
+    err = ctypes.create_string_buffer(512)
+    o = opt or options()
+    st = lib().kso_ac(pk.tref(), _ptr(pk.values), ctypes.byref(o), _ptr(f), len(f), _ptr(x), err, 512)
+    return st, x[..., 0] + 1j * x[..., 1], err.value.decode()
+
+
 def batch_op(pk, nc, opt=None, x0=None, nthreads=0):
     n, _ = unknowns(Packed(pk.elements, pk.topo.n_nodes, pk.values[0]))
     x = np.zeros((nc, n))

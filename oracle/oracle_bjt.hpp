@@ -240,6 +240,23 @@ struct BJT : Device {
     if (SUBS > 0) ic -= isb;
     return ic;
   }
+  void loadAC(ACCtx& c) override {  // device/bjt.go:689-711
+    DC d = evalDC(vbeAcc, vbcAcc);
+    Ch h = charges(vbeAcc, vbcAcc, vbxAcc, vcsAcc, d);
+    const double w = c.omega;
+    typedef std::complex<double> cx;
+    double isub, gsub;
+    substrate(vcsAcc, &isub, &gsub);
+    cx ybe(0, w * h.c[0]), ybeBC(0, w * h.dqbeDvbc), ybc(0, w * h.c[1]), ybx(0, w * h.c[2]), ycs(gsub, w * h.c[3]);
+    c.branch(cp, ep, d.itBE, bp, ep, d.itBC, bp, cp);
+    c.branch(bp, ep, cx(d.gpi) + ybe, bp, ep, ybeBC, bp, cp);
+    c.branch(bp, cp, cx(d.gmu) + ybc, bp, cp, 0.0, 0, 0);
+    c.branch(b, cp, ybx, b, cp, 0.0, 0, 0);
+    c.branch(sa, sb, ycs, sa, sb, 0.0, 0, 0);
+    if (bp != b) c.stampY(b, bp, d.gx);
+    if (cp != uc) c.stampY(uc, cp, gcpr);
+    if (ep != ue) c.stampY(ue, ep, gepr);
+  }
   void accept(const double* x, double t, int mode) override {  // :579-601
     double be, bc, bx, cs;
     voltages(x, &be, &bc, &bx, &cs);

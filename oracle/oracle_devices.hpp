@@ -103,8 +103,26 @@ struct SetupCtx {  // device/device.go:36-100
   int size() const { return numNodes - 1 + branches; }
 };
 
+// Complex small-signal stamping, device.ACContext (device/device.go): Y = G + jwC and
+// the AC source phasors.
+struct ACCtx {
+  int n = 0;
+  double omega = 0;
+  std::vector<std::complex<double>>* A = nullptr;  // row-major n x n
+  std::vector<std::complex<double>>* rhs = nullptr;
+  void add(int i, int j, std::complex<double> v) { if (i >= 0 && j >= 0) (*A)[(size_t)i * n + j] += v; }
+  void addRHS(int i, std::complex<double> v) { if (i >= 0) (*rhs)[i] += v; }
+  void stampY(int a, int b, std::complex<double> y) { add(a, a, y); add(b, b, y); add(a, b, -y); add(b, a, -y); }  // device/device.go:333-338
+  // acBranch, device/bjt.go:713-726
+  void branch(int a, int b, std::complex<double> y1, int p1, int n1, std::complex<double> y2, int p2, int n2) {
+    if (y1 != 0.0) { add(a, p1, y1); add(a, n1, -y1); add(b, p1, -y1); add(b, n1, y1); }
+    if (y2 != 0.0) { add(a, p2, y2); add(a, n2, -y2); add(b, p2, -y2); add(b, n2, y2); }
+  }
+};
+
 struct Device {
   int n = 0;  // system size (set after setup)
+  virtual void loadAC(ACCtx& c) {}
   virtual ~Device() {}
   virtual void setup(SetupCtx& c) = 0;
   virtual void load(LoadCtx& c) = 0;
@@ -143,6 +161,7 @@ struct Resistor : TwoTerm {
     c.M->add(a, a, g); c.M->add(b, b, g); c.M->add(a, b, -g); c.M->add(b, a, -g);
   }
   double current(const double* x) override { return voltage(x) * g; }
+  void loadAC(ACCtx& c) override { c.stampY(u[0], u[1], g); }  // device/passive.go:116-123
 };
 
 // Capacitor, device/reactive.go:43-181.
@@ -182,6 +201,7 @@ struct Capacitor : TwoTerm {
     hist.push(t, C * vPrev);
   }
   void setInitialCondition() override { vPrev = 0; iPrev = 0; if (hasIC) vPrev = ic; }
+  void loadAC(ACCtx& c) override { c.stampY(u[0], u[1], std::complex<double>(0, c.omega * C)); }  // reactive.go:355-363
   double truncate(const double* x, const TruncCtx& tc) override {  // :178-181
     double v = voltage(x), i = current(x);
     return lteStep(hist, C * v, i, iPrev, tc.abstol, tc);
@@ -217,6 +237,11 @@ struct Inductor : TwoTerm {
     hist.push(t, L * iPrev);
   }
   void setInitialCondition() override { vPrev = 0; iPrev = 0; if (hasIC) iPrev = ic; }
+  void loadAC(ACCtx& c) override {  // device/reactive.go:377-393
+    int a = u[0], b = u[1], k = branch;
+    c.add(a, k, 1); c.add(b, k, -1); c.add(k, a, 1); c.add(k, b, -1);
+    c.add(k, k, std::complex<double>(0, -c.omega * L));
+  }
   double truncate(const double* x, const TruncCtx& tc) override {  // :346-349
     return lteStep(hist, L * x[branch], voltage(x), vPrev, tc.vntol, tc);
   }
@@ -331,6 +356,7 @@ struct Wave {
 // sourceValue, device/source.go:21-73.
 struct SourceValue {
   double dc; bool hasDC;
+  std::complex<double> ac = 0;  // AC phasor, magnitude at phase (degrees): device/source.go:34
   int wkind; std::vector<double> args;
   Wave w;
   double override_ = 0; bool overridden = false;
@@ -364,10 +390,16 @@ struct VSource : TwoTerm {  // device/source.go:75-121
   double nextBreakpoint(double t) override { return src.nextBreakpoint(t); }
   void setDCOverride(double v) override { src.override_ = v; src.overridden = true; }
   void clearDCOverride() override { src.overridden = false; }
+  void loadAC(ACCtx& c) override {  // device/source.go:186-194
+    int a = u[0], b = u[1], k = branch;
+    c.add(a, k, 1); c.add(b, k, -1); c.add(k, a, 1); c.add(k, b, -1);
+    c.addRHS(k, src.ac);
+  }
 };
 
 struct ISource : TwoTerm {  // device/source.go:131-177
   SourceValue src; double value = 0;
+  void loadAC(ACCtx& c) override { c.addRHS(u[0], -src.ac); c.addRHS(u[1], src.ac); }  // :208-212
   void setup(SetupCtx& c) override { setupNodes(c); src.setup(c); }
   void load(LoadCtx& c) override { value = src.at(c); c.addRHS(u[0], -value); c.addRHS(u[1], value); }
   double current(const double*) override { return value; }
@@ -421,6 +453,13 @@ struct Diode : TwoTerm {
     }
     double e = std::exp(std::min(-(xbv + v) / vte, 700.0));
     *id = -IS * e; *g = IS * e / vte;
+  }
+  void loadAC(ACCtx& c) override {  // device/diode.go:409-421
+    double id, gd, q, cap;
+    curr(vdAcc, &id, &gd);
+    charge(vdAcc, id, gd, &q, &cap);
+    c.stampY(ai, u[1], std::complex<double>(gd + gmin, c.omega * cap));
+    if (grs > 0) c.stampY(u[0], ai, grs);
   }
   void charge(double v, double id, double g, double* q, double* c) const {  // :191-211
     *q = TT * id; *c = TT * g;

@@ -650,6 +650,30 @@ struct MOSFET : Device {
     }
     return ich - ibd - iqv[1] - iqv[4];
   }
+  void loadAC(ACCtx& c) override {  // device/mosfet.go:779-813
+    typedef std::complex<double> cx;
+    double o[7];
+    channel(acc.vgs, acc.vds, acc.vbs, o);
+    double gch[3];
+    if (o[0] > 0) { gch[0] = o[2]; gch[1] = o[3]; gch[2] = o[4]; }
+    else { gch[0] = -o[2]; gch[1] = o[2] + o[3] + o[4]; gch[2] = -o[4]; }
+    double ib, gbsA, gbdA;
+    bulkDiode(acc.vbs, iss, &ib, &gbsA);
+    bulkDiode(acc.vbd, isd, &ib, &gbdA);
+    double mc[3], q, cbsA, cbdA;
+    meyerCaps(acc.vgs, acc.vgd, o[5], o[6], o[0], mc);
+    bulkCharge(acc.vbs, czbs, czbssw, &q, &cbsA);
+    bulkCharge(acc.vbd, czbd, czbdsw, &q, &cbdA);
+    double cap[5] = {mc[0] + cgso, mc[1] + cgdo, mc[2] + cgbo, cbsA, cbdA};
+    int ctrlP[3] = {g, dp, b}, ctrlN[3] = {sp, sp, sp};
+    for (int k = 0; k < 3; k++) c.branch(dp, sp, gch[k], ctrlP[k], ctrlN[k], 0.0, 0, 0);
+    c.stampY(b, sp, gbsA);
+    c.stampY(b, dp, gbdA);
+    int ends[5][2] = {{g, sp}, {g, dp}, {g, b}, {b, sp}, {b, dp}};
+    for (int k = 0; k < 5; k++) c.stampY(ends[k][0], ends[k][1], cx(0, c.omega * cap[k]));
+    if (dp != ud) c.stampY(ud, dp, gdpr);
+    if (sp != us) c.stampY(us, sp, gspr);
+  }
   void accept(const double* x, double t, int md) override {  // :668-705
     double vgs_, vds_, vbs_, vgb_;
     voltages(x, &vgs_, &vds_, &vbs_, &vgb_);

@@ -9,6 +9,7 @@
 // Auto picks Dense below 30 unknowns (solver/matrix.go:74-85).
 #pragma once
 #include <cmath>
+#include <complex>
 #include <cstdint>
 #include <cstring>
 #include <map>
@@ -324,5 +325,55 @@ struct Sparse : Matrix {
     return SOLVE_OK;
   }
 };
+
+// CDense, solver/cdense.go:77-193: complex LU with partial pivoting on |entry|
+// (hypot), the column-relative singular test of Dense, non-finite checks.
+inline int cdense_solve(int n, std::vector<std::complex<double>> lu, const std::vector<std::complex<double>>& b,
+                        std::vector<std::complex<double>>& x) {
+  auto finite = [](std::complex<double> v) { return std::isfinite(v.real()) && std::isfinite(v.imag()); };
+  double scale = 0;
+  for (auto& v : lu) {
+    if (!finite(v)) return SOLVE_NONFINITE;
+    scale = std::max(scale, std::abs(v));
+  }
+  if (scale == 0) return SOLVE_SINGULAR;
+  std::vector<double> col(n, 0.0);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) col[j] = std::max(col[j], std::abs(lu[(size_t)i * n + j]));
+  std::vector<int> piv(n);
+  for (int k = 0; k < n; k++) {
+    int p = k;
+    double maxv = std::abs(lu[(size_t)k * n + k]);
+    for (int i = k + 1; i < n; i++) {
+      double v = std::abs(lu[(size_t)i * n + k]);
+      if (v > maxv) { maxv = v; p = i; }
+    }
+    if (maxv <= col[k] * (double)n * 1e-14) return SOLVE_SINGULAR;
+    piv[k] = p;
+    if (p != k)
+      for (int j = 0; j < n; j++) std::swap(lu[(size_t)k * n + j], lu[(size_t)p * n + j]);
+    std::complex<double> pivot = lu[(size_t)k * n + k];
+    for (int i = k + 1; i < n; i++) {
+      std::complex<double> f = lu[(size_t)i * n + k] / pivot;
+      lu[(size_t)i * n + k] = f;
+      if (f == 0.0) continue;
+      for (int j = k + 1; j < n; j++) lu[(size_t)i * n + j] -= f * lu[(size_t)k * n + j];
+    }
+  }
+  x = b;
+  for (int k = 0; k < n; k++) if (piv[k] != k) std::swap(x[k], x[piv[k]]);
+  for (int i = 0; i < n; i++) {
+    std::complex<double> s = x[i];
+    for (int j = 0; j < i; j++) s -= lu[(size_t)i * n + j] * x[j];
+    x[i] = s;
+  }
+  for (int i = n - 1; i >= 0; i--) {
+    std::complex<double> s = x[i];
+    for (int j = i + 1; j < n; j++) s -= lu[(size_t)i * n + j] * x[j];
+    x[i] = s / lu[(size_t)i * n + i];
+  }
+  for (auto& v : x) if (!finite(v)) return SOLVE_NONFINITE;
+  return SOLVE_OK;
+}
 
 }  // namespace kso

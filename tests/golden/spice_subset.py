@@ -139,7 +139,8 @@ def _parse(text):
                 ckt["analyses"].append({"kind": "tran", "step": nums[0], "stop": nums[1], "start": nums[2],
                                         "max_step": nums[3], "uic": uic})
             elif head == ".ac":
-                return None, "AC analysis (not an engine row yet)"
+                ckt["analyses"].append({"kind": "ac", "variation": toks[1].lower(), "points": int(value(toks[2])),
+                                        "fstart": value(toks[3]), "fstop": value(toks[4])})
             else:
                 return None, "unsupported control line " + head
             continue

@@ -122,3 +122,58 @@ def sweep_values(start, stop, step):
     n = (stop - start) / step
     count = int(math.floor(n + 1e-9)) + 1
     return [start + k * step for k in range(count)]
+
+
+def ac_frequencies(variation, points, fstart, fstop):
+    """ACSpec.Frequencies, analysis/ac.go:33-72."""
+    import math
+    if points < 1 or fstop < fstart or fstart < 0:
+        raise ValueError("bad AC spec")
+    if variation == "lin":
+        if points == 1:
+            return [fstart]
+        step = (fstop - fstart) / (points - 1)
+        return [fstart + k * step for k in range(points)]
+    base = 10.0 if variation == "dec" else 2.0
+    ratio = math.pow(base, 1.0 / points)
+    n = int(math.floor(math.log(fstop / fstart) / math.log(ratio) + 1e-9)) + 1
+    return [fstart * math.pow(ratio, k) for k in range(n)]
+
+
+AC_REL, AC_PHASE_DEG = 1e-6, 1e-4  # internal/golden/golden.go:290-295
+
+
+def compare_ac(freq, get, want):
+    """CompareAC, internal/golden/golden.go:297-340: vm() to 1e-6 relative, vp() to 1e-4 degrees."""
+    import cmath
+    import math
+    msgs = []
+    xs = want["xs"]
+    if len(freq) != len(xs):
+        return ["frequency count %d, want %d" % (len(freq), len(xs))]
+    for k in range(len(freq)):
+        if abs(freq[k] - xs[k]) > 1e-9 * xs[k]:
+            return ["frequency %d is %g, want %g" % (k, freq[k], xs[k])]
+    for name in want["names"]:
+        if len(name) < 4 or name[:3] not in ("vm(", "vp("):
+            msgs.append("%s: unsupported AC column" % name)
+            continue
+        v = get(name[3:-1])
+        if v is None:
+            msgs.append("%s: node not in simulation" % name)
+            continue
+        for k, ref in enumerate(want["columns"][name]):
+            if name[:3] == "vm(":
+                got = abs(v[k])
+                if abs(got - ref) > AC_REL * max(abs(ref), 1e-12):
+                    msgs.append("%s at %g Hz: got %.10g, want %.10g" % (name, freq[k], got, ref))
+                    break
+            else:
+                got = cmath.phase(v[k]) * 180 / math.pi
+                d = math.fmod(abs(got - ref), 360)
+                if d > 180:
+                    d = 360 - d
+                if d > AC_PHASE_DEG:
+                    msgs.append("%s at %g Hz: got %.8g, want %.8g" % (name, freq[k], got, ref))
+                    break
+    return msgs

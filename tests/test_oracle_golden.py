@@ -1,7 +1,7 @@
 """Pin the CPU oracle against the reference's golden vectors.
 
 Mirrors TestGolden and TestNgspiceTwin (analysis/op_test.go:116-158, checkGolden
-:161-284): every in-scope golden netlist runs on the dense and on the sparse
+:161-284; AC at :214-236): every in-scope golden netlist runs on the dense and on the sparse
 backend and must match the independent reference (testdata/golden) and the
 ngspice-39 twin (testdata/golden/ngspice) with internal/golden/golden.go's
 tolerances.  The fixtures come from tests/golden/make_reference_fixtures.py.
@@ -70,6 +70,17 @@ def run_case(case, src, backend):
             e = ckt.element_index(name[2:-1])
             return None if e < 0 else cur[:, e]
         return gc.compare_sweep(vals, get, want)
+    acs = [a for a in an if a["kind"] == "ac"]
+    if acs:
+        a = acs[0]
+        freqs = gc.ac_frequencies(a["variation"], a["points"], a["fstart"], a["fstop"])
+        st, x, msg = orc.ac(pk, freqs, opt)
+        assert st == 0, msg
+
+        def get(node):
+            i = ckt.node_index(node)
+            return None if i < 0 else (np.zeros(len(freqs), complex) if i == 0 else x[:, i - 1])
+        return gc.compare_ac(freqs, get, want)
     tr = [a for a in an if a["kind"] == "tran"][-1]
     spec = orc.TranSpec(tr["step"], tr["stop"], tr["start"], tr["max_step"], int(tr["uic"]), 0, 0, 0, 0, 0, 0)
     st, t, x, cur, steps, iters, msg = orc.tran(pk, spec, opt)
@@ -94,5 +105,6 @@ def test_oracle_matches_golden(case, src, backend):
 
 
 def test_in_scope_cases_are_many():
-    # 27 of the reference's 45 golden netlists use only the engine's element kinds
-    assert sum(1 for c in CASES if not c["skip"]) >= 27
+    # 33 of the reference's 45 golden netlists use only the engine's element
+    # kinds and analyses (OP, DC sweep, transient, AC)
+    assert sum(1 for c in CASES if not c["skip"]) >= 33
