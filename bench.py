@@ -36,7 +36,10 @@ UNIT = "solves/s"
 RELTOL = 1e-6
 # workload -> (default circuits, compulsory bytes per solve: parameters in + node voltages out, 8 B each)
 WORKLOADS = {"bjt_ce": (16384, (7 + 5) * 8), "cmos_opamp": (65536, (24 + 7) * 8), "rc_ladder": (4096, 0),
-             "random_netlists": (8192, 0)}
+             "random_netlists": (8192, 0), "bjt_ce_ac": (16384, 0)}
+# AC workload: unit of work = the small-signal solve of one circuit at one frequency
+AC_UNIT = "AC frequency points/s"
+AC_SPEC = ("dec", 10, 10.0, 1e10)  # 10 points per decade, 10 Hz .. 10 GHz: 91 frequencies
 RANDOM_SPEC = dict(step=5e-9, stop=2000 * 5e-9, fixed_step=True, method="trap")  # 2,000 TRAP steps of 5 ns
 # transient workloads: unit of work = one accepted time point of one circuit
 TRAN_UNIT = "accepted time points/s"
@@ -46,7 +49,7 @@ RC_LADDER_SPEC = dict(step=10e-9, stop=10e-6, fixed_step=True, method="trap")  #
 def generator(name):
     from kronspice_gb300 import workloads
     return {"bjt_ce": workloads.bjt_ce_batch, "cmos_opamp": workloads.cmos_opamp_batch,
-            "rc_ladder": workloads.rc_ladder_batch}[name]
+            "rc_ladder": workloads.rc_ladder_batch, "bjt_ce_ac": workloads.bjt_ce_ac_batch}[name]
 
 
 def parse():
@@ -225,6 +228,54 @@ def run_reference_multi(args):
     print(json.dumps(line))
 
 
+def oracle_ac_points(el, nn, vals, freqs, nthreads, reps_min_wall=1.0, max_reps=50):
+    """AC sweeps of the oracle over a thread pool (each call releases the GIL):
+    (converged frequency points per second, passes, wall seconds)."""
+    from oracle import oracle as orc
+    import concurrent.futures as cf
+    opt = orc.options(reltol=RELTOL)
+
+    def one(i):
+        st, _, _ = orc.ac(orc.Packed(el, nn, vals[i]), freqs, opt)
+        return len(freqs) if st == 0 else 0
+    with cf.ThreadPoolExecutor(max_workers=nthreads) as ex:
+        list(ex.map(one, range(min(len(vals), nthreads))))  # warm-up
+        t0 = time.perf_counter()
+        pts, reps = 0, 0
+        while True:
+            pts += sum(ex.map(one, range(len(vals))))
+            reps += 1
+            wall = time.perf_counter() - t0
+            if wall >= reps_min_wall or reps >= max_reps:
+                break
+    return pts / wall, reps, wall
+
+
+def run_reference_ac(args):
+    from kronspice_gb300 import analysis
+    from oracle import oracle as orc
+    orc.build()
+    nthreads = os.cpu_count() or 1
+    el, nn, vals = generator(args.workload)(args.n_circ, args.seed)
+    freqs = analysis.ACSpec(*AC_SPEC).frequencies()
+    samp = vals[:min(len(vals), 64 * nthreads)]  # a bounded sample of the batch per step
+    oracle_ac_points(el, nn, samp[:nthreads], freqs, nthreads, 0.0, max(1, args.warmup))
+    value, reps, wall = oracle_ac_points(el, nn, samp, freqs, nthreads, 0.0, max(1, args.steps))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": AC_UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / reps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 complex",
+            "data": "synthetic (seeded Philox)",
+            "config": {"workload": "bjt_ce_ac_%d" % args.n_circ, "n_circuits": args.n_circ,
+                       "frequencies": len(freqs), "sweep": "dec 10 points, 10 Hz .. 10 GHz", "reltol": RELTOL,
+                       "host_threads": nthreads},
+            "cpu_baseline": {"value": value, "unit": AC_UNIT, "cores": nthreads, "kind": "port",
+                             "sample": "%d of the %d circuits per step (operating point, polish and %d complex "
+                                       "solves each) on %d host threads; oracle/ks_oracle.cpp (C++ restatement "
+                                       "of the Go path)" % (len(samp), args.n_circ, len(freqs), nthreads)},
+            "e2e": {"value": value, "unit": AC_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -234,6 +285,9 @@ def run_reference(args):
         return
     if args.workload == "random_netlists":
         run_reference_multi(args)
+        return
+    if args.workload == "bjt_ce_ac":
+        run_reference_ac(args)
         return
     el, nn, vals = generator(args.workload)(args.n_circ, args.seed)
     from oracle import oracle as orc
@@ -606,6 +660,192 @@ def bench_multi(args):
         torch.distributed.barrier()
 
 
+def bench_ac(args):
+    """AC sweeps of 16,384 seeded common-emitter amplifiers (input coupling and
+    emitter bypass capacitors, Gummel-Poon transistor with junction, transit-time
+    and substrate charges), 91 frequencies from 10 Hz to 10 GHz; unit of work =
+    one circuit's small-signal solve at one frequency.  One step = ks_ac_async:
+    operating point + polish + model + sweep of every circuit."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from kronspice_gb300 import analysis, build
+    build.build()
+    dev = torch.device("cuda", local)
+    el, nn, vals = generator(args.workload)(args.n_circ, args.seed + rank)
+    B = vals.shape[0]
+    plan = analysis.Plan(el, nn, vals.shape[1])
+    batch = analysis.Batch(plan, vals)
+    n = plan.n
+    freqs = analysis.ACSpec(*AC_SPEC).frequencies()
+    nf = len(freqs)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    f_dev = torch.from_numpy(freqs).to(dev)
+    xac = torch.empty((B, nf, n, 2), dtype=torch.float64, device=dev)
+    x_op = torch.empty((B, n), dtype=torch.float64, device=dev)
+    ints = torch.empty((3, B), dtype=torch.int32, device=dev)  # status, iters, sweep status
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    try:
+        kname, csec = plan.specialize("op")
+        spec_info = {"kernel": kname, "nvrtc_s": csec}
+    except RuntimeError as e:
+        spec_info = {"kernel": None, "error": str(e)[:200]}
+    spec_ok = spec_info["kernel"] is not None
+    plain_opt = analysis.Options(reltol=RELTOL, precision="fp64", kernel="generic")
+    chosen_opt = analysis.Options(reltol=RELTOL, precision="fp64", kernel="specialized" if spec_ok else "generic")
+
+    def step(opt):
+        batch.ac_async(opt, None, f_dev.data_ptr(), nf, xac.data_ptr(), ints[0].data_ptr(), ints[1].data_ptr(), sh)
+
+    def sweep(opt):
+        batch.ac_at_async(opt, x_op.data_ptr(), ints[0].data_ptr(), f_dev.data_ptr(), nf, xac.data_ptr(),
+                          ints[2].data_ptr(), sh)
+
+    def timed(fn, opt):
+        for _ in range(args.warmup):
+            fn(opt)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        evs = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn(opt)
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        total = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+        if world > 1:
+            t = torch.tensor([total], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total = float(t.item())
+        iv = ints.cpu().numpy()
+        return {"seconds": total, "ms_per_step": total / args.steps * 1e3, "ok": int((iv[0] == 0).sum()),
+                "iters_mean": float(iv[1].mean()), "status": iv[0].copy()}
+
+    clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp",
+                              "bench_clocks_%d.csv" % rank))
+    with clk:
+        plain = timed(step, plain_opt)
+        chosen = timed(step, chosen_opt)
+        x_chosen = xac[:64].cpu().numpy()
+        st_chosen = chosen["status"]
+        # the sweep alone (k_ac_model + k_ac_solve) about the operating points
+        batch.op_async(chosen_opt, None, x_op.data_ptr(), ints[0].data_ptr(), ints[1].data_ptr(), sh)
+        sw = timed(sweep, chosen_opt)
+    clocks = clk.summary(local)
+
+    # end to end through the C ABI: pinned host values in, host phasors out
+    L = __import__("kronspice_gb300._lib", fromlist=["x"]).load()
+    vals_pin = torch.from_numpy(vals.copy()).pin_memory()
+    x_host = torch.empty((B, nf, n, 2), dtype=torch.float64).pin_memory()
+    s_host = np.zeros(B, dtype=np.int32)
+    i_host = np.zeros(B, dtype=np.int32)
+    o = chosen_opt.c()
+
+    def e2e_step():
+        rc = L.ks_batch_set_values(batch.handle, ctypes.c_void_p(vals_pin.data_ptr()), 0, sh)
+        assert rc == 0
+        rc = L.ks_ac(batch.handle, ctypes.byref(o), None, freqs.ctypes.data, nf, ctypes.c_void_p(x_host.data_ptr()),
+                     s_host.ctypes.data, i_host.ctypes.data, sh)
+        assert rc == 0
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_t = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        torch.cuda.synchronize()
+        e2e_t += time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_t], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_value = world * int((s_host == 0).sum()) * nf * args.steps / e2e_t
+    value = world * chosen["ok"] * nf * args.steps / chosen["seconds"]
+    plain_value = world * plain["ok"] * nf * args.steps / plain["seconds"]
+    sweep_value = world * sw["ok"] * nf * args.steps / sw["seconds"]
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return
+
+    # accuracy against the oracle on a sample, relative to each unknown's largest magnitude over the sweep
+    from oracle import oracle as orc
+    orc.build()
+    worst = 0.0
+    for c in range(64):
+        so, xo, _ = orc.ac(orc.Packed(el, nn, vals[c]), freqs, orc.options(reltol=RELTOL))
+        if so or st_chosen[c]:
+            continue
+        xg = x_chosen[c, ..., 0] + 1j * x_chosen[c, ..., 1]
+        scale = np.maximum(np.abs(xo).max(axis=0), 1e-5 * np.abs(xo).max())
+        worst = max(worst, float((np.abs(xg - xo) / scale).max()))
+    nthreads = os.cpu_count() or 1
+    cval, reps, cwall = oracle_ac_points(el, nn, vals[:min(B, 16 * nthreads)], freqs, nthreads, 1.0, 20)
+    cpu = {"value": cval, "unit": AC_UNIT, "cores": nthreads, "kind": "port",
+           "sample": "%d passes over %d of the circuits (operating point, polish, %d complex solves each; %.2f s "
+                     "wall); oracle/ks_oracle.cpp" % (reps, min(B, 16 * nthreads), nf, cwall)}
+
+    # roofline of the sweep kernels: phasors out (16 B per unknown per point) plus each circuit's
+    # values, operating point and G / C / b columns once; FP64-bound (complex LU per point)
+    per_launch_s = sw["seconds"] / args.steps
+    alg_bytes = B * (nf * n * 16 + vals.shape[1] * 8 + n * 8 + (2 * n * n + 2 * n) * 8 * 2)
+    achieved = alg_bytes / per_launch_s / 1e9
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    # FP64 operations of one point (complex multiply-add = 8): Y build 2n^2, LU sum_k (n-k-1)^2 * 8 +
+    # (n-k-1) * 6, substitutions 8 n^2
+    lu = sum((n - k - 1) ** 2 * 8 + (n - k - 1) * 6 for k in range(n))
+    flops = 2 * n * n + lu + 8 * n * n
+    prof = traffic_from_profile().get("k_ac_solve_bjt_ce_ac", {})
+    traffic = prof.get("dram_bytes_per_circuit")
+    line = {
+        "metric": METRIC, "value": value, "unit": AC_UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": chosen["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 complex", "data": "synthetic (seeded Philox)",
+        "config": {"workload": "bjt_ce_ac_%d" % B, "n_circuits_per_gpu": B, "n_unknowns": n, "frequencies": nf,
+                   "sweep": "dec 10 points, 10 Hz .. 10 GHz", "reltol": RELTOL,
+                   "l2": "flushed between timed steps (512 MB write); the 238 MB phasor output is written once"},
+        "plain": {"value": plain_value, "ms_per_step": plain["ms_per_step"], "op_kernel": "generic"},
+        "chosen": {"value": value, "op_kernel": chosen_opt.kernel, "newton_iters_mean": chosen["iters_mean"]},
+        "chosen_vs_plain": value / plain_value if plain_value else None,
+        "sweep_only": {"value": sweep_value, "ms_per_step": sw["ms_per_step"]},
+        "per_topology_kernel": spec_info,
+        "max_phasor_err_vs_oracle_rel": worst,
+        "e2e": {"value": e2e_value, "unit": AC_UNIT, "h2d_bytes_per_step": int(vals.nbytes + freqs.nbytes),
+                "d2h_bytes_per_step": int(x_host.numel() * 8 + s_host.nbytes + i_host.nbytes)},
+        "gpu_launches": 5 * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None if traffic is None else traffic * B, "kernel": "k_ac_model + k_ac_solve",
+                     "algorithmic_bytes_per_circuit": alg_bytes / B, "kernel_ms": per_launch_s * 1e3,
+                     "fp64_flops_per_point": flops,
+                     "fp64_tflops": flops * B * nf / per_launch_s / 1e12,
+                     "note": "the sweep is bound by FP64 issue (complex LU per point, one point per thread; "
+                             "GB300 has 2 FP64 lanes/clk/SM, 1.25 TFLOP/s nominal), not by HBM"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.barrier()
+
+
 def main():
     args = parse()
     if args.n_circ <= 0:
@@ -618,6 +858,9 @@ def main():
         return
     if args.workload == "random_netlists":
         bench_multi(args)
+        return
+    if args.workload == "bjt_ce_ac":
+        bench_ac(args)
         return
     import torch
     rank, world, local = dist_env()

@@ -8,6 +8,7 @@
  *   (*Sim).dcSolve         analysis/newton.go:95     -> ks_op (fallback chain on device)
  *   analysis.Tran          analysis/tran.go:70       -> ks_tran
  *   analysis.DC            analysis/dc.go:51         -> ks_op with per-point source overrides
+ *   analysis.AC            analysis/ac.go:76         -> ks_ac
  *   analysis.Options       analysis/op.go:22-62      -> ks_options
  *   analysis.TranSpec/TranOptions analysis/tran.go:26-40 -> ks_tran_spec
  *   solver sentinels       solver/matrix.go:15-20,
@@ -339,6 +340,42 @@ int ks_op(ks_batch* b, const ks_options* opt, const double* x0, double* out_x,
  * stream).  x0_dev may be NULL. */
 int ks_op_async(ks_batch* b, const ks_options* opt, const double* x0_dev, double* out_x_dev,
                 int32_t* out_status_dev, int32_t* out_iters_dev, void* stream);
+
+/*
+ * AC small-signal sweep of every circuit of the batch (analysis.AC,
+ * analysis/ac.go:76-150): the operating point (as ks_op, followed by the
+ * polish of analysis/op.go:251-271: up to two more FP64 solves), then for each
+ * frequency f the complex system (G + j*2*pi*f*C) x = b of the devices' LoadAC
+ * stamps, solved as solver/cdense.go does.  freqs [n_freq] in Hz, the list of
+ * ACSpec.Frequencies (analysis/ac.go:33-72; made by the caller).
+ * out_x [n_circ][n_freq][n][2]: every unknown's phasor (real, imaginary), node
+ * voltages first (x[i] is node i+1), zeros at a frequency whose solve failed
+ * and at every frequency of a circuit whose operating point failed.
+ * out_status [n_circ]: the operating point's status, else that of the first
+ * failing frequency (KS_STATUS_SINGULAR: "f = %g Hz: singular matrix",
+ * KS_STATUS_NONFINITE).  out_iters [n_circ]: Newton solves of the operating point.
+ * ks_options.precision chooses the operating point's LU as in ks_op; the polish
+ * and the AC solves are FP64.  Replaces analysis.AC per circuit (ledger and
+ * element currents are the caller's post-processing of the phasors).
+ */
+int ks_ac(ks_batch* b, const ks_options* opt, const double* x0, const double* freqs, int32_t n_freq,
+          double* out_x, int32_t* out_status, int32_t* out_iters, void* stream);
+
+/* Same, on device buffers (freqs_dev, out_x_dev, out_status_dev, out_iters_dev;
+ * x0_dev, out_status_dev and out_iters_dev may be NULL), asynchronous on
+ * `stream` (NULL: the batch's own stream). */
+int ks_ac_async(ks_batch* b, const ks_options* opt, const double* x0_dev, const double* freqs_dev,
+                int32_t n_freq, double* out_x_dev, int32_t* out_status_dev, int32_t* out_iters_dev, void* stream);
+
+/* The sweep alone, about operating points the caller already has (device
+ * buffers): x_op_dev [n_circ][n] (a ks_op / ks_op_async result; the small-signal
+ * model is taken at exactly these values, so pass polished points for results
+ * independent of the Newton tolerance), status_dev [n_circ] (NULL: all solved;
+ * circuits with a non-zero status are skipped).  out_status_dev receives
+ * status_dev updated with each circuit's first failing frequency.  Only
+ * ks_options.gmin is read. */
+int ks_ac_at(ks_batch* b, const ks_options* opt, const double* x_op_dev, const int32_t* status_dev,
+             const double* freqs_dev, int32_t n_freq, double* out_x_dev, int32_t* out_status_dev, void* stream);
 
 /*
  * Transient analysis of every circuit of the batch (analysis.Tran for each).

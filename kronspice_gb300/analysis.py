@@ -215,6 +215,37 @@ class Batch:
                                          wave_dev, npts_dev, status_dev, steps_dev, iters_dev, stream),
                "ks_tran_async")
 
+    def ac(self, freqs, opt=None, x0=None, stream=None):
+        """analysis.AC for every circuit (ks_ac): (x [n_circ][n_freq][n] complex,
+        status [n_circ], operating-point iterations [n_circ])."""
+        o = (opt or Options()).c()
+        f = np.ascontiguousarray(freqs, dtype=np.float64)
+        if f.ndim != 1 or len(f) == 0:
+            raise ValueError("ac: freqs must be a non-empty 1-D array")
+        x = np.zeros((self.n_circ, len(f), self.plan.n, 2))
+        st = np.zeros(self.n_circ, dtype=np.int32)
+        it = np.zeros(self.n_circ, dtype=np.int32)
+        x0a = None
+        if x0 is not None:
+            x0a = np.ascontiguousarray(x0, dtype=np.float64)
+            assert x0a.shape == (self.n_circ, self.plan.n)
+        _check(_lib.load().ks_ac(self.handle, ctypes.byref(o), None if x0a is None else x0a.ctypes.data,
+                                 f.ctypes.data, len(f), x.ctypes.data, st.ctypes.data, it.ctypes.data, stream),
+               "ks_ac")
+        return x[..., 0] + 1j * x[..., 1], st, it
+
+    def ac_async(self, opt, x0_dev, freqs_dev, n_freq, x_dev, status_dev, iters_dev, stream):
+        """ks_ac_async on device pointers (ints) on a CUDA stream handle."""
+        o = (opt or Options()).c()
+        _check(_lib.load().ks_ac_async(self.handle, ctypes.byref(o), x0_dev, freqs_dev, n_freq, x_dev, status_dev,
+                                       iters_dev, stream), "ks_ac_async")
+
+    def ac_at_async(self, opt, x_op_dev, status_dev, freqs_dev, n_freq, x_dev, out_status_dev, stream):
+        """ks_ac_at: the sweep alone about given operating points (device pointers)."""
+        o = (opt or Options()).c()
+        _check(_lib.load().ks_ac_at(self.handle, ctypes.byref(o), x_op_dev, status_dev, freqs_dev, n_freq, x_dev,
+                                    out_status_dev, stream), "ks_ac_at")
+
     def op_async(self, opt, x0_dev, x_dev, status_dev, iters_dev, stream):
         """ks_op_async on device pointers (ints) on a CUDA stream handle."""
         o = (opt or Options()).c()
@@ -380,4 +411,86 @@ def op_batch(circuits, opt=None, nodeset=None):
             nv_ = np.zeros(c.n_nodes)
             nv_[1:] = x[r, :c.n_nodes - 1]
             results[i] = Result(list(c.node_names), nv_, x[r].copy(), int(it[r]))
+    return results, errors
+
+
+class ErrBadACSpec(KronspiceError):
+    """analysis.ErrBadACSpec (analysis/ac.go:16)."""
+
+
+MAX_AC_POINTS = 1_000_000  # analysis/ac.go:29
+
+
+@dataclass
+class ACSpec:
+    """analysis.ACSpec (analysis/ac.go:19-24)."""
+    variation: str   # "dec", "oct" or "lin"
+    points: int      # per decade / per octave, or total for lin
+    fstart: float
+    fstop: float
+
+    def frequencies(self):
+        """ACSpec.Frequencies (analysis/ac.go:33-72): the sweep's frequencies in Hz."""
+        import math
+        p, f0, f1 = self.points, self.fstart, self.fstop
+        if p < 1 or f1 < f0 or f0 < 0 or math.isnan(f0 + f1) or math.isinf(f1):
+            raise ErrBadACSpec("analysis: invalid AC specification: %r" % (self,))
+        if self.variation == "lin":
+            if p == 1:
+                return np.array([f0])
+            step = (f1 - f0) / (p - 1)
+            out = [f0 + k * step for k in range(p)]
+        elif self.variation in ("dec", "oct"):
+            if f0 <= 0:
+                raise ErrBadACSpec("analysis: invalid AC specification: logarithmic sweep needs fstart > 0")
+            ratio = math.pow(10.0 if self.variation == "dec" else 2.0, 1.0 / p)
+            n = int(math.floor(math.log(f1 / f0) / math.log(ratio) + 1e-9)) + 1
+            if n > MAX_AC_POINTS:
+                raise ErrBadACSpec("analysis: invalid AC specification: %d points" % n)
+            out = [f0 * math.pow(ratio, k) for k in range(n)]
+        else:
+            raise ErrBadACSpec("analysis: invalid AC specification: sweep type %r" % self.variation)
+        if len(out) > MAX_AC_POINTS:
+            raise ErrBadACSpec("analysis: invalid AC specification: %d points" % len(out))
+        return np.array(out)
+
+
+@dataclass
+class ACResult:
+    """The phasor part of output.ACResult (output/result.go): V[node][freq], ground first."""
+    node_names: list
+    freq: np.ndarray
+    node_voltages: np.ndarray          # [n_nodes][n_freq] complex, row 0 (ground) zero
+    x: np.ndarray                      # [n_freq][n] complex, all MNA unknowns
+    iterations: int = 0
+
+
+def ac_batch(circuits, spec, opt=None):
+    """analysis.AC for every circuit: (results, errors), one entry per circuit."""
+    opt = opt or Options()
+    freqs = spec.frequencies() if hasattr(spec, "frequencies") else np.asarray(spec, dtype=np.float64)
+    results, errors = [None] * len(circuits), [None] * len(circuits)
+    groups, packed = {}, []
+    for i, c in enumerate(circuits):
+        err = validate(c)
+        if err is not None:
+            errors[i] = err
+            packed.append(None)
+            continue
+        el, vals, key = c.pack()
+        packed.append((el, vals))
+        groups.setdefault(key, []).append(i)
+    for key, idx in groups.items():
+        el = packed[idx[0]][0]
+        plan = Plan(el, circuits[idx[0]].n_nodes, len(packed[idx[0]][1]))
+        b = Batch(plan, np.stack([packed[i][1] for i in idx]))
+        x, st, it = b.ac(freqs, opt)
+        for r, i in enumerate(idx):
+            if st[r] != 0:
+                errors[i] = status_error(st[r])
+                continue
+            c = circuits[i]
+            v = np.zeros((c.n_nodes, len(freqs)), dtype=complex)
+            v[1:] = x[r, :, :c.n_nodes - 1].T
+            results[i] = ACResult(list(c.node_names), freqs, v, x[r].copy(), int(it[r]))
     return results, errors

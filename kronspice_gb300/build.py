@@ -18,7 +18,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "550"]
 
-UNITS = ["ks_host.cpp", "ks_api.cu", "ks_kernels.cu", "ks_tran.cu", "ks_mlp.cu", "ks_jit.cpp", "ks_noalloc.cu", "ks_sparse.cpp",
+UNITS = ["ks_host.cpp", "ks_api.cu", "ks_kernels.cu", "ks_tran.cu", "ks_mlp.cu", "ks_jit.cpp", "ks_noalloc.cu", "ks_ac.cu", "ks_sparse.cpp",
          "ks_multi.cu"]
 # device headers embedded in the library for the per-topology kernels (NVRTC),
 # under the names their #include lines use

@@ -53,6 +53,12 @@ struct ks_batch {
   double* d_time = nullptr;
   size_t d_time_elems = 0;
   int32_t* d_tints = nullptr;
+  // ks_ac's device scratch (operating point, G / C / b columns, status, first
+  // failing frequency) and output, kept between calls (grow only)
+  unsigned char* d_ac = nullptr;
+  size_t d_ac_bytes = 0;
+  double* d_acout = nullptr;
+  size_t d_acout_bytes = 0;
 };
 
 // Derived constants for an analysis with print step / stop time (0, 0 outside a transient).
@@ -130,9 +136,6 @@ extern "C" int ks_plan_info(const ks_plan* p, int32_t* n_unknowns, int32_t* n_va
 static int batch_stage(ks_batch* b, size_t bytes) {
   if (b->h_pin_bytes >= bytes) return KS_OK;
   if (b->h_pin) cudaFreeHost(b->h_pin);
-  cudaFree(b->d_wave);
-  cudaFree(b->d_time);
-  cudaFree(b->d_tints);
   b->h_pin = nullptr;
   b->h_pin_bytes = 0;
   CK(cudaMallocHost(&b->h_pin, bytes));
@@ -225,6 +228,8 @@ extern "C" void ks_batch_destroy(ks_batch* b) {
   cudaFree(b->d_wave);
   cudaFree(b->d_time);
   cudaFree(b->d_tints);
+  cudaFree(b->d_ac);
+  cudaFree(b->d_acout);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -346,6 +351,132 @@ extern "C" int ks_op(ks_batch* b, const ks_options* opt, const double* x0, doubl
   if (out_x) std::memcpy(out_x, hp_bytes, xbytes);
   if (out_status) std::memcpy(out_status, hp_bytes + xbytes, sizeof(int32_t) * B);
   if (out_iters) std::memcpy(out_iters, hp_bytes + xbytes + sizeof(int32_t) * B, sizeof(int32_t) * B);
+  return KS_OK;
+}
+
+static int grow(void** p, size_t* have, size_t need) {
+  if (*have >= need) return KS_OK;
+  cudaFree(*p);
+  *p = nullptr;
+  *have = 0;
+  if (cudaMalloc(p, need) != cudaSuccess) { set_error("ks_ac: device allocation failed"); return KS_ENOMEM; }
+  *have = need;
+  return KS_OK;
+}
+
+static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// ks_ac's device scratch: x at the operating point, status, first failing
+// frequency, then the G / C / b columns.
+struct AcScratch { double* x_op; int32_t* status; int32_t* err_at; double* cols; };
+
+static int ac_scratch(ks_batch* b, AcScratch* s) {
+  const int64_t B = b->B;
+  const int n = b->plan->hp.n;
+  const size_t xb = a256(sizeof(double) * n * B), sb = a256(sizeof(int32_t) * B);
+  const size_t need = xb + 2 * sb + sizeof(double) * ks_ac_scratch_doubles(n, B);
+  int rc = grow(reinterpret_cast<void**>(&b->d_ac), &b->d_ac_bytes, need);
+  if (rc) return rc;
+  s->x_op = reinterpret_cast<double*>(b->d_ac);
+  s->status = reinterpret_cast<int32_t*>(b->d_ac + xb);
+  s->err_at = reinterpret_cast<int32_t*>(b->d_ac + xb + sb);
+  s->cols = reinterpret_cast<double*>(b->d_ac + xb + 2 * sb);
+  return KS_OK;
+}
+
+static int ac_sweep(ks_batch* b, const KOpts& o, const double* x_op, int32_t* status, const double* freqs_dev,
+                    int32_t n_freq, double* out_x_dev, const AcScratch& s, cudaStream_t st) {
+  int rc = batch_setup(b, 0.0, 0.0, st);
+  if (rc) return rc;
+  rc = ks_launch_ac(b->dev, o.gmin, x_op, freqs_dev, n_freq, s.cols, s.err_at, status, out_x_dev, st);
+  if (rc == -2) { set_error("ks_ac: system too large for the AC kernel"); return KS_EUNSUPPORTED; }
+  if (rc) { set_error(std::string("ks_ac: kernel launch failed: ") + cudaGetErrorString(cudaGetLastError())); return KS_ECUDA; }
+  return KS_OK;
+}
+
+extern "C" int ks_ac_async(ks_batch* b, const ks_options* opt, const double* x0_dev, const double* freqs_dev,
+                           int32_t n_freq, double* out_x_dev, int32_t* out_status_dev, int32_t* out_iters_dev,
+                           void* stream) {
+  if (!b || n_freq <= 0 || !freqs_dev || !out_x_dev) { set_error("ks_ac: bad argument"); return KS_EINVAL; }
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+  AcScratch s;
+  int rc = ac_scratch(b, &s);
+  if (rc) return rc;
+  KOpts o = make_opts(opt);
+  o.polish = 1;
+  const KsSpec* ks = nullptr;
+  rc = pick_kernel(b, opt, ksj::KIND_OP, &ks);
+  if (rc) return rc;
+  rc = batch_setup(b, 0.0, 0.0, st);
+  if (rc) return rc;
+  rc = ks_launch_op(b->dev, o, x0_dev, s.x_op, s.status, out_iters_dev, opt ? opt->deadline_s : 0.0, st, ks);
+  if (rc == -2) { set_error("ks_ac: system too large for the dense kernels"); return KS_EUNSUPPORTED; }
+  if (rc && ks) return KS_ECUDA;
+  if (rc) { set_error(std::string("op kernel launch failed: ") + cudaGetErrorString(cudaGetLastError())); return KS_ECUDA; }
+  rc = ac_sweep(b, o, s.x_op, s.status, freqs_dev, n_freq, out_x_dev, s, st);
+  if (rc) return rc;
+  if (out_status_dev) CK(cudaMemcpyAsync(out_status_dev, s.status, sizeof(int32_t) * b->B, cudaMemcpyDeviceToDevice, st));
+  return KS_OK;
+}
+
+extern "C" int ks_ac_at(ks_batch* b, const ks_options* opt, const double* x_op_dev, const int32_t* status_dev,
+                        const double* freqs_dev, int32_t n_freq, double* out_x_dev, int32_t* out_status_dev,
+                        void* stream) {
+  if (!b || n_freq <= 0 || !x_op_dev || !freqs_dev || !out_x_dev || !out_status_dev) {
+    set_error("ks_ac_at: bad argument");
+    return KS_EINVAL;
+  }
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+  AcScratch s;
+  int rc = ac_scratch(b, &s);
+  if (rc) return rc;
+  if (status_dev) {
+    if (status_dev != out_status_dev)
+      CK(cudaMemcpyAsync(out_status_dev, status_dev, sizeof(int32_t) * b->B, cudaMemcpyDeviceToDevice, st));
+  } else {
+    CK(cudaMemsetAsync(out_status_dev, 0, sizeof(int32_t) * b->B, st));
+  }
+  return ac_sweep(b, make_opts(opt), x_op_dev, out_status_dev, freqs_dev, n_freq, out_x_dev, s, st);
+}
+
+extern "C" int ks_ac(ks_batch* b, const ks_options* opt, const double* x0, const double* freqs, int32_t n_freq,
+                     double* out_x, int32_t* out_status, int32_t* out_iters, void* stream) {
+  if (!b || n_freq <= 0 || !freqs) { set_error("ks_ac: bad argument"); return KS_EINVAL; }
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+  const size_t B = b->B, n = b->plan->hp.n;
+  const size_t xbytes = sizeof(double) * n * B, obytes = sizeof(double) * 2 * n * B * (size_t)n_freq;
+  const size_t fbytes = sizeof(double) * (size_t)n_freq;
+  const size_t fb = a256(fbytes);
+  int rc = grow(reinterpret_cast<void**>(&b->d_acout), &b->d_acout_bytes, a256(obytes) + fb);
+  if (rc) return rc;
+  double* d_freq = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(b->d_acout) + a256(obytes));
+  rc = batch_stage(b, std::max(obytes, std::max(xbytes, fbytes)) + 2 * sizeof(int32_t) * B + 64);
+  if (rc) return rc;
+  std::memcpy(b->h_pin, freqs, fbytes);
+  CK(cudaMemcpyAsync(d_freq, b->h_pin, fbytes, cudaMemcpyHostToDevice, st));
+  if (x0) {
+    // after the frequencies' copy has left the staging buffer
+    CK(cudaStreamSynchronize(st));
+    std::memcpy(b->h_pin, x0, xbytes);
+    CK(cudaMemcpyAsync(b->d_x0, b->h_pin, xbytes, cudaMemcpyHostToDevice, st));
+  }
+  rc = ks_ac_async(b, opt, x0 ? b->d_x0 : nullptr, d_freq, n_freq, b->d_acout, b->d_status, b->d_iters, st);
+  if (rc) return rc;
+  // page-locked output (cudaHostAlloc / cudaHostRegister) takes the phasors
+  // directly; pageable output goes through the batch's pinned staging
+  cudaPointerAttributes pa{};
+  const bool pinned_out = out_x && cudaPointerGetAttributes(&pa, out_x) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+  cudaGetLastError();  // a pageable pointer may leave an error behind on older drivers
+  char* hp_bytes = reinterpret_cast<char*>(b->h_pin);
+  const size_t xoff = pinned_out ? 0 : obytes;
+  if (pinned_out) CK(cudaMemcpyAsync(out_x, b->d_acout, obytes, cudaMemcpyDeviceToHost, st));
+  else if (out_x) CK(cudaMemcpyAsync(hp_bytes, b->d_acout, obytes, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hp_bytes + xoff, b->d_status, sizeof(int32_t) * B, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hp_bytes + xoff + sizeof(int32_t) * B, b->d_iters, sizeof(int32_t) * B, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (out_x && !pinned_out) std::memcpy(out_x, hp_bytes, obytes);
+  if (out_status) std::memcpy(out_status, hp_bytes + xoff, sizeof(int32_t) * B);
+  if (out_iters) std::memcpy(out_iters, hp_bytes + xoff + sizeof(int32_t) * B, sizeof(int32_t) * B);
   return KS_OK;
 }
 

@@ -86,6 +86,8 @@ struct KOpts {
   int32_t max_iter_total;  // bound on all solves of one circuit (0 = default)
   int32_t passes;          // mixed: most refinement passes per solve
   double refine_tol;       // mixed: refinement stops when the correction is below this fraction of x
+  int32_t polish;          // OP: the polish of analysis/op.go:251-271 (AC operating points)
+  int32_t reserved;
 };
 
 #ifndef __CUDACC_RTC__

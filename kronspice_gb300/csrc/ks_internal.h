@@ -64,6 +64,12 @@ int ks_launch_tran(const KsDeviceBatch& b, const KOpts& o, const ks_tran_spec& s
                    double deadline_s, void* stream, const KsSpec* kspec);
 int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, double* out_x, int32_t* out_status,
                  int32_t* out_iters, double deadline_s, void* stream, const KsSpec* kspec);
+// AC sweep after the operating point x_op [B][n] (ks_ac.cu): G / C / b columns in
+// scratch (ks_ac_scratch_doubles), out_x [B][nf][n][2]; status updated with the
+// first failing frequency.  -2: the system does not fit the solve kernel.
+size_t ks_ac_scratch_doubles(int n, int64_t B);
+int ks_launch_ac(const KsDeviceBatch& b, double gmin, const double* x_op, const double* freqs_dev, int32_t nf,
+                 double* scratch, int32_t* err_at, int32_t* status, double* out_x, void* stream);
 
 // One per-topology kernel of a plan on one device (ks_jit.cpp).
 struct KsSpec {

@@ -319,6 +319,25 @@ __device__ __forceinline__ void dc_advance(Thr<SY, P>& t, OpState& st, int res) 
   }
 }
 
+// polish, analysis/op.go:251-271: up to two more FP64 solves at the accepted
+// operating point, so that the small-signal model of an AC sweep is taken at x
+// exact to round-off instead of at the Newton tolerance.
+template <class SY, class P>
+__device__ __forceinline__ int polish(Thr<SY, P>& t, OpState& st, const LoadParams& lp) {
+  st.initJct = false; st.ptG = 0; st.diagGmin = 0; st.srcStepping = false; st.srcFact = 0; st.fp64 = true;
+  const int n = t.n();
+  for (int k = 0; k < 2; k++) {
+    int err = solve_once(t, st, lp);
+    if (err) return err;
+    bool done = true;
+#pragma unroll
+    for (int i = 0; i < n; i++)
+      if (prog_owns(t.prog, i) && fabs(t.s.xn(i) - t.s.xo(i)) > 1e-12 * fmax(1.0, fabs(t.s.xn(i)))) done = false;
+    if (prog_all(t.prog, done)) break;
+  }
+  return KS_STATUS_OK;
+}
+
 // The operating point of one circuit after another, pulled from the queue.
 template <class SY, class P>
 __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* values, const double* derived, double* state,
@@ -348,6 +367,10 @@ __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* value
     }
     if (!done) continue;
     if (st.status == KS_STATUS_OK) accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, ModeOP, o.gmin, false);
+    if (st.status == KS_STATUS_OK && o.polish && !t.prog.nonlin_empty) {
+      st.status = polish(t, st, lp);
+      if (st.status == KS_STATUS_OK) accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, ModeOP, o.gmin, false);
+    }
     if (out_x) {
       const int n = t.n();  // per circuit for the multi-topology kernels
       const int64_t base = t.prog.x_base(c, n);

@@ -66,6 +66,50 @@ def bjt_ce_features(vals, el):
     return np.stack(cols, axis=1)
 
 
+# ------------------------------------------------------------------ BJT CE small-signal sweep
+BJT_CE_AC_MODEL = {"is": 2e-15, "bf": 150.0, "vaf": 80.0, "ikf": 0.05, "rb": 120.0, "rbm": 40.0, "re": 0.8,
+                   "rc": 6.0, "cje": 1.2e-11, "vje": 0.75, "mje": 0.35, "tf": 3e-10, "xtf": 3.0, "vtf": 4.0,
+                   "itf": 0.04, "cjc": 5e-12, "vjc": 0.6, "mjc": 0.4, "xcjc": 0.6, "tr": 1e-08, "cjs": 3e-12,
+                   "vjs": 0.7, "mjs": 0.3}
+
+
+def bjt_ce_ac_template():
+    """Common-emitter amplifier with input coupling and emitter bypass capacitors and a
+    Gummel-Poon transistor with base, emitter and collector resistances and junction,
+    transit-time and substrate charges (the shape of the reference's bjt_ce_ac netlist):
+    10 unknowns (vcc, in, b, c, e, three internal transistor nodes, two source branches)."""
+    b = Builder("bjt common emitter, small signal")
+    b.voltage_source("VCC", "vcc", "0", 12.0)
+    b.voltage_source("VIN", "in", "0", 0.0, ac=(1.0, 0.0))
+    b.capacitor("CIN", "in", "b", 10e-6)
+    b.resistor("R1", "vcc", "b", 47e3)
+    b.resistor("R2", "b", "0", 10e3)
+    b.resistor("RC", "vcc", "c", 3.3e3)
+    b.resistor("RE", "e", "0", 1e3)
+    b.capacitor("CE", "e", "0", 100e-6)
+    b.model("qac", "npn", dict(BJT_CE_AC_MODEL))
+    b.bjt("Q1", "c", "b", "e", "qac")
+    return b.build()
+
+
+def bjt_ce_ac_batch(n_circ, seed=0):
+    """Bias divider R1 log-U[20k, 100k], R2 log-U[5k, 20k], RC log-U[1k, 10k], RE log-U[300, 3k] ohm,
+    Vcc U[5, 15] V, IS log-U[1e-16, 1e-14] A, BF U[50, 300], CJE / CJC / TF x log-U[0.5, 2]."""
+    c = bjt_ce_ac_template()
+    el, v0, off = _offsets(c)
+    g = rng(6, seed)
+    vals = np.tile(v0, (n_circ, 1))
+    q = off["Q1"]
+    vals[:, q + Q_KEYS.index("is")] = log_uniform(g, 1e-16, 1e-14, n_circ)
+    vals[:, q + Q_KEYS.index("bf")] = g.uniform(50, 300, n_circ)
+    for k in ("cje", "cjc", "tf"):
+        vals[:, q + Q_KEYS.index(k)] *= log_uniform(g, 0.5, 2.0, n_circ)
+    for r, lo, hi in (("R1", 20e3, 100e3), ("R2", 5e3, 20e3), ("RC", 1e3, 10e3), ("RE", 300, 3e3)):
+        vals[:, off[r]] = log_uniform(g, lo, hi, n_circ)
+    vals[:, off["VCC"]] = g.uniform(5, 15, n_circ)
+    return el, c.n_nodes, vals
+
+
 # ------------------------------------------------------------------ RC ladder transient
 def rc_ladder_template(sections=10):
     """V1 PULSE(0 1 0 1n 1n 1u) driving `sections` series-R shunt-C sections."""

@@ -64,6 +64,7 @@ def lib():
         L.kso_batch_op.argtypes = [P, P, ctypes.c_int, P, P, ctypes.c_int, P, P, P]
         L.kso_batch_tran.argtypes = [P, P, ctypes.c_int, P, P, ctypes.c_int, P, P, P, P]
         L.kso_unknowns.argtypes = [P, P, P, P]
+        L.kso_ac.argtypes = [P, P, P, P, ctypes.c_int, P, ctypes.c_char_p, ctypes.c_int]
         _lib = L
     return _lib
 

@@ -152,3 +152,33 @@ def test_per_topology_source_compiles_with_nvrtc():
     assert rc == nvrtc.nvrtcResult.NVRTC_SUCCESS, log.decode()[:2000]
     _, size = nvrtc.nvrtcGetCUBINSize(prog)
     assert size > 0
+
+
+def test_ac_frequencies_match_golden_sweeps():
+    """ACSpec.Frequencies (analysis/ac.go:33-72) reproduces the golden AC tables' frequency columns."""
+    import json
+    from kronspice_gb300.analysis import ACSpec
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_cases.json")) as f:
+        cases = [c for c in json.load(f)["cases"] if not c["skip"] and c["circuit"]["analyses"][0]["kind"] == "ac"]
+    assert cases
+    for c in cases:
+        a = c["circuit"]["analyses"][0]
+        got = ACSpec(a["variation"], a["points"], a["fstart"], a["fstop"]).frequencies()
+        for src, want in c["golden"].items():
+            assert len(got) == len(want["xs"]), (c["name"], src)
+            assert np.all(np.abs(got - np.array(want["xs"])) <= 1e-9 * np.array(want["xs"])), (c["name"], src)
+
+
+@pytest.mark.parametrize("spec", [("dec", 0, 1.0, 10.0), ("dec", 10, 10.0, 1.0), ("lin", 5, -1.0, 1.0),
+                                  ("dec", 10, 0.0, 1e3), ("log", 10, 1.0, 1e3), ("lin", 2, 1.0, float("inf")),
+                                  ("dec", 100000, 1.0, 1e30)])
+def test_ac_spec_rejects_bad_sweeps(spec):
+    from kronspice_gb300.analysis import ACSpec, ErrBadACSpec
+    with pytest.raises(ErrBadACSpec):
+        ACSpec(*spec).frequencies()
+
+
+def test_ac_lin_single_point():
+    from kronspice_gb300.analysis import ACSpec
+    assert list(ACSpec("lin", 1, 5.0, 5.0).frequencies()) == [5.0]
+    assert list(ACSpec("lin", 3, 0.0, 2.0).frequencies()) == [0.0, 1.0, 2.0]
