@@ -202,8 +202,9 @@ __global__ void k_ac_solve(int n, int64_t B, int32_t nf, const double* __restric
   double* Ai = Ar + (int64_t)nn * T;  // [nn][T]
   double* xr = Ai + (int64_t)nn * T;  // [n][T]
   double* xi = xr + (int64_t)n * T;
-  // squared column maxima [n][T], only compared against a tolerance: float
-  float* cm = reinterpret_cast<float*>(xi + (int64_t)n * T);
+  // squared column maxima [n][T], only compared against a tolerance: float,
+  // after the T threads' double arrays
+  float* cm = reinterpret_cast<float*>(sm + (int64_t)(2 * nn + 2 * n) * T) + tid;
   const int64_t units = B * (int64_t)nf;
   for (int64_t u = (int64_t)blockIdx.x * T + tid; u < units; u += (int64_t)gridDim.x * T) {
     const int32_t f = (int32_t)(u / B);
