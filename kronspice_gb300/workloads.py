@@ -278,3 +278,74 @@ def random_netlists(n_circ, seed=0, nodes=(10, 400)):
     """n_circ seeded random netlists of uneven size (the multi-topology workload)."""
     g = rng(3, seed)
     return [random_netlist(g, k, nodes) for k in range(n_circ)]
+
+
+# ------------------------------------------------------------------ power grid (Kron tearing)
+def power_grid_template(N=256, P=4, loads=1024, seed=0):
+    """An N x N resistive-capacitive power-grid mesh torn into P x P square pieces.
+
+    Grid node g{r}_{c}; resistor RH{r}_{c} to the right neighbour and RV{r}_{c} to
+    the one below (nominal 0.1 ohm), capacitor CG{r}_{c} to ground (10 pF).  One
+    supply pad per piece at its centre: source VP{k} (1 V) at node pad{k}, joined
+    to the grid through RPAD{k} (0.05 ohm).  `loads` current loads at seeded grid
+    nodes (the same for every variant): a PULSE current sink IL{k} from the node
+    to ground with a clamp diode DL{k} across it (IS 1e-14, N 2: a forward-biased
+    junction drawing microamps at 1 V).  Returns (circuit, torn element names):
+    the resistors that cross a piece boundary."""
+    b = Builder("power grid %dx%d" % (N, N))
+    g = lambda r, c: "g%d_%d" % (r, c)
+    s = N // P
+    torn = []
+    for r in range(N):
+        for c in range(N):
+            if c + 1 < N:
+                b.resistor("RH%d_%d" % (r, c), g(r, c), g(r, c + 1), 0.1)
+                if (c + 1) % s == 0:
+                    torn.append("RH%d_%d" % (r, c))
+            if r + 1 < N:
+                b.resistor("RV%d_%d" % (r, c), g(r, c), g(r + 1, c), 0.1)
+                if (r + 1) % s == 0:
+                    torn.append("RV%d_%d" % (r, c))
+            b.capacitor("CG%d_%d" % (r, c), g(r, c), "0", 10e-12)
+    for pr in range(P):
+        for pc in range(P):
+            k = pr * P + pc
+            b.voltage_source("VP%d" % k, "pad%d" % k, "0", 1.0)
+            b.resistor("RPAD%d" % k, "pad%d" % k, g(pr * s + s // 2, pc * s + s // 2), 0.05)
+    rg = rng(5, seed)
+    where = rg.choice(N * N, size=loads, replace=False)
+    for k, w in enumerate(sorted(int(v) for v in where)):
+        node = g(w // N, w % N)
+        b.current_wave("IL%d" % k, node, "0", "pulse", [0.0, 5e-3, 0.0, 0.5e-9, 0.5e-9, 5e-9, 20e-9])
+        b.model("dl%d" % k, "d", {"is": 1e-14, "n": 2.0})
+        b.diode("DL%d" % k, node, "0", "dl%d" % k)
+    return b.build(), torn
+
+
+def power_grid_batch(n_var, seed=0, N=256, P=4, loads=1024):
+    """Seeded variants of power_grid_template: every grid resistor log-U[0.01, 1]
+    ohm, every grid capacitor log-U[1, 100] pF, each load's peak current log-U[1,
+    10] mA, delay U[0, 20] ns, width U[2, 10] ns, period U[15, 30] ns, and its
+    clamp diode's emission coefficient U[1.8, 2.2].
+    Returns (elements, n_nodes, values[n_var][n_values], torn element indices, circuit)."""
+    c, torn = power_grid_template(N, P, loads, seed)
+    el, v0, off = _offsets(c)
+    names = [e.name for e in c.elements]
+    idx = {nm: i for i, nm in enumerate(names)}
+    kinds = np.array([nm[:2] for nm in names])
+    gen = rng(5, 1000 + seed)
+    vals = np.tile(v0, (n_var, 1))
+    params = np.array([int(e["param"]) for e in el])
+    rgrid = params[(kinds == "RH") | (kinds == "RV")]
+    vals[:, rgrid] = log_uniform(gen, 0.01, 1.0, n_var * len(rgrid)).reshape(n_var, -1)
+    cgrid = params[kinds == "CG"]
+    vals[:, cgrid] = log_uniform(gen, 1e-12, 100e-12, n_var * len(cgrid)).reshape(n_var, -1)
+    il = params[kinds == "IL"] + 3  # KS_SRC_P_ARGS: v1, v2, td, tr, tf, pw, per
+    vals[:, il + 1] = log_uniform(gen, 1e-3, 10e-3, n_var * len(il)).reshape(n_var, -1)
+    vals[:, il + 2] = gen.uniform(0, 20e-9, (n_var, len(il)))
+    vals[:, il + 5] = gen.uniform(2e-9, 10e-9, (n_var, len(il)))
+    vals[:, il + 6] = gen.uniform(15e-9, 30e-9, (n_var, len(il)))
+    dl = params[kinds == "DL"] + D_KEYS.index("n")
+    vals[:, dl] = gen.uniform(1.8, 2.2, (n_var, len(dl)))
+    torn_idx = np.array(sorted(idx[t] for t in torn), dtype=np.int32)
+    return el, c.n_nodes, vals, torn_idx, c

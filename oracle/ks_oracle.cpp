@@ -14,6 +14,7 @@
 #include "oracle_devices.hpp"
 #include "oracle_bjt.hpp"
 #include "oracle_mos.hpp"
+#include "oracle_torn.hpp"
 
 #include <atomic>
 #include <chrono>
@@ -65,6 +66,11 @@ struct Sim {
   std::string msg;
 
   // newSim, analysis/op.go:160-208
+  // kron.JacobianTearing as the linear solver (Options.Solver), when set
+  const std::vector<std::pair<int, int>>* tornCuts = nullptr;
+  double tornReuseTol = 0;
+  TornStats tornStats;
+
   int build(const ks_topology* t, const double* v, double step, double stop, int backend) {
     numNodes = t->n_nodes;
     for (int e = 0; e < t->n_elem; e++) {
@@ -106,7 +112,9 @@ struct Sim {
     n = sc.size();
     for (auto& d : devs) d->n = n;
     int be = backend == KS_BACKEND_AUTO ? (n < 30 ? KS_BACKEND_DENSE : KS_BACKEND_SPARSE) : backend;
-    if (be == KS_BACKEND_SPARSE) M.reset(new Sparse(n)); else M.reset(new Dense(n));
+    if (tornCuts) M.reset(new Torn(n, *tornCuts, tornReuseTol, &tornStats));
+    else if (be == KS_BACKEND_SPARSE) M.reset(new Sparse(n));
+    else M.reset(new Dense(n));
     x.assign(n, 0); xOld.assign(n, 0); rhs.assign(n, 0);
     isV.assign(n, 0);
     for (int i = 0; i < numNodes - 1; i++) isV[i] = 1;
@@ -536,6 +544,100 @@ extern "C" int kso_tran(const ks_topology* t, const double* values, const ks_tra
   if (npts) *npts = std::min(rec.npts, capacity);
   if (steps) *steps = st;
   if (iters) *iters = s.iters;
+  copyMsg(e ? s.msg : std::string(), err, errlen);
+  return e;
+}
+
+// tearTerminals + NewJacobianTearing, kron/jacobian.go:92-232: the node-unknown
+// pairs of the torn elements, with the reference's refusals.
+extern "C" int kso_torn_cuts(const ks_topology* t, const int32_t* elems, int n_elems, int32_t* pairs, int cap,
+                             int32_t* n_pairs, char* err, int errlen) {
+  std::vector<std::pair<int, int>> out;
+  std::vector<char> seen(t->n_elem, 0);
+  for (int k = 0; k < n_elems; k++) {
+    int e = elems[k];
+    if (e < 0 || e >= t->n_elem) { copyMsg("kron: unsupported: no element", err, errlen); return KS_EINVAL; }
+    char name[32];
+    snprintf(name, sizeof name, "element %d", e);
+    if (seen[e]) { copyMsg(std::string("kron: unsupported: ") + name + " is torn twice", err, errlen); return KS_EINVAL; }
+    seen[e] = 1;
+    const ks_element& el = t->elem[e];
+    if (el.kind == KS_ELEM_V || el.kind == KS_ELEM_L) {
+      copyMsg(std::string("kron: unsupported: tearing ") + name +
+              ": its coupling runs through a branch-current unknown; tear a neighbouring element", err, errlen);
+      return KS_EINVAL;
+    }
+    int nn = el.kind == KS_ELEM_Q || el.kind == KS_ELEM_M ? 4 : 2;
+    std::vector<int> terms;
+    for (int a = 0; a < nn; a++) {
+      int node = el.node[a];
+      if (node == 0) continue;
+      bool dup = false;
+      for (int m : terms) dup = dup || m == node;
+      if (!dup) terms.push_back(node);
+    }
+    if (terms.size() < 2) {
+      copyMsg(std::string("kron: unsupported: tearing ") + name + ": it connects to ground, so tearing it separates nothing",
+              err, errlen);
+      return KS_EINVAL;
+    }
+    for (size_t x = 0; x < terms.size(); x++)
+      for (size_t y = x + 1; y < terms.size(); y++)
+        if (terms[x] != terms[y]) out.push_back({terms[x] - 1, terms[y] - 1});
+  }
+  *n_pairs = (int32_t)out.size();
+  for (size_t i = 0; i < out.size() && (int)i < cap; i++) { pairs[2 * i] = out[i].first; pairs[2 * i + 1] = out[i].second; }
+  copyMsg(std::string(), err, errlen);
+  return KS_OK;
+}
+
+static std::vector<std::pair<int, int>> cut_pairs(const int32_t* pairs, int n) {
+  std::vector<std::pair<int, int>> c;
+  for (int i = 0; i < n; i++) c.push_back({pairs[2 * i], pairs[2 * i + 1]});
+  return c;
+}
+
+static void torn_stats_out(const TornStats& s, int64_t* out) {
+  if (!out) return;
+  out[0] = s.solves; out[1] = s.factors; out[2] = s.reuses; out[3] = s.stale;
+  out[4] = s.fallbacks; out[5] = s.refines; out[6] = s.maxPieces;
+}
+
+extern "C" int kso_op_torn(const ks_topology* t, const double* values, const ks_options* o, const int32_t* pairs,
+                           int n_pairs, double reuse_tol, double* x_out, int32_t* iters, int64_t* stats, char* err,
+                           int errlen) {
+  Sim s;
+  Opts opt(o);
+  auto cuts = cut_pairs(pairs, n_pairs);
+  s.tornCuts = &cuts;
+  s.tornReuseTol = reuse_tol;
+  if (s.build(t, values, 0, 0, opt.backend)) { copyMsg(s.msg, err, errlen); return KS_STATUS_NOT_RUN; }
+  int e = s.op(opt, nullptr);
+  if (x_out) for (int i = 0; i < s.n; i++) x_out[i] = s.x[i];
+  if (iters) *iters = s.iters;
+  torn_stats_out(s.tornStats, stats);
+  copyMsg(e ? s.msg : std::string(), err, errlen);
+  return e;
+}
+
+extern "C" int kso_tran_torn(const ks_topology* t, const double* values, const ks_tran_spec* spec,
+                             const ks_options* o, const int32_t* pairs, int n_pairs, double reuse_tol, int capacity,
+                             double* t_out, double* x_out, int32_t* npts, int32_t* steps, int32_t* iters,
+                             int64_t* stats, char* err, int errlen) {
+  Sim s;
+  Opts opt(o);
+  auto cuts = cut_pairs(pairs, n_pairs);
+  s.tornCuts = &cuts;
+  s.tornReuseTol = reuse_tol;
+  if (s.build(t, values, spec->step, spec->stop, opt.backend)) { copyMsg(s.msg, err, errlen); return KS_STATUS_NOT_RUN; }
+  Sim::Rec rec;
+  rec.cap = capacity; rec.t = t_out; rec.x = x_out; rec.i = nullptr; rec.n = s.n; rec.ne = (int)s.devs.size();
+  int st = 0;
+  int e = s.tran(*spec, opt, rec, &st);
+  if (npts) *npts = std::min(rec.npts, capacity);
+  if (steps) *steps = st;
+  if (iters) *iters = s.iters;
+  torn_stats_out(s.tornStats, stats);
   copyMsg(e ? s.msg : std::string(), err, errlen);
   return e;
 }

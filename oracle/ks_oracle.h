@@ -49,6 +49,20 @@ int kso_batch_tran(const ks_topology* t, const double* values, int nc, const ks_
                    const ks_options* o, int nthreads, double* x_out, int32_t* status,
                    int32_t* steps, int32_t* iters);
 
+/* kron.JacobianTearing (kron/jacobian.go) as the linear solver.  kso_torn_cuts
+ * turns torn element indices into node-unknown pairs (tearTerminals, with the
+ * reference's refusals as KS_EINVAL + message); kso_op_torn / kso_tran_torn run
+ * the analyses with every linear system solved torn (reuse_tol: ReuseTol).
+ * stats [7]: solves, pieces factored, reused, stale reuses, untorn fallbacks,
+ * refinement steps, most pieces. */
+int kso_torn_cuts(const ks_topology* t, const int32_t* elems, int n_elems, int32_t* pairs, int cap,
+                  int32_t* n_pairs, char* err, int errlen);
+int kso_op_torn(const ks_topology* t, const double* values, const ks_options* o, const int32_t* pairs,
+                int n_pairs, double reuse_tol, double* x_out, int32_t* iters, int64_t* stats, char* err, int errlen);
+int kso_tran_torn(const ks_topology* t, const double* values, const ks_tran_spec* spec, const ks_options* o,
+                  const int32_t* pairs, int n_pairs, double reuse_tol, int capacity, double* t_out, double* x_out,
+                  int32_t* npts, int32_t* steps, int32_t* iters, int64_t* stats, char* err, int errlen);
+
 /* Unknown count and layout of one circuit (device Setup), for the tests. */
 int kso_unknowns(const ks_topology* t, const double* values, int32_t* n, int32_t* is_v);
 

@@ -13,7 +13,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libks_oracle.so")
 SOURCES = ["ks_oracle.cpp"]
-HEADERS = ["ks_oracle.h", "oracle_solver.hpp", "oracle_devices.hpp", "oracle_bjt.hpp", "oracle_mos.hpp"]
+HEADERS = ["ks_oracle.h", "oracle_solver.hpp", "oracle_devices.hpp", "oracle_bjt.hpp", "oracle_mos.hpp",
+           "oracle_torn.hpp"]
 
 
 def build(force=False):
@@ -65,6 +66,10 @@ def lib():
         L.kso_batch_tran.argtypes = [P, P, ctypes.c_int, P, P, ctypes.c_int, P, P, P, P]
         L.kso_unknowns.argtypes = [P, P, P, P]
         L.kso_ac.argtypes = [P, P, P, P, ctypes.c_int, P, ctypes.c_char_p, ctypes.c_int]
+        L.kso_torn_cuts.argtypes = [P, P, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_char_p, ctypes.c_int]
+        L.kso_op_torn.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_double, P, P, P, ctypes.c_char_p, ctypes.c_int]
+        L.kso_tran_torn.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.c_double, ctypes.c_int, P, P, P, P, P, P,
+                                    ctypes.c_char_p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -155,6 +160,49 @@ def ac(pk, freqs, opt=None):
     o = opt or options()
     st = lib().kso_ac(pk.tref(), _ptr(pk.values), ctypes.byref(o), _ptr(f), len(f), _ptr(x), err, 512)
     return st, x[..., 0] + 1j * x[..., 1], err.value.decode()
+
+
+TORN_STATS = ("solves", "factors", "reuses", "stale", "fallbacks", "refines", "max_pieces")
+
+
+def torn_cuts(pk, elems):
+    """NewJacobianTearing's cut (kron/jacobian.go:92-232): (status, pairs [k][2], message)."""
+    e = np.ascontiguousarray(elems, dtype=np.int32)
+    cap = 64 * max(1, len(e))
+    pairs = np.zeros((cap, 2), dtype=np.int32)
+    npairs = ctypes.c_int32()
+    err = ctypes.create_string_buffer(512)
+    st = lib().kso_torn_cuts(pk.tref(), _ptr(e), len(e), _ptr(pairs), cap, ctypes.byref(npairs), err, 512)
+    return st, pairs[:npairs.value].copy(), err.value.decode()
+
+
+def op_torn(pk, pairs, opt=None, reuse_tol=0.0):
+    """analysis.OP with Options.Solver = kron.JacobianTearing: (status, x, iters, stats, message)."""
+    n, _ = unknowns(pk)
+    p = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+    x = np.zeros(n)
+    it = ctypes.c_int32()
+    stats = np.zeros(7, dtype=np.int64)
+    err = ctypes.create_string_buffer(512)
+    st = lib().kso_op_torn(pk.tref(), _ptr(pk.values), ctypes.byref(opt or options()), _ptr(p), len(p),
+                           float(reuse_tol), _ptr(x), ctypes.byref(it), _ptr(stats), err, 512)
+    return st, x, it.value, dict(zip(TORN_STATS, stats.tolist())), err.value.decode()
+
+
+def tran_torn(pk, spec, pairs, opt=None, reuse_tol=0.0, capacity=200000):
+    """analysis.Tran with every linear system solved torn: (status, t, x [npts][n], steps, iters, stats, message)."""
+    n, _ = unknowns(pk)
+    p = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+    t = np.zeros(capacity)
+    x = np.zeros((capacity, n))
+    npts, steps, it = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    stats = np.zeros(7, dtype=np.int64)
+    err = ctypes.create_string_buffer(512)
+    st = lib().kso_tran_torn(pk.tref(), _ptr(pk.values), ctypes.byref(spec), ctypes.byref(opt or options()), _ptr(p),
+                             len(p), float(reuse_tol), capacity, _ptr(t), _ptr(x), ctypes.byref(npts),
+                             ctypes.byref(steps), ctypes.byref(it), _ptr(stats), err, 512)
+    k = npts.value
+    return st, t[:k].copy(), x[:k].copy(), steps.value, it.value, dict(zip(TORN_STATS, stats.tolist())), err.value.decode()
 
 
 def batch_op(pk, nc, opt=None, x0=None, nthreads=0):
