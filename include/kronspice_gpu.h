@@ -429,6 +429,44 @@ int ks_mlp_grad(ks_mlp* m, const float* X, const float* T, int32_t rows, float* 
  * rows (a multiple of 64). */
 int ks_mlp_train(ks_mlp* m, ks_batch* b, const double* x_dev, const int32_t* idx_dev, int32_t n_train,
                  int32_t epochs, int32_t mb, float lr, float* last_loss, void* stream);
+/*
+ * Torn solves of large circuits, batched over variants of one topology
+ * (kron.JacobianTearing as analysis.Options.Solver, kron/jacobian.go:92-589,
+ * under analysis.OP and analysis.Tran).  ks_torn_create takes the topology,
+ * n_variants value vectors ([n_variants][n_values], row-major) and the indices
+ * of the torn elements (kron.Tearing.Torn; refused as NewJacobianTearing
+ * refuses: a voltage source or inductor, an element to ground, one torn twice,
+ * KS_EINVAL with the reference's message).  The pieces are the connected
+ * components of the Jacobian's pattern without the torn node pairs
+ * (buildPlan, :296-389); each is factored as a band matrix, the
+ * interconnection I + M.Q.B^-1.P of each variant as a dense matrix.
+ * reuse = 1 keeps factors while the refinement against the exact Jacobian
+ * (backward error <= 1e-14, accepted at 1e-12) converges on them (ReuseTol
+ * without a bound); reuse = 0 refactors at every solve.  Errors per variant as
+ * ks_status; a solve that is not accepted after a fresh refactor ends that
+ * variant with KS_STATUS_SINGULAR (the reference would fall back to an untorn
+ * LU of the whole system).  stats [8]: solves, refactors, refinement steps,
+ * most refinement steps of one solve, solves not accepted, pieces, coupling
+ * rows, largest band (kl + ku).
+ */
+typedef struct ks_torn ks_torn;
+int ks_torn_create(const ks_topology* topo, int32_t n_variants, const double* values, const int32_t* torn_elems,
+                   int32_t n_torn, ks_torn** out);
+void ks_torn_destroy(ks_torn* t);
+int ks_torn_info(const ks_torn* t, int32_t* n_unknowns, int32_t* n_pieces, int32_t* n_coupling_rows,
+                 int32_t* max_piece, int32_t* max_band);
+/* analysis.OP of every variant (Newton from zero, InitJct; no gmin / source
+ * stepping fallback).  out_x [n_variants][n]. */
+int ks_torn_op(ks_torn* t, const ks_options* opt, int32_t reuse, double* out_x, int32_t* out_status,
+               int32_t* out_iters, int64_t* stats);
+/* Fixed-step analysis.Tran of every variant from its transient operating
+ * point: n_points = round(stop / step) + 1, backward Euler at the first step,
+ * then spec->method.  out_wave [n_points][n_variants][n_probes] holds the
+ * unknowns listed in probes; out_x [n_variants][n] the last point. */
+int ks_torn_tran(ks_torn* t, const ks_tran_spec* spec, const ks_options* opt, int32_t reuse, const int32_t* probes,
+                 int32_t n_probes, double* out_wave, double* out_x, int32_t* out_status, int32_t* out_steps,
+                 int32_t* out_iters, int64_t* stats);
+
 /* Predicted starting points x0_dev [n_circ][n] (device memory) for ks_op_async. */
 int ks_mlp_predict(ks_mlp* m, ks_batch* b, double* x0_dev, void* stream);
 #endif /* __CUDACC_RTC__ */

@@ -330,6 +330,67 @@ class MultiBatch:
             self.handle = None
 
 
+TORN_STATS = ("solves", "refactors", "refines", "max_passes", "not_accepted", "pieces", "coupling_rows", "max_band")
+
+
+class TornBatch:
+    """Variants of one large topology solved torn into pieces (ks_torn_create):
+    kron.JacobianTearing as analysis.Options.Solver, batched over the variants."""
+
+    def __init__(self, elements, n_nodes, values, torn):
+        L = _lib.load()
+        self._el = np.ascontiguousarray(elements, dtype=ELEMENT_DTYPE)
+        self.values = np.ascontiguousarray(values, dtype=np.float64)
+        if self.values.ndim == 1:
+            self.values = self.values[None, :]
+        self.n_var = self.values.shape[0]
+        self._torn = np.ascontiguousarray(torn, dtype=np.int32)
+        topo = _lib.KsTopology(int(n_nodes), len(self._el), self.values.shape[1], 0, self._el.ctypes.data)
+        h = ctypes.c_void_p()
+        _check(L.ks_torn_create(ctypes.byref(topo), self.n_var, self.values.ctypes.data,
+                                self._torn.ctypes.data if len(self._torn) else None, len(self._torn), ctypes.byref(h)),
+               "ks_torn_create")
+        self.handle = h
+        info = [ctypes.c_int32() for _ in range(5)]
+        L.ks_torn_info(self.handle, *[ctypes.byref(i) for i in info])
+        self.n, self.pieces, self.coupling_rows, self.max_piece, self.max_band = (i.value for i in info)
+
+    def op(self, opt=None, reuse=True):
+        """(x [n_var][n], status, iterations, stats) of analysis.OP for every variant."""
+        o = (opt or Options()).c()
+        x = np.zeros((self.n_var, self.n))
+        st = np.zeros(self.n_var, dtype=np.int32)
+        it = np.zeros(self.n_var, dtype=np.int32)
+        stats = np.zeros(8, dtype=np.int64)
+        _check(_lib.load().ks_torn_op(self.handle, ctypes.byref(o), int(reuse), x.ctypes.data, st.ctypes.data,
+                                      it.ctypes.data, stats.ctypes.data), "ks_torn_op")
+        return x, st, it, dict(zip(TORN_STATS, stats.tolist()))
+
+    def tran(self, spec, opt=None, reuse=True, probes=()):
+        """Fixed-step analysis.Tran of every variant: (wave [n_points][n_var][n_probes],
+        last x [n_var][n], status, steps, iterations, stats)."""
+        o = (opt or Options()).c()
+        sp = spec.c() if hasattr(spec, "c") else spec
+        npts = int(round(sp.stop / sp.step)) + 1
+        pr = np.ascontiguousarray(probes, dtype=np.int32)
+        wave = np.zeros((npts, self.n_var, len(pr)))
+        x = np.zeros((self.n_var, self.n))
+        st = np.zeros(self.n_var, dtype=np.int32)
+        steps = np.zeros(self.n_var, dtype=np.int32)
+        it = np.zeros(self.n_var, dtype=np.int32)
+        stats = np.zeros(8, dtype=np.int64)
+        _check(_lib.load().ks_torn_tran(self.handle, ctypes.byref(sp), ctypes.byref(o), int(reuse),
+                                        pr.ctypes.data if len(pr) else None, len(pr),
+                                        wave.ctypes.data if len(pr) else None, x.ctypes.data, st.ctypes.data,
+                                        steps.ctypes.data, it.ctypes.data, stats.ctypes.data), "ks_torn_tran")
+        return wave, x, st, steps, it, dict(zip(TORN_STATS, stats.tolist()))
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib._lib is not None:
+            _lib._lib.ks_torn_destroy(self.handle)
+            self.handle = None
+
+
 def validate(circuit, transient=False):
     """circuit.Validate: None or the typed validation error."""
     el, vals, _ = circuit.pack()

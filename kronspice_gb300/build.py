@@ -18,7 +18,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "550"]
 
-UNITS = ["ks_host.cpp", "ks_api.cu", "ks_kernels.cu", "ks_tran.cu", "ks_mlp.cu", "ks_jit.cpp", "ks_noalloc.cu", "ks_ac.cu", "ks_sparse.cpp",
+UNITS = ["ks_host.cpp", "ks_api.cu", "ks_kernels.cu", "ks_tran.cu", "ks_mlp.cu", "ks_jit.cpp", "ks_noalloc.cu", "ks_ac.cu", "ks_torn.cu", "ks_sparse.cpp",
          "ks_multi.cu"]
 # device headers embedded in the library for the per-topology kernels (NVRTC),
 # under the names their #include lines use
@@ -82,7 +82,7 @@ def build(force=False, verbose=False):
         objs = list(ex.map(_compile, units))
     tmp = LIB + ".tmp%d" % os.getpid()
     cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + [
-        "-lcudart", "-lnvrtc"]
+        "-lcudart", "-lnvrtc", "-lcublas"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))

@@ -539,36 +539,55 @@ __device__ __forceinline__ bool converged(const P& prog, const Col& Vb, const Co
   return prog_all(prog, ok);
 }
 
+// Accept one element at the new iterate (its Accept).
+template <class SY>
+__device__ __forceinline__ void elem_accept(const KElem& e, const Col& Vb, const Col& Db, const Col& Sb, SY& s,
+                                            double t, int mode, double gmin, bool nonlinOnly) {
+  Col S = state_col(Sb, e);
+  switch (e.kind) {
+    case KS_ELEM_C: {  // device/reactive.go:144-161
+      if (nonlinOnly) break;
+      double v = xn_(s, e.u[0]) - xn_(s, e.u[1]);
+      if (mode == ModeUICInit) { S[SC_IPREV] = 0; hist_reset(S, SC_HIST); }
+      else if (mode == ModeOP || mode == ModeTranOP) { S[SC_VPREV] = v; S[SC_IPREV] = 0; hist_reset(S, SC_HIST); }
+      else { double i = S[SC_TRAN] != 0 ? S[SC_GEQ] * v + S[SC_IHIST] : 0.0; S[SC_VPREV] = v; S[SC_IPREV] = i; }
+      hist_push(S, SC_HIST, t, Vb[e.param] * S[SC_VPREV]);
+      break;
+    }
+    case KS_ELEM_L: {  // device/reactive.go:312-329
+      if (nonlinOnly) break;
+      double v = xn_(s, e.u[0]) - xn_(s, e.u[1]), i = xn_(s, e.u[2]);
+      if (mode == ModeUICInit) { S[SL_VPREV] = 0; hist_reset(S, SL_HIST); }
+      else if (mode == ModeOP || mode == ModeTranOP) { S[SL_VPREV] = 0; S[SL_IPREV] = i; hist_reset(S, SL_HIST); }
+      else { S[SL_VPREV] = v; S[SL_IPREV] = i; }
+      hist_push(S, SL_HIST, t, Vb[e.param] * S[SL_IPREV]);
+      break;
+    }
+    case KS_ELEM_D: diode_accept(e, Vb, Db, S, s, t, mode); break;
+    case KS_ELEM_Q: bjt_accept(e, Vb, Db, S, s, t, mode, gmin); break;
+    case KS_ELEM_M: mos_accept(e, Vb, Db, S, s, t, mode); break;
+  }
+}
+
+// One element's part of converged (analysis/newton.go:59-82): not limited at
+// its last load, and its ConvTest passes.
+template <class SY>
+__device__ __forceinline__ bool elem_converged(const KElem& e, const Col& Vb, const Col& Db, const Col& Sb, SY& s,
+                                               const KOpts& o, double gmin) {
+  const int ls = lim_slot(e.kind);
+  if (ls < 0) return true;
+  Col S = state_col(Sb, e);
+  if (S[ls] != 0) return false;
+  if (e.kind == KS_ELEM_D) return diode_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
+  if (e.kind == KS_ELEM_Q) return bjt_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
+  return mos_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
+}
+
 // Accept every element at the new iterate (analysis/op.go:324-328).
 template <class SY, class P>
 __device__ __forceinline__ void accept_all(const P& prog, const Col& Vb, const Col& Db, const Col& Sb, SY& s, double t,
                                   int mode, double gmin, bool nonlinOnly) {
-  prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
-    Col S = state_col(Sb, e);
-    switch (e.kind) {
-      case KS_ELEM_C: {  // device/reactive.go:144-161
-        if (nonlinOnly) break;
-        double v = xn_(s, e.u[0]) - xn_(s, e.u[1]);
-        if (mode == ModeUICInit) { S[SC_IPREV] = 0; hist_reset(S, SC_HIST); }
-        else if (mode == ModeOP || mode == ModeTranOP) { S[SC_VPREV] = v; S[SC_IPREV] = 0; hist_reset(S, SC_HIST); }
-        else { double i = S[SC_TRAN] != 0 ? S[SC_GEQ] * v + S[SC_IHIST] : 0.0; S[SC_VPREV] = v; S[SC_IPREV] = i; }
-        hist_push(S, SC_HIST, t, Vb[e.param] * S[SC_VPREV]);
-        break;
-      }
-      case KS_ELEM_L: {  // device/reactive.go:312-329
-        if (nonlinOnly) break;
-        double v = xn_(s, e.u[0]) - xn_(s, e.u[1]), i = xn_(s, e.u[2]);
-        if (mode == ModeUICInit) { S[SL_VPREV] = 0; hist_reset(S, SL_HIST); }
-        else if (mode == ModeOP || mode == ModeTranOP) { S[SL_VPREV] = 0; S[SL_IPREV] = i; hist_reset(S, SL_HIST); }
-        else { S[SL_VPREV] = v; S[SL_IPREV] = i; }
-        hist_push(S, SL_HIST, t, Vb[e.param] * S[SL_IPREV]);
-        break;
-      }
-      case KS_ELEM_D: diode_accept(e, Vb, Db, S, s, t, mode); break;
-      case KS_ELEM_Q: bjt_accept(e, Vb, Db, S, s, t, mode, gmin); break;
-      case KS_ELEM_M: mos_accept(e, Vb, Db, S, s, t, mode); break;
-    }
-  });
+  prog.each([&](const KElem& e) KS_INLINE_LAMBDA { elem_accept(e, Vb, Db, Sb, s, t, mode, gmin, nonlinOnly); });
   prog_sync(prog);
 }
 

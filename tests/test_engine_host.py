@@ -182,3 +182,17 @@ def test_ac_lin_single_point():
     from kronspice_gb300.analysis import ACSpec
     assert list(ACSpec("lin", 1, 5.0, 5.0).frequencies()) == [5.0]
     assert list(ACSpec("lin", 3, 0.0, 2.0).frequencies()) == [0.0, 1.0, 2.0]
+
+
+def test_torn_refusals_match_reference():
+    """TestJacobianErrors (kron/jacobian_test.go:284-308): the torn engine refuses
+    a voltage source, an element to ground and an element torn twice with the
+    reference's messages, before touching the GPU."""
+    from kronspice_gb300 import workloads
+    el, nn, vals, torn, c = workloads.power_grid_batch(1, N=16, P=2, loads=16)
+    names = [e.name for e in c.elements]
+    for bad, want in (([names.index("VP0")], "branch-current unknown"), ([names.index("CG0_0")], "connects to ground"),
+                      ([int(torn[0]), int(torn[0])], "torn twice"), ([len(names)], "no element")):
+        with pytest.raises(RuntimeError) as e:
+            analysis.TornBatch(el, nn, vals, bad)
+        assert want in str(e.value), str(e.value)

@@ -1,0 +1,123 @@
+"""GPU parity of the torn solves (ks_torn_*) against the oracle.
+
+The engine tears each variant's Jacobian as kron.JacobianTearing does and
+refines every solve against the exact Jacobian to a componentwise backward
+error of 1e-14 (kron/jacobian.go:551-589), so its Newton iterates are those of
+an untorn solve up to round-off: operating points and backward-Euler
+transients of seeded power grids must match the oracle's untorn runs (and its
+restatement of the torn solver) to 1e-9 of the largest node voltage, with and
+without factor reuse.  The reference's own tearing cases (TestJacobianErrors,
+kron/jacobian_test.go:284-308) are refused with its messages.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from kronspice_gb300 import analysis, build, workloads
+from kronspice_gb300 import circuit as kc
+from oracle import oracle as orc
+
+import golden_compare as gc
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    build.build()
+
+
+def grid(V, N, P, loads, seed=0):
+    el, nn, vals, torn, c = workloads.power_grid_batch(V, seed=seed, N=N, P=P, loads=loads)
+    return el, nn, vals, torn, c
+
+
+@pytest.mark.parametrize("reuse", [True, False])
+def test_power_grid_op_matches_oracle(reuse):
+    el, nn, vals, torn, c = grid(4, 16, 2, 16)
+    tb = analysis.TornBatch(el, nn, vals, torn)
+    assert tb.pieces == 4 and tb.coupling_rows > 0
+    x, st, it, stats = tb.op(analysis.Options(reltol=1e-6), reuse=reuse)
+    assert np.all(st == 0), st
+    for v in range(len(vals)):
+        s0, x0, _, it0, msg = orc.op(orc.Packed(el, nn, vals[v]), orc.options(reltol=1e-6))
+        assert s0 == 0, msg
+        assert np.abs(x[v] - x0).max() <= 1e-9 * np.abs(x0).max(), np.abs(x[v] - x0).max()
+        assert it[v] == it0
+    if not reuse:
+        assert stats["refactors"] == stats["solves"]
+
+
+@pytest.mark.parametrize("reuse", [True, False])
+def test_power_grid_transient_matches_oracle(reuse):
+    el, nn, vals, torn, c = grid(3, 16, 2, 16, seed=1)
+    tb = analysis.TornBatch(el, nn, vals, torn)
+    spec = analysis.TranSpec(step=0.1e-9, stop=40 * 0.1e-9, fixed_step=True, method="be")
+    probes = np.arange(0, tb.n, 7)
+    wave, x, st, steps, it, stats = tb.tran(spec, analysis.Options(reltol=1e-6), reuse=reuse, probes=probes)
+    assert np.all(st == 0) and np.all(steps == 40), (st, steps)
+    ospec = orc.TranSpec(0.1e-9, 40 * 0.1e-9, 0.0, 0.0, 0, 1, 1, 0, 0.0, 0.0, 0.0)
+    for v in range(len(vals)):
+        r = orc.tran(orc.Packed(el, nn, vals[v]), ospec, orc.options(reltol=1e-6))
+        assert r[0] == 0, r[-1]
+        xo = r[2]
+        assert xo.shape[0] == wave.shape[0]
+        scale = np.abs(xo).max()
+        assert np.abs(wave[:, v, :] - xo[:, probes]).max() <= 1e-9 * scale
+        assert np.abs(x[v] - xo[-1]).max() <= 1e-9 * scale
+        assert it[v] == r[5]
+    if reuse:
+        assert stats["refactors"] < stats["solves"] // 4, stats
+
+
+def test_medium_grid_transient_matches_oracle_restatement():
+    """64 x 64 grid in 16 pieces of 256 nodes: the torn oracle (the reference's
+    algorithm restated) and the engine agree step by step."""
+    el, nn, vals, torn, c = grid(2, 64, 4, 64, seed=2)
+    tb = analysis.TornBatch(el, nn, vals, torn)
+    assert tb.pieces == 16
+    spec = analysis.TranSpec(step=0.1e-9, stop=10 * 0.1e-9, fixed_step=True, method="be")
+    probes = np.arange(0, tb.n, 13)
+    wave, x, st, steps, it, stats = tb.tran(spec, analysis.Options(reltol=1e-6), probes=probes)
+    assert np.all(st == 0)
+    ospec = orc.TranSpec(0.1e-9, 10 * 0.1e-9, 0.0, 0.0, 0, 1, 1, 0, 0.0, 0.0, 0.0)
+    for v in range(len(vals)):
+        pk = orc.Packed(el, nn, vals[v])
+        s, pairs, msg = orc.torn_cuts(pk, torn)
+        assert s == 0, msg
+        s, t, xo, nsteps, its, ostats, msg = orc.tran_torn(pk, ospec, pairs, orc.options(reltol=1e-6))
+        assert s == 0 and ostats["max_pieces"] == 16, msg
+        assert np.abs(wave[:, v, :] - xo[:, probes]).max() <= 1e-9 * np.abs(xo).max()
+
+
+with open(os.path.join(HERE, "golden", "reference_cases.json")) as f:
+    OP_CASES = [c for c in json.load(f)["cases"] if not c["skip"] and c["circuit"]["analyses"][0]["kind"] == "op"]
+
+
+@pytest.mark.parametrize("case", OP_CASES, ids=[c["name"] for c in OP_CASES])
+def test_golden_operating_points_torn(case):
+    """Each golden operating-point netlist torn along all its tearable elements
+    (jacobianCuts, kron/jacobian_test.go:25-42) still meets its golden values."""
+    ckt = kc.from_dict(case["circuit"])
+    el, vals, _ = ckt.pack()
+    pk = orc.Packed(el, ckt.n_nodes, vals)
+    cut = []
+    for i in range(len(ckt.elements)):
+        st, pairs, _ = orc.torn_cuts(pk, [i])
+        if st == 0 and len(pairs):
+            cut.append(i)
+    tb = analysis.TornBatch(el, ckt.n_nodes, vals, cut)
+    x, st, it, stats = tb.op(analysis.Options())
+    assert st[0] == 0, st
+    want = case["golden"]["independent"]
+    got = {}
+    for k in want["values"]:
+        if k.startswith("v("):
+            i = ckt.node_index(k[2:-1])
+            if i >= 0:
+                got[k] = 0.0 if i == 0 else x[0, i - 1]
+    msgs = gc.compare_values(got, {k: v for k, v in want["values"].items() if k.startswith("v(")})
+    assert not msgs, msgs
