@@ -36,7 +36,10 @@ UNIT = "solves/s"
 RELTOL = 1e-6
 # workload -> (default circuits, compulsory bytes per solve: parameters in + node voltages out, 8 B each)
 WORKLOADS = {"bjt_ce": (16384, (7 + 5) * 8), "cmos_opamp": (65536, (24 + 7) * 8), "rc_ladder": (4096, 0),
-             "random_netlists": (8192, 0), "bjt_ce_ac": (16384, 0)}
+             "random_netlists": (8192, 0), "bjt_ce_ac": (16384, 0), "power_grid": (64, 0)}
+# torn power grid: 256 x 256 mesh in 4 x 4 pieces, 1,024 clamped loads, 500 backward-Euler steps of 0.1 ns
+POWER_GRID = dict(N=256, P=4, loads=1024)
+POWER_STEPS, POWER_H = 500, 0.1e-9
 # AC workload: unit of work = the small-signal solve of one circuit at one frequency
 AC_UNIT = "AC frequency points/s"
 AC_SPEC = ("dec", 10, 10.0, 1e10)  # 10 points per decade, 10 Hz .. 10 GHz: 91 frequencies
@@ -61,6 +64,7 @@ def parse():
     p.add_argument("--n-circ", type=int, default=0)
     p.add_argument("--workload", default="bjt_ce", choices=sorted(WORKLOADS))
     p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--tran-steps", type=int, default=0, help="time steps of the transient workloads (0: the workload's)")
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
                    help="LU precision of the chosen path")
     p.add_argument("--variants", type=int, default=1, help="also time every kernel/precision/start combination")
@@ -276,6 +280,50 @@ def run_reference_ac(args):
     print(json.dumps(line))
 
 
+def oracle_grid_points(el, nn, vals, steps, min_wall=10.0):
+    """Accepted points/s of the oracle's untorn sparse transient (the reference's
+    backend for large systems) on the power grid: a bounded sample of steps of
+    one variant per host thread, timed in parallel."""
+    from oracle import oracle as orc
+    import concurrent.futures as cf
+    nthreads = os.cpu_count() or 1
+    spec = orc.TranSpec(POWER_H, steps * POWER_H, 0.0, 0.0, 0, 1, 1, 0, 0.0, 0.0, 0.0)
+
+    def one(v):
+        r = orc.tran(orc.Packed(el, nn, vals[v % len(vals)]), spec, orc.options(reltol=RELTOL), capacity=2,
+                     currents=False)
+        return r[4] if r[0] == 0 else 0
+    t0 = time.perf_counter()
+    pts, runs = 0, 0
+    with cf.ThreadPoolExecutor(max_workers=nthreads) as ex:
+        while time.perf_counter() - t0 < min_wall or runs == 0:
+            pts += sum(ex.map(one, range(runs, runs + nthreads)))
+            runs += nthreads
+    wall = time.perf_counter() - t0
+    return pts / wall, runs, wall, nthreads
+
+
+def run_reference_torn(args):
+    from kronspice_gb300 import workloads
+    from oracle import oracle as orc
+    orc.build()
+    el, nn, vals, torn, _ = workloads.power_grid_batch(min(args.n_circ, 16), args.seed, **POWER_GRID)
+    steps = 2
+    value, runs, wall, nthreads = oracle_grid_points(el, nn, vals, steps, min_wall=0.0)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": TRAN_UNIT, "n_gpus": args.gpus,
+            "steps": 1, "warmup": 0, "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox)",
+            "config": {"workload": "power_grid_tran_%d" % args.n_circ, "variants": args.n_circ, "grid": "256x256",
+                       "pieces": 16, "steps_per_variant": POWER_STEPS, "method": "be", "host_threads": nthreads},
+            "cpu_baseline": {"value": value, "unit": TRAN_UNIT, "cores": nthreads, "kind": "port",
+                             "sample": "%d runs of %d backward-Euler steps (one variant each, operating point "
+                                       "included) with the oracle's untorn sparse LU, one run per host thread; the "
+                                       "reference's torn path refactors a dense 4,096-unknown piece per change and is "
+                                       "slower still" % (runs, steps)},
+            "e2e": {"value": value, "unit": TRAN_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -288,6 +336,9 @@ def run_reference(args):
         return
     if args.workload == "bjt_ce_ac":
         run_reference_ac(args)
+        return
+    if args.workload == "power_grid":
+        run_reference_torn(args)
         return
     el, nn, vals = generator(args.workload)(args.n_circ, args.seed)
     from oracle import oracle as orc
@@ -846,6 +897,127 @@ def bench_ac(args):
         torch.distributed.barrier()
 
 
+def bench_torn(args):
+    """Torn transients of 64 seeded 256 x 256 power grids (65,568 unknowns each,
+    16 pieces of about 4,100 unknowns, 1,024 diode-clamped PULSE loads), 500
+    backward-Euler steps of 0.1 ns; unit of work = one accepted time point of one
+    variant.  One step = one ks_torn_tran of every variant."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from kronspice_gb300 import analysis, build, workloads
+    build.build()
+    dev = torch.device("cuda", local)
+    nsteps = args.tran_steps or POWER_STEPS
+    el, nn, vals, torn, circ = workloads.power_grid_batch(args.n_circ, args.seed + rank, **POWER_GRID)
+    V = vals.shape[0]
+    t0 = time.perf_counter()
+    tb = analysis.TornBatch(el, nn, vals, torn)
+    create_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream(dev)
+    tb.set_stream(ctypes.c_void_p(stream.cuda_stream))
+    spec = analysis.TranSpec(step=POWER_H, stop=nsteps * POWER_H, fixed_step=True, method="be")
+    names = [e.name for e in circ.elements]
+    grid_nodes = [circ.node_index("g%d_%d" % (r, c)) - 1 for r in (0, 128, 255) for c in (0, 128, 255)]
+    opt = analysis.Options(reltol=RELTOL)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def timed(reuse, steps_timed, spec_):
+        for _ in range(args.warmup):
+            tb.tran(spec_, opt, reuse=reuse, probes=grid_nodes)
+        torch.cuda.synchronize()
+        tot, pts = 0.0, 0
+        for _ in range(steps_timed):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            wave, x, st, steps, it, stats = tb.tran(spec_, opt, reuse=reuse, probes=grid_nodes)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1) / 1e3
+            pts += int(steps[st == 0].sum())
+        return {"seconds": tot, "points": pts, "stats": stats, "status": st, "iters": it, "wave": wave}
+
+    clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp",
+                              "bench_clocks_%d.csv" % rank))
+    with clk:
+        chosen = timed(True, args.steps, spec)
+        plain_steps = max(2, nsteps // 50)
+        plain_spec = analysis.TranSpec(step=POWER_H, stop=plain_steps * POWER_H, fixed_step=True, method="be")
+        plain = timed(False, 1, plain_spec)
+    clocks = clk.summary(local)
+    value = chosen["points"] / chosen["seconds"]
+    plain_value = plain["points"] / plain["seconds"]
+
+    # end to end: the torn batch made from the host values (symbolic plan, upload, per-variant setup) and the
+    # transient's probe waveforms back on the host, both inside the timed region
+    e2e_t, e2e_pts = 0.0, 0
+    for _ in range(max(1, min(args.steps, 2))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tb2 = analysis.TornBatch(el, nn, vals, torn)
+        wave, x, st, steps, it, stats = tb2.tran(spec, opt, reuse=True, probes=grid_nodes)
+        del tb2
+        torch.cuda.synchronize()
+        e2e_t += time.perf_counter() - t0
+        e2e_pts += int(steps[st == 0].sum())
+    e2e_value = e2e_pts / e2e_t
+
+    # accuracy: the first few steps of variant 0 against the oracle's untorn transient
+    from oracle import oracle as orc
+    orc.build()
+    chk = 3
+    ospec = orc.TranSpec(POWER_H, chk * POWER_H, 0.0, 0.0, 0, 1, 1, 0, 0.0, 0.0, 0.0)
+    r = orc.tran(orc.Packed(el, nn, vals[0]), ospec, orc.options(reltol=RELTOL), capacity=chk + 1, currents=False)
+    max_err = float(np.abs(chosen["wave"][:chk + 1, 0, :] - r[2][:, grid_nodes]).max()) if r[0] == 0 else None
+    cval, cruns, cwall, nthreads = oracle_grid_points(el, nn, vals, 2, min_wall=5.0)
+    cpu = {"value": cval, "unit": TRAN_UNIT, "cores": nthreads, "kind": "port",
+           "sample": "%d runs of 2 backward-Euler steps of one variant (operating point included, which the rate "
+                     "counts against: an upper bound on the oracle's speed per step is not claimed) with the oracle's "
+                     "untorn sparse LU, one run per host thread (%.1f s wall)" % (cruns, cwall)}
+
+    st = chosen["stats"]
+    n, P, R = tb.n, tb.pieces, tb.coupling_rows
+    # algorithmic bytes of one transient: every application of the torn factors streams the band factors of all
+    # pieces twice (z = B^-1 b, then x = B^-1 (b - P w)) and the interconnection factors once
+    applies = st["solves"] + st["refines"]
+    per_apply = V * (2 * st["band_doubles"] * 8 + R * R * 8)
+    per_run_s = chosen["seconds"] / args.steps
+    achieved = applies * per_apply / per_run_s / 1e9
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": TRAN_UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": chosen["seconds"] / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox)",
+        "config": {"workload": "power_grid_tran_%d" % V, "variants": V, "grid": "256x256", "unknowns": n,
+                   "pieces": P, "coupling_rows": R, "largest_piece": tb.max_piece, "band": tb.max_band,
+                   "steps_per_variant": nsteps, "method": "be", "step_s": POWER_H, "reltol": RELTOL,
+                   "l2": "flushed before each timed transient (512 MB write); factors exceed L2"},
+        "chosen": {"value": value, "reuse": True, "stats": st},
+        "plain": {"value": plain_value, "reuse": False, "steps_timed": plain_steps, "stats": plain["stats"]},
+        "chosen_vs_plain": value / plain_value if plain_value else None,
+        "create_s": create_s,
+        "max_node_voltage_err_vs_oracle": max_err,
+        "e2e": {"value": e2e_value, "unit": TRAN_UNIT, "h2d_bytes_per_step": int(vals.nbytes),
+                "d2h_bytes_per_step": int((nsteps + 1) * V * len(grid_nodes) * 8 + V * n * 8)},
+        "gpu_launches": int(st["launches"]) * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "k_tl_band_solve + k_tl_ic_solve (factor streaming)",
+                     "algorithmic_bytes_per_apply": per_apply, "applies_per_run": applies,
+                     "note": "achieved = factor bytes streamed by every application of the torn factors over the "
+                             "whole transient's event time (refactors, loads and convergence tests included)"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.n_circ <= 0:
@@ -861,6 +1033,9 @@ def main():
         return
     if args.workload == "bjt_ce_ac":
         bench_ac(args)
+        return
+    if args.workload == "power_grid":
+        bench_torn(args)
         return
     import torch
     rank, world, local = dist_env()

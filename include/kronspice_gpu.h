@@ -445,14 +445,18 @@ int ks_mlp_train(ks_mlp* m, ks_batch* b, const double* x_dev, const int32_t* idx
  * without a bound); reuse = 0 refactors at every solve.  Errors per variant as
  * ks_status; a solve that is not accepted after a fresh refactor ends that
  * variant with KS_STATUS_SINGULAR (the reference would fall back to an untorn
- * LU of the whole system).  stats [8]: solves, refactors, refinement steps,
+ * LU of the whole system).  stats [10]: solves, refactors, refinement steps,
  * most refinement steps of one solve, solves not accepted, pieces, coupling
- * rows, largest band (kl + ku).
+ * rows, largest band (kl + ku), band-factor doubles per variant, kernel
+ * launches of the call.
  */
 typedef struct ks_torn ks_torn;
 int ks_torn_create(const ks_topology* topo, int32_t n_variants, const double* values, const int32_t* torn_elems,
                    int32_t n_torn, ks_torn** out);
 void ks_torn_destroy(ks_torn* t);
+/* Stream of the later calls (NULL: the one ks_torn_create made).  The calls
+ * still return only when their results are on the host. */
+int ks_torn_set_stream(ks_torn* t, void* stream);
 int ks_torn_info(const ks_torn* t, int32_t* n_unknowns, int32_t* n_pieces, int32_t* n_coupling_rows,
                  int32_t* max_piece, int32_t* max_band);
 /* analysis.OP of every variant (Newton from zero, InitJct; no gmin / source

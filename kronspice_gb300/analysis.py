@@ -330,7 +330,8 @@ class MultiBatch:
             self.handle = None
 
 
-TORN_STATS = ("solves", "refactors", "refines", "max_passes", "not_accepted", "pieces", "coupling_rows", "max_band")
+TORN_STATS = ("solves", "refactors", "refines", "max_passes", "not_accepted", "pieces", "coupling_rows", "max_band",
+              "band_doubles", "launches")
 
 
 class TornBatch:
@@ -355,13 +356,17 @@ class TornBatch:
         L.ks_torn_info(self.handle, *[ctypes.byref(i) for i in info])
         self.n, self.pieces, self.coupling_rows, self.max_piece, self.max_band = (i.value for i in info)
 
+    def set_stream(self, stream):
+        """Run the later analyses on a CUDA stream handle (None: the batch's own)."""
+        _check(_lib.load().ks_torn_set_stream(self.handle, stream), "ks_torn_set_stream")
+
     def op(self, opt=None, reuse=True):
         """(x [n_var][n], status, iterations, stats) of analysis.OP for every variant."""
         o = (opt or Options()).c()
         x = np.zeros((self.n_var, self.n))
         st = np.zeros(self.n_var, dtype=np.int32)
         it = np.zeros(self.n_var, dtype=np.int32)
-        stats = np.zeros(8, dtype=np.int64)
+        stats = np.zeros(10, dtype=np.int64)
         _check(_lib.load().ks_torn_op(self.handle, ctypes.byref(o), int(reuse), x.ctypes.data, st.ctypes.data,
                                       it.ctypes.data, stats.ctypes.data), "ks_torn_op")
         return x, st, it, dict(zip(TORN_STATS, stats.tolist()))
@@ -378,7 +383,7 @@ class TornBatch:
         st = np.zeros(self.n_var, dtype=np.int32)
         steps = np.zeros(self.n_var, dtype=np.int32)
         it = np.zeros(self.n_var, dtype=np.int32)
-        stats = np.zeros(8, dtype=np.int64)
+        stats = np.zeros(10, dtype=np.int64)
         _check(_lib.load().ks_torn_tran(self.handle, ctypes.byref(sp), ctypes.byref(o), int(reuse),
                                         pr.ctypes.data if len(pr) else None, len(pr),
                                         wave.ctypes.data if len(pr) else None, x.ctypes.data, st.ctypes.data,

@@ -674,7 +674,7 @@ struct ks_torn {
   std::vector<HostPiece> pieces;
   std::vector<int> rp, ci;
   std::vector<void*> owned;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr, own = nullptr;  // the stream in use, the one created here
   cublasHandle_t blas = nullptr;
   // device symbolic
   KElem* d_elem = nullptr;
@@ -693,7 +693,7 @@ struct ks_torn {
   uint8_t *mask, *active;
   std::vector<uint8_t> have;  // factors exist, per variant
   // counters
-  int64_t solves = 0, refactors = 0, refines = 0, max_passes = 0, failed = 0;
+  int64_t solves = 0, refactors = 0, refines = 0, max_passes = 0, failed = 0, launches = 0;
   KPlan view() const {
     KPlan p;
     p.n = hp.n; p.n_elem = hp.n_elem; p.n_values = hp.n_values; p.n_derived = hp.n_derived;
@@ -704,7 +704,7 @@ struct ks_torn {
   ~ks_torn() {
     if (blas) cublasDestroy(blas);
     for (void* p : owned) cudaFree(p);
-    if (st) cudaStreamDestroy(st);
+    if (own) cudaStreamDestroy(own);
   }
 };
 
@@ -970,18 +970,25 @@ int refactor(ks_torn* T, const std::vector<int32_t>& list) {
   int rc = set_mask(T, m);
   if (rc) return rc;
   if (ck(cudaMemsetAsync(T->bad, 0, sizeof(int32_t) * V, s), "memset")) return KS_ECUDA;
+  T->launches++;
   k_tl_equil_rows<<<blocks_for(n * V, 256), 256, 0, s>>>(n, V, T->d_rp, T->d_slot_in, T->J, T->rs, T->bad, T->mask);
+  T->launches++;
   k_tl_equil_cols<<<blocks_for(n * V, 256), 256, 0, s>>>(n, V, T->d_cp, T->d_cslot, T->d_crow, T->J, T->rs, T->cs,
                                                          T->bad, T->mask);
   const unsigned grid = (unsigned)(V * T->P);
+  T->launches++;
   k_tl_band_fill<<<grid, 256, 0, s>>>(T->d_pcs, T->P, V, T->band_stride, T->band, T->d_pslot, T->d_pli, T->d_plj,
                                       T->d_pidx, T->J, T->rs, T->cs, T->mask);
+  T->launches++;
   k_tl_band_lu<<<grid, 256, 0, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->bad, T->mask);
   if (R > 0) {
+    T->launches++;
     k_tl_wc<<<grid, 256, 0, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->d_plocal,
                                  T->d_ports_g, T->d_cc_g, T->rs, T->cs, T->y_stride, T->Y, T->wc_stride, T->Wc, T->mask);
     const int64_t per = (int64_t)R * R;
+    T->launches++;
     k_tl_zero_ic<<<blocks_for(per * V, 256), 256, 0, s>>>(per, V, T->IC, T->mask);
+    T->launches++;
     k_tl_ic_build<<<blocks_for((int64_t)R * V, 128), 128, 0, s>>>(R, V, T->d_offp, T->d_offs, T->d_ci, T->d_pieceOf,
                                                                   T->d_slot_cc, T->d_pcs, T->d_port_a, T->J,
                                                                   T->wc_stride, T->Wc, T->IC, T->mask);
@@ -993,11 +1000,15 @@ int refactor(ks_torn* T, const std::vector<int32_t>& list) {
     cublasSetStream(T->blas, s);
     for (int k0 = 0; k0 < R; k0 += nb) {
       const int jb = std::min(nb, R - k0);
+      T->launches++;
       k_tl_ic_panel<<<(unsigned)V, 1024, 0, s>>>(R, k0, jb, T->IC, T->icpiv, T->bad, T->mask);
+      T->launches++;
       k_tl_ic_swap<<<blocks_for((int64_t)R * V, 256), 256, 0, s>>>(R, k0, jb, T->IC, T->icpiv, V, T->mask);
       const int rest = R - k0 - jb;
       if (rest <= 0) continue;
+      T->launches++;
       k_tl_ic_trsm<<<blocks_for((int64_t)rest * V, 128), 128, 0, s>>>(R, k0, jb, T->IC, V, T->mask);
+      T->launches++;
       k_tl_gemm_ptrs<<<blocks_for(count, 128), 128, 0, s>>>(count, T->list, T->IC, R, k0, jb, T->Aptr, T->Bptr, T->Cptr);
       cublasStatus_t bs = cublasDgemmBatched(T->blas, CUBLAS_OP_N, CUBLAS_OP_N, rest, rest, jb, &minus, T->Aptr, R,
                                              T->Bptr, R, &one, T->Cptr, R, count);
@@ -1017,14 +1028,19 @@ int apply(ks_torn* T, const double* b, double* out) {
   const unsigned grid = (unsigned)(V * T->P);
   const size_t sm = sizeof(double) * T->max_piece;
   if (R == 0) {
+    T->launches++;
     k_tl_band_solve<<<grid, 128, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
                                           T->cs, b, T->d_row_a, nullptr, out, T->mask);
     return ck(cudaGetLastError(), "apply");
   }
+  T->launches++;
   k_tl_band_solve<<<grid, 128, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
                                         T->cs, b, T->d_row_a, nullptr, T->z, T->mask);
+  T->launches++;
   k_tl_h<<<blocks_for((int64_t)R * V, 256), 256, 0, s>>>(R, V, T->d_offp, T->d_offs, T->d_ci, T->J, T->z, T->h, T->mask);
+  T->launches++;
   k_tl_ic_solve<<<(unsigned)V, 1024, sizeof(double) * R, s>>>(R, V, T->IC, T->icpiv, T->h, T->w, T->mask);
+  T->launches++;
   k_tl_band_solve<<<grid, 128, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
                                         T->cs, b, T->d_row_a, T->w, out, T->mask);
   return ck(cudaGetLastError(), "apply");
@@ -1053,6 +1069,7 @@ int torn_solve(ks_torn* T, const std::vector<uint8_t>& want, bool reuse, std::ve
     for (;; pass++) {
       if ((rc = set_mask(T, refine))) return rc;
       if ((rc = ck(cudaMemsetAsync(T->berr, 0, sizeof(unsigned long long) * V, s), "memset"))) return rc;
+      T->launches++;
       k_tl_resid<<<blocks_for(n * V, 256), 256, 0, s>>>((int)n, V, T->d_rp, T->d_ci, T->J, T->rhs, T->x, T->r, T->berr,
                                                         T->mask);
       if ((rc = ck(cudaMemcpyAsync(be.data(), T->berr, sizeof(unsigned long long) * V, cudaMemcpyDeviceToHost, s), "berr")))
@@ -1072,6 +1089,7 @@ int torn_solve(ks_torn* T, const std::vector<uint8_t>& want, bool reuse, std::ve
       }
       if (!any) break;
       if ((rc = set_mask(T, refine)) || (rc = apply(T, T->r, T->dx))) return rc;
+      T->launches++;
       k_tl_axpy_masked<<<blocks_for(n * V, 256), 256, 0, s>>>(n, V, T->dx, T->x, T->mask);
       T->refines++;
     }
@@ -1105,11 +1123,13 @@ int newton(ks_torn* T, LoadParams lp, const KOpts& o, int max_iter, bool reuse, 
     if (!any) return KS_OK;
     int rc = set_mask(T, live);
     if (rc) return rc;
+    T->launches++;
     k_tl_copy_masked<<<blocks_for(n * V, 256), 256, 0, s>>>(n, V, T->x, T->xo, T->mask);
     if ((rc = ck(cudaMemsetAsync(T->J, 0, sizeof(double) * (size_t)T->nnz * V, s), "memset")) ||
         (rc = ck(cudaMemsetAsync(T->rhs, 0, sizeof(double) * n * V, s), "memset")))
       return rc;
     lp.initJct = initJct;
+    T->launches++;
     k_tl_load<<<blocks_for((int64_t)plan.n_elem * V, 256), 256, 0, s>>>(plan, T->values, T->derived, T->state, V, T->d_rp,
                                                                          T->d_ci, T->J, T->rhs, T->x, T->xo, lp, T->mask);
     std::vector<uint8_t> ok;
@@ -1125,7 +1145,9 @@ int newton(ks_torn* T, LoadParams lp, const KOpts& o, int max_iter, bool reuse, 
     if (initJct) { initJct = false; continue; }
     if ((rc = set_mask(T, live))) return rc;
     if ((rc = ck(cudaMemsetAsync(T->flags, 0, sizeof(int32_t) * V, s), "memset"))) return rc;
+    T->launches++;
     k_tl_conv_x<<<blocks_for(n * V, 256), 256, 0, s>>>((int)n, V, T->d_isv, T->x, T->xo, o, T->mask, T->flags);
+    T->launches++;
     k_tl_conv_elem<<<blocks_for((int64_t)T->n_nonlin * V, 256), 256, 0, s>>>(
         plan, T->values, T->derived, T->state, V, T->d_nonlin, T->n_nonlin, T->x, T->xo, o, T->mask, T->flags);
     std::vector<int32_t> fl(V);
@@ -1160,12 +1182,13 @@ extern "C" int ks_torn_create(const ks_topology* topo, int32_t n_variants, const
   if ((rc = alloc_numeric(T))) { delete T; return rc; }
   const size_t band_smem = sizeof(double) * (size_t)T->max_piece;
   if (band_smem > 48 * 1024) cudaFuncSetAttribute(k_tl_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
-  if (cudaStreamCreateWithFlags(&T->st, cudaStreamNonBlocking) != cudaSuccess ||
+  if (cudaStreamCreateWithFlags(&T->own, cudaStreamNonBlocking) != cudaSuccess ||
       cublasCreate(&T->blas) != CUBLAS_STATUS_SUCCESS) {
     set_error("ks_torn_create: stream or cuBLAS handle");
     delete T;
     return KS_ECUDA;
   }
+  T->st = T->own;
   // values to [n_values][V], then the per-variant constants
   const int64_t V = n_variants;
   double* rows = nullptr;
@@ -1184,6 +1207,12 @@ extern "C" int ks_torn_create(const ks_topology* topo, int32_t n_variants, const
 
 extern "C" void ks_torn_destroy(ks_torn* T) { delete T; }
 
+extern "C" int ks_torn_set_stream(ks_torn* T, void* stream) {
+  if (!T) return KS_EINVAL;
+  T->st = stream ? static_cast<cudaStream_t>(stream) : T->own;
+  return KS_OK;
+}
+
 extern "C" int ks_torn_info(const ks_torn* T, int32_t* n_unknowns, int32_t* n_pieces, int32_t* n_coupling_rows,
                             int32_t* max_piece, int32_t* max_band) {
   if (!T) return KS_EINVAL;
@@ -1200,7 +1229,7 @@ namespace {
 void stats_out(const ks_torn* T, int64_t* s) {
   if (!s) return;
   s[0] = T->solves; s[1] = T->refactors; s[2] = T->refines; s[3] = T->max_passes; s[4] = T->failed;
-  s[5] = T->P; s[6] = T->R; s[7] = T->max_band;
+  s[5] = T->P; s[6] = T->R; s[7] = T->max_band; s[8] = T->band_stride; s[9] = T->launches;
 }
 
 int fresh_state(ks_torn* T, double step, double stop) {
@@ -1209,10 +1238,13 @@ int fresh_state(ks_torn* T, double step, double stop) {
   KsDeviceBatch b{};
   b.plan = plan; b.B = V; b.values = T->values; b.derived = T->derived; b.state = T->state;
   if (ks_launch_setup(b, step, stop, T->st)) return ck(cudaGetLastError(), "setup");
+  T->launches++;
   k_tl_init_state<<<blocks_for((int64_t)(plan.n_state + 1) * V, 256), 256, 0, T->st>>>(plan, T->derived, T->state, V);
+  T->launches++;
   k_tl_init_mos<<<blocks_for((int64_t)plan.n_elem * V, 256), 256, 0, T->st>>>(plan, T->derived, T->state, V);
   if (ck(cudaMemsetAsync(T->x, 0, sizeof(double) * T->n * V, T->st), "memset")) return KS_ECUDA;
   T->solves = T->refactors = T->refines = T->max_passes = T->failed = 0;
+  T->launches = 3;
   T->have.assign(T->V, 0);
   return ck(cudaGetLastError(), "init");
 }
@@ -1223,6 +1255,7 @@ int accept_all_variants(ks_torn* T, const std::vector<int32_t>& status, double t
   int rc = set_mask(T, m);
   if (rc) return rc;
   KPlan plan = T->view();
+  T->launches++;
   k_tl_accept<<<blocks_for((int64_t)plan.n_elem * T->V, 256), 256, 0, T->st>>>(plan, T->values, T->derived, T->state,
                                                                                 T->V, T->x, t, mode, gmin, T->mask);
   return ck(cudaGetLastError(), "accept");
@@ -1289,9 +1322,11 @@ extern "C" int ks_torn_tran(ks_torn* T, const ks_tran_spec* spec, const ks_optio
     cudaMemcpyAsync(d_probes, probes, sizeof(int32_t) * n_probes, cudaMemcpyHostToDevice, T->st);
   }
   auto record = [&](long k) {
-    if (n_probes > 0)
+    if (n_probes > 0) {
+      T->launches++;
       k_tl_record<<<blocks_for((int64_t)n_probes * V, 256), 256, 0, T->st>>>(n_probes, d_probes, V, T->x,
                                                                                d_wave + (size_t)k * V * n_probes);
+    }
   };
   // the transient operating point (analysis/tran.go: dcSolve at ModeTranOP, Accept)
   LoadParams lp;

@@ -104,11 +104,12 @@ def options(reltol=0.0, abstol=0.0, vntol=0.0, gmin=0.0, itl1=0, itl4=0, backend
 
 def unknowns(pk):
     n = ctypes.c_int32()
-    isv = np.zeros(4096, dtype=np.int32)
-    rc = lib().kso_unknowns(pk.tref(), _ptr(pk.values), ctypes.byref(n), _ptr(isv))
+    rc = lib().kso_unknowns(pk.tref(), _ptr(pk.values), ctypes.byref(n), None)
     if rc:
         raise ValueError("kso_unknowns failed")
-    return n.value, isv[:n.value].astype(bool)
+    isv = np.zeros(n.value, dtype=np.int32)
+    lib().kso_unknowns(pk.tref(), _ptr(pk.values), ctypes.byref(n), _ptr(isv))
+    return n.value, isv.astype(bool)
 
 
 def op(pk, opt=None, x0=None):
