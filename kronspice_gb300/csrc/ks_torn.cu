@@ -308,7 +308,11 @@ __global__ void __launch_bounds__(256) k_tl_band_lu(const PieceD* pcs, int64_t V
 
 // Solve of every piece of the selected variants: out = cs . Ab^-1 (rs . (b - P.w)),
 // with the subtraction only when w is given (the second solve of the apply).
-__global__ void __launch_bounds__(128) k_tl_band_solve(const PieceD* pcs, int64_t V, int64_t band_stride,
+// Thread t owns the band rows t, t + T, ... (at most KS_TORN_NR of them): the
+// next column's entries are loaded while the current column is applied, so
+// the column-by-column sweep waits on a barrier, not on memory.
+#define KS_TORN_NR 4
+__global__ void __launch_bounds__(512) k_tl_band_solve(const PieceD* pcs, int64_t V, int64_t band_stride,
                                                        const double* band, int64_t piv_stride, const int32_t* piv_all,
                                                        const int32_t* pidx, const double* rs, const double* cs,
                                                        const double* b, const int32_t* row_a, const double* w,
@@ -320,7 +324,8 @@ __global__ void __launch_bounds__(128) k_tl_band_solve(const PieceD* pcs, int64_
   const double* AB = band + (int64_t)v * band_stride + pc.band_off;
   const int32_t* piv = piv_all + (int64_t)v * piv_stride + pc.idx_off;
   const int n = pc.n, kl = pc.kl, ldab = pc.ldab, kv = pc.kl + pc.ku;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  const int t = threadIdx.x, T = blockDim.x;
+  for (int i = t; i < n; i += T) {
     const int g = pidx[pc.idx_off + i];
     double bi = b[(int64_t)g * V + v];
     if (w) {
@@ -330,28 +335,65 @@ __global__ void __launch_bounds__(128) k_tl_band_solve(const PieceD* pcs, int64_
     y[i] = bi * rs[(int64_t)g * V + v];
   }
   __syncthreads();
-  // L: row interchanges and the unit lower band, column by column
+  // L: row interchanges and the unit lower band; row j+1+o of column j, o = t + r T
+  double lc[KS_TORN_NR], ln[KS_TORN_NR];
+#pragma unroll
+  for (int r = 0; r < KS_TORN_NR; r++) {
+    const int o = t + r * T;
+    lc[r] = (o < kl && 1 + o < n) ? AB[kv + 1 + o] : 0.0;
+  }
+  int pcur = piv[0];
   for (int j = 0; j < n; j++) {
     const int km = min(kl, n - 1 - j);
-    const int pj = piv[j];
-    if (pj != j) {  // the same for every thread
-      if (threadIdx.x == 0) { const double t = y[j]; y[j] = y[pj]; y[pj] = t; }
+#pragma unroll
+    for (int r = 0; r < KS_TORN_NR; r++) {
+      const int o = t + r * T;
+      ln[r] = (o < kl && j + 2 + o < n) ? AB[kv + 1 + o + (int64_t)(j + 1) * ldab] : 0.0;
+    }
+    const int pnext = j + 1 < n ? piv[j + 1] : 0;
+    if (pcur != j) {  // the same for every thread
+      if (t == 0) { const double tmp = y[j]; y[j] = y[pcur]; y[pcur] = tmp; }
       __syncthreads();
     }
     const double yj = y[j];
-    for (int i = 1 + (int)threadIdx.x; i <= km; i += blockDim.x) y[j + i] -= AB[kv + i + (int64_t)j * ldab] * yj;
+#pragma unroll
+    for (int r = 0; r < KS_TORN_NR; r++) {
+      const int o = t + r * T;
+      if (o < km) y[j + 1 + o] -= lc[r] * yj;
+      lc[r] = ln[r];
+    }
     __syncthreads();
+    pcur = pnext;
   }
-  // U: the upper band (kl + ku above the diagonal), column by column
+  // U: column j holds rows j-kv .. j at AB[o + j ldab] (row j - kv + o) and the diagonal at AB[kv + j ldab]
+  double uc[KS_TORN_NR], un[KS_TORN_NR];
+#pragma unroll
+  for (int r = 0; r < KS_TORN_NR; r++) {
+    const int o = t + r * T;
+    uc[r] = (o < kv && n - 1 - kv + o >= 0) ? AB[o + (int64_t)(n - 1) * ldab] : 0.0;
+  }
+  double dcur = AB[kv + (int64_t)(n - 1) * ldab];
   for (int j = n - 1; j >= 0; j--) {
-    const double yj = y[j] / AB[kv + (int64_t)j * ldab];
+#pragma unroll
+    for (int r = 0; r < KS_TORN_NR; r++) {
+      const int o = t + r * T;
+      un[r] = (j > 0 && o < kv && j - 1 - kv + o >= 0) ? AB[o + (int64_t)(j - 1) * ldab] : 0.0;
+    }
+    const double dnext = j > 0 ? AB[kv + (int64_t)(j - 1) * ldab] : 1.0;
+    const double yj = y[j] / dcur;
     __syncthreads();
-    if (threadIdx.x == 0) y[j] = yj;
-    const int top = max(0, j - kv);
-    for (int i = top + (int)threadIdx.x; i < j; i += blockDim.x) y[i] -= AB[kv + i - j + (int64_t)j * ldab] * yj;
+    if (t == 0) y[j] = yj;
+#pragma unroll
+    for (int r = 0; r < KS_TORN_NR; r++) {
+      const int o = t + r * T;
+      const int i = j - kv + o;
+      if (o < kv && i >= 0) y[i] -= uc[r] * yj;
+      uc[r] = un[r];
+    }
     __syncthreads();
+    dcur = dnext;
   }
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int i = t; i < n; i += T) {
     const int g = pidx[pc.idx_off + i];
     out[(int64_t)g * V + v] = y[i] * cs[(int64_t)g * V + v];
   }
@@ -552,7 +594,10 @@ __global__ void k_tl_gemm_ptrs(int count, const int32_t* list, double* IC, int R
   Cp[t] = A + (k0 + jb) + (int64_t)(k0 + jb) * R;
 }
 
-// w = IC^-1 h with the factors (getrs: interchanges, unit lower, upper); one CTA per variant.
+// w = IC^-1 h with the factors (getrs: interchanges, unit lower, upper), one CTA
+// per variant, by panels of 32 columns: the small triangle of a panel column by
+// column, then the rest of the vector updated by the panel as one matrix-vector
+// product (coalesced column reads by all threads).
 __global__ void __launch_bounds__(1024) k_tl_ic_solve(int R, int64_t V, const double* IC, const int32_t* ipiv,
                                                       const double* h, double* w, const uint8_t* mask) {
   extern __shared__ double y[];
@@ -560,29 +605,49 @@ __global__ void __launch_bounds__(1024) k_tl_ic_solve(int R, int64_t V, const do
   if (!mask[v]) return;
   const double* A = IC + (int64_t)v * R * R;
   const int32_t* piv = ipiv + (int64_t)v * R;
-  for (int i = threadIdx.x; i < R; i += blockDim.x) y[i] = h[(int64_t)i * V + v];
+  const int t = threadIdx.x, T = blockDim.x;
+  constexpr int NB = 32;
+  for (int i = t; i < R; i += T) y[i] = h[(int64_t)i * V + v];
   __syncthreads();
-  if (threadIdx.x == 0)
+  if (t == 0)
     for (int j = 0; j < R; j++) {
       const int p = piv[j];
-      if (p != j) { const double t = y[j]; y[j] = y[p]; y[p] = t; }
+      if (p != j) { const double tmp = y[j]; y[j] = y[p]; y[p] = tmp; }
     }
   __syncthreads();
-  for (int j = 0; j < R; j++) {
-    const double yj = y[j];
-    if (yj != 0)
-      for (int i = j + 1 + (int)threadIdx.x; i < R; i += blockDim.x) y[i] -= A[i + (int64_t)j * R] * yj;
+  for (int k0 = 0; k0 < R; k0 += NB) {
+    const int k1 = min(k0 + NB, R);
+    for (int j = k0; j < k1; j++) {  // unit lower triangle of the panel
+      const double yj = y[j];
+      const int i = j + 1 + t;
+      if (i < k1) y[i] -= A[i + (int64_t)j * R] * yj;
+      __syncthreads();
+    }
+    for (int i = k1 + t; i < R; i += T) {  // the rows below: y_i -= L(i, k0:k1) . y(k0:k1)
+      double s = 0;
+      for (int j = k0; j < k1; j++) s += A[i + (int64_t)j * R] * y[j];
+      y[i] -= s;
+    }
     __syncthreads();
   }
-  for (int j = R - 1; j >= 0; j--) {
-    const double yj = y[j] / A[j + (int64_t)j * R];
-    __syncthreads();
-    if (threadIdx.x == 0) y[j] = yj;
-    if (yj != 0)
-      for (int i = threadIdx.x; i < j; i += blockDim.x) y[i] -= A[i + (int64_t)j * R] * yj;
+  for (int k1 = R; k1 > 0; k1 -= NB) {
+    const int k0 = max(0, k1 - NB);
+    for (int j = k1 - 1; j >= k0; j--) {  // upper triangle of the panel
+      const double yj = y[j] / A[j + (int64_t)j * R];
+      __syncthreads();
+      if (t == 0) y[j] = yj;
+      const int i = k0 + t;
+      if (i < j) y[i] -= A[i + (int64_t)j * R] * yj;
+      __syncthreads();
+    }
+    for (int i = t; i < k0; i += T) {  // the rows above: y_i -= U(i, k0:k1) . y(k0:k1)
+      double s = 0;
+      for (int j = k0; j < k1; j++) s += A[i + (int64_t)j * R] * y[j];
+      y[i] -= s;
+    }
     __syncthreads();
   }
-  for (int i = threadIdx.x; i < R; i += blockDim.x) w[(int64_t)i * V + v] = y[i];
+  for (int i = t; i < R; i += T) w[(int64_t)i * V + v] = y[i];
 }
 
 // h = M.Q.z: each coupling row's entries times z at their columns.
@@ -617,7 +682,28 @@ struct HostPiece {
   std::vector<int> slots;  // in-piece slots
 };
 
-// reverse Cuthill-McKee order of a piece (symmetric pattern within the piece)
+// Breadth-first levels from k within the unseen part of a piece: the last level's
+// node of least degree and the eccentricity (George and Liu's pseudo-peripheral
+// node search, 1979).
+std::pair<int, int> far_node(int k, const std::vector<int>& nodes, const std::vector<std::vector<int>>& adj,
+                             const std::vector<int>& local, const std::vector<int>& deg, const std::vector<char>& seen) {
+  std::vector<int> d(nodes.size(), -1), q{k};
+  d[k] = 0;
+  for (size_t h = 0; h < q.size(); h++)
+    for (int g : adj[nodes[q[h]]]) {
+      const int j = local[g];
+      if (j >= 0 && !seen[j] && d[j] < 0) { d[j] = d[q[h]] + 1; q.push_back(j); }
+    }
+  const int ecc = d[q.back()];
+  int best = q.back();
+  for (int j : q)
+    if (d[j] == ecc && (deg[j] < deg[best] || (deg[j] == deg[best] && j < best))) best = j;
+  return {best, ecc};
+}
+
+// reverse Cuthill-McKee order of a piece (symmetric pattern within the piece),
+// each component started at a pseudo-peripheral node, so a grid piece gets
+// levels across its diagonal and a band about as wide as one of its sides
 std::vector<int> rcm(const std::vector<int>& nodes, const std::vector<std::vector<int>>& adj, const std::vector<int>& local) {
   const int m = (int)nodes.size();
   std::vector<int> deg(m), order;
@@ -628,6 +714,13 @@ std::vector<int> rcm(const std::vector<int>& nodes, const std::vector<std::vecto
     int start = -1;
     for (int k = 0; k < m; k++)
       if (!seen[k] && (start < 0 || deg[k] < deg[start])) start = k;
+    auto f = far_node(start, nodes, adj, local, deg, seen);
+    for (int it = 0; it < 8; it++) {
+      auto g = far_node(f.first, nodes, adj, local, deg, seen);
+      if (g.second <= f.second) break;
+      f = g;
+    }
+    start = f.first;
     seen[start] = 1;
     size_t head = order.size();
     order.push_back(start);
@@ -671,6 +764,7 @@ struct ks_torn {
   ksh::HostPlan hp;
   int V = 0, n = 0, nnz = 0, R = 0, P = 0, n_nonlin = 0;
   int max_piece = 0, max_band = 0;
+  int solve_threads = 128;  // block of the band solves: every band row owned by one thread
   std::vector<HostPiece> pieces;
   std::vector<int> rp, ci;
   std::vector<void*> owned;
@@ -886,6 +980,12 @@ int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_t
     if (d.n > 12000) { *err = "ks_torn: a piece of " + std::to_string(d.n) + " unknowns (the band solve holds at most 12,000)"; return KS_EUNSUPPORTED; }
   }
   T->band_stride = band; T->piv_stride = n; T->wc_stride = wc; T->y_stride = y;
+  {
+    int need = (T->max_band + KS_TORN_NR - 1) / KS_TORN_NR;  // rows per thread at most KS_TORN_NR
+    need = std::max(64, (need + 31) / 32 * 32);
+    if (need > 512) { *err = "ks_torn: a piece's band (" + std::to_string(T->max_band) + ") is wider than 2,048"; return KS_EUNSUPPORTED; }
+    T->solve_threads = need;
+  }
   if (T->R > 6000) { *err = "ks_torn: " + std::to_string(T->R) + " coupling rows (the interconnection solve holds at most 6,000)"; return KS_EUNSUPPORTED; }
   // CSC of the in-piece slots (column equilibration)
   std::vector<int32_t> cp(n + 1, 0), cslot, crow;
@@ -1027,21 +1127,22 @@ int apply(ks_torn* T, const double* b, double* out) {
   cudaStream_t s = T->st;
   const unsigned grid = (unsigned)(V * T->P);
   const size_t sm = sizeof(double) * T->max_piece;
+  const int bt = T->solve_threads;
   if (R == 0) {
     T->launches++;
-    k_tl_band_solve<<<grid, 128, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
+    k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
                                           T->cs, b, T->d_row_a, nullptr, out, T->mask);
     return ck(cudaGetLastError(), "apply");
   }
   T->launches++;
-  k_tl_band_solve<<<grid, 128, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
+  k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
                                         T->cs, b, T->d_row_a, nullptr, T->z, T->mask);
   T->launches++;
   k_tl_h<<<blocks_for((int64_t)R * V, 256), 256, 0, s>>>(R, V, T->d_offp, T->d_offs, T->d_ci, T->J, T->z, T->h, T->mask);
   T->launches++;
   k_tl_ic_solve<<<(unsigned)V, 1024, sizeof(double) * R, s>>>(R, V, T->IC, T->icpiv, T->h, T->w, T->mask);
   T->launches++;
-  k_tl_band_solve<<<grid, 128, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
+  k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
                                         T->cs, b, T->d_row_a, T->w, out, T->mask);
   return ck(cudaGetLastError(), "apply");
 }
@@ -1064,6 +1165,7 @@ int torn_solve(ks_torn* T, const std::vector<uint8_t>& want, bool reuse, std::ve
     if (rc) return rc;
     if ((rc = set_mask(T, cur)) || (rc = apply(T, T->rhs, T->x))) return rc;
     std::vector<unsigned long long> be(V);
+    std::vector<double> prev(V, INFINITY);
     std::vector<uint8_t> refine = cur;
     int pass = 0;
     for (;; pass++) {
@@ -1080,7 +1182,11 @@ int torn_solve(ks_torn* T, const std::vector<uint8_t>& want, bool reuse, std::ve
         if (!refine[v]) continue;
         double e;
         memcpy(&e, &be[v], sizeof e);
-        if (e <= 1e-14 || pass == 12) {
+        // stop at 1e-14, after 12 passes, or when a pass no longer divides the
+        // error by 20 (stale factors too far from J: a refactor is cheaper)
+        const bool stalled = pass >= 2 && e > 0.05 * prev[v];
+        prev[v] = e;
+        if (e <= 1e-14 || pass == 12 || stalled) {
           refine[v] = 0;
           if (e <= 1e-12) (*ok)[v] = 1;
         } else {
@@ -1336,6 +1442,8 @@ extern "C" int ks_torn_tran(ks_torn* T, const ks_tran_spec* spec, const ks_optio
   if (!rc) rc = accept_all_variants(T, status, 0.0, ModeTranOP, o.gmin);
   if (!rc) record(0);
   // fixed steps; backward Euler at the first, then the spec's method
+  // the companion models change every Jacobian at the first step: fresh factors
+  T->have.assign(V, 0);
   int order = BE;
   const int method = spec->method == KS_METHOD_BE ? BE : TRAP;
   for (long k = 1; k < npts && !rc; k++) {
