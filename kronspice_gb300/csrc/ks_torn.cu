@@ -27,6 +27,7 @@
 // Device loads, limiting, convergence tests and Accept are the engine's
 // per-element device code (ks_solve.cuh), one thread per (element, variant).
 #include <cublas_v2.h>
+#include <cuda_pipeline.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -308,16 +309,17 @@ __global__ void __launch_bounds__(256) k_tl_band_lu(const PieceD* pcs, int64_t V
 
 // Solve of every piece of the selected variants: out = cs . Ab^-1 (rs . (b - P.w)),
 // with the subtraction only when w is given (the second solve of the apply).
-// Thread t owns the band rows t, t + T, ... (at most KS_TORN_NR of them): the
-// next column's entries are loaded while the current column is applied, so
-// the column-by-column sweep waits on a barrier, not on memory.
-#define KS_TORN_NR 4
+// The band is swept column by column, each column a barrier apart; the columns
+// are staged into shared memory KS_TORN_CH at a time with asynchronous copies,
+// the next block of columns in flight while the current one is applied, so the
+// sweep waits on barriers, not on memory.  ldab is even (16-byte aligned columns).
+#define KS_TORN_CH 16
 __global__ void __launch_bounds__(512) k_tl_band_solve(const PieceD* pcs, int64_t V, int64_t band_stride,
                                                        const double* band, int64_t piv_stride, const int32_t* piv_all,
                                                        const int32_t* pidx, const double* rs, const double* cs,
                                                        const double* b, const int32_t* row_a, const double* w,
-                                                       double* out, const uint8_t* mask) {
-  extern __shared__ double y[];
+                                                       double* out, const uint8_t* mask, int max_n, int max_ldab) {
+  extern __shared__ __align__(16) double smem[];
   const int v = blockIdx.x % V, p = blockIdx.x / V;
   if (!mask[v]) return;
   const PieceD pc = pcs[p];
@@ -325,6 +327,10 @@ __global__ void __launch_bounds__(512) k_tl_band_solve(const PieceD* pcs, int64_
   const int32_t* piv = piv_all + (int64_t)v * piv_stride + pc.idx_off;
   const int n = pc.n, kl = pc.kl, ldab = pc.ldab, kv = pc.kl + pc.ku;
   const int t = threadIdx.x, T = blockDim.x;
+  double* y = smem;                                                // [max_n], rounded to 2
+  double* buf = smem + ((max_n + 1) & ~1);                          // [2][KS_TORN_CH][max_ldab]
+  __shared__ int spiv[2][KS_TORN_CH];
+  const int bufsz = KS_TORN_CH * max_ldab;
   for (int i = t; i < n; i += T) {
     const int g = pidx[pc.idx_off + i];
     double bi = b[(int64_t)g * V + v];
@@ -334,65 +340,69 @@ __global__ void __launch_bounds__(512) k_tl_band_solve(const PieceD* pcs, int64_
     }
     y[i] = bi * rs[(int64_t)g * V + v];
   }
-  __syncthreads();
-  // L: row interchanges and the unit lower band; row j+1+o of column j, o = t + r T
-  double lc[KS_TORN_NR], ln[KS_TORN_NR];
-#pragma unroll
-  for (int r = 0; r < KS_TORN_NR; r++) {
-    const int o = t + r * T;
-    lc[r] = (o < kl && 1 + o < n) ? AB[kv + 1 + o] : 0.0;
-  }
-  int pcur = piv[0];
-  for (int j = 0; j < n; j++) {
-    const int km = min(kl, n - 1 - j);
-#pragma unroll
-    for (int r = 0; r < KS_TORN_NR; r++) {
-      const int o = t + r * T;
-      ln[r] = (o < kl && j + 2 + o < n) ? AB[kv + 1 + o + (int64_t)(j + 1) * ldab] : 0.0;
-    }
-    const int pnext = j + 1 < n ? piv[j + 1] : 0;
-    if (pcur != j) {  // the same for every thread
-      if (t == 0) { const double tmp = y[j]; y[j] = y[pcur]; y[pcur] = tmp; }
+  const int nch = (n + KS_TORN_CH - 1) / KS_TORN_CH;
+  // stage block c (columns c*CH ..) into buffer c & 1
+  auto stage = [&](int c) {
+    const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
+    const int units = cols * ldab / 2;
+    const double* src = AB + (int64_t)j0 * ldab;
+    double* dst = buf + (c & 1) * bufsz;
+    for (int u = t; u < units; u += T) __pipeline_memcpy_async(dst + 2 * u, src + 2 * u, 16);
+    __pipeline_commit();
+    if (t < cols) spiv[c & 1][t] = piv[j0 + t];
+  };
+  // L: row interchanges and the unit lower band
+  stage(0);
+  for (int c = 0; c < nch; c++) {
+    if (c + 1 < nch) stage(c + 1); else __pipeline_commit();
+    __pipeline_wait_prior(1);
+    __syncthreads();
+    const double* B = buf + (c & 1) * bufsz;
+    const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
+    for (int jj = 0; jj < cols; jj++) {
+      const int j = j0 + jj;
+      const int km = min(kl, n - 1 - j);
+      const int pj = spiv[c & 1][jj];
+      if (pj != j) {  // the same for every thread
+        if (t == 0) { const double tmp = y[j]; y[j] = y[pj]; y[pj] = tmp; }
+        __syncthreads();
+      }
+      const double yj = y[j];
+      for (int o = t; o < km; o += T) y[j + 1 + o] -= B[kv + 1 + o + jj * ldab] * yj;
       __syncthreads();
     }
-    const double yj = y[j];
-#pragma unroll
-    for (int r = 0; r < KS_TORN_NR; r++) {
-      const int o = t + r * T;
-      if (o < km) y[j + 1 + o] -= lc[r] * yj;
-      lc[r] = ln[r];
-    }
-    __syncthreads();
-    pcur = pnext;
   }
-  // U: column j holds rows j-kv .. j at AB[o + j ldab] (row j - kv + o) and the diagonal at AB[kv + j ldab]
-  double uc[KS_TORN_NR], un[KS_TORN_NR];
-#pragma unroll
-  for (int r = 0; r < KS_TORN_NR; r++) {
-    const int o = t + r * T;
-    uc[r] = (o < kv && n - 1 - kv + o >= 0) ? AB[o + (int64_t)(n - 1) * ldab] : 0.0;
-  }
-  double dcur = AB[kv + (int64_t)(n - 1) * ldab];
-  for (int j = n - 1; j >= 0; j--) {
-#pragma unroll
-    for (int r = 0; r < KS_TORN_NR; r++) {
-      const int o = t + r * T;
-      un[r] = (j > 0 && o < kv && j - 1 - kv + o >= 0) ? AB[o + (int64_t)(j - 1) * ldab] : 0.0;
-    }
-    const double dnext = j > 0 ? AB[kv + (int64_t)(j - 1) * ldab] : 1.0;
-    const double yj = y[j] / dcur;
+  // U: column j holds rows j-kv .. j (row j - kv + o at offset o, the diagonal at kv)
+  __pipeline_wait_prior(0);
+  __syncthreads();
+  auto stage_back = [&](int c, int slot) {
+    const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
+    const int units = cols * ldab / 2;
+    const double* src = AB + (int64_t)j0 * ldab;
+    double* dst = buf + slot * bufsz;
+    for (int u = t; u < units; u += T) __pipeline_memcpy_async(dst + 2 * u, src + 2 * u, 16);
+    __pipeline_commit();
+  };
+  stage_back(nch - 1, 0);
+  for (int c = nch - 1, k = 0; c >= 0; c--, k++) {
+    if (c > 0) stage_back(c - 1, (k + 1) & 1); else __pipeline_commit();
+    __pipeline_wait_prior(1);
     __syncthreads();
-    if (t == 0) y[j] = yj;
-#pragma unroll
-    for (int r = 0; r < KS_TORN_NR; r++) {
-      const int o = t + r * T;
-      const int i = j - kv + o;
-      if (o < kv && i >= 0) y[i] -= uc[r] * yj;
-      uc[r] = un[r];
+    const double* B = buf + (k & 1) * bufsz;
+    const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
+    for (int jj = cols - 1; jj >= 0; jj--) {
+      const int j = j0 + jj;
+      const double yj = y[j] / B[kv + jj * ldab];
+      __syncthreads();
+      if (t == 0) y[j] = yj;
+      for (int o = t; o < kv; o += T) {
+        const int i = j - kv + o;
+        if (i >= 0) y[i] -= B[o + jj * ldab] * yj;
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    dcur = dnext;
   }
+  __pipeline_wait_prior(0);
   for (int i = t; i < n; i += T) {
     const int g = pidx[pc.idx_off + i];
     out[(int64_t)g * V + v] = y[i] * cs[(int64_t)g * V + v];
@@ -764,7 +774,8 @@ struct ks_torn {
   ksh::HostPlan hp;
   int V = 0, n = 0, nnz = 0, R = 0, P = 0, n_nonlin = 0;
   int max_piece = 0, max_band = 0;
-  int solve_threads = 128;  // block of the band solves: every band row owned by one thread
+  int solve_threads = 128;  // block of the band solves
+  int max_ldab = 0;
   std::vector<HostPiece> pieces;
   std::vector<int> rp, ci;
   std::vector<void*> owned;
@@ -827,6 +838,11 @@ void stamp_pattern(const ksh::HostPlan& hp, std::vector<std::vector<int>>& rows)
     }
   }
   for (int i = 0; i < hp.n; i++) add(i, i);
+}
+
+size_t torn_solve_smem(const ks_torn* T) {
+  return sizeof(double) * (((size_t)T->max_piece + 1) & ~(size_t)1) +
+         sizeof(double) * 2 * (size_t)KS_TORN_CH * (size_t)T->max_ldab;
 }
 
 int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_torn, std::string* err) {
@@ -960,7 +976,7 @@ int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_t
   for (int p = 0; p < P; p++) {
     HostPiece& h = T->pieces[p];
     PieceD& d = pcs[p];
-    d.n = (int)h.idx.size(); d.kl = h.kl; d.ku = h.ku; d.ldab = 2 * h.kl + h.ku + 1;
+    d.n = (int)h.idx.size(); d.kl = h.kl; d.ku = h.ku; d.ldab = (2 * h.kl + h.ku + 2) & ~1;  // even: aligned columns
     d.band_off = band; band += (int64_t)d.ldab * d.n;
     d.idx_off = (int)pidx.size();
     pidx.insert(pidx.end(), h.idx.begin(), h.idx.end());
@@ -976,15 +992,16 @@ int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_t
       pslot.push_back(s); pli.push_back(plocal[i]); plj.push_back(plocal[T->ci[s]]);
     }
     T->max_piece = std::max(T->max_piece, d.n);
+    T->max_ldab = std::max(T->max_ldab, d.ldab);
     T->max_band = std::max(T->max_band, d.kl + d.ku);
     if (d.n > 12000) { *err = "ks_torn: a piece of " + std::to_string(d.n) + " unknowns (the band solve holds at most 12,000)"; return KS_EUNSUPPORTED; }
   }
   T->band_stride = band; T->piv_stride = n; T->wc_stride = wc; T->y_stride = y;
-  {
-    int need = (T->max_band + KS_TORN_NR - 1) / KS_TORN_NR;  // rows per thread at most KS_TORN_NR
-    need = std::max(64, (need + 31) / 32 * 32);
-    if (need > 512) { *err = "ks_torn: a piece's band (" + std::to_string(T->max_band) + ") is wider than 2,048"; return KS_EUNSUPPORTED; }
-    T->solve_threads = need;
+  T->solve_threads = std::min(256, std::max(64, (T->max_band + 31) / 32 * 32));
+  if (torn_solve_smem(T) > 227 * 1024) {
+    *err = "ks_torn: a piece of " + std::to_string(T->max_piece) + " unknowns with a band of " +
+           std::to_string(T->max_band) + " does not fit the band solve's shared memory";
+    return KS_EUNSUPPORTED;
   }
   if (T->R > 6000) { *err = "ks_torn: " + std::to_string(T->R) + " coupling rows (the interconnection solve holds at most 6,000)"; return KS_EUNSUPPORTED; }
   // CSC of the in-piece slots (column equilibration)
@@ -1126,24 +1143,24 @@ int apply(ks_torn* T, const double* b, double* out) {
   const int R = T->R;
   cudaStream_t s = T->st;
   const unsigned grid = (unsigned)(V * T->P);
-  const size_t sm = sizeof(double) * T->max_piece;
+  const size_t sm = torn_solve_smem(T);
   const int bt = T->solve_threads;
   if (R == 0) {
     T->launches++;
     k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
-                                          T->cs, b, T->d_row_a, nullptr, out, T->mask);
+                                          T->cs, b, T->d_row_a, nullptr, out, T->mask, T->max_piece, T->max_ldab);
     return ck(cudaGetLastError(), "apply");
   }
   T->launches++;
   k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
-                                        T->cs, b, T->d_row_a, nullptr, T->z, T->mask);
+                                        T->cs, b, T->d_row_a, nullptr, T->z, T->mask, T->max_piece, T->max_ldab);
   T->launches++;
   k_tl_h<<<blocks_for((int64_t)R * V, 256), 256, 0, s>>>(R, V, T->d_offp, T->d_offs, T->d_ci, T->J, T->z, T->h, T->mask);
   T->launches++;
   k_tl_ic_solve<<<(unsigned)V, 1024, sizeof(double) * R, s>>>(R, V, T->IC, T->icpiv, T->h, T->w, T->mask);
   T->launches++;
   k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
-                                        T->cs, b, T->d_row_a, T->w, out, T->mask);
+                                        T->cs, b, T->d_row_a, T->w, out, T->mask, T->max_piece, T->max_ldab);
   return ck(cudaGetLastError(), "apply");
 }
 
@@ -1182,9 +1199,9 @@ int torn_solve(ks_torn* T, const std::vector<uint8_t>& want, bool reuse, std::ve
         if (!refine[v]) continue;
         double e;
         memcpy(&e, &be[v], sizeof e);
-        // stop at 1e-14, after 12 passes, or when a pass no longer divides the
-        // error by 20 (stale factors too far from J: a refactor is cheaper)
-        const bool stalled = pass >= 2 && e > 0.05 * prev[v];
+        // stop at 1e-14, after 12 passes, or when a pass no longer halves the
+        // error (stale factors too far from J: a refactor follows)
+        const bool stalled = pass >= 2 && e > 0.5 * prev[v];
         prev[v] = e;
         if (e <= 1e-14 || pass == 12 || stalled) {
           refine[v] = 0;
@@ -1286,7 +1303,7 @@ extern "C" int ks_torn_create(const ks_topology* topo, int32_t n_variants, const
   rc = build_plan(T, topo, torn_elems, n_torn, &err);
   if (rc) { set_error(err); delete T; return rc; }
   if ((rc = alloc_numeric(T))) { delete T; return rc; }
-  const size_t band_smem = sizeof(double) * (size_t)T->max_piece;
+  const size_t band_smem = torn_solve_smem(T);
   if (band_smem > 48 * 1024) cudaFuncSetAttribute(k_tl_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
   if (cudaStreamCreateWithFlags(&T->own, cudaStreamNonBlocking) != cudaSuccess ||
       cublasCreate(&T->blas) != CUBLAS_STATUS_SUCCESS) {
