@@ -309,16 +309,17 @@ __global__ void __launch_bounds__(256) k_tl_band_lu(const PieceD* pcs, int64_t V
 
 // Solve of every piece of the selected variants: out = cs . Ab^-1 (rs . (b - P.w)),
 // with the subtraction only when w is given (the second solve of the apply).
-// The band is swept column by column, each column a barrier apart; the columns
-// are staged into shared memory KS_TORN_CH at a time with asynchronous copies,
-// the next block of columns in flight while the current one is applied, so the
-// sweep waits on barriers, not on memory.  ldab is even (16-byte aligned columns).
-#define KS_TORN_CH 16
-__global__ void __launch_bounds__(512) k_tl_band_solve(const PieceD* pcs, int64_t V, int64_t band_stride,
-                                                       const double* band, int64_t piv_stride, const int32_t* piv_all,
-                                                       const int32_t* pidx, const double* rs, const double* cs,
-                                                       const double* b, const int32_t* row_a, const double* w,
-                                                       double* out, const uint8_t* mask, int max_n, int max_ldab) {
+// One warp per (variant, piece): the band is swept column by column with warp
+// barriers only (a column step is a few shared-memory accesses and one
+// multiply-add per lane), and the columns are staged into shared memory
+// KS_TORN_CH at a time with asynchronous copies, the next block in flight while
+// the current one is applied.  ldab is even, so every column is 16-byte aligned.
+#define KS_TORN_CH 8
+__global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t V, int64_t band_stride,
+                                                      const double* band, int64_t piv_stride, const int32_t* piv_all,
+                                                      const int32_t* pidx, const double* rs, const double* cs,
+                                                      const double* b, const int32_t* row_a, const double* w,
+                                                      double* out, const uint8_t* mask, int max_n, int max_ldab) {
   extern __shared__ __align__(16) double smem[];
   const int v = blockIdx.x % V, p = blockIdx.x / V;
   if (!mask[v]) return;
@@ -326,12 +327,12 @@ __global__ void __launch_bounds__(512) k_tl_band_solve(const PieceD* pcs, int64_
   const double* AB = band + (int64_t)v * band_stride + pc.band_off;
   const int32_t* piv = piv_all + (int64_t)v * piv_stride + pc.idx_off;
   const int n = pc.n, kl = pc.kl, ldab = pc.ldab, kv = pc.kl + pc.ku;
-  const int t = threadIdx.x, T = blockDim.x;
-  double* y = smem;                                                // [max_n], rounded to 2
-  double* buf = smem + ((max_n + 1) & ~1);                          // [2][KS_TORN_CH][max_ldab]
-  __shared__ int spiv[2][KS_TORN_CH];
+  const int t = threadIdx.x;
+  double* y = smem;                                // [max_n], rounded to 2
+  double* buf = smem + ((max_n + 1) & ~1);         // [2][KS_TORN_CH][max_ldab]
+  int* spiv = reinterpret_cast<int*>(buf + 2 * KS_TORN_CH * max_ldab);  // [2][KS_TORN_CH]
   const int bufsz = KS_TORN_CH * max_ldab;
-  for (int i = t; i < n; i += T) {
+  for (int i = t; i < n; i += 32) {
     const int g = pidx[pc.idx_off + i];
     double bi = b[(int64_t)g * V + v];
     if (w) {
@@ -341,69 +342,62 @@ __global__ void __launch_bounds__(512) k_tl_band_solve(const PieceD* pcs, int64_
     y[i] = bi * rs[(int64_t)g * V + v];
   }
   const int nch = (n + KS_TORN_CH - 1) / KS_TORN_CH;
-  // stage block c (columns c*CH ..) into buffer c & 1
-  auto stage = [&](int c) {
-    const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
-    const int units = cols * ldab / 2;
-    const double* src = AB + (int64_t)j0 * ldab;
-    double* dst = buf + (c & 1) * bufsz;
-    for (int u = t; u < units; u += T) __pipeline_memcpy_async(dst + 2 * u, src + 2 * u, 16);
-    __pipeline_commit();
-    if (t < cols) spiv[c & 1][t] = piv[j0 + t];
-  };
-  // L: row interchanges and the unit lower band
-  stage(0);
-  for (int c = 0; c < nch; c++) {
-    if (c + 1 < nch) stage(c + 1); else __pipeline_commit();
-    __pipeline_wait_prior(1);
-    __syncthreads();
-    const double* B = buf + (c & 1) * bufsz;
-    const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
-    for (int jj = 0; jj < cols; jj++) {
-      const int j = j0 + jj;
-      const int km = min(kl, n - 1 - j);
-      const int pj = spiv[c & 1][jj];
-      if (pj != j) {  // the same for every thread
-        if (t == 0) { const double tmp = y[j]; y[j] = y[pj]; y[pj] = tmp; }
-        __syncthreads();
-      }
-      const double yj = y[j];
-      for (int o = t; o < km; o += T) y[j + 1 + o] -= B[kv + 1 + o + jj * ldab] * yj;
-      __syncthreads();
-    }
-  }
-  // U: column j holds rows j-kv .. j (row j - kv + o at offset o, the diagonal at kv)
-  __pipeline_wait_prior(0);
-  __syncthreads();
-  auto stage_back = [&](int c, int slot) {
+  auto stage = [&](int c, int slot, bool pivots) {
     const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
     const int units = cols * ldab / 2;
     const double* src = AB + (int64_t)j0 * ldab;
     double* dst = buf + slot * bufsz;
-    for (int u = t; u < units; u += T) __pipeline_memcpy_async(dst + 2 * u, src + 2 * u, 16);
+    for (int u = t; u < units; u += 32) __pipeline_memcpy_async(dst + 2 * u, src + 2 * u, 16);
     __pipeline_commit();
+    if (pivots && t < cols) spiv[slot * KS_TORN_CH + t] = piv[j0 + t];
   };
-  stage_back(nch - 1, 0);
-  for (int c = nch - 1, k = 0; c >= 0; c--, k++) {
-    if (c > 0) stage_back(c - 1, (k + 1) & 1); else __pipeline_commit();
+  // L: row interchanges and the unit lower band
+  stage(0, 0, true);
+  for (int c = 0; c < nch; c++) {
+    if (c + 1 < nch) stage(c + 1, (c + 1) & 1, true); else __pipeline_commit();
     __pipeline_wait_prior(1);
-    __syncthreads();
+    __syncwarp();
+    const double* B = buf + (c & 1) * bufsz;
+    const int* P = spiv + (c & 1) * KS_TORN_CH;
+    const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
+    for (int jj = 0; jj < cols; jj++) {
+      const int j = j0 + jj;
+      const int km = min(kl, n - 1 - j);
+      const int pj = P[jj];
+      if (pj != j) {  // the same for every lane
+        if (t == 0) { const double tmp = y[j]; y[j] = y[pj]; y[pj] = tmp; }
+        __syncwarp();
+      }
+      const double yj = y[j];
+      for (int o = t; o < km; o += 32) y[j + 1 + o] -= B[kv + 1 + o + jj * ldab] * yj;
+      __syncwarp();
+    }
+  }
+  __pipeline_wait_prior(0);
+  __syncwarp();
+  // U: column j holds rows j-kv .. j (row j - kv + o at offset o, the diagonal at kv)
+  stage(nch - 1, 0, false);
+  for (int c = nch - 1, k = 0; c >= 0; c--, k++) {
+    if (c > 0) stage(c - 1, (k + 1) & 1, false); else __pipeline_commit();
+    __pipeline_wait_prior(1);
+    __syncwarp();
     const double* B = buf + (k & 1) * bufsz;
     const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
     for (int jj = cols - 1; jj >= 0; jj--) {
       const int j = j0 + jj;
       const double yj = y[j] / B[kv + jj * ldab];
-      __syncthreads();
+      __syncwarp();
       if (t == 0) y[j] = yj;
-      for (int o = t; o < kv; o += T) {
+      for (int o = t; o < kv; o += 32) {
         const int i = j - kv + o;
         if (i >= 0) y[i] -= B[o + jj * ldab] * yj;
       }
-      __syncthreads();
+      __syncwarp();
     }
   }
   __pipeline_wait_prior(0);
-  for (int i = t; i < n; i += T) {
+  __syncwarp();
+  for (int i = t; i < n; i += 32) {
     const int g = pidx[pc.idx_off + i];
     out[(int64_t)g * V + v] = y[i] * cs[(int64_t)g * V + v];
   }
@@ -842,7 +836,7 @@ void stamp_pattern(const ksh::HostPlan& hp, std::vector<std::vector<int>>& rows)
 
 size_t torn_solve_smem(const ks_torn* T) {
   return sizeof(double) * (((size_t)T->max_piece + 1) & ~(size_t)1) +
-         sizeof(double) * 2 * (size_t)KS_TORN_CH * (size_t)T->max_ldab;
+         sizeof(double) * 2 * (size_t)KS_TORN_CH * (size_t)T->max_ldab + sizeof(int) * 2 * KS_TORN_CH;
 }
 
 int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_torn, std::string* err) {
@@ -997,7 +991,7 @@ int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_t
     if (d.n > 12000) { *err = "ks_torn: a piece of " + std::to_string(d.n) + " unknowns (the band solve holds at most 12,000)"; return KS_EUNSUPPORTED; }
   }
   T->band_stride = band; T->piv_stride = n; T->wc_stride = wc; T->y_stride = y;
-  T->solve_threads = std::min(256, std::max(64, (T->max_band + 31) / 32 * 32));
+  T->solve_threads = 32;
   if (torn_solve_smem(T) > 227 * 1024) {
     *err = "ks_torn: a piece of " + std::to_string(T->max_piece) + " unknowns with a band of " +
            std::to_string(T->max_band) + " does not fit the band solve's shared memory";
