@@ -445,10 +445,11 @@ int ks_mlp_train(ks_mlp* m, ks_batch* b, const double* x_dev, const int32_t* idx
  * without a bound); reuse = 0 refactors at every solve.  Errors per variant as
  * ks_status; a solve that is not accepted after a fresh refactor ends that
  * variant with KS_STATUS_SINGULAR (the reference would fall back to an untorn
- * LU of the whole system).  stats [10]: solves, refactors, refinement steps,
+ * LU of the whole system).  stats [14]: solves, refactors, refinement steps,
  * most refinement steps of one solve, solves not accepted, pieces, coupling
  * rows, largest band (kl + ku), band-factor doubles per variant, kernel
- * launches of the call.
+ * launches of the call, then the device time (microseconds, CUDA events) of
+ * the refactors, the applications of the factors, the loads and the residuals.
  */
 typedef struct ks_torn ks_torn;
 int ks_torn_create(const ks_topology* topo, int32_t n_variants, const double* values, const int32_t* torn_elems,

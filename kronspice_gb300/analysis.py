@@ -331,7 +331,7 @@ class MultiBatch:
 
 
 TORN_STATS = ("solves", "refactors", "refines", "max_passes", "not_accepted", "pieces", "coupling_rows", "max_band",
-              "band_doubles", "launches")
+              "band_doubles", "launches", "refactor_us", "apply_us", "load_us", "residual_us")
 
 
 class TornBatch:
@@ -366,7 +366,7 @@ class TornBatch:
         x = np.zeros((self.n_var, self.n))
         st = np.zeros(self.n_var, dtype=np.int32)
         it = np.zeros(self.n_var, dtype=np.int32)
-        stats = np.zeros(10, dtype=np.int64)
+        stats = np.zeros(14, dtype=np.int64)
         _check(_lib.load().ks_torn_op(self.handle, ctypes.byref(o), int(reuse), x.ctypes.data, st.ctypes.data,
                                       it.ctypes.data, stats.ctypes.data), "ks_torn_op")
         return x, st, it, dict(zip(TORN_STATS, stats.tolist()))
@@ -383,7 +383,7 @@ class TornBatch:
         st = np.zeros(self.n_var, dtype=np.int32)
         steps = np.zeros(self.n_var, dtype=np.int32)
         it = np.zeros(self.n_var, dtype=np.int32)
-        stats = np.zeros(10, dtype=np.int64)
+        stats = np.zeros(14, dtype=np.int64)
         _check(_lib.load().ks_torn_tran(self.handle, ctypes.byref(sp), ctypes.byref(o), int(reuse),
                                         pr.ctypes.data if len(pr) else None, len(pr),
                                         wave.ctypes.data if len(pr) else None, x.ctypes.data, st.ctypes.data,

@@ -599,34 +599,39 @@ __global__ void k_tl_gemm_ptrs(int count, const int32_t* list, double* IC, int R
 }
 
 // w = IC^-1 h with the factors (getrs: interchanges, unit lower, upper), one CTA
-// per variant, by panels of 32 columns: the small triangle of a panel column by
-// column, then the rest of the vector updated by the panel as one matrix-vector
-// product (coalesced column reads by all threads).
+// per variant, by panels of 32 columns: warp 0 solves a panel's small triangle
+// with warp barriers, then every thread updates the rest of the vector by the
+// panel as one matrix-vector product (coalesced column reads).
 __global__ void __launch_bounds__(1024) k_tl_ic_solve(int R, int64_t V, const double* IC, const int32_t* ipiv,
                                                       const double* h, double* w, const uint8_t* mask) {
-  extern __shared__ double y[];
+  extern __shared__ double y[];  // [R] then the pivots [R]
   const int v = blockIdx.x;
   if (!mask[v]) return;
+  int* sp = reinterpret_cast<int*>(y + R);
   const double* A = IC + (int64_t)v * R * R;
   const int32_t* piv = ipiv + (int64_t)v * R;
-  const int t = threadIdx.x, T = blockDim.x;
+  const int t = threadIdx.x, T = blockDim.x, lane = t & 31;
   constexpr int NB = 32;
-  for (int i = t; i < R; i += T) y[i] = h[(int64_t)i * V + v];
+  for (int i = t; i < R; i += T) { y[i] = h[(int64_t)i * V + v]; sp[i] = piv[i]; }
   __syncthreads();
   if (t == 0)
     for (int j = 0; j < R; j++) {
-      const int p = piv[j];
+      const int p = sp[j];
       if (p != j) { const double tmp = y[j]; y[j] = y[p]; y[p] = tmp; }
     }
   __syncthreads();
   for (int k0 = 0; k0 < R; k0 += NB) {
     const int k1 = min(k0 + NB, R);
-    for (int j = k0; j < k1; j++) {  // unit lower triangle of the panel
-      const double yj = y[j];
-      const int i = j + 1 + t;
-      if (i < k1) y[i] -= A[i + (int64_t)j * R] * yj;
-      __syncthreads();
+    if (t < 32) {  // unit lower triangle of the panel: lane l owns row k0 + l
+      const int i = k0 + lane;
+      double yi = i < k1 ? y[i] : 0.0;
+      for (int j = k0; j < k1; j++) {
+        const double yj = __shfl_sync(0xffffffffu, yi, j - k0);
+        if (i > j && i < k1) yi -= A[i + (int64_t)j * R] * yj;
+      }
+      if (i < k1) y[i] = yi;
     }
+    __syncthreads();
     for (int i = k1 + t; i < R; i += T) {  // the rows below: y_i -= L(i, k0:k1) . y(k0:k1)
       double s = 0;
       for (int j = k0; j < k1; j++) s += A[i + (int64_t)j * R] * y[j];
@@ -636,14 +641,17 @@ __global__ void __launch_bounds__(1024) k_tl_ic_solve(int R, int64_t V, const do
   }
   for (int k1 = R; k1 > 0; k1 -= NB) {
     const int k0 = max(0, k1 - NB);
-    for (int j = k1 - 1; j >= k0; j--) {  // upper triangle of the panel
-      const double yj = y[j] / A[j + (int64_t)j * R];
-      __syncthreads();
-      if (t == 0) y[j] = yj;
-      const int i = k0 + t;
-      if (i < j) y[i] -= A[i + (int64_t)j * R] * yj;
-      __syncthreads();
+    if (t < 32) {  // upper triangle of the panel
+      const int i = k0 + lane;
+      double yi = i < k1 ? y[i] : 0.0;
+      for (int j = k1 - 1; j >= k0; j--) {
+        if (i == j) yi /= A[j + (int64_t)j * R];
+        const double yj = __shfl_sync(0xffffffffu, yi, j - k0);
+        if (i < j) yi -= A[i + (int64_t)j * R] * yj;
+      }
+      if (i < k1) y[i] = yi;
     }
+    __syncthreads();
     for (int i = t; i < k0; i += T) {  // the rows above: y_i -= U(i, k0:k1) . y(k0:k1)
       double s = 0;
       for (int j = k0; j < k1; j++) s += A[i + (int64_t)j * R] * y[j];
@@ -793,6 +801,33 @@ struct ks_torn {
   std::vector<uint8_t> have;  // factors exist, per variant
   // counters
   int64_t solves = 0, refactors = 0, refines = 0, max_passes = 0, failed = 0, launches = 0;
+  // device time per phase (refactor, apply, load, residual): event pairs summed at the end of a call
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+  double phase_ms[4] = {0, 0, 0, 0};
+  cudaEvent_t ev() {
+    if (ev_used == ev_pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_used++];
+  }
+  void mark_begin(int ph, cudaEvent_t* b) { *b = ev(); cudaEventRecord(*b, st); (void)ph; }
+  void mark_end(int ph, cudaEvent_t b) {
+    cudaEvent_t e = ev();
+    cudaEventRecord(e, st);
+    marks.push_back({ph, {b, e}});
+  }
+  void collect() {  // after a stream synchronisation
+    for (auto& m : marks) {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, m.second.first, m.second.second) == cudaSuccess) phase_ms[m.first] += ms;
+    }
+    marks.clear();
+    ev_used = 0;
+  }
   KPlan view() const {
     KPlan p;
     p.n = hp.n; p.n_elem = hp.n_elem; p.n_values = hp.n_values; p.n_derived = hp.n_derived;
@@ -801,6 +836,7 @@ struct ks_torn {
     return p;
   }
   ~ks_torn() {
+    for (auto e : ev_pool) cudaEventDestroy(e);
     if (blas) cublasDestroy(blas);
     for (void* p : owned) cudaFree(p);
     if (own) cudaStreamDestroy(own);
@@ -1076,6 +1112,8 @@ int refactor(ks_torn* T, const std::vector<int32_t>& list) {
   cudaStream_t s = T->st;
   if (list.empty()) return KS_OK;
   T->refactors++;
+  cudaEvent_t e0;
+  T->mark_begin(0, &e0);
   std::vector<uint8_t> m(V, 0);
   for (int v : list) m[v] = 1;
   int rc = set_mask(T, m);
@@ -1127,12 +1165,23 @@ int refactor(ks_torn* T, const std::vector<int32_t>& list) {
     }
   }
   if (ck(cudaGetLastError(), "refactor launch")) return KS_ECUDA;
+  T->mark_end(0, e0);
   for (int v : list) T->have[v] = 1;
   return KS_OK;
 }
 
+int apply_(ks_torn* T, const double* b, double* out);
+
 // out = M^-1 b with the current factors, for the masked variants.
 int apply(ks_torn* T, const double* b, double* out) {
+  cudaEvent_t e0;
+  T->mark_begin(1, &e0);
+  int rc = apply_(T, b, out);
+  T->mark_end(1, e0);
+  return rc;
+}
+
+int apply_(ks_torn* T, const double* b, double* out) {
   const int64_t V = T->V;
   const int R = T->R;
   cudaStream_t s = T->st;
@@ -1151,7 +1200,7 @@ int apply(ks_torn* T, const double* b, double* out) {
   T->launches++;
   k_tl_h<<<blocks_for((int64_t)R * V, 256), 256, 0, s>>>(R, V, T->d_offp, T->d_offs, T->d_ci, T->J, T->z, T->h, T->mask);
   T->launches++;
-  k_tl_ic_solve<<<(unsigned)V, 1024, sizeof(double) * R, s>>>(R, V, T->IC, T->icpiv, T->h, T->w, T->mask);
+  k_tl_ic_solve<<<(unsigned)V, 1024, (sizeof(double) + sizeof(int)) * R, s>>>(R, V, T->IC, T->icpiv, T->h, T->w, T->mask);
   T->launches++;
   k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
                                         T->cs, b, T->d_row_a, T->w, out, T->mask, T->max_piece, T->max_ldab);
@@ -1182,12 +1231,16 @@ int torn_solve(ks_torn* T, const std::vector<uint8_t>& want, bool reuse, std::ve
     for (;; pass++) {
       if ((rc = set_mask(T, refine))) return rc;
       if ((rc = ck(cudaMemsetAsync(T->berr, 0, sizeof(unsigned long long) * V, s), "memset"))) return rc;
+      cudaEvent_t e0;
+      T->mark_begin(3, &e0);
       T->launches++;
       k_tl_resid<<<blocks_for(n * V, 256), 256, 0, s>>>((int)n, V, T->d_rp, T->d_ci, T->J, T->rhs, T->x, T->r, T->berr,
                                                         T->mask);
+      T->mark_end(3, e0);
       if ((rc = ck(cudaMemcpyAsync(be.data(), T->berr, sizeof(unsigned long long) * V, cudaMemcpyDeviceToHost, s), "berr")))
         return rc;
       if ((rc = ck(cudaStreamSynchronize(s), "sync"))) return rc;
+      T->collect();
       bool any = false;
       for (int64_t v = 0; v < V; v++) {
         if (!refine[v]) continue;
@@ -1246,9 +1299,12 @@ int newton(ks_torn* T, LoadParams lp, const KOpts& o, int max_iter, bool reuse, 
         (rc = ck(cudaMemsetAsync(T->rhs, 0, sizeof(double) * n * V, s), "memset")))
       return rc;
     lp.initJct = initJct;
+    cudaEvent_t e0;
+    T->mark_begin(2, &e0);
     T->launches++;
     k_tl_load<<<blocks_for((int64_t)plan.n_elem * V, 256), 256, 0, s>>>(plan, T->values, T->derived, T->state, V, T->d_rp,
                                                                          T->d_ci, T->J, T->rhs, T->x, T->xo, lp, T->mask);
+    T->mark_end(2, e0);
     std::vector<uint8_t> ok;
     if ((rc = torn_solve(T, live, reuse, &ok))) return rc;
     for (int64_t v = 0; v < V; v++) {
@@ -1347,6 +1403,7 @@ void stats_out(const ks_torn* T, int64_t* s) {
   if (!s) return;
   s[0] = T->solves; s[1] = T->refactors; s[2] = T->refines; s[3] = T->max_passes; s[4] = T->failed;
   s[5] = T->P; s[6] = T->R; s[7] = T->max_band; s[8] = T->band_stride; s[9] = T->launches;
+  for (int k = 0; k < 4; k++) s[10 + k] = (int64_t)(T->phase_ms[k] * 1000.0);  // microseconds
 }
 
 int fresh_state(ks_torn* T, double step, double stop) {
@@ -1362,6 +1419,9 @@ int fresh_state(ks_torn* T, double step, double stop) {
   if (ck(cudaMemsetAsync(T->x, 0, sizeof(double) * T->n * V, T->st), "memset")) return KS_ECUDA;
   T->solves = T->refactors = T->refines = T->max_passes = T->failed = 0;
   T->launches = 3;
+  for (double& m : T->phase_ms) m = 0;
+  T->marks.clear();
+  T->ev_used = 0;
   T->have.assign(T->V, 0);
   return ck(cudaGetLastError(), "init");
 }
@@ -1379,11 +1439,16 @@ int accept_all_variants(ks_torn* T, const std::vector<int32_t>& status, double t
 }
 
 int x_out(ks_torn* T, double* out) {  // [V][n] from [n][V]
-  if (!out) return KS_OK;
+  if (!out) {
+    if (ck(cudaStreamSynchronize(T->st), "sync")) return KS_ECUDA;
+    T->collect();
+    return KS_OK;
+  }
   std::vector<double> h((size_t)T->n * T->V);
   if (ck(cudaMemcpyAsync(h.data(), T->x, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, T->st), "x") ||
       ck(cudaStreamSynchronize(T->st), "sync"))
     return KS_ECUDA;
+  T->collect();
   for (int64_t v = 0; v < T->V; v++)
     for (int i = 0; i < T->n; i++) out[(size_t)v * T->n + i] = h[(size_t)i * T->V + v];
   return KS_OK;
