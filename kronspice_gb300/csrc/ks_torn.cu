@@ -1353,6 +1353,8 @@ extern "C" int ks_torn_create(const ks_topology* topo, int32_t n_variants, const
   rc = build_plan(T, topo, torn_elems, n_torn, &err);
   if (rc) { set_error(err); delete T; return rc; }
   if ((rc = alloc_numeric(T))) { delete T; return rc; }
+  const size_t ic_smem = (sizeof(double) + sizeof(int)) * (size_t)T->R;
+  if (ic_smem > 48 * 1024) cudaFuncSetAttribute(k_tl_ic_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ic_smem);
   const size_t band_smem = torn_solve_smem(T);
   if (band_smem > 48 * 1024) cudaFuncSetAttribute(k_tl_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
   if (cudaStreamCreateWithFlags(&T->own, cudaStreamNonBlocking) != cudaSuccess ||
