@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(256) k_tl_band_lu(const PieceD* pcs, int64_t V
 // multiply-add per lane), and the columns are staged into shared memory
 // KS_TORN_CH at a time with asynchronous copies, the next block in flight while
 // the current one is applied.  ldab is even, so every column is 16-byte aligned.
-#define KS_TORN_CH 8
+#define KS_TORN_CH 4
 __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t V, int64_t band_stride,
                                                       const double* band, int64_t piv_stride, const int32_t* piv_all,
                                                       const int32_t* pidx, const double* rs, const double* cs,
@@ -369,7 +369,22 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
         __syncwarp();
       }
       const double yj = y[j];
-      for (int o = t; o < km; o += 32) y[j + 1 + o] -= B[kv + 1 + o + jj * ldab] * yj;
+      if (kl <= 128) {  // up to 4 rows a lane: loads first, then the updates (independent)
+        double lv[4], yv[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+          const int o = t + 32 * r;
+          lv[r] = o < km ? B[kv + 1 + o + jj * ldab] : 0.0;
+          yv[r] = o < km ? y[j + 1 + o] : 0.0;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+          const int o = t + 32 * r;
+          if (o < km) y[j + 1 + o] = yv[r] - lv[r] * yj;
+        }
+      } else {
+        for (int o = t; o < km; o += 32) y[j + 1 + o] -= B[kv + 1 + o + jj * ldab] * yj;
+      }
       __syncwarp();
     }
   }
@@ -388,9 +403,25 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
       const double yj = y[j] / B[kv + jj * ldab];
       __syncwarp();
       if (t == 0) y[j] = yj;
-      for (int o = t; o < kv; o += 32) {
-        const int i = j - kv + o;
-        if (i >= 0) y[i] -= B[o + jj * ldab] * yj;
+      if (kv <= 256) {  // up to 8 rows a lane: loads first, then the updates
+        double uv[8], yv[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+          const int o = t + 32 * r, i = j - kv + o;
+          const bool on = o < kv && i >= 0;
+          uv[r] = on ? B[o + jj * ldab] : 0.0;
+          yv[r] = on ? y[i] : 0.0;
+        }
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+          const int o = t + 32 * r, i = j - kv + o;
+          if (o < kv && i >= 0) y[i] = yv[r] - uv[r] * yj;
+        }
+      } else {
+        for (int o = t; o < kv; o += 32) {
+          const int i = j - kv + o;
+          if (i >= 0) y[i] -= B[o + jj * ldab] * yj;
+        }
       }
       __syncwarp();
     }
@@ -1144,7 +1175,7 @@ int refactor(ks_torn* T, const std::vector<int32_t>& list) {
     if (ck(cudaMemcpyAsync(T->list, list.data(), sizeof(int32_t) * list.size(), cudaMemcpyHostToDevice, s), "list"))
       return KS_ECUDA;
     const int count = (int)list.size();
-    const int nb = 32;
+    const int nb = 64;
     const double one = 1.0, minus = -1.0;
     cublasSetStream(T->blas, s);
     for (int k0 = 0; k0 < R; k0 += nb) {
