@@ -311,15 +311,18 @@ __global__ void __launch_bounds__(256) k_tl_band_lu(const PieceD* pcs, int64_t V
 // with the subtraction only when w is given (the second solve of the apply).
 // One warp per (variant, piece): the band is swept column by column with warp
 // barriers only (a column step is a few shared-memory accesses and one
-// multiply-add per lane), and the columns are staged into shared memory
-// KS_TORN_CH at a time with asynchronous copies, the next block in flight while
-// the current one is applied.  ldab is even, so every column is 16-byte aligned.
+// multiply-add per row a lane owns).  The part of each column a sweep reads (the
+// kl multipliers below the diagonal going down, the kl + ku entries above it
+// and the diagonal coming back) is staged into shared memory KS_TORN_CH columns
+// at a time with asynchronous copies, KS_TORN_NBUF - 1 blocks ahead, so the
+// sweep waits on barriers, not on memory.
 #define KS_TORN_CH 4
+#define KS_TORN_NBUF 4
 __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t V, int64_t band_stride,
                                                       const double* band, int64_t piv_stride, const int32_t* piv_all,
                                                       const int32_t* pidx, const double* rs, const double* cs,
                                                       const double* b, const int32_t* row_a, const double* w,
-                                                      double* out, const uint8_t* mask, int max_n, int max_ldab) {
+                                                      double* out, const uint8_t* mask, int max_n, int max_colw) {
   extern __shared__ __align__(16) double smem[];
   const int v = blockIdx.x % V, p = blockIdx.x / V;
   if (!mask[v]) return;
@@ -328,10 +331,10 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
   const int32_t* piv = piv_all + (int64_t)v * piv_stride + pc.idx_off;
   const int n = pc.n, kl = pc.kl, ldab = pc.ldab, kv = pc.kl + pc.ku;
   const int t = threadIdx.x;
-  double* y = smem;                                // [max_n], rounded to 2
-  double* buf = smem + ((max_n + 1) & ~1);         // [2][KS_TORN_CH][max_ldab]
-  int* spiv = reinterpret_cast<int*>(buf + 2 * KS_TORN_CH * max_ldab);  // [2][KS_TORN_CH]
-  const int bufsz = KS_TORN_CH * max_ldab;
+  double* y = smem;                                 // [max_n], rounded to 2
+  double* buf = smem + ((max_n + 1) & ~1);          // [NBUF][CH][max_colw]
+  int* spiv = reinterpret_cast<int*>(buf + KS_TORN_NBUF * KS_TORN_CH * max_colw);  // [NBUF][CH]
+  const int bufsz = KS_TORN_CH * max_colw;
   for (int i = t; i < n; i += 32) {
     const int g = pidx[pc.idx_off + i];
     double bi = b[(int64_t)g * V + v];
@@ -342,23 +345,26 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
     y[i] = bi * rs[(int64_t)g * V + v];
   }
   const int nch = (n + KS_TORN_CH - 1) / KS_TORN_CH;
-  auto stage = [&](int c, int slot, bool pivots) {
+  // stage block c: `width` doubles of each column from row offset `first`
+  auto stage = [&](int c, int first, int width, bool pivots) {
+    if (c < 0 || c >= nch) { __pipeline_commit(); return; }
     const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
-    const int units = cols * ldab / 2;
-    const double* src = AB + (int64_t)j0 * ldab;
-    double* dst = buf + slot * bufsz;
-    for (int u = t; u < units; u += 32) __pipeline_memcpy_async(dst + 2 * u, src + 2 * u, 16);
+    double* dst = buf + (c % KS_TORN_NBUF) * bufsz;
+    for (int u = t; u < cols * width; u += 32) {
+      const int jj = u / width, r = u - jj * width;
+      __pipeline_memcpy_async(dst + jj * max_colw + r, AB + first + r + (int64_t)(j0 + jj) * ldab, 8);
+    }
     __pipeline_commit();
-    if (pivots && t < cols) spiv[slot * KS_TORN_CH + t] = piv[j0 + t];
+    if (pivots && t < cols) spiv[(c % KS_TORN_NBUF) * KS_TORN_CH + t] = piv[j0 + t];
   };
-  // L: row interchanges and the unit lower band
-  stage(0, 0, true);
+  // L: row interchanges and the unit lower band (staged: rows kv+1 .. kv+kl of each column)
+  for (int c = 0; c < KS_TORN_NBUF - 1; c++) stage(c, kv + 1, kl, true);
   for (int c = 0; c < nch; c++) {
-    if (c + 1 < nch) stage(c + 1, (c + 1) & 1, true); else __pipeline_commit();
-    __pipeline_wait_prior(1);
+    stage(c + KS_TORN_NBUF - 1, kv + 1, kl, true);
+    __pipeline_wait_prior(KS_TORN_NBUF - 1);
     __syncwarp();
-    const double* B = buf + (c & 1) * bufsz;
-    const int* P = spiv + (c & 1) * KS_TORN_CH;
+    const double* B = buf + (c % KS_TORN_NBUF) * bufsz;
+    const int* P = spiv + (c % KS_TORN_NBUF) * KS_TORN_CH;
     const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
     for (int jj = 0; jj < cols; jj++) {
       const int j = j0 + jj;
@@ -374,7 +380,7 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
 #pragma unroll
         for (int r = 0; r < 4; r++) {
           const int o = t + 32 * r;
-          lv[r] = o < km ? B[kv + 1 + o + jj * ldab] : 0.0;
+          lv[r] = o < km ? B[jj * max_colw + o] : 0.0;
           yv[r] = o < km ? y[j + 1 + o] : 0.0;
         }
 #pragma unroll
@@ -383,24 +389,24 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
           if (o < km) y[j + 1 + o] = yv[r] - lv[r] * yj;
         }
       } else {
-        for (int o = t; o < km; o += 32) y[j + 1 + o] -= B[kv + 1 + o + jj * ldab] * yj;
+        for (int o = t; o < km; o += 32) y[j + 1 + o] -= B[jj * max_colw + o] * yj;
       }
       __syncwarp();
     }
   }
   __pipeline_wait_prior(0);
   __syncwarp();
-  // U: column j holds rows j-kv .. j (row j - kv + o at offset o, the diagonal at kv)
-  stage(nch - 1, 0, false);
-  for (int c = nch - 1, k = 0; c >= 0; c--, k++) {
-    if (c > 0) stage(c - 1, (k + 1) & 1, false); else __pipeline_commit();
-    __pipeline_wait_prior(1);
+  // U: rows 0 .. kv of each column (row j - kv + o at o, the diagonal at kv), last block first
+  for (int k = 0; k < KS_TORN_NBUF - 1; k++) stage(nch - 1 - k, 0, kv + 1, false);
+  for (int c = nch - 1; c >= 0; c--) {
+    stage(c - (KS_TORN_NBUF - 1), 0, kv + 1, false);
+    __pipeline_wait_prior(KS_TORN_NBUF - 1);
     __syncwarp();
-    const double* B = buf + (k & 1) * bufsz;
+    const double* B = buf + (c % KS_TORN_NBUF) * bufsz;
     const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
     for (int jj = cols - 1; jj >= 0; jj--) {
       const int j = j0 + jj;
-      const double yj = y[j] / B[kv + jj * ldab];
+      const double yj = y[j] / B[jj * max_colw + kv];
       __syncwarp();
       if (t == 0) y[j] = yj;
       if (kv <= 256) {  // up to 8 rows a lane: loads first, then the updates
@@ -409,7 +415,7 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
         for (int r = 0; r < 8; r++) {
           const int o = t + 32 * r, i = j - kv + o;
           const bool on = o < kv && i >= 0;
-          uv[r] = on ? B[o + jj * ldab] : 0.0;
+          uv[r] = on ? B[jj * max_colw + o] : 0.0;
           yv[r] = on ? y[i] : 0.0;
         }
 #pragma unroll
@@ -420,7 +426,7 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
       } else {
         for (int o = t; o < kv; o += 32) {
           const int i = j - kv + o;
-          if (i >= 0) y[i] -= B[o + jj * ldab] * yj;
+          if (i >= 0) y[i] -= B[jj * max_colw + o] * yj;
         }
       }
       __syncwarp();
@@ -633,7 +639,7 @@ __global__ void k_tl_gemm_ptrs(int count, const int32_t* list, double* IC, int R
 // per variant, by panels of 32 columns: warp 0 solves a panel's small triangle
 // with warp barriers, then every thread updates the rest of the vector by the
 // panel as one matrix-vector product (coalesced column reads).
-__global__ void __launch_bounds__(1024) k_tl_ic_solve(int R, int64_t V, const double* IC, const int32_t* ipiv,
+__global__ void __launch_bounds__(512) k_tl_ic_solve(int R, int64_t V, const double* IC, const int32_t* ipiv,
                                                       const double* h, double* w, const uint8_t* mask) {
   extern __shared__ double y[];  // [R] then the pivots [R]
   const int v = blockIdx.x;
@@ -653,12 +659,15 @@ __global__ void __launch_bounds__(1024) k_tl_ic_solve(int R, int64_t V, const do
   __syncthreads();
   for (int k0 = 0; k0 < R; k0 += NB) {
     const int k1 = min(k0 + NB, R);
-    if (t < 32) {  // unit lower triangle of the panel: lane l owns row k0 + l
+    if (t < 32) {  // unit lower triangle of the panel: lane l owns row k0 + l (its row loaded first)
       const int i = k0 + lane;
-      double yi = i < k1 ? y[i] : 0.0;
-      for (int j = k0; j < k1; j++) {
-        const double yj = __shfl_sync(0xffffffffu, yi, j - k0);
-        if (i > j && i < k1) yi -= A[i + (int64_t)j * R] * yj;
+      double yi = i < k1 ? y[i] : 0.0, a[NB];
+#pragma unroll
+      for (int q = 0; q < NB; q++) a[q] = (i < k1 && k0 + q < i) ? A[i + (int64_t)(k0 + q) * R] : 0.0;
+#pragma unroll
+      for (int q = 0; q < NB; q++) {
+        const double yj = __shfl_sync(0xffffffffu, yi, q);
+        if (k0 + q < k1) yi -= a[q] * yj;
       }
       if (i < k1) y[i] = yi;
     }
@@ -672,13 +681,17 @@ __global__ void __launch_bounds__(1024) k_tl_ic_solve(int R, int64_t V, const do
   }
   for (int k1 = R; k1 > 0; k1 -= NB) {
     const int k0 = max(0, k1 - NB);
-    if (t < 32) {  // upper triangle of the panel
+    if (t < 32) {  // upper triangle of the panel (the lane's row and diagonal loaded first)
       const int i = k0 + lane;
-      double yi = i < k1 ? y[i] : 0.0;
-      for (int j = k1 - 1; j >= k0; j--) {
-        if (i == j) yi /= A[j + (int64_t)j * R];
-        const double yj = __shfl_sync(0xffffffffu, yi, j - k0);
-        if (i < j) yi -= A[i + (int64_t)j * R] * yj;
+      double yi = i < k1 ? y[i] : 0.0, a[NB];
+#pragma unroll
+      for (int q = 0; q < NB; q++) a[q] = (i < k1 && k0 + q >= i && k0 + q < k1) ? A[i + (int64_t)(k0 + q) * R] : 0.0;
+#pragma unroll
+      for (int q = NB - 1; q >= 0; q--) {
+        if (k0 + q >= k1) continue;
+        if (lane == q) yi /= a[q];
+        const double yj = __shfl_sync(0xffffffffu, yi, q);
+        if (lane < q) yi -= a[q] * yj;
       }
       if (i < k1) y[i] = yi;
     }
@@ -808,7 +821,7 @@ struct ks_torn {
   int V = 0, n = 0, nnz = 0, R = 0, P = 0, n_nonlin = 0;
   int max_piece = 0, max_band = 0;
   int solve_threads = 128;  // block of the band solves
-  int max_ldab = 0;
+  int max_ldab = 0, max_colw = 0;
   std::vector<HostPiece> pieces;
   std::vector<int> rp, ci;
   std::vector<void*> owned;
@@ -903,7 +916,7 @@ void stamp_pattern(const ksh::HostPlan& hp, std::vector<std::vector<int>>& rows)
 
 size_t torn_solve_smem(const ks_torn* T) {
   return sizeof(double) * (((size_t)T->max_piece + 1) & ~(size_t)1) +
-         sizeof(double) * 2 * (size_t)KS_TORN_CH * (size_t)T->max_ldab + sizeof(int) * 2 * KS_TORN_CH;
+         sizeof(double) * KS_TORN_NBUF * (size_t)KS_TORN_CH * (size_t)T->max_colw + sizeof(int) * KS_TORN_NBUF * KS_TORN_CH;
 }
 
 int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_torn, std::string* err) {
@@ -1054,6 +1067,7 @@ int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_t
     }
     T->max_piece = std::max(T->max_piece, d.n);
     T->max_ldab = std::max(T->max_ldab, d.ldab);
+    T->max_colw = std::max(T->max_colw, std::max(d.kl, d.kl + d.ku + 1));
     T->max_band = std::max(T->max_band, d.kl + d.ku);
     if (d.n > 12000) { *err = "ks_torn: a piece of " + std::to_string(d.n) + " unknowns (the band solve holds at most 12,000)"; return KS_EUNSUPPORTED; }
   }
@@ -1222,19 +1236,19 @@ int apply_(ks_torn* T, const double* b, double* out) {
   if (R == 0) {
     T->launches++;
     k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
-                                          T->cs, b, T->d_row_a, nullptr, out, T->mask, T->max_piece, T->max_ldab);
+                                          T->cs, b, T->d_row_a, nullptr, out, T->mask, T->max_piece, T->max_colw);
     return ck(cudaGetLastError(), "apply");
   }
   T->launches++;
   k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
-                                        T->cs, b, T->d_row_a, nullptr, T->z, T->mask, T->max_piece, T->max_ldab);
+                                        T->cs, b, T->d_row_a, nullptr, T->z, T->mask, T->max_piece, T->max_colw);
   T->launches++;
   k_tl_h<<<blocks_for((int64_t)R * V, 256), 256, 0, s>>>(R, V, T->d_offp, T->d_offs, T->d_ci, T->J, T->z, T->h, T->mask);
   T->launches++;
-  k_tl_ic_solve<<<(unsigned)V, 1024, (sizeof(double) + sizeof(int)) * R, s>>>(R, V, T->IC, T->icpiv, T->h, T->w, T->mask);
+  k_tl_ic_solve<<<(unsigned)V, 512, (sizeof(double) + sizeof(int)) * R, s>>>(R, V, T->IC, T->icpiv, T->h, T->w, T->mask);
   T->launches++;
   k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
-                                        T->cs, b, T->d_row_a, T->w, out, T->mask, T->max_piece, T->max_ldab);
+                                        T->cs, b, T->d_row_a, T->w, out, T->mask, T->max_piece, T->max_colw);
   return ck(cudaGetLastError(), "apply");
 }
 
