@@ -350,10 +350,9 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
     if (c < 0 || c >= nch) { __pipeline_commit(); return; }
     const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
     double* dst = buf + (c % KS_TORN_NBUF) * bufsz;
-    for (int u = t; u < cols * width; u += 32) {
-      const int jj = u / width, r = u - jj * width;
-      __pipeline_memcpy_async(dst + jj * max_colw + r, AB + first + r + (int64_t)(j0 + jj) * ldab, 8);
-    }
+    const double* src = AB + first + (int64_t)j0 * ldab;
+    for (int jj = 0; jj < cols; jj++, dst += max_colw, src += ldab)
+      for (int r = t; r < width; r += 32) __pipeline_memcpy_async(dst + r, src + r, 8);
     __pipeline_commit();
     if (pivots && t < cols) spiv[(c % KS_TORN_NBUF) * KS_TORN_CH + t] = piv[j0 + t];
   };
