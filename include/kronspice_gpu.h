@@ -455,6 +455,13 @@ typedef struct ks_torn ks_torn;
 int ks_torn_create(const ks_topology* topo, int32_t n_variants, const double* values, const int32_t* torn_elems,
                    int32_t n_torn, ks_torn** out);
 void ks_torn_destroy(ks_torn* t);
+/* The tearing alone, on the host (no GPU): piece_of [n] (pieces numbered in
+ * order of their first unknown, as buildPlan numbers them), the coupling rows
+ * (up to rows_cap), the largest piece and band (kl + ku).  Any output may be
+ * NULL. */
+int ks_torn_plan(const ks_topology* topo, const int32_t* torn_elems, int32_t n_torn, int32_t* piece_of,
+                 int32_t* n_pieces, int32_t* rows, int32_t rows_cap, int32_t* n_rows, int32_t* max_piece,
+                 int32_t* max_band);
 /* Stream of the later calls (NULL: the one ks_torn_create made).  The calls
  * still return only when their results are on the host. */
 int ks_torn_set_stream(ks_torn* t, void* stream);

@@ -334,6 +334,24 @@ TORN_STATS = ("solves", "refactors", "refines", "max_passes", "not_accepted", "p
               "band_doubles", "launches", "refactor_us", "apply_us", "load_us", "residual_us")
 
 
+def torn_plan(elements, n_nodes, n_values, torn):
+    """The tearing of a topology on the host (ks_torn_plan): (piece of each
+    unknown, coupling rows, largest piece, largest band)."""
+    L = _lib.load()
+    el = np.ascontiguousarray(elements, dtype=ELEMENT_DTYPE)
+    tr = np.ascontiguousarray(torn, dtype=np.int32)
+    topo = _lib.KsTopology(int(n_nodes), len(el), int(n_values), 0, el.ctypes.data)
+    n = ctypes.c_int32()
+    _check(L.ks_unknowns(ctypes.byref(topo), ctypes.byref(n), None), "ks_unknowns")
+    piece = np.zeros(n.value, dtype=np.int32)
+    rows = np.zeros(n.value, dtype=np.int32)
+    npc, nr, mp, mb = (ctypes.c_int32() for _ in range(4))
+    _check(L.ks_torn_plan(ctypes.byref(topo), tr.ctypes.data if len(tr) else None, len(tr), piece.ctypes.data,
+                          ctypes.byref(npc), rows.ctypes.data, n.value, ctypes.byref(nr), ctypes.byref(mp),
+                          ctypes.byref(mb)), "ks_torn_plan")
+    return piece, rows[:nr.value].copy(), mp.value, mb.value
+
+
 class TornBatch:
     """Variants of one large topology solved torn into pieces (ks_torn_create):
     kron.JacobianTearing as analysis.Options.Solver, batched over the variants."""

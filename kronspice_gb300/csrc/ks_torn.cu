@@ -823,6 +823,7 @@ struct ks_torn {
   int max_ldab = 0, max_colw = 0;
   std::vector<HostPiece> pieces;
   std::vector<int> rp, ci;
+  std::vector<int> h_pieceOf, h_rows;  // piece of each unknown, coupling rows (the plan, host side)
   std::vector<void*> owned;
   cudaStream_t st = nullptr, own = nullptr;  // the stream in use, the one created here
   cublasHandle_t blas = nullptr;
@@ -918,7 +919,8 @@ size_t torn_solve_smem(const ks_torn* T) {
          sizeof(double) * KS_TORN_NBUF * (size_t)KS_TORN_CH * (size_t)T->max_colw + sizeof(int) * KS_TORN_NBUF * KS_TORN_CH;
 }
 
-int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_torn, std::string* err) {
+int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_torn, std::string* err,
+               bool to_device = true) {
   const ksh::HostPlan& hp = T->hp;
   const int n = hp.n;
   T->n = n;
@@ -1093,6 +1095,9 @@ int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_t
     if (k == KS_ELEM_D || k == KS_ELEM_Q || k == KS_ELEM_M) nonlin.push_back(e);
   }
   T->n_nonlin = (int)nonlin.size();
+  T->h_pieceOf = pieceOf;
+  T->h_rows = rows_list;
+  if (!to_device) return KS_OK;
   auto& o = T->owned;
   std::vector<int32_t> rp32(T->rp.begin(), T->rp.end()), ci32(T->ci.begin(), T->ci.end()), pof(pieceOf.begin(), pieceOf.end());
   std::vector<int32_t> pl(plocal.begin(), plocal.end()), ra(row_a.begin(), row_a.end());
@@ -1421,6 +1426,25 @@ extern "C" int ks_torn_create(const ks_topology* topo, int32_t n_variants, const
   cudaFree(rows);
   if (rc || e != cudaSuccess) { set_error(std::string("ks_torn_create: ") + cudaGetErrorString(e)); delete T; return KS_ECUDA; }
   *out = T;
+  return KS_OK;
+}
+
+extern "C" int ks_torn_plan(const ks_topology* topo, const int32_t* torn_elems, int32_t n_torn, int32_t* piece_of,
+                            int32_t* n_pieces, int32_t* rows, int32_t rows_cap, int32_t* n_rows, int32_t* max_piece,
+                            int32_t* max_band) {
+  if (!topo || (n_torn > 0 && !torn_elems)) { set_error("ks_torn_plan: bad argument"); return KS_EINVAL; }
+  ks_torn T;
+  std::string err;
+  int rc = ksh::plan_layout(topo, &T.hp, &err);
+  if (rc) { set_error(err); return rc; }
+  rc = build_plan(&T, topo, torn_elems, n_torn, &err, false);
+  if (rc) { set_error(err); return rc; }
+  if (piece_of) for (int i = 0; i < T.n; i++) piece_of[i] = T.h_pieceOf[i];
+  if (n_pieces) *n_pieces = T.P;
+  if (rows) for (int a = 0; a < T.R && a < rows_cap; a++) rows[a] = T.h_rows[a];
+  if (n_rows) *n_rows = T.R;
+  if (max_piece) *max_piece = T.max_piece;
+  if (max_band) *max_band = T.max_band;
   return KS_OK;
 }
 

@@ -642,6 +642,30 @@ extern "C" int kso_tran_torn(const ks_topology* t, const double* values, const k
   return e;
 }
 
+// The plan buildPlan (kron/jacobian.go:296-389) makes for the Jacobian of one
+// backward-Euler step of length h (the transient pattern): piece of each
+// unknown and the coupling rows in the reference's order.
+extern "C" int kso_torn_plan(const ks_topology* t, const double* values, const int32_t* pairs, int n_pairs, double h,
+                             int32_t* piece_of, int32_t* n_pieces, int32_t* rows, int cap, int32_t* n_rows) {
+  Sim s;
+  Opts opt(nullptr);
+  auto cuts = cut_pairs(pairs, n_pairs);
+  s.tornCuts = &cuts;
+  ks_tran_spec sp{};
+  sp.step = h; sp.stop = h; sp.method = KS_METHOD_BE; sp.fixed_step = 1;
+  if (s.build(t, values, sp.step, sp.stop, 0)) return KS_EINVAL;
+  Sim::Rec rec;
+  int st = 0;
+  int e = s.tran(sp, opt, rec, &st);
+  Torn* T = dynamic_cast<Torn*>(s.M.get());
+  if (e || !T || !T->havePlan) return KS_EINVAL;
+  for (int i = 0; i < s.n; i++) piece_of[i] = T->pieceOf[i];
+  *n_pieces = (int32_t)T->pieces.size();
+  *n_rows = (int32_t)T->rows.size();
+  for (size_t a = 0; a < T->rows.size() && (int)a < cap; a++) rows[a] = T->rows[a];
+  return KS_OK;
+}
+
 template <class F>
 static void parallelFor(int nc, int nthreads, F f) {
   if (nthreads <= 0) nthreads = (int)std::thread::hardware_concurrency();

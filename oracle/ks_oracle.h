@@ -63,6 +63,11 @@ int kso_tran_torn(const ks_topology* t, const double* values, const ks_tran_spec
                   const int32_t* pairs, int n_pairs, double reuse_tol, int capacity, double* t_out, double* x_out,
                   int32_t* npts, int32_t* steps, int32_t* iters, int64_t* stats, char* err, int errlen);
 
+/* buildPlan's pieces and coupling rows for the Jacobian of one backward-Euler
+ * step of length h: piece_of [n], rows [cap]. */
+int kso_torn_plan(const ks_topology* t, const double* values, const int32_t* pairs, int n_pairs, double h,
+                  int32_t* piece_of, int32_t* n_pieces, int32_t* rows, int cap, int32_t* n_rows);
+
 /* Unknown count and layout of one circuit (device Setup), for the tests. */
 int kso_unknowns(const ks_topology* t, const double* values, int32_t* n, int32_t* is_v);
 

@@ -66,6 +66,7 @@ def lib():
         L.kso_batch_tran.argtypes = [P, P, ctypes.c_int, P, P, ctypes.c_int, P, P, P, P]
         L.kso_unknowns.argtypes = [P, P, P, P]
         L.kso_ac.argtypes = [P, P, P, P, ctypes.c_int, P, ctypes.c_char_p, ctypes.c_int]
+        L.kso_torn_plan.argtypes = [P, P, P, ctypes.c_int, ctypes.c_double, P, P, P, ctypes.c_int, P]
         L.kso_torn_cuts.argtypes = [P, P, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_char_p, ctypes.c_int]
         L.kso_op_torn.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_double, P, P, P, ctypes.c_char_p, ctypes.c_int]
         L.kso_tran_torn.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.c_double, ctypes.c_int, P, P, P, P, P, P,
@@ -175,6 +176,20 @@ def torn_cuts(pk, elems):
     err = ctypes.create_string_buffer(512)
     st = lib().kso_torn_cuts(pk.tref(), _ptr(e), len(e), _ptr(pairs), cap, ctypes.byref(npairs), err, 512)
     return st, pairs[:npairs.value].copy(), err.value.decode()
+
+
+def torn_plan(pk, pairs, h):
+    """buildPlan's (piece of each unknown, coupling rows) for one backward-Euler step of length h."""
+    n, _ = unknowns(pk)
+    p = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+    piece = np.zeros(n, dtype=np.int32)
+    rows = np.zeros(n, dtype=np.int32)
+    npc, nr = ctypes.c_int32(), ctypes.c_int32()
+    st = lib().kso_torn_plan(pk.tref(), _ptr(pk.values), _ptr(p), len(p), float(h), _ptr(piece), ctypes.byref(npc),
+                             _ptr(rows), n, ctypes.byref(nr))
+    if st:
+        raise ValueError("kso_torn_plan failed")
+    return piece, rows[:nr.value].copy(), npc.value
 
 
 def op_torn(pk, pairs, opt=None, reuse_tol=0.0):
