@@ -1,11 +1,15 @@
 """Minimal SPICE netlist reader for the golden fixtures (test infrastructure).
 
 Reads the subset of SPICE the reference's golden netlists use for the element
-kinds of the engine (R, C, L, V, I, D, Q, M; .model, .op, .dc, .tran) into a
-plain dict: the same information circuit.FromDeck (circuit/builder.go:307)
-extracts from a parsed deck.  Netlists with other elements or with .subckt /
-.param return None from parse() with the reason, and the golden tests skip them.
+kinds of the engine (R, C, L, V, I, D, Q, M; .model, .op, .dc, .tran, .ac,
+.param with {expression} / 'expression' values, .subckt with params and
+nesting, expanded into a flat circuit) into a plain dict: the same information
+circuit.FromDeck (circuit/builder.go:307) extracts from a parsed deck.
+Netlists with other elements return None from parse() with the reason, and the
+golden tests skip them.
 """
+import ast
+import math
 import re
 
 _SUFFIX = [("meg", 1e6), ("mil", 25.4e-6), ("t", 1e12), ("g", 1e9), ("k", 1e3),
@@ -87,11 +91,187 @@ def _source(toks):
     return src
 
 
+# ---------------------------------------------------------------- expressions
+_FUNCS = {"sqrt": math.sqrt, "exp": math.exp, "log": math.log, "ln": math.log, "sin": math.sin, "cos": math.cos,
+          "abs": abs, "pow": math.pow, "min": min, "max": max}
+
+
+def _py_expr(text):
+    """A SPICE expression as Python source: numbers with engineering suffixes
+    converted, identifiers lower-cased, '^' as power."""
+    out, i = [], 0
+    while i < len(text):
+        c = text[i]
+        if c.isdigit() or (c == "." and i + 1 < len(text) and text[i + 1].isdigit()):
+            j = i
+            while j < len(text) and (text[j].isdigit() or text[j] == "."):
+                j += 1
+            if j < len(text) and text[j] in "eE" and j + 1 < len(text) and (text[j + 1].isdigit() or text[j + 1] in "+-"):
+                j += 2
+                while j < len(text) and text[j].isdigit():
+                    j += 1
+            k = j
+            while k < len(text) and text[k].isalpha():
+                k += 1
+            out.append(repr(value(text[i:k])))
+            i = k
+        elif c.isalpha() or c == "_":
+            j = i
+            while j < len(text) and (text[j].isalnum() or text[j] == "_"):
+                j += 1
+            out.append(text[i:j].lower())
+            i = j
+        elif c == "^":
+            out.append("**")
+            i += 1
+        else:
+            out.append(c)
+            i += 1
+    return "".join(out)
+
+
+def evaluate(text, scope):
+    """Value of a SPICE expression over the parameters in scope (names
+    lower-case, values numbers or unevaluated expressions)."""
+    tree = ast.parse(_py_expr(text).strip(), mode="eval")
+
+    def ev(n):
+        if isinstance(n, ast.Expression):
+            return ev(n.body)
+        if isinstance(n, ast.Constant) and isinstance(n.value, (int, float)):
+            return float(n.value)
+        if isinstance(n, ast.Name):
+            if n.id not in scope:
+                raise ValueError("unknown parameter %r" % n.id)
+            v = scope[n.id]
+            return v if isinstance(v, float) else evaluate(v, scope)
+        if isinstance(n, ast.BinOp):
+            a, b = ev(n.left), ev(n.right)
+            ops = {ast.Add: lambda: a + b, ast.Sub: lambda: a - b, ast.Mult: lambda: a * b,
+                   ast.Div: lambda: a / b, ast.Pow: lambda: a ** b}
+            if type(n.op) not in ops:
+                raise ValueError("operator in %r" % text)
+            return ops[type(n.op)]()
+        if isinstance(n, ast.UnaryOp) and isinstance(n.op, (ast.USub, ast.UAdd)):
+            v = ev(n.operand)
+            return -v if isinstance(n.op, ast.USub) else v
+        if isinstance(n, ast.Call) and isinstance(n.func, ast.Name) and n.func.id in _FUNCS:
+            return float(_FUNCS[n.func.id](*[ev(a) for a in n.args]))
+        raise ValueError("unsupported expression %r" % text)
+    return ev(tree)
+
+
+_GROUP = re.compile(r"\{[^{}]*\}|'[^']*'")
+
+
+def _protect(line):
+    """Replace {...} and '...' expressions by placeholders before tokenising."""
+    exprs = []
+
+    def sub(m):
+        exprs.append(m.group(0)[1:-1])
+        return "@%d@" % (len(exprs) - 1)
+    return _GROUP.sub(sub, line), exprs
+
+
+def _assignments(toks):
+    out = []
+    for t in toks:
+        if "=" in t:
+            k, v = t.split("=", 1)
+            out.append((k.lower(), v))
+    return out
+
+
+def _expand(lines):
+    """Flatten .param / .subckt: element lines with their nodes renamed and
+    every {expression} evaluated; other lines as they are."""
+    glob, subckts, top = {}, {}, []
+    cur = None
+    for ln in lines:
+        pl, exprs = _protect(ln)
+        toks = _tokens(pl)
+        if not toks:
+            continue
+        head = toks[0].lower()
+        if head == ".subckt":
+            pnames = [t for t in toks[2:] if "=" in t]
+            nodes = [t for t in toks[2:] if "=" not in t and t.lower() != "params:"]
+            cur = {"nodes": nodes, "params": [(k, _unprotect(v, exprs)) for k, v in _assignments(pnames)], "body": []}
+            subckts[toks[1].lower()] = cur
+            continue
+        if head == ".ends":
+            cur = None
+            continue
+        if head == ".param":
+            for k, v in _assignments(toks[1:]):
+                glob[k] = _unprotect(v, exprs)
+            continue
+        (cur["body"] if cur is not None else top).append(ln)
+    out = []
+
+    def emit(body, nodemap, prefix, scope):
+        for ln in body:
+            pl, exprs = _protect(ln)
+            toks = _tokens(pl)
+            head = toks[0].lower()
+            if head.startswith("."):
+                out.append(ln)
+                continue
+            if head[0] == "x":
+                args = [t for t in toks[1:] if "=" not in t]
+                sub = subckts.get(args[-1].lower())
+                if sub is None:
+                    raise ValueError("unknown subcircuit %r" % args[-1])
+                actual = [nodemap.get(a, a if a == "0" else prefix + a) for a in args[:-1]]
+                inner = dict(scope)
+                over = {k: _num(_unprotect(v, exprs), scope) for k, v in _assignments(toks[1:])}
+                for k, v in sub["params"]:
+                    inner[k] = over[k] if k in over else _num(v, inner)
+                m = dict(zip(sub["nodes"], actual))
+                emit(sub["body"], m, prefix + toks[0] + ".", inner)
+                continue
+            # an element: rename nodes, evaluate expressions
+            n_nodes = {"r": 2, "c": 2, "l": 2, "v": 2, "i": 2, "d": 2, "q": 4, "m": 4}.get(head[0], 2)
+            new = [toks[0] + ("." + prefix[:-1] if prefix else "")]  # kind letter first: R1.XA.X1
+            for k, t in enumerate(toks[1:]):
+                if k < n_nodes and t not in ("(", ")") and "=" not in t and not t.startswith("@"):
+                    new.append(nodemap.get(t, t if t == "0" else prefix + t))
+                else:
+                    new.append(_evaltok(t, exprs, scope))
+            out.append(" ".join(new))
+
+    scope0 = {k: v for k, v in glob.items()}
+    emit(top, {}, "", scope0)
+    return out
+
+
+def _unprotect(v, exprs):
+    m = re.fullmatch(r"@(\d+)@", v)
+    return exprs[int(m.group(1))] if m else v
+
+
+def _num(v, scope):
+    m = _NUM.match(v.strip())
+    if m and re.fullmatch(r"[a-zA-Z]*", m.group(2)):  # a plain number, with or without a suffix
+        return value(v)
+    return evaluate(v, scope)
+
+
+def _evaltok(t, exprs, scope):
+    if "@" not in t:
+        return t
+    if "=" in t:
+        k, v = t.split("=", 1)
+        return "%s=%r" % (k, _num(_unprotect(v, exprs), scope))
+    return repr(_num(_unprotect(t, exprs), scope))
+
+
 def parse(text):
     """Return (circuit dict, None) or (None, reason)."""
     try:
         return _parse(text)
-    except (ValueError, IndexError) as e:
+    except (ValueError, IndexError, ZeroDivisionError) as e:
         return None, "unsupported netlist: %s" % e
 
 
@@ -108,10 +288,10 @@ def _parse(text):
             lines[-1] += " " + s[1:]
         else:
             lines.append(s)
+    lines = [ln.split(";", 1)[0] if ";" in ln else ln for ln in lines]
+    lines = _expand(lines)
     ckt = {"title": raw[0].strip() if raw else "", "elements": [], "models": {}, "analyses": []}
     for ln in lines:
-        if ";" in ln:
-            ln = ln.split(";", 1)[0]
         toks = _tokens(ln)
         if not toks:
             continue
