@@ -905,6 +905,9 @@ def bench_torn(args):
     import torch
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     from kronspice_gb300 import analysis, build, workloads
     build.build()
     dev = torch.device("cuda", local)
@@ -926,6 +929,8 @@ def bench_torn(args):
         for _ in range(args.warmup):
             tb.tran(spec_, opt, reuse=reuse, probes=grid_nodes)
         torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
         tot, pts = 0.0, 0
         for _ in range(steps_timed):
             flush.fill_(1.0)
@@ -936,6 +941,11 @@ def bench_torn(args):
             torch.cuda.synchronize()
             tot += e0.elapsed_time(e1) / 1e3
             pts += int(steps[st == 0].sum())
+        if world > 1:  # every rank's variants, the slowest rank's time
+            t = torch.tensor([tot, float(pts)], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(t[:1], op=torch.distributed.ReduceOp.MAX)
+            torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+            tot, pts = float(t[0].item()), int(t[1].item())
         return {"seconds": tot, "points": pts, "stats": stats, "status": st, "iters": it, "wave": wave}
 
     clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp",
@@ -961,7 +971,16 @@ def bench_torn(args):
         torch.cuda.synchronize()
         e2e_t += time.perf_counter() - t0
         e2e_pts += int(steps[st == 0].sum())
+    if world > 1:
+        t = torch.tensor([e2e_t, float(e2e_pts)], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        e2e_t, e2e_pts = float(t[0].item()), int(t[1].item())
     e2e_value = e2e_pts / e2e_t
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return
 
     # accuracy: the first few steps of variant 0 against the oracle's untorn transient
     from oracle import oracle as orc
@@ -992,8 +1011,9 @@ def bench_torn(args):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     line = {
-        "metric": METRIC, "value": value, "unit": TRAN_UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": chosen["seconds"] / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": value, "unit": TRAN_UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": chosen["seconds"] / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox)",
         "config": {"workload": "power_grid_tran_%d" % V, "variants": V, "grid": "256x256", "unknowns": n,
                    "pieces": P, "coupling_rows": R, "largest_piece": tb.max_piece, "band": tb.max_band,
@@ -1016,6 +1036,8 @@ def bench_torn(args):
         "clocks": clocks,
     }
     print(json.dumps(line))
+    if world > 1:
+        torch.distributed.barrier()
 
 
 def main():

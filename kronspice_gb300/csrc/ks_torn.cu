@@ -819,8 +819,7 @@ struct ks_torn {
   ksh::HostPlan hp;
   int V = 0, n = 0, nnz = 0, R = 0, P = 0, n_nonlin = 0;
   int max_piece = 0, max_band = 0;
-  int solve_threads = 128;  // block of the band solves
-  int max_ldab = 0, max_colw = 0;
+  int max_colw = 0;  // widest staged column part of a band solve (max of kl, kl + ku + 1)
   std::vector<HostPiece> pieces;
   std::vector<int> rp, ci;
   std::vector<int> h_pieceOf, h_rows;  // piece of each unknown, coupling rows (the plan, host side)
@@ -841,7 +840,7 @@ struct ks_torn {
   const double **Aptr, **Bptr;
   double** Cptr;
   unsigned long long* berr;
-  uint8_t *mask, *active;
+  uint8_t* mask;  // variants a launch works on
   std::vector<uint8_t> have;  // factors exist, per variant
   // counters
   int64_t solves = 0, refactors = 0, refines = 0, max_passes = 0, failed = 0, launches = 0;
@@ -1067,13 +1066,11 @@ int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_t
       pslot.push_back(s); pli.push_back(plocal[i]); plj.push_back(plocal[T->ci[s]]);
     }
     T->max_piece = std::max(T->max_piece, d.n);
-    T->max_ldab = std::max(T->max_ldab, d.ldab);
     T->max_colw = std::max(T->max_colw, std::max(d.kl, d.kl + d.ku + 1));
     T->max_band = std::max(T->max_band, d.kl + d.ku);
     if (d.n > 12000) { *err = "ks_torn: a piece of " + std::to_string(d.n) + " unknowns (the band solve holds at most 12,000)"; return KS_EUNSUPPORTED; }
   }
   T->band_stride = band; T->piv_stride = n; T->wc_stride = wc; T->y_stride = y;
-  T->solve_threads = 32;
   if (torn_solve_smem(T) > 227 * 1024) {
     *err = "ks_torn: a piece of " + std::to_string(T->max_piece) + " unknowns with a band of " +
            std::to_string(T->max_band) + " does not fit the band solve's shared memory";
@@ -1136,7 +1133,7 @@ int alloc_numeric(ks_torn* T) {
   T->h = dalloc<double>((size_t)T->R * V, o); T->w = dalloc<double>((size_t)T->R * V, o);
   T->bad = dalloc<int32_t>(V, o); T->flags = dalloc<int32_t>(V, o);
   T->berr = dalloc<unsigned long long>(V, o);
-  T->mask = dalloc<uint8_t>(V, o); T->active = dalloc<uint8_t>(V, o);
+  T->mask = dalloc<uint8_t>(V, o);
   T->list = dalloc<int32_t>(V, o);
   T->Aptr = (const double**)dalloc<double*>(V, o); T->Bptr = (const double**)dalloc<double*>(V, o);
   T->Cptr = dalloc<double*>(V, o);
@@ -1144,7 +1141,7 @@ int alloc_numeric(ks_torn* T) {
   for (void* p : {(void*)T->values, (void*)T->derived, (void*)T->state, (void*)T->x, (void*)T->xo, (void*)T->J,
                   (void*)T->rhs, (void*)T->r, (void*)T->dx, (void*)T->z, (void*)T->rs, (void*)T->cs, (void*)T->band,
                   (void*)T->piv, (void*)T->Y, (void*)T->Wc, (void*)T->IC, (void*)T->icpiv, (void*)T->h, (void*)T->w,
-                  (void*)T->bad, (void*)T->flags, (void*)T->berr, (void*)T->mask, (void*)T->active,
+                  (void*)T->bad, (void*)T->flags, (void*)T->berr, (void*)T->mask,
                   (void*)T->list, (void*)T->Aptr, (void*)T->Bptr, (void*)T->Cptr})
     if (!p) { set_error("ks_torn: device allocation failed"); return KS_ENOMEM; }
   return KS_OK;
@@ -1236,7 +1233,7 @@ int apply_(ks_torn* T, const double* b, double* out) {
   cudaStream_t s = T->st;
   const unsigned grid = (unsigned)(V * T->P);
   const size_t sm = torn_solve_smem(T);
-  const int bt = T->solve_threads;
+  const int bt = 32;  // one warp per (variant, piece)
   if (R == 0) {
     T->launches++;
     k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
