@@ -24,6 +24,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -439,7 +440,7 @@ def bench_tran(args):
         return {"seconds": total, "ms_per_step": total / args.steps * 1e3, "points": pts, "ok": int(ok.sum()),
                 "iters_per_point": float(iv[3][ok].sum() / max(pts, 1)), "status": iv[1].copy()}
 
-    clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp",
+    clk = Clocks(os.path.join(tempfile.gettempdir(),
                               "bench_clocks_%d.csv" % rank))
     variants = {}
     with clk:
@@ -624,7 +625,7 @@ def bench_multi(args):
                 "ok": int(ok.sum()), "iters_per_point": float(iv[3][ok].sum() / max(1, iv[2][ok].sum())),
                 "status": iv[1].copy()}
 
-    clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp",
+    clk = Clocks(os.path.join(tempfile.gettempdir(),
                               "bench_clocks_%d.csv" % rank))
     with clk:
         plain = timed(plain_opt)
@@ -781,7 +782,7 @@ def bench_ac(args):
         return {"seconds": total, "ms_per_step": total / args.steps * 1e3, "ok": int((iv[0] == 0).sum()),
                 "iters_mean": float(iv[1].mean()), "status": iv[0].copy()}
 
-    clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp",
+    clk = Clocks(os.path.join(tempfile.gettempdir(),
                               "bench_clocks_%d.csv" % rank))
     with clk:
         plain = timed(step, plain_opt)
@@ -948,7 +949,7 @@ def bench_torn(args):
             tot, pts = float(t[0].item()), int(t[1].item())
         return {"seconds": tot, "points": pts, "stats": stats, "status": st, "iters": it, "wave": wave}
 
-    clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp",
+    clk = Clocks(os.path.join(tempfile.gettempdir(),
                               "bench_clocks_%d.csv" % rank))
     with clk:
         chosen = timed(True, args.steps, spec)
@@ -1135,7 +1136,7 @@ def main():
     plain_opt = analysis.Options(reltol=RELTOL, precision="fp64", kernel="generic")
     chosen_opt = analysis.Options(reltol=RELTOL, precision=args.precision,
                                   kernel="specialized" if spec_ok else "generic")
-    clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp",
+    clk = Clocks(os.path.join(tempfile.gettempdir(),
                               "bench_clocks_%d.csv" % rank))
     variants = {}
     with clk:
