@@ -5,16 +5,25 @@ single-stage BJT common-emitter amplifiers (IS log-U[1e-16, 1e-14] A, BF
 U[50, 300], R1 R2 RC RE log-U[100 ohm, 1 Mohm], Vcc U[5, 15] V) at SPICE reltol
 1e-6 / abstol 1e-12.  One step = one batched operating point of all circuits.
 
-  plain  : FP64 LU, standard Newton start (InitJct), the reference's algorithm
-  chosen : FP32 LU + FP64 Newton residual, with the learned Newton start when
-           the MLP is available (otherwise the standard start)
+  plain  : generic kernel, FP64 LU, standard Newton start (InitJct): the
+           reference's algorithm as it stands
+  chosen : per-topology kernel, FP32 LU + FP64 Newton residual, the learned
+           Newton start (BF16 MLP) refined by the FP32 Newton stage, then the
+           FP64 Newton (FP64 device evaluation, the reference's convergence
+           test and fallback chain) and the learned start's basin check
 
-value is the chosen path with inputs resident in HBM; e2e is the same through
-the C ABI with host buffers (values H2D, solutions D2H) inside the timed region.
-Between timed steps L2 is flushed (a 512 MB write); each step is timed with CUDA
-events on the launching stream.  --impl reference times the CPU restatement of
-the reference's Go path (the reference cannot be built here: no Go toolchain)
-over all host cores on a bounded sample of the same workload.
+Every combination of kernel, LU precision, start and FP32 stage is timed as a
+variant.  value is the chosen path with inputs resident in HBM; e2e is the same
+through the C ABI with host buffers (values H2D, solutions D2H) inside the timed
+region.  Between timed steps L2 is flushed (a 512 MB write); each step is timed
+with CUDA events on the launching stream.  The chosen path's results are
+checked against the CPU oracle (status per circuit, node voltages within
+reltol/vntol) and the run exits 3 after printing its line when they are not.
+With the headline workload the line also carries the op-amp workload
+(65,536 two-stage CMOS op-amps, 24-D parameters, learned start) under
+"cmos_opamp", measured the same way.  --impl reference times the CPU
+restatement of the reference's Go path (the reference cannot be built here: no
+Go toolchain) over all host cores on a bounded sample of the same workload.
 """
 import argparse
 import ctypes
@@ -38,6 +47,11 @@ RELTOL = 1e-6
 # workload -> (default circuits, compulsory bytes per solve: parameters in + node voltages out, 8 B each)
 WORKLOADS = {"bjt_ce": (16384, (7 + 5) * 8), "cmos_opamp": (65536, (24 + 7) * 8), "rc_ladder": (4096, 0),
              "random_netlists": (8192, 0), "bjt_ce_ac": (16384, 0), "power_grid": (64, 0)}
+# timed steps when --steps is not given (the headline times about 200 steps)
+DEFAULT_STEPS = {"bjt_ce": 200, "cmos_opamp": 5, "rc_ladder": 20, "random_netlists": 1, "bjt_ce_ac": 20,
+                 "power_grid": 1}
+# most FP32 Newton iterations of the chosen path's start stage (its gmin / source-stepping chain included)
+FP32_START = {"bjt_ce": 200, "cmos_opamp": 6000}
 # torn power grid: 256 x 256 mesh in 4 x 4 pieces, 1,024 clamped loads, 500 backward-Euler steps of 0.1 ns
 POWER_GRID = dict(N=256, P=4, loads=1024)
 POWER_STEPS, POWER_H = 500, 0.1e-9
@@ -59,7 +73,7 @@ def generator(name):
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=0, help="timed steps (0: the workload's default)")
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
     p.add_argument("--n-circ", type=int, default=0)
@@ -71,6 +85,10 @@ def parse():
     p.add_argument("--variants", type=int, default=1, help="also time every kernel/precision/start combination")
     p.add_argument("--start-cache", default=None,
                    help="learned-start network file (.npz): loaded when present, else trained and saved there")
+    p.add_argument("--fp32-start", type=int, default=-1,
+                   help="most FP32 Newton iterations of the chosen path's start stage (-1: the workload's, 0: off)")
+    p.add_argument("--secondary", type=int, default=1,
+                   help="with the headline workload, also run the op-amp learned-start workload")
     return p.parse_args()
 
 
@@ -1041,10 +1059,171 @@ def bench_torn(args):
         torch.distributed.barrier()
 
 
+def op_workload(args, name, B, steps, warmup, with_variants, cache, dev, stream, world, rank):
+    """One operating-point workload: plain (generic kernel, FP64, InitJct) against
+    chosen (per-topology kernel where the system fits in registers, FP32 LU + FP64
+    residual, learned start refined by the FP32 Newton stage, the learned start's
+    basin check), each step one batched operating point of all B circuits, L2
+    flushed between steps, CUDA events on the launching stream.  Returns the
+    numbers of both paths, the variants, the end-to-end rate through the C ABI
+    with host buffers, the one-time costs and the parity against the oracle."""
+    import torch
+    from kronspice_gb300 import analysis, learned_start
+    el, nn, vals = generator(name)(B, args.seed + rank)
+    plan = analysis.Plan(el, nn, vals.shape[1])
+    batch = analysis.Batch(plan, vals)
+    n = plan.n
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    x_dev = torch.empty((B, n), dtype=torch.float64, device=dev)
+    st_dev = torch.empty(B, dtype=torch.int32, device=dev)
+    it_dev = torch.empty(B, dtype=torch.int32, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    learned = learned_start.for_workload(name, el, nn, vals, batch, dev, cache=cache)
+
+    def step(opt, x0_dev=None):
+        batch.op_async(opt, None if x0_dev is None else x0_dev.data_ptr(), x_dev.data_ptr(), st_dev.data_ptr(),
+                       it_dev.data_ptr(), sh)
+
+    def timed(opt, with_start, k=steps):
+        launches = 1 + (learned.launches_per_step if with_start else 0)
+        for _ in range(warmup):
+            step(opt, learned.predict(stream) if with_start else None)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        times = []
+        for _ in range(k):
+            flush.fill_(1.0)
+            e0, em, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            x0 = learned.predict(stream) if with_start else None
+            em.record(stream)
+            step(opt, x0)
+            e1.record(stream)
+            times.append((e0, em, e1))
+        torch.cuda.synchronize()
+        total = sum(a.elapsed_time(c) for a, b, c in times) / 1e3
+        op_s = sum(b.elapsed_time(c) for a, b, c in times) / 1e3 / k
+        if world > 1:
+            t = torch.tensor([total], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total = float(t.item())
+        st = st_dev.cpu().numpy()
+        it = it_dev.cpu().numpy()
+        return {"seconds": total, "ms_per_step": total / k * 1e3, "ok": int((st == 0).sum()), "op_kernel_s": op_s,
+                "iters_mean": float(it.mean()), "iters_max": int(it.max()), "launches": launches * k,
+                "x": x_dev.cpu().numpy(), "status": st, "steps": k}
+
+    def rate(r):
+        return world * r["ok"] * r["steps"] / r["seconds"] if r["seconds"] > 0 else 0.0
+
+    spec_info = {"kernel": None}
+    if n <= 6:  # systems that fit in registers get the per-topology kernel
+        try:
+            kname, csec = plan.specialize("op")
+            spec_info = {"kernel": kname, "nvrtc_s": csec}
+        except RuntimeError as e:
+            spec_info = {"kernel": None, "error": str(e)[:200]}
+    spec_ok = spec_info["kernel"] is not None
+    kern = "specialized" if spec_ok else "generic"
+    s32 = FP32_START.get(name, 200) if args.fp32_start < 0 else args.fp32_start
+    plain_opt = analysis.Options(reltol=RELTOL, precision="fp64", kernel="generic")
+    chosen_opt = analysis.Options(reltol=RELTOL, precision=args.precision, kernel=kern, fp32_start_iters=s32,
+                                  start_check=learned.start_check)
+    clk = Clocks(os.path.join(tempfile.gettempdir(), "bench_clocks_%s_%d.csv" % (name, rank)))
+    variants = {}
+    with clk:
+        plain = timed(plain_opt, False)
+        chosen = timed(chosen_opt, True)
+        if with_variants:  # each ingredient of the chosen path alone and combined
+            kerns = ["generic", "specialized"] if spec_ok else ["generic"]
+            precs = ("fp64", "mixed") if name == "bjt_ce" else ("mixed",)
+            for kn in kerns:
+                for prec in precs:
+                    for ws in (False, True):
+                        for st32 in (0, s32):
+                            o = analysis.Options(reltol=RELTOL, precision=prec, kernel=kn, fp32_start_iters=st32,
+                                                 start_check=learned.start_check if ws else 0.0)
+                            r = timed(o, ws)
+                            variants["%s/%s/%s%s" % (kn, prec, "learned" if ws else "InitJct",
+                                                     "+fp32stage" if st32 else "")] = {
+                                "ms_per_step": r["ms_per_step"], "solves_per_s": rate(r),
+                                "newton_iters_mean": r["iters_mean"], "newton_iters_max": r["iters_max"]}
+    clocks = clk.summary(dev.index)
+
+    # end to end through the C ABI: pinned host values in, host solutions out
+    vals_pin = torch.from_numpy(vals.copy()).pin_memory()
+    x_host = torch.empty((B, n), dtype=torch.float64).pin_memory()
+    s_host = torch.empty(B, dtype=torch.int32).pin_memory()
+    i_host = torch.empty(B, dtype=torch.int32).pin_memory()
+    L = __import__("kronspice_gb300._lib", fromlist=["x"]).load()
+    o = chosen_opt.c()
+
+    def e2e_step():
+        rc = L.ks_batch_set_values(batch.handle, ctypes.c_void_p(vals_pin.data_ptr()), 0, sh)
+        assert rc == 0
+        x0 = learned.predict(stream)
+        rc = L.ks_op_async(batch.handle, ctypes.byref(o), ctypes.c_void_p(x0.data_ptr()), x_dev.data_ptr(),
+                           st_dev.data_ptr(), it_dev.data_ptr(), sh)
+        assert rc == 0
+        x_host.copy_(x_dev, non_blocking=True)
+        s_host.copy_(st_dev, non_blocking=True)
+        i_host.copy_(it_dev, non_blocking=True)
+        stream.synchronize()
+    for _ in range(warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_t = 0.0
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_t += time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_t], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e = {"value": world * B * steps / e2e_t, "unit": UNIT, "h2d_bytes_per_step": int(vals.nbytes),
+           "d2h_bytes_per_step": int(B * n * 8 + 2 * B * 4)}
+
+    # parity of the chosen path against the CPU oracle: status and node voltages
+    from oracle import oracle as orc
+    samp = min(B if name == "bjt_ce" else 8192, B)
+    so, xo, io = orc.batch_op(orc.Packed(el, nn, vals[:samp]), samp, orc.options(reltol=RELTOL))
+    okm = (so == 0) & (chosen["status"][:samp] == 0)
+    xc = chosen["x"][:samp]
+    dv = np.abs(xc[okm, :nn - 1] - xo[okm, :nn - 1])
+    tolv = 1e-6 + RELTOL * np.abs(xo[okm, :nn - 1])
+    parity = {"circuits": int(samp), "status_equal": bool(np.array_equal(chosen["status"][:samp], so)),
+              "max_node_voltage_err_v": float(dv.max()) if dv.size else None,
+              "within_tolerance": bool(np.all(dv <= tolv)), "tolerance": "1e-6 V + 1e-6 |v| per node (reltol/vntol)"}
+    parity["ok"] = parity["status_equal"] and parity["within_tolerance"]
+
+    value, plain_value = rate(chosen), rate(plain)
+    info = dict(learned.info)
+    one_time = {"nvrtc_s": spec_info.get("nvrtc_s"), "train_solve_s": info.get("train_solve_s"),
+                "train_s": info.get("train_s")}
+    if info.get("loaded_from"):
+        one_time["note"] = "network loaded from %s (trained in an earlier run)" % info["loaded_from"]
+    total_once = sum(v for v in (one_time["train_solve_s"], one_time["train_s"], one_time["nvrtc_s"]) if v)
+    saved = (plain["ms_per_step"] - chosen["ms_per_step"]) / 1e3
+    one_time["total_s"] = total_once
+    one_time["saved_per_batch_s"] = saved
+    one_time["break_even_batches"] = total_once / saved if saved > 0 else None
+    return {"name": name, "B": B, "n": n, "nn": nn, "el": el, "vals": vals, "plain": plain, "chosen": chosen,
+            "value": value, "plain_value": plain_value, "variants": variants, "e2e": e2e, "parity": parity,
+            "spec_info": spec_info, "learned": info, "one_time": one_time, "clocks": clocks,
+            "chosen_opt": chosen_opt, "s32": s32, "steps": steps}
+
+
 def main():
     args = parse()
     if args.n_circ <= 0:
         args.n_circ = WORKLOADS[args.workload][0]
+    if args.steps <= 0:
+        args.steps = DEFAULT_STEPS[args.workload]
     if args.impl == "reference":
         run_reference(args)
         return
@@ -1066,159 +1245,32 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    from kronspice_gb300 import analysis, build, workloads
+    from kronspice_gb300 import build, _lib
     build.build()
     dev = torch.device("cuda", local)
-    el, nn, vals = generator(args.workload)(args.n_circ, args.seed + rank)
-    B = vals.shape[0]
-    plan = analysis.Plan(el, nn, vals.shape[1])
-    batch = analysis.Batch(plan, vals)
-    n = plan.n
     stream = torch.cuda.Stream(dev)  # a real stream: kernels and events on the same one
     torch.cuda.set_stream(stream)
-    sh = ctypes.c_void_p(stream.cuda_stream)
-    x_dev = torch.empty((B, n), dtype=torch.float64, device=dev)
-    st_dev = torch.empty(B, dtype=torch.int32, device=dev)
-    it_dev = torch.empty(B, dtype=torch.int32, device=dev)
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-
-    learned = None
-    try:
-        from kronspice_gb300 import learned_start
-        learned = learned_start.for_workload(args.workload, el, nn, vals, batch, dev, cache=args.start_cache)
-    except (ImportError, AttributeError):
-        learned = None
-
-    def step(opt, x0_dev=None):
-        batch.op_async(opt, None if x0_dev is None else x0_dev.data_ptr(), x_dev.data_ptr(), st_dev.data_ptr(),
-                       it_dev.data_ptr(), sh)
-
-    def timed(opt, with_start):
-        launches = 1 + (learned.launches_per_step if (with_start and learned) else 0)
-        for _ in range(args.warmup):
-            x0 = learned.predict(stream) if (with_start and learned) else None
-            step(opt, x0)
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
-        times = []
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            e0, em, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-            e0.record(stream)
-            x0 = learned.predict(stream) if (with_start and learned) else None
-            em.record(stream)
-            step(opt, x0)
-            e1.record(stream)
-            times.append((e0, em, e1))
-        torch.cuda.synchronize()
-        ms = [a.elapsed_time(c) for a, b, c in times]
-        op_ms = [b.elapsed_time(c) for a, b, c in times]
-        total = sum(ms) / 1e3
-        if world > 1:
-            t = torch.tensor([total], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            total = float(t.item())
-        st = st_dev.cpu().numpy()
-        it = it_dev.cpu().numpy()
-        return {"seconds": total, "ms_per_step": total / args.steps * 1e3, "ok": int((st == 0).sum()),
-                "op_kernel_s": sum(op_ms) / 1e3 / args.steps,
-                "iters_mean": float(it.mean()), "iters_max": int(it.max()), "launches": launches * args.steps,
-                "x": x_dev.cpu().numpy(), "status": st}
-
-    spec_info = None
-    try:
-        kname, csec = plan.specialize("op")
-        spec_info = {"kernel": kname, "nvrtc_s": csec}
-    except RuntimeError as e:  # no per-topology kernel: everything runs on the generic one
-        spec_info = {"kernel": None, "error": str(e)[:200]}
-    spec_ok = spec_info["kernel"] is not None
-    plain_opt = analysis.Options(reltol=RELTOL, precision="fp64", kernel="generic")
-    chosen_opt = analysis.Options(reltol=RELTOL, precision=args.precision,
-                                  kernel="specialized" if spec_ok else "generic")
-    clk = Clocks(os.path.join(tempfile.gettempdir(),
-                              "bench_clocks_%d.csv" % rank))
-    variants = {}
-    with clk:
-        plain = timed(plain_opt, False)
-        chosen = timed(chosen_opt, True)
-        if args.variants:  # each ingredient of the chosen path alone and combined
-            for kern in (["generic", "specialized"] if spec_ok else ["generic"]):
-                for prec in ("fp64", "mixed"):
-                    for ws in ((False, True) if learned else (False,)):
-                        r = timed(analysis.Options(reltol=RELTOL, precision=prec, kernel=kern), ws)
-                        variants["%s/%s/%s" % (kern, prec, "learned" if ws else "InitJct")] = {
-                            "ms_per_step": r["ms_per_step"], "solves_per_s": r["ok"] * args.steps / r["seconds"],
-                            "newton_iters_mean": r["iters_mean"], "newton_iters_max": r["iters_max"]}
-            # one unchecked FP64-residual pass per Newton step
-            r = timed(dataclasses.replace(chosen_opt, precision="mixed", mixed_passes=1), True)
-            variants["%s/mixed-1pass/learned" % chosen_opt.kernel] = {
-                "ms_per_step": r["ms_per_step"], "solves_per_s": r["ok"] * args.steps / r["seconds"],
-                "newton_iters_mean": r["iters_mean"], "newton_iters_max": r["iters_max"]}
-    clocks = clk.summary(local)
-
-    # end to end through the C ABI: pinned host values in, host solutions out
-    import torch as _t
-    vals_pin = _t.from_numpy(vals.copy()).pin_memory()
-    x_host = np.zeros((B, n))
-    s_host = np.zeros(B, dtype=np.int32)
-    i_host = np.zeros(B, dtype=np.int32)
-    L = __import__("kronspice_gb300._lib", fromlist=["x"]).load()
-    o = chosen_opt.c()
-
-    def e2e_step():
-        rc = L.ks_batch_set_values(batch.handle, ctypes.c_void_p(vals_pin.data_ptr()), 0, sh)
-        assert rc == 0
-        x0p = None
-        if learned:
-            x0 = learned.predict(stream)
-            x0p = x0.data_ptr()
-        if x0p is not None:
-            rc = L.ks_op_async(batch.handle, ctypes.byref(o), ctypes.c_void_p(x0p), x_dev.data_ptr(),
-                               st_dev.data_ptr(), it_dev.data_ptr(), sh)
-            assert rc == 0
-            x_host[:] = x_dev.cpu().numpy()
-            s_host[:] = st_dev.cpu().numpy()
-            i_host[:] = it_dev.cpu().numpy()
-        else:
-            rc = L.ks_op(batch.handle, ctypes.byref(o), None, x_host.ctypes.data, s_host.ctypes.data,
-                         i_host.ctypes.data, sh)
-            assert rc == 0
-    for _ in range(args.warmup):
-        e2e_step()
-    torch.cuda.synchronize()
-    e2e_t = 0.0
-    for _ in range(args.steps):
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e2e_step()
-        torch.cuda.synchronize()
-        e2e_t += time.perf_counter() - t0
-    e2e_value = world * B * args.steps / e2e_t if world == 1 else None
-    if world > 1:
-        t = torch.tensor([e2e_t], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_value = world * B * args.steps / float(t.item())
-
-    value = world * chosen["ok"] * args.steps / chosen["seconds"] if chosen["seconds"] > 0 else 0.0
-    plain_value = world * plain["ok"] * args.steps / plain["seconds"] if plain["seconds"] > 0 else 0.0
+    r = op_workload(args, args.workload, args.n_circ, args.steps, args.warmup, bool(args.variants), args.start_cache,
+                    dev, stream, world, rank)
+    second = None
+    if args.workload == "bjt_ce" and args.secondary:
+        cache2 = None
+        if args.start_cache:
+            base, ext = os.path.splitext(args.start_cache)
+            cache2 = base + "_cmos_opamp" + (ext or ".npz")
+        second = op_workload(args, "cmos_opamp", WORKLOADS["cmos_opamp"][0], DEFAULT_STEPS["cmos_opamp"],
+                             min(args.warmup, 3), True, cache2, dev, stream, world, rank)
     if rank != 0:
         if world > 1:
             torch.distributed.barrier()
         return
 
-    # accuracy of the chosen path against the CPU oracle on a sample
-    from oracle import oracle as orc
-    samp = min(2048, B)
-    so, xo, io = orc.batch_op(orc.Packed(el, nn, vals[:samp]), samp, orc.options(reltol=RELTOL))
-    okm = (so == 0) & (chosen["status"][:samp] == 0)
-    max_err = float(np.max(np.abs(chosen["x"][:samp][okm, :nn - 1] - xo[okm, :nn - 1]))) if okm.any() else None
-    cpu = cpu_baseline(el, nn, vals)
-
+    B, n, chosen = r["B"], r["n"], r["chosen"]
+    cpu = cpu_baseline(r["el"], r["nn"], r["vals"])
     per_launch_s = chosen["op_kernel_s"]  # the operating-point kernel alone (events around its launch)
+    kname = "ks_spec_op" if r["chosen_opt"].kernel == "specialized" else "k_op"
     # algorithmic bytes of one solve: its value vector in, its solution, status and iteration count out
-    nv = vals.shape[1]
+    nv = r["vals"].shape[1]
     alg_bytes = (nv + n) * 8 + 8
     achieved = alg_bytes * B / per_launch_s / 1e9
     peaks = {}
@@ -1228,45 +1280,84 @@ def main():
     except OSError:
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
-    prof = traffic_from_profile().get("%s_%s" % ("ks_spec_op" if chosen_opt.kernel == "specialized" else "k_op",
-                                                 args.workload), {})
+    prof = traffic_from_profile().get("%s_%s" % (kname, args.workload), {})
     traffic = prof.get("dram_bytes_per_circuit")
+    # FP64 roofline: the kernel's FP64 operations per circuit (ncu instruction
+    # counts of the same launch) over its event time, against this device's FP64
+    # FMA rate measured now
+    fp64_peak, fma_clk = ctypes.c_double(), ctypes.c_double()
+    L = _lib.load()
+    fp64 = None
+    if L.ks_fp64_peak(ctypes.byref(fp64_peak), ctypes.byref(fma_clk)) == 0:
+        flops_c = prof.get("fp64_flops_per_circuit")
+        fp64 = {"bound": "fp64", "peak": fp64_peak.value / 1e12, "unit": "TFLOP/s",
+                "peak_fma_lanes_per_clk_per_sm": fma_clk.value,
+                "peak_source": "ks_fp64_peak: FMA chains on every SM of this device, measured in this run",
+                "achieved": None if flops_c is None else flops_c * B / per_launch_s / 1e12,
+                "flops_per_circuit": flops_c, "kernel": kname,
+                "lanes_per_fp64_instruction": prof.get("fp64_lanes_per_instruction"),
+                "source": prof.get("source")}
+        if fp64["achieved"] is not None:
+            fp64["frac"] = fp64["achieved"] / fp64["peak"]
+    plain = r["plain"]
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": chosen["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64 device eval + residual, f32 LU" if args.precision == "mixed" else "f64", "data": "synthetic (seeded Philox)",
-        "config": {"workload": "%s_op_%d" % (args.workload, B), "n_circuits_per_gpu": B, "n_unknowns": n, "reltol": RELTOL,
-                   "abstol": 1e-12, "l2": "flushed between timed steps (512 MB write)",
-                   "learned_start": learned is not None},
-        "plain": {"value": plain_value, "ms_per_step": plain["ms_per_step"], "newton_iters_mean": plain["iters_mean"],
-                  "newton_iters_max": plain["iters_max"], "precision": "fp64", "start": "InitJct"},
-        "chosen": {"value": value, "newton_iters_mean": chosen["iters_mean"], "newton_iters_max": chosen["iters_max"],
+        "dtype": "f64 device eval + residual, f32 LU" if args.precision == "mixed" else "f64",
+        "data": "synthetic (seeded Philox)",
+        "config": {"workload": "%s_op_%d" % (args.workload, B), "n_circuits_per_gpu": B, "n_unknowns": n,
+                   "reltol": RELTOL, "abstol": 1e-12, "l2": "flushed between timed steps (512 MB write)",
+                   "learned_start": True, "fp32_start_iters": r["s32"]},
+        "plain": {"value": r["plain_value"], "ms_per_step": plain["ms_per_step"],
+                  "newton_iters_mean": plain["iters_mean"], "newton_iters_max": plain["iters_max"],
+                  "precision": "fp64", "kernel": "generic", "start": "InitJct"},
+        "chosen": {"value": r["value"], "ms_per_step": chosen["ms_per_step"],
+                   "newton_iters_mean": chosen["iters_mean"], "newton_iters_max": chosen["iters_max"],
+                   "newton_iters_note": "FP64 Newton solves per circuit (the FP32 stage's iterations not counted)",
                    "precision": "fp32 LU + fp64 residual" if args.precision == "mixed" else "fp64",
-                   "kernel": chosen_opt.kernel, "start": "learned (MLP)" if learned is not None else "InitJct"},
-        "per_topology_kernel": spec_info,
-        "variants": variants or None,
-        "chosen_vs_plain": value / plain_value if plain_value else None,
-        "learned_start": None if learned is None else learned.info,
-        "max_node_voltage_err_vs_oracle": max_err,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(vals.nbytes),
-                "d2h_bytes_per_step": int(x_host.nbytes + s_host.nbytes + i_host.nbytes)},
+                   "kernel": r["chosen_opt"].kernel,
+                   "start": "learned (MLP) refined by the FP32 Newton stage; basin check at %.3g V"
+                            % r["chosen_opt"].start_check},
+        "per_topology_kernel": r["spec_info"],
+        "variants": r["variants"] or None,
+        "chosen_vs_plain": r["value"] / r["plain_value"] if r["plain_value"] else None,
+        "learned_start": r["learned"],
+        "one_time_costs": r["one_time"],
+        "parity_vs_oracle": r["parity"],
+        "max_node_voltage_err_vs_oracle": r["parity"]["max_node_voltage_err_v"],
+        "e2e": r["e2e"],
         "gpu_launches": chosen["launches"],
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak,
-                     "traffic": None if traffic is None else traffic * B,
-                     "kernel": "ks_spec_op" if chosen_opt.kernel == "specialized" else "k_op",
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None if traffic is None else traffic * B, "kernel": kname,
                      "algorithmic_bytes_per_solve": alg_bytes, "kernel_ms": per_launch_s * 1e3,
-                     "note": "the operating-point kernel is bound by FP64 issue (GB300: 2 FP64 lanes/clk/SM; one "
-                             "circuit per thread), not by HBM: achieved counts the value vector in and the "
-                             "solution out per solve over the launch's event time, peak is the measured copy "
-                             "bandwidth"},
+                     "note": "the operating-point kernel is bound by FP64 issue, not by HBM: achieved counts the "
+                             "value vector in and the solution out per solve over the launch's event time, peak "
+                             "is the measured copy bandwidth; roofline_fp64 gives the FP64 fraction"},
+        "roofline_fp64": fp64,
         "cpu_baseline": cpu,
-        "clocks": clocks,
+        "clocks": r["clocks"],
     }
+    if second is not None:
+        s2 = second
+        line["cmos_opamp"] = {
+            "config": {"workload": "cmos_opamp_op_%d" % s2["B"], "n_unknowns": s2["n"], "steps": s2["steps"],
+                       "fp32_start_iters": s2["s32"]},
+            "plain": {"value": s2["plain_value"], "ms_per_step": s2["plain"]["ms_per_step"],
+                      "newton_iters_mean": s2["plain"]["iters_mean"], "newton_iters_max": s2["plain"]["iters_max"]},
+            "chosen": {"value": s2["value"], "ms_per_step": s2["chosen"]["ms_per_step"],
+                       "newton_iters_mean": s2["chosen"]["iters_mean"], "newton_iters_max": s2["chosen"]["iters_max"],
+                       "kernel": s2["chosen_opt"].kernel},
+            "chosen_vs_plain": s2["value"] / s2["plain_value"] if s2["plain_value"] else None,
+            "variants": s2["variants"], "learned_start": s2["learned"], "one_time_costs": s2["one_time"],
+            "parity_vs_oracle": s2["parity"], "e2e": s2["e2e"], "clocks": s2["clocks"]}
     print(json.dumps(line))
     if world > 1:
         torch.distributed.barrier()
+    # a chosen path whose results leave the oracle's tolerance is not a result
+    if not r["parity"]["ok"] or (second is not None and not second["parity"]["ok"]):
+        sys.stderr.write("bench: chosen path fails parity against the oracle\n")
+        sys.exit(3)
 
 
 if __name__ == "__main__":

@@ -194,7 +194,26 @@ typedef struct {
                              to FP64.  1: one unchecked pass, each Newton step
                              the FP32 solve of the FP64 residual
                              (well-conditioned systems only). */
-  int32_t reserved;
+  int32_t fp32_start_iters; /* operating points (ks_op, ks_ac): > 0 runs an FP32
+                             stage of at most this many Newton iterations from the
+                             start (x0, or InitJct without one), with the devices
+                             evaluated and the system factored in FP32 and
+                             dcSolve's gmin / source stepping when Newton fails,
+                             and starts the FP64 solve from the point it reaches
+                             (NodeSet semantics).  The FP64 Newton, its convergence
+                             test and its fallback chain are unchanged, so the
+                             stage changes how many FP64 iterations a circuit
+                             takes, not its result.  Circuits whose stage fails
+                             keep their start.  Covers R, C, L, V, I, diodes, BJTs
+                             and level-1 MOSFETs; other topologies skip it.
+                             0: off. */
+  double start_check;     /* operating points with x0: > 0 solves a circuit again
+                             from the standard start (InitJct and the full dcSolve
+                             chain) when its solution ends farther than this many
+                             volts from x0 at any node: the check a learned start
+                             uses to catch a prediction that led Newton to another
+                             operating point.  Its iterations count in out_iters.
+                             0: no check. */
 } ks_options;
 
 /* ---- transient request (analysis/tran.go:26-59) ------------------------- */
@@ -481,6 +500,14 @@ int ks_torn_tran(ks_torn* t, const ks_tran_spec* spec, const ks_options* opt, in
 
 /* Predicted starting points x0_dev [n_circ][n] (device memory) for ks_op_async. */
 int ks_mlp_predict(ks_mlp* m, ks_batch* b, double* x0_dev, void* stream);
+
+/* ---- measurement ----------------------------------------------------------
+ * No counterpart in the reference.  FP64 throughput of the current device: FMA
+ * chains on every SM (16 warps, eight independent chains per lane), the fastest
+ * of three timed runs.  *flops_per_s counts an FMA as two operations;
+ * *fma_per_clk_per_sm (optional) is FMA lanes per SM clock at the device's
+ * rated clock.  The denominator of FP64 roofline fractions. */
+int ks_fp64_peak(double* flops_per_s, double* fma_per_clk_per_sm);
 #endif /* __CUDACC_RTC__ */
 
 #ifdef __cplusplus

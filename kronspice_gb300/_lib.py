@@ -21,7 +21,8 @@ class KsOptions(ctypes.Structure):
                 ("no_gmin_stepping", ctypes.c_int32), ("no_source_stepping", ctypes.c_int32),
                 ("no_pseudo_transient", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("backend", ctypes.c_int32), ("max_iter_total", ctypes.c_int32),
-                ("deadline_s", ctypes.c_double), ("mixed_passes", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("deadline_s", ctypes.c_double), ("mixed_passes", ctypes.c_int32),
+                ("fp32_start_iters", ctypes.c_int32), ("start_check", ctypes.c_double)]
 
 
 class KsTranSpec(ctypes.Structure):
@@ -38,7 +39,8 @@ EXPORTS = ["ks_version", "ks_last_error", "ks_validate", "ks_unknowns", "ks_plan
            "ks_batch_last_kernel", "ks_op_noalloc", "ks_op_noalloc_scratch_bytes", "ks_multi_create",
            "ks_multi_destroy", "ks_multi_info", "ks_multi_op", "ks_multi_op_async", "ks_multi_tran",
            "ks_multi_tran_async", "ks_sparse_analyze", "ks_ac", "ks_ac_async", "ks_ac_at", "ks_torn_create",
-           "ks_torn_destroy", "ks_torn_plan", "ks_torn_set_stream", "ks_torn_info", "ks_torn_op", "ks_torn_tran"]
+           "ks_torn_destroy", "ks_torn_plan", "ks_torn_set_stream", "ks_torn_info", "ks_torn_op", "ks_torn_tran",
+           "ks_fp64_peak"]
 
 _lib = None
 
@@ -102,6 +104,7 @@ def load(build_if_missing=False):
     L.ks_torn_info.argtypes = [P, P, P, P, P, P]
     L.ks_torn_op.argtypes = [P, P, ctypes.c_int32, P, P, P, P]
     L.ks_torn_tran.argtypes = [P, P, P, ctypes.c_int32, P, ctypes.c_int32, P, P, P, P, P, P]
+    L.ks_fp64_peak.argtypes = [P, P]
     _lib = L
     return L
 

@@ -85,12 +85,15 @@ class Options:
     deadline_s: float = 0.0
     kernel: str = "auto"
     mixed_passes: int = 0
+    fp32_start_iters: int = 0   # FP32 Newton stage before the FP64 solve (operating points; 0: off)
+    start_check: float = 0.0    # re-solve from InitJct when the solution ends this far (V) from x0 (0: off)
 
     def c(self):
         return _lib.KsOptions(self.reltol, self.abstol, self.vntol, self.gmin, self.itl1, self.itl4,
                               int(self.no_gmin_stepping), int(self.no_source_stepping),
                               int(self.no_pseudo_transient), PREC[self.precision], KERNEL[self.kernel],
-                              self.max_iter_total, self.deadline_s, self.mixed_passes, 0)
+                              self.max_iter_total, self.deadline_s, self.mixed_passes, int(self.fp32_start_iters),
+                              float(self.start_check))
 
 
 def _check(rc, what):

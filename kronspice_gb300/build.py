@@ -19,10 +19,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "550"]
 
 UNITS = ["ks_host.cpp", "ks_api.cu", "ks_kernels.cu", "ks_tran.cu", "ks_mlp.cu", "ks_jit.cpp", "ks_noalloc.cu", "ks_ac.cu", "ks_torn.cu", "ks_sparse.cpp",
-         "ks_multi.cu"]
+         "ks_multi.cu", "ks_peak.cu"]
 # device headers embedded in the library for the per-topology kernels (NVRTC),
 # under the names their #include lines use
-JIT_HEADERS = [("ks_tran.cuh", "ks_tran.cuh"), ("ks_newton.cuh", "ks_newton.cuh"), ("ks_solve.cuh", "ks_solve.cuh"),
+JIT_HEADERS = [("ks_tran.cuh", "ks_tran.cuh"), ("ks_newton.cuh", "ks_newton.cuh"), ("ks_start32.cuh", "ks_start32.cuh"),
+               ("ks_solve.cuh", "ks_solve.cuh"),
                ("ks_devices.cuh", "ks_devices.cuh"), ("ks_mos.cuh", "ks_mos.cuh"), ("ks_engine.h", "ks_engine.h"),
                ("../../include/kronspice_gpu.h", os.path.join("..", "..", "include", "kronspice_gpu.h"))]
 

@@ -96,6 +96,8 @@ static KOpts make_opts(const ks_options* o) {  // analysis/op.go:91-110
   // linear ones, whose single solve per point is final, refine to 1e-11)
   k.refine_tol = std::min(1e-9, 1e-3 * k.reltol);
   k.max_iter_total = o ? o->max_iter_total : 0;
+  k.start32 = o && o->fp32_start_iters > 0 ? std::min(o->fp32_start_iters, 100000) : 0;
+  k.start_check = o && o->start_check > 0 ? o->start_check : 0.0;
   return k;
 }
 
@@ -187,7 +189,10 @@ extern "C" int ks_batch_create(ks_plan* plan, int32_t n_circ, const double* valu
       cudaMalloc(&b->d_x0, sizeof(double) * hp.n * B) != cudaSuccess ||
       cudaMalloc(&b->d_status, sizeof(int32_t) * B) != cudaSuccess ||
       cudaMalloc(&b->d_iters, sizeof(int32_t) * B) != cudaSuccess ||
-      cudaMalloc(&b->dev.queue, 64) != cudaSuccess) {
+      cudaMalloc(&b->dev.queue, 64) != cudaSuccess ||
+      cudaMalloc(&b->dev.values32, sizeof(float) * hp.n_values * B) != cudaSuccess ||
+      cudaMalloc(&b->dev.derived32, sizeof(float) * (hp.n_derived + 1) * B) != cudaSuccess ||
+      cudaMalloc(&b->dev.state32, sizeof(float) * (hp.n_state + 1) * B) != cudaSuccess) {
     set_error("ks_batch_create: device allocation failed");
     return fail(KS_ENOMEM);
   }
@@ -223,6 +228,7 @@ extern "C" void ks_batch_destroy(ks_batch* b) {
   if (!b) return;
   cudaFree(b->dev.values); cudaFree(b->dev.derived); cudaFree(b->dev.state); cudaFree(b->dev.work);
   cudaFree(b->dev.queue);
+  cudaFree(b->dev.values32); cudaFree(b->dev.derived32); cudaFree(b->dev.state32);
   cudaFree(b->d_rows); cudaFree(b->d_x); cudaFree(b->d_x0); cudaFree(b->d_status); cudaFree(b->d_iters);
   if (b->h_pin) cudaFreeHost(b->h_pin);
   cudaFree(b->d_wave);

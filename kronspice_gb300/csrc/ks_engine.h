@@ -87,7 +87,9 @@ struct KOpts {
   int32_t passes;          // mixed: most refinement passes per solve
   double refine_tol;       // mixed: refinement stops when the correction is below this fraction of x
   int32_t polish;          // OP: the polish of analysis/op.go:251-271 (AC operating points)
-  int32_t reserved;
+  int32_t start32;         // OP: most iterations of the FP32 start stage (0: no FP32 stage)
+  double start_check;      // OP with a given start: a circuit whose solution ends farther than this (volts, any
+                           // node) from its start is solved again from the standard start (0: no check)
 };
 
 #ifndef __CUDACC_RTC__

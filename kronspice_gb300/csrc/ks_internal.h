@@ -48,6 +48,11 @@ struct KsDeviceBatch {
   double* state;       // [n_state][B]
   double* work;        // [3*n][B]: save, ptPrev, xacc
   unsigned long long* queue;  // next-circuit counter of the persistent kernels
+  // FP32 copies of values and derived, and the FP32 start stage's state (null:
+  // no FP32 stage for this batch)
+  float* values32 = nullptr;   // [n_values][B]
+  float* derived32 = nullptr;  // [n_derived][B]
+  float* state32 = nullptr;    // [n_state][B]
 };
 
 int ks_launch_transpose(const double* src_rows, double* dst_cols, int64_t rows, int64_t cols, void* stream);

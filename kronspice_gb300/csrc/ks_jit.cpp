@@ -167,9 +167,13 @@ bool symbolic(const ksh::HostPlan& hp, Symbolic* sy) {
 }
 
 // Straight-line factor + solve in type T ("double" or "float"), reading A from
-// the system; mixed = FP32 factor with FP64-residual refinement.
-std::string emit_lu(const Symbolic& sy, bool mixed) {
+// the system.  mode LU_FP64: x = A^-1 rhs in FP64; LU_MIXED: FP32 factor of the
+// FP64 matrix with FP64-residual refinement; LU_F32: the FP32 start stage's
+// system, x32 = a32^-1 r32 entirely in FP32.
+enum { LU_FP64 = 0, LU_MIXED = 1, LU_F32 = 2 };
+std::string emit_lu(const Symbolic& sy, int mode) {
   const int n = sy.n;
+  const bool mixed = mode != LU_FP64;
   const char* T = mixed ? "float" : "double";
   auto C = [&](int k, int l) { return (sy.Cmask[k] >> l) & 1ull; };
   std::string o;
@@ -180,7 +184,8 @@ std::string emit_lu(const Symbolic& sy, bool mixed) {
     for (int l = 0; l < n; l++) {
       if (!C(k, l)) continue;
       bool inA = (sy.Amask[sy.prow[k]] >> sy.q[l]) & 1u;
-      if (inA) snprintf(b, sizeof b, "    %s %s = (%s)s.a(%d, %d);\n", T, f(k, l).c_str(), T, sy.prow[k], sy.q[l]);
+      if (inA && mode == LU_F32) snprintf(b, sizeof b, "    float %s = s.a32(%d, %d);\n", f(k, l).c_str(), sy.prow[k], sy.q[l]);
+      else if (inA) snprintf(b, sizeof b, "    %s %s = (%s)s.a(%d, %d);\n", T, f(k, l).c_str(), T, sy.prow[k], sy.q[l]);
       else snprintf(b, sizeof b, "    %s %s = 0;\n", T, f(k, l).c_str());
       o += b;
     }
@@ -251,6 +256,13 @@ std::string emit_lu(const Symbolic& sy, bool mixed) {
     }
     return r;
   };
+  if (mode == LU_F32) {
+    o += "    {\n" + solve("s.r32", "s.x32") + "    }\n";
+    o += "    int kx = 0;\n";
+    for (int i = 0; i < n; i++) { snprintf(b, sizeof b, "    kx = max(kx, ks_exp32(s.x32(%d)));\n", i); o += b; }
+    o += "    return kx >= 255 ? SOLVE_NONFINITE : SOLVE_OK;\n";
+    return o;
+  }
   if (!mixed) {
     o += "    {\n" + solve("s.rhs", "s.xn") + "    }\n";
     o += "    long long kx = 0;\n";
@@ -323,9 +335,11 @@ std::string source(const ksh::HostPlan& hp, int T, int kind, bool* reg_out) {
     s += "; A columns";
     for (int k = 0; k < hp.n; k++) s += " " + std::to_string(sy.q[k]);
     s += ")\n  template <class SY>\n  __device__ __forceinline__ int lu_fp64(SY& s) const {\n";
-    s += emit_lu(sy, false);
+    s += emit_lu(sy, LU_FP64);
     s += "  }\n  template <class SY>\n  __device__ __forceinline__ int lu_mixed(SY& s, int passes, double rtol) const {\n";
-    s += emit_lu(sy, true);
+    s += emit_lu(sy, LU_MIXED);
+    s += "  }\n  template <class SY>\n  __device__ __forceinline__ int lu_f32(SY& s) const {\n";
+    s += emit_lu(sy, LU_F32);
     s += "  }\n";
   } else {
     s += "  static constexpr bool kStaticLU = false;  // a structurally zero pivot: partial pivoting\n";
@@ -344,11 +358,12 @@ std::string source(const ksh::HostPlan& hp, int T, int kind, bool* reg_out) {
 extern "C" __global__ void __launch_bounds__(KS_T)
 ks_spec_op(KOpts o, const double* __restrict__ values, const double* __restrict__ derived, double* state,
            double* work, int64_t B, const double* __restrict__ x0, double* out_x, int32_t* out_status,
-           int32_t* out_iters, uint64_t deadline_ns, unsigned long long* queue) {
+           int32_t* out_iters, uint64_t deadline_ns, unsigned long long* queue, K32 k32) {
   Thr<Sys, GenProg> t;
   KS_BIND(t)
   t.o = o;
-  op_persistent(t, values, derived, state, work, B, x0, out_x, out_status, out_iters, deadline_ns, queue);
+  op_persistent(t, values, derived, state, work, B, x0, out_x, out_status, out_iters, deadline_ns, queue,
+                k32.values ? &k32 : nullptr);
 }
 )";
   else s += R"(

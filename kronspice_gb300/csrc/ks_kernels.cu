@@ -48,10 +48,30 @@ __global__ void k_setup(KPlan plan, const double* __restrict__ values, double* d
   for (int k = 0; k < plan.n_elem; k++) setup_elem(plan.elem[k], V, D, step, stop);
 }
 
+// FP32 copies of the value and derived-constant columns (the FP32 start stage's inputs).
+__global__ void k_to32(const double* __restrict__ a, float* __restrict__ a32, int64_t na,
+                       const double* __restrict__ b, float* __restrict__ b32, int64_t nb) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < na + nb; i += stride) {
+    if (i < na) a32[i] = (float)a[i];
+    else b32[i - na] = (float)b[i - na];
+  }
+}
+
 int ks_launch_setup(const KsDeviceBatch& b, double step, double stop, void* stream) {
   int tpb = 128;
   unsigned grid = (unsigned)((b.B + tpb - 1) / tpb);
   k_setup<<<grid, tpb, 0, (cudaStream_t)stream>>>(b.plan, b.values, b.derived, b.B, step, stop);
+  if (cudaGetLastError() != cudaSuccess) return -1;
+  if (b.values32 && b.derived32) {
+    const int64_t na = (int64_t)b.plan.n_values * b.B, nb = (int64_t)b.plan.n_derived * b.B;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = (na + nb + 255) / 256, cap = (int64_t)sms * 8;
+    k_to32<<<(unsigned)(want < cap ? want : cap), 256, 0, (cudaStream_t)stream>>>(b.values, b.values32, na, b.derived,
+                                                                                   b.derived32, nb);
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -65,13 +85,14 @@ __global__ void __launch_bounds__(T) k_op(KPlan plan, KOpts o, const double* __r
                                           const double* __restrict__ derived, double* state, double* work,
                                           int64_t B, const double* __restrict__ x0, double* out_x,
                                           int32_t* out_status, int32_t* out_iters, uint64_t deadline_ns,
-                                          unsigned long long* queue) {
+                                          unsigned long long* queue, K32 k32) {
   extern __shared__ __align__(16) unsigned char smem[];
   Thr<SmemSys<T>, RtProg> t;
   smem_layout<T>(t, plan, smem);
   t.o = o;
   __syncthreads();
-  op_persistent(t, values, derived, state, work, B, x0, out_x, out_status, out_iters, deadline_ns, queue);
+  op_persistent(t, values, derived, state, work, B, x0, out_x, out_status, out_iters, deadline_ns, queue,
+                k32.values ? &k32 : nullptr);
 }
 
 // Blocks of T threads that keep every SM full (persistent grid), capped by the work.
@@ -99,7 +120,9 @@ int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, doubl
     double *state = b.state, *work = b.work;
     int64_t B = b.B;
     unsigned long long* queue = b.queue;
-    void* args[] = {&ko, &values, &derived, &state, &work, &B, &x0, &out_x, &out_status, &out_iters, &dl, &queue};
+    K32 k32{b.values32, b.derived32, b.state32};
+    if (!b.values32 || !b.derived32 || !b.state32) k32 = K32{nullptr, nullptr, nullptr};
+    void* args[] = {&ko, &values, &derived, &state, &work, &B, &x0, &out_x, &out_status, &out_iters, &dl, &queue, &k32};
     int64_t need = (B + (int64_t)kspec->T * circuits_per_thread() - 1) / ((int64_t)kspec->T * circuits_per_thread());
     unsigned grid = (unsigned)(need < kspec->blocks ? need : kspec->blocks);
     std::string err;
@@ -115,16 +138,18 @@ int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, doubl
   if (sm > (size_t)maxSmem) return -2;
   cudaStream_t st = (cudaStream_t)stream;
   if (cudaMemsetAsync(b.queue, 0, sizeof(unsigned long long), st) != cudaSuccess) return -1;
+  K32 k32{b.values32, b.derived32, b.state32};
+  if (!b.values32 || !b.derived32 || !b.state32) k32 = K32{nullptr, nullptr, nullptr};
   if (T == 64) {
     cudaFuncSetAttribute(k_op<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     unsigned grid = persistent_grid(k_op<64>, 64, sm, b.B);
     k_op<64><<<grid, 64, sm, st>>>(b.plan, o, b.values, b.derived, b.state, b.work, b.B, x0, out_x, out_status,
-                                   out_iters, dl, b.queue);
+                                   out_iters, dl, b.queue, k32);
   } else {
     cudaFuncSetAttribute(k_op<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     unsigned grid = persistent_grid(k_op<32>, 32, sm, b.B);
     k_op<32><<<grid, 32, sm, st>>>(b.plan, o, b.values, b.derived, b.state, b.work, b.B, x0, out_x, out_status,
-                                   out_iters, dl, b.queue);
+                                   out_iters, dl, b.queue, k32);
   }
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -8,7 +8,7 @@
 //                                stepping, pseudo-transient continuation)
 // with every loop bounded by the reference's own limits.
 #pragma once
-#include "ks_solve.cuh"
+#include "ks_start32.cuh"
 
 namespace ksg {
 
@@ -186,20 +186,45 @@ __device__ __forceinline__ void x_zero(Thr<SY, P>& t, const Col& also) {
 }
 
 // dcSolve start, analysis/newton.go:96-102, with applyNodeSet (:221-243) when x0
-// holds a starting point (node voltages; other unknowns start at 0).
+// holds a starting point (node voltages; other unknowns start at 0).  With the
+// FP32 start stage on (k32, o.start32 > 0; one thread per circuit), the point the
+// stage reaches from x0 (or from InitJct when x0 is null) is the NodeSet instead;
+// where the stage fails the start is x0 (or InitJct) as without it.
 template <class SY, class P>
-__device__ __forceinline__ void dc_start(Thr<SY, P>& t, OpState& st, const double* x0, int64_t c) {
+__device__ __forceinline__ void dc_start(Thr<SY, P>& t, OpState& st, const double* x0, int64_t c,
+                                         const K32* k32 = nullptr, int64_t B = 0) {
   op_state_reset(st, t.o);
   const int n = t.n();
+  bool seeded = false;
+  if constexpr (!P::kWarp) {
+    if (k32 && t.o.start32 > 0) seeded = start32(t, *k32, x0, c, B, t.o.start32);
+  }
+  if (!seeded) {
 #pragma unroll
-  for (int i = 0; i < n; i++) t.s.xn(i) = 0.0;
-  if (x0) {
+    for (int i = 0; i < n; i++) t.s.xn(i) = 0.0;
+    if (x0) {
 #pragma unroll
-    for (int i = 0; i < n; i++)
-      if (i < t.prog.n_nodes - 1) t.s.xn(i) = x0[c * n + i];
+      for (int i = 0; i < n; i++)
+        if (i < t.prog.n_nodes - 1) t.s.xn(i) = x0[c * n + i];
+      seeded = true;
+    }
+  }
+  if (seeded) {
     accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, ModeOP, t.o.gmin, true);
     st.initJct = false;
   }
+}
+
+// The learned start's own check: largest distance of a node voltage of the
+// solution from the start x0.
+template <class SY, class P>
+__device__ __forceinline__ double start_distance(Thr<SY, P>& t, const double* x0, int64_t c) {
+  const int n = t.n();
+  long long k = 0;
+#pragma unroll
+  for (int i = 0; i < n; i++)
+    if (i < t.prog.n_nodes - 1) k = key_max(k, mag_key(t.s.xn(i) - x0[c * n + i]));
+  return key_mag(k);
 }
 
 // Advance dcSolve with the result of a finished newton() call.  Sets st.phase to
@@ -342,7 +367,8 @@ __device__ __forceinline__ int polish(Thr<SY, P>& t, OpState& st, const LoadPara
 template <class SY, class P>
 __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* values, const double* derived, double* state,
                                      double* work, int64_t B, const double* x0, double* out_x, int32_t* out_status,
-                                     int32_t* out_iters, uint64_t deadline_ns, unsigned long long* queue) {
+                                     int32_t* out_iters, uint64_t deadline_ns, unsigned long long* queue,
+                                     const K32* k32 = nullptr) {
   const uint64_t t0 = deadline_ns ? prog_clock(t.prog) : 0;
   const KOpts& o = t.o;
   const int maxTotal = o.max_iter_total > 0 ? o.max_iter_total : 3300 * o.itl1 + 16;
@@ -350,11 +376,12 @@ __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* value
   lp.mode = ModeOP; lp.method = BE; lp.time = 0; lp.h = 0; lp.rh = 0; lp.initJct = false; lp.gmin = o.gmin;
   lp.srcStepping = false; lp.srcFact = 0;
   OpState st;
+  bool restarted = false;  // the circuit is being solved again from the standard start
   int64_t c = prog_next(t.prog, queue);
   if (c < B) {
     thr_bind(t, values, derived, state, work, B, c);
     init_state(t.prog, t.D, t.Sb);
-    dc_start(t, st, x0, c);
+    dc_start(t, st, x0, c, k32, B);
   }
   while (c < B) {
     bool done = false;
@@ -366,6 +393,18 @@ __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* value
       done = st.phase == PH_DONE;
     }
     if (!done) continue;
+    // a solution far from the learned start: the start led Newton elsewhere (another
+    // basin of a circuit with several operating points, or a prediction too poor
+    // to trust); solve the circuit again as the reference does, from InitJct
+    if (x0 && !restarted && t.o.start_check > 0 && st.status == KS_STATUS_OK &&
+        start_distance(t, x0, c) > t.o.start_check) {
+      const int spent = st.total;
+      restarted = true;
+      init_state(t.prog, t.D, t.Sb);
+      dc_start(t, st, nullptr, c);
+      st.total = spent;
+      continue;
+    }
     if (st.status == KS_STATUS_OK) accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, ModeOP, o.gmin, false);
     if (st.status == KS_STATUS_OK && o.polish && !t.prog.nonlin_empty) {
       st.status = polish(t, st, lp);
@@ -380,10 +419,11 @@ __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* value
     if (out_status) out_status[c] = st.status;
     if (out_iters) out_iters[c] = st.total;
     c = prog_next(t.prog, queue);
+    restarted = false;
     if (c < B) {
       thr_bind(t, values, derived, state, work, B, c);
       init_state(t.prog, t.D, t.Sb);
-      dc_start(t, st, x0, c);
+      dc_start(t, st, x0, c, k32, B);
     }
   }
 }

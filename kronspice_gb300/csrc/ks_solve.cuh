@@ -39,6 +39,13 @@ struct SmemSys {
   __device__ __forceinline__ double& col(int i) { return col_[i * T]; }
   __device__ __forceinline__ int& piv(int i) { return piv_[i * T]; }
   __device__ __forceinline__ float& l(int i, int j) { return L_[(i * size() + j) * T]; }
+  // FP32 start stage: the matrix in the FP32 factor's storage, the vectors in
+  // the low halves of the FP64 rhs / x / x_old / col slots (unused while it runs)
+  __device__ __forceinline__ float& a32(int i, int j) { return l(i, j); }
+  __device__ __forceinline__ float& r32(int i) { return *reinterpret_cast<float*>(rhs_ + i * T); }
+  __device__ __forceinline__ float& x32(int i) { return *reinterpret_cast<float*>(x_ + i * T); }
+  __device__ __forceinline__ float& xo32(int i) { return *reinterpret_cast<float*>(xold_ + i * T); }
+  __device__ __forceinline__ float& sv32(int i) { return *reinterpret_cast<float*>(col_ + i * T); }
 };
 
 // Register system of compile-time size N.
@@ -52,6 +59,7 @@ struct RegSys {
   double A_[N * N], rhs_[N], x_[N], xold_[N], col_[N];
   int piv_[N];
   float L_[N * N];
+  float r32_[N], x32_[N], xo32_[N], sv32_[N];  // FP32 start stage (the matrix is L_)
   __device__ __forceinline__ static constexpr int size() { return N; }
   __device__ __forceinline__ double& a(int i, int j) { return A_[i * N + j]; }
   __device__ __forceinline__ double& rhs(int i) { return rhs_[i]; }
@@ -60,6 +68,11 @@ struct RegSys {
   __device__ __forceinline__ double& col(int i) { return col_[i]; }
   __device__ __forceinline__ int& piv(int i) { return piv_[i]; }
   __device__ __forceinline__ float& l(int i, int j) { return L_[i * N + j]; }
+  __device__ __forceinline__ float& a32(int i, int j) { return L_[i * N + j]; }
+  __device__ __forceinline__ float& r32(int i) { return r32_[i]; }
+  __device__ __forceinline__ float& x32(int i) { return x32_[i]; }
+  __device__ __forceinline__ float& xo32(int i) { return xo32_[i]; }
+  __device__ __forceinline__ float& sv32(int i) { return sv32_[i]; }
 };
 
 // breakdownVoltage, device/diode.go:166-187.

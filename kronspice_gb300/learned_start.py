@@ -120,11 +120,17 @@ def features_host(vals, cols, logmask):
 
 
 class LearnedStart:
-    """A trained MLP bound to one batch: predict() fills x0 for ks_op_async."""
-    launches_per_step = 6  # features, four GEMMs, decode
+    """A trained MLP bound to one batch: predict() fills x0 for ks_op_async.
+
+    start_check (volts) is the network's own error bound: a circuit whose
+    solution ends farther than this from its prediction at any node is solved
+    again from the standard start (ks_options.start_check), which catches a
+    prediction that led Newton to another operating point."""
+    launches_per_step = 1  # the fused inference kernel
 
     def __init__(self, mlp, batch, x0, info):
         self.mlp, self.batch, self.x0, self.info = mlp, batch, x0, info
+        self.start_check = float(info.get("start_check_v", 0.0))
 
     def predict(self, stream):
         self.mlp.predict(self.batch, self.x0.data_ptr(), ctypes.c_void_p(stream.cuda_stream))
@@ -197,9 +203,22 @@ def train_for(name, el, nn, vals, batch, device, n_train=131072, epochs=40, mb=2
                                 float(lr_r), sh))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t1
+    # the network's error on its training circuits sets its basin check: at least
+    # four times the 99.9th percentile and 1.5 times the largest node-voltage error
+    # (a solution that far from its prediction is not the network's usual miss)
+    # and 0.1 V
+    xp = torch.zeros((n_train, n), dtype=torch.float64, device=device)
+    mlp.predict(tb, xp.data_ptr(), sh)
+    torch.cuda.synchronize()
+    pe = np.abs(xp.cpu().numpy()[ok, :dout] - xs[ok, :dout]).max(axis=1)
+    check = max(0.1, 4.0 * float(np.percentile(pe, 99.9)), 1.5 * float(pe.max()))
+    del xp
     x0 = torch.zeros((batch.n_circ, n), dtype=torch.float64, device=device)
     info = {"n_train": int(n_use), "epochs": epochs, "minibatch": mb, "final_loss": losses[-1],
-            "train_solve_s": t_solve, "train_s": t_train, "hidden": hidden, "layers": "in-%d-%d-%d-out" % (hidden, hidden, hidden)}
+            "train_solve_s": t_solve, "train_s": t_train, "hidden": hidden, "layers": "in-%d-%d-%d-out" % (hidden, hidden, hidden),
+            "pred_err_v": {"p50": float(np.percentile(pe, 50)), "p99": float(np.percentile(pe, 99)),
+                           "p99.9": float(np.percentile(pe, 99.9)), "max": float(pe.max())},
+            "start_check_v": check}
     del tb
     return LearnedStart(mlp, batch, x0, info)
 

@@ -142,8 +142,12 @@ def cmos_opamp_template():
     """Two-stage Miller op-amp in unity-gain feedback (level-1 MOSFETs): NMOS input
     pair M1/M2 with PMOS mirror load M3/M4 and tail M5, PMOS common-source second
     stage M6 with NMOS current-source load M7, bias mirror M8 fed by RB, Miller
-    capacitor CC and load CL.  The output drives the inverting input, so the
-    operating point is defined: v(out) follows the common-mode input VCM."""
+    capacitor CC and load CL.  The output drives the inverting input, the gate of
+    M1 (the input on the mirror's diode side: raising it lowers v(out) through the
+    mirror and the inverting second stage), and VCM the non-inverting gate of M2.
+    The loop is negative feedback, so the operating point is unique: v(out)
+    follows VCM.  (Fed back to M2's gate, the loop would be positive and every
+    variant would have three operating points, two of them at the rails.)"""
     b = Builder("two-stage cmos op-amp")
     b.voltage_source("VDD", "vdd", "0", 5.0)
     b.voltage_source("VCM", "inp", "0", 2.5)
@@ -151,8 +155,8 @@ def cmos_opamp_template():
     b.model("nch", "nmos", {"level": 1, "vto": 0.6, "kp": 100e-6, "lambda": 0.04, "gamma": 0.4, "phi": 0.7})
     b.model("pch", "pmos", {"level": 1, "vto": -0.6, "kp": 40e-6, "lambda": 0.05, "gamma": 0.45, "phi": 0.7})
     L = 1e-6
-    b.mosfet("M1", "n1", "inp", "tail", "0", "nch", {"l": L, "w": 10 * L})
-    b.mosfet("M2", "n2", "out", "tail", "0", "nch", {"l": L, "w": 10 * L})
+    b.mosfet("M1", "n1", "out", "tail", "0", "nch", {"l": L, "w": 10 * L})
+    b.mosfet("M2", "n2", "inp", "tail", "0", "nch", {"l": L, "w": 10 * L})
     b.mosfet("M3", "n1", "n1", "vdd", "vdd", "pch", {"l": L, "w": 20 * L})
     b.mosfet("M4", "n2", "n1", "vdd", "vdd", "pch", {"l": L, "w": 20 * L})
     b.mosfet("M5", "tail", "nb", "0", "0", "nch", {"l": L, "w": 20 * L})

@@ -118,3 +118,40 @@ def test_fused_inference_matches_cpu_network():
     y_gpu = (got[:, :nn - 1] / sc[:, None] - tmean) / tstd
     assert np.all(np.abs(y_gpu - Y) <= 0.03 + 0.02 * np.abs(Y)), np.abs(y_gpu - Y).max()
     assert np.all(got[:, nn - 1:] == 0.0)
+
+
+@pytest.mark.gpu
+def test_opamp_learned_start_matches_oracle_on_bench_seed():
+    """The op-amp workload's chosen path: the network trained on the GPU on
+    plain-solver operating points, its prediction refined by the FP32 Newton
+    stage, FP32 LU with FP64 residual, the learned start's basin check, on the
+    first 8,192 circuits of the bench's batch (65,536 variants, seed 0).  Every
+    status must equal the oracle's and every node voltage must lie within
+    reltol 1e-6 / vntol 1e-6 V of it; the learned start must cut the FP64 Newton
+    iterations against the standard start."""
+    import torch
+    from kronspice_gb300 import analysis, build, learned_start as ls, workloads
+    from oracle import oracle as orc
+    build.build()
+    dev = torch.device("cuda", 0)
+    el, nn, vals = workloads.cmos_opamp_batch(65536, seed=0)
+    vals = np.ascontiguousarray(vals[:8192])
+    batch = analysis.Batch(analysis.Plan(el, nn, vals.shape[1]), vals)
+    start = ls.train_for("cmos_opamp", el, nn, vals, batch, dev, n_train=262144, epochs=40)
+    assert start.start_check > 0
+    stream = torch.cuda.current_stream(dev)
+    x0 = start.predict(stream)
+    torch.cuda.synchronize()
+    x0h = x0.cpu().numpy()
+    so, xo, io = orc.batch_op(orc.Packed(el, nn, vals), len(vals), orc.options(reltol=1e-6))
+    ok = so == 0
+    assert ok.mean() > 0.99
+    chosen = analysis.Options(reltol=1e-6, precision="mixed", fp32_start_iters=6000, start_check=start.start_check)
+    learned_only = analysis.Options(reltol=1e-6, precision="mixed")
+    xp, sp_, ip = batch.op(analysis.Options(reltol=1e-6, precision="fp64"))
+    for opt in (chosen, learned_only):
+        xl, sl, il = batch.op(opt, x0h)
+        assert np.array_equal(sl, so), np.nonzero(sl != so)
+        dv = np.abs(xl[ok, :nn - 1] - xo[ok, :nn - 1])
+        assert np.all(dv <= 1e-6 + 1e-6 * np.abs(xo[ok, :nn - 1])), dv.max()
+        assert np.median(il[ok]) <= 0.25 * np.median(ip[ok]), (np.median(il[ok]), np.median(ip[ok]))
