@@ -14,7 +14,7 @@
  *   solver sentinels       solver/matrix.go:15-20,
  *   analysis sentinels     analysis/newton.go:20, analysis/tran.go:18-22 -> ks_status
  *
- * A Go caller binds these through cgo (see INTEGRATION.md); a Python caller
+ * A Go caller binds these through cgo; a Python caller
  * through ctypes (kronspice_gb300/_lib.py).  Every pointer argument is plain
  * host memory unless the name ends in _dev (device memory).  No function keeps
  * a caller pointer after it returns.  Every function returns a ks_rc.
@@ -331,10 +331,14 @@ int ks_multi_tran_async(ks_multi* m, const ks_tran_spec* spec, const ks_options*
  * [n_circ][n_values] row-major; out_x_dev [n_circ][n], out_status_dev and
  * out_iters_dev [n_circ]: device memory.  Returns KS_EINVAL when the batch needs
  * more scratch than that (ks_op_noalloc_scratch_bytes gives the need).  Runs the
- * generic kernel, standard start.  All calls share the scratch: calls that
- * overlap on the GPU race.  The first call on a device looks up the scratch
- * address; make it before any stream capture.  It returns once the element
- * table is on the device; the solve runs on `stream`. */
+ * generic kernel from the standard start without the FP32 start stage; a
+ * request for the per-topology kernels (KS_BACKEND_SPECIALIZED) is refused with
+ * KS_EUNSUPPORTED, since loading their code allocates device memory.  All calls
+ * share the scratch: calls that overlap on the GPU race.  The first call on a
+ * device looks up the scratch address; make it before any stream capture.  The
+ * call copies the element table to the device on `stream` and waits for that
+ * copy (so it also waits for the work queued on `stream` before it); the solve
+ * itself is queued on `stream` and the call returns without waiting for it. */
 #define KS_NOALLOC_SCRATCH_BYTES (64u << 20)
 int ks_op_noalloc(const ks_topology* topo, int32_t n_circ, const double* values_dev, const ks_options* opt,
                   double* out_x_dev, int32_t* out_status_dev, int32_t* out_iters_dev, void* stream);

@@ -37,7 +37,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[KS_NOALLOC_SCRA
 namespace {
 
 std::mutex g_mu;
-void* g_scratch_dev[64];  // device address of g_noalloc_scratch, per device ordinal
+// Device address of g_noalloc_scratch, per device ordinal, looked up once per
+// process.  A cudaDeviceReset ends the context this address belongs to: a
+// process that resets a device must not call ks_op_noalloc on it again.
+void* g_scratch_dev[64];
 
 // Device address of the scratch array on the current device (set-up on the
 // device's first call).
@@ -85,6 +88,10 @@ extern "C" int ks_op_noalloc(const ks_topology* topo, int32_t n_circ, const doub
   if (!topo || n_circ <= 0 || !values_dev || !out_x_dev || !out_status_dev) {
     set_error("ks_op_noalloc: bad argument");
     return KS_EINVAL;
+  }
+  if (opt && opt->backend == KS_BACKEND_SPECIALIZED) {
+    set_error("ks_op_noalloc: runs the generic kernel only (loading the per-topology kernels allocates device memory)");
+    return KS_EUNSUPPORTED;
   }
   ksh::HostPlan hp;
   std::string err;

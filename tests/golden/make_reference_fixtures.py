@@ -6,7 +6,8 @@ ngspice-39 twins in testdata/golden/ngspice/*.csv -- and writes them, parsed,
 into one JSON fixture, so the tests need no reference checkout at run time.
 Dense ngspice transient tables are thinned to at most 800 rows.
 
-Run in a container that has the reference:  python tests/golden/make_reference_fixtures.py [REF_ROOT]
+Run where a checkout of the reference exists:
+    python tests/golden/make_reference_fixtures.py REF_ROOT
 """
 import json
 import os
@@ -15,7 +16,7 @@ import sys
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 import spice_subset  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = None  # the reference checkout, the script's one argument
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_cases.json")
 
 
@@ -34,6 +35,10 @@ def thin(tab, limit=800):
 
 
 def main():
+    global REF
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_reference_fixtures.py REF_ROOT  (the reference checkout)")
+    REF = sys.argv[1]
     nl_dir = os.path.join(REF, "testdata", "netlists")
     cases = []
     for fn in sorted(os.listdir(nl_dir)):
