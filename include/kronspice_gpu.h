@@ -285,6 +285,16 @@ int ks_batch_create(ks_plan* plan, int32_t n_circ, const double* values, ks_batc
 int ks_batch_set_values(ks_batch* b, const double* values, int values_are_device, void* stream);
 /* KS_KERNEL_* that ran the batch's last analysis (-1 before the first). */
 int ks_batch_last_kernel(const ks_batch* b);
+/* The batch's cancel word, the context cancellation of Options.Context
+ * (analysis/op.go:81-89, checked per Newton iteration, step and frequency there):
+ * an int32 in page-locked host memory mapped into the device's address space,
+ * allocated by the first call and valid until ks_batch_destroy.  While it is
+ * non-zero, the batch's operating-point, AC and transient kernels end every
+ * unfinished circuit with KS_STATUS_INTERRUPTED, the running ones included: each
+ * circuit reads the word before its first Newton iteration and every eighth one
+ * after.  The host writes it from any thread while the kernels run (the Go
+ * wrapper on ctx.Done()); reset it to 0 before the next analysis. */
+int ks_batch_cancel_word(ks_batch* b, volatile int32_t** word);
 
 /* ---- batches of different topologies --------------------------------------
  * analysis.OP / analysis.Tran for n_circ circuits that share nothing: each has

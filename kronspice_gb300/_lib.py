@@ -40,7 +40,7 @@ EXPORTS = ["ks_version", "ks_last_error", "ks_validate", "ks_unknowns", "ks_plan
            "ks_multi_destroy", "ks_multi_info", "ks_multi_op", "ks_multi_op_async", "ks_multi_tran",
            "ks_multi_tran_async", "ks_sparse_analyze", "ks_ac", "ks_ac_async", "ks_ac_at", "ks_torn_create",
            "ks_torn_destroy", "ks_torn_plan", "ks_torn_set_stream", "ks_torn_info", "ks_torn_op", "ks_torn_tran",
-           "ks_fp64_peak"]
+           "ks_fp64_peak", "ks_batch_cancel_word"]
 
 _lib = None
 
@@ -105,6 +105,7 @@ def load(build_if_missing=False):
     L.ks_torn_op.argtypes = [P, P, ctypes.c_int32, P, P, P, P]
     L.ks_torn_tran.argtypes = [P, P, P, ctypes.c_int32, P, ctypes.c_int32, P, P, P, P, P, P]
     L.ks_fp64_peak.argtypes = [P, P]
+    L.ks_batch_cancel_word.argtypes = [P, P]
     _lib = L
     return L
 

@@ -249,6 +249,14 @@ class Batch:
         _check(_lib.load().ks_ac_at(self.handle, ctypes.byref(o), x_op_dev, status_dev, freqs_dev, n_freq, x_dev,
                                     out_status_dev, stream), "ks_ac_at")
 
+    def cancel_word(self):
+        """The batch's cancel word (ks_batch_cancel_word) as a ctypes int32 in
+        mapped page-locked memory: set .value = 1 to interrupt the batch's
+        running analysis, 0 before the next one."""
+        p = ctypes.POINTER(ctypes.c_int32)()
+        _check(_lib.load().ks_batch_cancel_word(self.handle, ctypes.byref(p)), "ks_batch_cancel_word")
+        return p.contents
+
     def op_async(self, opt, x0_dev, x_dev, status_dev, iters_dev, stream):
         """ks_op_async on device pointers (ints) on a CUDA stream handle."""
         o = (opt or Options()).c()

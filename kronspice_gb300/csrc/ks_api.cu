@@ -59,6 +59,9 @@ struct ks_batch {
   size_t d_ac_bytes = 0;
   double* d_acout = nullptr;
   size_t d_acout_bytes = 0;
+  // cancel word (ks_batch_cancel_word): page-locked, mapped for the device
+  int32_t* h_cancel = nullptr;
+  int32_t* d_cancel = nullptr;
 };
 
 // Derived constants for an analysis with print step / stop time (0, 0 outside a transient).
@@ -236,6 +239,7 @@ extern "C" void ks_batch_destroy(ks_batch* b) {
   cudaFree(b->d_tints);
   cudaFree(b->d_ac);
   cudaFree(b->d_acout);
+  if (b->h_cancel) cudaFreeHost(b->h_cancel);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -315,12 +319,33 @@ extern "C" int ks_plan_kernel_source(const ks_plan* plan, int32_t analysis, char
 
 extern "C" int ks_batch_last_kernel(const ks_batch* b) { return b ? b->last_kernel : -1; }
 
+extern "C" int ks_batch_cancel_word(ks_batch* b, volatile int32_t** word) {
+  if (!b || !word) { set_error("ks_batch_cancel_word: null argument"); return KS_EINVAL; }
+  if (!b->h_cancel) {
+    int32_t* h = nullptr;
+    int32_t* d = nullptr;
+    CK(cudaHostAlloc(reinterpret_cast<void**>(&h), 64, cudaHostAllocMapped));
+    *h = 0;
+    cudaError_t e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&d), h, 0);
+    if (e != cudaSuccess) {
+      cudaFreeHost(h);
+      set_error(std::string("ks_batch_cancel_word: ") + cudaGetErrorString(e));
+      return KS_ECUDA;
+    }
+    b->h_cancel = h;
+    b->d_cancel = d;
+  }
+  *word = b->h_cancel;
+  return KS_OK;
+}
+
 extern "C" int ks_op_async(ks_batch* b, const ks_options* opt, const double* x0_dev, double* out_x_dev,
                            int32_t* out_status_dev, int32_t* out_iters_dev, void* stream) {
   if (!b) return KS_EINVAL;
   cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
   const ksh::HostPlan& hp = b->plan->hp;
   KOpts o = make_opts(opt);
+  o.cancel = b->d_cancel;
   (void)hp;
   const KsSpec* ks = nullptr;
   int rc = pick_kernel(b, opt, ksj::KIND_OP, &ks);
@@ -409,6 +434,7 @@ extern "C" int ks_ac_async(ks_batch* b, const ks_options* opt, const double* x0_
   int rc = ac_scratch(b, &s);
   if (rc) return rc;
   KOpts o = make_opts(opt);
+  o.cancel = b->d_cancel;
   o.polish = 1;
   const KsSpec* ks = nullptr;
   rc = pick_kernel(b, opt, ksj::KIND_OP, &ks);
@@ -502,6 +528,7 @@ extern "C" int ks_tran_async(ks_batch* b, const ks_tran_spec* spec, const ks_opt
   if (!spec->fixed_step && capacity <= 0 && (out_time_dev || out_wave_dev)) { set_error("ks_tran: capacity"); return KS_EINVAL; }
   cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
   KOpts o = make_opts(opt);
+  o.cancel = b->d_cancel;
   const KsSpec* ks = nullptr;
   int rc = pick_kernel(b, opt, ksj::KIND_TRAN, &ks);
   if (rc) return rc;

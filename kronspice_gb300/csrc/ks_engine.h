@@ -90,6 +90,7 @@ struct KOpts {
   int32_t start32;         // OP: most iterations of the FP32 start stage (0: no FP32 stage)
   double start_check;      // OP with a given start: a circuit whose solution ends farther than this (volts, any
                            // node) from its start is solved again from the standard start (0: no check)
+  const int32_t* cancel;   // the batch's cancel word (page-locked host memory mapped for the device), or null
 };
 
 #ifndef __CUDACC_RTC__

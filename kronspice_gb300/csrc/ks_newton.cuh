@@ -386,7 +386,9 @@ __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* value
   while (c < B) {
     bool done = false;
     if (deadline_ns && prog_clock(t.prog) - t0 > deadline_ns) { st.status = KS_STATUS_INTERRUPTED; done = true; }
-    else if (st.total >= maxTotal) { st.status = KS_STATUS_NO_CONVERGENCE; done = true; }
+    else if (o.cancel && (st.total & 7) == 0 && prog_cancelled(t.prog, o.cancel)) {  // every 8th solve
+      st.status = KS_STATUS_INTERRUPTED; done = true;
+    } else if (st.total >= maxTotal) { st.status = KS_STATUS_NO_CONVERGENCE; done = true; }
     else {
       int res = newton_step(t, st, lp);
       if (res >= 0) dc_advance(t, st, res);

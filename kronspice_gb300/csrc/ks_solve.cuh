@@ -622,6 +622,16 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
   return t;
 }
 
+// The batch's cancel word, written by the host while the kernel runs: a volatile
+// load of the mapped host word (lane 0's reading for warp programs, so a cancel
+// ends the circuit on all lanes together).
+template <class P>
+__device__ __forceinline__ bool prog_cancelled(const P&, const int32_t* w) {
+  int v = *reinterpret_cast<const volatile int32_t*>(w);
+  if constexpr (P::kWarp) v = __shfl_sync(0xffffffffu, v, 0);
+  return v != 0;
+}
+
 // The wall clock as every lane of a warp program sees it (lane 0's reading), so a
 // deadline ends the circuit on all lanes together.
 template <class P>

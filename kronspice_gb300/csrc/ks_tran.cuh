@@ -206,7 +206,9 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
   while (c < B) {
     if (phase != TR_DONE) {
       if (deadline_ns && prog_clock(t.prog) - t0 > deadline_ns) { status = KS_STATUS_INTERRUPTED; phase = TR_DONE; }
-      else if (st.total >= maxTotal) { status = KS_STATUS_NO_CONVERGENCE; phase = TR_DONE; }
+      else if (o.cancel && (st.total & 7) == 0 && prog_cancelled(t.prog, o.cancel)) {
+        status = KS_STATUS_INTERRUPTED; phase = TR_DONE;
+      } else if (st.total >= maxTotal) { status = KS_STATUS_NO_CONVERGENCE; phase = TR_DONE; }
     }
     if (phase != TR_DONE) {
       int res = newton_step(t, st, lp);
