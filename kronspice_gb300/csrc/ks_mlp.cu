@@ -10,6 +10,7 @@
 // ReLU, the ReLU-backward mask, or split-K atomic accumulation of weight
 // gradients.  Dimensions are padded: batch to 64, feature and output widths to
 // 64, so every tile is full and every 16-byte access aligned.
+#include <cuda.h>  // CUtensorMap and its encoder's signature (the encoder is fetched at run time)
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cmath>
@@ -18,6 +19,7 @@
 #include <string>
 #include <vector>
 #include "ks_internal.h"
+#include "ks_tc.cuh"
 
 using ksh::set_error;
 
@@ -362,6 +364,178 @@ __global__ void __launch_bounds__(256) k_mlp_infer(InferArgs a) {
         }
 }
 
+// ---------------------------------------------------------------- inference on tcgen05
+// The learned start's whole inference in one kernel on the 5th-generation tensor
+// cores: a CTA of 128 threads takes 128 circuits (the MMA's M).  Thread r
+// computes circuit r's standardized features from the SoA values and writes them
+// as BF16 into shared memory in the 128-byte-swizzled K-major layout; TMA
+// (cp.async.bulk.tensor, 128-byte swizzle) brings each layer's BF16 weights
+// W[out][in] into shared memory in the same layout, the next layer's while the
+// current one computes where the buffers allow; one thread issues the layer's
+// tcgen05.mma (M = 128, N = the layer's width, K = 16 per instruction, FP32
+// accumulation in tensor memory) and commits it to an mbarrier; each warp then
+// reads its 32 rows of the accumulator back with tcgen05.ld, adds the bias,
+// applies ReLU and writes the next layer's BF16 operand over the previous one.
+// The output layer is decoded straight into the Newton starting points.
+// Shared memory: activations 64 KB (hidden width <= 256), the hidden layers'
+// weights 128 KB, the first / last layer's weights 32 KB; 256 TMEM columns.
+// Every wait is bounded: a wait that gives up sets *err, writes zero starts for
+// the CTA's circuits, and the CTA still frees its tensor memory.
+constexpr int TC_M = 128;
+constexpr size_t TC_ACT = 65536, TC_WBIG = 131072, TC_WSM = 32768;
+constexpr size_t TC_SMEM = TC_ACT + TC_WBIG + TC_WSM + 64 + 1024;  // + barriers, + alignment slack
+
+struct TcArgs {
+  const double* vals; int64_t B; int n;
+  const int32_t* cols; uint64_t logmask; const float *fmean, *fstd;
+  int din, h, dout;
+  const float* bias[4];
+  const float *tmean, *tstd; int scale_col;
+  double* x0;
+  int* err;
+};
+
+__global__ void __launch_bounds__(128, 1)
+k_mlp_infer_tc(TcArgs a, const __grid_constant__ CUtensorMap tw0, const __grid_constant__ CUtensorMap tw1,
+               const __grid_constant__ CUtensorMap tw2, const __grid_constant__ CUtensorMap tw3) {
+  extern __shared__ __align__(1024) unsigned char sm_raw[];
+  unsigned char* sm = sm_raw + ((1024 - (ktc::smem_u32(sm_raw) & 1023)) & 1023);
+  unsigned char* act = sm;
+  unsigned char* wbig = sm + TC_ACT;
+  unsigned char* wsm = wbig + TC_WBIG;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(wsm + TC_WSM);  // [0] small weights, [1] big weights, [2] MMA
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 3);
+  int* abort_flag = reinterpret_cast<int*>(tslot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, H = a.h, NC = a.h >> 6;
+  const int64_t c = (int64_t)blockIdx.x * TC_M + tid;  // this thread's circuit (its accumulator row)
+  if (tid == 0) {
+    ktc::mbar_init(&bars[0], 1);
+    ktc::mbar_init(&bars[1], 1);
+    ktc::mbar_init(&bars[2], 1);
+    *abort_flag = 0;
+    ktc::mbar_fence_init();
+  }
+  if (warp == 0) ktc::tmem_alloc(tslot, 256);
+  ktc::tc_fence_before();
+  __syncthreads();
+  ktc::tc_fence_after();
+  const uint32_t tmem = *tslot;
+  if (tid == 0) {  // first layer's weights [H][64] and the first hidden layer's [H][H]
+    ktc::tma_prefetch(&tw0); ktc::tma_prefetch(&tw1); ktc::tma_prefetch(&tw2); ktc::tma_prefetch(&tw3);
+    ktc::mbar_expect_tx(&bars[0], (uint32_t)H * 128u);
+    ktc::tma_load_2d(wsm, &tw0, 0, 0, &bars[0]);
+    ktc::mbar_expect_tx(&bars[1], (uint32_t)NC * H * 128u);
+    for (int k = 0; k < NC; k++) ktc::tma_load_2d(wbig + (size_t)k * H * 128, &tw1, 64 * k, 0, &bars[1]);
+  }
+  // features: 64 K-elements (the inputs, then zeros), 8 units of 8 BF16
+#pragma unroll 1
+  for (int u = 0; u < 8; u++) {
+    uint32_t w[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      float f[2];
+#pragma unroll
+      for (int h2 = 0; h2 < 2; h2++) {
+        const int j = u * 8 + e * 2 + h2;
+        f[h2] = 0.f;
+        if (c < a.B && j < a.din) {
+          float x = (float)a.vals[(int64_t)a.cols[j] * a.B + c];
+          if ((a.logmask >> j) & 1) x = logf(x);
+          f[h2] = (x - a.fmean[j]) / a.fstd[j];
+        }
+      }
+      __nv_bfloat162 b2 = __floats2bfloat162_rn(f[0], f[1]);
+      w[e] = *reinterpret_cast<uint32_t*>(&b2);
+    }
+    *reinterpret_cast<uint4*>(act + ktc::sw128_offset(tid, u * 8, TC_M)) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+  ktc::fence_proxy_async();
+  __syncthreads();
+  const uint32_t wait_parity[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};  // (weights barrier, its parity) per layer
+  bool bad = false;
+#pragma unroll 1
+  for (int l = 0; l < 4; l++) {
+    const int N = l == 3 ? 64 : H, KC = l == 0 ? 1 : NC, brows = l == 0 ? H : N;
+    unsigned char* Bs = (l == 1 || l == 2) ? wbig : wsm;
+    if (tid == 0) {
+      if (!ktc::mbar_wait(&bars[wait_parity[l][0]], wait_parity[l][1])) {
+        *abort_flag = 1;
+      } else {
+        ktc::tc_fence_after();
+        const uint32_t idesc = ktc::bf16_idesc(TC_M, N);
+        for (int kc = 0; kc < KC; kc++)
+          for (int ks = 0; ks < 4; ks++) {
+            const uint64_t ad = ktc::sw128_desc(ktc::smem_u32(act) + kc * TC_M * 128 + ks * 32);
+            const uint64_t bd = ktc::sw128_desc(ktc::smem_u32(Bs) + kc * brows * 128 + ks * 32);
+            ktc::mma_bf16(tmem, ad, bd, idesc, (kc | ks) != 0);
+          }
+        ktc::mma_commit(&bars[2]);
+      }
+    }
+    __syncthreads();
+    if (*abort_flag) { bad = true; break; }
+    if (!ktc::mbar_wait(&bars[2], (uint32_t)(l & 1))) bad = true;
+    if (__syncthreads_or(bad)) { bad = true; break; }
+    ktc::tc_fence_after();
+    if (tid == 0 && l == 0) {  // the first layer's weights are consumed: the output layer's [64][H] into their place
+      ktc::mbar_expect_tx(&bars[0], (uint32_t)NC * 64u * 128u);
+      for (int k = 0; k < NC; k++) ktc::tma_load_2d(wsm + (size_t)k * 64 * 128, &tw3, 64 * k, 0, &bars[0]);
+    }
+    if (tid == 0 && l == 1) {  // the first hidden layer's weights are consumed: the second's into their place
+      ktc::mbar_expect_tx(&bars[1], (uint32_t)NC * H * 128u);
+      for (int k = 0; k < NC; k++) ktc::tma_load_2d(wbig + (size_t)k * H * 128, &tw2, 64 * k, 0, &bars[1]);
+    }
+    const uint32_t row_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    const float* bias = a.bias[l];
+    if (l < 3) {  // bias + ReLU, BF16, over the activations this layer consumed
+#pragma unroll 1
+      for (int cb = 0; cb < (H >> 5); cb++) {
+        float v[32];
+        ktc::tmem_ld32(row_addr + cb * 32, v);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          uint32_t w[4];
+#pragma unroll
+          for (int e = 0; e < 4; e++) {
+            const int k0 = cb * 32 + u * 8 + e * 2;
+            __nv_bfloat162 b2 = __floats2bfloat162_rn(fmaxf(v[u * 8 + e * 2] + bias[k0], 0.f),
+                                                      fmaxf(v[u * 8 + e * 2 + 1] + bias[k0 + 1], 0.f));
+            w[e] = *reinterpret_cast<uint32_t*>(&b2);
+          }
+          *reinterpret_cast<uint4*>(act + ktc::sw128_offset(tid, cb * 32 + u * 8, TC_M)) =
+              make_uint4(w[0], w[1], w[2], w[3]);
+        }
+      }
+      ktc::fence_proxy_async();
+      ktc::tc_fence_before();
+      __syncthreads();
+    } else {  // decode the output layer into the Newton start (every lane loads: warp-collective)
+      float v[64];
+      ktc::tmem_ld32(row_addr, v);
+      ktc::tmem_ld32(row_addr + 32, v + 32);
+      if (c < a.B) {
+        const double sc = a.scale_col >= 0 ? a.vals[(int64_t)a.scale_col * a.B + c] : 1.0;
+        for (int col = 0; col < a.n && col < 64; col++) {
+          const double y = (double)v[col] + bias[col];
+          a.x0[(size_t)c * a.n + col] = col < a.dout ? (y * a.tstd[col] + a.tmean[col]) * sc : 0.0;
+        }
+      }
+    }
+  }
+  if (bad) {  // a wait gave up: report it, leave defined (zero) starts, wait briefly for copies in flight
+    if (tid == 0) {
+      atomicExch(a.err, 1);
+      ktc::mbar_wait(&bars[0], 1, 100000000ull);
+      ktc::mbar_wait(&bars[1], 1, 100000000ull);
+    }
+    if (c < a.B)
+      for (int col = 0; col < a.n; col++) a.x0[(size_t)c * a.n + col] = 0.0;
+  }
+  ktc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) ktc::tmem_dealloc(tmem, 256);
+}
+
 }  // namespace
 
 struct ks_mlp {
@@ -385,7 +559,45 @@ struct ks_mlp {
   __nv_bfloat16 *X = nullptr, *H[3] = {}, *dH[3] = {}, *dYb = nullptr;
   float *Y = nullptr, *T = nullptr, *loss = nullptr;
   int32_t* idx = nullptr;
+  // tcgen05 inference: TMA descriptors of the four BF16 weight matrices (encoded
+  // once: the matrices stay where they are) and the kernel's error word
+  CUtensorMap tmap[4];
+  int tc_state = 0;  // 0: not tried, 1: ready, -1: descriptors not available
+  int* tc_err = nullptr;
 };
+
+// TMA descriptor of a BF16 [rows][cols] row-major matrix, boxes of 64 columns x
+// box_rows rows with 128-byte swizzle (the tcgen05 K-major operand layout).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static int tc_prepare(ks_mlp* p) {
+  if (p->tc_state) return p->tc_state;
+  p->tc_state = -1;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn)
+    return p->tc_state;
+  EncodeTiledFn enc = reinterpret_cast<EncodeTiledFn>(fn);
+  for (int l = 0; l < 4; l++) {
+    cuuint64_t dims[2] = {(cuuint64_t)p->ldi[l], (cuuint64_t)p->ldo[l]};
+    cuuint64_t strides[1] = {(cuuint64_t)p->ldi[l] * 2};
+    cuuint32_t box[2] = {64, (cuuint32_t)p->ldo[l]};
+    cuuint32_t estr[2] = {1, 1};
+    if (enc(&p->tmap[l], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, p->Wq[l], dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return p->tc_state;
+  }
+  if (!p->tc_err && cudaMalloc(&p->tc_err, sizeof(int)) != cudaSuccess) return p->tc_state;
+  if (cudaMemset(p->tc_err, 0, sizeof(int)) != cudaSuccess) return p->tc_state;
+  if (cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM) != cudaSuccess)
+    return p->tc_state;
+  p->tc_state = 1;
+  return p->tc_state;
+}
 
 static int mlp_alloc_batch(ks_mlp* p, int rows) {
   int R = pad64(rows);
@@ -512,6 +724,7 @@ extern "C" void ks_mlp_destroy(ks_mlp* p) {
   for (int l = 0; l < 4; l++) { cudaFree(p->Wq[l]); cudaFree(p->WTq[l]); cudaFree(p->bias_pad[l]); }
   cudaFree(p->X); cudaFree(p->Y); cudaFree(p->T); cudaFree(p->dYb); cudaFree(p->idx); cudaFree(p->loss);
   for (int i = 0; i < 3; i++) { cudaFree(p->H[i]); cudaFree(p->dH[i]); }
+  cudaFree(p->tc_err);
   delete p;
 }
 
@@ -646,6 +859,16 @@ extern "C" int ks_mlp_predict(ks_mlp* p, ks_batch* b, double* x0_dev, void* stre
   int rc = mlp_alloc_batch(p, (int)B);
   if (rc) return rc;
   int R = pad64((int)B);
+  if (p->h % 64 == 0 && p->h <= 256 && p->dip == 64 && p->dop == 64 && n <= 64 && tc_prepare(p) == 1) {
+    TcArgs a;  // the tcgen05 kernel
+    a.vals = vals; a.B = B; a.n = n; a.cols = p->fcols; a.logmask = p->logmask; a.fmean = p->fmean; a.fstd = p->fstd;
+    a.din = p->din; a.h = p->h; a.dout = p->dout;
+    for (int l = 0; l < 4; l++) a.bias[l] = p->bias_pad[l];
+    a.tmean = p->tmean; a.tstd = p->tstd; a.scale_col = p->scale_col; a.x0 = x0_dev; a.err = p->tc_err;
+    k_mlp_infer_tc<<<(unsigned)((B + TC_M - 1) / TC_M), TC_M, TC_SMEM, st>>>(a, p->tmap[0], p->tmap[1], p->tmap[2],
+                                                                             p->tmap[3]);
+    return cudaGetLastError() == cudaSuccess ? KS_OK : KS_ECUDA;
+  }
   if (p->h % 64 == 0 && p->h <= 256 && p->dip <= p->h && p->dop == 64 && n <= 64) {  // the fused kernel's shapes
     InferArgs a;
     a.vals = vals; a.B = B; a.n = n; a.cols = p->fcols; a.logmask = p->logmask; a.fmean = p->fmean; a.fstd = p->fstd;
