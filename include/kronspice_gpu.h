@@ -473,17 +473,24 @@ int ks_mlp_train(ks_mlp* m, ks_batch* b, const double* x_dev, const int32_t* idx
  * components of the Jacobian's pattern without the torn node pairs
  * (buildPlan, :296-389); each is factored as a band matrix, the
  * interconnection I + M.Q.B^-1.P of each variant as a dense matrix.
- * reuse = 1 keeps factors while the refinement against the exact Jacobian
- * (backward error <= 1e-14, accepted at 1e-12) converges on them (ReuseTol
- * without a bound); reuse = 0 refactors at every solve.  Errors per variant as
- * ks_status; a solve that is not accepted after a fresh refactor ends that
- * variant with KS_STATUS_SINGULAR (the reference would fall back to an untorn
- * LU of the whole system).  stats [14]: solves, refactors, refinement steps,
- * most refinement steps of one solve, solves not accepted, pieces, coupling
- * rows, largest band (kl + ku), band-factor doubles per variant, kernel
- * launches of the call, then the device time (microseconds, CUDA events) of
- * the refactors, the applications of the factors, the loads and the residuals.
+ * reuse = KS_TORN_REUSE keeps factors while the refinement against the exact
+ * Jacobian (backward error <= 1e-14, accepted at 1e-12) converges on them
+ * (ReuseTol without a bound); KS_TORN_REFACTOR refactors at every solve;
+ * KS_TORN_UNTORN solves every system untorn (one band LU per connected
+ * component of the whole Jacobian: the analysis without Options.Solver, for
+ * torn-versus-untorn comparisons).  A variant whose torn solve is not accepted
+ * after a fresh refactor is solved untorn, as the reference falls back to a
+ * plain LU of the whole system (kron/jacobian.go:412-434); a system whose
+ * connected component is too large for one band piece (12,000 unknowns) has
+ * no untorn solver and such a variant ends with KS_STATUS_SINGULAR.  Errors
+ * per variant as ks_status.  stats [15]: solves, refactors, refinement steps,
+ * most refinement steps of one solve, torn solves not accepted, pieces,
+ * coupling rows, largest band (kl + ku), band-factor doubles per variant,
+ * kernel launches of the call, the device time (microseconds, CUDA events) of
+ * the refactors, the applications of the factors, the loads and the
+ * residuals, then the variant solves that went untorn.
  */
+enum { KS_TORN_REFACTOR = 0, KS_TORN_REUSE = 1, KS_TORN_UNTORN = 2 };
 typedef struct ks_torn ks_torn;
 int ks_torn_create(const ks_topology* topo, int32_t n_variants, const double* values, const int32_t* torn_elems,
                    int32_t n_torn, ks_torn** out);

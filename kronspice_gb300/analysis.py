@@ -342,7 +342,7 @@ class MultiBatch:
 
 
 TORN_STATS = ("solves", "refactors", "refines", "max_passes", "not_accepted", "pieces", "coupling_rows", "max_band",
-              "band_doubles", "launches", "refactor_us", "apply_us", "load_us", "residual_us")
+              "band_doubles", "launches", "refactor_us", "apply_us", "load_us", "residual_us", "untorn")
 
 
 def torn_plan(elements, n_nodes, n_values, torn):
@@ -389,14 +389,20 @@ class TornBatch:
         """Run the later analyses on a CUDA stream handle (None: the batch's own)."""
         _check(_lib.load().ks_torn_set_stream(self.handle, stream), "ks_torn_set_stream")
 
+    @staticmethod
+    def _mode(reuse):
+        """ks_torn's reuse argument: True (keep factors while they refine), False
+        (refactor at every solve) or "untorn" (every system untorn)."""
+        return 2 if reuse == "untorn" else int(bool(reuse))
+
     def op(self, opt=None, reuse=True):
         """(x [n_var][n], status, iterations, stats) of analysis.OP for every variant."""
         o = (opt or Options()).c()
         x = np.zeros((self.n_var, self.n))
         st = np.zeros(self.n_var, dtype=np.int32)
         it = np.zeros(self.n_var, dtype=np.int32)
-        stats = np.zeros(14, dtype=np.int64)
-        _check(_lib.load().ks_torn_op(self.handle, ctypes.byref(o), int(reuse), x.ctypes.data, st.ctypes.data,
+        stats = np.zeros(15, dtype=np.int64)
+        _check(_lib.load().ks_torn_op(self.handle, ctypes.byref(o), self._mode(reuse), x.ctypes.data, st.ctypes.data,
                                       it.ctypes.data, stats.ctypes.data), "ks_torn_op")
         return x, st, it, dict(zip(TORN_STATS, stats.tolist()))
 
@@ -412,8 +418,8 @@ class TornBatch:
         st = np.zeros(self.n_var, dtype=np.int32)
         steps = np.zeros(self.n_var, dtype=np.int32)
         it = np.zeros(self.n_var, dtype=np.int32)
-        stats = np.zeros(14, dtype=np.int64)
-        _check(_lib.load().ks_torn_tran(self.handle, ctypes.byref(sp), ctypes.byref(o), int(reuse),
+        stats = np.zeros(15, dtype=np.int64)
+        _check(_lib.load().ks_torn_tran(self.handle, ctypes.byref(sp), ctypes.byref(o), self._mode(reuse),
                                         pr.ctypes.data if len(pr) else None, len(pr),
                                         wave.ctypes.data if len(pr) else None, x.ctypes.data, st.ctypes.data,
                                         steps.ctypes.data, it.ctypes.data, stats.ctypes.data), "ks_torn_tran")

@@ -83,7 +83,7 @@ def build(force=False, verbose=False):
         objs = list(ex.map(_compile, units))
     tmp = LIB + ".tmp%d" % os.getpid()
     cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + [
-        "-lcudart", "-lnvrtc", "-lcublas"]
+        "-lcudart", "-lnvrtc"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))

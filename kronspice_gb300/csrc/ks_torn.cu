@@ -16,17 +16,22 @@
 //     denseLU does, partial pivoting in the band as LAPACK's gbtf2): one CTA per
 //     (variant, piece), all pieces of all variants in one launch;
 //   * the interconnection matrix of each variant is dense, column-major,
-//     factored by a blocked right-looking LU (panel and triangular kernels here,
-//     the trailing update as a strided-batched DGEMM over all variants);
+//     factored by a blocked right-looking LU (panel, interchange, triangular and
+//     trailing-update kernels here: the update is a batched FP64 GEMM over the
+//     variants being refactored, 64 x 64 tiles of C per CTA);
 //   * factors are kept between Newton iterations and time steps while the
 //     refinement against the exact J (componentwise backward error <= 1e-14,
 //     accepted at 1e-12, kron/jacobian.go:551-589) converges on them; when it
 //     does not, every variant is refactored at its current J and the solve is
 //     repeated (the reference's stale-factor retry, :404-411).  With reuse off
 //     the factors are remade at every solve.
+//   * a variant whose torn solve is still not accepted is solved untorn, as the
+//     reference falls back to a plain LU of the whole J (:412-434): a second
+//     instance of the same topology without torn elements (one band piece per
+//     connected component, no interconnection), built at the first fallback,
+//     takes that variant's J and right-hand side.
 // Device loads, limiting, convergence tests and Accept are the engine's
 // per-element device code (ks_solve.cuh), one thread per (element, variant).
-#include <cublas_v2.h>
 #include <cuda_pipeline.h>
 #include <cuda_runtime.h>
 
@@ -623,15 +628,54 @@ __global__ void k_tl_zero_ic(int64_t per, int64_t V, double* IC, const uint8_t* 
   IC[t] = 0.0;
 }
 
-// Pointers of the trailing update A22 -= A21 U12 of the listed variants.
-__global__ void k_tl_gemm_ptrs(int count, const int32_t* list, double* IC, int R, int k0, int jb, const double** Ap,
-                               const double** Bp, double** Cp) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= count) return;
-  double* A = IC + (int64_t)list[t] * R * R;
-  Ap[t] = A + (k0 + jb) + (int64_t)k0 * R;
-  Bp[t] = A + k0 + (int64_t)(k0 + jb) * R;
-  Cp[t] = A + (k0 + jb) + (int64_t)(k0 + jb) * R;
+// Trailing update of the blocked LU, A22 -= A21 U12, for the listed variants
+// (blockIdx.z: the variant's place in the list): A21 = A(k0+jb.., k0..k0+jb),
+// U12 = A(k0..k0+jb, k0+jb..), column-major with leading dimension R.  A CTA of
+// 256 threads owns a 64 x 64 tile of A22: both operand panels (jb <= 64 columns /
+// rows) in shared memory, each thread 4 x 4 entries of the tile (rows tr + 16 r,
+// columns tc + 16 c: 16 consecutive threads touch 16 consecutive rows of a
+// column, so every global access is coalesced and every shared read is a
+// broadcast or conflict-free), FP64 multiply-adds over jb.
+#define KS_IC_TILE 64
+__global__ void __launch_bounds__(256) k_tl_ic_gemm(int R, int k0, int jb, double* IC, const int32_t* list) {
+  __shared__ double As[KS_IC_TILE][KS_IC_TILE + 1];  // [k][i]
+  __shared__ double Bs[KS_IC_TILE][KS_IC_TILE + 1];  // [k][j]
+  double* A = IC + (int64_t)list[blockIdx.z] * R * R;
+  const int rest = R - k0 - jb, i0 = blockIdx.x * KS_IC_TILE, j0 = blockIdx.y * KS_IC_TILE;
+  const int t = threadIdx.x, tr = t & 15, tc = t >> 4;
+  const int off = k0 + jb;
+  for (int e = t; e < KS_IC_TILE * KS_IC_TILE; e += 256) {
+    const int ii = e & 63, kk = e >> 6;  // consecutive threads: consecutive rows of a column
+    As[kk][ii] = (kk < jb && i0 + ii < rest) ? A[(off + i0 + ii) + (int64_t)(k0 + kk) * R] : 0.0;
+    Bs[ii][kk] = (ii < jb && j0 + kk < rest) ? A[(k0 + ii) + (int64_t)(off + j0 + kk) * R] : 0.0;
+  }
+  __syncthreads();
+  double acc[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; r++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) acc[r][c] = 0.0;
+  for (int kk = 0; kk < jb; kk++) {
+    double a[4], b[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) a[r] = As[kk][tr + 16 * r];
+#pragma unroll
+    for (int c = 0; c < 4; c++) b[c] = Bs[kk][tc + 16 * c];
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+  }
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    const int j = j0 + tc + 16 * c;
+    if (j >= rest) continue;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const int i = i0 + tr + 16 * r;
+      if (i < rest) A[(off + i) + (int64_t)(off + j) * R] -= acc[r][c];
+    }
+  }
 }
 
 // w = IC^-1 h with the factors (getrs: interchanges, unit lower, upper), one CTA
@@ -825,7 +869,6 @@ struct ks_torn {
   std::vector<int> h_pieceOf, h_rows;  // piece of each unknown, coupling rows (the plan, host side)
   std::vector<void*> owned;
   cudaStream_t st = nullptr, own = nullptr;  // the stream in use, the one created here
-  cublasHandle_t blas = nullptr;
   // device symbolic
   KElem* d_elem = nullptr;
   int8_t* d_isv = nullptr;
@@ -837,13 +880,14 @@ struct ks_torn {
   // device numeric
   double *values, *derived, *state, *x, *xo, *J, *rhs, *r, *dx, *z, *rs, *cs, *band, *Y, *Wc, *IC, *h, *w;
   int32_t *piv, *icpiv, *bad, *flags, *list;
-  const double **Aptr, **Bptr;
-  double** Cptr;
   unsigned long long* berr;
   uint8_t* mask;  // variants a launch works on
   std::vector<uint8_t> have;  // factors exist, per variant
   // counters
-  int64_t solves = 0, refactors = 0, refines = 0, max_passes = 0, failed = 0, launches = 0;
+  int64_t solves = 0, refactors = 0, refines = 0, max_passes = 0, failed = 0, launches = 0, fallbacks = 0;
+  // the untorn instance of the same topology (the fallback solver), built on first use
+  ks_torn* untorn = nullptr;
+  bool is_untorn = false, untorn_failed = false;
   // device time per phase (refactor, apply, load, residual): event pairs summed at the end of a call
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
@@ -879,8 +923,8 @@ struct ks_torn {
     return p;
   }
   ~ks_torn() {
+    delete untorn;
     for (auto e : ev_pool) cudaEventDestroy(e);
-    if (blas) cublasDestroy(blas);
     for (void* p : owned) cudaFree(p);
     if (own) cudaStreamDestroy(own);
   }
@@ -1135,14 +1179,12 @@ int alloc_numeric(ks_torn* T) {
   T->berr = dalloc<unsigned long long>(V, o);
   T->mask = dalloc<uint8_t>(V, o);
   T->list = dalloc<int32_t>(V, o);
-  T->Aptr = (const double**)dalloc<double*>(V, o); T->Bptr = (const double**)dalloc<double*>(V, o);
-  T->Cptr = dalloc<double*>(V, o);
   T->have.assign(V, 0);
   for (void* p : {(void*)T->values, (void*)T->derived, (void*)T->state, (void*)T->x, (void*)T->xo, (void*)T->J,
                   (void*)T->rhs, (void*)T->r, (void*)T->dx, (void*)T->z, (void*)T->rs, (void*)T->cs, (void*)T->band,
                   (void*)T->piv, (void*)T->Y, (void*)T->Wc, (void*)T->IC, (void*)T->icpiv, (void*)T->h, (void*)T->w,
                   (void*)T->bad, (void*)T->flags, (void*)T->berr, (void*)T->mask,
-                  (void*)T->list, (void*)T->Aptr, (void*)T->Bptr, (void*)T->Cptr})
+                  (void*)T->list})
     if (!p) { set_error("ks_torn: device allocation failed"); return KS_ENOMEM; }
   return KS_OK;
 }
@@ -1190,9 +1232,7 @@ int refactor(ks_torn* T, const std::vector<int32_t>& list) {
     if (ck(cudaMemcpyAsync(T->list, list.data(), sizeof(int32_t) * list.size(), cudaMemcpyHostToDevice, s), "list"))
       return KS_ECUDA;
     const int count = (int)list.size();
-    const int nb = 64;
-    const double one = 1.0, minus = -1.0;
-    cublasSetStream(T->blas, s);
+    const int nb = KS_IC_TILE;
     for (int k0 = 0; k0 < R; k0 += nb) {
       const int jb = std::min(nb, R - k0);
       T->launches++;
@@ -1204,10 +1244,8 @@ int refactor(ks_torn* T, const std::vector<int32_t>& list) {
       T->launches++;
       k_tl_ic_trsm<<<blocks_for((int64_t)rest * V, 128), 128, 0, s>>>(R, k0, jb, T->IC, V, T->mask);
       T->launches++;
-      k_tl_gemm_ptrs<<<blocks_for(count, 128), 128, 0, s>>>(count, T->list, T->IC, R, k0, jb, T->Aptr, T->Bptr, T->Cptr);
-      cublasStatus_t bs = cublasDgemmBatched(T->blas, CUBLAS_OP_N, CUBLAS_OP_N, rest, rest, jb, &minus, T->Aptr, R,
-                                             T->Bptr, R, &one, T->Cptr, R, count);
-      if (bs != CUBLAS_STATUS_SUCCESS) { set_error("ks_torn: cuBLAS DGEMM failed"); return KS_ECUDA; }
+      const unsigned tiles = (unsigned)((rest + KS_IC_TILE - 1) / KS_IC_TILE);
+      k_tl_ic_gemm<<<dim3(tiles, tiles, (unsigned)count), 256, 0, s>>>(R, k0, jb, T->IC, T->list);
     }
   }
   if (ck(cudaGetLastError(), "refactor launch")) return KS_ECUDA;
@@ -1217,6 +1255,7 @@ int refactor(ks_torn* T, const std::vector<int32_t>& list) {
 }
 
 int apply_(ks_torn* T, const double* b, double* out);
+int untorn_solve(ks_torn* T, const std::vector<uint8_t>& want, std::vector<uint8_t>* ok);
 
 // out = M^-1 b with the current factors, for the masked variants.
 int apply(ks_torn* T, const double* b, double* out) {
@@ -1320,12 +1359,80 @@ int torn_solve(ks_torn* T, const std::vector<uint8_t>& want, bool reuse, std::ve
   }
   for (int64_t v = 0; v < V; v++)
     if (want[v] && !(*ok)[v]) T->failed++;
+  if (T->is_untorn) return KS_OK;
+  // not accepted torn, even on fresh factors: the untorn LU (kron/jacobian.go:412-414)
+  std::vector<uint8_t> fb(V, 0), okf;
+  bool anyf = false;
+  for (int64_t v = 0; v < V; v++) { fb[v] = want[v] && !(*ok)[v]; anyf = anyf || fb[v]; }
+  if (!anyf) return KS_OK;
+  int rc = untorn_solve(T, fb, &okf);
+  if (rc) return rc;
+  for (int64_t v = 0; v < V; v++) if (okf[v]) (*ok)[v] = 1;
+  return KS_OK;
+}
+
+// The untorn instance of T's topology: every unknown in the band piece of its
+// connected component, no coupling rows (buildPlan of an empty tearing), its own
+// factors and vectors for T's variants, on T's stream.  Null when a component is
+// too large for a band piece (those variants then keep their failed status).
+ks_torn* untorn_of(ks_torn* T) {
+  if (T->untorn || T->untorn_failed || T->is_untorn) return T->untorn;
+  ks_torn* U = new ks_torn();
+  U->hp = T->hp;
+  U->V = T->V;
+  U->is_untorn = true;
+  ks_topology topo{T->hp.n_nodes, T->hp.n_elem, T->hp.n_values, 0, T->hp.src.data()};
+  std::string err;
+  if (build_plan(U, &topo, nullptr, 0, &err) || alloc_numeric(U)) {
+    delete U;
+    T->untorn_failed = true;
+    return nullptr;
+  }
+  const size_t band_smem = torn_solve_smem(U);
+  if (band_smem > 48 * 1024 && band_smem > torn_solve_smem(T))
+    cudaFuncSetAttribute(k_tl_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
+  U->st = T->st;
+  T->untorn = U;
+  return U;
+}
+
+int torn_solve(ks_torn* T, const std::vector<uint8_t>& want, bool reuse, std::vector<uint8_t>* ok);
+
+// J x = rhs untorn for the variants in `want` (kron/jacobian.go:418-434): J and
+// the right-hand side go to the untorn instance, which factors afresh and
+// refines against the same J; x comes back for those variants.  ok[v] = 1 when
+// accepted.
+int untorn_solve(ks_torn* T, const std::vector<uint8_t>& want, std::vector<uint8_t>* ok) {
+  const int64_t V = T->V, n = T->n;
+  ok->assign(V, 0);
+  int64_t count = 0;
+  for (auto w : want) count += w != 0;
+  if (!count) return KS_OK;
+  ks_torn* U = untorn_of(T);
+  if (!U) return KS_OK;
+  cudaStream_t s = T->st;
+  U->st = s;
+  if (ck(cudaMemcpyAsync(U->J, T->J, sizeof(double) * (size_t)T->nnz * V, cudaMemcpyDeviceToDevice, s), "untorn J") ||
+      ck(cudaMemcpyAsync(U->rhs, T->rhs, sizeof(double) * n * V, cudaMemcpyDeviceToDevice, s), "untorn rhs"))
+    return KS_ECUDA;
+  U->have.assign(V, 0);
+  const int64_t l0 = U->launches;
+  std::vector<uint8_t> oku;
+  int rc = torn_solve(U, want, false, &oku);
+  if (rc) return rc;
+  if ((rc = set_mask(U, want))) return rc;
+  U->launches++;
+  k_tl_copy_masked<<<blocks_for(n * V, 256), 256, 0, s>>>(n, V, U->x, T->x, U->mask);
+  if ((rc = ck(cudaGetLastError(), "untorn x"))) return rc;
+  for (int64_t v = 0; v < V; v++) (*ok)[v] = want[v] && oku[v];
+  T->fallbacks += count;
+  T->launches += U->launches - l0 + 2;
   return KS_OK;
 }
 
 // One Newton solve (newton(), analysis/newton.go:36-57) of every active variant.
 // status[v] receives KS_STATUS_NO_CONVERGENCE / SINGULAR on failure.
-int newton(ks_torn* T, LoadParams lp, const KOpts& o, int max_iter, bool reuse, std::vector<int32_t>& status,
+int newton(ks_torn* T, LoadParams lp, const KOpts& o, int max_iter, int reuse, std::vector<int32_t>& status,
            std::vector<int32_t>& iters) {
   const int64_t V = T->V, n = T->n;
   cudaStream_t s = T->st;
@@ -1352,7 +1459,9 @@ int newton(ks_torn* T, LoadParams lp, const KOpts& o, int max_iter, bool reuse, 
                                                                          T->d_ci, T->J, T->rhs, T->x, T->xo, lp, T->mask);
     T->mark_end(2, e0);
     std::vector<uint8_t> ok;
-    if ((rc = torn_solve(T, live, reuse, &ok))) return rc;
+    if (reuse == KS_TORN_UNTORN) rc = untorn_solve(T, live, &ok);  // every system untorn
+    else rc = torn_solve(T, live, reuse != 0, &ok);
+    if (rc) return rc;
     for (int64_t v = 0; v < V; v++) {
       if (!live[v]) continue;
       iters[v]++;
@@ -1403,9 +1512,8 @@ extern "C" int ks_torn_create(const ks_topology* topo, int32_t n_variants, const
   if (ic_smem > 48 * 1024) cudaFuncSetAttribute(k_tl_ic_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ic_smem);
   const size_t band_smem = torn_solve_smem(T);
   if (band_smem > 48 * 1024) cudaFuncSetAttribute(k_tl_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
-  if (cudaStreamCreateWithFlags(&T->own, cudaStreamNonBlocking) != cudaSuccess ||
-      cublasCreate(&T->blas) != CUBLAS_STATUS_SUCCESS) {
-    set_error("ks_torn_create: stream or cuBLAS handle");
+  if (cudaStreamCreateWithFlags(&T->own, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("ks_torn_create: stream creation failed");
     delete T;
     return KS_ECUDA;
   }
@@ -1471,6 +1579,7 @@ void stats_out(const ks_torn* T, int64_t* s) {
   s[0] = T->solves; s[1] = T->refactors; s[2] = T->refines; s[3] = T->max_passes; s[4] = T->failed;
   s[5] = T->P; s[6] = T->R; s[7] = T->max_band; s[8] = T->band_stride; s[9] = T->launches;
   for (int k = 0; k < 4; k++) s[10 + k] = (int64_t)(T->phase_ms[k] * 1000.0);  // microseconds
+  s[14] = T->fallbacks;
 }
 
 int fresh_state(ks_torn* T, double step, double stop) {
@@ -1484,7 +1593,7 @@ int fresh_state(ks_torn* T, double step, double stop) {
   T->launches++;
   k_tl_init_mos<<<blocks_for((int64_t)plan.n_elem * V, 256), 256, 0, T->st>>>(plan, T->derived, T->state, V);
   if (ck(cudaMemsetAsync(T->x, 0, sizeof(double) * T->n * V, T->st), "memset")) return KS_ECUDA;
-  T->solves = T->refactors = T->refines = T->max_passes = T->failed = 0;
+  T->solves = T->refactors = T->refines = T->max_passes = T->failed = T->fallbacks = 0;
   T->launches = 3;
   for (double& m : T->phase_ms) m = 0;
   T->marks.clear();
@@ -1533,7 +1642,7 @@ extern "C" int ks_torn_op(ks_torn* T, const ks_options* opt, int32_t reuse, doub
   lp.mode = ModeOP; lp.method = BE; lp.time = 0; lp.h = 0; lp.rh = 0; lp.initJct = true; lp.gmin = o.gmin;
   lp.srcStepping = false; lp.srcFact = 0;
   std::vector<int32_t> status(T->V, KS_STATUS_OK), iters(T->V, 0);
-  if ((rc = newton(T, lp, o, o.itl1, reuse != 0, status, iters))) return rc;
+  if ((rc = newton(T, lp, o, o.itl1, reuse, status, iters))) return rc;
   if ((rc = accept_all_variants(T, status, 0.0, ModeOP, o.gmin))) return rc;
   if ((rc = x_out(T, out_x))) return rc;
   if (out_status) memcpy(out_status, status.data(), sizeof(int32_t) * T->V);
@@ -1581,7 +1690,7 @@ extern "C" int ks_torn_tran(ks_torn* T, const ks_tran_spec* spec, const ks_optio
   LoadParams lp;
   lp.mode = ModeTranOP; lp.method = BE; lp.time = 0; lp.h = 0; lp.rh = 0; lp.initJct = true; lp.gmin = o.gmin;
   lp.srcStepping = false; lp.srcFact = 0;
-  rc = newton(T, lp, o, o.itl1, reuse != 0, status, iters);
+  rc = newton(T, lp, o, o.itl1, reuse, status, iters);
   if (!rc) rc = accept_all_variants(T, status, 0.0, ModeTranOP, o.gmin);
   if (!rc) record(0);
   // fixed steps; backward Euler at the first, then the spec's method
@@ -1592,7 +1701,7 @@ extern "C" int ks_torn_tran(ks_torn* T, const ks_tran_spec* spec, const ks_optio
   for (long k = 1; k < npts && !rc; k++) {
     const double t = (double)k * spec->step, h = spec->step;
     lp.mode = ModeTran; lp.time = t; lp.h = h; lp.rh = 1 / h; lp.method = order; lp.initJct = false;
-    rc = newton(T, lp, o, o.itl4, reuse != 0, status, iters);
+    rc = newton(T, lp, o, o.itl4, reuse, status, iters);
     if (rc) break;
     rc = accept_all_variants(T, status, t, ModeTran, o.gmin);
     if (rc) break;

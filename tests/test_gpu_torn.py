@@ -121,3 +121,48 @@ def test_golden_operating_points_torn(case):
                 got[k] = 0.0 if i == 0 else x[0, i - 1]
     msgs = gc.compare_values(got, {k: v for k, v in want["values"].items() if k.startswith("v(")})
     assert not msgs, msgs
+
+
+def test_untorn_mode_matches_oracle():
+    """reuse="untorn": every system solved untorn (one band LU per connected
+    component of the whole Jacobian, the solver of the untorn fallback): the
+    power-grid transient matches the oracle's untorn run, and no solve is torn."""
+    el, nn, vals, torn, c = grid(2, 16, 2, 16, seed=4)
+    tb = analysis.TornBatch(el, nn, vals, torn)
+    spec = analysis.TranSpec(step=0.1e-9, stop=20 * 0.1e-9, fixed_step=True, method="be")
+    probes = np.arange(0, tb.n, 5)
+    wave, x, st, steps, it, stats = tb.tran(spec, analysis.Options(reltol=1e-6), reuse="untorn", probes=probes)
+    assert np.all(st == 0) and np.all(steps == 20), (st, steps)
+    assert stats["untorn"] == stats["solves"] * len(vals) and stats["refactors"] == stats["solves"], stats
+    ospec = orc.TranSpec(0.1e-9, 20 * 0.1e-9, 0.0, 0.0, 0, 1, 1, 0, 0.0, 0.0, 0.0)
+    for v in range(len(vals)):
+        r = orc.tran(orc.Packed(el, nn, vals[v]), ospec, orc.options(reltol=1e-6))
+        assert r[0] == 0, r[-1]
+        scale = np.abs(r[2]).max()
+        assert np.abs(wave[:, v, :] - r[2][:, probes]).max() <= 1e-9 * scale
+        assert it[v] == r[5]
+
+
+def test_singular_circuit_falls_back_untorn():
+    """TestJacobianErrors' fallback case (kron/jacobian_test.go:298-305): two
+    voltage sources in parallel, torn along R1.  The torn solve fails, the
+    variant is solved untorn, and the untorn LU reports what plain MNA reports:
+    a singular matrix, for both variants of the batch."""
+    b = kc.Builder("loop")
+    b.voltage_source("V1", "1", "0", 1.0)
+    b.voltage_source("V2", "1", "0", 2.0)
+    b.resistor("R1", "1", "2", 1e3)
+    b.resistor("R2", "2", "0", 1e3)
+    ckt = b.build()
+    el, v0, _ = ckt.pack()
+    names = [e.name for e in ckt.elements]
+    vals = np.tile(v0, (2, 1))
+    vals[1, int(el[names.index("V2")]["param"])] = 0.0  # still two sources in parallel: singular as well
+    opt = analysis.Options(no_gmin_stepping=True, no_source_stepping=True, no_pseudo_transient=True)
+    tb = analysis.TornBatch(el, ckt.n_nodes, vals, [names.index("R1")])
+    x, st, it, stats = tb.op(opt)
+    so, xo, _, _, msg = orc.op(orc.Packed(el, ckt.n_nodes, vals[0]),
+                               orc.options(no_gmin=True, no_source=True, no_pt=True))
+    assert so == 1 and "singular" in msg, msg
+    assert np.all(st == 1), st  # KS_STATUS_SINGULAR from the untorn LU
+    assert stats["untorn"] >= 2, stats
