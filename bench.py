@@ -941,10 +941,11 @@ def bench_torn(args):
     spec = analysis.TranSpec(step=POWER_H, stop=nsteps * POWER_H, fixed_step=True, method="be")
     names = [e.name for e in circ.elements]
     grid_nodes = [circ.node_index("g%d_%d" % (r, c)) - 1 for r in (0, 128, 255) for c in (0, 128, 255)]
-    opt = analysis.Options(reltol=RELTOL)
+    opt = analysis.Options(reltol=RELTOL, precision=args.precision)  # chosen: FP32 factors (mixed) by default
+    opt64 = analysis.Options(reltol=RELTOL, precision="fp64")
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    def timed(reuse, steps_timed, spec_):
+    def timed(reuse, steps_timed, spec_, opt=opt):
         for _ in range(args.warmup):
             tb.tran(spec_, opt, reuse=reuse, probes=grid_nodes)
         torch.cuda.synchronize()
@@ -973,7 +974,8 @@ def bench_torn(args):
         chosen = timed(True, args.steps, spec)
         plain_steps = max(2, nsteps // 50)
         plain_spec = analysis.TranSpec(step=POWER_H, stop=plain_steps * POWER_H, fixed_step=True, method="be")
-        plain = timed(False, 1, plain_spec)
+        plain = timed(False, 1, plain_spec, opt64)
+        reuse64 = timed(True, 1, spec, opt64) if args.variants else None  # FP64 factors kept (no FP32 copies)
     clocks = clk.summary(local)
     value = chosen["points"] / chosen["seconds"]
     plain_value = plain["points"] / plain["seconds"]
@@ -1019,7 +1021,8 @@ def bench_torn(args):
     # algorithmic bytes of one transient: every application of the torn factors streams the band factors of all
     # pieces twice (z = B^-1 b, then x = B^-1 (b - P w)) and the interconnection factors once
     applies = st["solves"] + st["refines"]
-    per_apply = V * (2 * st["band_doubles"] * 8 + R * R * 8)
+    fw = 4 if args.precision == "mixed" else 8  # bytes per factor entry streamed
+    per_apply = V * (2 * st["band_doubles"] * fw + R * R * fw)
     per_run_s = chosen["seconds"] / args.steps
     achieved = applies * per_apply / per_run_s / 1e9
     peaks = {}
@@ -1033,13 +1036,17 @@ def bench_torn(args):
         "metric": METRIC, "value": value, "unit": TRAN_UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": chosen["seconds"] / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox)",
+        "vs_baseline": None, "dtype": "f64 loads and residuals, f32 factors" if args.precision == "mixed" else "f64", "data": "synthetic (seeded Philox)",
         "config": {"workload": "power_grid_tran_%d" % V, "variants": V, "grid": "256x256", "unknowns": n,
                    "pieces": P, "coupling_rows": R, "largest_piece": tb.max_piece, "band": tb.max_band,
                    "steps_per_variant": nsteps, "method": "be", "step_s": POWER_H, "reltol": RELTOL,
                    "l2": "flushed before each timed transient (512 MB write); factors exceed L2"},
-        "chosen": {"value": value, "reuse": True, "stats": st},
-        "plain": {"value": plain_value, "reuse": False, "steps_timed": plain_steps, "stats": plain["stats"]},
+        "chosen": {"value": value, "reuse": True, "factors": "fp32 copies streamed, fp64 refinement" if
+                   args.precision == "mixed" else "fp64", "stats": st},
+        "plain": {"value": plain_value, "reuse": False, "factors": "fp64", "steps_timed": plain_steps,
+                  "stats": plain["stats"]},
+        "variants": None if reuse64 is None else {
+            "reuse/fp64": {"points_per_s": reuse64["points"] / reuse64["seconds"], "stats": reuse64["stats"]}},
         "chosen_vs_plain": value / plain_value if plain_value else None,
         "create_s": create_s,
         "max_node_voltage_err_vs_oracle": max_err,

@@ -323,21 +323,23 @@ __global__ void __launch_bounds__(256) k_tl_band_lu(const PieceD* pcs, int64_t V
 // sweep waits on barriers, not on memory.
 #define KS_TORN_CH 4
 #define KS_TORN_NBUF 4
+template <typename F>
 __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t V, int64_t band_stride,
-                                                      const double* band, int64_t piv_stride, const int32_t* piv_all,
+                                                      const F* band, int64_t piv_stride, const int32_t* piv_all,
                                                       const int32_t* pidx, const double* rs, const double* cs,
                                                       const double* b, const int32_t* row_a, const double* w,
                                                       double* out, const uint8_t* mask, int max_n, int max_colw) {
-  extern __shared__ __align__(16) double smem[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  F* smem = reinterpret_cast<F*>(smem_raw);
   const int v = blockIdx.x % V, p = blockIdx.x / V;
   if (!mask[v]) return;
   const PieceD pc = pcs[p];
-  const double* AB = band + (int64_t)v * band_stride + pc.band_off;
+  const F* AB = band + (int64_t)v * band_stride + pc.band_off;
   const int32_t* piv = piv_all + (int64_t)v * piv_stride + pc.idx_off;
   const int n = pc.n, kl = pc.kl, ldab = pc.ldab, kv = pc.kl + pc.ku;
   const int t = threadIdx.x;
-  double* y = smem;                                 // [max_n], rounded to 2
-  double* buf = smem + ((max_n + 1) & ~1);          // [NBUF][CH][max_colw]
+  F* y = smem;                                      // [max_n], rounded to 2
+  F* buf = smem + ((max_n + 1) & ~1);               // [NBUF][CH][max_colw]
   int* spiv = reinterpret_cast<int*>(buf + KS_TORN_NBUF * KS_TORN_CH * max_colw);  // [NBUF][CH]
   const int bufsz = KS_TORN_CH * max_colw;
   for (int i = t; i < n; i += 32) {
@@ -347,17 +349,17 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
       const int a = row_a[g];
       if (a >= 0) bi -= w[(int64_t)a * V + v];
     }
-    y[i] = bi * rs[(int64_t)g * V + v];
+    y[i] = (F)(bi * rs[(int64_t)g * V + v]);
   }
   const int nch = (n + KS_TORN_CH - 1) / KS_TORN_CH;
   // stage block c: `width` doubles of each column from row offset `first`
   auto stage = [&](int c, int first, int width, bool pivots) {
     if (c < 0 || c >= nch) { __pipeline_commit(); return; }
     const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
-    double* dst = buf + (c % KS_TORN_NBUF) * bufsz;
-    const double* src = AB + first + (int64_t)j0 * ldab;
+    F* dst = buf + (c % KS_TORN_NBUF) * bufsz;
+    const F* src = AB + first + (int64_t)j0 * ldab;
     for (int jj = 0; jj < cols; jj++, dst += max_colw, src += ldab)
-      for (int r = t; r < width; r += 32) __pipeline_memcpy_async(dst + r, src + r, 8);
+      for (int r = t; r < width; r += 32) __pipeline_memcpy_async(dst + r, src + r, sizeof(F));
     __pipeline_commit();
     if (pivots && t < cols) spiv[(c % KS_TORN_NBUF) * KS_TORN_CH + t] = piv[j0 + t];
   };
@@ -367,7 +369,7 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
     stage(c + KS_TORN_NBUF - 1, kv + 1, kl, true);
     __pipeline_wait_prior(KS_TORN_NBUF - 1);
     __syncwarp();
-    const double* B = buf + (c % KS_TORN_NBUF) * bufsz;
+    const F* B = buf + (c % KS_TORN_NBUF) * bufsz;
     const int* P = spiv + (c % KS_TORN_NBUF) * KS_TORN_CH;
     const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
     for (int jj = 0; jj < cols; jj++) {
@@ -375,17 +377,17 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
       const int km = min(kl, n - 1 - j);
       const int pj = P[jj];
       if (pj != j) {  // the same for every lane
-        if (t == 0) { const double tmp = y[j]; y[j] = y[pj]; y[pj] = tmp; }
+        if (t == 0) { const F tmp = y[j]; y[j] = y[pj]; y[pj] = tmp; }
         __syncwarp();
       }
-      const double yj = y[j];
+      const F yj = y[j];
       if (kl <= 128) {  // up to 4 rows a lane: loads first, then the updates (independent)
-        double lv[4], yv[4];
+        F lv[4], yv[4];
 #pragma unroll
         for (int r = 0; r < 4; r++) {
           const int o = t + 32 * r;
-          lv[r] = o < km ? B[jj * max_colw + o] : 0.0;
-          yv[r] = o < km ? y[j + 1 + o] : 0.0;
+          lv[r] = o < km ? B[jj * max_colw + o] : F(0);
+          yv[r] = o < km ? y[j + 1 + o] : F(0);
         }
 #pragma unroll
         for (int r = 0; r < 4; r++) {
@@ -406,21 +408,21 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
     stage(c - (KS_TORN_NBUF - 1), 0, kv + 1, false);
     __pipeline_wait_prior(KS_TORN_NBUF - 1);
     __syncwarp();
-    const double* B = buf + (c % KS_TORN_NBUF) * bufsz;
+    const F* B = buf + (c % KS_TORN_NBUF) * bufsz;
     const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
     for (int jj = cols - 1; jj >= 0; jj--) {
       const int j = j0 + jj;
-      const double yj = y[j] / B[jj * max_colw + kv];
+      const F yj = y[j] * B[jj * max_colw + kv];  // the diagonal slot holds 1 / u_jj
       __syncwarp();
       if (t == 0) y[j] = yj;
       if (kv <= 256) {  // up to 8 rows a lane: loads first, then the updates
-        double uv[8], yv[8];
+        F uv[8], yv[8];
 #pragma unroll
         for (int r = 0; r < 8; r++) {
           const int o = t + 32 * r, i = j - kv + o;
           const bool on = o < kv && i >= 0;
-          uv[r] = on ? B[jj * max_colw + o] : 0.0;
-          yv[r] = on ? y[i] : 0.0;
+          uv[r] = on ? B[jj * max_colw + o] : F(0);
+          yv[r] = on ? y[i] : F(0);
         }
 #pragma unroll
         for (int r = 0; r < 8; r++) {
@@ -440,8 +442,36 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
   __syncwarp();
   for (int i = t; i < n; i += 32) {
     const int g = pidx[pc.idx_off + i];
-    out[(int64_t)g * V + v] = y[i] * cs[(int64_t)g * V + v];
+    out[(int64_t)g * V + v] = (double)y[i] * cs[(int64_t)g * V + v];
   }
+}
+
+// After a refactor (the port columns made): each band's U diagonal replaced by
+// its reciprocal (the solves multiply by it) and the FP32 copy of the factors
+// the applications stream under mixed precision.
+__global__ void __launch_bounds__(256) k_tl_band_finish(const PieceD* pcs, int64_t V, int64_t band_stride, double* band,
+                                                        float* band32, const uint8_t* mask) {
+  const int v = blockIdx.x % V, p = blockIdx.x / V;
+  if (!mask[v]) return;
+  const PieceD pc = pcs[p];
+  double* AB = band + (int64_t)v * band_stride + pc.band_off;
+  float* AB32 = band32 + (int64_t)v * band_stride + pc.band_off;
+  const int kv = pc.kl + pc.ku;
+  for (int j = threadIdx.x; j < pc.n; j += blockDim.x) AB[kv + (int64_t)j * pc.ldab] = 1.0 / AB[kv + (int64_t)j * pc.ldab];
+  __syncthreads();
+  const int64_t total = (int64_t)pc.ldab * pc.n;
+  for (int64_t q = threadIdx.x; q < total; q += blockDim.x) AB32[q] = (float)AB[q];
+}
+
+// The same for the interconnection factors (column-major [R][R] per variant).
+__global__ void k_tl_ic_finish(int R, int64_t V, double* IC, float* IC32, const uint8_t* mask) {
+  const int64_t per = (int64_t)R * R;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= per * V || !mask[t / per]) return;
+  const int64_t e = t % per;
+  double a = IC[t];
+  if (e % R == e / R) { a = 1.0 / a; IC[t] = a; }
+  IC32[t] = (float)a;
 }
 
 // W_c = (B^-1 e_port) at the piece's coupling-column unknowns, for every port of
@@ -682,41 +712,43 @@ __global__ void __launch_bounds__(256) k_tl_ic_gemm(int R, int k0, int jb, doubl
 // per variant, by panels of 32 columns: warp 0 solves a panel's small triangle
 // with warp barriers, then every thread updates the rest of the vector by the
 // panel as one matrix-vector product (coalesced column reads).
-__global__ void __launch_bounds__(512) k_tl_ic_solve(int R, int64_t V, const double* IC, const int32_t* ipiv,
+template <typename F>
+__global__ void __launch_bounds__(512) k_tl_ic_solve(int R, int64_t V, const F* IC, const int32_t* ipiv,
                                                       const double* h, double* w, const uint8_t* mask) {
-  extern __shared__ double y[];  // [R] then the pivots [R]
+  extern __shared__ __align__(16) unsigned char ic_smem[];  // y [R] then the pivots [R]
+  F* y = reinterpret_cast<F*>(ic_smem);
   const int v = blockIdx.x;
   if (!mask[v]) return;
   int* sp = reinterpret_cast<int*>(y + R);
-  const double* A = IC + (int64_t)v * R * R;
+  const F* A = IC + (int64_t)v * R * R;
   const int32_t* piv = ipiv + (int64_t)v * R;
   const int t = threadIdx.x, T = blockDim.x, lane = t & 31;
   constexpr int NB = 32;
-  for (int i = t; i < R; i += T) { y[i] = h[(int64_t)i * V + v]; sp[i] = piv[i]; }
+  for (int i = t; i < R; i += T) { y[i] = (F)h[(int64_t)i * V + v]; sp[i] = piv[i]; }
   __syncthreads();
   if (t == 0)
     for (int j = 0; j < R; j++) {
       const int p = sp[j];
-      if (p != j) { const double tmp = y[j]; y[j] = y[p]; y[p] = tmp; }
+      if (p != j) { const F tmp = y[j]; y[j] = y[p]; y[p] = tmp; }
     }
   __syncthreads();
   for (int k0 = 0; k0 < R; k0 += NB) {
     const int k1 = min(k0 + NB, R);
     if (t < 32) {  // unit lower triangle of the panel: lane l owns row k0 + l (its row loaded first)
       const int i = k0 + lane;
-      double yi = i < k1 ? y[i] : 0.0, a[NB];
+      F yi = i < k1 ? y[i] : F(0), a[NB];
 #pragma unroll
-      for (int q = 0; q < NB; q++) a[q] = (i < k1 && k0 + q < i) ? A[i + (int64_t)(k0 + q) * R] : 0.0;
+      for (int q = 0; q < NB; q++) a[q] = (i < k1 && k0 + q < i) ? A[i + (int64_t)(k0 + q) * R] : F(0);
 #pragma unroll
       for (int q = 0; q < NB; q++) {
-        const double yj = __shfl_sync(0xffffffffu, yi, q);
+        const F yj = __shfl_sync(0xffffffffu, yi, q);
         if (k0 + q < k1) yi -= a[q] * yj;
       }
       if (i < k1) y[i] = yi;
     }
     __syncthreads();
     for (int i = k1 + t; i < R; i += T) {  // the rows below: y_i -= L(i, k0:k1) . y(k0:k1)
-      double s = 0;
+      F s = 0;
       for (int j = k0; j < k1; j++) s += A[i + (int64_t)j * R] * y[j];
       y[i] -= s;
     }
@@ -726,27 +758,27 @@ __global__ void __launch_bounds__(512) k_tl_ic_solve(int R, int64_t V, const dou
     const int k0 = max(0, k1 - NB);
     if (t < 32) {  // upper triangle of the panel (the lane's row and diagonal loaded first)
       const int i = k0 + lane;
-      double yi = i < k1 ? y[i] : 0.0, a[NB];
+      F yi = i < k1 ? y[i] : F(0), a[NB];
 #pragma unroll
-      for (int q = 0; q < NB; q++) a[q] = (i < k1 && k0 + q >= i && k0 + q < k1) ? A[i + (int64_t)(k0 + q) * R] : 0.0;
+      for (int q = 0; q < NB; q++) a[q] = (i < k1 && k0 + q >= i && k0 + q < k1) ? A[i + (int64_t)(k0 + q) * R] : F(0);
 #pragma unroll
       for (int q = NB - 1; q >= 0; q--) {
         if (k0 + q >= k1) continue;
-        if (lane == q) yi /= a[q];
-        const double yj = __shfl_sync(0xffffffffu, yi, q);
+        if (lane == q) yi *= a[q];  // the diagonal holds 1 / u_ii
+        const F yj = __shfl_sync(0xffffffffu, yi, q);
         if (lane < q) yi -= a[q] * yj;
       }
       if (i < k1) y[i] = yi;
     }
     __syncthreads();
     for (int i = t; i < k0; i += T) {  // the rows above: y_i -= U(i, k0:k1) . y(k0:k1)
-      double s = 0;
+      F s = 0;
       for (int j = k0; j < k1; j++) s += A[i + (int64_t)j * R] * y[j];
       y[i] -= s;
     }
     __syncthreads();
   }
-  for (int i = t; i < R; i += T) w[(int64_t)i * V + v] = y[i];
+  for (int i = t; i < R; i += T) w[(int64_t)i * V + v] = (double)y[i];
 }
 
 // h = M.Q.z: each coupling row's entries times z at their columns.
@@ -879,6 +911,8 @@ struct ks_torn {
   int64_t band_stride = 0, piv_stride = 0, wc_stride = 0, y_stride = 0;
   // device numeric
   double *values, *derived, *state, *x, *xo, *J, *rhs, *r, *dx, *z, *rs, *cs, *band, *Y, *Wc, *IC, *h, *w;
+  float *band32 = nullptr, *IC32 = nullptr;  // FP32 copies of the factors (mixed precision applications)
+  bool fp32 = false;                          // this call's applications stream the FP32 copies
   int32_t *piv, *icpiv, *bad, *flags, *list;
   unsigned long long* berr;
   uint8_t* mask;  // variants a launch works on
@@ -1169,10 +1203,12 @@ int alloc_numeric(ks_torn* T) {
   T->r = dalloc<double>(n * V, o); T->dx = dalloc<double>(n * V, o); T->z = dalloc<double>(n * V, o);
   T->rs = dalloc<double>(n * V, o); T->cs = dalloc<double>(n * V, o);
   T->band = dalloc<double>((size_t)T->band_stride * V, o);
+  T->band32 = dalloc<float>((size_t)T->band_stride * V, o);
   T->piv = dalloc<int32_t>((size_t)T->piv_stride * V, o);
   T->Y = dalloc<double>((size_t)T->y_stride * V, o);
   T->Wc = dalloc<double>((size_t)T->wc_stride * V, o);
   T->IC = dalloc<double>((size_t)T->R * T->R * V, o);
+  T->IC32 = dalloc<float>((size_t)T->R * T->R * V, o);
   T->icpiv = dalloc<int32_t>((size_t)T->R * V, o);
   T->h = dalloc<double>((size_t)T->R * V, o); T->w = dalloc<double>((size_t)T->R * V, o);
   T->bad = dalloc<int32_t>(V, o); T->flags = dalloc<int32_t>(V, o);
@@ -1184,7 +1220,7 @@ int alloc_numeric(ks_torn* T) {
                   (void*)T->rhs, (void*)T->r, (void*)T->dx, (void*)T->z, (void*)T->rs, (void*)T->cs, (void*)T->band,
                   (void*)T->piv, (void*)T->Y, (void*)T->Wc, (void*)T->IC, (void*)T->icpiv, (void*)T->h, (void*)T->w,
                   (void*)T->bad, (void*)T->flags, (void*)T->berr, (void*)T->mask,
-                  (void*)T->list})
+                  (void*)T->list, (void*)T->band32, (void*)T->IC32})
     if (!p) { set_error("ks_torn: device allocation failed"); return KS_ENOMEM; }
   return KS_OK;
 }
@@ -1247,7 +1283,11 @@ int refactor(ks_torn* T, const std::vector<int32_t>& list) {
       const unsigned tiles = (unsigned)((rest + KS_IC_TILE - 1) / KS_IC_TILE);
       k_tl_ic_gemm<<<dim3(tiles, tiles, (unsigned)count), 256, 0, s>>>(R, k0, jb, T->IC, T->list);
     }
+    T->launches++;
+    k_tl_ic_finish<<<blocks_for((int64_t)R * R * V, 256), 256, 0, s>>>(R, V, T->IC, T->IC32, T->mask);
   }
+  T->launches++;  // after the port columns: the bands' reciprocal diagonals and FP32 copies
+  k_tl_band_finish<<<grid, 256, 0, s>>>(T->d_pcs, V, T->band_stride, T->band, T->band32, T->mask);
   if (ck(cudaGetLastError(), "refactor launch")) return KS_ECUDA;
   T->mark_end(0, e0);
   for (int v : list) T->have[v] = 1;
@@ -1273,22 +1313,33 @@ int apply_(ks_torn* T, const double* b, double* out) {
   const unsigned grid = (unsigned)(V * T->P);
   const size_t sm = torn_solve_smem(T);
   const int bt = 32;  // one warp per (variant, piece)
-  if (R == 0) {
+  // the band solves: FP32 factors under mixed precision, else FP64
+  auto band_solve = [&](const double* w, double* o) {
     T->launches++;
-    k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
-                                          T->cs, b, T->d_row_a, nullptr, out, T->mask, T->max_piece, T->max_colw);
+    if (T->fp32)
+      k_tl_band_solve<float><<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band32, T->piv_stride, T->piv,
+                                                  T->d_pidx, T->rs, T->cs, b, T->d_row_a, w, o, T->mask, T->max_piece,
+                                                  T->max_colw);
+    else
+      k_tl_band_solve<double><<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv,
+                                                   T->d_pidx, T->rs, T->cs, b, T->d_row_a, w, o, T->mask, T->max_piece,
+                                                   T->max_colw);
+  };
+  if (R == 0) {
+    band_solve(nullptr, out);
     return ck(cudaGetLastError(), "apply");
   }
-  T->launches++;
-  k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
-                                        T->cs, b, T->d_row_a, nullptr, T->z, T->mask, T->max_piece, T->max_colw);
+  band_solve(nullptr, T->z);
   T->launches++;
   k_tl_h<<<blocks_for((int64_t)R * V, 256), 256, 0, s>>>(R, V, T->d_offp, T->d_offs, T->d_ci, T->J, T->z, T->h, T->mask);
   T->launches++;
-  k_tl_ic_solve<<<(unsigned)V, 512, (sizeof(double) + sizeof(int)) * R, s>>>(R, V, T->IC, T->icpiv, T->h, T->w, T->mask);
-  T->launches++;
-  k_tl_band_solve<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
-                                        T->cs, b, T->d_row_a, T->w, out, T->mask, T->max_piece, T->max_colw);
+  if (T->fp32)
+    k_tl_ic_solve<float><<<(unsigned)V, 512, (sizeof(float) + sizeof(int)) * R, s>>>(R, V, T->IC32, T->icpiv, T->h,
+                                                                                     T->w, T->mask);
+  else
+    k_tl_ic_solve<double><<<(unsigned)V, 512, (sizeof(double) + sizeof(int)) * R, s>>>(R, V, T->IC, T->icpiv, T->h,
+                                                                                       T->w, T->mask);
+  band_solve(T->w, out);
   return ck(cudaGetLastError(), "apply");
 }
 
@@ -1389,9 +1440,12 @@ ks_torn* untorn_of(ks_torn* T) {
     return nullptr;
   }
   const size_t band_smem = torn_solve_smem(U);
-  if (band_smem > 48 * 1024 && band_smem > torn_solve_smem(T))
-    cudaFuncSetAttribute(k_tl_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
+  if (band_smem > 48 * 1024 && band_smem > torn_solve_smem(T)) {
+    cudaFuncSetAttribute(k_tl_band_solve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
+    cudaFuncSetAttribute(k_tl_band_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
+  }
   U->st = T->st;
+  U->fp32 = T->fp32;
   T->untorn = U;
   return U;
 }
@@ -1416,7 +1470,7 @@ int untorn_solve(ks_torn* T, const std::vector<uint8_t>& want, std::vector<uint8
       ck(cudaMemcpyAsync(U->rhs, T->rhs, sizeof(double) * n * V, cudaMemcpyDeviceToDevice, s), "untorn rhs"))
     return KS_ECUDA;
   U->have.assign(V, 0);
-  const int64_t l0 = U->launches;
+  const int64_t l0 = U->launches, s0 = U->solves, f0 = U->refactors, r0 = U->refines;
   std::vector<uint8_t> oku;
   int rc = torn_solve(U, want, false, &oku);
   if (rc) return rc;
@@ -1427,6 +1481,10 @@ int untorn_solve(ks_torn* T, const std::vector<uint8_t>& want, std::vector<uint8
   for (int64_t v = 0; v < V; v++) (*ok)[v] = want[v] && oku[v];
   T->fallbacks += count;
   T->launches += U->launches - l0 + 2;
+  T->solves += U->solves - s0;
+  T->refactors += U->refactors - f0;
+  T->refines += U->refines - r0;
+  T->max_passes = std::max(T->max_passes, U->max_passes);
   return KS_OK;
 }
 
@@ -1509,9 +1567,15 @@ extern "C" int ks_torn_create(const ks_topology* topo, int32_t n_variants, const
   if (rc) { set_error(err); delete T; return rc; }
   if ((rc = alloc_numeric(T))) { delete T; return rc; }
   const size_t ic_smem = (sizeof(double) + sizeof(int)) * (size_t)T->R;
-  if (ic_smem > 48 * 1024) cudaFuncSetAttribute(k_tl_ic_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ic_smem);
+  if (ic_smem > 48 * 1024) {
+    cudaFuncSetAttribute(k_tl_ic_solve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ic_smem);
+    cudaFuncSetAttribute(k_tl_ic_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ic_smem);
+  }
   const size_t band_smem = torn_solve_smem(T);
-  if (band_smem > 48 * 1024) cudaFuncSetAttribute(k_tl_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
+  if (band_smem > 48 * 1024) {
+    cudaFuncSetAttribute(k_tl_band_solve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
+    cudaFuncSetAttribute(k_tl_band_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
+  }
   if (cudaStreamCreateWithFlags(&T->own, cudaStreamNonBlocking) != cudaSuccess) {
     set_error("ks_torn_create: stream creation failed");
     delete T;
@@ -1638,6 +1702,8 @@ extern "C" int ks_torn_op(ks_torn* T, const ks_options* opt, int32_t reuse, doub
   int rc = fresh_state(T, 0.0, 0.0);
   if (rc) return rc;
   KOpts o = ks_kopts_from(opt);
+  T->fp32 = o.mixed != 0;
+  if (T->untorn) T->untorn->fp32 = T->fp32;
   LoadParams lp;
   lp.mode = ModeOP; lp.method = BE; lp.time = 0; lp.h = 0; lp.rh = 0; lp.initJct = true; lp.gmin = o.gmin;
   lp.srcStepping = false; lp.srcFact = 0;
@@ -1666,6 +1732,8 @@ extern "C" int ks_torn_tran(ks_torn* T, const ks_tran_spec* spec, const ks_optio
   int rc = fresh_state(T, spec->step, spec->stop);
   if (rc) return rc;
   KOpts o = ks_kopts_from(opt);
+  T->fp32 = o.mixed != 0;
+  if (T->untorn) T->untorn->fp32 = T->fp32;
   std::vector<int32_t> status(V, KS_STATUS_OK), iters(V, 0), steps(V, 0);
   int32_t* d_probes = nullptr;
   double* d_wave = nullptr;
