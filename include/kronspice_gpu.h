@@ -56,7 +56,8 @@ typedef enum {
   KS_STATUS_TIMESTEP_TOO_SMALL = 4,/* analysis.ErrTimestepTooSmall analysis/tran.go:19 */
   KS_STATUS_TOO_MANY_STEPS = 5,    /* analysis.ErrTooManySteps     analysis/tran.go:20 */
   KS_STATUS_INTERRUPTED = 6,       /* context deadline / cancel    analysis/op.go:81-89 */
-  KS_STATUS_NOT_RUN = 7            /* circuit was not solved (earlier error)          */
+  KS_STATUS_NOT_RUN = 7,           /* circuit was not solved (earlier error)          */
+  KS_STATUS_LEDGER = 8             /* em.ErrLedgerResidual         em/energy.go:18    */
 } ks_status;
 
 /* ---- element kinds (circuit/circuit.go:41-99) --------------------------- */
@@ -214,6 +215,13 @@ typedef struct {
                              uses to catch a prediction that led Newton to another
                              operating point.  Its iterations count in out_iters.
                              0: no check. */
+  double ledger_tol;      /* ks_op_results / ks_tran_results: relative ledger
+                             residual above which a circuit gets KS_STATUS_LEDGER
+                             (Options.LedgerTolerance; <= 0: 1e-9,
+                             em.DefaultTolerance em/energy.go:21) */
+  int32_t skip_energy_check; /* Options.SkipEnergyCheck: build the ledger, never
+                             fail a circuit on it */
+  int32_t reserved0;
 } ks_options;
 
 /* ---- transient request (analysis/tran.go:26-59) ------------------------- */
@@ -433,6 +441,77 @@ int ks_tran_async(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, 
 
 /* Number of points a fixed-step transient records. */
 int ks_tran_points(const ks_tran_spec* spec, int32_t* n_points);
+
+/* ---- element results and the energy ledger -------------------------------
+ * What the reference's analyses return beside the solution: each element's
+ * operating point and power, and the open-system energy ledger.  Computed on
+ * the device at the accepted solution, from the linearization of each device's
+ * last load, as (*Sim).result (analysis/op.go:361-403) and the transient
+ * recorder (analysis/tran.go:291-386) do; the ledger sums follow
+ * em.Accumulator (em/energy.go:24-80): a port's power goes to dissipation when
+ * it leaves through the thermal port, else to inflow or outflow; storage
+ * powers and model-supplied powers in their own columns.  Round-off estimate:
+ * 64 * 2^-52 * sum |x_i| (|A| |x| + |rhs|)_i of the last linear system
+ * (analysis/op.go:275-282).  These calls run on the generic kernels.
+ *
+ * Columns of one element's row (output.ElementResult): */
+enum { KS_RES_VOLTAGE = 0,        /* Voltage (terminal 1 - terminal 2)            */
+       KS_RES_CURRENT = 1,        /* Current (into terminal 1)                    */
+       KS_RES_POWER = 2,          /* PowerAbsorbed                                */
+       KS_RES_STORAGE_POWER = 3,  /* StoragePower (energy-storing elements)       */
+       KS_RES_STORED_ENERGY = 4,  /* StoredEnergy                                 */
+       KS_RES_EXTERIOR_POWER = 5, /* ExteriorPower through the element's modeled
+                                     exterior port: thermal for R > 0, D, Q, M;
+                                     electrical for V and I; none for C, L and
+                                     R < 0 (0)                                    */
+       KS_RES_MODEL_SUPPLIED = 6, /* ModelSuppliedPower (R < 0)                   */
+       KS_RES_COLS = 7 };
+/* Columns of an operating point's ledger (output.Ledger, em.BuildLedger
+ * em/energy.go:90-121): */
+enum { KS_LEDGER_INFLOW = 0, KS_LEDGER_OUTFLOW = 1, KS_LEDGER_DISSIPATION = 2, KS_LEDGER_STORAGE_RATE = 3,
+       KS_LEDGER_MODEL_SUPPLIED = 4, KS_LEDGER_RESIDUAL = 5, KS_LEDGER_SCALE = 6, KS_LEDGER_ROUNDOFF = 7,
+       KS_LEDGER_COLS = 8 };
+/* Columns of one transient point's ledger (the Waveform's Ledger series,
+ * analysis/tran.go:336-345): */
+enum { KS_TPOINT_INFLOW = 0, KS_TPOINT_OUTFLOW = 1, KS_TPOINT_DISSIPATION = 2, KS_TPOINT_STORAGE_RATE = 3,
+       KS_TPOINT_MODEL_SUPPLIED = 4, KS_TPOINT_RESIDUAL = 5, KS_TPOINT_STORED_ENERGY = 6, KS_TPOINT_COLS = 7 };
+/* Columns of a transient's ledger summary (recorder.finish, analysis/tran.go:350-386): */
+enum { KS_TSUM_MAX_RELATIVE_RESIDUAL = 0, KS_TSUM_ENERGY_IN = 1, KS_TSUM_ENERGY_OUT = 2,
+       KS_TSUM_ENERGY_DISSIPATED = 3, KS_TSUM_ENERGY_MODEL_SUPPLIED = 4, KS_TSUM_STORED_START = 5,
+       KS_TSUM_STORED_END = 6, KS_TSUM_INTEGRATION_MISMATCH = 7, KS_TSUM_COLS = 8 };
+
+/* The operating point of every circuit (as ks_op) with its results:
+ *   out_elem   [n_circ][n_elem][KS_RES_COLS]   (NULL: not written)
+ *   out_ledger [n_circ][KS_LEDGER_COLS]        (NULL: not written)
+ * and em.CheckLedger (em/energy.go:123-128) on each solved circuit: a relative
+ * residual above ks_options.ledger_tol gives KS_STATUS_LEDGER unless
+ * skip_energy_check.  Rows of circuits that did not solve are zeros.
+ * Replaces analysis.OP's *output.Result (analysis/op.go:340-357). */
+int ks_op_results(ks_batch* b, const ks_options* opt, const double* x0, double* out_x, int32_t* out_status,
+                  int32_t* out_iters, double* out_elem, double* out_ledger, void* stream);
+int ks_op_results_async(ks_batch* b, const ks_options* opt, const double* x0_dev, double* out_x_dev,
+                        int32_t* out_status_dev, int32_t* out_iters_dev, double* out_elem_dev,
+                        double* out_ledger_dev, void* stream);
+
+/* A transient (as ks_tran) with the Waveform's element series and ledger at
+ * every recorded point, laid out as out_wave (fixed-step: [n_points][n_circ][...],
+ * adaptive: [n_circ][capacity][...]):
+ *   out_elem   [...][n_elem][2]  current and absorbed power (Waveform.I, .P)
+ *   out_ledger [...][KS_TPOINT_COLS]
+ *   out_summary [n_circ][KS_TSUM_COLS]
+ * Every point is checked as recorder.record does (analysis/tran.go:291-318):
+ * a point out of balance by more than 1e-3 of the run's peak power stops the
+ * circuit with KS_STATUS_LEDGER, and so does a largest relative residual above
+ * ks_options.ledger_tol at the end (unless skip_energy_check).  The imposed
+ * first point of a UIC run is recorded, not checked.  In fixed-step mode the
+ * recorded (grid) points are the checked points.  Any output may be NULL. */
+int ks_tran_results(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
+                    double* out_time, double* out_wave, double* out_elem, double* out_ledger, double* out_summary,
+                    int32_t* out_npts, int32_t* out_status, int32_t* out_steps, int32_t* out_iters, void* stream);
+int ks_tran_results_async(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
+                          double* out_time_dev, double* out_wave_dev, double* out_elem_dev, double* out_ledger_dev,
+                          double* out_summary_dev, int32_t* out_npts_dev, int32_t* out_status_dev,
+                          int32_t* out_steps_dev, int32_t* out_iters_dev, void* stream);
 
 /* ---- learned Newton start ------------------------------------------------
  * A BF16 MLP in -> H -> H -> H -> out (ReLU) on the GPU's tensor cores that

@@ -26,7 +26,30 @@ namespace kso {
 
 enum Err { E_OK = 0, E_SINGULAR = KS_STATUS_SINGULAR, E_NONFINITE = KS_STATUS_NONFINITE,
            E_NOCONV = KS_STATUS_NO_CONVERGENCE, E_TSTEP = KS_STATUS_TIMESTEP_TOO_SMALL,
-           E_TOOMANY = KS_STATUS_TOO_MANY_STEPS, E_INTR = KS_STATUS_INTERRUPTED, E_BAD = 100 };
+           E_TOOMANY = KS_STATUS_TOO_MANY_STEPS, E_INTR = KS_STATUS_INTERRUPTED, E_LEDGER = KS_STATUS_LEDGER,
+           E_BAD = 100 };
+
+// em.Accumulator, em/energy.go:24-80: one set of classification rules for the
+// operating point's ledger and every transient point's.
+struct Acc {
+  double in = 0, out = 0, diss = 0, store = 0, sup = 0, scale = 0;
+  void port(int ch, double pw) {  // AddPort :33-51
+    if (pw == 0) return;
+    scale += std::fabs(pw);
+    if (ch == CH_THERMAL && pw < 0) diss += -pw;
+    else if (pw > 0) in += pw;
+    else out += -pw;
+  }
+  void storage(double p) { store += p; scale += std::fabs(p); }  // AddStorage :54-57
+  void supplied(double p) {  // AddModelSupplied :62-68
+    if (p == 0) return;
+    sup += p; scale += std::fabs(p);
+  }
+  double residual() const { return in + sup - out - diss - store; }  // :71-73
+};
+
+constexpr double kLedgerAbsFloor = 1e-21;  // output/result.go:96
+constexpr double kGrossTol = 1e-3;         // analysis/tran.go:272
 
 struct Opts {  // analysis.Options with defaults, analysis/op.go:91-110
   double reltol, abstol, vntol, gmin;
@@ -328,7 +351,38 @@ struct Sim {
     return E_OK;
   }
 
-  int op(const Opts& o, const double* nodeset) {  // analysis/op.go:340-357 (ledger not built)
+  // roundoff, analysis/op.go:275-282: the residual round-off alone can make,
+  // from the last linear system and the solution.
+  double roundoff() {
+    std::vector<double> ab(n);
+    M->absProduct(x.data(), ab.data());
+    double sum = 0;
+    for (int i = 0; i < n; i++) sum += std::fabs(x[i]) * (ab[i] + std::fabs(rhs[i]));
+    return 64 * 0x1p-52 * sum;
+  }
+
+  // result + em.BuildLedger, analysis/op.go:361-403 and em/energy.go:90-121:
+  // element rows [ne][KS_RES_COLS] and the ledger [KS_LEDGER_COLS].
+  void opResult(double* elem, double* ledger) {
+    Acc a;
+    for (size_t k = 0; k < devs.size(); k++) {
+      OpPt o = devs[k]->operating(x.data());
+      if (elem) {
+        double* r = elem + k * KS_RES_COLS;
+        r[KS_RES_VOLTAGE] = o.v; r[KS_RES_CURRENT] = o.i; r[KS_RES_POWER] = o.p; r[KS_RES_STORAGE_POWER] = o.ps;
+        r[KS_RES_STORED_ENERGY] = o.w; r[KS_RES_EXTERIOR_POWER] = o.ext; r[KS_RES_MODEL_SUPPLIED] = o.sup;
+      }
+      a.port(o.ch, o.ext);
+      if (o.stores) a.storage(o.ps);
+      if (o.sup != 0) a.supplied(o.sup);
+    }
+    ledger[KS_LEDGER_INFLOW] = a.in; ledger[KS_LEDGER_OUTFLOW] = a.out; ledger[KS_LEDGER_DISSIPATION] = a.diss;
+    ledger[KS_LEDGER_STORAGE_RATE] = a.store; ledger[KS_LEDGER_MODEL_SUPPLIED] = a.sup;
+    ledger[KS_LEDGER_RESIDUAL] = a.residual(); ledger[KS_LEDGER_SCALE] = a.scale;
+    ledger[KS_LEDGER_ROUNDOFF] = roundoff();
+  }
+
+  int op(const Opts& o, const double* nodeset) {  // analysis/op.go:340-357 (ledger: opResult)
     lc.mode = ModeOP; lc.time = 0;
     int e = dcSolve(o, nodeset);
     if (e) return e;
@@ -347,14 +401,96 @@ struct Sim {
     double *t = nullptr, *x = nullptr, *i = nullptr;
     int n = 0, ne = 0;
     double start = 0;
+    // the energy ledger of every point (recorder, analysis/tran.go:248-386); on
+    // when `ledger` is set.  ip [cap][ne][2] current and absorbed power, lp
+    // [cap][KS_TPOINT_COLS].
+    bool ledger = false, check = true;
+    double *ip = nullptr, *lp = nullptr;
+    double peakScale = 0, worstAbs = 0, worstT = 0, tol = 1e-9;
+    bool imposedFirst = false;
+    int recorded = 0;  // points recorded (capacity aside)
+    double tPrev = 0, yPrev[4] = {0, 0, 0, 0}, e[4] = {0, 0, 0, 0};  // trapezoid sums: in, out, dissipated, supplied
+    double storedStart = 0, storedEnd = 0;
   };
-  void record(Rec& r, double t) {
-    if (t < r.start) return;
-    if (r.npts >= r.cap) { r.npts++; return; }
+  // recorder.record, analysis/tran.go:291-347.  Returns E_LEDGER when the
+  // point is out of balance by more than kGrossTol of the run's peak power.
+  int record(Rec& r, double t, bool imposed = false) {
+    int err = E_OK;
+    std::vector<OpPt> ops;
+    Acc a;
+    double stored = 0;
+    if (r.ledger) {
+      ops.resize(devs.size());
+      for (size_t k = 0; k < devs.size(); k++) ops[k] = devs[k]->operating(x.data());
+      for (size_t k = 0; k < devs.size(); k++) a.port(ops[k].ch, ops[k].ext);  // s.ports, element order
+      for (size_t k = 0; k < devs.size(); k++) a.supplied(ops[k].sup);        // s.supply
+      for (int k : reactive) { a.storage(ops[k].ps); stored += ops[k].w; }    // s.reactive
+      if (a.scale > r.peakScale) r.peakScale = a.scale;
+      double res = std::fabs(a.residual());
+      if (!imposed && res > std::max(kLedgerAbsFloor, roundoff())) {
+        if (res > r.worstAbs) { r.worstAbs = res; r.worstT = t; }
+        double rr = res / r.peakScale;
+        if (rr > kGrossTol && r.check) {
+          char buf[192];
+          snprintf(buf, sizeof buf, "em: energy ledger does not balance at t = %g s: residual %.3g W (relative %.3g)", t,
+                   a.residual(), rr);
+          msg = buf;
+          err = E_LEDGER;
+        }
+      }
+    }
+    if (t < r.start) return err;
+    if (r.ledger) {  // the running trapezoid sums of recorder.finish, :362-381
+      double y[4] = {a.in, a.out, a.diss, a.sup};
+      if (r.recorded == 0) { r.imposedFirst = imposed; r.storedStart = stored; }
+      else
+        for (int q = 0; q < 4; q++)
+          r.e[q] += (r.recorded == 1 && r.imposedFirst) ? y[q] * (t - r.tPrev) : 0.5 * (y[q] + r.yPrev[q]) * (t - r.tPrev);
+      for (int q = 0; q < 4; q++) r.yPrev[q] = y[q];
+      r.tPrev = t; r.storedEnd = stored;
+    }
+    r.recorded++;
+    if (r.npts >= r.cap) { r.npts++; return err; }
     int k = r.npts++;
     if (r.t) r.t[k] = t;
     if (r.x) for (int j = 0; j < n; j++) r.x[(size_t)k * n + j] = x[j];
     if (r.i) for (int j = 0; j < (int)devs.size(); j++) r.i[(size_t)k * devs.size() + j] = devs[j]->current(x.data());
+    if (r.ledger && r.ip)
+      for (size_t j = 0; j < devs.size(); j++) {
+        r.ip[((size_t)k * devs.size() + j) * 2] = ops[j].i;
+        r.ip[((size_t)k * devs.size() + j) * 2 + 1] = ops[j].p;
+      }
+    if (r.ledger && r.lp) {
+      double* l = r.lp + (size_t)k * KS_TPOINT_COLS;
+      l[KS_TPOINT_INFLOW] = a.in; l[KS_TPOINT_OUTFLOW] = a.out; l[KS_TPOINT_DISSIPATION] = a.diss;
+      l[KS_TPOINT_STORAGE_RATE] = a.store; l[KS_TPOINT_MODEL_SUPPLIED] = a.sup; l[KS_TPOINT_RESIDUAL] = a.residual();
+      l[KS_TPOINT_STORED_ENERGY] = stored;
+    }
+    return err;
+  }
+  // recorder.finish, analysis/tran.go:350-386: summary [KS_TSUM_COLS]; E_LEDGER
+  // when the largest residual relative to the run's peak power exceeds tol.
+  int finish(Rec& r, double* sum) {
+    int err = E_OK;
+    double mrr = 0;
+    if (r.peakScale > 0) {
+      mrr = r.worstAbs / r.peakScale;
+      if (mrr > r.tol && r.check) {
+        char buf[192];
+        snprintf(buf, sizeof buf, "em: energy ledger does not balance at t = %g s: residual %.3g W (relative to the run's peak power %.3g)",
+                 r.worstT, r.worstAbs, mrr);
+        msg = buf;
+        err = E_LEDGER;
+      }
+    }
+    if (sum) {
+      sum[KS_TSUM_MAX_RELATIVE_RESIDUAL] = mrr;
+      sum[KS_TSUM_ENERGY_IN] = r.e[0]; sum[KS_TSUM_ENERGY_OUT] = r.e[1];
+      sum[KS_TSUM_ENERGY_DISSIPATED] = r.e[2]; sum[KS_TSUM_ENERGY_MODEL_SUPPLIED] = r.e[3];
+      sum[KS_TSUM_STORED_START] = r.storedStart; sum[KS_TSUM_STORED_END] = r.storedEnd;
+      sum[KS_TSUM_INTEGRATION_MISMATCH] = r.e[0] + r.e[3] - r.e[1] - r.e[2] - (r.storedEnd - r.storedStart);
+    }
+    return err;
   }
 
   // analysis/tran.go:95-231 (adaptive) and the fixed-step mode.
@@ -380,7 +516,7 @@ struct Sim {
       if (e) { msg = "transient operating point: " + msg; return e; }
       accept(0, ModeTranOP);
     }
-    record(rec, 0);
+    if (int le = record(rec, 0, sp.uic != 0)) { *stepsOut = 0; return le; }  // the UIC point is imposed: not checked
     TruncCtx tc{0, 0, BE, o.reltol, o.abstol, o.vntol, chgtol, trtol};
     double t = 0;
     double h = fixed ? sp.step : std::min(maxStep, std::min(sp.step, sp.stop / 100)) / 10;
@@ -442,7 +578,9 @@ struct Sim {
         }
       }
       accept(tn, ModeTran);
-      if (!fixed || onGrid) record(rec, tn);
+      if (!fixed || onGrid) {
+        if (int le = record(rec, tn)) { *stepsOut = accepted; return le; }
+      }
       xAcc = x;
       accepted++;
       t = tn;
@@ -497,6 +635,37 @@ extern "C" int kso_op(const ks_topology* t, const double* values, const ks_optio
   return e;
 }
 
+// analysis.OP with its *output.Result: element rows, the ledger, and
+// em.CheckLedger (analysis/op.go:340-357).
+extern "C" int kso_op_results(const ks_topology* t, const double* values, const ks_options* o, const double* x0,
+                              double* x_out, double* elem_out, double* ledger_out, int32_t* iters, char* err,
+                              int errlen) {
+  Sim s;
+  Opts opt(o);
+  if (s.build(t, values, 0, 0, opt.backend)) { copyMsg(s.msg, err, errlen); return KS_STATUS_NOT_RUN; }
+  int e = s.op(opt, x0);
+  if (iters) *iters = s.iters;
+  if (x_out) for (int i = 0; i < s.n; i++) x_out[i] = s.x[i];
+  if (e == E_OK) {
+    double led[KS_LEDGER_COLS];
+    s.opResult(elem_out, led);
+    if (ledger_out) for (int i = 0; i < KS_LEDGER_COLS; i++) ledger_out[i] = led[i];
+    // RelativeResidual (output/result.go:100-109) against the tolerance, CheckLedger em/energy.go:123-128
+    double res = std::fabs(led[KS_LEDGER_RESIDUAL]), rr = 0;
+    if (led[KS_LEDGER_SCALE] != 0 && res > std::max(kLedgerAbsFloor, led[KS_LEDGER_ROUNDOFF])) rr = res / led[KS_LEDGER_SCALE];
+    double tol = o && o->ledger_tol > 0 ? o->ledger_tol : 1e-9;
+    if (rr > tol && !(o && o->skip_energy_check)) {
+      char buf[160];
+      snprintf(buf, sizeof buf, "em: energy ledger does not balance: residual %.3g W (relative %.3g > %.3g)",
+               led[KS_LEDGER_RESIDUAL], rr, tol);
+      s.msg = buf;
+      e = E_LEDGER;
+    }
+  }
+  copyMsg(e ? s.msg : std::string(), err, errlen);
+  return e;
+}
+
 extern "C" int kso_ac(const ks_topology* t, const double* values, const ks_options* o, const double* freqs, int nf,
                       double* x_out, char* err, int errlen) {
   Sim s;
@@ -541,6 +710,31 @@ extern "C" int kso_tran(const ks_topology* t, const double* values, const ks_tra
   rec.cap = capacity; rec.t = t_out; rec.x = x_out; rec.i = i_out; rec.n = s.n; rec.ne = (int)s.devs.size();
   int st = 0;
   int e = s.tran(*spec, opt, rec, &st);
+  if (npts) *npts = std::min(rec.npts, capacity);
+  if (steps) *steps = st;
+  if (iters) *iters = s.iters;
+  copyMsg(e ? s.msg : std::string(), err, errlen);
+  return e;
+}
+
+// analysis.Tran with the Waveform's element series and ledger (recorder,
+// analysis/tran.go:248-386).
+extern "C" int kso_tran_results(const ks_topology* t, const double* values, const ks_tran_spec* spec,
+                                const ks_options* o, int capacity, double* t_out, double* x_out, double* elem_out,
+                                double* ledger_out, double* summary_out, int32_t* npts, int32_t* steps,
+                                int32_t* iters, char* err, int errlen) {
+  Sim s;
+  Opts opt(o);
+  if (s.build(t, values, spec->step, spec->stop, opt.backend)) { copyMsg(s.msg, err, errlen); return KS_STATUS_NOT_RUN; }
+  Sim::Rec rec;
+  rec.cap = capacity; rec.t = t_out; rec.x = x_out; rec.n = s.n; rec.ne = (int)s.devs.size();
+  rec.ledger = true; rec.ip = elem_out; rec.lp = ledger_out;
+  rec.check = !(o && o->skip_energy_check);
+  rec.tol = o && o->ledger_tol > 0 ? o->ledger_tol : 1e-9;
+  int st = 0;
+  int e = s.tran(*spec, opt, rec, &st);
+  int fe = s.finish(rec, summary_out);
+  if (e == E_OK) e = fe;
   if (npts) *npts = std::min(rec.npts, capacity);
   if (steps) *steps = st;
   if (iters) *iters = s.iters;

@@ -40,6 +40,21 @@ int kso_tran(const ks_topology* t, const double* values, const ks_tran_spec* spe
              const ks_options* o, int capacity, double* t_out, double* x_out, double* i_out,
              int32_t* npts, int32_t* steps, int32_t* iters, char* err, int errlen);
 
+/* analysis.OP with its result (analysis/op.go:340-403): elem_out [n_elem][KS_RES_COLS],
+ * ledger_out [KS_LEDGER_COLS] (nullable), and em.CheckLedger: KS_STATUS_LEDGER when
+ * the relative residual exceeds o->ledger_tol (1e-9) unless o->skip_energy_check. */
+int kso_op_results(const ks_topology* t, const double* values, const ks_options* o, const double* x0,
+                   double* x_out, double* elem_out, double* ledger_out, int32_t* iters, char* err, int errlen);
+
+/* analysis.Tran with the Waveform's element series and ledger (analysis/tran.go:248-386):
+ * elem_out [cap][n_elem][2] current and absorbed power, ledger_out [cap][KS_TPOINT_COLS],
+ * summary_out [KS_TSUM_COLS] (all nullable).  KS_STATUS_LEDGER as recorder.record
+ * and recorder.finish decide it. */
+int kso_tran_results(const ks_topology* t, const double* values, const ks_tran_spec* spec,
+                     const ks_options* o, int capacity, double* t_out, double* x_out, double* elem_out,
+                     double* ledger_out, double* summary_out, int32_t* npts, int32_t* steps, int32_t* iters,
+                     char* err, int errlen);
+
 /* Batches over host threads (the timed CPU baseline).  values [nc][n_values];
  * x0 nullable [nc][n]; x_out [nc][n]. */
 int kso_batch_op(const ks_topology* t, const double* values, int nc, const ks_options* o,

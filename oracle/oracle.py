@@ -40,7 +40,10 @@ class Options(ctypes.Structure):
                 ("no_gmin_stepping", ctypes.c_int32), ("no_source_stepping", ctypes.c_int32),
                 ("no_pseudo_transient", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("backend", ctypes.c_int32), ("max_iter_total", ctypes.c_int32),
-                ("deadline_s", ctypes.c_double)]
+                ("deadline_s", ctypes.c_double), ("mixed_passes", ctypes.c_int32),
+                ("fp32_start_iters", ctypes.c_int32), ("start_check", ctypes.c_double),
+                ("ledger_tol", ctypes.c_double), ("skip_energy_check", ctypes.c_int32),
+                ("reserved0", ctypes.c_int32)]
 
 
 class TranSpec(ctypes.Structure):
@@ -62,6 +65,9 @@ def lib():
         L.kso_op.argtypes = [P, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
         L.kso_dc.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, P, P, ctypes.c_char_p, ctypes.c_int]
         L.kso_tran.argtypes = [P, P, P, P, ctypes.c_int, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
+        L.kso_op_results.argtypes = [P, P, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
+        L.kso_tran_results.argtypes = [P, P, P, P, ctypes.c_int, P, P, P, P, P, P, P, P, ctypes.c_char_p,
+                                       ctypes.c_int]
         L.kso_batch_op.argtypes = [P, P, ctypes.c_int, P, P, ctypes.c_int, P, P, P]
         L.kso_batch_tran.argtypes = [P, P, ctypes.c_int, P, P, ctypes.c_int, P, P, P, P]
         L.kso_unknowns.argtypes = [P, P, P, P]
@@ -98,9 +104,9 @@ class Packed:
 
 
 def options(reltol=0.0, abstol=0.0, vntol=0.0, gmin=0.0, itl1=0, itl4=0, backend=0,
-            no_gmin=False, no_source=False, no_pt=False, deadline_s=0.0):
+            no_gmin=False, no_source=False, no_pt=False, deadline_s=0.0, ledger_tol=0.0, skip_energy_check=False):
     return Options(reltol, abstol, vntol, gmin, itl1, itl4, int(no_gmin), int(no_source), int(no_pt),
-                   0, backend, 0, deadline_s)
+                   0, backend, 0, deadline_s, 0, 0, 0.0, ledger_tol, int(skip_energy_check), 0)
 
 
 def unknowns(pk):
@@ -125,6 +131,50 @@ def op(pk, opt=None, x0=None):
     st = lib().kso_op(pk.tref(), _ptr(pk.values), ctypes.byref(o), _ptr(x0a), _ptr(x), _ptr(cur),
                       ctypes.byref(it), err, 512)
     return st, x, cur[:len(pk.elements)], it.value, err.value.decode()
+
+
+RES_COLS, LEDGER_COLS, TPOINT_COLS, TSUM_COLS = 7, 8, 7, 8
+RES = dict(voltage=0, current=1, power=2, storage_power=3, stored_energy=4, exterior_power=5, model_supplied=6)
+LEDGER = dict(inflow=0, outflow=1, dissipation=2, storage_rate=3, model_supplied=4, residual=5, scale=6, roundoff=7)
+TPOINT = dict(inflow=0, outflow=1, dissipation=2, storage_rate=3, model_supplied=4, residual=5, stored_energy=6)
+TSUM = dict(max_relative_residual=0, energy_in=1, energy_out=2, energy_dissipated=3, energy_model_supplied=4,
+            stored_start=5, stored_end=6, integration_mismatch=7)
+
+
+def op_results(pk, opt=None, x0=None):
+    """analysis.OP with its result: (status, x, elem [ne][RES_COLS], ledger [LEDGER_COLS], iters, message)."""
+    n, _ = unknowns(pk)
+    x = np.zeros(n)
+    elem = np.zeros((max(1, len(pk.elements)), RES_COLS))
+    led = np.zeros(LEDGER_COLS)
+    it = ctypes.c_int32()
+    err = ctypes.create_string_buffer(512)
+    o = opt or options()
+    x0a = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
+    st = lib().kso_op_results(pk.tref(), _ptr(pk.values), ctypes.byref(o), _ptr(x0a), _ptr(x), _ptr(elem), _ptr(led),
+                              ctypes.byref(it), err, 512)
+    return st, x, elem[:len(pk.elements)], led, it.value, err.value.decode()
+
+
+def tran_results(pk, spec, opt=None, capacity=200000):
+    """analysis.Tran with the Waveform's element series and ledger:
+    (status, t, x, elem [k][ne][2], ledger [k][TPOINT_COLS], summary [TSUM_COLS], steps, iters, message)."""
+    n, _ = unknowns(pk)
+    ne = max(1, len(pk.elements))
+    t = np.zeros(capacity)
+    x = np.zeros((capacity, n))
+    elem = np.zeros((capacity, ne, 2))
+    led = np.zeros((capacity, TPOINT_COLS))
+    summ = np.zeros(TSUM_COLS)
+    npts, steps, it = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    err = ctypes.create_string_buffer(512)
+    o = opt or options()
+    st = lib().kso_tran_results(pk.tref(), _ptr(pk.values), ctypes.byref(spec), ctypes.byref(o), capacity, _ptr(t),
+                                _ptr(x), _ptr(elem), _ptr(led), _ptr(summ), ctypes.byref(npts), ctypes.byref(steps),
+                                ctypes.byref(it), err, 512)
+    k = npts.value
+    return (st, t[:k], x[:k], elem[:k, :len(pk.elements)], led[:k], summ, steps.value, it.value,
+            err.value.decode())
 
 
 def dc(pk, src, vals, opt=None):

@@ -221,24 +221,68 @@ struct BJT : Device {
     return std::fabs(ichat - ic) <= reltol * std::max(std::fabs(ichat), std::fabs(ic)) + abstol &&
            std::fabs(ibhat - ib) <= reltol * std::max(std::fabs(ibhat), std::fabs(ib)) + abstol;
   }
-  double current(const double* x) override {  // terminalCurrents :537-567, collector current
+  // terminalCurrents, :537-567: currents into the collector, base, emitter and
+  // substrate terminals from the linearization of the last load, and the power
+  // into the junction charges; v4 receives the junction voltages.
+  void terminals(const double* x, double* ic, double* ib, double* ie, double* is, double* ps, double v4[4]) const {
     double be, bc, bx, cs;
     voltages(x, &be, &bc, &bx, &cs);
     double t = Type;
     const DC& d = dc;
     double dbe = be - vbe, dbc = bc - vbc;
     double it = t * (d.it + d.itBE * dbe + d.itBC * dbc);
+    double ibe = t * (d.ibe + d.gpi * dbe);
     double ibc = t * (d.ibc + d.gmu * dbc);
-    double iqbc = 0, iqbx = 0, iqcs = 0;
+    double iqbe = 0, iqbc = 0, iqbx = 0, iqcs = 0;
+    *ps = 0;
     if (tran) {
+      iqbe = t * (iq[0] + ag * ch.c[0] * dbe + ag * ch.dqbeDvbc * dbc);
       iqbc = t * (iq[1] + ag * ch.c[1] * dbc);
       iqbx = t * (iq[2] + ag * ch.c[2] * (bx - vbx));
       iqcs = t * (iq[3] + ag * ch.c[3] * (cs - vcs));
+      *ps = be * t * iqbe + bc * t * iqbc + bx * t * iqbx + cs * t * iqcs;
     }
     double isb = t * (isub + gsub * (cs - vcs)) + iqcs;
-    double ic = it - ibc - iqbc - iqbx;
-    if (SUBS > 0) ic -= isb;
+    *ic = it - ibc - iqbc - iqbx;
+    *ib = ibe + ibc + iqbe + iqbc + iqbx;
+    *ie = -it - ibe - iqbe;
+    if (SUBS > 0) { *is = isb; *ic = *ic - isb; }
+    else { *ib = *ib + isb; *is = -isb; }
+    v4[0] = be; v4[1] = bc; v4[2] = bx; v4[3] = cs;
+  }
+  double current(const double* x) override {  // Operating :571-576, collector current
+    double ic, ib, ie, is, ps, v4[4];
+    terminals(x, &ic, &ib, &ie, &is, &ps, v4);
     return ic;
+  }
+  // StoredEnergy, :630-650: co-energy of the four charges, each along its own
+  // voltage with the others held (quadrature on 8 panels).
+  double storedEnergy(const double v[4]) const {
+    if (!hasCharge) return 0;
+    double w = 0;
+    for (int k = 0; k < 4; k++) {
+      if (v[k] == 0) continue;
+      auto qk = [&](double u) {
+        double vv[4] = {v[0], v[1], v[2], v[3]};
+        vv[k] = u;
+        DC d = evalDC(vv[0], vv[1]);
+        return charges(vv[0], vv[1], vv[2], vv[3], d).q[k];
+      };
+      w += v[k] * qk(v[k]) - integrate(qk, 0, v[k], 8);
+    }
+    return w;
+  }
+  OpPt operating(const double* x) override {  // Operating :571-576, ExteriorPower :675-680
+    double ic, ib, ie, is, ps, v4[4];
+    terminals(x, &ic, &ib, &ie, &is, &ps, v4);
+    OpPt o;
+    double vc = at(x, n, uc), ve = at(x, n, ue);
+    o.p = vc * ic + at(x, n, b) * ib + ve * ie + at(x, n, s) * is;
+    o.v = vc - ve; o.i = ic; o.ps = ps;
+    o.ext = -(o.p - o.ps);
+    o.w = storedEnergy(v4);
+    o.stores = true;
+    return o;
   }
   void loadAC(ACCtx& c) override {  // device/bjt.go:689-711
     DC d = evalDC(vbeAcc, vbcAcc);

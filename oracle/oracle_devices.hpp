@@ -120,6 +120,37 @@ struct ACCtx {
   }
 };
 
+// One element's operating point (device.OperatingPoint, device/device.go) with its
+// ledger entries: ExteriorPower on its one modeled exterior port (channel ch; 0
+// when the port is not modeled), ModelSuppliedPower (device.ModelSupplier),
+// StoredEnergy and whether it is a device.Reactive element (its storage power
+// enters the ledger).
+enum { CH_ELECTRICAL = 0, CH_THERMAL = 1 };
+struct OpPt {
+  double v = 0, i = 0, p = 0, ps = 0;  // Voltage, Current, PowerAbsorbed, StoragePower
+  double w = 0;                        // StoredEnergy
+  double ext = 0;                      // ExteriorPower on channel ch
+  double sup = 0;                      // ModelSuppliedPower
+  int ch = CH_THERMAL;
+  bool stores = false;
+};
+
+// integrate, device/bjt.go:607-627: 16-point Gauss-Legendre on n equal panels
+// (nodes and weights of Abramowitz & Stegun, Table 25.4).
+template <class F>
+static double integrate(F&& f, double a, double b, int n) {
+  static const double gx[8] = {0.0950125098376374, 0.2816035507792589, 0.4580167776572274, 0.6178762444026438,
+                               0.7554044083550030, 0.8656312023878318, 0.9445750230732326, 0.9894009349916499};
+  static const double gw[8] = {0.1894506104550685, 0.1826034150449236, 0.1691565193950025, 0.1495959888165767,
+                               0.1246289712555339, 0.0951585116824928, 0.0622535239386479, 0.0271524594117541};
+  double h = (b - a) / n, s = 0;
+  for (int p = 0; p < n; p++) {
+    double mid = a + (p + 0.5) * h, half = h / 2;
+    for (int k = 0; k < 8; k++) s += gw[k] * (f(mid - half * gx[k]) + f(mid + half * gx[k]));
+  }
+  return s * h / 2;
+}
+
 struct Device {
   int n = 0;  // system size (set after setup)
   virtual void loadAC(ACCtx& c) {}
@@ -127,6 +158,7 @@ struct Device {
   virtual void setup(SetupCtx& c) = 0;
   virtual void load(LoadCtx& c) = 0;
   virtual double current(const double* x) = 0;  // Operating(x).Current
+  virtual OpPt operating(const double* x) = 0;  // Operating, ExteriorPower, ModelSuppliedPower, StoredEnergy
   virtual void accept(const double* x, double t, int mode) {}
   virtual bool nonlinear() const { return false; }
   virtual bool limited() const { return false; }
@@ -161,6 +193,13 @@ struct Resistor : TwoTerm {
     c.M->add(a, a, g); c.M->add(b, b, g); c.M->add(a, b, -g); c.M->add(b, a, -g);
   }
   double current(const double* x) override { return voltage(x) * g; }
+  OpPt operating(const double* x) override {  // device/passive.go:86-113
+    OpPt o;
+    o.v = voltage(x); o.i = o.v * g; o.p = o.v * o.i;
+    if (R > 0) o.ext = -o.p;  // Joule heat out through the thermal port
+    else o.sup = -o.p;        // negative resistance: model-supplied, thermal port not modeled
+    return o;
+  }
   void loadAC(ACCtx& c) override { c.stampY(u[0], u[1], g); }  // device/passive.go:116-123
 };
 
@@ -194,6 +233,13 @@ struct Capacitor : TwoTerm {
     c.addRHS(a, -ihist); c.addRHS(b, ihist);
   }
   double current(const double* x) override { return tran ? geq * voltage(x) + ihist : 0.0; }
+  OpPt operating(const double* x) override {  // :109-130, StoredEnergy :172-175
+    OpPt o;
+    o.v = voltage(x); o.i = current(x); o.p = o.v * o.i; o.ps = o.v * o.i;
+    o.w = 0.5 * C * o.v * o.v;
+    o.stores = true;
+    return o;
+  }
   void accept(const double* x, double t, int mode) override {  // :144-161
     if (mode == ModeUICInit) { iPrev = 0; hist.reset(); }
     else if (mode == ModeOP || mode == ModeTranOP) { vPrev = voltage(x); iPrev = 0; hist.reset(); }
@@ -230,6 +276,13 @@ struct Inductor : TwoTerm {
     c.addRHS(k, r);
   }
   double current(const double* x) override { return x[branch]; }
+  OpPt operating(const double* x) override {  // :289-300, StoredEnergy :340-342
+    OpPt o;
+    o.v = voltage(x); o.i = x[branch]; o.p = o.v * o.i; o.ps = o.v * o.i;
+    o.w = 0.5 * L * o.i * o.i;
+    o.stores = true;
+    return o;
+  }
   void accept(const double* x, double t, int mode) override {  // :312-329
     if (mode == ModeUICInit) { vPrev = 0; hist.reset(); }
     else if (mode == ModeOP || mode == ModeTranOP) { vPrev = 0; iPrev = x[branch]; hist.reset(); }
@@ -386,6 +439,11 @@ struct VSource : TwoTerm {  // device/source.go:75-121
     c.addRHS(k, value);
   }
   double current(const double* x) override { return x[branch]; }
+  OpPt operating(const double* x) override {  // :114-129: delivered power enters from the electrical exterior
+    OpPt o;
+    o.v = voltage(x); o.i = x[branch]; o.p = o.v * o.i; o.ext = -o.p; o.ch = CH_ELECTRICAL;
+    return o;
+  }
   bool breakpointer() const override { return true; }
   double nextBreakpoint(double t) override { return src.nextBreakpoint(t); }
   void setDCOverride(double v) override { src.override_ = v; src.overridden = true; }
@@ -403,6 +461,11 @@ struct ISource : TwoTerm {  // device/source.go:131-177
   void setup(SetupCtx& c) override { setupNodes(c); src.setup(c); }
   void load(LoadCtx& c) override { value = src.at(c); c.addRHS(u[0], -value); c.addRHS(u[1], value); }
   double current(const double*) override { return value; }
+  OpPt operating(const double* x) override {  // :163-177
+    OpPt o;
+    o.v = voltage(x); o.i = value; o.p = o.v * value; o.ext = -o.p; o.ch = CH_ELECTRICAL;
+    return o;
+  }
   bool breakpointer() const override { return true; }
   double nextBreakpoint(double t) override { return src.nextBreakpoint(t); }
   void setDCOverride(double v) override { src.override_ = v; src.overridden = true; }
@@ -520,6 +583,46 @@ struct Diode : TwoTerm {
   double current(const double* x) override {  // :293-301
     double v = at(x, n, ai) - at(x, n, u[1]);
     return (cd + gd * (v - vd)) + (iq + geq * (v - vd));
+  }
+  // intDepletion, :340-361: integral of the depletion charge from 0 to v.
+  double intDepletion(double v) const {
+    if (CJO == 0) return 0;
+    double fcv = FC * VJ;
+    auto below = [&](double w) { return CJO * VJ / (1 - M) * (w + VJ / (2 - M) * (std::pow(1 - w / VJ, 2 - M) - 1)); };
+    if (v < fcv) return below(v);
+    double f1 = VJ * (1 - std::pow(1 - FC, 1 - M)) / (1 - M), f2 = std::pow(1 - FC, 1 + M), f3 = 1 - FC * (1 + M);
+    double dv = v - fcv;
+    return below(fcv) + CJO * f1 * dv + CJO / f2 * (f3 * dv * dv / 2 + M / (2 * VJ) * ((v * v * v - fcv * fcv * fcv) / 3 - fcv * fcv * dv));
+  }
+  // intCurrent, :363-387: integral of the junction current (no gmin) from 0 to v.
+  double intCurrent(double v) const {
+    auto fwd = [&](double w) { return IS * (vte * std::expm1(std::min(w / vte, 700.0)) - w); };
+    double v1 = -3 * vte;
+    if (v >= v1) return fwd(v);
+    double total = fwd(v1);
+    double a3 = std::pow(3 * vte / kE, 3);
+    auto rev = [&](double w) { return -IS * (w - a3 / (2 * w * w)); };
+    double v2 = v;
+    if (hasBV && v < -xbv) v2 = -xbv;
+    total += rev(v2) - rev(v1);
+    if (v2 == v) return total;
+    auto brk = [&](double w) { return IS * vte * std::exp(std::min(-(xbv + w) / vte, 700.0)); };
+    return total + brk(v) - brk(v2);
+  }
+  OpPt operating(const double* x) override {  // Operating :293-301, StoredEnergy :329-334, ExteriorPower :400-405
+    OpPt o;
+    double vj = at(x, n, ai) - at(x, n, u[1]);
+    double ir = cd + gd * (vj - vd), ic = iq + geq * (vj - vd);
+    o.i = ir + ic; o.v = voltage(x); o.p = o.v * o.i; o.ps = vj * ic;
+    o.ext = -(o.p - o.ps);
+    o.stores = true;
+    if (hasCharge) {
+      double id, g, q, cc;
+      curr(vj, &id, &g);
+      charge(vj, id, g, &q, &cc);
+      o.w = vj * q - intDepletion(vj) - TT * intCurrent(vj);
+    }
+    return o;
   }
   void accept(const double* x, double t, int mode) override {  // :304-322
     double v = at(x, n, ai) - at(x, n, u[1]);

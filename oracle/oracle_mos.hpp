@@ -634,7 +634,10 @@ struct MOSFET : Device {
     auto ok = [&](double a, double bb) { return std::fabs(a - bb) <= reltol * std::max(std::fabs(a), std::fabs(bb)) + abstol; };
     return ok(ich - ibd, ichN - ibdN) && ok(ibs + ibd, ibsN + ibdN);
   }
-  double current(const double* x) override {  // terminalCurrents :635-657, drain current
+  // terminalCurrents, :635-657: currents into drain, gate, source and bulk from
+  // the linearization of the last load, and the power into storage; v5 receives
+  // {vgs, vgd, vgb, vbs, vbd}.
+  void terminals(const double* x, double* id, double* ig, double* is, double* ib, double* ps, double v5[5]) const {
     double vgs_, vds_, vbs_, vgb_;
     voltages(x, &vgs_, &vds_, &vbs_, &vgb_);
     double vbd_ = vbs_ - vds_, vgd_ = vgs_ - vds_;
@@ -642,13 +645,59 @@ struct MOSFET : Device {
     double i0, gc[3];
     channelBranch(&i0, gc);
     double ich = t * (i0 + gc[0] * (vgs_ - vgs) + gc[1] * (vds_ - vds) + gc[2] * (vbs_ - vbs));
+    double ibs = t * (cbs + gbs * (vbs_ - vbs));
     double ibd = t * (cbd + gbd * (vbd_ - vbd));
     double iqv[5] = {0, 0, 0, 0, 0};
+    double v[5] = {vgs_, vgd_, vgb_, vbs_, vbd_};
+    *ps = 0;
     if (tran) {
-      double v[5] = {vgs_, vgd_, vgb_, vbs_, vbd_};
-      for (int k = 0; k < 5; k++) iqv[k] = t * (iq[k] + ag * cap(k) * (v[k] - dv[k]));
+      for (int k = 0; k < 5; k++) {
+        iqv[k] = t * (iq[k] + ag * cap(k) * (v[k] - dv[k]));
+        *ps += v[k] * t * iqv[k];
+      }
     }
-    return ich - ibd - iqv[1] - iqv[4];
+    *id = ich - ibd - iqv[1] - iqv[4];
+    *is = -ich - ibs - iqv[0] - iqv[3];
+    *ig = iqv[0] + iqv[1] + iqv[2];
+    *ib = ibs + ibd - iqv[2] + iqv[3] + iqv[4];
+    for (int k = 0; k < 5; k++) v5[k] = v[k];
+  }
+  double current(const double* x) override {  // Operating :660-665, drain current
+    double id, ig, is, ib, ps, v5[5];
+    terminals(x, &id, &ig, &is, &ib, &ps, v5);
+    return id;
+  }
+  // StoredEnergy, :710-731: co-energy of the junction charges (quadrature on 8
+  // panels) and C*v^2/2 of the gate capacitances at the present voltages.
+  double storedEnergy(const double v[5]) const {
+    if (!hasGcap && !hasJcap) return 0;
+    double w = 0;
+    const double cz[2][2] = {{czbs, czbssw}, {czbd, czbdsw}};
+    for (int k = 0; k < 2; k++) {
+      double vv = v[3 + k];
+      if (vv == 0 || cz[k][0] + cz[k][1] == 0) continue;
+      auto qf = [&](double u) { double q, c; bulkCharge(u, cz[k][0], cz[k][1], &q, &c); return q; };
+      w += vv * qf(vv) - integrate(qf, 0, vv, 8);
+    }
+    double o[7];
+    channel(v[0], v[0] - v[1], v[3], o);
+    double mc[3];
+    meyerCaps(v[0], v[1], o[5], o[6], o[0], mc);
+    const double ov[3] = {cgso, cgdo, cgbo};
+    for (int k = 0; k < 3; k++) w += 0.5 * (mc[k] + ov[k]) * v[k] * v[k];
+    return w;
+  }
+  OpPt operating(const double* x) override {  // Operating :660-665, ExteriorPower :760-765
+    double id, ig, is, ib, ps, v5[5];
+    terminals(x, &id, &ig, &is, &ib, &ps, v5);
+    OpPt o;
+    double vd = at(x, n, ud), vs = at(x, n, us);
+    o.p = vd * id + at(x, n, g) * ig + vs * is + at(x, n, b) * ib;
+    o.v = vd - vs; o.i = id; o.ps = ps;
+    o.ext = -(o.p - o.ps);
+    o.w = storedEnergy(v5);
+    o.stores = true;
+    return o;
   }
   void loadAC(ACCtx& c) override {  // device/mosfet.go:779-813
     typedef std::complex<double> cx;
