@@ -22,7 +22,9 @@ class KsOptions(ctypes.Structure):
                 ("no_pseudo_transient", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("backend", ctypes.c_int32), ("max_iter_total", ctypes.c_int32),
                 ("deadline_s", ctypes.c_double), ("mixed_passes", ctypes.c_int32),
-                ("fp32_start_iters", ctypes.c_int32), ("start_check", ctypes.c_double)]
+                ("fp32_start_iters", ctypes.c_int32), ("start_check", ctypes.c_double),
+                ("ledger_tol", ctypes.c_double), ("skip_energy_check", ctypes.c_int32),
+                ("reserved0", ctypes.c_int32)]
 
 
 class KsTranSpec(ctypes.Structure):
@@ -40,7 +42,8 @@ EXPORTS = ["ks_version", "ks_last_error", "ks_validate", "ks_unknowns", "ks_plan
            "ks_multi_destroy", "ks_multi_info", "ks_multi_op", "ks_multi_op_async", "ks_multi_tran",
            "ks_multi_tran_async", "ks_sparse_analyze", "ks_ac", "ks_ac_async", "ks_ac_at", "ks_torn_create",
            "ks_torn_destroy", "ks_torn_plan", "ks_torn_set_stream", "ks_torn_info", "ks_torn_op", "ks_torn_tran",
-           "ks_fp64_peak", "ks_batch_cancel_word"]
+           "ks_fp64_peak", "ks_batch_cancel_word", "ks_op_results", "ks_op_results_async", "ks_tran_results",
+           "ks_tran_results_async"]
 
 _lib = None
 
@@ -78,6 +81,10 @@ def load(build_if_missing=False):
     L.ks_op_async.argtypes = [P, P, P, P, P, P, P]
     L.ks_tran.argtypes = [P, P, P, ctypes.c_int32, P, P, P, P, P, P, P]
     L.ks_tran_async.argtypes = [P, P, P, ctypes.c_int32, P, P, P, P, P, P, P]
+    L.ks_op_results.argtypes = [P, P, P, P, P, P, P, P, P]
+    L.ks_op_results_async.argtypes = [P, P, P, P, P, P, P, P, P]
+    L.ks_tran_results.argtypes = [P, P, P, ctypes.c_int32, P, P, P, P, P, P, P, P, P, P]
+    L.ks_tran_results_async.argtypes = [P, P, P, ctypes.c_int32, P, P, P, P, P, P, P, P, P, P]
     L.ks_tran_points.argtypes = [P, P]
     L.ks_plan_specialize.argtypes = [P, ctypes.c_int32, P, P]
     L.ks_plan_kernel_source.argtypes = [P, ctypes.c_int32, ctypes.c_char_p, ctypes.c_size_t, P]

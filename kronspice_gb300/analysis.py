@@ -45,6 +45,10 @@ class ErrInterrupted(KronspiceError):
     """context deadline or cancel (analysis/op.go:81-89)."""
 
 
+class ErrLedgerResidual(KronspiceError):
+    """em.ErrLedgerResidual (em/energy.go:18): the energy ledger does not balance."""
+
+
 class ErrValidation(KronspiceError):
     """circuit.Validate failures (ErrFloatingNode, ErrBadValue, ... circuit/circuit.go:21-31)."""
 
@@ -59,7 +63,16 @@ STATUS_ERRORS = {1: (ErrSingularMatrix, "solver: singular matrix"),
                  4: (ErrTimestepTooSmall, "analysis: timestep too small"),
                  5: (ErrTooManySteps, "analysis: too many time steps"),
                  6: (ErrInterrupted, "analysis interrupted: context deadline exceeded"),
-                 7: (KronspiceError, "not run")}
+                 7: (KronspiceError, "not run"),
+                 8: (ErrLedgerResidual, "em: energy ledger does not balance")}
+
+# Columns of the element results and the ledgers (include/kronspice_gpu.h)
+RES_COLS, LEDGER_COLS, TPOINT_COLS, TSUM_COLS = 7, 8, 7, 8
+RES = dict(voltage=0, current=1, power=2, storage_power=3, stored_energy=4, exterior_power=5, model_supplied=6)
+LEDGER = dict(inflow=0, outflow=1, dissipation=2, storage_rate=3, model_supplied=4, residual=5, scale=6, roundoff=7)
+TPOINT = dict(inflow=0, outflow=1, dissipation=2, storage_rate=3, model_supplied=4, residual=5, stored_energy=6)
+TSUM = dict(max_relative_residual=0, energy_in=1, energy_out=2, energy_dissipated=3, energy_model_supplied=4,
+            stored_start=5, stored_end=6, integration_mismatch=7)
 
 PREC = {"fp64": 0, "mixed": 1}
 # GPU kernel choice: "auto" (per-topology kernels for large batches), "generic", "specialized"
@@ -87,13 +100,15 @@ class Options:
     mixed_passes: int = 0
     fp32_start_iters: int = 0   # FP32 Newton stage before the FP64 solve (operating points; 0: off)
     start_check: float = 0.0    # re-solve from InitJct when the solution ends this far (V) from x0 (0: off)
+    ledger_tol: float = 0.0     # Options.LedgerTolerance (0: 1e-9)
+    skip_energy_check: bool = False  # Options.SkipEnergyCheck
 
     def c(self):
         return _lib.KsOptions(self.reltol, self.abstol, self.vntol, self.gmin, self.itl1, self.itl4,
                               int(self.no_gmin_stepping), int(self.no_source_stepping),
                               int(self.no_pseudo_transient), PREC[self.precision], KERNEL[self.kernel],
                               self.max_iter_total, self.deadline_s, self.mixed_passes, int(self.fp32_start_iters),
-                              float(self.start_check))
+                              float(self.start_check), float(self.ledger_tol), int(self.skip_energy_check), 0)
 
 
 def _check(rc, what):
@@ -183,6 +198,51 @@ class Batch:
         _check(_lib.load().ks_op(self.handle, ctypes.byref(o), None if x0a is None else x0a.ctypes.data,
                                  x.ctypes.data, st.ctypes.data, it.ctypes.data, stream), "ks_op")
         return x, st, it
+
+    def op_results(self, opt=None, x0=None, stream=None):
+        """analysis.OP with its results for every circuit (ks_op_results): (x, status,
+        iterations, elem [n_circ][n_elem][RES_COLS], ledger [n_circ][LEDGER_COLS])."""
+        o = (opt or Options()).c()
+        B, ne = self.n_circ, len(self.plan.elements)
+        x = np.zeros((B, self.plan.n))
+        st = np.zeros(B, dtype=np.int32)
+        it = np.zeros(B, dtype=np.int32)
+        elem = np.zeros((B, ne, RES_COLS))
+        led = np.zeros((B, LEDGER_COLS))
+        x0a = None
+        if x0 is not None:
+            x0a = np.ascontiguousarray(x0, dtype=np.float64)
+            assert x0a.shape == (B, self.plan.n)
+        _check(_lib.load().ks_op_results(self.handle, ctypes.byref(o), None if x0a is None else x0a.ctypes.data,
+                                         x.ctypes.data, st.ctypes.data, it.ctypes.data, elem.ctypes.data,
+                                         led.ctypes.data, stream), "ks_op_results")
+        return x, st, it, elem, led
+
+    def tran_results(self, spec, opt=None, capacity=0, stream=None):
+        """analysis.Tran with the Waveform's element series and ledger (ks_tran_results):
+        (wave, time, elem [..][n_elem][2], ledger [..][TPOINT_COLS], summary [n_circ][TSUM_COLS],
+        npts, status, steps, iters), laid out as tran() lays out the waveforms."""
+        L = _lib.load()
+        o = (opt or Options()).c()
+        sp = spec.c() if hasattr(spec, "c") else spec
+        B, n, ne = self.n_circ, self.plan.n, len(self.plan.elements)
+        if sp.fixed_step:
+            lead = (int(round(sp.stop / sp.step)) + 1, B)
+            tim = None
+        else:
+            lead = (B, capacity)
+            tim = np.zeros(lead)
+        wave = np.zeros(lead + (n,))
+        elem = np.zeros(lead + (ne, 2))
+        led = np.zeros(lead + (TPOINT_COLS,))
+        summ = np.zeros((B, TSUM_COLS))
+        np_, st, steps, it = (np.zeros(B, dtype=np.int32) for _ in range(4))
+        rc = L.ks_tran_results(self.handle, ctypes.byref(sp), ctypes.byref(o), int(capacity),
+                               None if tim is None else tim.ctypes.data, wave.ctypes.data, elem.ctypes.data,
+                               led.ctypes.data, summ.ctypes.data, np_.ctypes.data, st.ctypes.data, steps.ctypes.data,
+                               it.ctypes.data, stream)
+        _check(rc, "ks_tran_results")
+        return wave, tim, elem, led, summ, np_, st, steps, it
 
     def tran(self, spec, opt=None, capacity=0, record=True, stream=None):
         """analysis.Tran for every circuit (ks_tran).  Fixed-step specs return

@@ -62,6 +62,21 @@ struct ks_batch {
   // cancel word (ks_batch_cancel_word): page-locked, mapped for the device
   int32_t* h_cancel = nullptr;
   int32_t* d_cancel = nullptr;
+  // results (ks_op_results, ks_tran_results): the state copy of the round-off
+  // load [n_state][B], and the host calls' device output staging (grow only)
+  void* d_res_scratch = nullptr;
+  size_t d_res_scratch_bytes = 0;
+  void* d_res_out = nullptr;
+  size_t d_res_out_bytes = 0;
+};
+
+// Element results and ledger outputs of one call (device pointers; on: the
+// results instantiation of the generic kernels runs).
+struct ResOut {
+  double* elem = nullptr;
+  double* ledger = nullptr;
+  double* summary = nullptr;
+  bool on = false;
 };
 
 // Derived constants for an analysis with print step / stop time (0, 0 outside a transient).
@@ -239,6 +254,8 @@ extern "C" void ks_batch_destroy(ks_batch* b) {
   cudaFree(b->d_tints);
   cudaFree(b->d_ac);
   cudaFree(b->d_acout);
+  cudaFree(b->d_res_scratch);
+  cudaFree(b->d_res_out);
   if (b->h_cancel) cudaFreeHost(b->h_cancel);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -339,16 +356,49 @@ extern "C" int ks_batch_cancel_word(ks_batch* b, volatile int32_t** word) {
   return KS_OK;
 }
 
-extern "C" int ks_op_async(ks_batch* b, const ks_options* opt, const double* x0_dev, double* out_x_dev,
-                           int32_t* out_status_dev, int32_t* out_iters_dev, void* stream) {
+// Grow-only device buffer.
+static int grow_dev(void** p, size_t* have, size_t need, const char* what) {
+  if (*have >= need) return KS_OK;
+  cudaFree(*p);
+  *p = nullptr;
+  *have = 0;
+  if (cudaMalloc(p, need) != cudaSuccess) { set_error(std::string(what) + ": device allocation failed"); return KS_ENOMEM; }
+  *have = need;
+  return KS_OK;
+}
+
+// The results options of a call: output pointers, the scratch state of the
+// round-off load, the ledger tolerance; the results run on the generic kernels.
+static int results_opts(ks_batch* b, const ks_options* opt, const ResOut& r, KOpts* o) {
+  if (!r.on) return KS_OK;
+  const size_t need = sizeof(double) * (b->plan->hp.n_state + 1) * b->B;
+  int rc = grow_dev(&b->d_res_scratch, &b->d_res_scratch_bytes, need, "results");
+  if (rc) return rc;
+  o->res_elem = r.elem; o->res_ledger = r.ledger; o->res_summary = r.summary;
+  o->res_scratch = static_cast<double*>(b->d_res_scratch);
+  o->ledger_tol = opt && opt->ledger_tol > 0 ? opt->ledger_tol : 1e-9;  // em.DefaultTolerance, em/energy.go:21
+  o->energy_check = !(opt && opt->skip_energy_check);
+  return KS_OK;
+}
+
+static int op_async(ks_batch* b, const ks_options* opt, const double* x0_dev, double* out_x_dev,
+                    int32_t* out_status_dev, int32_t* out_iters_dev, const ResOut& res, void* stream) {
   if (!b) return KS_EINVAL;
   cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
-  const ksh::HostPlan& hp = b->plan->hp;
   KOpts o = make_opts(opt);
   o.cancel = b->d_cancel;
-  (void)hp;
   const KsSpec* ks = nullptr;
-  int rc = pick_kernel(b, opt, ksj::KIND_OP, &ks);
+  int rc = KS_OK;
+  if (res.on) {
+    rc = results_opts(b, opt, res, &o);
+    if (rc) return rc;
+    const size_t ne = b->plan->hp.n_elem;
+    if (res.elem) CK(cudaMemsetAsync(res.elem, 0, sizeof(double) * KS_RES_COLS * ne * b->B, st));
+    if (res.ledger) CK(cudaMemsetAsync(res.ledger, 0, sizeof(double) * KS_LEDGER_COLS * b->B, st));
+    b->last_kernel = KS_KERNEL_GENERIC;
+  } else {
+    rc = pick_kernel(b, opt, ksj::KIND_OP, &ks);
+  }
   if (rc) return rc;
   rc = batch_setup(b, 0.0, 0.0, st);
   if (rc) return rc;
@@ -359,30 +409,71 @@ extern "C" int ks_op_async(ks_batch* b, const ks_options* opt, const double* x0_
   return KS_OK;
 }
 
-extern "C" int ks_op(ks_batch* b, const ks_options* opt, const double* x0, double* out_x, int32_t* out_status,
-                     int32_t* out_iters, void* stream) {
+extern "C" int ks_op_async(ks_batch* b, const ks_options* opt, const double* x0_dev, double* out_x_dev,
+                           int32_t* out_status_dev, int32_t* out_iters_dev, void* stream) {
+  return op_async(b, opt, x0_dev, out_x_dev, out_status_dev, out_iters_dev, ResOut{}, stream);
+}
+
+extern "C" int ks_op_results_async(ks_batch* b, const ks_options* opt, const double* x0_dev, double* out_x_dev,
+                                   int32_t* out_status_dev, int32_t* out_iters_dev, double* out_elem_dev,
+                                   double* out_ledger_dev, void* stream) {
+  ResOut r;
+  r.elem = out_elem_dev; r.ledger = out_ledger_dev; r.on = true;
+  return op_async(b, opt, x0_dev, out_x_dev, out_status_dev, out_iters_dev, r, stream);
+}
+
+// ks_op / ks_op_results on host buffers: results staged on the device, copied
+// back through the batch's page-locked buffer.
+static int op_host(ks_batch* b, const ks_options* opt, const double* x0, double* out_x, int32_t* out_status,
+                   int32_t* out_iters, double* out_elem, double* out_ledger, bool results, void* stream) {
   if (!b) return KS_EINVAL;
   cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
   const ksh::HostPlan& hp = b->plan->hp;
   size_t B = b->B, n = hp.n;
   size_t xbytes = sizeof(double) * n * B;
-  int rc = batch_stage(b, xbytes + 2 * sizeof(int32_t) * B + 64);
+  size_t ebytes = results && out_elem ? sizeof(double) * KS_RES_COLS * hp.n_elem * B : 0;
+  size_t lbytes = results && out_ledger ? sizeof(double) * KS_LEDGER_COLS * B : 0;
+  int rc = batch_stage(b, xbytes + 2 * sizeof(int32_t) * B + ebytes + lbytes + 64);
   if (rc) return rc;
+  ResOut r;
+  if (results) {
+    rc = grow_dev(&b->d_res_out, &b->d_res_out_bytes, ebytes + lbytes + 64, "ks_op_results");
+    if (rc) return rc;
+    r.on = true;
+    r.elem = ebytes ? static_cast<double*>(b->d_res_out) : nullptr;
+    r.ledger = lbytes ? reinterpret_cast<double*>(static_cast<char*>(b->d_res_out) + ebytes) : nullptr;
+  }
   if (x0) {
     std::memcpy(b->h_pin, x0, xbytes);
     CK(cudaMemcpyAsync(b->d_x0, b->h_pin, xbytes, cudaMemcpyHostToDevice, st));
   }
-  rc = ks_op_async(b, opt, x0 ? b->d_x0 : nullptr, b->d_x, b->d_status, b->d_iters, st);
+  rc = op_async(b, opt, x0 ? b->d_x0 : nullptr, b->d_x, b->d_status, b->d_iters, r, st);
   if (rc) return rc;
   char* hp_bytes = reinterpret_cast<char*>(b->h_pin);
+  const size_t so = xbytes, io = so + sizeof(int32_t) * B, eo = io + sizeof(int32_t) * B, lo = eo + ebytes;
   CK(cudaMemcpyAsync(hp_bytes, b->d_x, xbytes, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(hp_bytes + xbytes, b->d_status, sizeof(int32_t) * B, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(hp_bytes + xbytes + sizeof(int32_t) * B, b->d_iters, sizeof(int32_t) * B, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hp_bytes + so, b->d_status, sizeof(int32_t) * B, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hp_bytes + io, b->d_iters, sizeof(int32_t) * B, cudaMemcpyDeviceToHost, st));
+  if (ebytes) CK(cudaMemcpyAsync(hp_bytes + eo, r.elem, ebytes, cudaMemcpyDeviceToHost, st));
+  if (lbytes) CK(cudaMemcpyAsync(hp_bytes + lo, r.ledger, lbytes, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (out_x) std::memcpy(out_x, hp_bytes, xbytes);
-  if (out_status) std::memcpy(out_status, hp_bytes + xbytes, sizeof(int32_t) * B);
-  if (out_iters) std::memcpy(out_iters, hp_bytes + xbytes + sizeof(int32_t) * B, sizeof(int32_t) * B);
+  if (out_status) std::memcpy(out_status, hp_bytes + so, sizeof(int32_t) * B);
+  if (out_iters) std::memcpy(out_iters, hp_bytes + io, sizeof(int32_t) * B);
+  if (ebytes) std::memcpy(out_elem, hp_bytes + eo, ebytes);
+  if (lbytes) std::memcpy(out_ledger, hp_bytes + lo, lbytes);
   return KS_OK;
+}
+
+extern "C" int ks_op(ks_batch* b, const ks_options* opt, const double* x0, double* out_x, int32_t* out_status,
+                     int32_t* out_iters, void* stream) {
+  return op_host(b, opt, x0, out_x, out_status, out_iters, nullptr, nullptr, false, stream);
+}
+
+extern "C" int ks_op_results(ks_batch* b, const ks_options* opt, const double* x0, double* out_x,
+                             int32_t* out_status, int32_t* out_iters, double* out_elem, double* out_ledger,
+                             void* stream) {
+  return op_host(b, opt, x0, out_x, out_status, out_iters, out_elem, out_ledger, true, stream);
 }
 
 static int grow(void** p, size_t* have, size_t need) {
@@ -520,17 +611,40 @@ static bool tran_spec_ok(const ks_tran_spec* sp) {
          !std::isnan(sum) && !std::isinf(sp->stop);
 }
 
-extern "C" int ks_tran_async(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
-                             double* out_time_dev, double* out_wave_dev, int32_t* out_npts_dev,
-                             int32_t* out_status_dev, int32_t* out_steps_dev, int32_t* out_iters_dev, void* stream) {
+static int tran_host(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
+                     double* out_time, double* out_wave, int32_t* out_npts, int32_t* out_status, int32_t* out_steps,
+                     int32_t* out_iters, const ResOut& res, void* stream);
+
+// Points a transient records per circuit in the output layouts: fixed-step
+// n_points, adaptive the capacity.
+static size_t tran_slots(const ks_tran_spec* spec, int32_t capacity) {
+  return spec->fixed_step ? (size_t)llround(spec->stop / spec->step) + 1 : (size_t)std::max(capacity, 0);
+}
+
+static int tran_async(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
+                      double* out_time_dev, double* out_wave_dev, int32_t* out_npts_dev, int32_t* out_status_dev,
+                      int32_t* out_steps_dev, int32_t* out_iters_dev, const ResOut& res, void* stream) {
   if (!b) return KS_EINVAL;
   if (!tran_spec_ok(spec)) { set_error("analysis: invalid transient specification"); return KS_EINVAL; }
-  if (!spec->fixed_step && capacity <= 0 && (out_time_dev || out_wave_dev)) { set_error("ks_tran: capacity"); return KS_EINVAL; }
+  if (!spec->fixed_step && capacity <= 0 && (out_time_dev || out_wave_dev || res.elem || res.ledger)) {
+    set_error("ks_tran: capacity"); return KS_EINVAL;
+  }
   cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
   KOpts o = make_opts(opt);
   o.cancel = b->d_cancel;
   const KsSpec* ks = nullptr;
-  int rc = pick_kernel(b, opt, ksj::KIND_TRAN, &ks);
+  int rc = KS_OK;
+  if (res.on) {
+    rc = results_opts(b, opt, res, &o);
+    if (rc) return rc;
+    const size_t slots = tran_slots(spec, capacity) * b->B, ne = b->plan->hp.n_elem;
+    if (res.elem) CK(cudaMemsetAsync(res.elem, 0, sizeof(double) * 2 * ne * slots, st));
+    if (res.ledger) CK(cudaMemsetAsync(res.ledger, 0, sizeof(double) * KS_TPOINT_COLS * slots, st));
+    if (res.summary) CK(cudaMemsetAsync(res.summary, 0, sizeof(double) * KS_TSUM_COLS * b->B, st));
+    b->last_kernel = KS_KERNEL_GENERIC;
+  } else {
+    rc = pick_kernel(b, opt, ksj::KIND_TRAN, &ks);
+  }
   if (rc) return rc;
   rc = batch_setup(b, spec->step, spec->stop, st);
   if (rc) return rc;
@@ -542,9 +656,64 @@ extern "C" int ks_tran_async(ks_batch* b, const ks_tran_spec* spec, const ks_opt
   return KS_OK;
 }
 
+extern "C" int ks_tran_async(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
+                             double* out_time_dev, double* out_wave_dev, int32_t* out_npts_dev,
+                             int32_t* out_status_dev, int32_t* out_steps_dev, int32_t* out_iters_dev, void* stream) {
+  return tran_async(b, spec, opt, capacity, out_time_dev, out_wave_dev, out_npts_dev, out_status_dev, out_steps_dev,
+                    out_iters_dev, ResOut{}, stream);
+}
+
+extern "C" int ks_tran_results_async(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
+                                     double* out_time_dev, double* out_wave_dev, double* out_elem_dev,
+                                     double* out_ledger_dev, double* out_summary_dev, int32_t* out_npts_dev,
+                                     int32_t* out_status_dev, int32_t* out_steps_dev, int32_t* out_iters_dev,
+                                     void* stream) {
+  ResOut r;
+  r.elem = out_elem_dev; r.ledger = out_ledger_dev; r.summary = out_summary_dev; r.on = true;
+  return tran_async(b, spec, opt, capacity, out_time_dev, out_wave_dev, out_npts_dev, out_status_dev, out_steps_dev,
+                    out_iters_dev, r, stream);
+}
+
+extern "C" int ks_tran_results(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
+                               double* out_time, double* out_wave, double* out_elem, double* out_ledger,
+                               double* out_summary, int32_t* out_npts, int32_t* out_status, int32_t* out_steps,
+                               int32_t* out_iters, void* stream) {
+  if (!b) return KS_EINVAL;
+  if (!tran_spec_ok(spec)) { set_error("analysis: invalid transient specification"); return KS_EINVAL; }
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+  const size_t slots = tran_slots(spec, capacity) * b->B, ne = b->plan->hp.n_elem;
+  const size_t eb = out_elem ? sizeof(double) * 2 * ne * slots : 0, lb = out_ledger ? sizeof(double) * KS_TPOINT_COLS * slots : 0;
+  const size_t sb = out_summary ? sizeof(double) * KS_TSUM_COLS * b->B : 0;
+  int rc = grow_dev(&b->d_res_out, &b->d_res_out_bytes, eb + lb + sb + 64, "ks_tran_results");
+  if (rc) return rc;
+  char* base = static_cast<char*>(b->d_res_out);
+  ResOut r;
+  r.on = true;
+  r.elem = eb ? reinterpret_cast<double*>(base) : nullptr;
+  r.ledger = lb ? reinterpret_cast<double*>(base + eb) : nullptr;
+  r.summary = sb ? reinterpret_cast<double*>(base + eb + lb) : nullptr;
+  rc = tran_host(b, spec, opt, capacity, out_time, out_wave, out_npts, out_status, out_steps, out_iters, r, st);
+  if (rc) return rc;
+  cudaError_t e = cudaSuccess;
+  if (eb) e = cudaMemcpyAsync(out_elem, r.elem, eb, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && lb) e = cudaMemcpyAsync(out_ledger, r.ledger, lb, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && sb) e = cudaMemcpyAsync(out_summary, r.summary, sb, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) { set_error(std::string("ks_tran_results: ") + cudaGetErrorString(e)); return KS_ECUDA; }
+  return KS_OK;
+}
+
 extern "C" int ks_tran(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
                        double* out_time, double* out_wave, int32_t* out_npts, int32_t* out_status, int32_t* out_steps,
                        int32_t* out_iters, void* stream) {
+  return tran_host(b, spec, opt, capacity, out_time, out_wave, out_npts, out_status, out_steps, out_iters, ResOut{},
+                   stream);
+}
+
+// ks_tran / ks_tran_results on host buffers (the results' device outputs are the caller's r).
+static int tran_host(ks_batch* b, const ks_tran_spec* spec, const ks_options* opt, int32_t capacity,
+                     double* out_time, double* out_wave, int32_t* out_npts, int32_t* out_status, int32_t* out_steps,
+                     int32_t* out_iters, const ResOut& res, void* stream) {
   if (!b) return KS_EINVAL;
   if (!tran_spec_ok(spec)) { set_error("analysis: invalid transient specification"); return KS_EINVAL; }
   cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
@@ -575,7 +744,7 @@ extern "C" int ks_tran(ks_batch* b, const ks_tran_spec* spec, const ks_options* 
   double* d_time = (out_time && time_elems) ? b->d_time : nullptr;
   int32_t* d_ints = b->d_tints;
   auto cleanup = [&]() {};
-  int rc = ks_tran_async(b, spec, opt, capacity, d_time, d_wave, d_ints, d_ints + B, d_ints + 2 * B, d_ints + 3 * B, st);
+  int rc = tran_async(b, spec, opt, capacity, d_time, d_wave, d_ints, d_ints + B, d_ints + 2 * B, d_ints + 3 * B, res, st);
   if (rc) { cleanup(); return rc; }
   cudaError_t e = cudaSuccess;
   if (out_wave && d_wave) e = cudaMemcpyAsync(out_wave, d_wave, wave_elems * sizeof(double), cudaMemcpyDeviceToHost, st);

@@ -12,7 +12,7 @@
 #include <cuda_runtime.h>
 #include <cstdio>
 #include "ks_internal.h"
-#include "ks_newton.cuh"
+#include "ks_results.cuh"
 
 using namespace ksg;
 
@@ -79,8 +79,9 @@ int ks_launch_setup(const KsDeviceBatch& b, double step, double stop, void* stre
 // analysis.OP for every circuit: dcSolve (Newton, then the fallback chain) at
 // ModeOP, then Accept.  Persistent: each thread takes the next circuit from the
 // queue counter as soon as its circuit is done, so a warp's lanes stay busy
-// while circuits need different numbers of Newton iterations.
-template <int T>
+// while circuits need different numbers of Newton iterations.  R: with the
+// element results and the energy ledger (ks_results.cuh).
+template <int T, bool R>
 __global__ void __launch_bounds__(T) k_op(KPlan plan, KOpts o, const double* __restrict__ values,
                                           const double* __restrict__ derived, double* state, double* work,
                                           int64_t B, const double* __restrict__ x0, double* out_x,
@@ -91,8 +92,8 @@ __global__ void __launch_bounds__(T) k_op(KPlan plan, KOpts o, const double* __r
   smem_layout<T>(t, plan, smem);
   t.o = o;
   __syncthreads();
-  op_persistent(t, values, derived, state, work, B, x0, out_x, out_status, out_iters, deadline_ns, queue,
-                k32.values ? &k32 : nullptr);
+  op_persistent<SmemSys<T>, RtProg, R>(t, values, derived, state, work, B, x0, out_x, out_status, out_iters,
+                                       deadline_ns, queue, k32.values ? &k32 : nullptr);
 }
 
 // Blocks of T threads that keep every SM full (persistent grid), capped by the work.
@@ -113,7 +114,8 @@ int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, doubl
   int n = b.plan.n, ne = b.plan.n_elem;
   if (n > KS_MAX_DENSE) return -2;
   uint64_t dl = deadline_s > 0 ? (uint64_t)(deadline_s * 1e9) : 0;
-  if (kspec) {  // per-topology kernel of the plan (ks_jit.cpp)
+  const bool res = o.res_scratch != nullptr;  // results: the generic kernels' results instantiation
+  if (kspec && !res) {  // per-topology kernel of the plan (ks_jit.cpp)
     if (cudaMemsetAsync(b.queue, 0, sizeof(unsigned long long), (cudaStream_t)stream) != cudaSuccess) return -1;
     KOpts ko = o;
     const double *values = b.values, *derived = b.derived;
@@ -140,16 +142,13 @@ int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, doubl
   if (cudaMemsetAsync(b.queue, 0, sizeof(unsigned long long), st) != cudaSuccess) return -1;
   K32 k32{b.values32, b.derived32, b.state32};
   if (!b.values32 || !b.derived32 || !b.state32) k32 = K32{nullptr, nullptr, nullptr};
-  if (T == 64) {
-    cudaFuncSetAttribute(k_op<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    unsigned grid = persistent_grid(k_op<64>, 64, sm, b.B);
-    k_op<64><<<grid, 64, sm, st>>>(b.plan, o, b.values, b.derived, b.state, b.work, b.B, x0, out_x, out_status,
-                                   out_iters, dl, b.queue, k32);
-  } else {
-    cudaFuncSetAttribute(k_op<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    unsigned grid = persistent_grid(k_op<32>, 32, sm, b.B);
-    k_op<32><<<grid, 32, sm, st>>>(b.plan, o, b.values, b.derived, b.state, b.work, b.B, x0, out_x, out_status,
-                                   out_iters, dl, b.queue, k32);
-  }
+  auto go = [&](auto kernel, int threads) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    unsigned grid = persistent_grid(kernel, threads, sm, b.B);
+    kernel<<<grid, threads, sm, st>>>(b.plan, o, b.values, b.derived, b.state, b.work, b.B, x0, out_x, out_status,
+                                      out_iters, dl, b.queue, k32);
+  };
+  if (T == 64) res ? go(k_op<64, true>, 64) : go(k_op<64, false>, 64);
+  else res ? go(k_op<32, true>, 32) : go(k_op<32, false>, 32);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

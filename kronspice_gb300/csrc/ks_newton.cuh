@@ -363,8 +363,14 @@ __device__ __forceinline__ int polish(Thr<SY, P>& t, OpState& st, const LoadPara
   return KS_STATUS_OK;
 }
 
-// The operating point of one circuit after another, pulled from the queue.
+// Element results and the ledger of circuit c at its accepted operating point
+// (ks_results.cuh; the results instantiation of the generic kernels only).
 template <class SY, class P>
+__device__ inline int op_results(Thr<SY, P>& t, const LoadParams& lp, int64_t c, int64_t B);
+
+// The operating point of one circuit after another, pulled from the queue.
+// kRes: with the element results and the energy ledger (ks_op_results).
+template <class SY, class P, bool kRes = false>
 __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* values, const double* derived, double* state,
                                      double* work, int64_t B, const double* x0, double* out_x, int32_t* out_status,
                                      int32_t* out_iters, uint64_t deadline_ns, unsigned long long* queue,
@@ -407,11 +413,17 @@ __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* value
       st.total = spent;
       continue;
     }
-    if (st.status == KS_STATUS_OK) accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, ModeOP, o.gmin, false);
     if (st.status == KS_STATUS_OK && o.polish && !t.prog.nonlin_empty) {
+      accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, ModeOP, o.gmin, false);
       st.status = polish(t, st, lp);
-      if (st.status == KS_STATUS_OK) accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, ModeOP, o.gmin, false);
     }
+    // the results read each device's linearization before its Accept (which
+    // leaves that linearization as it is, analysis/op.go:348-349)
+    if constexpr (kRes) {
+      if (st.status == KS_STATUS_OK) st.status = op_results(t, lp, c, B);
+    }
+    if (st.status == KS_STATUS_OK || st.status == KS_STATUS_LEDGER)
+      accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, ModeOP, o.gmin, false);
     if (out_x) {
       const int n = t.n();  // per circuit for the multi-topology kernels
       const int64_t base = t.prog.x_base(c, n);

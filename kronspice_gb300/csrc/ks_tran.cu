@@ -1,11 +1,12 @@
 // ks_tran.cu — launch of the generic batched transient kernel of the GB300 engine.
 #include <cuda_runtime.h>
 #include "ks_internal.h"
-#include "ks_tran.cuh"
+#include "ks_results.cuh"
 
 using namespace ksg;
 
-template <int T>
+// R: with the element results and the energy ledger of every point (ks_results.cuh).
+template <int T, bool R>
 __global__ void __launch_bounds__(T) k_tran(KPlan plan, KOpts o, TranSpecK sp, const double* __restrict__ values,
                                             const double* __restrict__ derived, double* state, double* work, int64_t B,
                                             double* out_time, double* out_wave, int32_t* out_npts, int32_t* out_status,
@@ -16,8 +17,8 @@ __global__ void __launch_bounds__(T) k_tran(KPlan plan, KOpts o, TranSpecK sp, c
   smem_layout<T>(t, plan, smem);
   t.o = o;
   __syncthreads();
-  tran_persistent(t, sp, values, derived, state, work, B, out_time, out_wave, out_npts, out_status, out_steps,
-                  out_iters, deadline_ns, queue);
+  tran_persistent<SmemSys<T>, RtProg, R>(t, sp, values, derived, state, work, B, out_time, out_wave, out_npts,
+                                         out_status, out_steps, out_iters, deadline_ns, queue);
 }
 
 int ks_launch_tran(const KsDeviceBatch& b, const KOpts& o, const ks_tran_spec& spec, int cap, double* out_time,
@@ -40,7 +41,8 @@ int ks_launch_tran(const KsDeviceBatch& b, const KOpts& o, const ks_tran_spec& s
   sp.cap = cap;
   sp.npts = (int)llround(spec.stop / spec.step) + 1;
   uint64_t dl = deadline_s > 0 ? (uint64_t)(deadline_s * 1e9) : 0;
-  if (kspec) {  // per-topology kernel of the plan (ks_jit.cpp)
+  const bool res = o.res_scratch != nullptr;  // results: the generic kernels' results instantiation
+  if (kspec && !res) {  // per-topology kernel of the plan (ks_jit.cpp)
     if (cudaMemsetAsync(b.queue, 0, sizeof(unsigned long long), (cudaStream_t)stream) != cudaSuccess) return -1;
     KOpts ko = o;
     const double *values = b.values, *derived = b.derived;
@@ -64,22 +66,19 @@ int ks_launch_tran(const KsDeviceBatch& b, const KOpts& o, const ks_tran_spec& s
   if (sm > (size_t)maxSmem) return -2;
   cudaStream_t st = (cudaStream_t)stream;
   if (cudaMemsetAsync(b.queue, 0, sizeof(unsigned long long), st) != cudaSuccess) return -1;
-  int sms = 0, per = 0;
+  int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (T == 64) {
-    cudaFuncSetAttribute(k_tran<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tran<64>, 64, sm);
-  } else {
-    cudaFuncSetAttribute(k_tran<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_tran<32>, 32, sm);
-  }
-  int64_t need = (b.B + (int64_t)T * circuits_per_thread() - 1) / ((int64_t)T * circuits_per_thread()), cap_blocks = (int64_t)sms * (per > 0 ? per : 1);
-  unsigned grid = (unsigned)(need < cap_blocks ? need : cap_blocks);
-  if (T == 64)
-    k_tran<64><<<grid, 64, sm, st>>>(b.plan, o, sp, b.values, b.derived, b.state, b.work, b.B, out_time, out_wave,
-                                     out_npts, out_status, out_steps, out_iters, dl, b.queue);
-  else
-    k_tran<32><<<grid, 32, sm, st>>>(b.plan, o, sp, b.values, b.derived, b.state, b.work, b.B, out_time, out_wave,
-                                     out_npts, out_status, out_steps, out_iters, dl, b.queue);
+  auto go = [&](auto kernel, int threads) {
+    int per = 0;
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, sm);
+    int64_t need = (b.B + (int64_t)threads * circuits_per_thread() - 1) / ((int64_t)threads * circuits_per_thread());
+    int64_t cap_blocks = (int64_t)sms * (per > 0 ? per : 1);
+    unsigned grid = (unsigned)(need < cap_blocks ? need : cap_blocks);
+    kernel<<<grid, threads, sm, st>>>(b.plan, o, sp, b.values, b.derived, b.state, b.work, b.B, out_time, out_wave,
+                                      out_npts, out_status, out_steps, out_iters, dl, b.queue);
+  };
+  if (T == 64) res ? go(k_tran<64, true>, 64) : go(k_tran<64, false>, 64);
+  else res ? go(k_tran<32, true>, 32) : go(k_tran<32, false>, 32);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

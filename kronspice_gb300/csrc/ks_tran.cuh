@@ -139,8 +139,32 @@ __device__ __forceinline__ void record(Thr<SY, P>& t, const TranSpecK& sp, int64
 }
 
 
-// analysis.Tran of one circuit after another, pulled from the queue.
+// The transient recorder's running ledger state for one circuit
+// (analysis/tran.go:248-386): peak power, worst residual, the trapezoid sums of
+// inflow, outflow, dissipation and model-supplied power, stored energy at the
+// first and last recorded points.
+struct TranLedger {
+  double peakScale, worstAbs, tPrev, yPrev[4], e[4], storedStart, storedEnd;
+  int recorded;
+  bool imposedFirst;
+  __device__ __forceinline__ void reset() {
+    peakScale = worstAbs = tPrev = storedStart = storedEnd = 0;
+    for (int q = 0; q < 4; q++) { yPrev[q] = 0; e[q] = 0; }
+    recorded = 0;
+    imposedFirst = false;
+  }
+};
+
+// recorder.record and recorder.finish with the element results (ks_results.cuh;
+// the results instantiation of the generic kernels only).
 template <class SY, class P>
+__device__ inline bool tran_point_results(Thr<SY, P>& t, TranLedger& L, const LoadParams& lp, int64_t c, int64_t B,
+                                          double tp, bool imposed, bool stored_point, int64_t row);
+__device__ inline bool tran_finish(const KOpts& o, const TranLedger& L, int64_t c);
+
+// analysis.Tran of one circuit after another, pulled from the queue.  kRes: with
+// the element results and the energy ledger of every point (ks_tran_results).
+template <class SY, class P, bool kRes = false>
 __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& sp, const double* values, const double* derived,
                                        double* state, double* work, int64_t B, double* out_time, double* out_wave,
                                        int32_t* out_npts, int32_t* out_status, int32_t* out_steps, int32_t* out_iters,
@@ -156,11 +180,28 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
   bool hitBreak = false, onGrid = false;
   double tnow = 0, h = 0, tn = 0;
   int64_t c = B;
+  TranLedger L;
+  // The results of the point at tp before its Accept; true: out of balance (the
+  // transient stops after recording it).  Its rows go where record() puts the
+  // point: fixed-step [points][B], adaptive [B][cap] (not stored before `start`
+  // or beyond the capacity).
+  auto point_results = [&](double tp, int k, bool imposed) -> bool {
+    if constexpr (kRes) {
+      bool stored = sp.fixed || tp >= sp.start;
+      int64_t row = -1;
+      if (sp.fixed) { if (k < sp.npts) row = (int64_t)k * B + c; }
+      else if (stored && npts < sp.cap) row = c * sp.cap + npts;
+      return tran_point_results(t, L, lp, c, B, tp, imposed, stored, row);
+    } else {
+      return false;
+    }
+  };
 
   // Starting point of circuit c: analysis/tran.go:103-126.
   auto start = [&]() {
     thr_bind(t, values, derived, state, work, B, c);
     init_state(t.prog, t.D, t.Sb);
+    if constexpr (kRes) L.reset();
     lp.method = BE; lp.time = 0; lp.h = 0; lp.rh = 0;
     phase = TR_START; status = KS_STATUS_OK; accepted = 0; npts = 0; kgrid = 1; order = BE;
     tnow = 0; h = 0; tn = 0;
@@ -221,14 +262,18 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
         }
         if (res != KS_STATUS_OK) { status = res; phase = TR_DONE; }
         else {
+          const bool unbalanced = point_results(0.0, 0, sp.uic != 0);  // the UIC point is imposed: not checked
           accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, sp.uic ? ModeUICInit : ModeTranOP, o.gmin, false);
           record(t, sp, c, B, 0.0, 0, &npts, out_time, out_wave);
-          x_to_col(t, t.xacc);
-          phase = TR_STEP;
-          st.initJct = false;
-          h = sp.fixed ? sp.step : fmin(sp.maxStep, fmin(sp.step, sp.stop / 100)) / 10;
-          order = BE;
-          begin_step();
+          if (unbalanced) { status = KS_STATUS_LEDGER; phase = TR_DONE; }
+          else {
+            x_to_col(t, t.xacc);
+            phase = TR_STEP;
+            st.initJct = false;
+            h = sp.fixed ? sp.step : fmin(sp.maxStep, fmin(sp.step, sp.stop / 100)) / 10;
+            order = BE;
+            begin_step();
+          }
         }
       } else if (res != KS_STATUS_OK) {  // a time step's newton failed
         if (!retryable(res) || t.prog.nonlin_empty) { status = res; phase = TR_DONE; }
@@ -248,9 +293,14 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
             if (reject(h)) begin_step();
           }
         }
+        bool unbalanced = false;
+        if (!rejected && (!sp.fixed || onGrid)) unbalanced = point_results(tn, kgrid, false);
         if (!rejected) {
           accept_all(t.prog, t.V, t.D, t.Sb, t.s, tn, ModeTran, o.gmin, false);  // :200-208
           if (!sp.fixed || onGrid) record(t, sp, c, B, tn, kgrid, &npts, out_time, out_wave);
+        }
+        if (unbalanced) { status = KS_STATUS_LEDGER; phase = TR_DONE; }
+        else if (!rejected) {
           x_to_col(t, t.xacc);
           accepted++;
           tnow = tn;
@@ -273,6 +323,9 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
       if (phase != TR_DONE) continue;
     }
     // circuit c finished: write its results and take the next one
+    if constexpr (kRes) {
+      if (tran_finish(o, L, c) && status == KS_STATUS_OK) status = KS_STATUS_LEDGER;
+    }
     if (out_status) out_status[c] = status;
     if (out_steps) out_steps[c] = accepted;
     if (out_iters) out_iters[c] = st.total;
