@@ -323,6 +323,12 @@ int ks_batch_cancel_word(ks_batch* b, volatile int32_t** word);
  * row).  Output pointers are optional. */
 int ks_sparse_analyze(const ks_topology* topo, const double* values, double step, int32_t* n, int64_t* slots, int64_t* lu_flops, int32_t* prow,
                       int32_t* pcol, int32_t* rowptr, int32_t* cols);
+/* The pattern the analysis above orders (solver/sparse.go:114-143: every entry
+ * the elements' loads stamp over an operating point (transient = 0) or a
+ * transient, plus every diagonal), as an n x n byte matrix, row-major.  The
+ * column order (pcol of ks_sparse_analyze) is minimumDegree of it
+ * (solver/sparse.go:412-452). */
+int ks_sparse_pattern(const ks_topology* topo, const double* values, int32_t transient, int32_t* n, uint8_t* pattern);
 int ks_multi_create(int32_t n_circ, const ks_topology* topos, const double* values, const int64_t* value_offsets,
                     ks_multi** out);
 void ks_multi_destroy(ks_multi* m);

@@ -43,7 +43,7 @@ EXPORTS = ["ks_version", "ks_last_error", "ks_validate", "ks_unknowns", "ks_plan
            "ks_multi_tran_async", "ks_sparse_analyze", "ks_ac", "ks_ac_async", "ks_ac_at", "ks_torn_create",
            "ks_torn_destroy", "ks_torn_plan", "ks_torn_set_stream", "ks_torn_info", "ks_torn_op", "ks_torn_tran",
            "ks_fp64_peak", "ks_batch_cancel_word", "ks_op_results", "ks_op_results_async", "ks_tran_results",
-           "ks_tran_results_async"]
+           "ks_tran_results_async", "ks_sparse_pattern"]
 
 _lib = None
 
@@ -93,6 +93,7 @@ def load(build_if_missing=False):
     L.ks_op_noalloc_scratch_bytes.argtypes = [P, ctypes.c_int32, P]
     L.ks_multi_create.argtypes = [ctypes.c_int32, P, P, P, ctypes.POINTER(ctypes.c_void_p)]
     L.ks_sparse_analyze.argtypes = [P, P, ctypes.c_double, P, P, P, P, P, P, P]
+    L.ks_sparse_pattern.argtypes = [P, P, ctypes.c_int32, P, P]
     L.ks_multi_destroy.argtypes = [P]
     L.ks_multi_destroy.restype = None
     L.ks_multi_info.argtypes = [P, P, P, P, P]

@@ -423,6 +423,26 @@ def torn_plan(elements, n_nodes, n_values, torn):
     return piece, rows[:nr.value].copy(), mp.value, mb.value
 
 
+def sparse_analysis(elements, n_nodes, values, step=0.0):
+    """The host's sparse analysis of one circuit (ks_sparse_analyze, ks_sparse_pattern):
+    (column order [n], pivot rows [n], pattern [n][n] bool); step > 0: the
+    transient's pattern and pivots."""
+    L = _lib.load()
+    el = np.ascontiguousarray(elements, dtype=ELEMENT_DTYPE)
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    topo = _lib.KsTopology(int(n_nodes), len(el), len(v), 0, el.ctypes.data)
+    n = ctypes.c_int32()
+    _check(L.ks_unknowns(ctypes.byref(topo), ctypes.byref(n), None), "ks_unknowns")
+    pcol = np.zeros(n.value, dtype=np.int32)
+    prow = np.zeros(n.value, dtype=np.int32)
+    pat = np.zeros((n.value, n.value), dtype=np.uint8)
+    _check(L.ks_sparse_analyze(ctypes.byref(topo), v.ctypes.data, float(step), None, None, None, prow.ctypes.data,
+                               pcol.ctypes.data, None, None), "ks_sparse_analyze")
+    _check(L.ks_sparse_pattern(ctypes.byref(topo), v.ctypes.data, int(step > 0), None, pat.ctypes.data),
+           "ks_sparse_pattern")
+    return pcol, prow, pat.astype(bool)
+
+
 class TornBatch:
     """Variants of one large topology solved torn into pieces (ks_torn_create):
     kron.JacobianTearing as analysis.Options.Solver, batched over the variants."""

@@ -36,6 +36,8 @@ struct SparseSym {
 };
 // h = 0: pivot rows chosen at DC; h > 0: with the companion models of step h.
 int sparse_symbolic(const HostPlan& hp, const double* values, double h, SparseSym* sy, std::string* err);
+// The reference's stamp pattern of one circuit (operating point, or transient), n x n bytes.
+void sparse_pattern(const HostPlan& hp, const double* values, bool transient, uint8_t* out);
 
 }  // namespace ksh
 

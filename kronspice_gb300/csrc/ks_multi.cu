@@ -584,6 +584,18 @@ extern "C" int ks_sparse_analyze(const ks_topology* topo, const double* values, 
   return KS_OK;
 }
 
+extern "C" int ks_sparse_pattern(const ks_topology* topo, const double* values, int32_t transient, int32_t* n,
+                                 uint8_t* pattern) {
+  if (!topo) return KS_EINVAL;
+  ksh::HostPlan hp;
+  std::string err;
+  int rc = ksh::plan_layout(topo, &hp, &err);
+  if (rc) { set_error(err); return rc; }
+  if (n) *n = hp.n;
+  if (pattern) ksh::sparse_pattern(hp, values, transient != 0, pattern);
+  return KS_OK;
+}
+
 extern "C" void ks_multi_destroy(ks_multi* m) {
   if (!m) return;
   cudaFree(m->buf);

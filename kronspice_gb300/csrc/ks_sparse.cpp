@@ -4,9 +4,9 @@
 // Done once per circuit on the host (the role of solver/sparse.go:154-187
 // analyze and :412-452 minimumDegree, with the pivot rows of its threshold
 // partial pivoting chosen once instead of at every factorization):
-//   1. the structural pattern: every entry any element stamps in any mode
-//      (devices as dense blocks over their terminals) plus every diagonal (gmin
-//      and pseudo-transient stepping add to them);
+//   1. the reference's pattern: every entry the elements' loads stamp in the
+//      analysis's modes (stamp_rows), plus every diagonal (gmin and
+//      pseudo-transient stepping add to them);
 //   2. columns: minimum degree on the pattern of A + A^T, ties to the lowest index;
 //   3. rows: threshold partial pivoting with diagonal preference in that column
 //      order on a representative matrix of the circuit's own values (at DC, or
@@ -35,22 +35,65 @@ struct Bits {
   void clear(int i) { w[i >> 6] &= ~(1ull << (i & 63)); }
 };
 
-void stamp_rows(const HostPlan& hp, std::vector<Bits>& rows) {
+// The reference's pattern: every entry an element's Load stamps in the
+// analysis's modes (Sparse.add keeps each new (i, j) as a slot for the rest of
+// the run, solver/sparse.go:114-143), restated per device from its stamp
+// sequence: passive.go:72-84, reactive.go:60-106 and :230-259, source.go:102-112,
+// diode.go:229-275, bjt.go:463-515, mosfet.go:563-611.  Operating point: the
+// DC stamps; transient: the union of the DC stamps (its operating point) and
+// the companion stamps of the time steps.  Entries that a device stamps only
+// while one of its conductances is non-zero are all included (a fixed pivot
+// sequence must hold every entry any Newton iteration may stamp); entries that
+// depend only on parameters follow them (the BJT's base-to-collector junction
+// capacitance outside the intrinsic base: CJC (1 - XCJC) != 0).  Every diagonal
+// is added too (gmin stepping and pseudo-transient continuation add to them);
+// minimum degree does not look at diagonals.
+void stamp_rows(const HostPlan& hp, const double* values, bool transient, std::vector<Bits>& rows) {
   auto add = [&](int i, int j) { if (i >= 0 && j >= 0) rows[i].set(j); };
-  auto block = [&](const int* u, int k) {
-    for (int a = 0; a < k; a++)
-      for (int b = 0; b < k; b++) add(u[a], u[b]);
-  };
+  auto g4 = [&](int a, int b) { add(a, a); add(b, b); add(a, b); add(b, a); };
+  // bjt.go:463-480 / mosfet.go:563-578: a current from a to b controlled by v(p) - v(n)
+  auto ctl = [&](int a, int b, int p, int q) { add(a, p); add(a, q); add(b, p); add(b, q); };
   for (const KElem& e : hp.elem) {
     const int* u = e.u;
     switch (e.kind) {
-      case KS_ELEM_R: case KS_ELEM_C: block(u, 2); break;
+      case KS_ELEM_R: g4(u[0], u[1]); break;
+      case KS_ELEM_C: if (transient) g4(u[0], u[1]); break;
       case KS_ELEM_V: case KS_ELEM_L:
-        add(u[0], u[2]); add(u[1], u[2]); add(u[2], u[0]); add(u[2], u[1]); add(u[2], u[2]); break;
+        add(u[0], u[2]); add(u[1], u[2]); add(u[2], u[0]); add(u[2], u[1]);
+        if (e.kind == KS_ELEM_L && transient) add(u[2], u[2]);
+        break;
       case KS_ELEM_I: break;
-      case KS_ELEM_D: block(u, 3); break;
-      case KS_ELEM_Q: block(u, 9); break;
-      case KS_ELEM_M: block(u, 6); break;
+      case KS_ELEM_D:  // u = {anode, cathode, internal anode}
+        g4(u[2], u[1]);
+        if (u[2] != u[0]) g4(u[0], u[2]);
+        break;
+      case KS_ELEM_Q: {  // u = {c, e, b, s, c', b', e', sa, sb}
+        const int uc = u[0], ue = u[1], b = u[2], cp = u[4], bp = u[5], ep = u[6], sa = u[7], sb = u[8];
+        ctl(cp, ep, bp, ep); ctl(cp, ep, bp, cp);  // transport current on vbe and vbc
+        ctl(bp, ep, bp, ep);                       // base-emitter
+        ctl(bp, cp, bp, cp);                       // base-collector
+        ctl(sa, sb, sa, sb);                       // substrate
+        if (transient) {
+          // the charge branches fall on the entries above, except the junction
+          // capacitance between the external base and the collector
+          const double cjc = values ? values[e.param + KS_Q_P_CJC] : 1.0;
+          const double xcjc = values ? values[e.param + KS_Q_P_XCJC] : 0.0;
+          if (cjc - cjc * xcjc != 0) ctl(b, cp, b, cp);
+        }
+        if (bp != b) g4(b, bp);
+        if (cp != uc) g4(uc, cp);
+        if (ep != ue) g4(ue, ep);
+        break;
+      }
+      case KS_ELEM_M: {  // u = {d, s, g, b, d', s'}
+        const int ud = u[0], us = u[1], g = u[2], b = u[3], dp = u[4], sp = u[5];
+        ctl(dp, sp, g, sp); ctl(dp, sp, dp, sp); ctl(dp, sp, b, sp);  // channel on vgs, vds, vbs
+        ctl(b, sp, b, sp); ctl(b, dp, b, dp);                           // bulk junctions
+        if (transient) { g4(g, sp); g4(g, dp); g4(g, b); g4(b, sp); g4(b, dp); }  // Meyer and junction charges
+        if (dp != ud) g4(ud, dp);
+        if (sp != us) g4(us, sp);
+        break;
+      }
       default: break;
     }
   }
@@ -59,12 +102,22 @@ void stamp_rows(const HostPlan& hp, std::vector<Bits>& rows) {
 
 }  // namespace
 
+// The pattern stamp_rows gives, as an n x n byte matrix (the symbolic-parity tests).
+void sparse_pattern(const HostPlan& hp, const double* values, bool transient, uint8_t* out) {
+  const int n = hp.n;
+  std::vector<Bits> A(n);
+  for (auto& r : A) r.init(n);
+  stamp_rows(hp, values, transient, A);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) out[(size_t)i * n + j] = A[i].get(j) ? 1 : 0;
+}
+
 int sparse_symbolic(const HostPlan& hp, const double* values, double h, SparseSym* sy, std::string* err) {
   const int n = hp.n;
   if (n < 1) { *err = "empty system"; return KS_EINVAL; }
   std::vector<Bits> A(n);
   for (auto& r : A) r.init(n);
-  stamp_rows(hp, A);
+  stamp_rows(hp, values, h > 0, A);
   // 2. columns: minimum degree on the pattern of A + A^T, ties to the lowest
   //    index (solver/sparse.go:412-452)
   std::vector<Bits> G(n);
@@ -97,8 +150,8 @@ int sparse_symbolic(const HostPlan& hp, const double* values, double h, SparseSy
   // 3. rows: threshold partial pivoting with the reference's diagonal preference
   //    (solver/sparse.go:256-281, DiagPivotTol 1e-3) in that column order, on a
   //    representative matrix: resistors at their conductance, sources and
-  //    inductors at their +-1 incidence, gmin on node diagonals, transistor
-  //    terminals at 1 mS; at DC (h = 0) capacitors are open, for a transient of
+  //    inductors at their +-1 incidence, gmin on node diagonals, transistors
+  //    conducting (on their own stamp pattern); at DC (h = 0) capacitors are open, for a transient of
   //    step h capacitors are 2C/h and inductor branches -2L/h (the trapezoidal
   //    companions).  The GPU refactors every Newton iteration on this fixed
   //    pivot sequence.
@@ -106,6 +159,8 @@ int sparse_symbolic(const HostPlan& hp, const double* values, double h, SparseSy
   auto at = [&](int i, int j) -> double& { return M[(size_t)i * n + j]; };
   auto madd = [&](int i, int j, double g) { if (i >= 0 && j >= 0) at(i, j) += g; };
   auto cond = [&](int a, int b, double g) { madd(a, a, g); madd(b, b, g); madd(a, b, -g); madd(b, a, -g); };
+  // a current from a to b of g (v(p) - v(q))
+  auto ctl = [&](int a, int b, int p, int q, double g) { madd(a, p, g); madd(a, q, -g); madd(b, p, -g); madd(b, q, g); };
   std::vector<char> branch(n, 0);
   for (const KElem& e : hp.elem) {
     const int* u = e.u;
@@ -133,19 +188,34 @@ int sparse_symbolic(const HostPlan& hp, const double* values, double h, SparseSy
           cond(u[0], u[2], rs > 0 ? 1.0 / rs : 1.0);
         }
         break;
-      case KS_ELEM_Q:
-        for (int t = 0; t < 9; t++)
-          for (int v = t + 1; v < 9; v++) if (u[t] >= 0 && u[v] >= 0 && u[t] != u[v]) cond(u[t], u[v], 1e-3);
+      case KS_ELEM_Q: {  // a forward-active transistor: gm 40 mS, gpi 1 mS, gmu 1 uS, series resistances
+        const int uc = u[0], ue = u[1], b = u[2], cp = u[4], bp = u[5], ep = u[6];
+        ctl(cp, ep, bp, ep, 4e-2);
+        cond(bp, ep, 1e-3);
+        cond(bp, cp, 1e-6);
+        auto rser = [&](int k) { double r = values ? values[e.param + k] : 0.0; return r > 0 ? 1.0 / r : 1.0; };
+        if (bp != b) cond(b, bp, rser(KS_Q_P_RB));
+        if (cp != uc) cond(uc, cp, rser(KS_Q_P_RC));
+        if (ep != ue) cond(ue, ep, rser(KS_Q_P_RE));
         break;
-      case KS_ELEM_M:
-        for (int t = 0; t < 6; t++)
-          for (int v = t + 1; v < 6; v++) if (u[t] >= 0 && u[v] >= 0 && u[t] != u[v]) cond(u[t], u[v], 1e-3);
+      }
+      case KS_ELEM_M: {  // a conducting channel: gm 1 mS, gds 0.1 mS; at a step of h, 1 pF gate capacitances
+        const int ud = u[0], us = u[1], g = u[2], b = u[3], dp = u[4], sp = u[5];
+        ctl(dp, sp, g, sp, 1e-3);
+        cond(dp, sp, 1e-4);
+        if (h > 0) { cond(g, sp, 2e-12 / h); cond(g, dp, 2e-12 / h); cond(g, b, 2e-12 / h); }
+        if (dp != ud) cond(ud, dp, 1.0);
+        if (sp != us) cond(us, sp, 1.0);
         break;
+      }
       default: break;
     }
   }
   for (int i = 0; i < n; i++)
     if (!branch[i]) at(i, i) += 1e-12;
+  for (int i = 0; i < n; i++)  // every stamp above falls on the pattern; keep it so
+    for (int j = 0; j < n; j++)
+      if (!A[i].get(j)) at(i, j) = 0;
   std::vector<int> pr(n, -1);  // pr[column] = pivot row
   std::vector<char> used(n, 0);
   for (int k = 0; k < n; k++) {

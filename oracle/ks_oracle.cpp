@@ -717,6 +717,44 @@ extern "C" int kso_tran(const ks_topology* t, const double* values, const ks_tra
   return e;
 }
 
+// The sparse backend's column order after an analysis (solver/sparse.go:154-187:
+// minimumDegree of the pattern every load of the run stamped) and that pattern.
+extern "C" int kso_sparse_order(const ks_topology* t, const double* values, const ks_tran_spec* spec,
+                                const ks_options* o, int32_t* n_out, int32_t* order, uint8_t* pattern) {
+  Sim s;
+  ks_options oo = o ? *o : ks_options{};
+  oo.backend = KS_BACKEND_SPARSE;
+  Opts opt(&oo);
+  if (s.build(t, values, spec ? spec->step : 0, spec ? spec->stop : 0, KS_BACKEND_SPARSE)) return KS_STATUS_NOT_RUN;
+  int e;
+  if (spec) {
+    Sim::Rec rec;
+    int st = 0;
+    e = s.tran(*spec, opt, rec, &st);
+  } else {
+    e = s.op(opt, nullptr);
+  }
+  Sparse* sp = dynamic_cast<Sparse*>(s.M.get());
+  if (!sp) return KS_STATUS_NOT_RUN;
+  if (n_out) *n_out = s.n;
+  if (order) for (int k = 0; k < s.n; k++) order[k] = sp->q[k];
+  if (pattern) {
+    std::fill(pattern, pattern + (size_t)s.n * s.n, 0);
+    for (size_t k = 0; k < sp->ri.size(); k++) pattern[(size_t)sp->ri[k] * s.n + sp->ci[k]] = 1;
+  }
+  return e;
+}
+
+// minimumDegree (solver/sparse.go:412-452) of an n x n byte pattern.
+extern "C" void kso_min_degree(int n, const uint8_t* pattern, int32_t* order) {
+  std::vector<int32_t> ri, ci;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      if (pattern[(size_t)i * n + j]) { ri.push_back(i); ci.push_back(j); }
+  std::vector<int> q = minimumDegree(n, ri, ci);
+  for (int k = 0; k < n; k++) order[k] = q[k];
+}
+
 // analysis.Tran with the Waveform's element series and ledger (recorder,
 // analysis/tran.go:248-386).
 extern "C" int kso_tran_results(const ks_topology* t, const double* values, const ks_tran_spec* spec,

@@ -83,6 +83,14 @@ int kso_tran_torn(const ks_topology* t, const double* values, const ks_tran_spec
 int kso_torn_plan(const ks_topology* t, const double* values, const int32_t* pairs, int n_pairs, double h,
                   int32_t* piece_of, int32_t* n_pieces, int32_t* rows, int cap, int32_t* n_rows);
 
+/* The sparse backend's column order after an operating point (spec NULL) or a
+ * transient, with the pattern it ordered (every entry the run's loads stamped,
+ * n x n bytes); returns the analysis's status.  kso_min_degree: minimumDegree
+ * (solver/sparse.go:412-452) of a given pattern. */
+int kso_sparse_order(const ks_topology* t, const double* values, const ks_tran_spec* spec, const ks_options* o,
+                     int32_t* n, int32_t* order, uint8_t* pattern);
+void kso_min_degree(int n, const uint8_t* pattern, int32_t* order);
+
 /* Unknown count and layout of one circuit (device Setup), for the tests. */
 int kso_unknowns(const ks_topology* t, const double* values, int32_t* n, int32_t* is_v);
 

@@ -66,6 +66,9 @@ def lib():
         L.kso_dc.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, P, P, ctypes.c_char_p, ctypes.c_int]
         L.kso_tran.argtypes = [P, P, P, P, ctypes.c_int, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
         L.kso_op_results.argtypes = [P, P, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
+        L.kso_sparse_order.argtypes = [P, P, P, P, P, P, P]
+        L.kso_min_degree.argtypes = [ctypes.c_int, P, P]
+        L.kso_min_degree.restype = None
         L.kso_tran_results.argtypes = [P, P, P, P, ctypes.c_int, P, P, P, P, P, P, P, P, ctypes.c_char_p,
                                        ctypes.c_int]
         L.kso_batch_op.argtypes = [P, P, ctypes.c_int, P, P, ctypes.c_int, P, P, P]
@@ -175,6 +178,26 @@ def tran_results(pk, spec, opt=None, capacity=200000):
     k = npts.value
     return (st, t[:k], x[:k], elem[:k, :len(pk.elements)], led[:k], summ, steps.value, it.value,
             err.value.decode())
+
+
+def sparse_order(pk, spec=None, opt=None):
+    """The sparse backend's column order after an operating point (or a transient
+    when spec is given) and the pattern it ordered: (status, order [n], pattern [n][n] bool)."""
+    n, _ = unknowns(pk)
+    order = np.zeros(n, dtype=np.int32)
+    pat = np.zeros((n, n), dtype=np.uint8)
+    o = opt or options()
+    st = lib().kso_sparse_order(pk.tref(), _ptr(pk.values), None if spec is None else ctypes.byref(spec),
+                                ctypes.byref(o), None, _ptr(order), _ptr(pat))
+    return st, order, pat.astype(bool)
+
+
+def min_degree(pattern):
+    """minimumDegree (solver/sparse.go:412-452) of an n x n pattern."""
+    p = np.ascontiguousarray(pattern, dtype=np.uint8)
+    order = np.zeros(p.shape[0], dtype=np.int32)
+    lib().kso_min_degree(p.shape[0], _ptr(p), _ptr(order))
+    return order
 
 
 def dc(pk, src, vals, opt=None):
