@@ -221,7 +221,16 @@ typedef struct {
                              em.DefaultTolerance em/energy.go:21) */
   int32_t skip_energy_check; /* Options.SkipEnergyCheck: build the ledger, never
                              fail a circuit on it */
-  int32_t reserved0;
+  int32_t step_predictor; /* transients: > 0 starts each time step's Newton from
+                             the extrapolation of the accepted history (the
+                             polynomial through the last three accepted points,
+                             two before there are three) instead of from the
+                             last one (analysis/tran.go:164); never across a
+                             breakpoint.  The Newton, its convergence test, the
+                             device limiting (from the accepted junction
+                             voltages) and the step control are the reference's,
+                             so the start changes how many iterations a step
+                             takes.  0: off. */
 } ks_options;
 
 /* ---- transient request (analysis/tran.go:26-59) ------------------------- */

@@ -102,13 +102,15 @@ class Options:
     start_check: float = 0.0    # re-solve from InitJct when the solution ends this far (V) from x0 (0: off)
     ledger_tol: float = 0.0     # Options.LedgerTolerance (0: 1e-9)
     skip_energy_check: bool = False  # Options.SkipEnergyCheck
+    step_predictor: bool = False     # transients: each step's Newton starts from the extrapolated history
 
     def c(self):
         return _lib.KsOptions(self.reltol, self.abstol, self.vntol, self.gmin, self.itl1, self.itl4,
                               int(self.no_gmin_stepping), int(self.no_source_stepping),
                               int(self.no_pseudo_transient), PREC[self.precision], KERNEL[self.kernel],
                               self.max_iter_total, self.deadline_s, self.mixed_passes, int(self.fp32_start_iters),
-                              float(self.start_check), float(self.ledger_tol), int(self.skip_energy_check), 0)
+                              float(self.start_check), float(self.ledger_tol), int(self.skip_energy_check),
+                              int(self.step_predictor))
 
 
 def _check(rc, what):

@@ -116,6 +116,7 @@ static KOpts make_opts(const ks_options* o) {  // analysis/op.go:91-110
   k.max_iter_total = o ? o->max_iter_total : 0;
   k.start32 = o && o->fp32_start_iters > 0 ? std::min(o->fp32_start_iters, 100000) : 0;
   k.start_check = o && o->start_check > 0 ? o->start_check : 0.0;
+  k.predict = o && o->step_predictor > 0 ? 1 : 0;
   return k;
 }
 

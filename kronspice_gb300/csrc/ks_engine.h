@@ -91,6 +91,7 @@ struct KOpts {
   double start_check;      // OP with a given start: a circuit whose solution ends farther than this (volts, any
                            // node) from its start is solved again from the standard start (0: no check)
   const int32_t* cancel;   // the batch's cancel word (page-locked host memory mapped for the device), or null
+  int32_t predict;         // transients: start each step's Newton from the extrapolated accepted history
   // element results and the energy ledger (read by the generic kernels' results instantiation only)
   double* res_elem;        // op: [B][ne][KS_RES_COLS]; transient: per recorded point [..][ne][2]
   double* res_ledger;      // op: [B][KS_LEDGER_COLS]; transient: per recorded point [..][KS_TPOINT_COLS]

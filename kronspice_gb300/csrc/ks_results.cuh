@@ -380,7 +380,9 @@ __device__ inline bool tran_point_results(Thr<SY, P>& t, TranLedger& L, const Lo
 // recorder.finish, analysis/tran.go:350-386: the summary row of circuit c; returns
 // true when the largest residual relative to the run's peak power exceeds the
 // tolerance.
-__device__ inline bool tran_finish(const KOpts& o, const TranLedger& L, int64_t c) {
+template <class SY, class P>
+__device__ inline bool tran_finish(Thr<SY, P>& t, const TranLedger& L, int64_t c) {
+  const KOpts& o = t.o;
   const double mrr = L.peakScale > 0 ? L.worstAbs / L.peakScale : 0.0;
   if (o.res_summary) {
     double* s = o.res_summary + c * KS_TSUM_COLS;

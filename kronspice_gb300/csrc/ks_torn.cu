@@ -793,6 +793,19 @@ __global__ void k_tl_h(int R, int64_t V, const int32_t* offp, const int32_t* off
   h[t] = s;
 }
 
+// Step predictor on fixed steps: x <- the extrapolation of the accepted
+// history (x_n in x, x_(n-1) in x1, x_(n-2) in x2) through its last `order` + 1
+// points, and the history shifted (x1 <- x_n, x2 <- x_(n-1)).
+__global__ void k_tl_predict(int64_t n, int order, double* x, double* x1, double* x2) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double a = x[i], b = x1[i];
+    x[i] = order >= 2 ? 3 * a - 3 * b + x2[i] : order == 1 ? 2 * a - b : a;
+    x2[i] = b;
+    x1[i] = a;
+  }
+}
+
 __global__ void k_tl_record(int n_probes, const int32_t* probes, int64_t V, const double* x, double* out) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)n_probes * V) return;
@@ -1737,11 +1750,17 @@ extern "C" int ks_torn_tran(ks_torn* T, const ks_tran_spec* spec, const ks_optio
   std::vector<int32_t> status(V, KS_STATUS_OK), iters(V, 0), steps(V, 0);
   int32_t* d_probes = nullptr;
   double* d_wave = nullptr;
+  double* d_xprev = nullptr;  // step predictor: the two accepted points before the last
+  if (o.predict && cudaMalloc(&d_xprev, 2 * sizeof(double) * (size_t)T->n * V) != cudaSuccess) {
+    set_error("ks_torn_tran: allocation");
+    return KS_ENOMEM;
+  }
   const size_t wave_elems = (size_t)npts * V * std::max(n_probes, 0);
   if (n_probes > 0) {
     if (cudaMalloc(&d_probes, sizeof(int32_t) * n_probes) != cudaSuccess ||
         cudaMalloc(&d_wave, sizeof(double) * wave_elems) != cudaSuccess) {
       cudaFree(d_probes);
+      cudaFree(d_xprev);
       set_error("ks_torn_tran: allocation");
       return KS_ENOMEM;
     }
@@ -1769,6 +1788,12 @@ extern "C" int ks_torn_tran(ks_torn* T, const ks_tran_spec* spec, const ks_optio
   for (long k = 1; k < npts && !rc; k++) {
     const double t = (double)k * spec->step, h = spec->step;
     lp.mode = ModeTran; lp.time = t; lp.h = h; lp.rh = 1 / h; lp.method = order; lp.initJct = false;
+    if (d_xprev) {  // Newton from the extrapolated history (x_0 .. x_(k-1) accepted)
+      const int64_t nv = T->n * V;
+      T->launches++;
+      k_tl_predict<<<blocks_for(nv, 256), 256, 0, T->st>>>(nv, (int)std::min<long>(k - 1, 2), T->x, d_xprev,
+                                                           d_xprev + nv);
+    }
     rc = newton(T, lp, o, o.itl4, reuse, status, iters);
     if (rc) break;
     rc = accept_all_variants(T, status, t, ModeTran, o.gmin);
@@ -1787,6 +1812,7 @@ extern "C" int ks_torn_tran(ks_torn* T, const ks_tran_spec* spec, const ks_optio
   }
   cudaFree(d_probes);
   cudaFree(d_wave);
+  cudaFree(d_xprev);
   if (rc) return rc;
   if ((rc = x_out(T, out_x))) return rc;
   if (out_status) memcpy(out_status, status.data(), sizeof(int32_t) * V);

@@ -160,7 +160,8 @@ struct TranLedger {
 template <class SY, class P>
 __device__ inline bool tran_point_results(Thr<SY, P>& t, TranLedger& L, const LoadParams& lp, int64_t c, int64_t B,
                                           double tp, bool imposed, bool stored_point, int64_t row);
-__device__ inline bool tran_finish(const KOpts& o, const TranLedger& L, int64_t c);
+template <class SY, class P>
+__device__ inline bool tran_finish(Thr<SY, P>& t, const TranLedger& L, int64_t c);
 
 // analysis.Tran of one circuit after another, pulled from the queue.  kRes: with
 // the element results and the energy ledger of every point (ks_tran_results).
@@ -179,6 +180,12 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
   int phase = TR_DONE, status = KS_STATUS_OK, accepted = 0, npts = 0, kgrid = 1, order = BE;
   bool hitBreak = false, onGrid = false;
   double tnow = 0, h = 0, tn = 0;
+  // step predictor: the accepted history xacc = x_n, save = x_(n-1), ptPrev =
+  // x_(n-2) (the DC fallbacks that use save and ptPrev are over by then), the
+  // steps h1 = t_n - t_(n-1) and h2 = t_(n-1) - t_(n-2), and how many of those
+  // points lie on the present side of the last breakpoint
+  double h1 = 0, h2 = 0;
+  int hist = 0;
   int64_t c = B;
   TranLedger L;
   // The results of the point at tp before its Accept; true: out of balance (the
@@ -204,7 +211,7 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
     if constexpr (kRes) L.reset();
     lp.method = BE; lp.time = 0; lp.h = 0; lp.rh = 0;
     phase = TR_START; status = KS_STATUS_OK; accepted = 0; npts = 0; kgrid = 1; order = BE;
-    tnow = 0; h = 0; tn = 0;
+    tnow = 0; h = 0; tn = 0; h1 = 0; h2 = 0; hist = 0;
     if (sp.uic) {
       set_initial_conditions(t);
       op_state_reset(st, o);
@@ -235,6 +242,22 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
     if (h != lp.h) lp.rh = 1 / h;  // one division per new step size
     lp.mode = ModeTran; lp.time = tn; lp.h = h; lp.method = order;
     st.it = 0; st.maxIter = o.itl4;
+    if (o.predict && hist >= 2) {  // Newton starts from the extrapolated history
+      // Lagrange extrapolation through the last three points (two after a corner)
+      double w0, w1, w2 = 0;
+      if (hist >= 3) {
+        w0 = (h + h1) * (h + h1 + h2) / (h1 * (h1 + h2));
+        w1 = -h * (h + h1 + h2) / (h1 * h2);
+        w2 = h * (h + h1) / (h2 * (h1 + h2));
+      } else {
+        w0 = 1 + h / h1;
+        w1 = -h / h1;
+      }
+#pragma unroll
+      for (int i = 0; i < t.n(); i++)
+        t.s.xn(i) = w0 * t.xacc[i] + w1 * t.save[i] + (hist >= 3 ? w2 * t.ptPrev[i] : 0.0);
+      prog_sync(t.prog);
+    }
   };
   auto reject = [&](double hNew) -> bool {  // analysis/tran.go:136-143
     x_from_col(t, t.xacc);
@@ -267,6 +290,7 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
           record(t, sp, c, B, 0.0, 0, &npts, out_time, out_wave);
           if (unbalanced) { status = KS_STATUS_LEDGER; phase = TR_DONE; }
           else {
+            hist = 1;
             x_to_col(t, t.xacc);
             phase = TR_STEP;
             st.initJct = false;
@@ -301,6 +325,14 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
         }
         if (unbalanced) { status = KS_STATUS_LEDGER; phase = TR_DONE; }
         else if (!rejected) {
+          if (o.predict) {  // shift the history before x_n <- the new point
+#pragma unroll
+            for (int i = 0; i < t.n(); i++) { t.ptPrev[i] = t.save[i]; t.save[i] = t.xacc[i]; }
+            prog_sync(t.prog);
+            h2 = h1; h1 = h;
+            // a point on a source corner starts a new history: no extrapolation across it
+            hist = hitBreak ? 1 : hist + 1;
+          }
           x_to_col(t, t.xacc);
           accepted++;
           tnow = tn;
@@ -324,7 +356,7 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
     }
     // circuit c finished: write its results and take the next one
     if constexpr (kRes) {
-      if (tran_finish(o, L, c) && status == KS_STATUS_OK) status = KS_STATUS_LEDGER;
+      if (tran_finish(t, L, c) && status == KS_STATUS_OK) status = KS_STATUS_LEDGER;
     }
     if (out_status) out_status[c] = status;
     if (out_steps) out_steps[c] = accepted;

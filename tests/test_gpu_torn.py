@@ -191,3 +191,28 @@ def test_fp32_factors_transient_matches_oracle(N, P, loads):
         scale = np.abs(r[2]).max()
         assert np.abs(wave[:, v, :] - r[2][:, probes]).max() <= 1e-9 * scale
         assert np.array_equal(it[v], it64[v])
+
+
+def test_step_predictor_on_the_power_grid():
+    """Each time step's Newton starting from the extrapolated history
+    (ks_options.step_predictor) converges to the oracle's points within the
+    Newton tolerance.  On the grid it saves no iterations: the pads' branch
+    currents relax exponentially over a few steps after every load edge, and the
+    extrapolation misses them by far more than the 1e-3 relative current
+    tolerance, so a step still takes the two solves it takes from the last point."""
+    el, nn, vals, torn, c = grid(3, 16, 2, 16, seed=4)
+    tb = analysis.TornBatch(el, nn, vals, torn)
+    spec = analysis.TranSpec(step=0.1e-9, stop=60 * 0.1e-9, fixed_step=True, method="be")
+    probes = np.arange(0, tb.n, 5)
+    _, _, st0, steps0, it0, _ = tb.tran(spec, analysis.Options(), probes=probes)
+    wave, x, st, steps, it, stats = tb.tran(spec, analysis.Options(step_predictor=True), probes=probes)
+    assert np.all(st == 0) and np.all(st0 == 0) and np.all(steps == 60)
+    assert it.sum() <= it0.sum(), (it, it0)
+    w6, x6, st6, _, it6, _ = tb.tran(spec, analysis.Options(reltol=1e-6, step_predictor=True), probes=probes)
+    assert np.all(st6 == 0)
+    ospec = orc.TranSpec(0.1e-9, 60 * 0.1e-9, 0.0, 0.0, 0, 1, 1, 0, 0.0, 0.0, 0.0)
+    for v in range(len(vals)):
+        r = orc.tran(orc.Packed(el, nn, vals[v]), ospec, orc.options(reltol=1e-6))
+        assert r[0] == 0, r[-1]
+        xo = r[2]
+        assert np.all(np.abs(w6[:, v, :] - xo[:, probes]) <= 1e-6 * np.abs(xo[:, probes]) + 2e-6)

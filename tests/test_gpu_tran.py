@@ -73,6 +73,50 @@ def test_diode_rectifier_fixed_step_batch():
     assert np.all(np.abs(wave[..., :2] - xo[..., :2]) <= 1e-6 * volt[..., :2] + 1e-6)
 
 
+@pytest.mark.parametrize("kernel", ["generic", "specialized"])
+def test_step_predictor_rectifier_batch(kernel):
+    """Newton from the extrapolated history (ks_options.step_predictor) on the
+    diode rectifier at a tight tolerance: a fifth fewer iterations, the same
+    waveforms within the tolerance."""
+    el, nn, vals = rectifier_batch(128, 9)
+    sp = analysis.TranSpec(step=5e-6, stop=2e-3, fixed_step=True)
+    b = analysis.Batch(analysis.Plan(el, nn, vals.shape[1]), vals)
+    w0, _, n0, st0, steps0, it0 = b.tran(sp, analysis.Options(reltol=1e-6, kernel=kernel))
+    w1, _, n1, st1, steps1, it1 = b.tran(sp, analysis.Options(reltol=1e-6, kernel=kernel, step_predictor=True))
+    assert np.all(st0 == 0) and np.all(st1 == 0) and np.array_equal(steps0, steps1)
+    assert it1.sum() < 0.9 * it0.sum(), (it1.sum(), it0.sum())
+    so, xo, so_steps, io = orc.batch_tran(orc.Packed(el, nn, vals), 128, ospec(sp), orc.options(reltol=1e-6))
+    assert np.all(so == 0)
+    assert np.all(np.abs(w1[..., :2] - xo[..., :2]) <= 1e-5 * np.abs(xo[..., :2]) + 1e-5)
+
+
+def test_step_predictor_adaptive_golden():
+    """Adaptive golden transients with the predictor: the same accepted grid to
+    within a few steps and the golden tables still met."""
+    for case in TRAN_CASES:
+        ckt = kc.from_dict(case["circuit"])
+        tr = [a for a in case["circuit"]["analyses"] if a["kind"] == "tran"][-1]
+        sp = analysis.TranSpec(step=tr["step"], stop=tr["stop"], start=tr["start"], max_step=tr["max_step"],
+                               uic=tr["uic"])
+        el, vals, _ = ckt.pack()
+        b = analysis.Batch(analysis.Plan(el, ckt.n_nodes, len(vals)), vals[None, :])
+        wave, tim, npts, st, steps, it = b.tran(sp, analysis.Options(step_predictor=True), capacity=200000)
+        assert st[0] == 0, case["name"]
+        k = int(npts[0])
+        t = list(tim[0, :k])
+        x = wave[0, :k]
+
+        def get(name):
+            if not name.startswith("v("):
+                return None
+            i = ckt.node_index(name[2:-1])
+            return None if i < 0 else (np.zeros(k) if i == 0 else list(x[:, i - 1]))
+        want = case["golden"]["independent"]
+        want = dict(want, names=[nm for nm in want["names"] if nm.startswith("v(")])
+        if want["names"]:
+            assert not gc.compare_table(t, get, want), case["name"]
+
+
 with open(os.path.join(ROOT, "tests", "golden", "reference_cases.json")) as f:
     CASES = [c for c in json.load(f)["cases"] if not c["skip"]]
 TRAN_CASES = [c for c in CASES if any(a["kind"] == "tran" for a in c["circuit"]["analyses"])]
