@@ -37,6 +37,8 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -318,12 +320,10 @@ __global__ void __launch_bounds__(256) k_tl_band_lu(const PieceD* pcs, int64_t V
 // barriers only (a column step is a few shared-memory accesses and one
 // multiply-add per row a lane owns).  The part of each column a sweep reads (the
 // kl multipliers below the diagonal going down, the kl + ku entries above it
-// and the diagonal coming back) is staged into shared memory KS_TORN_CH columns
-// at a time with asynchronous copies, KS_TORN_NBUF - 1 blocks ahead, so the
-// sweep waits on barriers, not on memory.
-#define KS_TORN_CH 4
-#define KS_TORN_NBUF 4
-template <typename F>
+// and the diagonal coming back) is staged into shared memory CH columns at a
+// time with asynchronous copies, NB - 1 blocks ahead, so the sweep waits on
+// barriers, not on memory.
+template <typename F, int CH, int NB>
 __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t V, int64_t band_stride,
                                                       const F* band, int64_t piv_stride, const int32_t* piv_all,
                                                       const int32_t* pidx, const double* rs, const double* cs,
@@ -340,8 +340,8 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
   const int t = threadIdx.x;
   F* y = smem;                                      // [max_n], rounded to 2
   F* buf = smem + ((max_n + 1) & ~1);               // [NBUF][CH][max_colw]
-  int* spiv = reinterpret_cast<int*>(buf + KS_TORN_NBUF * KS_TORN_CH * max_colw);  // [NBUF][CH]
-  const int bufsz = KS_TORN_CH * max_colw;
+  int* spiv = reinterpret_cast<int*>(buf + NB * CH * max_colw);  // [NBUF][CH]
+  const int bufsz = CH * max_colw;
   for (int i = t; i < n; i += 32) {
     const int g = pidx[pc.idx_off + i];
     double bi = b[(int64_t)g * V + v];
@@ -351,27 +351,27 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
     }
     y[i] = (F)(bi * rs[(int64_t)g * V + v]);
   }
-  const int nch = (n + KS_TORN_CH - 1) / KS_TORN_CH;
+  const int nch = (n + CH - 1) / CH;
   // stage block c: `width` doubles of each column from row offset `first`
   auto stage = [&](int c, int first, int width, bool pivots) {
     if (c < 0 || c >= nch) { __pipeline_commit(); return; }
-    const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
-    F* dst = buf + (c % KS_TORN_NBUF) * bufsz;
+    const int j0 = c * CH, cols = min(CH, n - j0);
+    F* dst = buf + (c % NB) * bufsz;
     const F* src = AB + first + (int64_t)j0 * ldab;
     for (int jj = 0; jj < cols; jj++, dst += max_colw, src += ldab)
       for (int r = t; r < width; r += 32) __pipeline_memcpy_async(dst + r, src + r, sizeof(F));
     __pipeline_commit();
-    if (pivots && t < cols) spiv[(c % KS_TORN_NBUF) * KS_TORN_CH + t] = piv[j0 + t];
+    if (pivots && t < cols) spiv[(c % NB) * CH + t] = piv[j0 + t];
   };
   // L: row interchanges and the unit lower band (staged: rows kv+1 .. kv+kl of each column)
-  for (int c = 0; c < KS_TORN_NBUF - 1; c++) stage(c, kv + 1, kl, true);
+  for (int c = 0; c < NB - 1; c++) stage(c, kv + 1, kl, true);
   for (int c = 0; c < nch; c++) {
-    stage(c + KS_TORN_NBUF - 1, kv + 1, kl, true);
-    __pipeline_wait_prior(KS_TORN_NBUF - 1);
+    stage(c + NB - 1, kv + 1, kl, true);
+    __pipeline_wait_prior(NB - 1);
     __syncwarp();
-    const F* B = buf + (c % KS_TORN_NBUF) * bufsz;
-    const int* P = spiv + (c % KS_TORN_NBUF) * KS_TORN_CH;
-    const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
+    const F* B = buf + (c % NB) * bufsz;
+    const int* P = spiv + (c % NB) * CH;
+    const int j0 = c * CH, cols = min(CH, n - j0);
     for (int jj = 0; jj < cols; jj++) {
       const int j = j0 + jj;
       const int km = min(kl, n - 1 - j);
@@ -403,13 +403,13 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
   __pipeline_wait_prior(0);
   __syncwarp();
   // U: rows 0 .. kv of each column (row j - kv + o at o, the diagonal at kv), last block first
-  for (int k = 0; k < KS_TORN_NBUF - 1; k++) stage(nch - 1 - k, 0, kv + 1, false);
+  for (int k = 0; k < NB - 1; k++) stage(nch - 1 - k, 0, kv + 1, false);
   for (int c = nch - 1; c >= 0; c--) {
-    stage(c - (KS_TORN_NBUF - 1), 0, kv + 1, false);
-    __pipeline_wait_prior(KS_TORN_NBUF - 1);
+    stage(c - (NB - 1), 0, kv + 1, false);
+    __pipeline_wait_prior(NB - 1);
     __syncwarp();
-    const F* B = buf + (c % KS_TORN_NBUF) * bufsz;
-    const int j0 = c * KS_TORN_CH, cols = min(KS_TORN_CH, n - j0);
+    const F* B = buf + (c % NB) * bufsz;
+    const int j0 = c * CH, cols = min(CH, n - j0);
     for (int jj = cols - 1; jj >= 0; jj--) {
       const int j = j0 + jj;
       const F yj = y[j] * B[jj * max_colw + kv];  // the diagonal slot holds 1 / u_jj
@@ -1004,9 +1004,49 @@ void stamp_pattern(const ksh::HostPlan& hp, std::vector<std::vector<int>>& rows)
   for (int i = 0; i < hp.n; i++) add(i, i);
 }
 
+// Staging of a band solve: CH columns a block, NB blocks in shared memory.  FP32
+// factors take twice the blocks in the same space, so the sweep runs further
+// ahead of its loads; KS_TORN_BAND="CH,NB" picks another of the built shapes.
+struct BandCfg { int ch, nb; };
+constexpr BandCfg kBandShapes[] = {{4, 4}, {4, 6}, {8, 3}, {8, 4}, {2, 8}, {4, 8}, {8, 6}};
+BandCfg band_cfg(bool fp32) {
+  BandCfg d = fp32 ? BandCfg{8, 3} : BandCfg{4, 4};  // measured best at 64 variants of the 256 x 256 grid
+  if (const char* e = getenv("KS_TORN_BAND")) {
+    int c = 0, b = 0;
+    if (sscanf(e, "%d,%d", &c, &b) == 2)
+      for (const BandCfg& k : kBandShapes)
+        if (k.ch == c && k.nb == b) return k;
+  }
+  return d;
+}
+
+// Dynamic shared memory of a band solve with elements of `es` bytes: the
+// right-hand side of the largest piece, NB x CH staged columns, their pivots.
+size_t band_smem(const ks_torn* T, size_t es, BandCfg c) {
+  return es * (((size_t)T->max_piece + 1) & ~(size_t)1) + es * (size_t)c.nb * c.ch * (size_t)T->max_colw +
+         sizeof(int) * (size_t)c.nb * c.ch;
+}
 size_t torn_solve_smem(const ks_torn* T) {
-  return sizeof(double) * (((size_t)T->max_piece + 1) & ~(size_t)1) +
-         sizeof(double) * KS_TORN_NBUF * (size_t)KS_TORN_CH * (size_t)T->max_colw + sizeof(int) * KS_TORN_NBUF * KS_TORN_CH;
+  return std::max(band_smem(T, sizeof(double), band_cfg(false)), band_smem(T, sizeof(float), band_cfg(true)));
+}
+
+// The kernel instance of a band-solve shape (its shared memory opted in once).
+template <typename F>
+using BandSolveFn = void (*)(const PieceD*, int64_t, int64_t, const F*, int64_t, const int32_t*, const int32_t*,
+                             const double*, const double*, const double*, const int32_t*, const double*, double*,
+                             const uint8_t*, int, int);
+template <typename F>
+BandSolveFn<F> band_solve_fn(BandCfg c, size_t smem) {
+  BandSolveFn<F> f = nullptr;
+  if (c.ch == 4 && c.nb == 4) f = k_tl_band_solve<F, 4, 4>;
+  else if (c.ch == 4 && c.nb == 6) f = k_tl_band_solve<F, 4, 6>;
+  else if (c.ch == 8 && c.nb == 3) f = k_tl_band_solve<F, 8, 3>;
+  else if (c.ch == 8 && c.nb == 4) f = k_tl_band_solve<F, 8, 4>;
+  else if (c.ch == 2 && c.nb == 8) f = k_tl_band_solve<F, 2, 8>;
+  else if (c.ch == 4 && c.nb == 8) f = k_tl_band_solve<F, 4, 8>;
+  else f = k_tl_band_solve<F, 8, 6>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return f;
 }
 
 int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_torn, std::string* err,
@@ -1324,19 +1364,23 @@ int apply_(ks_torn* T, const double* b, double* out) {
   const int R = T->R;
   cudaStream_t s = T->st;
   const unsigned grid = (unsigned)(V * T->P);
-  const size_t sm = torn_solve_smem(T);
   const int bt = 32;  // one warp per (variant, piece)
   // the band solves: FP32 factors under mixed precision, else FP64
   auto band_solve = [&](const double* w, double* o) {
     T->launches++;
-    if (T->fp32)
-      k_tl_band_solve<float><<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band32, T->piv_stride, T->piv,
-                                                  T->d_pidx, T->rs, T->cs, b, T->d_row_a, w, o, T->mask, T->max_piece,
-                                                  T->max_colw);
-    else
-      k_tl_band_solve<double><<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv,
-                                                   T->d_pidx, T->rs, T->cs, b, T->d_row_a, w, o, T->mask, T->max_piece,
-                                                   T->max_colw);
+    if (T->fp32) {
+      const BandCfg c = band_cfg(true);
+      const size_t sm = band_smem(T, sizeof(float), c);
+      band_solve_fn<float>(c, sm)<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band32, T->piv_stride, T->piv,
+                                                        T->d_pidx, T->rs, T->cs, b, T->d_row_a, w, o, T->mask,
+                                                        T->max_piece, T->max_colw);
+    } else {
+      const BandCfg c = band_cfg(false);
+      const size_t sm = band_smem(T, sizeof(double), c);
+      band_solve_fn<double>(c, sm)<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv,
+                                                         T->d_pidx, T->rs, T->cs, b, T->d_row_a, w, o, T->mask,
+                                                         T->max_piece, T->max_colw);
+    }
   };
   if (R == 0) {
     band_solve(nullptr, out);
@@ -1452,11 +1496,7 @@ ks_torn* untorn_of(ks_torn* T) {
     T->untorn_failed = true;
     return nullptr;
   }
-  const size_t band_smem = torn_solve_smem(U);
-  if (band_smem > 48 * 1024 && band_smem > torn_solve_smem(T)) {
-    cudaFuncSetAttribute(k_tl_band_solve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
-    cudaFuncSetAttribute(k_tl_band_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
-  }
+
   U->st = T->st;
   U->fp32 = T->fp32;
   T->untorn = U;
@@ -1583,11 +1623,6 @@ extern "C" int ks_torn_create(const ks_topology* topo, int32_t n_variants, const
   if (ic_smem > 48 * 1024) {
     cudaFuncSetAttribute(k_tl_ic_solve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ic_smem);
     cudaFuncSetAttribute(k_tl_ic_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ic_smem);
-  }
-  const size_t band_smem = torn_solve_smem(T);
-  if (band_smem > 48 * 1024) {
-    cudaFuncSetAttribute(k_tl_band_solve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
-    cudaFuncSetAttribute(k_tl_band_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem);
   }
   if (cudaStreamCreateWithFlags(&T->own, cudaStreamNonBlocking) != cudaSuccess) {
     set_error("ks_torn_create: stream creation failed");
