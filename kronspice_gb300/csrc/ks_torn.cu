@@ -446,6 +446,175 @@ __global__ void __launch_bounds__(32) k_tl_band_solve(const PieceD* pcs, int64_t
   }
 }
 
+// Blocked form of the same solve, the rows a block of 32 columns can reach held
+// in registers: lane l keeps rows base + 32 k + l (k < NS) of a window that
+// slides 32 rows per block, so a column step is one shuffle broadcast of the
+// pivot row and one shared-memory load and multiply-add per slot, and the
+// sweep's dependency chain runs at register latency.  Each staged column sits
+// in a zero-padded row (its entries from 32 going forward, from PB coming back)
+// so that window slot k of lane l reads 31 + l - jj + 32 k (jj: the column's
+// place in its block of 32): the multiply-adds need no bounds tests, rows the
+// column does not reach read zeros.  Rows enter the window from the
+// right-hand side (forward) or from the scratch ys (backward) and leave it
+// final; the band's columns stream through shared memory in chunks of SC, NBUF
+// deep.  NSL >= 1 + kl / 32 and NSU >= 1 + (kl + ku) / 32.
+template <typename F, int NSL, int NSU, int SC, int NBUF>
+__global__ void __launch_bounds__(32) k_tl_band_solve_rw(const PieceD* pcs, int64_t V, int64_t band_stride,
+                                                         const F* band, int64_t piv_stride, const int32_t* piv_all,
+                                                         const int32_t* pidx, const double* rs, const double* cs,
+                                                         const double* b, const int32_t* row_a, const double* w,
+                                                         double* out, F* ys_all, const uint8_t* mask, int max_colw) {
+  static_assert(32 % SC == 0, "chunks tile the 32-column blocks");
+  constexpr int WF = 32 * NSL + 32, WB = 32 * NSU + 32;  // padded row widths, forward and backward
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  F* buf = reinterpret_cast<F*>(smem_raw);                                 // [NBUF][SC][WF or WB]
+  F* dg = buf + NBUF * SC * WB;                                            // [NBUF][SC] 1 / u_jj
+  int* spiv = reinterpret_cast<int*>(dg + NBUF * SC);                      // [NBUF][SC]
+  const int v = blockIdx.x % V, p = blockIdx.x / V;
+  if (!mask[v]) return;
+  const PieceD pc = pcs[p];
+  const F* AB = band + (int64_t)v * band_stride + pc.band_off;
+  const int32_t* piv = piv_all + (int64_t)v * piv_stride + pc.idx_off;
+  F* ys = ys_all + (int64_t)v * piv_stride + pc.idx_off;
+  const int n = pc.n, kl = pc.kl, ldab = pc.ldab, kv = pc.kl + pc.ku;
+  const int lane = threadIdx.x;
+  const int nch = (n + SC - 1) / SC;
+  const int PB = 32 * NSU - kv - 1;  // backward: U(j - kv + o, j) at PB + o
+  auto zero_buf = [&](int width) {
+    for (int q = lane; q < NBUF * SC * width; q += 32) buf[q] = F(0);
+    __syncwarp();
+  };
+  // stage chunk c: `width` entries from row offset `first` of each of its
+  // columns to its rows (c % NBUF, j % SC), at 32 going forward and at PB back
+  // (the rest of every row stays zero)
+  auto stage = [&](int c, int first, int width, int W, bool fwd) {
+    if (c < 0 || c >= nch) { __pipeline_commit(); return; }
+    const int j0 = c * SC, cols = min(SC, n - j0);
+    for (int jj = 0; jj < cols; jj++) {
+      const int j = j0 + jj;
+      F* dst = buf + ((c % NBUF) * SC + jj) * W + (fwd ? 32 : PB);
+      const F* src = AB + first + (int64_t)j * ldab;
+      for (int r = lane; r < width; r += 32) __pipeline_memcpy_async(dst + r, src + r, sizeof(F));
+    }
+    __pipeline_commit();
+    if (fwd && lane < cols) spiv[(c % NBUF) * SC + lane] = piv[j0 + lane];
+  };
+  auto rhs_row = [&](int i) -> F {  // (b - P.w) of row i, scaled by the row equilibration
+    if (i < 0 || i >= n) return F(0);
+    const int g = pidx[pc.idx_off + i];
+    double bi = b[(int64_t)g * V + v];
+    if (w) {
+      const int a = row_a[g];
+      if (a >= 0) bi -= w[(int64_t)a * V + v];
+    }
+    return (F)(bi * rs[(int64_t)g * V + v]);
+  };
+  // ---- forward: row interchanges and the unit lower band
+  zero_buf(WF);
+  F y[NSL];
+#pragma unroll
+  for (int k = 0; k < NSL; k++) y[k] = rhs_row(32 * k + lane);
+  for (int c = 0; c < NBUF - 1; c++) stage(c, kv + 1, kl, WF, true);
+  for (int j0 = 0; j0 < n; j0 += 32) {
+#pragma unroll
+    for (int jj = 0; jj < 32; jj++) {
+      const int j = j0 + jj;
+      if (j < n) {
+        if (jj % SC == 0) {
+          __syncwarp();  // every lane is done with the buffer the next chunk goes to
+          stage(j / SC + NBUF - 1, kv + 1, kl, WF, true);
+          __pipeline_wait_prior(NBUF - 1);
+          __syncwarp();
+        }
+        const int slot = ((j / SC) % NBUF) * SC + jj % SC;
+        const int dp = spiv[slot] - j0;  // pivot row, window coordinates
+        if (dp != jj) {                  // interchange rows j and p (warp-uniform, rare)
+          const int ks = dp >> 5, ls = dp & 31;
+          F at_p = y[0];
+#pragma unroll
+          for (int k = 1; k < NSL; k++)
+            if (k == ks) at_p = y[k];
+          const F vp = __shfl_sync(0xffffffffu, at_p, ls);
+          const F vj = __shfl_sync(0xffffffffu, y[0], jj);
+          if (lane == jj) y[0] = vp;
+#pragma unroll
+          for (int k = 0; k < NSL; k++)
+            if (k == ks && lane == ls) y[k] = vj;
+        }
+        const F yj = __shfl_sync(0xffffffffu, y[0], jj);
+        const F* B = buf + slot * WF + 31 + lane - jj;
+#pragma unroll
+        for (int k = 0; k < NSL; k++) y[k] -= B[32 * k] * yj;
+      }
+    }
+    // rows j0 .. j0 + 31 are final: out to the scratch, the window slides
+    if (j0 + lane < n) ys[j0 + lane] = y[0];
+#pragma unroll
+    for (int k = 0; k + 1 < NSL; k++) y[k] = y[k + 1];
+    y[NSL - 1] = rhs_row(j0 + 32 * NSL + lane);
+  }
+  __pipeline_wait_prior(0);
+  __syncwarp();
+  // ---- backward: the upper band (U(j - kv + o, j) at o, 1 / u_jj at kv)
+  zero_buf(WB);
+  const int nb = (n + 31) / 32;
+  F u[NSU];
+  {
+    const int base = 32 * (nb - 1) + 32 - 32 * NSU;
+#pragma unroll
+    for (int k = 0; k < NSU; k++) {
+      const int i = base + 32 * k + lane;
+      u[k] = (i >= 0 && i < n) ? ys[i] : F(0);
+    }
+  }
+  // chunks in descending order; chunk c's diagonal moved out of its rows once it lands
+  auto land = [&](int c) {
+    const int j0 = c * SC, cols = min(SC, n - j0);
+    if (lane < cols) {
+      F* row = buf + ((c % NBUF) * SC + lane) * WB + PB;
+      dg[(c % NBUF) * SC + lane] = row[kv];
+      row[kv] = F(0);
+    }
+    __syncwarp();
+  };
+  for (int k = 0; k < NBUF - 1; k++) stage(nch - 1 - k, 0, kv + 1, WB, false);
+  for (int j0 = 32 * (nb - 1); j0 >= 0; j0 -= 32) {
+#pragma unroll
+    for (int jj = 31; jj >= 0; jj--) {
+      const int j = j0 + jj;
+      if (j < n) {
+        if (jj % SC == SC - 1 || j == n - 1) {
+          const int c = j / SC;
+          __syncwarp();
+          stage(c - (NBUF - 1), 0, kv + 1, WB, false);
+          __pipeline_wait_prior(NBUF - 1);
+          __syncwarp();
+          land(c);
+        }
+        const int slot = ((j / SC) % NBUF) * SC + jj % SC;
+        if (lane == jj) u[NSU - 1] *= dg[slot];
+        const F yj = __shfl_sync(0xffffffffu, u[NSU - 1], jj);
+        const F* B = buf + slot * WB + 31 + lane - jj;
+#pragma unroll
+        for (int k = 0; k < NSU; k++) u[k] -= B[32 * k] * yj;
+      }
+    }
+    {  // rows j0 .. j0 + 31 are final: out, unscaled by the column equilibration
+      const int i = j0 + lane;
+      if (i < n) {
+        const int g = pidx[pc.idx_off + i];
+        out[(int64_t)g * V + v] = (double)u[NSU - 1] * cs[(int64_t)g * V + v];
+      }
+    }
+#pragma unroll
+    for (int k = NSU - 1; k > 0; k--) u[k] = u[k - 1];
+    const int i = j0 - 32 * NSU + lane;  // the window's new bottom rows
+    u[0] = (i >= 0 && i < n) ? ys[i] : F(0);
+  }
+  __pipeline_wait_prior(0);
+  __syncwarp();
+}
+
 // After a refactor (the port columns made): each band's U diagonal replaced by
 // its reciprocal (the solves multiply by it) and the FP32 copy of the factors
 // the applications stream under mixed precision.
@@ -909,6 +1078,7 @@ struct ks_torn {
   int V = 0, n = 0, nnz = 0, R = 0, P = 0, n_nonlin = 0;
   int max_piece = 0, max_band = 0;
   int max_colw = 0;  // widest staged column part of a band solve (max of kl, kl + ku + 1)
+  int max_klu = 0;   // largest lower or upper bandwidth of a piece
   std::vector<HostPiece> pieces;
   std::vector<int> rp, ci;
   std::vector<int> h_pieceOf, h_rows;  // piece of each unknown, coupling rows (the plan, host side)
@@ -924,6 +1094,7 @@ struct ks_torn {
   int64_t band_stride = 0, piv_stride = 0, wc_stride = 0, y_stride = 0;
   // device numeric
   double *values, *derived, *state, *x, *xo, *J, *rhs, *r, *dx, *z, *rs, *cs, *band, *Y, *Wc, *IC, *h, *w;
+  double* ysweep = nullptr;  // the blocked band solve's rows between its two sweeps [V][piv_stride]
   float *band32 = nullptr, *IC32 = nullptr;  // FP32 copies of the factors (mixed precision applications)
   bool fp32 = false;                          // this call's applications stream the FP32 copies
   int32_t *piv, *icpiv, *bad, *flags, *list;
@@ -1028,6 +1199,47 @@ size_t band_smem(const ks_torn* T, size_t es, BandCfg c) {
 }
 size_t torn_solve_smem(const ks_torn* T) {
   return std::max(band_smem(T, sizeof(double), band_cfg(false)), band_smem(T, sizeof(float), band_cfg(true)));
+}
+
+// The blocked band solve (k_tl_band_solve_rw): register window of NS = (32 +
+// the widest lower or upper band) / 32 slots going forward, 2 NS - 1 coming
+// back, for bands up to 160 wide; chunks of 8 columns, RW_NBUF deep (the
+// shared memory holds only the staged columns).
+constexpr int kRwSC = 8, kRwMaxNS = 5;
+int rw_nbuf() {
+  const char* e = getenv("KS_TORN_RW_NBUF");
+  const int nb = e ? atoi(e) : 3;
+  return nb == 2 || nb == 4 ? nb : 3;
+}
+int rw_slots(const ks_torn* T) { return std::max(2, (32 + T->max_klu + 31) / 32); }
+size_t rw_smem(const ks_torn* T, size_t es, int nbuf) {
+  const int nsu = 2 * rw_slots(T) - 1;  // the backward rows are the wider ones
+  return es * (size_t)nbuf * kRwSC * (32 * nsu + 32) + es * nbuf * kRwSC + sizeof(int) * (size_t)nbuf * kRwSC;
+}
+template <typename F>
+using BandSolveRwFn = void (*)(const PieceD*, int64_t, int64_t, const F*, int64_t, const int32_t*, const int32_t*,
+                               const double*, const double*, const double*, const int32_t*, const double*, double*, F*,
+                               const uint8_t*, int);
+template <typename F, int NS>
+BandSolveRwFn<F> rw_fn_ns(int nbuf) {
+  switch (nbuf) {
+    case 2: return k_tl_band_solve_rw<F, NS, 2 * NS - 1, kRwSC, 2>;
+    case 4: return k_tl_band_solve_rw<F, NS, 2 * NS - 1, kRwSC, 4>;
+    default: return k_tl_band_solve_rw<F, NS, 2 * NS - 1, kRwSC, 3>;
+  }
+}
+template <typename F>
+BandSolveRwFn<F> rw_fn(int ns, int nbuf, size_t smem) {
+  BandSolveRwFn<F> f = nullptr;
+  switch (ns) {
+    case 2: f = rw_fn_ns<F, 2>(nbuf); break;
+    case 3: f = rw_fn_ns<F, 3>(nbuf); break;
+    case 4: f = rw_fn_ns<F, 4>(nbuf); break;
+    case 5: f = rw_fn_ns<F, 5>(nbuf); break;
+    default: return nullptr;
+  }
+  if (smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return f;
 }
 
 // The kernel instance of a band-solve shape (its shared memory opted in once).
@@ -1199,6 +1411,7 @@ int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_t
     T->max_piece = std::max(T->max_piece, d.n);
     T->max_colw = std::max(T->max_colw, std::max(d.kl, d.kl + d.ku + 1));
     T->max_band = std::max(T->max_band, d.kl + d.ku);
+    T->max_klu = std::max(T->max_klu, std::max(d.kl, d.ku));
     if (d.n > 12000) { *err = "ks_torn: a piece of " + std::to_string(d.n) + " unknowns (the band solve holds at most 12,000)"; return KS_EUNSUPPORTED; }
   }
   T->band_stride = band; T->piv_stride = n; T->wc_stride = wc; T->y_stride = y;
@@ -1258,6 +1471,7 @@ int alloc_numeric(ks_torn* T) {
   T->band = dalloc<double>((size_t)T->band_stride * V, o);
   T->band32 = dalloc<float>((size_t)T->band_stride * V, o);
   T->piv = dalloc<int32_t>((size_t)T->piv_stride * V, o);
+  T->ysweep = dalloc<double>((size_t)T->piv_stride * V, o);
   T->Y = dalloc<double>((size_t)T->y_stride * V, o);
   T->Wc = dalloc<double>((size_t)T->wc_stride * V, o);
   T->IC = dalloc<double>((size_t)T->R * T->R * V, o);
@@ -1271,7 +1485,7 @@ int alloc_numeric(ks_torn* T) {
   T->have.assign(V, 0);
   for (void* p : {(void*)T->values, (void*)T->derived, (void*)T->state, (void*)T->x, (void*)T->xo, (void*)T->J,
                   (void*)T->rhs, (void*)T->r, (void*)T->dx, (void*)T->z, (void*)T->rs, (void*)T->cs, (void*)T->band,
-                  (void*)T->piv, (void*)T->Y, (void*)T->Wc, (void*)T->IC, (void*)T->icpiv, (void*)T->h, (void*)T->w,
+                  (void*)T->piv, (void*)T->ysweep, (void*)T->Y, (void*)T->Wc, (void*)T->IC, (void*)T->icpiv, (void*)T->h, (void*)T->w,
                   (void*)T->bad, (void*)T->flags, (void*)T->berr, (void*)T->mask,
                   (void*)T->list, (void*)T->band32, (void*)T->IC32})
     if (!p) { set_error("ks_torn: device allocation failed"); return KS_ENOMEM; }
@@ -1366,8 +1580,30 @@ int apply_(ks_torn* T, const double* b, double* out) {
   const unsigned grid = (unsigned)(V * T->P);
   const int bt = 32;  // one warp per (variant, piece)
   // the band solves: FP32 factors under mixed precision, else FP64
+  const int ns = rw_slots(T);  // 2 .. kRwMaxNS: the blocked solve has an instance
+  const char* rwe = getenv("KS_TORN_RW");  // "0": the column-by-column solve
+  const bool rw = ns <= kRwMaxNS && !(rwe && atoi(rwe) == 0);
   auto band_solve = [&](const double* w, double* o) {
     T->launches++;
+    if (rw) {  // the blocked solve
+      const int nbuf = rw_nbuf();
+      if (T->fp32) {
+        const size_t sm = rw_smem(T, sizeof(float), nbuf);
+        if (auto f = rw_fn<float>(ns, nbuf, sm)) {
+          f<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band32, T->piv_stride, T->piv, T->d_pidx, T->rs,
+                                 T->cs, b, T->d_row_a, w, o, reinterpret_cast<float*>(T->ysweep), T->mask,
+                                 T->max_colw);
+          return;
+        }
+      } else {
+        const size_t sm = rw_smem(T, sizeof(double), nbuf);
+        if (auto f = rw_fn<double>(ns, nbuf, sm)) {
+          f<<<grid, bt, sm, s>>>(T->d_pcs, V, T->band_stride, T->band, T->piv_stride, T->piv, T->d_pidx, T->rs,
+                                 T->cs, b, T->d_row_a, w, o, T->ysweep, T->mask, T->max_colw);
+          return;
+        }
+      }
+    }
     if (T->fp32) {
       const BandCfg c = band_cfg(true);
       const size_t sm = band_smem(T, sizeof(float), c);
