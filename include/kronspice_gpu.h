@@ -69,7 +69,12 @@ typedef enum {
   KS_ELEM_I = 5,  /* current source    device/source.go:133   */
   KS_ELEM_D = 6,  /* junction diode    device/diode.go:61     */
   KS_ELEM_Q = 7,  /* Gummel-Poon BJT   device/bjt.go:78       */
-  KS_ELEM_M = 8   /* MOSFET level 1-3  device/mosfet.go:43    */
+  KS_ELEM_M = 8,  /* MOSFET level 1-3  device/mosfet.go:43    */
+  KS_ELEM_E = 9,  /* VCVS              device/controlled.go:29 */
+  KS_ELEM_F = 10, /* CCCS              device/controlled.go:29 */
+  KS_ELEM_G = 11, /* VCCS              device/controlled.go:29 */
+  KS_ELEM_H = 12, /* CCVS              device/controlled.go:29 */
+  KS_ELEM_K = 13  /* mutual inductance device/mutual.go:30     */
 } ks_elem_kind;
 
 /* source waveforms (circuit/circuit.go WaveKind; device/waveform.go) */
@@ -104,6 +109,13 @@ enum {
  *                 -- Element.Nodes/Extra of circuit/builder.go:101
  *   M (MOSFET)  : node[0] = drain, node[1] = source, node[2] = gate,
  *                 node[3] = bulk    -- circuit/builder.go:108
+ *   E, G        : node[0] = n+, node[1] = n-, node[2] = nc+, node[3] = nc-
+ *                 (the controlling voltage, Element.CtrlNodes)
+ *   F, H        : node[0] = n+, node[1] = n-, node[2] = index in elem[] of
+ *                 the controlling voltage source (Element.CtrlSource; its
+ *                 branch current, positive into its n+ terminal)
+ *   K           : node[0], node[1] = indices in elem[] of the two coupled
+ *                 inductors (Element.Couples); no circuit nodes
  * param is the offset of the element's block in the per-circuit value vector;
  * the block layouts are the KS_*_P_* enums below.
  */
@@ -129,6 +141,8 @@ typedef struct {
 /* value blocks -------------------------------------------------------------*/
 /* R: [R]   C: [C, IC]   L: [L, IC] */
 enum { KS_RCL_P_VALUE = 0, KS_RCL_P_IC = 1, KS_RCL_NP = 2 };
+/* E, F, G, H: [gain]   K: [coupling coefficient k] */
+enum { KS_CTL_P_GAIN = 0, KS_K_P_COUPLING = 0, KS_CTL_NP = 1 };
 /* V, I: [dc, ac_mag, ac_phase_deg, arg0 .. arg(nargs-1)] */
 enum { KS_SRC_P_DC = 0, KS_SRC_P_ACMAG = 1, KS_SRC_P_ACPHASE = 2, KS_SRC_P_ARGS = 3 };
 /* D: DiodeParams of device/diode.go:23 after defaults and area scaling */

@@ -15,7 +15,8 @@ import math
 
 import numpy as np
 
-KIND = {"R": 1, "C": 2, "L": 3, "V": 4, "I": 5, "D": 6, "Q": 7, "M": 8}
+KIND = {"R": 1, "C": 2, "L": 3, "V": 4, "I": 5, "D": 6, "Q": 7, "M": 8, "E": 9, "F": 10, "G": 11, "H": 12,
+        "K": 13}
 WAVE = {None: 0, "pulse": 1, "sin": 2, "exp": 3, "pwl": 4}
 
 F_HAS_DC, F_HAS_IC, F_HAS_BV, F_PTYPE = 1, 2, 4, 8
@@ -51,7 +52,7 @@ class CircuitError(ValueError):
 
 class Element:
     __slots__ = ("name", "kind", "nodes", "value", "ic", "has_ic", "dc", "has_dc", "wave", "args",
-                 "ac", "model", "area", "params")
+                 "ac", "model", "area", "params", "ctrl", "couples")
 
     def __init__(self, name, kind, nodes, **kw):
         self.name, self.kind, self.nodes = name, kind, list(nodes)
@@ -62,6 +63,8 @@ class Element:
         self.ac = list(kw.get("ac", [0.0, 0.0]))
         self.model, self.area = kw.get("model"), kw.get("area", 0.0)
         self.params = dict(kw.get("params") or {})
+        self.ctrl = kw.get("ctrl")            # F, H: the controlling voltage source's name
+        self.couples = kw.get("couples")      # K: the two inductors' names
 
 
 class Builder:
@@ -109,6 +112,26 @@ class Builder:
 
     def current_wave(self, name, plus, minus, wave, args):
         return self.current_source(name, plus, minus, 0.0, wave=wave, args=args, has_dc=False)
+
+    def vcvs(self, name, plus, minus, ctrl_plus, ctrl_minus, gain):
+        """E: V(n+) - V(n-) = gain (V(nc+) - V(nc-)) (device/controlled.go:15-23)."""
+        return self._add(Element(name, "E", [plus, minus, ctrl_plus, ctrl_minus], value=float(gain)))
+
+    def vccs(self, name, plus, minus, ctrl_plus, ctrl_minus, gain):
+        """G: i(n+ -> n-) = gain (V(nc+) - V(nc-))."""
+        return self._add(Element(name, "G", [plus, minus, ctrl_plus, ctrl_minus], value=float(gain)))
+
+    def cccs(self, name, plus, minus, source, gain):
+        """F: i(n+ -> n-) = gain I(source), I positive into the source's n+ terminal."""
+        return self._add(Element(name, "F", [plus, minus], value=float(gain), ctrl=source))
+
+    def ccvs(self, name, plus, minus, source, gain):
+        """H: V(n+) - V(n-) = gain I(source)."""
+        return self._add(Element(name, "H", [plus, minus], value=float(gain), ctrl=source))
+
+    def mutual(self, name, inductor1, inductor2, k):
+        """K: mutual inductance k sqrt(L1 L2) between two inductors (device/mutual.go:15-29)."""
+        return self._add(Element(name, "K", [], value=float(k), couples=[inductor1, inductor2]))
 
     def model(self, name, typ, params):
         self.models[name.lower()] = (typ.lower(), {k.lower(): float(v) for k, v in params.items()})
@@ -158,11 +181,22 @@ class Circuit:
             nodes = [self.node_index(n) for n in e.nodes]
             if any(n < 0 for n in nodes):
                 raise CircuitError("%s: unknown node" % e.name)
+            if e.kind in ("F", "H"):  # node[2]: the controlling source, by element index
+                j = self.element_index(e.ctrl)
+                if j < 0:
+                    raise CircuitError("%s: controlling source %s not found" % (e.name, e.ctrl))
+                nodes = nodes[:2] + [j]
+            elif e.kind == "K":  # node[0..1]: the coupled inductors, by element index
+                nodes = [self.element_index(x) for x in e.couples]
+                if any(n < 0 for n in nodes):
+                    raise CircuitError("%s: inductor not found" % e.name)
             nn = nodes + [0] * (4 - len(nodes))
             r["node"] = nn
             r["param"] = len(vals)
             flags = 0
-            if e.kind in ("R", "C", "L"):
+            if e.kind in ("E", "F", "G", "H", "K"):
+                vals += [e.value]
+            elif e.kind in ("R", "C", "L"):
                 if e.kind != "R" and e.has_ic:
                     flags |= F_HAS_IC
                 vals += [e.value, e.ic]
@@ -323,6 +357,14 @@ def from_dict(d):
         elif k == "M":
             n = e["nodes"]
             b.mosfet(e["name"], n[0], n[1], n[2], n[3], e["model"], e.get("params"))
+        elif k in ("E", "G"):
+            f = b.vcvs if k == "E" else b.vccs
+            f(e["name"], *e["nodes"], *e["ctrl_nodes"], e["value"])
+        elif k in ("F", "H"):
+            f = b.cccs if k == "F" else b.ccvs
+            f(e["name"], *e["nodes"], e["ctrl_source"], e["value"])
+        elif k == "K":
+            b.mutual(e["name"], e["couples"][0], e["couples"][1], e["value"])
     return b.build()
 
 

@@ -182,6 +182,29 @@ __global__ void __launch_bounds__(128) k_ac_model(KPlan plan, const double* __re
       case KS_ELEM_D: diode_ac(e, V, D, xv, y, gmin); break;
       case KS_ELEM_Q: bjt_ac(e, V, D, xv, y, gmin); break;
       case KS_ELEM_M: mos_ac(e, V, D, xv, y, gmin); break;
+      case KS_ELEM_E: case KS_ELEM_H: {                                          // device/controlled.go:144-148
+        const double g = V[e.param + KS_CTL_P_GAIN];
+        const int br_ = e.u[2];
+        y.add(a, br_, 1, 0); y.add(b, br_, -1, 0); y.add(br_, a, 1, 0); y.add(br_, b, -1, 0);
+        y.add(br_, e.u[3], -g, 0);
+        if (e.kind == KS_ELEM_E) y.add(br_, e.u[4], g, 0);
+        break;
+      }
+      case KS_ELEM_G: {
+        const double g = V[e.param + KS_CTL_P_GAIN];
+        y.add(a, e.u[3], g, 0); y.add(a, e.u[4], -g, 0); y.add(b, e.u[3], -g, 0); y.add(b, e.u[4], g, 0);
+        break;
+      }
+      case KS_ELEM_F: {
+        const double g = V[e.param + KS_CTL_P_GAIN];
+        y.add(a, e.u[3], g, 0); y.add(b, e.u[3], -g, 0);
+        break;
+      }
+      case KS_ELEM_K: {                                                          // device/mutual.go:146-151
+        const double m = D[e.derived + DK_M];
+        y.add(e.u[0], e.u[1], 0, -m); y.add(e.u[1], e.u[0], 0, -m);
+        break;
+      }
       default: break;
     }
   }

@@ -38,6 +38,11 @@ struct KElem {
 //   D       : u[0] = anode, u[1] = cathode, u[2] = internal anode ai (= u[0] without RS)
 //   Q       : u[0] = c, u[1] = e, u[2] = b, u[3] = s, u[4] = cp, u[5] = bp, u[6] = ep, u[7] = sa, u[8] = sb
 //   M       : u[0] = d, u[1] = s, u[2] = g, u[3] = b, u[4] = dp, u[5] = sp
+//   E       : u[0] = n+, u[1] = n-, u[2] = branch, u[3] = nc+, u[4] = nc-
+//   G       : u[0] = n+, u[1] = n-, u[3] = nc+, u[4] = nc-
+//   F       : u[0] = n+, u[1] = n-, u[3] = the controlling source's branch
+//   H       : u[0] = n+, u[1] = n-, u[2] = branch, u[3] = the controlling source's branch
+//   K       : u[0], u[1] = the coupled inductors' branches, u[2], u[3] = their value blocks
 
 // Derived constants per kind (offsets within the element's derived block).
 enum { DR_G = 0, DR_N = 1 };
@@ -63,6 +68,8 @@ enum { H_T0 = 0, H_T1, H_T2, H_Q0, H_Q1, H_Q2, H_N, H_SIZE };
 enum { SC_GEQ = 0, SC_IHIST, SC_VPREV, SC_IPREV, SC_TRAN, SC_HIST, SC_N = SC_HIST + H_SIZE };
 enum { SL_VPREV = 0, SL_IPREV, SL_HIST, SL_N = SL_HIST + H_SIZE };
 enum { SV_VALUE = 0, SV_OVR, SV_OVRON, SV_N };
+enum { SK_I1PREV = 0, SK_I2PREV, SK_N };  // mutual inductance: the accepted branch currents
+enum { DK_M = 0, DK_N = 1 };              // mutual inductance M = k sqrt(L1 L2)
 enum { SD_VD = 0, SD_CD, SD_GD, SD_IQ, SD_GEQ, SD_QPREV, SD_IQPREV, SD_VDACC, SD_LIM, SD_TRAN,
        SD_HIST, SD_N = SD_HIST + H_SIZE };
 enum { SQ_VBE = 0, SQ_VBC, SQ_VBX, SQ_VCS,

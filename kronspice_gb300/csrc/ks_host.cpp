@@ -36,7 +36,10 @@ int plan_layout(const ks_topology* t, HostPlan* hp, std::string* err) {
     e.kind = s.kind; e.flags = s.flags; e.level = s.level; e.wave = s.wave;
     e.nargs = s.nargs; e.param = s.param; e.given = s.given;
     for (int i = 0; i < 10; i++) e.u[i] = -1;
+    // F, H: node[2] and K: node[0..1] index elements (linked below), not nodes
     for (int i = 0; i < 4; i++) {
+      const bool elem_ref = (s.kind == KS_ELEM_K && i < 2) || ((s.kind == KS_ELEM_F || s.kind == KS_ELEM_H) && i == 2);
+      if (elem_ref) continue;
       if (s.node[i] < 0 || s.node[i] >= t->n_nodes) {
         char buf[128];
         snprintf(buf, sizeof buf, "circuit: invalid element value: element %d has node index %d out of range", k, s.node[i]);
@@ -44,8 +47,9 @@ int plan_layout(const ks_topology* t, HostPlan* hp, std::string* err) {
         return KS_EINVAL;
       }
     }
+    const bool ctl = s.kind >= KS_ELEM_E && s.kind <= KS_ELEM_K;
     int need = s.kind == KS_ELEM_D ? KS_D_NP : s.kind == KS_ELEM_Q ? KS_Q_NP : s.kind == KS_ELEM_M ? KS_M_NP
-             : (s.kind == KS_ELEM_V || s.kind == KS_ELEM_I) ? KS_SRC_P_ARGS + s.nargs : KS_RCL_NP;
+             : (s.kind == KS_ELEM_V || s.kind == KS_ELEM_I) ? KS_SRC_P_ARGS + s.nargs : ctl ? KS_CTL_NP : KS_RCL_NP;
     if (s.nargs < 0 || s.nargs > 1 << 20 || s.param < 0 || (int64_t)s.param + need > t->n_values) {
       *err = "ks_topology: element value block outside the value vector";
       return KS_EINVAL;
@@ -89,9 +93,38 @@ int plan_layout(const ks_topology* t, HostPlan* hp, std::string* err) {
         nd += DM_N; ns += SM_N; hp->n_nonlin++; hp->n_reactive++;
         break;
       }
+      case KS_ELEM_E: case KS_ELEM_H:  // device/controlled.go:55-66: a voltage output has a branch
+        e.u[0] = u0; e.u[1] = u1; e.u[2] = alloc_branch();
+        if (s.kind == KS_ELEM_E) { e.u[3] = s.node[2] - 1; e.u[4] = s.node[3] - 1; }
+        break;
+      case KS_ELEM_G:
+        e.u[0] = u0; e.u[1] = u1; e.u[3] = s.node[2] - 1; e.u[4] = s.node[3] - 1;
+        break;
+      case KS_ELEM_F: e.u[0] = u0; e.u[1] = u1; break;
+      case KS_ELEM_K: nd += DK_N; ns += SK_N; hp->n_reactive++; break;
       default:
         *err = "device: unsupported element kind";
         return KS_EUNSUPPORTED;
+    }
+  }
+  // Link (device/controlled.go:69-80, device/mutual.go:54-70): the branches a
+  // CCCS / CCVS senses and a mutual inductance couples, once every branch exists
+  for (int k = 0; k < t->n_elem; k++) {
+    const ks_element& s = t->elem[k];
+    KElem& e = hp->elem[k];
+    auto branch_of = [&](int j, int want) -> int {
+      if (j < 0 || j >= t->n_elem || t->elem[j].kind != want) return -1;
+      return hp->elem[j].u[2];
+    };
+    if (s.kind == KS_ELEM_F || s.kind == KS_ELEM_H) {
+      e.u[3] = branch_of(s.node[2], KS_ELEM_V);
+      if (e.u[3] < 0) { *err = "device: unsupported element kind: controlling source not found"; return KS_EUNSUPPORTED; }
+    } else if (s.kind == KS_ELEM_K) {
+      e.u[0] = branch_of(s.node[0], KS_ELEM_L);
+      e.u[1] = branch_of(s.node[1], KS_ELEM_L);
+      if (e.u[0] < 0 || e.u[1] < 0) { *err = "device: unsupported element kind: inductor not found"; return KS_EUNSUPPORTED; }
+      e.u[2] = t->elem[s.node[0]].param;
+      e.u[3] = t->elem[s.node[1]].param;
     }
   }
   hp->n = next;
@@ -138,8 +171,29 @@ int validate(const ks_topology* t, const double* v, bool transient, std::string*
   if (!t || t->n_elem <= 0) { *err = "circuit: no elements"; return KS_EVALIDATE; }
   if (t->n_nodes > 100000 || t->n_elem > 1000000) { *err = "circuit: too many nodes or elements"; return KS_EVALIDATE; }
   bool groundUsed = false;
+  std::vector<std::pair<int, int>> coupled;  // validateMutual's pairs
   for (int k = 0; k < t->n_elem; k++) {
     const ks_element& e = t->elem[k];
+    if (e.kind == KS_ELEM_K) {  // validateMutual, circuit/circuit.go:807-831 (no nodes of its own)
+      const double kc = v[e.param + KS_K_P_COUPLING];
+      if (!(kc > 0 && kc <= 1)) {
+        char buf[128]; snprintf(buf, sizeof buf, "circuit: invalid element value: element %d: coupling coefficient %g must be in (0, 1]", k, kc);
+        *err = buf; return KS_EVALIDATE;
+      }
+      int a = e.node[0], b = e.node[1];
+      if (a == b) { *err = "circuit: invalid element value: a mutual inductance couples an inductor with itself"; return KS_EVALIDATE; }
+      for (int j : {a, b})
+        if (j < 0 || j >= t->n_elem || t->elem[j].kind != KS_ELEM_L) {
+          *err = "circuit: invalid element value: a mutual inductance couples an element that is not a linear inductor";
+          return KS_EVALIDATE;
+        }
+      if (a > b) std::swap(a, b);
+      for (auto& pr : coupled)
+        if (pr.first == a && pr.second == b) { *err = "circuit: invalid element value: the inductors are already coupled"; return KS_EVALIDATE; }
+      coupled.push_back({a, b});
+      if (!finite(kc)) { *err = "circuit: invalid element value: non-finite value"; return KS_EVALIDATE; }
+      continue;
+    }
     int nn = (e.kind == KS_ELEM_Q || e.kind == KS_ELEM_M) ? 4 : 2;
     for (int i = 0; i < nn; i++) {
       if (e.node[i] < 0 || e.node[i] >= t->n_nodes) { *err = "circuit: invalid element value: node index out of range"; return KS_EVALIDATE; }
@@ -175,6 +229,22 @@ int validate(const ks_topology* t, const double* v, bool transient, std::string*
         }
         break;
       }
+      case KS_ELEM_E: case KS_ELEM_G:  // validateControl, circuit/circuit.go:865-876
+        if (!finite(p[0])) { *err = "circuit: invalid element value: non-finite value"; return KS_EVALIDATE; }
+        for (int i = 2; i < 4; i++)
+          if (e.node[i] < 0 || e.node[i] >= t->n_nodes) { *err = "circuit: invalid element value: control node index out of range"; return KS_EVALIDATE; }
+        if (e.node[2] == e.node[3]) {
+          char buf[128]; snprintf(buf, sizeof buf, "circuit: invalid element value: element %d is controlled by a voltage that is always 0", k);
+          *err = buf; return KS_EVALIDATE;
+        }
+        break;
+      case KS_ELEM_F: case KS_ELEM_H:  // validateControl, :877-881
+        if (!finite(p[0])) { *err = "circuit: invalid element value: non-finite value"; return KS_EVALIDATE; }
+        if (e.node[2] < 0 || e.node[2] >= t->n_elem || t->elem[e.node[2]].kind != KS_ELEM_V) {
+          char buf[128]; snprintf(buf, sizeof buf, "circuit: invalid element value: element %d is controlled by an element that is not a voltage source", k);
+          *err = buf; return KS_EVALIDATE;
+        }
+        break;
       default: *err = "circuit: unknown element kind"; return KS_EVALIDATE;
     }
   }
@@ -189,7 +259,10 @@ int validate(const ks_topology* t, const double* v, bool transient, std::string*
   auto unite = [&](int a, int b) { a = find(a); b = find(b); if (a != b) parent[a] = b; };
   for (int k = 0; k < t->n_elem; k++) {
     const ks_element& e = t->elem[k];
-    if (e.kind == KS_ELEM_I || (e.kind == KS_ELEM_C && !transient)) continue;
+    // current sources, mutual inductances and controlled current outputs are no path
+    if (e.kind == KS_ELEM_I || e.kind == KS_ELEM_K || e.kind == KS_ELEM_F || e.kind == KS_ELEM_G ||
+        (e.kind == KS_ELEM_C && !transient))
+      continue;
     unite(e.node[0], e.node[1]);
     if (e.kind == KS_ELEM_M) unite(e.node[3], e.node[0]);
     if (e.kind == KS_ELEM_Q) unite(e.node[2], e.node[0]);

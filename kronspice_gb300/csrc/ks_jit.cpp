@@ -100,6 +100,13 @@ void stamp_pattern(const ksh::HostPlan& hp, std::vector<uint32_t>& m) {
       case KS_ELEM_D: block(u, 3); break;
       case KS_ELEM_Q: block(u, 9); break;
       case KS_ELEM_M: block(u, 6); break;
+      case KS_ELEM_E: case KS_ELEM_H:  // device/controlled.go:83-100
+        add(u[0], u[2]); add(u[1], u[2]); add(u[2], u[0]); add(u[2], u[1]); add(u[2], u[3]);
+        if (e.kind == KS_ELEM_E) add(u[2], u[4]);
+        break;
+      case KS_ELEM_G: add(u[0], u[3]); add(u[0], u[4]); add(u[1], u[3]); add(u[1], u[4]); break;
+      case KS_ELEM_F: add(u[0], u[3]); add(u[1], u[3]); break;
+      case KS_ELEM_K: add(u[0], u[1]); add(u[1], u[0]); break;  // device/mutual.go:110-113
       default: break;
     }
   }

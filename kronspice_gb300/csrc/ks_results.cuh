@@ -230,6 +230,23 @@ __device__ inline ElemOp elem_operating(const KElem& e, const Col& V, const Col&
       }
       break;
     }
+    case KS_ELEM_E: case KS_ELEM_F: case KS_ELEM_G: case KS_ELEM_H: {  // device/controlled.go:123-140
+      o.v = X(e.u[0]) - X(e.u[1]);
+      if (e.kind == KS_ELEM_E || e.kind == KS_ELEM_H) o.i = X(e.u[2]);
+      else {
+        const double ctl = e.kind == KS_ELEM_G ? X(e.u[3]) - X(e.u[4]) : X(e.u[3]);
+        o.i = V[p + KS_CTL_P_GAIN] * ctl;
+      }
+      o.p = o.v * o.i;
+      o.sup = -o.p;  // idealized: its power is model-supplied, it has no exterior port
+      o.thermal = false;
+      break;
+    }
+    case KS_ELEM_K: {  // device/mutual.go:120-133: no voltage, current or power of its own
+      if (energy) o.w = Dv[dd + DK_M] * X(e.u[0]) * X(e.u[1]);
+      o.stores = true;
+      break;
+    }
     default: break;
   }
   return o;
@@ -340,13 +357,15 @@ __device__ inline bool tran_point_results(Thr<SY, P>& t, TranLedger& L, const Lo
     }
     k++;
   });
-  t.prog.each([&](const KElem& e) {
-    if (e.kind != KS_ELEM_R) return;  // the only model supplier among the engine's elements
+  t.prog.each([&](const KElem& e) {  // the model suppliers: negative resistances, controlled sources
+    if (e.kind != KS_ELEM_R && !(e.kind >= KS_ELEM_E && e.kind <= KS_ELEM_H)) return;
     ElemOp r = elem_operating(e, t.V, t.D, state_col(t.Sb, e), t.s, o.gmin, false);
     a.supplied(r.sup);
   });
-  t.prog.each([&](const KElem& e) {
-    if (e.kind == KS_ELEM_R || e.kind == KS_ELEM_V || e.kind == KS_ELEM_I) return;
+  t.prog.each([&](const KElem& e) {  // the energy-storing elements
+    if (!(e.kind == KS_ELEM_C || e.kind == KS_ELEM_L || e.kind == KS_ELEM_D || e.kind == KS_ELEM_Q ||
+          e.kind == KS_ELEM_M || e.kind == KS_ELEM_K))
+      return;
     ElemOp r = elem_operating(e, t.V, t.D, state_col(t.Sb, e), t.s, o.gmin, true);
     a.storage(r.ps);
     stored += r.w;

@@ -141,6 +141,9 @@ __device__ inline void setup_elem(const KElem& e, const Col& V, const Col& D, do
       break;
     }
     case KS_ELEM_M: mos_derive(e, V, D); break;
+    case KS_ELEM_K:  // NewMutual, device/mutual.go:44-49: M = k sqrt(L1 L2)
+      D[d + DK_M] = V[p + KS_K_P_COUPLING] * sqrt(V[e.u[2] + KS_RCL_P_VALUE] * V[e.u[3] + KS_RCL_P_VALUE]);
+      break;
     default: break;
   }
 }
@@ -274,6 +277,33 @@ __device__ __forceinline__ void elem_load(const KElem& e, const Col& Vb, const C
     case KS_ELEM_D: diode_load(e, Vb, Db, S, sys, lp); break;
     case KS_ELEM_Q: bjt_load(e, Vb, Db, S, sys, lp); break;
     case KS_ELEM_M: mos_load(e, Vb, Db, S, sys, lp); break;
+    case KS_ELEM_E: case KS_ELEM_H: {  // device/controlled.go:83-100: the output branch row
+      const double g = Vb[e.param + KS_CTL_P_GAIN];
+      const int a = e.u[0], b = e.u[1], kk = e.u[2];
+      sadd(sys, a, kk, 1); sadd(sys, b, kk, -1); sadd(sys, kk, a, 1); sadd(sys, kk, b, -1);
+      if (e.kind == KS_ELEM_E) { sadd(sys, kk, e.u[3], -g); sadd(sys, kk, e.u[4], g); }
+      else sadd(sys, kk, e.u[3], -g);
+      break;
+    }
+    case KS_ELEM_G: {  // device/controlled.go:101-106
+      const double g = Vb[e.param + KS_CTL_P_GAIN];
+      sadd(sys, e.u[0], e.u[3], g); sadd(sys, e.u[0], e.u[4], -g);
+      sadd(sys, e.u[1], e.u[3], -g); sadd(sys, e.u[1], e.u[4], g);
+      break;
+    }
+    case KS_ELEM_F: {  // device/controlled.go:107-110
+      const double g = Vb[e.param + KS_CTL_P_GAIN];
+      sadd(sys, e.u[0], e.u[3], g); sadd(sys, e.u[1], e.u[3], -g);
+      break;
+    }
+    case KS_ELEM_K: {  // device/mutual.go:75-118 (no torsion terms): the coupling of a time step
+      if (lp.mode == ModeOP || lp.mode == ModeTranOP || lp.mode == ModeUICInit) break;
+      const double f = (lp.method == TRAP ? 2 : 1) * Db[e.derived + DK_M] * lp.rh;
+      const int k1 = e.u[0], k2 = e.u[1];
+      sadd(sys, k1, k2, -f); sadd(sys, k2, k1, -f);
+      srhs(sys, k1, -f * S[SK_I2PREV]); srhs(sys, k2, -f * S[SK_I1PREV]);
+      break;
+    }
   }
 }
 
@@ -579,6 +609,10 @@ __device__ __forceinline__ void elem_accept(const KElem& e, const Col& Vb, const
     case KS_ELEM_D: diode_accept(e, Vb, Db, S, s, t, mode); break;
     case KS_ELEM_Q: bjt_accept(e, Vb, Db, S, s, t, mode, gmin); break;
     case KS_ELEM_M: mos_accept(e, Vb, Db, S, s, t, mode); break;
+    case KS_ELEM_K:  // device/mutual.go:134-137
+      if (nonlinOnly) break;
+      S[SK_I1PREV] = xn_(s, e.u[0]); S[SK_I2PREV] = xn_(s, e.u[1]);
+      break;
   }
 }
 

@@ -94,6 +94,13 @@ void stamp_rows(const HostPlan& hp, const double* values, bool transient, std::v
         if (sp != us) g4(us, sp);
         break;
       }
+      case KS_ELEM_E: case KS_ELEM_H:  // device/controlled.go:83-100
+        add(u[0], u[2]); add(u[1], u[2]); add(u[2], u[0]); add(u[2], u[1]); add(u[2], u[3]);
+        if (e.kind == KS_ELEM_E) add(u[2], u[4]);
+        break;
+      case KS_ELEM_G: add(u[0], u[3]); add(u[0], u[4]); add(u[1], u[3]); add(u[1], u[4]); break;
+      case KS_ELEM_F: add(u[0], u[3]); add(u[1], u[3]); break;
+      case KS_ELEM_K: if (transient) { add(u[0], u[1]); add(u[1], u[0]); } break;  // device/mutual.go:75-118
       default: break;
     }
   }
@@ -208,6 +215,31 @@ int sparse_symbolic(const HostPlan& hp, const double* values, double h, SparseSy
         if (sp != us) cond(us, sp, 1.0);
         break;
       }
+      case KS_ELEM_E: case KS_ELEM_H: {  // the output branch row at its gain
+        const double g = values ? values[e.param + KS_CTL_P_GAIN] : 1.0;
+        madd(u[0], u[2], 1); madd(u[1], u[2], -1); madd(u[2], u[0], 1); madd(u[2], u[1], -1);
+        madd(u[2], u[3], -g);
+        if (e.kind == KS_ELEM_E) madd(u[2], u[4], g);
+        if (u[2] >= 0) branch[u[2]] = 1;
+        break;
+      }
+      case KS_ELEM_G: {
+        const double g = values ? values[e.param + KS_CTL_P_GAIN] : 1.0;
+        madd(u[0], u[3], g); madd(u[0], u[4], -g); madd(u[1], u[3], -g); madd(u[1], u[4], g);
+        break;
+      }
+      case KS_ELEM_F: {
+        const double g = values ? values[e.param + KS_CTL_P_GAIN] : 1.0;
+        madd(u[0], u[3], g); madd(u[1], u[3], -g);
+        break;
+      }
+      case KS_ELEM_K:  // the trapezoidal coupling 2M/h of a time step
+        if (h > 0 && values) {
+          const double m = values[e.param + KS_K_P_COUPLING] *
+                           std::sqrt(values[u[2] + KS_RCL_P_VALUE] * values[u[3] + KS_RCL_P_VALUE]);
+          madd(u[0], u[1], -2 * m / h); madd(u[1], u[0], -2 * m / h);
+        }
+        break;
       default: break;
     }
   }

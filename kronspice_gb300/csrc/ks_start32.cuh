@@ -330,7 +330,9 @@ __device__ __forceinline__ void mos_load32(const KElem& e, const Col32& V, const
 }
 
 // ---------------------------------------------------------------- element dispatch
-__device__ __forceinline__ bool elem_ok32(const KElem& e) { return e.kind != KS_ELEM_M || e.level == 1; }
+__device__ __forceinline__ bool elem_ok32(const KElem& e) {
+  return e.kind <= KS_ELEM_M && (e.kind != KS_ELEM_M || e.level == 1);
+}
 
 template <class SY>
 __device__ __forceinline__ void elem_load32(const KElem& e, const Col32& V, const Col32& D, const Col32& Sb, SY& s,

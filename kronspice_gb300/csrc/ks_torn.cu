@@ -1169,6 +1169,13 @@ void stamp_pattern(const ksh::HostPlan& hp, std::vector<std::vector<int>>& rows)
       case KS_ELEM_D: block(u, 3); break;
       case KS_ELEM_Q: block(u, 9); break;
       case KS_ELEM_M: block(u, 6); break;
+      case KS_ELEM_E: case KS_ELEM_H:  // device/controlled.go:83-100
+        add(u[0], u[2]); add(u[1], u[2]); add(u[2], u[0]); add(u[2], u[1]); add(u[2], u[3]);
+        if (e.kind == KS_ELEM_E) add(u[2], u[4]);
+        break;
+      case KS_ELEM_G: add(u[0], u[3]); add(u[0], u[4]); add(u[1], u[3]); add(u[1], u[4]); break;
+      case KS_ELEM_F: add(u[0], u[3]); add(u[1], u[3]); break;
+      case KS_ELEM_K: add(u[0], u[1]); add(u[1], u[0]); break;  // device/mutual.go:110-113
       default: break;
     }
   }
@@ -1289,12 +1296,13 @@ int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_t
     if (seen[e]) { *err = "kron: unsupported: element " + std::to_string(e) + " is torn twice"; return KS_EINVAL; }
     seen[e] = 1;
     const ks_element& el = hp.src[e];
-    if (el.kind == KS_ELEM_V || el.kind == KS_ELEM_L) {
+    if (el.kind == KS_ELEM_V || el.kind == KS_ELEM_L || el.kind == KS_ELEM_E || el.kind == KS_ELEM_F ||
+        el.kind == KS_ELEM_H || el.kind == KS_ELEM_K) {  // tearTerminals, kron/jacobian.go:143-147
       *err = "kron: unsupported: tearing element " + std::to_string(e) +
              ": its coupling runs through a branch-current unknown; tear a neighbouring element";
       return KS_EINVAL;
     }
-    const int nn = el.kind == KS_ELEM_Q || el.kind == KS_ELEM_M ? 4 : 2;
+    const int nn = el.kind == KS_ELEM_Q || el.kind == KS_ELEM_M || el.kind == KS_ELEM_G ? 4 : 2;
     std::vector<int> terms;
     for (int a = 0; a < nn; a++)
       if (el.node[a] != 0 && std::find(terms.begin(), terms.end(), el.node[a]) == terms.end()) terms.push_back(el.node[a]);

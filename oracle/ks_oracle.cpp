@@ -120,6 +120,23 @@ struct Sim {
           if (m->bad) { delete m; msg = "device: unsupported element kind: MOSFET parameters"; return E_BAD; }
           d = m; break;
         }
+        case KS_ELEM_E: case KS_ELEM_F: case KS_ELEM_G: case KS_ELEM_H: {
+          auto* c = new Controlled(el.kind, p[KS_CTL_P_GAIN]);
+          c->nodes[0] = el.node[0]; c->nodes[1] = el.node[1];
+          if (el.kind == KS_ELEM_E || el.kind == KS_ELEM_G) { c->cn[0] = el.node[2]; c->cn[1] = el.node[3]; }
+          else c->ctrlElem = el.node[2];
+          d = c; break;
+        }
+        case KS_ELEM_K: {
+          if (el.node[0] < 0 || el.node[0] >= t->n_elem || el.node[1] < 0 || el.node[1] >= t->n_elem ||
+              t->elem[el.node[0]].kind != KS_ELEM_L || t->elem[el.node[1]].kind != KS_ELEM_L) {
+            msg = "device: unsupported element kind: inductor not found"; return E_BAD;
+          }
+          const double l1 = v[t->elem[el.node[0]].param + KS_RCL_P_VALUE], l2 = v[t->elem[el.node[1]].param + KS_RCL_P_VALUE];
+          auto* m = new Mutual(p[KS_K_P_COUPLING], l1, l2);
+          m->l[0] = el.node[0]; m->l[1] = el.node[1];
+          d = m; break;
+        }
         default: msg = "device: unsupported element kind"; return E_BAD;
       }
       devs.emplace_back(d);
@@ -131,6 +148,22 @@ struct Sim {
       if (devs[i]->reactive()) reactive.push_back((int)i);
       if (devs[i]->nonlinear()) nonlin.push_back((int)i);
       if (devs[i]->breakpointer()) breakp.push_back((int)i);
+    }
+    // Link, device/controlled.go:69-80 and device/mutual.go:54-70: the branches
+    // a CCCS / CCVS senses and a mutual inductance couples
+    for (size_t i = 0; i < devs.size(); i++) {
+      if (auto* c = dynamic_cast<Controlled*>(devs[i].get())) {
+        if (c->ctrlElem >= 0) {
+          auto* vs = c->ctrlElem < (int)devs.size() ? dynamic_cast<VSource*>(devs[c->ctrlElem].get()) : nullptr;
+          if (!vs) { msg = "device: unsupported element kind: controlling source not found"; return E_BAD; }
+          c->ck = vs->branch;
+        }
+      } else if (auto* m = dynamic_cast<Mutual*>(devs[i].get())) {
+        auto* a = dynamic_cast<Inductor*>(devs[m->l[0]].get());
+        auto* b = dynamic_cast<Inductor*>(devs[m->l[1]].get());
+        if (!a || !b) { msg = "device: unsupported element kind: inductor not found"; return E_BAD; }
+        m->k1 = a->branch; m->k2 = b->branch;
+      }
     }
     n = sc.size();
     for (auto& d : devs) d->n = n;
@@ -794,12 +827,13 @@ extern "C" int kso_torn_cuts(const ks_topology* t, const int32_t* elems, int n_e
     if (seen[e]) { copyMsg(std::string("kron: unsupported: ") + name + " is torn twice", err, errlen); return KS_EINVAL; }
     seen[e] = 1;
     const ks_element& el = t->elem[e];
-    if (el.kind == KS_ELEM_V || el.kind == KS_ELEM_L) {
+    if (el.kind == KS_ELEM_V || el.kind == KS_ELEM_L || el.kind == KS_ELEM_E || el.kind == KS_ELEM_F ||
+        el.kind == KS_ELEM_H || el.kind == KS_ELEM_K) {  // tearTerminals, kron/jacobian.go:143-147
       copyMsg(std::string("kron: unsupported: tearing ") + name +
               ": its coupling runs through a branch-current unknown; tear a neighbouring element", err, errlen);
       return KS_EINVAL;
     }
-    int nn = el.kind == KS_ELEM_Q || el.kind == KS_ELEM_M ? 4 : 2;
+    int nn = el.kind == KS_ELEM_Q || el.kind == KS_ELEM_M || el.kind == KS_ELEM_G ? 4 : 2;  // a VCCS: its control nodes too
     std::vector<int> terms;
     for (int a = 0; a < nn; a++) {
       int node = el.node[a];

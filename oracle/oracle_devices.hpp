@@ -472,6 +472,78 @@ struct ISource : TwoTerm {  // device/source.go:131-177
   void clearDCOverride() override { src.overridden = false; }
 };
 
+// Controlled, device/controlled.go:29-162: E (VCVS), F (CCCS), G (VCCS), H (CCVS).
+struct Controlled : TwoTerm {
+  int kind;
+  double gain;
+  int cn[2] = {0, 0}, cu[2] = {-1, -1};  // control nodes and their unknowns (E, G)
+  int ctrlElem = -1, ck = -1;            // controlling voltage source and its branch (F, H)
+  int branch = -1;                       // own branch (E, H)
+  Controlled(int k, double g) : kind(k), gain(g) {}
+  bool voltageOutput() const { return kind == KS_ELEM_E || kind == KS_ELEM_H; }
+  bool voltageControlled() const { return kind == KS_ELEM_E || kind == KS_ELEM_G; }
+  void setup(SetupCtx& c) override {  // :55-66
+    setupNodes(c);
+    if (voltageControlled()) { cu[0] = c.unknown(cn[0]); cu[1] = c.unknown(cn[1]); }
+    if (voltageOutput()) branch = c.allocBranch();
+  }
+  template <class ADD>
+  void stamp(ADD add) const {  // :83-110
+    const int p = u[0], nn = u[1];
+    if (voltageOutput()) {
+      const int k = branch;
+      add(p, k, 1); add(nn, k, -1); add(k, p, 1); add(k, nn, -1);
+      if (kind == KS_ELEM_E) { add(k, cu[0], -gain); add(k, cu[1], gain); }
+      else add(k, ck, -gain);
+      return;
+    }
+    if (kind == KS_ELEM_G) { add(p, cu[0], gain); add(p, cu[1], -gain); add(nn, cu[0], -gain); add(nn, cu[1], gain); }
+    else { add(p, ck, gain); add(nn, ck, -gain); }
+  }
+  void load(LoadCtx& c) override { stamp([&](int i, int j, double v) { c.M->add(i, j, v); }); }
+  void loadAC(ACCtx& c) override { stamp([&](int i, int j, double v) { c.add(i, j, v); }); }  // :143-148
+  double control(const double* x) const {
+    return voltageControlled() ? at(x, n, cu[0]) - at(x, n, cu[1]) : at(x, n, ck);
+  }
+  double current(const double* x) override { return voltageOutput() ? at(x, n, branch) : gain * control(x); }
+  OpPt operating(const double* x) override {  // :123-140: model-supplied, no exterior port
+    OpPt o;
+    o.v = voltage(x); o.i = current(x); o.p = o.v * o.i; o.sup = -o.p; o.ch = CH_ELECTRICAL;
+    return o;
+  }
+};
+
+// Mutual, device/mutual.go:30-157 (no torsion terms): M = k sqrt(L1 L2) between
+// the branch rows of two inductors.
+struct Mutual : Device {
+  double k, m;
+  int l[2] = {-1, -1};  // the inductors' element indices
+  int k1 = -1, k2 = -1;
+  double i1Prev = 0, i2Prev = 0;
+  Mutual(double kc, double l1, double l2) : k(kc), m(kc * std::sqrt(l1 * l2)) {}
+  void setup(SetupCtx&) override {}
+  bool reactive() const override { return true; }
+  void load(LoadCtx& c) override {  // :75-118
+    if (c.mode == ModeOP || c.mode == ModeTranOP || c.mode == ModeUICInit) return;
+    double f = m / c.h;
+    if (c.method == TRAP) f = 2 * m / c.h;
+    c.M->add(k1, k2, -f); c.M->add(k2, k1, -f);
+    c.addRHS(k1, -f * i2Prev); c.addRHS(k2, -f * i1Prev);
+  }
+  double current(const double*) override { return 0; }
+  OpPt operating(const double* x) override {  // :120-133, StoredEnergy :137
+    OpPt o;
+    o.w = m * at(x, n, k1) * at(x, n, k2);
+    o.stores = true;
+    return o;
+  }
+  void accept(const double* x, double, int) override { i1Prev = at(x, n, k1); i2Prev = at(x, n, k2); }  // :134-137
+  void loadAC(ACCtx& c) override {  // :146-151
+    c.add(k1, k2, std::complex<double>(0, -c.omega * m));
+    c.add(k2, k1, std::complex<double>(0, -c.omega * m));
+  }
+};
+
 // Diode, device/diode.go:61-397.
 struct Diode : TwoTerm {
   double IS, N, RS, CJO, VJ, M, TT, BV, IBV, FC; bool hasBV;

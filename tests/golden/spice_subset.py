@@ -1,7 +1,7 @@
 """Minimal SPICE netlist reader for the golden fixtures (test infrastructure).
 
 Reads the subset of SPICE the reference's golden netlists use for the element
-kinds of the engine (R, C, L, V, I, D, Q, M; .model, .op, .dc, .tran, .ac,
+kinds of the engine (R, C, L, V, I, D, Q, M, E, F, G, H, K; .model, .op, .dc, .tran, .ac,
 .param with {expression} / 'expression' values, .subckt with params and
 nesting, expanded into a flat circuit) into a plain dict: the same information
 circuit.FromDeck (circuit/builder.go:307) extracts from a parsed deck.
@@ -358,6 +358,14 @@ def _parse(text):
         elif kind == "m":
             ckt["elements"].append({"name": name, "kind": "M", "nodes": toks[1:5], "model": toks[5].lower(),
                                     "params": _params(toks[6:])})
+        elif kind in "eg":  # E/G n+ n- nc+ nc- gain
+            ckt["elements"].append({"name": name, "kind": kind.upper(), "nodes": toks[1:3], "ctrl_nodes": toks[3:5],
+                                    "value": value(toks[5])})
+        elif kind in "fh":  # F/H n+ n- vcontrol gain
+            ckt["elements"].append({"name": name, "kind": kind.upper(), "nodes": toks[1:3], "ctrl_source": toks[3],
+                                    "value": value(toks[4])})
+        elif kind == "k":  # K L1 L2 k
+            ckt["elements"].append({"name": name, "kind": "K", "couples": toks[1:3], "value": value(toks[3])})
         else:
             return None, "unsupported element " + name
     return ckt, None

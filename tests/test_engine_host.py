@@ -196,3 +196,15 @@ def test_torn_refusals_match_reference():
         with pytest.raises(RuntimeError) as e:
             analysis.TornBatch(el, nn, vals, bad)
         assert want in str(e.value), str(e.value)
+
+
+def test_validation_of_controlled_and_mutual():
+    """validateControl / validateMutual (circuit/circuit.go:807-881) on the host."""
+    b = kc.Builder("bad")
+    b.voltage_source("V1", "a", "0", 1).resistor("R1", "a", "0", 1e3)
+    b.vcvs("E1", "e", "0", "a", "a", 2.0).resistor("RE", "e", "0", 1e3)
+    assert analysis.validate(b.build()) is not None
+    b = kc.Builder("bad2")
+    b.voltage_source("V1", "a", "0", 1).inductor("L1", "a", "b", 1e-3).resistor("R1", "b", "0", 1)
+    b.inductor("L2", "c", "0", 1e-3).resistor("R2", "c", "0", 1).mutual("K1", "L1", "L2", 1.5)
+    assert analysis.validate(b.build()) is not None

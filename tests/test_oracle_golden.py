@@ -105,6 +105,6 @@ def test_oracle_matches_golden(case, src, backend):
 
 
 def test_in_scope_cases_are_many():
-    # 35 of the reference's 45 golden netlists use only the engine's element
+    # 38 of the reference's 45 golden netlists use only the engine's element
     # kinds and analyses (OP, DC sweep, transient, AC)
-    assert sum(1 for c in CASES if not c["skip"]) >= 35
+    assert sum(1 for c in CASES if not c["skip"]) >= 38
