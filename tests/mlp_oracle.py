@@ -33,6 +33,10 @@ def forward(params, X, round_bf16=False):
 
 
 def grad(p, shapes, X, T, round_bf16=False):
+    """Gradients of the loss.  round_bf16: the engine's storage precision, BF16
+    weights, inputs, activations and backward deltas (the loss gradient and each
+    ReLU-masked delta rounded to BF16 as the GEMM epilogues store them), every
+    product accumulated wide."""
     params = unpack(np.asarray(p, dtype=np.float64), shapes)
     if round_bf16:
         params = [(to_bf16(W), b) for W, b in params]
@@ -41,12 +45,16 @@ def grad(p, shapes, X, T, round_bf16=False):
     rows = X.shape[0]
     loss = np.sum((Y - T) ** 2) / rows
     d = 2 * (Y - T) / rows
+    if round_bf16:
+        d = to_bf16(d)
     grads = [None] * len(params)
     for l in range(len(params) - 1, -1, -1):
         W, b = params[l]
         grads[l] = (d.T @ acts[l], d.sum(0))
         if l > 0:
             d = (d @ W) * (acts[l] > 0)
+            if round_bf16:
+                d = to_bf16(d)
     flat = np.concatenate([np.concatenate([gW.ravel(), gb]) for gW, gb in grads])
     return flat, loss
 

@@ -46,7 +46,7 @@ def test_gpu_gradients_match_cpu_network():
             a, b = gg[k:k + size], gc[k:k + size]
             rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
             cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-30))
-            assert rel < 5e-2 and cos > 0.998, (o, i, size, rel, cos)
+            assert rel < 1e-2 and cos > 0.9999, (o, i, size, rel, cos)
             k += size
 
 
