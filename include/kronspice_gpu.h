@@ -74,7 +74,9 @@ typedef enum {
   KS_ELEM_F = 10, /* CCCS              device/controlled.go:29 */
   KS_ELEM_G = 11, /* VCCS              device/controlled.go:29 */
   KS_ELEM_H = 12, /* CCVS              device/controlled.go:29 */
-  KS_ELEM_K = 13  /* mutual inductance device/mutual.go:30     */
+  KS_ELEM_K = 13, /* mutual inductance device/mutual.go:30     */
+  KS_ELEM_S = 14, /* voltage-controlled switch device/switch.go:57 */
+  KS_ELEM_W = 15  /* current-controlled switch device/switch.go:57 */
 } ks_elem_kind;
 
 /* source waveforms (circuit/circuit.go WaveKind; device/waveform.go) */
@@ -116,6 +118,10 @@ enum {
  *                 branch current, positive into its n+ terminal)
  *   K           : node[0], node[1] = indices in elem[] of the two coupled
  *                 inductors (Element.Couples); no circuit nodes
+ *   S           : node[0] = n+, node[1] = n-, node[2] = nc+, node[3] = nc-
+ *                 (the controlling voltage, Element.CtrlNodes)
+ *   W           : node[0] = n+, node[1] = n-, node[2] = index in elem[] of
+ *                 the controlling voltage source (Element.CtrlSource)
  * param is the offset of the element's block in the per-circuit value vector;
  * the block layouts are the KS_*_P_* enums below.
  */
@@ -143,6 +149,10 @@ typedef struct {
 enum { KS_RCL_P_VALUE = 0, KS_RCL_P_IC = 1, KS_RCL_NP = 2 };
 /* E, F, G, H: [gain]   K: [coupling coefficient k] */
 enum { KS_CTL_P_GAIN = 0, KS_K_P_COUPLING = 0, KS_CTL_NP = 1 };
+/* S, W: [threshold VT (S, volts) or IT (W, amperes), hysteresis VH or IH
+ * (negative: the smooth switch), RON, ROFF, initial state (1 = ON, 0 = OFF)]:
+ * circuit.SwitchParams of circuit/switch.go:36-50 after defaults */
+enum { KS_SW_P_VT = 0, KS_SW_P_VH = 1, KS_SW_P_RON = 2, KS_SW_P_ROFF = 3, KS_SW_P_ON = 4, KS_SW_NP = 5 };
 /* V, I: [dc, ac_mag, ac_phase_deg, arg0 .. arg(nargs-1)] */
 enum { KS_SRC_P_DC = 0, KS_SRC_P_ACMAG = 1, KS_SRC_P_ACPHASE = 2, KS_SRC_P_ARGS = 3 };
 /* D: DiodeParams of device/diode.go:23 after defaults and area scaling */

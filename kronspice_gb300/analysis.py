@@ -516,7 +516,14 @@ class TornBatch:
 def validate(circuit, transient=False):
     """circuit.Validate: None or the typed validation error."""
     el, vals, _ = circuit.pack()
-    topo = _lib.KsTopology(circuit.n_nodes, len(el), len(vals), 0, el.ctypes.data)
+    return validate_packed(el, circuit.n_nodes, vals, transient)
+
+
+def validate_packed(el, n_nodes, vals, transient=False):
+    """circuit.Validate of a packed topology and value vector."""
+    el = np.ascontiguousarray(el)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    topo = _lib.KsTopology(n_nodes, len(el), len(vals), 0, el.ctypes.data)
     rc = _lib.load().ks_validate(ctypes.byref(topo), vals.ctypes.data, int(transient))
     if rc == 0:
         return None

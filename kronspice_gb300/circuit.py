@@ -16,7 +16,7 @@ import math
 import numpy as np
 
 KIND = {"R": 1, "C": 2, "L": 3, "V": 4, "I": 5, "D": 6, "Q": 7, "M": 8, "E": 9, "F": 10, "G": 11, "H": 12,
-        "K": 13}
+        "K": 13, "S": 14, "W": 15}
 WAVE = {None: 0, "pulse": 1, "sin": 2, "exp": 3, "pwl": 4}
 
 F_HAS_DC, F_HAS_IC, F_HAS_BV, F_PTYPE = 1, 2, 4, 8
@@ -63,7 +63,7 @@ class Element:
         self.ac = list(kw.get("ac", [0.0, 0.0]))
         self.model, self.area = kw.get("model"), kw.get("area", 0.0)
         self.params = dict(kw.get("params") or {})
-        self.ctrl = kw.get("ctrl")            # F, H: the controlling voltage source's name
+        self.ctrl = kw.get("ctrl")            # F, H, W: the controlling voltage source's name
         self.couples = kw.get("couples")      # K: the two inductors' names
 
 
@@ -133,6 +133,18 @@ class Builder:
         """K: mutual inductance k sqrt(L1 L2) between two inductors (device/mutual.go:15-29)."""
         return self._add(Element(name, "K", [], value=float(k), couples=[inductor1, inductor2]))
 
+    def vswitch(self, name, a, b, ctrl_plus, ctrl_minus, model, on=None):
+        """Voltage-controlled switch (SPICE S, circuit/switch.go:81-86) with a model
+        of type "sw"; on: the initial state (None: OFF, as when no IC is given)."""
+        return self._add(Element(name, "S", [a, b, ctrl_plus, ctrl_minus], model=model.lower(),
+                                 ic=1.0 if on else 0.0, has_ic=on is not None))
+
+    def iswitch(self, name, a, b, source, model, on=None):
+        """Current-controlled switch (SPICE W, circuit/switch.go:88-94) with a model
+        of type "csw", set by the current of voltage source `source`."""
+        return self._add(Element(name, "W", [a, b], model=model.lower(), ctrl=source,
+                                 ic=1.0 if on else 0.0, has_ic=on is not None))
+
     def model(self, name, typ, params):
         self.models[name.lower()] = (typ.lower(), {k.lower(): float(v) for k, v in params.items()})
         return self
@@ -181,7 +193,7 @@ class Circuit:
             nodes = [self.node_index(n) for n in e.nodes]
             if any(n < 0 for n in nodes):
                 raise CircuitError("%s: unknown node" % e.name)
-            if e.kind in ("F", "H"):  # node[2]: the controlling source, by element index
+            if e.kind in ("F", "H", "W"):  # node[2]: the controlling source, by element index
                 j = self.element_index(e.ctrl)
                 if j < 0:
                     raise CircuitError("%s: controlling source %s not found" % (e.name, e.ctrl))
@@ -196,6 +208,8 @@ class Circuit:
             flags = 0
             if e.kind in ("E", "F", "G", "H", "K"):
                 vals += [e.value]
+            elif e.kind in ("S", "W"):
+                vals += self._switch(e)
             elif e.kind in ("R", "C", "L"):
                 if e.kind != "R" and e.has_ic:
                     flags |= F_HAS_IC
@@ -248,6 +262,13 @@ class Circuit:
         if typ not in want:
             raise CircuitError("%s needs a %s model, %r is type %s" % (e.name, "/".join(want), e.model, typ))
         return typ, params
+
+    def _switch(self, e):
+        """[VT or IT, VH or IH, RON, ROFF, initial state]: circuit.SwitchParams
+        (circuit/switch.go:36-50) with the ngspice defaults RON = 1, ROFF = 1e12."""
+        typ, mp = self._model(e, ("sw",) if e.kind == "S" else ("csw",))
+        vt, vh = (mp.get("vt", 0.0), mp.get("vh", 0.0)) if typ == "sw" else (mp.get("it", 0.0), mp.get("ih", 0.0))
+        return [vt, vh, mp.get("ron", 1.0), mp.get("roff", 1e12), e.ic if e.has_ic else 0.0]
 
     def _diode(self, e):
         _, mp = self._model(e, ("d",))
@@ -365,6 +386,12 @@ def from_dict(d):
             f(e["name"], *e["nodes"], e["ctrl_source"], e["value"])
         elif k == "K":
             b.mutual(e["name"], e["couples"][0], e["couples"][1], e["value"])
+        elif k in ("S", "W"):
+            on = (e["ic"] == 1) if e.get("has_ic") else None
+            if k == "S":
+                b.vswitch(e["name"], *e["nodes"], *e["ctrl_nodes"], e["model"], on=on)
+            else:
+                b.iswitch(e["name"], *e["nodes"], e["ctrl_source"], e["model"], on=on)
     return b.build()
 
 

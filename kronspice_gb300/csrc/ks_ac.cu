@@ -140,9 +140,11 @@ __device__ void mos_ac(const KElem& e, const Col& V, const Col& D, const XView& 
 
 }  // namespace
 
-// G, C and b of every circuit at its operating point x [B][n].
+// G, C and b of every circuit at its operating point x [B][n] (a switch: the
+// linearization of the last load, in the device state).
 __global__ void __launch_bounds__(128) k_ac_model(KPlan plan, const double* __restrict__ values,
-                                                  const double* __restrict__ derived, int64_t B,
+                                                  const double* __restrict__ derived,
+                                                  const double* __restrict__ state, int64_t B,
                                                   const double* __restrict__ x, double gmin, double* G, double* C,
                                                   double* br, double* bi) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -203,6 +205,16 @@ __global__ void __launch_bounds__(128) k_ac_model(KPlan plan, const double* __re
       case KS_ELEM_K: {                                                          // device/mutual.go:146-151
         const double m = D[e.derived + DK_M];
         y.add(e.u[0], e.u[1], 0, -m); y.add(e.u[1], e.u[0], 0, -m);
+        break;
+      }
+      case KS_ELEM_S: case KS_ELEM_W: {                                          // device/switch.go:314-329
+        const Col S{const_cast<double*>(state) + c + (int64_t)e.state * B, B};
+        y.y(a, b, S[SW_G], 0);
+        const double k = S[SW_K];
+        if (D[e.derived + DW_SMOOTH] != 0 && k != 0) {
+          if (e.kind == KS_ELEM_W) { y.add(a, e.u[3], k, 0); y.add(b, e.u[3], -k, 0); }
+          else { y.add(a, e.u[3], k, 0); y.add(a, e.u[4], -k, 0); y.add(b, e.u[3], -k, 0); y.add(b, e.u[4], k, 0); }
+        }
         break;
       }
       default: break;
@@ -348,7 +360,8 @@ int ks_launch_ac(const KsDeviceBatch& b, double gmin, const double* x_op, const 
   double* C = G + (int64_t)n * n * B;
   double* br = C + (int64_t)n * n * B;
   double* bi = br + (int64_t)n * B;
-  k_ac_model<<<(unsigned)((B + 127) / 128), 128, 0, st>>>(b.plan, b.values, b.derived, B, x_op, gmin, G, C, br, bi);
+  k_ac_model<<<(unsigned)((B + 127) / 128), 128, 0, st>>>(b.plan, b.values, b.derived, b.state, B, x_op, gmin, G, C,
+                                                          br, bi);
   k_fill_i32<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(err_at, B, INT_MAX);
   int dev = 0, sms = 0, maxSmem = 0, per = 0;
   cudaGetDevice(&dev);

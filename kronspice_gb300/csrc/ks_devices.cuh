@@ -576,4 +576,110 @@ __device__ __forceinline__ void bjt_accept(const KElem& e, const Col& V, const C
   }
 }
 
+// ---------------------------------------------------------------- switch
+// device/switch.go:28-332: S (u[3], u[4] the control nodes) and W (u[3] the
+// controlling source's branch).  Abrupt: RON or ROFF with hysteresis about VT,
+// the state referred to the last accepted solution and held through a transient
+// step; smooth (VH < 0): ln R a cubic in the control between VT -+ |VH|.
+// The control at the new iterate xn (NEW) or at the load's linearization point xo.
+template <bool NEW = true, class SY>
+__device__ __forceinline__ double sw_control(const KElem& e, SY& sys) {  // :132-137
+  auto X = [&](int i) { return NEW ? xn_(sys, i) : xo_(sys, i); };
+  return e.kind == KS_ELEM_W ? X(e.u[3]) : X(e.u[3]) - X(e.u[4]);
+}
+
+__device__ __forceinline__ bool sw_next(const Col& V, const Col& Dv, const KElem& e, double c, bool prev) {  // :140-148
+  const double vt = V[e.param + KS_SW_P_VT], vh = Dv[e.derived + DW_VH];
+  if (c > vt + vh) return true;
+  if (c < vt - vh) return false;
+  return prev;
+}
+
+// smoothG, :151-162: the smooth switch's conductance and dg/dc at control c.
+__device__ __forceinline__ void sw_smooth_g(const Col& V, const Col& Dv, const KElem& e, double c, double* g, double* dg) {
+  const double vt = V[e.param + KS_SW_P_VT], vh = Dv[e.derived + DW_VH];
+  const double x = (c - vt) / vh;
+  if (x >= 1) { *g = 1 / V[e.param + KS_SW_P_RON]; *dg = 0; return; }
+  if (x <= -1) { *g = 1 / V[e.param + KS_SW_P_ROFF]; *dg = 0; return; }
+  const double lratio = Dv[e.derived + DW_LRATIO];
+  *g = exp(-(Dv[e.derived + DW_LMEAN] + lratio * (3 * x - x * x * x) / 4));
+  *dg = -*g * lratio * 3 * (1 - x * x) / (4 * vh);
+}
+
+// Load, :174-226.
+template <class SY>
+__device__ __forceinline__ void sw_load(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+                                        const LoadParams& lp) {
+  const int a = e.u[0], b = e.u[1];
+  double g;
+  if (Dv[e.derived + DW_SMOOTH] != 0) {
+    double c = sw_control<false>(e, sys), v = xo_(sys, a) - xo_(sys, b);
+    if (lp.initJct) {
+      const double vt = V[e.param + KS_SW_P_VT], vh = Dv[e.derived + DW_VH];
+      c = Dv[e.derived + DW_INIT] != 0 ? vt + vh : vt - vh;
+      v = 0;
+    }
+    double dg;
+    sw_smooth_g(V, Dv, e, c, &g, &dg);
+    const double k = dg * v;
+    S[SW_G] = g; S[SW_K] = k; S[SW_C0] = c;
+    sadd(sys, a, a, g); sadd(sys, b, b, g); sadd(sys, a, b, -g); sadd(sys, b, a, -g);
+    if (k != 0) {
+      if (e.kind == KS_ELEM_W) { sadd(sys, a, e.u[3], k); sadd(sys, b, e.u[3], -k); }
+      else { sadd(sys, a, e.u[3], k); sadd(sys, a, e.u[4], -k); sadd(sys, b, e.u[3], -k); sadd(sys, b, e.u[4], k); }
+      const double j0 = -k * c;
+      srhs(sys, a, -j0); srhs(sys, b, j0);
+    }
+    return;
+  }
+  const bool frozen = lp.mode == ModeTran;
+  const bool acc = S[SW_ACC] != 0;
+  const bool on = (lp.initJct || frozen) ? acc : sw_next(V, Dv, e, sw_control<false>(e, sys), acc);
+  g = on ? 1 / V[e.param + KS_SW_P_RON] : 1 / V[e.param + KS_SW_P_ROFF];
+  S[SW_FROZEN] = frozen; S[SW_ON] = on; S[SW_G] = g; S[SW_K] = 0;
+  sadd(sys, a, a, g); sadd(sys, b, b, g); sadd(sys, a, b, -g); sadd(sys, b, a, -g);
+}
+
+// ConvTest, :231-243.
+template <class SY>
+__device__ __forceinline__ bool sw_conv(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+                                        double reltol, double abstol) {
+  const double c = sw_control(e, sys);
+  if (Dv[e.derived + DW_SMOOTH] == 0)
+    return S[SW_FROZEN] != 0 || sw_next(V, Dv, e, c, S[SW_ACC] != 0) == (S[SW_ON] != 0);
+  const double v = xn_(sys, e.u[0]) - xn_(sys, e.u[1]);
+  double g, dg;
+  sw_smooth_g(V, Dv, e, c, &g, &dg);
+  const double ihat = S[SW_G] * v + S[SW_K] * (c - S[SW_C0]), i = g * v;
+  return fabs(ihat - i) <= reltol * fmax(fabs(i), fabs(ihat)) + abstol;
+}
+
+// Accept, :253-261.
+template <class SY>
+__device__ __forceinline__ void sw_accept(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys) {
+  const double c = sw_control(e, sys);
+  S[SW_CACC] = c; S[SW_ACCEPTED] = 1;
+  if (Dv[e.derived + DW_SMOOTH] == 0) {
+    const bool acc = S[SW_ACC] != 0, on = sw_next(V, Dv, e, c, acc);
+    S[SW_FLIP] = on != acc;
+    S[SW_ACC] = on; S[SW_ON] = on;
+  }
+}
+
+// LimitStep, :268-285: cut a transient step in which an abrupt switch changed
+// state to just past the crossing, unless it lies in the step's last hundredth.
+template <class SY>
+__device__ __forceinline__ double sw_limit_step(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+                                                double h) {
+  if (Dv[e.derived + DW_SMOOTH] != 0 || S[SW_ACCEPTED] == 0) return KS_INF;
+  const double c = sw_control(e, sys), cacc = S[SW_CACC];
+  const bool acc = S[SW_ACC] != 0;
+  if (sw_next(V, Dv, e, c, acc) == acc || c == cacc) return KS_INF;
+  const double vt = V[e.param + KS_SW_P_VT], vh = Dv[e.derived + DW_VH];
+  const double th = acc ? vt - vh : vt + vh;
+  const double frac = (th - cacc) / (c - cacc);
+  if (!(frac > 0) || frac >= 0.99) return KS_INF;
+  return h * fmin(frac + 0.005, 1.0);
+}
+
 }  // namespace ksg

@@ -43,6 +43,8 @@ struct KElem {
 //   F       : u[0] = n+, u[1] = n-, u[3] = the controlling source's branch
 //   H       : u[0] = n+, u[1] = n-, u[2] = branch, u[3] = the controlling source's branch
 //   K       : u[0], u[1] = the coupled inductors' branches, u[2], u[3] = their value blocks
+//   S       : u[0] = n+, u[1] = n-, u[3] = nc+, u[4] = nc-
+//   W       : u[0] = n+, u[1] = n-, u[3] = the controlling source's branch
 
 // Derived constants per kind (offsets within the element's derived block).
 enum { DR_G = 0, DR_N = 1 };
@@ -70,6 +72,12 @@ enum { SL_VPREV = 0, SL_IPREV, SL_HIST, SL_N = SL_HIST + H_SIZE };
 enum { SV_VALUE = 0, SV_OVR, SV_OVRON, SV_N };
 enum { SK_I1PREV = 0, SK_I2PREV, SK_N };  // mutual inductance: the accepted branch currents
 enum { DK_M = 0, DK_N = 1 };              // mutual inductance M = k sqrt(L1 L2)
+// switch: |VH|, smooth (VH < 0), ln sqrt(RON ROFF), ln(RON/ROFF), initial state ON
+enum { DW_VH = 0, DW_SMOOTH, DW_LMEAN, DW_LRATIO, DW_INIT, DW_N };
+// switch: stamped state, accepted state, a solution accepted, state held by the
+// last load (transient step), the last Accept changed the state, and the
+// linearization i = g v + k (c - c0) of the last load; the accepted control
+enum { SW_ON = 0, SW_ACC, SW_ACCEPTED, SW_FROZEN, SW_FLIP, SW_G, SW_K, SW_C0, SW_CACC, SW_N };
 enum { SD_VD = 0, SD_CD, SD_GD, SD_IQ, SD_GEQ, SD_QPREV, SD_IQPREV, SD_VDACC, SD_LIM, SD_TRAN,
        SD_HIST, SD_N = SD_HIST + H_SIZE };
 enum { SQ_VBE = 0, SQ_VBC, SQ_VBX, SQ_VCS,

@@ -38,7 +38,8 @@ int plan_layout(const ks_topology* t, HostPlan* hp, std::string* err) {
     for (int i = 0; i < 10; i++) e.u[i] = -1;
     // F, H: node[2] and K: node[0..1] index elements (linked below), not nodes
     for (int i = 0; i < 4; i++) {
-      const bool elem_ref = (s.kind == KS_ELEM_K && i < 2) || ((s.kind == KS_ELEM_F || s.kind == KS_ELEM_H) && i == 2);
+      const bool elem_ref = (s.kind == KS_ELEM_K && i < 2) ||
+                            ((s.kind == KS_ELEM_F || s.kind == KS_ELEM_H || s.kind == KS_ELEM_W) && i == 2);
       if (elem_ref) continue;
       if (s.node[i] < 0 || s.node[i] >= t->n_nodes) {
         char buf[128];
@@ -48,8 +49,10 @@ int plan_layout(const ks_topology* t, HostPlan* hp, std::string* err) {
       }
     }
     const bool ctl = s.kind >= KS_ELEM_E && s.kind <= KS_ELEM_K;
+    const bool sw = s.kind == KS_ELEM_S || s.kind == KS_ELEM_W;
     int need = s.kind == KS_ELEM_D ? KS_D_NP : s.kind == KS_ELEM_Q ? KS_Q_NP : s.kind == KS_ELEM_M ? KS_M_NP
-             : (s.kind == KS_ELEM_V || s.kind == KS_ELEM_I) ? KS_SRC_P_ARGS + s.nargs : ctl ? KS_CTL_NP : KS_RCL_NP;
+             : (s.kind == KS_ELEM_V || s.kind == KS_ELEM_I) ? KS_SRC_P_ARGS + s.nargs : ctl ? KS_CTL_NP
+             : sw ? KS_SW_NP : KS_RCL_NP;
     if (s.nargs < 0 || s.nargs > 1 << 20 || s.param < 0 || (int64_t)s.param + need > t->n_values) {
       *err = "ks_topology: element value block outside the value vector";
       return KS_EINVAL;
@@ -102,6 +105,11 @@ int plan_layout(const ks_topology* t, HostPlan* hp, std::string* err) {
         break;
       case KS_ELEM_F: e.u[0] = u0; e.u[1] = u1; break;
       case KS_ELEM_K: nd += DK_N; ns += SK_N; hp->n_reactive++; break;
+      case KS_ELEM_S: case KS_ELEM_W:  // device/switch.go:111-117: nonlinear (ConvTest), no branch
+        e.u[0] = u0; e.u[1] = u1;
+        if (s.kind == KS_ELEM_S) { e.u[3] = s.node[2] - 1; e.u[4] = s.node[3] - 1; }
+        nd += DW_N; ns += SW_N; hp->n_nonlin++;
+        break;
       default:
         *err = "device: unsupported element kind";
         return KS_EUNSUPPORTED;
@@ -116,7 +124,7 @@ int plan_layout(const ks_topology* t, HostPlan* hp, std::string* err) {
       if (j < 0 || j >= t->n_elem || t->elem[j].kind != want) return -1;
       return hp->elem[j].u[2];
     };
-    if (s.kind == KS_ELEM_F || s.kind == KS_ELEM_H) {
+    if (s.kind == KS_ELEM_F || s.kind == KS_ELEM_H || s.kind == KS_ELEM_W) {  // W: device/switch.go:120-130
       e.u[3] = branch_of(s.node[2], KS_ELEM_V);
       if (e.u[3] < 0) { *err = "device: unsupported element kind: controlling source not found"; return KS_EUNSUPPORTED; }
     } else if (s.kind == KS_ELEM_K) {
@@ -245,6 +253,32 @@ int validate(const ks_topology* t, const double* v, bool transient, std::string*
           *err = buf; return KS_EVALIDATE;
         }
         break;
+      case KS_ELEM_S: case KS_ELEM_W: {  // validateSwitch, circuit/switch.go:52-72
+        for (int i = 0; i < KS_SW_NP; i++)
+          if (!finite(p[i])) { *err = "circuit: invalid element value: non-finite value"; return KS_EVALIDATE; }
+        if (!(p[KS_SW_P_RON] > 0) || !(p[KS_SW_P_ROFF] > 0)) {  // swParams: ron, roff pos
+          *err = "circuit: bad model: switch RON and ROFF must be > 0"; return KS_EVALIDATE;
+        }
+        if (p[KS_SW_P_VH] < 0 && p[KS_SW_P_RON] == p[KS_SW_P_ROFF]) {
+          *err = "circuit: bad model: a smooth switch (negative hysteresis) needs RON != ROFF"; return KS_EVALIDATE;
+        }
+        if (p[KS_SW_P_ON] != 0 && p[KS_SW_P_ON] != 1) {
+          char buf[128]; snprintf(buf, sizeof buf, "circuit: invalid element value: element %d initial state must be ON (1) or OFF (0)", k);
+          *err = buf; return KS_EVALIDATE;
+        }
+        if (e.kind == KS_ELEM_S) {  // validateControl, circuit/circuit.go:865-876
+          for (int i = 2; i < 4; i++)
+            if (e.node[i] < 0 || e.node[i] >= t->n_nodes) { *err = "circuit: invalid element value: control node index out of range"; return KS_EVALIDATE; }
+          if (e.node[2] == e.node[3]) {
+            char buf[128]; snprintf(buf, sizeof buf, "circuit: invalid element value: element %d is controlled by a voltage that is always 0", k);
+            *err = buf; return KS_EVALIDATE;
+          }
+        } else if (e.node[2] < 0 || e.node[2] >= t->n_elem || t->elem[e.node[2]].kind != KS_ELEM_V) {  // :877-881
+          char buf[128]; snprintf(buf, sizeof buf, "circuit: invalid element value: element %d is controlled by an element that is not a voltage source", k);
+          *err = buf; return KS_EVALIDATE;
+        }
+        break;
+      }
       default: *err = "circuit: unknown element kind"; return KS_EVALIDATE;
     }
   }

@@ -107,6 +107,9 @@ void stamp_pattern(const ksh::HostPlan& hp, std::vector<uint32_t>& m) {
       case KS_ELEM_G: add(u[0], u[3]); add(u[0], u[4]); add(u[1], u[3]); add(u[1], u[4]); break;
       case KS_ELEM_F: add(u[0], u[3]); add(u[1], u[3]); break;
       case KS_ELEM_K: add(u[0], u[1]); add(u[1], u[0]); break;  // device/mutual.go:110-113
+      case KS_ELEM_S:  // device/switch.go:174-226 (the smooth switch's transconductance too)
+        block(u, 2); add(u[0], u[3]); add(u[0], u[4]); add(u[1], u[3]); add(u[1], u[4]); break;
+      case KS_ELEM_W: block(u, 2); add(u[0], u[3]); add(u[1], u[3]); break;
       default: break;
     }
   }

@@ -247,6 +247,13 @@ __device__ inline ElemOp elem_operating(const KElem& e, const Col& V, const Col&
       o.stores = true;
       break;
     }
+    case KS_ELEM_S: case KS_ELEM_W: {  // device/switch.go:246-250, ExteriorPower :304-310
+      o.v = X(e.u[0]) - X(e.u[1]);
+      o.i = S[SW_G] * o.v + S[SW_K] * (sw_control(e, s) - S[SW_C0]);  // the current the solve used
+      o.p = o.v * o.i;
+      o.ext = -o.p;  // Joule heat out through the thermal port
+      break;
+    }
     default: break;
   }
   return o;

@@ -144,6 +144,15 @@ __device__ inline void setup_elem(const KElem& e, const Col& V, const Col& D, do
     case KS_ELEM_K:  // NewMutual, device/mutual.go:44-49: M = k sqrt(L1 L2)
       D[d + DK_M] = V[p + KS_K_P_COUPLING] * sqrt(V[e.u[2] + KS_RCL_P_VALUE] * V[e.u[3] + KS_RCL_P_VALUE]);
       break;
+    case KS_ELEM_S: case KS_ELEM_W: {  // NewSwitch, device/switch.go:92-108
+      const double vh = V[p + KS_SW_P_VH], ron = V[p + KS_SW_P_RON], roff = V[p + KS_SW_P_ROFF];
+      D[d + DW_VH] = fabs(vh);
+      D[d + DW_SMOOTH] = vh < 0;
+      D[d + DW_LMEAN] = vh < 0 ? log(sqrt(ron * roff)) : 0.0;
+      D[d + DW_LRATIO] = vh < 0 ? log(ron / roff) : 0.0;
+      D[d + DW_INIT] = V[p + KS_SW_P_ON] == 1;
+      break;
+    }
     default: break;
   }
 }
@@ -304,6 +313,7 @@ __device__ __forceinline__ void elem_load(const KElem& e, const Col& Vb, const C
       srhs(sys, k1, -f * S[SK_I2PREV]); srhs(sys, k2, -f * S[SK_I1PREV]);
       break;
     }
+    case KS_ELEM_S: case KS_ELEM_W: sw_load(e, Vb, Db, S, sys, lp); break;
   }
 }
 
@@ -578,6 +588,7 @@ __device__ __forceinline__ bool converged(const P& prog, const Col& Vb, const Co
     if (e.kind == KS_ELEM_D) ok = diode_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
     else if (e.kind == KS_ELEM_Q) ok = bjt_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
     else if (e.kind == KS_ELEM_M) ok = mos_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
+    else if (e.kind == KS_ELEM_S || e.kind == KS_ELEM_W) ok = sw_conv(e, Vb, Db, S, s, o.reltol, o.abstol);
   });
   return prog_all(prog, ok);
 }
@@ -613,6 +624,7 @@ __device__ __forceinline__ void elem_accept(const KElem& e, const Col& Vb, const
       if (nonlinOnly) break;
       S[SK_I1PREV] = xn_(s, e.u[0]); S[SK_I2PREV] = xn_(s, e.u[1]);
       break;
+    case KS_ELEM_S: case KS_ELEM_W: sw_accept(e, Vb, Db, S, s); break;  // nonlinear: seeded by a NodeSet too
   }
 }
 
@@ -621,6 +633,7 @@ __device__ __forceinline__ void elem_accept(const KElem& e, const Col& Vb, const
 template <class SY>
 __device__ __forceinline__ bool elem_converged(const KElem& e, const Col& Vb, const Col& Db, const Col& Sb, SY& s,
                                                const KOpts& o, double gmin) {
+  if (e.kind == KS_ELEM_S || e.kind == KS_ELEM_W) return sw_conv(e, Vb, Db, state_col(Sb, e), s, o.reltol, o.abstol);
   const int ls = lim_slot(e.kind);
   if (ls < 0) return true;
   Col S = state_col(Sb, e);
@@ -639,13 +652,16 @@ __device__ __forceinline__ void accept_all(const P& prog, const Col& Vb, const C
 }
 
 // Fresh device state of one circuit (the zero state of newly built devices, with
-// each MOSFET's limiting threshold at VTO, device/mosfet.go:321).
+// each MOSFET's limiting threshold at VTO, device/mosfet.go:321, and each
+// switch in its initial state).
 template <class P>
 __device__ inline void init_state(const P& prog, const Col& Db, const Col& Sb) {
   for (int k = 0; k < prog.n_state; k++) Sb[k] = 0.0;
   prog_sync(prog);
   prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
     if (e.kind == KS_ELEM_M) Sb[e.state + SM_AVON] = Db[e.derived + DM_VTO];
+    if (e.kind == KS_ELEM_S || e.kind == KS_ELEM_W)  // the ON / OFF initial state, device/switch.go:105-106
+      Sb[e.state + SW_ON] = Sb[e.state + SW_ACC] = Db[e.derived + DW_INIT];
   });
   prog_sync(prog);
 }

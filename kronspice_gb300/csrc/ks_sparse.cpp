@@ -101,6 +101,16 @@ void stamp_rows(const HostPlan& hp, const double* values, bool transient, std::v
       case KS_ELEM_G: add(u[0], u[3]); add(u[0], u[4]); add(u[1], u[3]); add(u[1], u[4]); break;
       case KS_ELEM_F: add(u[0], u[3]); add(u[1], u[3]); break;
       case KS_ELEM_K: if (transient) { add(u[0], u[1]); add(u[1], u[0]); } break;  // device/mutual.go:75-118
+      case KS_ELEM_S: case KS_ELEM_W: {  // device/switch.go:174-226
+        g4(u[0], u[1]);
+        // a smooth switch stamps its transconductance while its control is inside the band
+        const bool smooth = values ? values[e.param + KS_SW_P_VH] < 0 : true;
+        if (smooth) {
+          if (e.kind == KS_ELEM_W) { add(u[0], u[3]); add(u[1], u[3]); }
+          else ctl(u[0], u[1], u[3], u[4]);
+        }
+        break;
+      }
       default: break;
     }
   }
@@ -233,6 +243,8 @@ int sparse_symbolic(const HostPlan& hp, const double* values, double h, SparseSy
         madd(u[0], u[3], g); madd(u[1], u[3], -g);
         break;
       }
+      // switches are left out like the junctions: RON and ROFF lie six to twelve
+      // decades apart, and which one a Newton iteration stamps is not known here
       case KS_ELEM_K:  // the trapezoidal coupling 2M/h of a time step
         if (h > 0 && values) {
           const double m = values[e.param + KS_K_P_COUPLING] *

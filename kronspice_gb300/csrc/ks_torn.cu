@@ -1176,6 +1176,10 @@ void stamp_pattern(const ksh::HostPlan& hp, std::vector<std::vector<int>>& rows)
       case KS_ELEM_G: add(u[0], u[3]); add(u[0], u[4]); add(u[1], u[3]); add(u[1], u[4]); break;
       case KS_ELEM_F: add(u[0], u[3]); add(u[1], u[3]); break;
       case KS_ELEM_K: add(u[0], u[1]); add(u[1], u[0]); break;  // device/mutual.go:110-113
+      // an abrupt switch's conductance (device/switch.go:204-211); the plan has no
+      // values, so a smooth switch's transconductance is not in it (the torn
+      // engine itself takes no switches)
+      case KS_ELEM_S: case KS_ELEM_W: block(u, 2); break;
       default: break;
     }
   }
@@ -1297,12 +1301,12 @@ int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_t
     seen[e] = 1;
     const ks_element& el = hp.src[e];
     if (el.kind == KS_ELEM_V || el.kind == KS_ELEM_L || el.kind == KS_ELEM_E || el.kind == KS_ELEM_F ||
-        el.kind == KS_ELEM_H || el.kind == KS_ELEM_K) {  // tearTerminals, kron/jacobian.go:143-147
+        el.kind == KS_ELEM_H || el.kind == KS_ELEM_K || el.kind == KS_ELEM_W) {  // tearTerminals, kron/jacobian.go:143-147
       *err = "kron: unsupported: tearing element " + std::to_string(e) +
              ": its coupling runs through a branch-current unknown; tear a neighbouring element";
       return KS_EINVAL;
     }
-    const int nn = el.kind == KS_ELEM_Q || el.kind == KS_ELEM_M || el.kind == KS_ELEM_G ? 4 : 2;
+    const int nn = el.kind == KS_ELEM_Q || el.kind == KS_ELEM_M || el.kind == KS_ELEM_G || el.kind == KS_ELEM_S ? 4 : 2;
     std::vector<int> terms;
     for (int a = 0; a < nn; a++)
       if (el.node[a] != 0 && std::find(terms.begin(), terms.end(), el.node[a]) == terms.end()) terms.push_back(el.node[a]);
@@ -1859,6 +1863,12 @@ extern "C" int ks_torn_create(const ks_topology* topo, int32_t n_variants, const
   std::string err;
   int rc = ksh::plan_layout(topo, &T->hp, &err);
   if (rc) { set_error(err); delete T; return rc; }
+  for (const KElem& e : T->hp.elem)
+    if (e.kind == KS_ELEM_S || e.kind == KS_ELEM_W) {  // no step limit or state restart in the torn transient
+      set_error("ks_torn_create: switches (S, W) are not supported by the torn engine");
+      delete T;
+      return KS_EUNSUPPORTED;
+    }
   T->V = n_variants;
   rc = build_plan(T, topo, torn_elems, n_torn, &err);
   if (rc) { set_error(err); delete T; return rc; }

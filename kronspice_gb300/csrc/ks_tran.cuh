@@ -79,10 +79,24 @@ __device__ __forceinline__ double truncate_all(Thr<SY, P>& t, const TruncParams&
         }
         break;
       }
+      case KS_ELEM_S: case KS_ELEM_W:  // the step limiters, analysis/tran.go:186-190
+        prop = fmin(prop, sw_limit_step(e, t.V, t.D, S, x, tc.h));
+        break;
       default: break;
     }
   });
   return prog_min(t.prog, prop);
+}
+
+// Restart of every step limiter, analysis/tran.go:213-217: true when the solution
+// just accepted changed a switch's state.
+template <class SY, class P>
+__device__ __forceinline__ bool switch_restart(Thr<SY, P>& t) {
+  bool r = false;
+  t.prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
+    if ((e.kind == KS_ELEM_S || e.kind == KS_ELEM_W) && state_col(t.Sb, e)[SW_FLIP] != 0) r = true;
+  });
+  return prog_any(t.prog, r);
 }
 
 // (*Sim).nextBreakpoint, analysis/tran.go:233-243.
@@ -322,6 +336,7 @@ __device__ __forceinline__ void tran_persistent(Thr<SY, P>& t, const TranSpecK& 
         if (!rejected) {
           accept_all(t.prog, t.V, t.D, t.Sb, t.s, tn, ModeTran, o.gmin, false);  // :200-208
           if (!sp.fixed || onGrid) record(t, sp, c, B, tn, kgrid, &npts, out_time, out_wave);
+          if (switch_restart(t)) hitBreak = true;  // :213-217: restart like a corner
         }
         if (unbalanced) { status = KS_STATUS_LEDGER; phase = TR_DONE; }
         else if (!rejected) {

@@ -77,7 +77,7 @@ struct Opts {  // analysis.Options with defaults, analysis/op.go:91-110
 
 struct Sim {
   std::vector<std::unique_ptr<Device>> devs;
-  std::vector<int> reactive, nonlin, breakp;
+  std::vector<int> reactive, nonlin, breakp, limiters;
   std::vector<char> isV;
   int n = 0, numNodes = 0;
   std::vector<double> x, xOld, rhs, ptPrev;
@@ -137,6 +137,13 @@ struct Sim {
           m->l[0] = el.node[0]; m->l[1] = el.node[1];
           d = m; break;
         }
+        case KS_ELEM_S: case KS_ELEM_W: {
+          auto* w = new Switch(el.kind == KS_ELEM_W, p);
+          w->nodes[0] = el.node[0]; w->nodes[1] = el.node[1];
+          if (el.kind == KS_ELEM_S) { w->cn[0] = el.node[2]; w->cn[1] = el.node[3]; }
+          else w->ctrlElem = el.node[2];
+          d = w; break;
+        }
         default: msg = "device: unsupported element kind"; return E_BAD;
       }
       devs.emplace_back(d);
@@ -148,6 +155,7 @@ struct Sim {
       if (devs[i]->reactive()) reactive.push_back((int)i);
       if (devs[i]->nonlinear()) nonlin.push_back((int)i);
       if (devs[i]->breakpointer()) breakp.push_back((int)i);
+      if (devs[i]->limiter()) limiters.push_back((int)i);
     }
     // Link, device/controlled.go:69-80 and device/mutual.go:54-70: the branches
     // a CCCS / CCVS senses and a mutual inductance couples
@@ -157,6 +165,12 @@ struct Sim {
           auto* vs = c->ctrlElem < (int)devs.size() ? dynamic_cast<VSource*>(devs[c->ctrlElem].get()) : nullptr;
           if (!vs) { msg = "device: unsupported element kind: controlling source not found"; return E_BAD; }
           c->ck = vs->branch;
+        }
+      } else if (auto* w = dynamic_cast<Switch*>(devs[i].get())) {  // Link, device/switch.go:120-130
+        if (w->currentCtl) {
+          auto* vs = w->ctrlElem >= 0 && w->ctrlElem < (int)devs.size() ? dynamic_cast<VSource*>(devs[w->ctrlElem].get()) : nullptr;
+          if (!vs) { msg = "device: unsupported element kind: controlling source not found"; return E_BAD; }
+          w->ck = vs->branch;
         }
       } else if (auto* m = dynamic_cast<Mutual*>(devs[i].get())) {
         auto* a = dynamic_cast<Inductor*>(devs[m->l[0]].get());
@@ -603,6 +617,7 @@ struct Sim {
       if (!fixed) {
         tc.time = tn; tc.h = h; tc.method = order;
         for (int i : reactive) proposal = std::min(proposal, devs[i]->truncate(x.data(), tc));
+        for (int i : limiters) proposal = std::min(proposal, devs[i]->limitStep(x.data(), tc));  // :186-190
         if (proposal < 0.9 * h) {
           h = std::max(proposal, h / 8);
           int r = reject(h);
@@ -626,6 +641,8 @@ struct Sim {
       double next = std::min(proposal, 2 * h);
       next = std::min(next, maxStep);
       order = method;
+      for (int i : limiters)  // :213-217: a switch changed state: restart like a corner
+        if (devs[i]->restart()) hitBreak = true;
       if (hitBreak) {
         order = BE;
         double nb2 = nextBreakpoint(t);
@@ -828,12 +845,13 @@ extern "C" int kso_torn_cuts(const ks_topology* t, const int32_t* elems, int n_e
     seen[e] = 1;
     const ks_element& el = t->elem[e];
     if (el.kind == KS_ELEM_V || el.kind == KS_ELEM_L || el.kind == KS_ELEM_E || el.kind == KS_ELEM_F ||
-        el.kind == KS_ELEM_H || el.kind == KS_ELEM_K) {  // tearTerminals, kron/jacobian.go:143-147
+        el.kind == KS_ELEM_H || el.kind == KS_ELEM_K || el.kind == KS_ELEM_W) {  // tearTerminals, kron/jacobian.go:143-147
       copyMsg(std::string("kron: unsupported: tearing ") + name +
               ": its coupling runs through a branch-current unknown; tear a neighbouring element", err, errlen);
       return KS_EINVAL;
     }
-    int nn = el.kind == KS_ELEM_Q || el.kind == KS_ELEM_M || el.kind == KS_ELEM_G ? 4 : 2;  // a VCCS: its control nodes too
+    // a VCCS and an S switch: their control nodes too (:160-163)
+    int nn = el.kind == KS_ELEM_Q || el.kind == KS_ELEM_M || el.kind == KS_ELEM_G || el.kind == KS_ELEM_S ? 4 : 2;
     std::vector<int> terms;
     for (int a = 0; a < nn; a++) {
       int node = el.node[a];

@@ -170,6 +170,10 @@ struct Device {
   virtual void setInitialCondition() {}
   virtual void setDCOverride(double v) {}
   virtual void clearDCOverride() {}
+  // device.StepLimiter (device/switch.go:14-26)
+  virtual bool limiter() const { return false; }
+  virtual double limitStep(const double* x, const TruncCtx& tc) { return kInf; }
+  virtual bool restart() const { return false; }
 };
 
 struct TwoTerm : Device {
@@ -541,6 +545,122 @@ struct Mutual : Device {
   void loadAC(ACCtx& c) override {  // :146-151
     c.add(k1, k2, std::complex<double>(0, -c.omega * m));
     c.add(k2, k1, std::complex<double>(0, -c.omega * m));
+  }
+};
+
+// Switch, device/switch.go:28-332: S (voltage-controlled) and W (current-
+// controlled).  Abrupt (VH >= 0): RON or ROFF with hysteresis about VT, the
+// state referred to the last accepted solution, held through a transient step;
+// smooth (VH < 0): ln R a cubic in the control between VT - |VH| and VT + |VH|.
+struct Switch : TwoTerm {
+  bool currentCtl;
+  int cn[2] = {0, 0}, cu[2] = {-1, -1};  // control nodes and their unknowns (S)
+  int ctrlElem = -1, ck = -1;            // controlling voltage source and its branch (W)
+  double vt, vh, ron, roff;
+  bool smooth = false;
+  double lmean = 0, lratio = 0;  // ln sqrt(RON ROFF), ln(RON / ROFF)
+  bool initOn, on, accOn, accepted = false, frozen = false, flipped = false;
+  double g = 0, k = 0, c0 = 0, cAcc = 0;  // linearization i = g v + k (c - c0)
+  Switch(bool cur, const double* p) : currentCtl(cur) {  // NewSwitch, :92-108
+    vt = p[KS_SW_P_VT]; vh = p[KS_SW_P_VH]; ron = p[KS_SW_P_RON]; roff = p[KS_SW_P_ROFF];
+    if (vh < 0) {
+      smooth = true;
+      vh = -vh;
+      lmean = std::log(std::sqrt(ron * roff));
+      lratio = std::log(ron / roff);
+    }
+    initOn = p[KS_SW_P_ON] == 1;
+    on = accOn = initOn;
+  }
+  void setup(SetupCtx& c) override {  // :111-117
+    setupNodes(c);
+    if (!currentCtl) { cu[0] = c.unknown(cn[0]); cu[1] = c.unknown(cn[1]); }
+  }
+  bool nonlinear() const override { return true; }
+  bool limiter() const override { return true; }
+  double control(const double* x) const {  // :132-137
+    return currentCtl ? at(x, n, ck) : at(x, n, cu[0]) - at(x, n, cu[1]);
+  }
+  bool next(double c, bool prev) const {  // :140-148
+    if (c > vt + vh) return true;
+    if (c < vt - vh) return false;
+    return prev;
+  }
+  void smoothG(double c, double* gg, double* dg) const {  // :151-162
+    double xx = (c - vt) / vh;
+    if (xx >= 1) { *gg = 1 / ron; *dg = 0; return; }
+    if (xx <= -1) { *gg = 1 / roff; *dg = 0; return; }
+    *gg = std::exp(-(lmean + lratio * (3 * xx - xx * xx * xx) / 4));
+    *dg = -*gg * lratio * 3 * (1 - xx * xx) / (4 * vh);
+  }
+  double vab(const double* x) const { return at(x, n, u[0]) - at(x, n, u[1]); }
+  template <class ADD>
+  void stampCtrl(ADD add, double kk) const {  // :214-226
+    const int a = u[0], b = u[1];
+    if (currentCtl) { add(a, ck, kk); add(b, ck, -kk); return; }
+    add(a, cu[0], kk); add(a, cu[1], -kk); add(b, cu[0], -kk); add(b, cu[1], kk);
+  }
+  void load(LoadCtx& c) override {  // :174-212
+    const int a = u[0], b = u[1];
+    if (smooth) {
+      double cc = control(c.X), v = vab(c.X);
+      if (c.initJct) { cc = initOn ? vt + vh : vt - vh; v = 0; }
+      double gg, dg;
+      smoothG(cc, &gg, &dg);
+      g = gg; k = dg * v; c0 = cc;
+      c.M->add(a, a, g); c.M->add(b, b, g); c.M->add(a, b, -g); c.M->add(b, a, -g);
+      if (k != 0) {
+        stampCtrl([&](int i, int j, double vv) { c.M->add(i, j, vv); }, k);
+        const double j0 = -k * cc;
+        c.addRHS(a, -j0); c.addRHS(b, j0);
+      }
+      return;
+    }
+    frozen = c.mode == ModeTran;
+    if (c.initJct || frozen) on = accOn;
+    else on = next(control(c.X), accOn);
+    g = on ? 1 / ron : 1 / roff;
+    k = 0;
+    c.M->add(a, a, g); c.M->add(b, b, g); c.M->add(a, b, -g); c.M->add(b, a, -g);
+  }
+  bool convTest(const double* x, double reltol, double abstol) override {  // :231-243
+    const double cc = control(x);
+    if (!smooth) return frozen || next(cc, accOn) == on;
+    const double v = vab(x);
+    double gg, dg;
+    smoothG(cc, &gg, &dg);
+    const double ihat = g * v + k * (cc - c0), i = gg * v;
+    return std::fabs(ihat - i) <= reltol * std::max(std::fabs(i), std::fabs(ihat)) + abstol;
+  }
+  double current(const double* x) override { return g * vab(x) + k * (control(x) - c0); }
+  OpPt operating(const double* x) override {  // :246-250, ExteriorPower :304-310
+    OpPt o;
+    o.v = vab(x); o.i = current(x); o.p = o.v * o.i;
+    o.ext = -o.p;  // Joule heat out through the thermal port
+    return o;
+  }
+  void accept(const double* x, double, int) override {  // :253-261
+    const double c = control(x);
+    cAcc = c; accepted = true;
+    if (!smooth) {
+      const bool o = next(c, accOn);
+      flipped = o != accOn;
+      accOn = on = o;
+    }
+  }
+  bool restart() const override { return flipped; }  // :264
+  double limitStep(const double* x, const TruncCtx& tc) override {  // :268-285
+    if (smooth || !accepted) return kInf;
+    const double c = control(x);
+    if (next(c, accOn) == accOn || c == cAcc) return kInf;
+    const double th = accOn ? vt - vh : vt + vh;
+    const double frac = (th - cAcc) / (c - cAcc);
+    if (!(frac > 0) || frac >= 0.99) return kInf;
+    return tc.h * std::min(frac + 0.005, 1.0);
+  }
+  void loadAC(ACCtx& c) override {  // :314-329
+    c.stampY(u[0], u[1], std::complex<double>(g, 0));
+    if (smooth && k != 0) stampCtrl([&](int i, int j, double v) { c.add(i, j, v); }, k);
   }
 };
 

@@ -1,7 +1,7 @@
 """Minimal SPICE netlist reader for the golden fixtures (test infrastructure).
 
 Reads the subset of SPICE the reference's golden netlists use for the element
-kinds of the engine (R, C, L, V, I, D, Q, M, E, F, G, H, K; .model, .op, .dc, .tran, .ac,
+kinds of the engine (R, C, L, V, I, D, Q, M, E, F, G, H, K, S, W; .model, .op, .dc, .tran, .ac,
 .param with {expression} / 'expression' values, .subckt with params and
 nesting, expanded into a flat circuit) into a plain dict: the same information
 circuit.FromDeck (circuit/builder.go:307) extracts from a parsed deck.
@@ -366,6 +366,21 @@ def _parse(text):
                                     "value": value(toks[4])})
         elif kind == "k":  # K L1 L2 k
             ckt["elements"].append({"name": name, "kind": "K", "couples": toks[1:3], "value": value(toks[3])})
+        elif kind in "sw":  # S n+ n- nc+ nc- model [ON|OFF]; W n+ n- vname model [ON|OFF] (netlist/parser.go:480-501)
+            t = toks[1:]
+            init = None
+            if t and t[-1].lower() in ("on", "off"):
+                init = t[-1].lower()
+                t = t[:-1]
+            if len(t) != (5 if kind == "s" else 4):
+                return None, "bad switch line " + name
+            e = {"name": name, "kind": kind.upper(), "nodes": t[0:2], "model": t[-1].lower(),
+                 "ic": 1.0 if init == "on" else 0.0, "has_ic": init is not None}
+            if kind == "s":
+                e["ctrl_nodes"] = t[2:4]
+            else:
+                e["ctrl_source"] = t[2]
+            ckt["elements"].append(e)
         else:
             return None, "unsupported element " + name
     return ckt, None

@@ -58,6 +58,12 @@ def cutoff_mosfets(ckt):
 def test_operating_point_order_matches_reference(case):
     ckt = kc.from_dict(case["circuit"])
     st, oorder, opat, q, prow, epat = both(ckt)
+    if case["name"] == "switch_relax_tran":
+        # a relaxation oscillator has no consistent switch state at DC: its
+        # operating point does not converge (device/switch.go:39-42); the golden
+        # transient starts from UIC
+        assert st == 3  # KS_STATUS_NO_CONVERGENCE
+        return
     assert st == 0
     # the minimum degree restatement itself, bit for bit, on the engine's pattern
     assert np.array_equal(orc.min_degree(epat), q)
