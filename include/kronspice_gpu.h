@@ -76,7 +76,9 @@ typedef enum {
   KS_ELEM_H = 12, /* CCVS              device/controlled.go:29 */
   KS_ELEM_K = 13, /* mutual inductance device/mutual.go:30     */
   KS_ELEM_S = 14, /* voltage-controlled switch device/switch.go:57 */
-  KS_ELEM_W = 15  /* current-controlled switch device/switch.go:57 */
+  KS_ELEM_W = 15, /* current-controlled switch device/switch.go:57 */
+  KS_ELEM_CN = 16, /* nonlinear / time-varying capacitor device/nonlinear_reactive.go:291 */
+  KS_ELEM_LN = 17  /* nonlinear / time-varying inductor  device/nonlinear_reactive.go:500 */
 } ks_elem_kind;
 
 /* source waveforms (circuit/circuit.go WaveKind; device/waveform.go) */
@@ -122,6 +124,10 @@ enum {
  *                 (the controlling voltage, Element.CtrlNodes)
  *   W           : node[0] = n+, node[1] = n-, node[2] = index in elem[] of
  *                 the controlling voltage source (Element.CtrlSource)
+ *   CN, LN      : node[0] = n+, node[1] = n-; wave = the SCALE waveform
+ *                 (KS_WAVE_NONE: s = 1), nargs = its arguments, level = the
+ *                 number of curve values (2 x knots of Q=pwl / FLUX=pwl;
+ *                 0: the linear law value * x)
  * param is the offset of the element's block in the per-circuit value vector;
  * the block layouts are the KS_*_P_* enums below.
  */
@@ -153,6 +159,11 @@ enum { KS_CTL_P_GAIN = 0, KS_K_P_COUPLING = 0, KS_CTL_NP = 1 };
  * (negative: the smooth switch), RON, ROFF, initial state (1 = ON, 0 = OFF)]:
  * circuit.SwitchParams of circuit/switch.go:36-50 after defaults */
 enum { KS_SW_P_VT = 0, KS_SW_P_VH = 1, KS_SW_P_RON = 2, KS_SW_P_ROFF = 3, KS_SW_P_ON = 4, KS_SW_NP = 5 };
+/* CN, LN: [value (C or L of the linear law, 0 with a curve), IC, SCALE
+ * arguments (nargs), curve x0, y0, x1, y1, ... (level values)]: the charge
+ * q = s(t) Q(v) or flux linkage s(t) L(i) of circuit.NonlinearCapacitor /
+ * NonlinearInductor (Element.Value, IC, Scale, Curve) */
+enum { KS_NL_P_VALUE = 0, KS_NL_P_IC = 1, KS_NL_P_ARGS = 2 };
 /* V, I: [dc, ac_mag, ac_phase_deg, arg0 .. arg(nargs-1)] */
 enum { KS_SRC_P_DC = 0, KS_SRC_P_ACMAG = 1, KS_SRC_P_ACPHASE = 2, KS_SRC_P_ARGS = 3 };
 /* D: DiodeParams of device/diode.go:23 after defaults and area scaling */

@@ -16,7 +16,7 @@ import math
 import numpy as np
 
 KIND = {"R": 1, "C": 2, "L": 3, "V": 4, "I": 5, "D": 6, "Q": 7, "M": 8, "E": 9, "F": 10, "G": 11, "H": 12,
-        "K": 13, "S": 14, "W": 15}
+        "K": 13, "S": 14, "W": 15, "CN": 16, "LN": 17}
 WAVE = {None: 0, "pulse": 1, "sin": 2, "exp": 3, "pwl": 4}
 
 F_HAS_DC, F_HAS_IC, F_HAS_BV, F_PTYPE = 1, 2, 4, 8
@@ -52,7 +52,7 @@ class CircuitError(ValueError):
 
 class Element:
     __slots__ = ("name", "kind", "nodes", "value", "ic", "has_ic", "dc", "has_dc", "wave", "args",
-                 "ac", "model", "area", "params", "ctrl", "couples")
+                 "ac", "model", "area", "params", "ctrl", "couples", "curve")
 
     def __init__(self, name, kind, nodes, **kw):
         self.name, self.kind, self.nodes = name, kind, list(nodes)
@@ -65,6 +65,7 @@ class Element:
         self.params = dict(kw.get("params") or {})
         self.ctrl = kw.get("ctrl")            # F, H, W: the controlling voltage source's name
         self.couples = kw.get("couples")      # K: the two inductors' names
+        self.curve = [float(v) for v in kw.get("curve") or []]  # CN, LN: Q=pwl / FLUX=pwl knots x0, y0, ...
 
 
 class Builder:
@@ -93,11 +94,19 @@ class Builder:
     def resistor(self, name, a, b, ohms):
         return self._add(Element(name, "R", [a, b], value=float(ohms)))
 
-    def capacitor(self, name, a, b, farads, ic=None):
-        return self._add(Element(name, "C", [a, b], value=float(farads), ic=ic or 0.0, has_ic=ic is not None))
+    def capacitor(self, name, a, b, farads, ic=None, curve=None, scale=None, scale_args=()):
+        """A capacitor; with a charge curve (Q=pwl, farads 0) or a SCALE waveform
+        it is circuit.NonlinearCapacitor, q = s(t) Q(v)."""
+        kind = "CN" if curve or scale else "C"
+        return self._add(Element(name, kind, [a, b], value=float(farads), ic=ic or 0.0, has_ic=ic is not None,
+                                 curve=curve, wave=scale, args=scale_args))
 
-    def inductor(self, name, a, b, henries, ic=None):
-        return self._add(Element(name, "L", [a, b], value=float(henries), ic=ic or 0.0, has_ic=ic is not None))
+    def inductor(self, name, a, b, henries, ic=None, curve=None, scale=None, scale_args=()):
+        """An inductor; with a flux curve (FLUX=pwl, henries 0) or a SCALE waveform
+        it is circuit.NonlinearInductor, flux linkage s(t) L(i)."""
+        kind = "LN" if curve or scale else "L"
+        return self._add(Element(name, kind, [a, b], value=float(henries), ic=ic or 0.0, has_ic=ic is not None,
+                                 curve=curve, wave=scale, args=scale_args))
 
     def voltage_source(self, name, plus, minus, volts, wave=None, args=(), has_dc=True, ac=(0.0, 0.0)):
         return self._add(Element(name, "V", [plus, minus], dc=float(volts), has_dc=has_dc, wave=wave,
@@ -210,6 +219,13 @@ class Circuit:
                 vals += [e.value]
             elif e.kind in ("S", "W"):
                 vals += self._switch(e)
+            elif e.kind in ("CN", "LN"):
+                if e.has_ic:
+                    flags |= F_HAS_IC
+                r["wave"] = WAVE[e.wave]
+                r["nargs"] = len(e.args)
+                r["level"] = len(e.curve)
+                vals += [e.value, e.ic] + [float(a) for a in e.args] + e.curve
             elif e.kind in ("R", "C", "L"):
                 if e.kind != "R" and e.has_ic:
                     flags |= F_HAS_IC
@@ -361,10 +377,12 @@ def from_dict(d):
         k = e["kind"]
         if k == "R":
             b.resistor(e["name"], *e["nodes"], e["value"])
-        elif k == "C":
-            b.capacitor(e["name"], *e["nodes"], e["value"], e.get("ic"))
-        elif k == "L":
-            b.inductor(e["name"], *e["nodes"], e["value"], e.get("ic"))
+        elif k in ("C", "CN"):
+            b.capacitor(e["name"], *e["nodes"], e["value"], e.get("ic"), curve=e.get("curve"),
+                        scale=e.get("scale"), scale_args=e.get("scale_args", ()))
+        elif k in ("L", "LN"):
+            b.inductor(e["name"], *e["nodes"], e["value"], e.get("ic"), curve=e.get("curve"),
+                       scale=e.get("scale"), scale_args=e.get("scale_args", ()))
         elif k in ("V", "I"):
             f = b.voltage_source if k == "V" else b.current_source
             f(e["name"], *e["nodes"], e["dc"], wave=e["wave"], args=e["args"], has_dc=e["has_dc"],

@@ -207,6 +207,20 @@ __global__ void __launch_bounds__(128) k_ac_model(KPlan plan, const double* __re
         y.add(e.u[0], e.u[1], 0, -m); y.add(e.u[1], e.u[0], 0, -m);
         break;
       }
+      case KS_ELEM_CN: case KS_ELEM_LN: {  // device/nonlinear_reactive.go:440-449, :640-651: s f'(x) at the accepted point
+        const Col S{const_cast<double*>(state) + c + (int64_t)e.state * B, B};
+        NlLaw law(e, V, D);
+        double y0, dy;
+        law.f(S[SN_XACC], &y0, &dy);
+        const double inc = S[SN_SACC] * dy;
+        if (e.kind == KS_ELEM_CN) y.y(a, b, 0, inc);
+        else {
+          const int br_ = e.u[2];
+          y.add(a, br_, 1, 0); y.add(b, br_, -1, 0); y.add(br_, a, 1, 0); y.add(br_, b, -1, 0);
+          y.add(br_, br_, 0, -inc);
+        }
+        break;
+      }
       case KS_ELEM_S: case KS_ELEM_W: {                                          // device/switch.go:314-329
         const Col S{const_cast<double*>(state) + c + (int64_t)e.state * B, B};
         y.y(a, b, S[SW_G], 0);

@@ -179,6 +179,46 @@ __device__ inline double wave_value(int kind, const Col& D, int d, const Col& V,
   return 0;
 }
 
+// wave.slope, device/waveform.go:131-186.
+__device__ inline double wave_slope(int kind, const Col& D, int d, const Col& V, int args, int nargs, double t) {
+  if (kind == KS_WAVE_PULSE) {
+    double v1 = D[d], v2 = D[d + 1], td = D[d + 2], tr = D[d + 3], tf = D[d + 4], pw = D[d + 5], per = D[d + 6];
+    if (t <= td) return 0;
+    double tt = t - td;
+    if (per > 0) {
+      tt = fmod(tt, per);
+      if (tt == 0) tt = per;  // the end of the previous period
+    }
+    if (tt <= tr) return (v2 - v1) / tr;
+    if (tt <= tr + pw) return 0;
+    if (tt <= tr + pw + tf) return (v1 - v2) / tf;
+    return 0;
+  }
+  if (kind == KS_WAVE_SIN) {
+    double va = D[d + 1], f = D[d + 2], td = D[d + 3], theta = D[d + 4], ph = D[d + 5] * kPi / 180;
+    if (t <= td) return 0;
+    double tt = t - td, om = 2 * kPi * f;
+    return va * exp(-tt * theta) * (om * cos(om * tt + ph) - theta * sin(om * tt + ph));
+  }
+  if (kind == KS_WAVE_EXP) {
+    double v1 = D[d], v2 = D[d + 1], td1 = D[d + 2], tau1 = D[d + 3], td2 = D[d + 4], tau2 = D[d + 5];
+    if (t <= td1) return 0;
+    double r = (v2 - v1) / tau1 * exp(-(t - td1) / tau1);
+    if (t > td2) r += (v1 - v2) / tau2 * exp(-(t - td2) / tau2);
+    return r;
+  }
+  if (kind == KS_WAVE_PWL) {
+    int n = nargs / 2;
+    if (t <= V[args] || t > V[args + 2 * (n - 1)]) return 0;
+    int k = 1;  // segment k-1 -> k ends at or after t
+    while (k < n && !(V[args + 2 * k] >= t)) k++;
+    double t0 = V[args + 2 * (k - 1)], v0 = V[args + 2 * (k - 1) + 1], t1 = V[args + 2 * k], v1 = V[args + 2 * k + 1];
+    if (t1 == t0) return 0;
+    return (v1 - v0) / (t1 - t0);
+  }
+  return 0;
+}
+
 // wave.nextBreakpoint, device/waveform.go:190-239.
 __device__ inline double wave_next_breakpoint(int kind, const Col& D, int d, const Col& V, int args, int nargs, double t) {
   const double rel = 1e-12;
@@ -680,6 +720,242 @@ __device__ __forceinline__ double sw_limit_step(const KElem& e, const Col& V, co
   const double frac = (th - cacc) / (c - cacc);
   if (!(frac > 0) || frac >= 0.99) return KS_INF;
   return h * fmin(frac + 0.005, 1.0);
+}
+
+// ---------------------------------------------------------------- nonlinear / time-varying C and L
+// stateLaw, device/nonlinear_reactive.go:15-249: y(x, t) = s(t) f(x), f the
+// element's piecewise-linear curve (knots x0, y0, x1, y1, ... after the SCALE
+// arguments in its value block) or value * x.
+struct NlLaw {
+  const Col& V;
+  const Col& D;
+  int c0, n, d;      // first curve value, knots, derived block
+  double lin;
+  int wave, args, nargs;
+  __device__ __forceinline__ NlLaw(const KElem& e, const Col& V_, const Col& D_)
+      : V(V_), D(D_), c0(e.param + KS_NL_P_ARGS + e.nargs), n(e.level / 2), d(e.derived),
+        lin(V_[e.param + KS_NL_P_VALUE]), wave(e.wave), args(e.param + KS_NL_P_ARGS), nargs(e.nargs) {}
+  __device__ __forceinline__ double xs(int k) const { return V[c0 + 2 * k]; }
+  __device__ __forceinline__ double ys(int k) const { return V[c0 + 2 * k + 1]; }
+  // the first knot >= x (sort.SearchFloat64s)
+  __device__ __forceinline__ int lower(double x) const {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (xs(mid) < x) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+  }
+  __device__ __forceinline__ int segment(double x) const {  // :93-104
+    const int k = lower(x);
+    return k <= 0 ? 1 : k >= n ? n - 1 : k;
+  }
+  __device__ __forceinline__ void f(double x, double* y, double* dy) const {  // :107-115
+    if (n == 0) { *y = lin * x; *dy = lin; return; }
+    const int k = segment(x);
+    const double g = (ys(k) - ys(k - 1)) / (xs(k) - xs(k - 1));
+    *y = ys(k - 1) + g * (x - xs(k - 1));
+    *dy = g;
+  }
+  __device__ __forceinline__ double cum(double x) const {  // :118-123
+    const int k = segment(x);
+    const double g = (ys(k) - ys(k - 1)) / (xs(k) - xs(k - 1));
+    const double dx = x - xs(k - 1);
+    return D[d + DN_PRE + k - 1] + ys(k - 1) * dx + 0.5 * g * dx * dx;
+  }
+  __device__ __forceinline__ double coenergy(double x) const {  // :126-131
+    return n == 0 ? 0.5 * lin * x * x : cum(x) - D[d + DN_G0];
+  }
+  __device__ __forceinline__ double energy(double x) const {  // :134-137
+    double y, dy;
+    f(x, &y, &dy);
+    return x * y - coenergy(x);
+  }
+  __device__ __forceinline__ double s(double t) const {
+    return wave == KS_WAVE_NONE ? 1.0 : wave_value(wave, D, d + DN_A0, V, args, nargs, t);
+  }
+  __device__ __forceinline__ double sdot(double t) const {
+    return wave == KS_WAVE_NONE ? 0.0 : wave_slope(wave, D, d + DN_A0, V, args, nargs, t);
+  }
+  __device__ __forceinline__ double limit(double x, double prev, bool* lim) const {  // :150-159
+    *lim = false;
+    const double ms = D[d + DN_MAXSTEP];
+    if (ms == 0 || fabs(x - prev) <= ms) return x;
+    const double lo = xs(0), hi = xs(n - 1);
+    if ((x <= lo && prev <= lo) || (x >= hi && prev >= hi)) return x;
+    *lim = true;
+    return prev + copysign(ms, x - prev);
+  }
+  __device__ __forceinline__ double knot_step(double x0, double x1, double h) const {  // :171-206
+    if (n == 0 || x0 == x1) return KS_INF;
+    int k = lower(x0);
+    double xk;
+    if (x1 > x0) {
+      while (k < n && xs(k) <= x0) k++;
+      if (k == n || xs(k) >= x1) return KS_INF;
+      xk = xs(k);
+    } else {
+      if (--k < 0 || xs(k) <= x1) return KS_INF;
+      xk = xs(k);
+    }
+    double w = KS_INF;
+    if (k > 0) w = xs(k) - xs(k - 1);
+    if (k < n - 1) w = fmin(w, xs(k + 1) - xs(k));
+    if (fabs(xk - x0) <= 1e-3 * w) return KS_INF;
+    const double fr = (xk - x0) / (x1 - x0);
+    if (fr > 0.9) return KS_INF;
+    return fr * h;
+  }
+};
+
+// The per-circuit constants of the law (newStateLaw, :47-64): the integrals of
+// f from the first knot, and the Newton step limit.
+__device__ inline void nl_setup(const KElem& e, const Col& V, const Col& D, double step, double stop) {
+  const int d = e.derived;
+  if (e.wave != KS_WAVE_NONE) wave_resolve(e.wave, V, e.param + KS_NL_P_ARGS, e.nargs, D, d + DN_A0, step, stop);
+  const int c0 = e.param + KS_NL_P_ARGS + e.nargs, n = e.level / 2;
+  D[d + DN_G0] = 0; D[d + DN_MAXSTEP] = 0;
+  if (n < 2) return;
+  D[d + DN_PRE] = 0;
+  for (int k = 1; k < n; k++)
+    D[d + DN_PRE + k] = D[d + DN_PRE + k - 1] + 0.5 * (V[c0 + 2 * (k - 1) + 1] + V[c0 + 2 * k + 1]) * (V[c0 + 2 * k] - V[c0 + 2 * (k - 1)]);
+  const KElem& ee = e;
+  NlLaw law(ee, V, D);
+  D[d + DN_G0] = law.cum(0);
+  D[d + DN_MAXSTEP] = 4 * (V[c0 + 2 * (n - 1)] - V[c0]) / double(n - 1);
+}
+
+// NonlinearCapacitor.Load / NonlinearInductor.Load, :318-357 and :531-566.
+template <class SY>
+__device__ __forceinline__ void nl_load(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+                                        const LoadParams& lp) {
+  const int p = e.u[0], nn = e.u[1], k = e.u[2];
+  const bool ind = e.kind == KS_ELEM_LN;
+  S[SN_LIM] = 0; S[SN_T] = lp.time; S[SN_TRAN] = 0;
+  if (!ind) { S[SN_G] = 0; S[SN_Y0] = 0; }
+  if (ind) { sadd(sys, p, k, 1); sadd(sys, nn, k, -1); }
+  if (lp.mode == ModeOP || lp.mode == ModeTranOP) {
+    if (ind) { sadd(sys, k, p, 1); sadd(sys, k, nn, -1); }
+    return;
+  }
+  if (lp.mode == ModeUICInit) {
+    if (ind) { sadd(sys, k, k, 1); srhs(sys, k, S[SN_IPREV]); }
+    else {
+      const double g = 1e9, vp = S[SN_VPREV];  // uicConductance
+      sadd(sys, p, p, g); sadd(sys, nn, nn, g); sadd(sys, p, nn, -g); sadd(sys, nn, p, -g);
+      srhs(sys, p, g * vp); srhs(sys, nn, -g * vp);
+    }
+    return;
+  }
+  S[SN_TRAN] = 1;
+  NlLaw law(e, V, Dv);
+  bool lim;
+  const double xraw = ind ? xo_(sys, k) : xo_(sys, p) - xo_(sys, nn);
+  const double x = law.limit(xraw, S[SN_XITER], &lim);
+  S[SN_XITER] = x; S[SN_LIM] = lim; S[SN_X0] = x;
+  const double sn = law.s(lp.time);
+  S[SN_SN] = sn; S[SN_SDOT] = law.sdot(lp.time);
+  double a, b;
+  if (lp.method == TRAP) { a = 2 / lp.h; b = -2 * S[SN_QPREV] / lp.h - (ind ? S[SN_VPREV] : S[SN_IPREV]); }
+  else { a = 1 / lp.h; b = -S[SN_QPREV] / lp.h; }
+  S[SN_A] = a; S[SN_B] = b;
+  double y, dy;
+  law.f(x, &y, &dy);
+  if (ind) {
+    const double lam0 = sn * y, ld = sn * dy;
+    S[SN_Y0] = lam0; S[SN_G] = ld;
+    // V(n+) - V(n-) - a ld i = a (lam0 - ld i0) + b
+    sadd(sys, k, p, 1); sadd(sys, k, nn, -1); sadd(sys, k, k, -a * ld);
+    srhs(sys, k, a * (lam0 - ld * x) + b);
+  } else {
+    const double iq = a * sn * y + b, g = a * sn * dy;
+    S[SN_Y0] = iq; S[SN_G] = g;
+    sadd(sys, p, p, g); sadd(sys, nn, nn, g); sadd(sys, p, nn, -g); sadd(sys, nn, p, -g);
+    const double ieq = iq - g * x;
+    srhs(sys, p, -ieq); srhs(sys, nn, ieq);
+  }
+}
+
+// The element's current at the new iterate (the capacitor's linearized
+// companion current, the inductor's branch current).
+template <class SY>
+__device__ __forceinline__ double nl_current(const KElem& e, const Col& S, SY& sys) {
+  if (e.kind == KS_ELEM_LN) return xn_(sys, e.u[2]);
+  if (S[SN_TRAN] == 0) return 0.0;
+  return S[SN_Y0] + S[SN_G] * (xn_(sys, e.u[0]) - xn_(sys, e.u[1]) - S[SN_X0]);
+}
+
+// ConvTest of the curved elements, :458-468 and :672-682 (the inductor's
+// absolute tolerance is vntol's 1e-6).
+template <class SY>
+__device__ __forceinline__ bool nl_conv(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+                                        double reltol, double abstol) {
+  if (S[SN_TRAN] == 0 || e.level == 0) return true;
+  NlLaw law(e, V, Dv);
+  const double a = S[SN_A], b = S[SN_B], sn = S[SN_SN];
+  double y, dy;
+  if (e.kind == KS_ELEM_LN) {
+    const double i = xn_(sys, e.u[2]);
+    const double vhat = a * (S[SN_Y0] + S[SN_G] * (i - S[SN_X0])) + b;
+    law.f(i, &y, &dy);
+    const double v = a * sn * y + b;
+    return fabs(vhat - v) <= reltol * fmax(fabs(v), fabs(vhat)) + 1e-6;
+  }
+  const double v = xn_(sys, e.u[0]) - xn_(sys, e.u[1]);
+  const double ihat = S[SN_Y0] + S[SN_G] * (v - S[SN_X0]);
+  law.f(v, &y, &dy);
+  const double i = a * sn * y + b;
+  return fabs(ihat - i) <= reltol * fmax(fabs(i), fabs(ihat)) + abstol;
+}
+
+// Accept, :379-399 and :585-602.
+template <class SY>
+__device__ __forceinline__ void nl_accept(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+                                          double t, int mode) {
+  const bool ind = e.kind == KS_ELEM_LN;
+  double v = xn_(sys, e.u[0]) - xn_(sys, e.u[1]);
+  double x;
+  if (ind) {
+    double i = xn_(sys, e.u[2]);
+    if (mode == ModeUICInit) { i = S[SN_IPREV]; v = 0; hist_reset(S, SN_HIST); }
+    else if (mode == ModeOP || mode == ModeTranOP) { v = 0; hist_reset(S, SN_HIST); }
+    S[SN_IPREV] = i; S[SN_VPREV] = v;
+    x = i;
+  } else {
+    if (mode == ModeUICInit) { v = S[SN_VPREV]; S[SN_IPREV] = 0; hist_reset(S, SN_HIST); }
+    else if (mode == ModeOP || mode == ModeTranOP) { S[SN_IPREV] = 0; hist_reset(S, SN_HIST); }
+    else S[SN_IPREV] = S[SN_Y0] + S[SN_G] * (v - S[SN_X0]);
+    S[SN_VPREV] = v;
+    x = v;
+  }
+  S[SN_XITER] = x; S[SN_XACC] = x;
+  NlLaw law(e, V, Dv);
+  const double sa = law.s(t);
+  S[SN_SACC] = sa;
+  double y, dy;
+  law.f(x, &y, &dy);
+  S[SN_QPREV] = sa * y;
+  hist_push(S, SN_HIST, t, S[SN_QPREV]);
+  if (S[SN_KNOTT] != 0 && t >= S[SN_KNOTT]) S[SN_KNOTT] = 0;  // stateLaw.accepted, :222-226
+}
+
+// Truncate, :417-424 and :620-625: the LTE step of the charge (flux) history and
+// the landing of a crossed knot on a time point (registered as a breakpoint).
+template <class SY>
+__device__ __forceinline__ double nl_truncate(const KElem& e, const Col& V, const Col& Dv, const Col& S, SY& sys,
+                                              const TruncParams& tc) {
+  NlLaw law(e, V, Dv);
+  const bool ind = e.kind == KS_ELEM_LN;
+  const double v = xn_(sys, e.u[0]) - xn_(sys, e.u[1]);
+  const double i = nl_current(e, S, sys);
+  const double x = ind ? i : v;
+  double y, dy;
+  law.f(x, &y, &dy);
+  const double h = ind ? lte_step(S, SN_HIST, law.s(tc.time) * y, v, S[SN_VPREV], tc.vntol, tc)
+                       : lte_step(S, SN_HIST, law.s(tc.time) * y, i, S[SN_IPREV], tc.abstol, tc);
+  const double p = law.knot_step(S[SN_XACC], x, tc.h);
+  if (p < KS_INF) S[SN_KNOTT] = tc.time - tc.h + p;
+  return fmin(h, p);
 }
 
 }  // namespace ksg

@@ -43,6 +43,8 @@ struct KElem {
 //   F       : u[0] = n+, u[1] = n-, u[3] = the controlling source's branch
 //   H       : u[0] = n+, u[1] = n-, u[2] = branch, u[3] = the controlling source's branch
 //   K       : u[0], u[1] = the coupled inductors' branches, u[2], u[3] = their value blocks
+//   CN      : u[0] = n+, u[1] = n-
+//   LN      : u[0] = n+, u[1] = n-, u[2] = branch
 //   S       : u[0] = n+, u[1] = n-, u[3] = nc+, u[4] = nc-
 //   W       : u[0] = n+, u[1] = n-, u[3] = the controlling source's branch
 
@@ -78,6 +80,17 @@ enum { DW_VH = 0, DW_SMOOTH, DW_LMEAN, DW_LRATIO, DW_INIT, DW_N };
 // last load (transient step), the last Accept changed the state, and the
 // linearization i = g v + k (c - c0) of the last load; the accepted control
 enum { SW_ON = 0, SW_ACC, SW_ACCEPTED, SW_FROZEN, SW_FLIP, SW_G, SW_K, SW_C0, SW_CACC, SW_N };
+// nonlinear / time-varying C and L (the state law y = s(t) f(x)): the resolved
+// SCALE arguments a[0..6], the integral of f from the first knot to 0, the
+// Newton step limit, then the integral of f from the first knot to each knot
+enum { DN_A0 = 0, DN_G0 = 7, DN_MAXSTEP = 8, DN_PRE = 9 };
+// the last load's linearization (x0 and the law's value and slope there: the
+// capacitor's iq and geq, the inductor's lam0 and ld), the companion's a and b,
+// s and ds/dt at the load's time, that time, a companion stamped, the load
+// limited its update, the limited iterate; the accepted voltage, current and
+// charge (flux), the accepted x and s, a knot crossing's landing time, history
+enum { SN_X0 = 0, SN_Y0, SN_G, SN_A, SN_B, SN_SN, SN_SDOT, SN_T, SN_TRAN, SN_LIM, SN_XITER,
+       SN_VPREV, SN_IPREV, SN_QPREV, SN_XACC, SN_SACC, SN_KNOTT, SN_HIST, SN_N = SN_HIST + H_SIZE };
 enum { SD_VD = 0, SD_CD, SD_GD, SD_IQ, SD_GEQ, SD_QPREV, SD_IQPREV, SD_VDACC, SD_LIM, SD_TRAN,
        SD_HIST, SD_N = SD_HIST + H_SIZE };
 enum { SQ_VBE = 0, SQ_VBC, SQ_VBX, SQ_VCS,

@@ -7,6 +7,7 @@
 // engine's element kinds, with the same sentinel texts.
 #include "ks_internal.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -50,9 +51,14 @@ int plan_layout(const ks_topology* t, HostPlan* hp, std::string* err) {
     }
     const bool ctl = s.kind >= KS_ELEM_E && s.kind <= KS_ELEM_K;
     const bool sw = s.kind == KS_ELEM_S || s.kind == KS_ELEM_W;
+    const bool nl = s.kind == KS_ELEM_CN || s.kind == KS_ELEM_LN;
+    if (nl && (s.level < 0 || s.level > 1 << 20 || s.level % 2 != 0 || s.level == 2)) {
+      *err = "ks_topology: a curve needs two or more (x, y) pairs";
+      return KS_EINVAL;
+    }
     int need = s.kind == KS_ELEM_D ? KS_D_NP : s.kind == KS_ELEM_Q ? KS_Q_NP : s.kind == KS_ELEM_M ? KS_M_NP
              : (s.kind == KS_ELEM_V || s.kind == KS_ELEM_I) ? KS_SRC_P_ARGS + s.nargs : ctl ? KS_CTL_NP
-             : sw ? KS_SW_NP : KS_RCL_NP;
+             : sw ? KS_SW_NP : nl ? KS_NL_P_ARGS + s.nargs + s.level : KS_RCL_NP;
     if (s.nargs < 0 || s.nargs > 1 << 20 || s.param < 0 || (int64_t)s.param + need > t->n_values) {
       *err = "ks_topology: element value block outside the value vector";
       return KS_EINVAL;
@@ -105,6 +111,12 @@ int plan_layout(const ks_topology* t, HostPlan* hp, std::string* err) {
         break;
       case KS_ELEM_F: e.u[0] = u0; e.u[1] = u1; break;
       case KS_ELEM_K: nd += DK_N; ns += SK_N; hp->n_reactive++; break;
+      case KS_ELEM_CN: case KS_ELEM_LN:  // device/nonlinear_reactive.go:311-314, :522-527
+        e.u[0] = u0; e.u[1] = u1;
+        if (s.kind == KS_ELEM_LN) e.u[2] = alloc_branch();
+        nd += DN_PRE + s.level / 2; ns += SN_N; hp->n_reactive++; hp->n_breakpointer++;
+        if (s.level > 0) hp->n_nonlin++;  // curvedCapacitor / curvedInductor
+        break;
       case KS_ELEM_S: case KS_ELEM_W:  // device/switch.go:111-117: nonlinear (ConvTest), no branch
         e.u[0] = u0; e.u[1] = u1;
         if (s.kind == KS_ELEM_S) { e.u[3] = s.node[2] - 1; e.u[4] = s.node[3] - 1; }
@@ -253,6 +265,54 @@ int validate(const ks_topology* t, const double* v, bool transient, std::string*
           *err = buf; return KS_EVALIDATE;
         }
         break;
+      case KS_ELEM_CN: case KS_ELEM_LN: {  // validateStateLaw, circuit/circuit.go:890-942
+        const int nc = e.level, na = e.nargs;
+        for (int i = 0; i < KS_NL_P_ARGS + na + nc; i++)
+          if (!finite(p[i])) { *err = "circuit: invalid element value: non-finite value"; return KS_EVALIDATE; }
+        const double* c = p + KS_NL_P_ARGS + na;
+        if (nc == 0) {
+          if (!(p[KS_NL_P_VALUE] > 0)) {
+            char buf[128]; snprintf(buf, sizeof buf, "circuit: invalid element value: element %d must be > 0, got %g", k, p[0]);
+            *err = buf; return KS_EVALIDATE;
+          }
+        } else {
+          if (p[KS_NL_P_VALUE] != 0) { *err = "circuit: invalid element value: an element has both a value and a curve"; return KS_EVALIDATE; }
+          if (nc < 4 || nc % 2 != 0 || nc > 200000) { *err = "circuit: invalid element value: a curve needs 2 to 100000 (x, y) points"; return KS_EVALIDATE; }
+          double ymax = 0;
+          for (int i = 0; i < nc; i++) {
+            if (i >= 2 && !(c[i] > c[i - 2])) {
+              *err = "circuit: invalid element value: a curve must strictly increase in x and y"; return KS_EVALIDATE;
+            }
+            if (i % 2 == 1) ymax = std::max(ymax, std::fabs(c[i]));
+          }
+          // curveAt(curve, 0), :944-961: the end segments extend
+          const int n = nc / 2;
+          int j = 0;
+          while (j < n && c[2 * j] < 0) j++;
+          const int lo = j <= 0 ? 0 : j >= n ? n - 2 : j - 1;
+          const double y0 = c[2 * lo + 1] + (c[2 * lo + 3] - c[2 * lo + 1]) / (c[2 * lo + 2] - c[2 * lo]) * (0 - c[2 * lo]);
+          if (std::fabs(y0) > 1e-12 * ymax) { *err = "circuit: invalid element value: a curve must pass through the origin"; return KS_EVALIDATE; }
+        }
+        if (e.wave != KS_WAVE_NONE) {  // the scale: a valid waveform that stays > 0 (scaleLowerBound, :963-986)
+          ks_element w = e;
+          w.param = 0;
+          if (!validate_wave(w, p + KS_NL_P_ARGS, err)) return KS_EVALIDATE;
+          const double* a = p + KS_NL_P_ARGS;
+          auto arg = [&](int i) { return i < na ? a[i] : 0.0; };
+          double lo = 0;
+          bool ok = true;
+          if (e.wave == KS_WAVE_PULSE || e.wave == KS_WAVE_EXP) lo = std::min(arg(0), arg(1));
+          else if (e.wave == KS_WAVE_SIN) { ok = arg(4) >= 0; lo = arg(0) - std::fabs(arg(1)); }
+          else {
+            lo = 1e300;
+            for (int i = 1; i < na; i += 2) lo = std::min(lo, a[i]);
+            for (int i = 2; i < na; i += 2)
+              if (!(a[i] > a[i - 2])) { *err = "circuit: invalid source waveform: scale PWL times must strictly increase"; return KS_EVALIDATE; }
+          }
+          if (!ok || !(lo > 0)) { *err = "circuit: invalid source waveform: scale must stay > 0"; return KS_EVALIDATE; }
+        }
+        break;
+      }
       case KS_ELEM_S: case KS_ELEM_W: {  // validateSwitch, circuit/switch.go:52-72
         for (int i = 0; i < KS_SW_NP; i++)
           if (!finite(p[i])) { *err = "circuit: invalid element value: non-finite value"; return KS_EVALIDATE; }
@@ -295,7 +355,7 @@ int validate(const ks_topology* t, const double* v, bool transient, std::string*
     const ks_element& e = t->elem[k];
     // current sources, mutual inductances and controlled current outputs are no path
     if (e.kind == KS_ELEM_I || e.kind == KS_ELEM_K || e.kind == KS_ELEM_F || e.kind == KS_ELEM_G ||
-        (e.kind == KS_ELEM_C && !transient))
+        ((e.kind == KS_ELEM_C || e.kind == KS_ELEM_CN) && !transient))
       continue;
     unite(e.node[0], e.node[1]);
     if (e.kind == KS_ELEM_M) unite(e.node[3], e.node[0]);

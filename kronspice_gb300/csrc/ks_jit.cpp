@@ -93,8 +93,8 @@ void stamp_pattern(const ksh::HostPlan& hp, std::vector<uint32_t>& m) {
   for (const KElem& e : hp.elem) {
     const int* u = e.u;
     switch (e.kind) {
-      case KS_ELEM_R: case KS_ELEM_C: block(u, 2); break;
-      case KS_ELEM_V: case KS_ELEM_L:
+      case KS_ELEM_R: case KS_ELEM_C: case KS_ELEM_CN: block(u, 2); break;
+      case KS_ELEM_V: case KS_ELEM_L: case KS_ELEM_LN:
         add(u[0], u[2]); add(u[1], u[2]); add(u[2], u[0]); add(u[2], u[1]); add(u[2], u[2]); break;
       case KS_ELEM_I: break;
       case KS_ELEM_D: block(u, 3); break;

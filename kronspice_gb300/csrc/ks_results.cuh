@@ -247,6 +247,21 @@ __device__ inline ElemOp elem_operating(const KElem& e, const Col& V, const Col&
       o.stores = true;
       break;
     }
+    case KS_ELEM_CN: case KS_ELEM_LN: {  // device/nonlinear_reactive.go:368-376, :577-582; StoredEnergy :410, :612
+      NlLaw law(e, V, Dv);
+      o.v = X(e.u[0]) - X(e.u[1]);
+      o.i = nl_current(e, S, s);
+      o.p = o.v * o.i;
+      const double x = e.kind == KS_ELEM_LN ? o.i : o.v;
+      // scalePower, :360-365: s'(t) F(x) leaves through the scale's port
+      const double sp = (S[SN_TRAN] == 0 || S[SN_SDOT] == 0) ? 0.0 : S[SN_SDOT] * law.coenergy(x);
+      o.ps = o.p - sp;
+      if (energy) o.w = law.s(S[SN_T]) * law.energy(x);
+      o.stores = true;
+      o.thermal = false;  // the scale's port: mechanical
+      if (e.wave != KS_WAVE_NONE) o.ext = -sp;
+      break;
+    }
     case KS_ELEM_S: case KS_ELEM_W: {  // device/switch.go:246-250, ExteriorPower :304-310
       o.v = X(e.u[0]) - X(e.u[1]);
       o.i = S[SW_G] * o.v + S[SW_K] * (sw_control(e, s) - S[SW_C0]);  // the current the solve used
@@ -371,7 +386,7 @@ __device__ inline bool tran_point_results(Thr<SY, P>& t, TranLedger& L, const Lo
   });
   t.prog.each([&](const KElem& e) {  // the energy-storing elements
     if (!(e.kind == KS_ELEM_C || e.kind == KS_ELEM_L || e.kind == KS_ELEM_D || e.kind == KS_ELEM_Q ||
-          e.kind == KS_ELEM_M || e.kind == KS_ELEM_K))
+          e.kind == KS_ELEM_M || e.kind == KS_ELEM_K || e.kind == KS_ELEM_CN || e.kind == KS_ELEM_LN))
       return;
     ElemOp r = elem_operating(e, t.V, t.D, state_col(t.Sb, e), t.s, o.gmin, true);
     a.storage(r.ps);

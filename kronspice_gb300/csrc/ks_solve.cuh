@@ -144,6 +144,7 @@ __device__ inline void setup_elem(const KElem& e, const Col& V, const Col& D, do
     case KS_ELEM_K:  // NewMutual, device/mutual.go:44-49: M = k sqrt(L1 L2)
       D[d + DK_M] = V[p + KS_K_P_COUPLING] * sqrt(V[e.u[2] + KS_RCL_P_VALUE] * V[e.u[3] + KS_RCL_P_VALUE]);
       break;
+    case KS_ELEM_CN: case KS_ELEM_LN: nl_setup(e, V, D, step, stop); break;
     case KS_ELEM_S: case KS_ELEM_W: {  // NewSwitch, device/switch.go:92-108
       const double vh = V[p + KS_SW_P_VH], ron = V[p + KS_SW_P_RON], roff = V[p + KS_SW_P_ROFF];
       D[d + DW_VH] = fabs(vh);
@@ -224,7 +225,8 @@ __device__ __forceinline__ int64_t prog_next(const P&, unsigned long long* queue
 __device__ __forceinline__ Col state_col(const Col& Sb, const KElem& e) { return Col{Sb.p + (int64_t)e.state * Sb.B, Sb.B}; }
 
 __device__ __forceinline__ int lim_slot(int kind) {
-  return kind == KS_ELEM_D ? SD_LIM : kind == KS_ELEM_Q ? SQ_LIM : kind == KS_ELEM_M ? SM_LIM : -1;
+  return kind == KS_ELEM_D ? SD_LIM : kind == KS_ELEM_Q ? SQ_LIM : kind == KS_ELEM_M ? SM_LIM
+       : (kind == KS_ELEM_CN || kind == KS_ELEM_LN) ? SN_LIM : -1;
 }
 
 // Stamp one element at the linearization point (the element's Load).
@@ -314,6 +316,7 @@ __device__ __forceinline__ void elem_load(const KElem& e, const Col& Vb, const C
       break;
     }
     case KS_ELEM_S: case KS_ELEM_W: sw_load(e, Vb, Db, S, sys, lp); break;
+    case KS_ELEM_CN: case KS_ELEM_LN: nl_load(e, Vb, Db, S, sys, lp); break;
   }
 }
 
@@ -589,6 +592,7 @@ __device__ __forceinline__ bool converged(const P& prog, const Col& Vb, const Co
     else if (e.kind == KS_ELEM_Q) ok = bjt_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
     else if (e.kind == KS_ELEM_M) ok = mos_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
     else if (e.kind == KS_ELEM_S || e.kind == KS_ELEM_W) ok = sw_conv(e, Vb, Db, S, s, o.reltol, o.abstol);
+    else if (e.kind == KS_ELEM_CN || e.kind == KS_ELEM_LN) ok = nl_conv(e, Vb, Db, S, s, o.reltol, o.abstol);
   });
   return prog_all(prog, ok);
 }
@@ -625,6 +629,10 @@ __device__ __forceinline__ void elem_accept(const KElem& e, const Col& Vb, const
       S[SK_I1PREV] = xn_(s, e.u[0]); S[SK_I2PREV] = xn_(s, e.u[1]);
       break;
     case KS_ELEM_S: case KS_ELEM_W: sw_accept(e, Vb, Db, S, s); break;  // nonlinear: seeded by a NodeSet too
+    case KS_ELEM_CN: case KS_ELEM_LN:  // a curved law is nonlinear (seeded by a NodeSet), a linear one is not
+      if (nonlinOnly && e.level == 0) break;
+      nl_accept(e, Vb, Db, S, s, t, mode);
+      break;
   }
 }
 
@@ -640,6 +648,7 @@ __device__ __forceinline__ bool elem_converged(const KElem& e, const Col& Vb, co
   if (S[ls] != 0) return false;
   if (e.kind == KS_ELEM_D) return diode_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
   if (e.kind == KS_ELEM_Q) return bjt_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
+  if (e.kind == KS_ELEM_CN || e.kind == KS_ELEM_LN) return nl_conv(e, Vb, Db, S, s, o.reltol, o.abstol);
   return mos_conv(e, Vb, Db, S, s, o.reltol, o.abstol, gmin);
 }
 

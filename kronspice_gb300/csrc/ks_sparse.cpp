@@ -57,10 +57,10 @@ void stamp_rows(const HostPlan& hp, const double* values, bool transient, std::v
     const int* u = e.u;
     switch (e.kind) {
       case KS_ELEM_R: g4(u[0], u[1]); break;
-      case KS_ELEM_C: if (transient) g4(u[0], u[1]); break;
-      case KS_ELEM_V: case KS_ELEM_L:
+      case KS_ELEM_C: case KS_ELEM_CN: if (transient) g4(u[0], u[1]); break;
+      case KS_ELEM_V: case KS_ELEM_L: case KS_ELEM_LN:
         add(u[0], u[2]); add(u[1], u[2]); add(u[2], u[0]); add(u[2], u[1]);
-        if (e.kind == KS_ELEM_L && transient) add(u[2], u[2]);
+        if (e.kind != KS_ELEM_V && transient) add(u[2], u[2]);
         break;
       case KS_ELEM_I: break;
       case KS_ELEM_D:  // u = {anode, cathode, internal anode}
@@ -187,14 +187,18 @@ int sparse_symbolic(const HostPlan& hp, const double* values, double h, SparseSy
         cond(u[0], u[1], r > 0 ? 1.0 / r : 1.0);
         break;
       }
-      case KS_ELEM_C:
-        if (h > 0) cond(u[0], u[1], 2.0 * (values ? values[e.param + KS_RCL_P_VALUE] : 1e-12) / h);
+      case KS_ELEM_C: case KS_ELEM_CN: {  // a curved capacitor at 1 nF (the law's value is 0 with a curve)
+        const double cv = values ? values[e.param + KS_RCL_P_VALUE] : 1e-12;
+        if (h > 0) cond(u[0], u[1], 2.0 * (cv > 0 ? cv : 1e-9) / h);
         break;
-      case KS_ELEM_V: case KS_ELEM_L:
+      }
+      case KS_ELEM_V: case KS_ELEM_L: case KS_ELEM_LN: {
         madd(u[0], u[2], 1); madd(u[1], u[2], -1); madd(u[2], u[0], 1); madd(u[2], u[1], -1);
-        if (e.kind == KS_ELEM_L && h > 0) madd(u[2], u[2], -2.0 * (values ? values[e.param + KS_RCL_P_VALUE] : 1e-9) / h);
+        const double lv = values ? values[e.param + KS_RCL_P_VALUE] : 1e-9;
+        if (e.kind != KS_ELEM_V && h > 0) madd(u[2], u[2], -2.0 * (lv > 0 ? lv : 1e-3) / h);
         if (u[2] >= 0) branch[u[2]] = 1;
         break;
+      }
       case KS_ELEM_D:
         // junctions are left out: their conductance spans twelve decades over a
         // Newton solve, and a node row they feed stays diagonally dominant

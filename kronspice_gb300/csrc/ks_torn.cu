@@ -1163,8 +1163,8 @@ void stamp_pattern(const ksh::HostPlan& hp, std::vector<std::vector<int>>& rows)
   for (const KElem& e : hp.elem) {
     const int* u = e.u;
     switch (e.kind) {
-      case KS_ELEM_R: case KS_ELEM_C: block(u, 2); break;
-      case KS_ELEM_V: case KS_ELEM_L:
+      case KS_ELEM_R: case KS_ELEM_C: case KS_ELEM_CN: block(u, 2); break;
+      case KS_ELEM_V: case KS_ELEM_L: case KS_ELEM_LN:
         add(u[0], u[2]); add(u[1], u[2]); add(u[2], u[0]); add(u[2], u[1]); add(u[2], u[2]); break;
       case KS_ELEM_D: block(u, 3); break;
       case KS_ELEM_Q: block(u, 9); break;
@@ -1301,7 +1301,7 @@ int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_t
     seen[e] = 1;
     const ks_element& el = hp.src[e];
     if (el.kind == KS_ELEM_V || el.kind == KS_ELEM_L || el.kind == KS_ELEM_E || el.kind == KS_ELEM_F ||
-        el.kind == KS_ELEM_H || el.kind == KS_ELEM_K || el.kind == KS_ELEM_W) {  // tearTerminals, kron/jacobian.go:143-147
+        el.kind == KS_ELEM_H || el.kind == KS_ELEM_K || el.kind == KS_ELEM_W || el.kind == KS_ELEM_LN) {  // tearTerminals, kron/jacobian.go:143-147
       *err = "kron: unsupported: tearing element " + std::to_string(e) +
              ": its coupling runs through a branch-current unknown; tear a neighbouring element";
       return KS_EINVAL;
@@ -1864,8 +1864,9 @@ extern "C" int ks_torn_create(const ks_topology* topo, int32_t n_variants, const
   int rc = ksh::plan_layout(topo, &T->hp, &err);
   if (rc) { set_error(err); delete T; return rc; }
   for (const KElem& e : T->hp.elem)
-    if (e.kind == KS_ELEM_S || e.kind == KS_ELEM_W) {  // no step limit or state restart in the torn transient
-      set_error("ks_torn_create: switches (S, W) are not supported by the torn engine");
+    if (e.kind == KS_ELEM_S || e.kind == KS_ELEM_W || e.kind == KS_ELEM_CN || e.kind == KS_ELEM_LN) {
+      // no step limiter, state restart or knot breakpoints in the torn transient
+      set_error("ks_torn_create: switches and nonlinear or time-varying C and L are not supported by the torn engine");
       delete T;
       return KS_EUNSUPPORTED;
     }

@@ -82,6 +82,7 @@ __device__ __forceinline__ double truncate_all(Thr<SY, P>& t, const TruncParams&
       case KS_ELEM_S: case KS_ELEM_W:  // the step limiters, analysis/tran.go:186-190
         prop = fmin(prop, sw_limit_step(e, t.V, t.D, S, x, tc.h));
         break;
+      case KS_ELEM_CN: case KS_ELEM_LN: prop = fmin(prop, nl_truncate(e, t.V, t.D, S, x, tc)); break;
       default: break;
     }
   });
@@ -106,6 +107,14 @@ __device__ __forceinline__ double next_breakpoint(Thr<SY, P>& t, double tnow) {
   t.prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
     if ((e.kind == KS_ELEM_V || e.kind == KS_ELEM_I) && e.wave != KS_WAVE_NONE)
       nb = fmin(nb, wave_next_breakpoint(e.wave, t.D, e.derived, t.V, e.param + KS_SRC_P_ARGS, e.nargs, tnow));
+    if (e.kind == KS_ELEM_CN || e.kind == KS_ELEM_LN) {  // stateLaw.nextBreakpoint, device/nonlinear_reactive.go:228-237
+      double b = e.wave != KS_WAVE_NONE
+                     ? wave_next_breakpoint(e.wave, t.D, e.derived + DN_A0, t.V, e.param + KS_NL_P_ARGS, e.nargs, tnow)
+                     : KS_INF;
+      const double kt = state_col(t.Sb, e)[SN_KNOTT];
+      if (kt > tnow && kt < b) b = kt;
+      nb = fmin(nb, b);
+    }
   });
   return prog_min(t.prog, nb);
 }
@@ -118,6 +127,9 @@ __device__ __forceinline__ void set_initial_conditions(Thr<SY, P>& t) {
     bool has = e.flags & KS_F_HAS_IC;
     if (e.kind == KS_ELEM_C) { S[SC_VPREV] = has ? t.V[e.param + KS_RCL_P_IC] : 0.0; S[SC_IPREV] = 0; }
     if (e.kind == KS_ELEM_L) { S[SL_VPREV] = 0; S[SL_IPREV] = has ? t.V[e.param + KS_RCL_P_IC] : 0.0; }
+    // device/nonlinear_reactive.go:402-407, :605-610
+    if (e.kind == KS_ELEM_CN) { S[SN_VPREV] = has ? t.V[e.param + KS_NL_P_IC] : 0.0; S[SN_IPREV] = 0; }
+    if (e.kind == KS_ELEM_LN) { S[SN_VPREV] = 0; S[SN_IPREV] = has ? t.V[e.param + KS_NL_P_IC] : 0.0; }
   });
   prog_sync(t.prog);
 }

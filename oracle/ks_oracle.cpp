@@ -137,6 +137,21 @@ struct Sim {
           m->l[0] = el.node[0]; m->l[1] = el.node[1];
           d = m; break;
         }
+        case KS_ELEM_CN: case KS_ELEM_LN: {  // NewNonlinearCapacitor / NewNonlinearInductor
+          const double* curve = p + KS_NL_P_ARGS + el.nargs;
+          if (el.kind == KS_ELEM_CN) {
+            auto* c = new NonlinearCapacitor(p[KS_NL_P_IC], el.flags & KS_F_HAS_IC);
+            c->law.init(p[KS_NL_P_VALUE], curve, el.level, el.wave, p + KS_NL_P_ARGS, el.nargs);
+            c->nodes[0] = el.node[0]; c->nodes[1] = el.node[1];
+            d = c;
+          } else {
+            auto* l = new NonlinearInductor(p[KS_NL_P_IC], el.flags & KS_F_HAS_IC);
+            l->law.init(p[KS_NL_P_VALUE], curve, el.level, el.wave, p + KS_NL_P_ARGS, el.nargs);
+            l->nodes[0] = el.node[0]; l->nodes[1] = el.node[1];
+            d = l;
+          }
+          break;
+        }
         case KS_ELEM_S: case KS_ELEM_W: {
           auto* w = new Switch(el.kind == KS_ELEM_W, p);
           w->nodes[0] = el.node[0]; w->nodes[1] = el.node[1];
@@ -845,7 +860,7 @@ extern "C" int kso_torn_cuts(const ks_topology* t, const int32_t* elems, int n_e
     seen[e] = 1;
     const ks_element& el = t->elem[e];
     if (el.kind == KS_ELEM_V || el.kind == KS_ELEM_L || el.kind == KS_ELEM_E || el.kind == KS_ELEM_F ||
-        el.kind == KS_ELEM_H || el.kind == KS_ELEM_K || el.kind == KS_ELEM_W) {  // tearTerminals, kron/jacobian.go:143-147
+        el.kind == KS_ELEM_H || el.kind == KS_ELEM_K || el.kind == KS_ELEM_W || el.kind == KS_ELEM_LN) {  // tearTerminals, kron/jacobian.go:143-147
       copyMsg(std::string("kron: unsupported: tearing ") + name +
               ": its coupling runs through a branch-current unknown; tear a neighbouring element", err, errlen);
       return KS_EINVAL;

@@ -125,7 +125,7 @@ struct ACCtx {
 // when the port is not modeled), ModelSuppliedPower (device.ModelSupplier),
 // StoredEnergy and whether it is a device.Reactive element (its storage power
 // enters the ledger).
-enum { CH_ELECTRICAL = 0, CH_THERMAL = 1 };
+enum { CH_ELECTRICAL = 0, CH_THERMAL = 1, CH_MECHANICAL = 2 };
 struct OpPt {
   double v = 0, i = 0, p = 0, ps = 0;  // Voltage, Current, PowerAbsorbed, StoragePower
   double w = 0;                        // StoredEnergy
@@ -376,6 +376,47 @@ struct Wave {
     }
     return 0;
   }
+  double slope(double t) const {  // :131-186
+    switch (kind) {
+      case KS_WAVE_PULSE: {
+        double v1 = a[0], v2 = a[1], td = a[2], tr = a[3], tf = a[4], pw = a[5], per = a[6];
+        if (t <= td) return 0;
+        double tt = t - td;
+        if (per > 0) {
+          tt = std::fmod(tt, per);
+          if (tt == 0) tt = per;  // the end of the previous period
+        }
+        if (tt <= tr) return (v2 - v1) / tr;
+        if (tt <= tr + pw) return 0;
+        if (tt <= tr + pw + tf) return (v1 - v2) / tf;
+        return 0;
+      }
+      case KS_WAVE_SIN: {
+        double va = a[1], f = a[2], td = a[3], theta = a[4], ph = a[5] * kPi / 180;
+        if (t <= td) return 0;
+        double tt = t - td, om = 2 * kPi * f;
+        return va * std::exp(-tt * theta) * (om * std::cos(om * tt + ph) - theta * std::sin(om * tt + ph));
+      }
+      case KS_WAVE_EXP: {
+        double v1 = a[0], v2 = a[1], td1 = a[2], tau1 = a[3], td2 = a[4], tau2 = a[5];
+        if (t <= td1) return 0;
+        double d = (v2 - v1) / tau1 * std::exp(-(t - td1) / tau1);
+        if (t > td2) d += (v1 - v2) / tau2 * std::exp(-(t - td2) / tau2);
+        return d;
+      }
+      case KS_WAVE_PWL: {
+        const std::vector<double>& p = pwl;
+        int n = (int)p.size() / 2;
+        if (t <= p[0] || t > p[2 * (n - 1)]) return 0;
+        int k = 0;  // segment k-1 -> k ends at or after t
+        while (k < n && !(p[2 * k] >= t)) k++;
+        double t0 = p[2 * (k - 1)], v0 = p[2 * (k - 1) + 1], t1 = p[2 * k], v1 = p[2 * k + 1];
+        if (t1 == t0) return 0;
+        return (v1 - v0) / (t1 - t0);
+      }
+    }
+    return 0;
+  }
   double nextBreakpoint(double t) const {  // :190-239
     const double rel = 1e-12;
     auto after = [&](double b) { return b > t + rel * std::max(std::fabs(t), 1e-15); };
@@ -545,6 +586,271 @@ struct Mutual : Device {
   void loadAC(ACCtx& c) override {  // :146-151
     c.add(k1, k2, std::complex<double>(0, -c.omega * m));
     c.add(k2, k1, std::complex<double>(0, -c.omega * m));
+  }
+};
+
+// stateLaw, device/nonlinear_reactive.go:15-249: y(x, t) = s(t) f(x) with f a
+// piecewise-linear curve through the origin (or lin x) and s a scale waveform.
+struct StateLaw {
+  double lin = 0;
+  std::vector<double> xs, ys, pre;  // knots, and the integral of f from xs[0] to each knot
+  double g0 = 0, maxStep = 0, knotT = 0;
+  int skind = KS_WAVE_NONE;
+  std::vector<double> sargs;
+  Wave scale;
+  bool varies = false;
+  void init(double value, const double* curve, int ncurve, int wk, const double* args, int nargs) {  // :47-64
+    lin = value; skind = wk; varies = wk != KS_WAVE_NONE;
+    sargs.assign(args, args + nargs);
+    const int n = ncurve / 2;
+    if (n < 2) return;
+    xs.resize(n); ys.resize(n); pre.assign(n, 0.0);
+    for (int i = 0; i < n; i++) { xs[i] = curve[2 * i]; ys[i] = curve[2 * i + 1]; }
+    for (int k = 1; k < n; k++) pre[k] = pre[k - 1] + 0.5 * (ys[k - 1] + ys[k]) * (xs[k] - xs[k - 1]);
+    g0 = cum(0);
+    maxStep = 4 * (xs[n - 1] - xs[0]) / double(n - 1);
+  }
+  void resolve(double step, double stop) {  // :69-90 (the EXP bound is the host's)
+    if (varies) scale.resolve(skind, sargs.data(), (int)sargs.size(), step, stop);
+  }
+  int segment(double x) const {  // :93-104
+    const int n = (int)xs.size();
+    const int k = (int)(std::lower_bound(xs.begin(), xs.end(), x) - xs.begin());
+    if (k <= 0) return 1;
+    if (k >= n) return n - 1;
+    return k;
+  }
+  void f(double x, double* y, double* dy) const {  // :107-115
+    if (xs.empty()) { *y = lin * x; *dy = lin; return; }
+    const int k = segment(x);
+    const double g = (ys[k] - ys[k - 1]) / (xs[k] - xs[k - 1]);
+    *y = ys[k - 1] + g * (x - xs[k - 1]);
+    *dy = g;
+  }
+  double cum(double x) const {  // :118-123
+    const int k = segment(x);
+    const double g = (ys[k] - ys[k - 1]) / (xs[k] - xs[k - 1]);
+    const double d = x - xs[k - 1];
+    return pre[k - 1] + ys[k - 1] * d + 0.5 * g * d * d;
+  }
+  double coenergy(double x) const { return xs.empty() ? 0.5 * lin * x * x : cum(x) - g0; }  // :126-131
+  double energy(double x) const { double y, dy; f(x, &y, &dy); return x * y - coenergy(x); }  // :134-137
+  double s(double t) const { return varies ? scale.value(t) : 1.0; }
+  double sdot(double t) const { return varies ? scale.slope(t) : 0.0; }
+  double limit(double x, double prev, bool* lim) const {  // :150-159
+    *lim = false;
+    if (maxStep == 0 || std::fabs(x - prev) <= maxStep) return x;
+    const double lo = xs.front(), hi = xs.back();
+    if ((x <= lo && prev <= lo) || (x >= hi && prev >= hi)) return x;
+    *lim = true;
+    return prev + std::copysign(maxStep, x - prev);
+  }
+  double knotStep(double x0, double x1, double h) const {  // :171-206
+    if (xs.empty() || x0 == x1) return kInf;
+    const int n = (int)xs.size();
+    int k = (int)(std::lower_bound(xs.begin(), xs.end(), x0) - xs.begin());  // first knot >= x0
+    double xk;
+    if (x1 > x0) {
+      while (k < n && xs[k] <= x0) k++;
+      if (k == n || xs[k] >= x1) return kInf;
+      xk = xs[k];
+    } else {
+      if (--k < 0 || xs[k] <= x1) return kInf;
+      xk = xs[k];
+    }
+    double w = kInf;
+    if (k > 0) w = xs[k] - xs[k - 1];
+    if (k < n - 1) w = std::min(w, xs[k + 1] - xs[k]);
+    if (std::fabs(xk - x0) <= 1e-3 * w) return kInf;
+    const double fr = (xk - x0) / (x1 - x0);
+    if (fr > 0.9) return kInf;
+    return fr * h;
+  }
+  double truncate(double x0, double x1, const TruncCtx& tc) {  // :213-219
+    const double p = knotStep(x0, x1, tc.h);
+    if (p < kInf) knotT = tc.time - tc.h + p;
+    return p;
+  }
+  void accepted(double t) { if (knotT != 0 && t >= knotT) knotT = 0; }  // :222-226
+  double nextBreakpoint(double t) const {  // :228-237
+    double b = varies ? scale.nextBreakpoint(t) : kInf;
+    if (knotT > t && knotT < b) b = knotT;
+    return b;
+  }
+};
+
+// NonlinearCapacitor, device/nonlinear_reactive.go:263-465: q = s(t) Q(v), the
+// charge integrated by the companion models.
+struct NonlinearCapacitor : TwoTerm {
+  StateLaw law;
+  double ic; bool hasIC;
+  double v0 = 0, iq = 0, geq = 0, a = 0, b = 0, sn = 1, sd = 0, t = 0, vIter = 0, omega = 0;
+  bool tran = false, lim = false;
+  double vPrev = 0, qPrev = 0, iPrev = 0, vAcc = 0, sAcc = 1;
+  History hist;
+  NonlinearCapacitor(double ic_, bool has) : ic(ic_), hasIC(has) {}
+  void setup(SetupCtx& c) override { setupNodes(c); law.resolve(c.step, c.stop); }
+  bool reactive() const override { return true; }
+  bool nonlinear() const override { return !law.xs.empty(); }  // curvedCapacitor
+  bool limited() const override { return lim; }
+  bool breakpointer() const override { return true; }
+  double nextBreakpoint(double tt) override { return law.nextBreakpoint(tt); }
+  void load(LoadCtx& c) override {  // :318-357
+    const int p = u[0], nn = u[1];
+    lim = false; t = c.time; tran = false; geq = 0; iq = 0;
+    if (c.mode == ModeOP || c.mode == ModeTranOP) return;
+    if (c.mode == ModeUICInit) {
+      const double g = 1e9;  // uicConductance
+      c.M->add(p, p, g); c.M->add(nn, nn, g); c.M->add(p, nn, -g); c.M->add(nn, p, -g);
+      c.addRHS(p, g * vPrev); c.addRHS(nn, -g * vPrev);
+      return;
+    }
+    tran = true;
+    const double v = law.limit(voltage(c.X), vIter, &lim);
+    vIter = v; v0 = v;
+    sn = law.s(c.time); sd = law.sdot(c.time);
+    if (c.method == TRAP) { a = 2 / c.h; b = -2 * qPrev / c.h - iPrev; }
+    else { a = 1 / c.h; b = -qPrev / c.h; }
+    double q, dq;
+    law.f(v, &q, &dq);
+    iq = a * sn * q + b;
+    geq = a * sn * dq;
+    const double g = geq;
+    c.M->add(p, p, g); c.M->add(nn, nn, g); c.M->add(p, nn, -g); c.M->add(nn, p, -g);
+    const double ieq = iq - g * v;
+    c.addRHS(p, -ieq); c.addRHS(nn, ieq);
+  }
+  double scalePower(double v) const { return (!tran || sd == 0) ? 0.0 : sd * law.coenergy(v); }  // :360-365
+  double current(const double* x) override { return tran ? iq + geq * (voltage(x) - v0) : 0.0; }
+  OpPt operating(const double* x) override {  // :368-376, StoredEnergy :410-413, ExteriorPower :432-437
+    OpPt o;
+    o.v = voltage(x); o.i = current(x); o.p = o.v * o.i;
+    const double sp = scalePower(o.v);
+    o.ps = o.p - sp;
+    o.w = law.s(t) * law.energy(o.v);
+    o.stores = true;
+    o.ch = CH_MECHANICAL;
+    if (law.varies) o.ext = -sp;
+    return o;
+  }
+  void accept(const double* x, double tt, int mode) override {  // :379-399
+    double v = voltage(x);
+    if (mode == ModeUICInit) { v = vPrev; iPrev = 0; hist.reset(); }
+    else if (mode == ModeOP || mode == ModeTranOP) { iPrev = 0; hist.reset(); }
+    else iPrev = iq + geq * (v - v0);
+    vPrev = vIter = vAcc = v;
+    sAcc = law.s(tt);
+    double q, dq;
+    law.f(v, &q, &dq);
+    qPrev = sAcc * q;
+    hist.push(tt, qPrev);
+    law.accepted(tt);
+  }
+  void setInitialCondition() override { vPrev = 0; iPrev = 0; if (hasIC) vPrev = ic; }  // :402-407
+  double truncate(const double* x, const TruncCtx& tc) override {  // :417-424
+    const double v = voltage(x), i = current(x);
+    double q, dq;
+    law.f(v, &q, &dq);
+    const double h = lteStep(hist, law.s(tc.time) * q, i, iPrev, tc.abstol, tc);
+    return std::min(h, law.truncate(vAcc, v, tc));
+  }
+  bool convTest(const double* x, double reltol, double abstol) override {  // :458-468
+    if (!tran) return true;
+    const double v = voltage(x), ihat = iq + geq * (v - v0);
+    double q, dq;
+    law.f(v, &q, &dq);
+    const double i = a * sn * q + b;
+    return std::fabs(ihat - i) <= reltol * std::max(std::fabs(i), std::fabs(ihat)) + abstol;
+  }
+  void loadAC(ACCtx& c) override {  // :440-449
+    double q, dq;
+    law.f(vAcc, &q, &dq);
+    c.stampY(u[0], u[1], std::complex<double>(0, c.omega * sAcc * dq));
+  }
+};
+
+// NonlinearInductor, device/nonlinear_reactive.go:470-682: flux linkage
+// s(t) L(i) with a branch current, the flux integrated by the companion models.
+struct NonlinearInductor : TwoTerm {
+  StateLaw law;
+  double ic; bool hasIC;
+  int branch = -1;
+  double i0 = 0, lam0 = 0, ld = 0, a = 0, b = 0, sn = 1, sd = 0, t = 0, iIter = 0;
+  bool tran = false, lim = false;
+  double vPrev = 0, iPrev = 0, lamPrev = 0, iAcc = 0, sAcc = 1;
+  History hist;
+  NonlinearInductor(double ic_, bool has) : ic(ic_), hasIC(has) {}
+  void setup(SetupCtx& c) override { setupNodes(c); branch = c.allocBranch(); law.resolve(c.step, c.stop); }
+  bool reactive() const override { return true; }
+  bool nonlinear() const override { return !law.xs.empty(); }  // curvedInductor
+  bool limited() const override { return lim; }
+  bool breakpointer() const override { return true; }
+  double nextBreakpoint(double tt) override { return law.nextBreakpoint(tt); }
+  void load(LoadCtx& c) override {  // :531-566
+    const int p = u[0], nn = u[1], k = branch;
+    lim = false; t = c.time; tran = false;
+    c.M->add(p, k, 1); c.M->add(nn, k, -1);
+    if (c.mode == ModeOP || c.mode == ModeTranOP) { c.M->add(k, p, 1); c.M->add(k, nn, -1); return; }
+    if (c.mode == ModeUICInit) { c.M->add(k, k, 1); c.addRHS(k, iPrev); return; }
+    tran = true;
+    const double i = law.limit(at(c.X, n, k), iIter, &lim);
+    iIter = i; i0 = i;
+    sn = law.s(c.time); sd = law.sdot(c.time);
+    if (c.method == TRAP) { a = 2 / c.h; b = -2 * lamPrev / c.h - vPrev; }
+    else { a = 1 / c.h; b = -lamPrev / c.h; }
+    double lam, dl;
+    law.f(i, &lam, &dl);
+    lam0 = sn * lam; ld = sn * dl;
+    c.M->add(k, p, 1); c.M->add(k, nn, -1); c.M->add(k, k, -a * ld);
+    c.addRHS(k, a * (lam0 - ld * i0) + b);
+  }
+  double scalePower(double i) const { return (!tran || sd == 0) ? 0.0 : sd * law.coenergy(i); }  // :569-574
+  double current(const double* x) override { return at(x, n, branch); }
+  OpPt operating(const double* x) override {  // :577-582, StoredEnergy :612-615, ExteriorPower :632-637
+    OpPt o;
+    o.v = voltage(x); o.i = at(x, n, branch); o.p = o.v * o.i;
+    const double sp = scalePower(o.i);
+    o.ps = o.p - sp;
+    o.w = law.s(t) * law.energy(o.i);
+    o.stores = true;
+    o.ch = CH_MECHANICAL;
+    if (law.varies) o.ext = -sp;
+    return o;
+  }
+  void accept(const double* x, double tt, int mode) override {  // :585-602
+    double i = at(x, n, branch), v = voltage(x);
+    if (mode == ModeUICInit) { i = iPrev; v = 0; hist.reset(); }
+    else if (mode == ModeOP || mode == ModeTranOP) { v = 0; hist.reset(); }
+    iPrev = iIter = iAcc = i; vPrev = v;
+    sAcc = law.s(tt);
+    double lam, dl;
+    law.f(i, &lam, &dl);
+    lamPrev = sAcc * lam;
+    hist.push(tt, lamPrev);
+    law.accepted(tt);
+  }
+  void setInitialCondition() override { vPrev = 0; iPrev = 0; if (hasIC) iPrev = ic; }  // :605-610
+  double truncate(const double* x, const TruncCtx& tc) override {  // :620-625
+    const double i = at(x, n, branch), v = voltage(x);
+    double lam, dl;
+    law.f(i, &lam, &dl);
+    const double h = lteStep(hist, law.s(tc.time) * lam, v, vPrev, tc.vntol, tc);
+    return std::min(h, law.truncate(iAcc, i, tc));
+  }
+  bool convTest(const double* x, double reltol, double) override {  // :672-682 (vntol 1e-6)
+    if (!tran) return true;
+    const double i = at(x, n, branch), vhat = a * (lam0 + ld * (i - i0)) + b;
+    double lam, dl;
+    law.f(i, &lam, &dl);
+    const double v = a * sn * lam + b;
+    return std::fabs(vhat - v) <= reltol * std::max(std::fabs(v), std::fabs(vhat)) + 1e-6;
+  }
+  void loadAC(ACCtx& c) override {  // :640-651
+    const int p = u[0], nn = u[1], k = branch;
+    double lam, dl;
+    law.f(iAcc, &lam, &dl);
+    c.add(p, k, 1); c.add(nn, k, -1); c.add(k, p, 1); c.add(k, nn, -1);
+    c.add(k, k, std::complex<double>(0, -c.omega * sAcc * dl));
   }
 };
 

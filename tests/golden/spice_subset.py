@@ -329,10 +329,41 @@ def _parse(text):
         if kind == "r":
             ckt["elements"].append({"name": name, "kind": "R", "nodes": toks[1:3], "value": value(toks[3])})
         elif kind in "cl":
-            e = {"name": name, "kind": kind.upper(), "nodes": toks[1:3], "value": value(toks[3])}
-            p = _params(toks[4:])
+            # value | Q=pwl(v1 q1 ...) | FLUX=pwl(i1 l1 ...), [SCALE=wave(...)] [IC=x]
+            # (netlist/parser.go:703-800)
+            e = {"name": name, "kind": kind.upper(), "nodes": toks[1:3], "value": 0.0}
+            rest, i, p, curve, scale = toks[3:], 0, {}, None, None
+            while i < len(rest):
+                t = rest[i]
+                if "=" in t and i + 1 < len(rest) and rest[i + 1] == "(":
+                    key, fn = t.lower().split("=", 1)
+                    j, args = i + 2, []
+                    while j < len(rest) and rest[j] != ")":
+                        args.append(value(rest[j]))
+                        j += 1
+                    if key in ("q", "flux") and fn == "pwl":
+                        curve = args
+                    elif key == "scale" and fn in ("pulse", "sin", "exp", "pwl"):
+                        scale = (fn, args)
+                    else:
+                        return None, "unsupported %s=%s on %s" % (key, fn, name)
+                    i = j + 1
+                elif "=" in t:
+                    k, v = t.split("=", 1)
+                    p[k.lower()] = value(v)
+                    i += 1
+                else:
+                    e["value"] = value(t)
+                    i += 1
+            if set(p) - {"ic"}:
+                return None, "unsupported parameter on " + name
             if "ic" in p:
                 e["ic"] = p["ic"]
+            if curve is not None or scale is not None:
+                e["kind"] = kind.upper() + "N"
+                e["curve"] = curve or []
+                e["scale"] = scale[0] if scale else None
+                e["scale_args"] = scale[1] if scale else []
             ckt["elements"].append(e)
         elif kind in "vi":
             e = {"name": name, "kind": kind.upper(), "nodes": toks[1:3]}
