@@ -105,7 +105,6 @@ def test_oracle_matches_golden(case, src, backend):
 
 
 def test_in_scope_cases_are_many():
-    # 41 of the reference's 45 golden netlists use only the engine's element
-    # kinds and analyses (OP, DC sweep, transient, AC); the four others use the
-    # nonlinear and time-varying reactive elements
-    assert sum(1 for c in CASES if not c["skip"]) >= 41
+    # every one of the reference's 45 golden netlists uses only the engine's
+    # element kinds and analyses (OP, DC sweep, transient, AC)
+    assert sum(1 for c in CASES if not c["skip"]) == 45
