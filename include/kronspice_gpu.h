@@ -7,7 +7,8 @@
  *   analysis.OP            analysis/op.go:331        -> ks_op
  *   (*Sim).dcSolve         analysis/newton.go:95     -> ks_op (fallback chain on device)
  *   analysis.Tran          analysis/tran.go:70       -> ks_tran
- *   analysis.DC            analysis/dc.go:51         -> ks_op with per-point source overrides
+ *   analysis.DC            analysis/dc.go:51         -> ks_dc_sweep (the points chained per
+ *                                                       circuit), or ks_op with the points as circuits
  *   analysis.AC            analysis/ac.go:76         -> ks_ac
  *   analysis.Options       analysis/op.go:22-62      -> ks_options
  *   analysis.TranSpec/TranOptions analysis/tran.go:26-40 -> ks_tran_spec
@@ -457,6 +458,24 @@ int ks_ac(ks_batch* b, const ks_options* opt, const double* x0, const double* fr
  * `stream` (NULL: the batch's own stream). */
 int ks_ac_async(ks_batch* b, const ks_options* opt, const double* x0_dev, const double* freqs_dev,
                 int32_t n_freq, double* out_x_dev, int32_t* out_status_dev, int32_t* out_iters_dev, void* stream);
+
+/*
+ * DC sweep of every circuit of the batch (analysis.DC with one swept source,
+ * analysis/dc.go:51-133): element `src` (a V or I source) takes values[0 ..
+ * npts-1] in order as its DC value, and each point is an operating point
+ * warm-started from the previous point's solution and device state (no
+ * InitJct once a point has converged; a switch's state and the junctions'
+ * limiting history carry over), as the reference chains a sweep.  A circuit's
+ * sweep stops at its first failing point.
+ *   out_x      [n_circ][npts][n_unknowns]   (points after a failure: untouched)
+ *   out_status [n_circ]  KS_STATUS_OK, or the failing point's status
+ *   out_points [n_circ]  points solved
+ *   out_iters  [n_circ]  Newton iterations over the sweep
+ * Host buffers; synchronous.  Replaces analysis.DC per circuit (no ledger
+ * check per point).
+ */
+int ks_dc_sweep(ks_batch* b, const ks_options* opt, int32_t src, const double* values, int32_t npts,
+                double* out_x, int32_t* out_status, int32_t* out_points, int32_t* out_iters, void* stream);
 
 /* The sweep alone, about operating points the caller already has (device
  * buffers): x_op_dev [n_circ][n] (a ks_op / ks_op_async result; the small-signal

@@ -299,6 +299,23 @@ class Batch:
                "ks_ac")
         return x[..., 0] + 1j * x[..., 1], st, it
 
+    def dc_sweep(self, src, values, opt=None, stream=None):
+        """analysis.DC with one swept source for every circuit (ks_dc_sweep): element
+        `src` takes `values` in order, each point warm-started from the previous
+        one.  (x [n_circ][n_points][n], status [n_circ], points solved [n_circ],
+        Newton iterations [n_circ])."""
+        o = (opt or Options()).c()
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        if v.ndim != 1 or len(v) == 0:
+            raise ValueError("dc_sweep: values must be a non-empty 1-D array")
+        x = np.zeros((self.n_circ, len(v), self.plan.n))
+        st = np.zeros(self.n_circ, dtype=np.int32)
+        pts = np.zeros(self.n_circ, dtype=np.int32)
+        it = np.zeros(self.n_circ, dtype=np.int32)
+        _check(_lib.load().ks_dc_sweep(self.handle, ctypes.byref(o), int(src), v.ctypes.data, len(v), x.ctypes.data,
+                                       st.ctypes.data, pts.ctypes.data, it.ctypes.data, stream), "ks_dc_sweep")
+        return x, st, pts, it
+
     def ac_async(self, opt, x0_dev, freqs_dev, n_freq, x_dev, status_dev, iters_dev, stream):
         """ks_ac_async on device pointers (ints) on a CUDA stream handle."""
         o = (opt or Options()).c()

@@ -96,6 +96,23 @@ __global__ void __launch_bounds__(T) k_op(KPlan plan, KOpts o, const double* __r
                                        deadline_ns, queue, k32.values ? &k32 : nullptr);
 }
 
+// analysis.DC for every circuit: the sweep's points in order, each warm-started
+// from the previous one (dc_sweep_persistent, ks_newton.cuh).
+template <int T>
+__global__ void __launch_bounds__(T) k_dc_sweep(KPlan plan, KOpts o, const double* __restrict__ values,
+                                                const double* __restrict__ derived, double* state, double* work,
+                                                int64_t B, int src, const double* __restrict__ pts, int npts,
+                                                double* out_x, int32_t* out_status, int32_t* out_points,
+                                                int32_t* out_iters, uint64_t deadline_ns, unsigned long long* queue) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  Thr<SmemSys<T>, RtProg> t;
+  smem_layout<T>(t, plan, smem);
+  t.o = o;
+  __syncthreads();
+  dc_sweep_persistent(t, values, derived, state, work, B, src, pts, npts, out_x, out_status, out_points, out_iters,
+                      deadline_ns, queue);
+}
+
 // Blocks of T threads that keep every SM full (persistent grid), capped by the work.
 template <typename K>
 static unsigned persistent_grid(K kernel, int T, size_t smem, int64_t B) {
@@ -150,5 +167,30 @@ int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, doubl
   };
   if (T == 64) res ? go(k_op<64, true>, 64) : go(k_op<64, false>, 64);
   else res ? go(k_op<32, true>, 32) : go(k_op<32, false>, 32);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int ks_launch_dc_sweep(const KsDeviceBatch& b, const KOpts& o, int src, const double* pts, int npts, double* out_x,
+                       int32_t* out_status, int32_t* out_points, int32_t* out_iters, double deadline_s, void* stream) {
+  const int n = b.plan.n, ne = b.plan.n_elem;
+  if (n > KS_MAX_DENSE) return -2;
+  const uint64_t dl = deadline_s > 0 ? (uint64_t)(deadline_s * 1e9) : 0;
+  int maxSmem = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  int T = 64;
+  size_t sm = ks_sys_smem(n, ne, 64);
+  if (sm > (size_t)maxSmem) { T = 32; sm = ks_sys_smem(n, ne, 32); }
+  if (sm > (size_t)maxSmem) return -2;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemsetAsync(b.queue, 0, sizeof(unsigned long long), st) != cudaSuccess) return -1;
+  auto go = [&](auto kernel, int threads) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    unsigned grid = persistent_grid(kernel, threads, sm, b.B);
+    kernel<<<grid, threads, sm, st>>>(b.plan, o, b.values, b.derived, b.state, b.work, b.B, src, pts, npts, out_x,
+                                      out_status, out_points, out_iters, dl, b.queue);
+  };
+  if (T == 64) go(k_dc_sweep<64>, 64);
+  else go(k_dc_sweep<32>, 32);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

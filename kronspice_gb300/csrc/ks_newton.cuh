@@ -442,4 +442,67 @@ __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* value
   }
 }
 
+// analysis.DC (analysis/dc.go:51-133) of one circuit after another: the swept
+// source `src` (its .DC override, device/source.go:43-66) takes pts[0..npts-1]
+// in order, and each point is an operating point (dcSolve + Accept at ModeOP)
+// warm-started from the previous point's solution and device state, so no
+// InitJct once a point has converged (analysis/newton.go:96) and a switch's
+// state, a junction's limiting history follow the sweep.  The sweep of a circuit
+// stops at its first failing point: out_status[c] is that point's status
+// (KS_STATUS_OK when all converged), out_points[c] the points solved, out_x
+// [B][npts][n] their solutions.
+template <class SY, class P>
+__device__ __forceinline__ void dc_sweep_persistent(Thr<SY, P>& t, const double* values, const double* derived,
+                                                    double* state, double* work, int64_t B, int src,
+                                                    const double* pts, int npts, double* out_x, int32_t* out_status,
+                                                    int32_t* out_points, int32_t* out_iters, uint64_t deadline_ns,
+                                                    unsigned long long* queue) {
+  const uint64_t t0 = deadline_ns ? prog_clock(t.prog) : 0;
+  const KOpts& o = t.o;
+  const int maxTotal = o.max_iter_total > 0 ? o.max_iter_total : 3300 * o.itl1 + 16;
+  LoadParams lp;
+  lp.mode = ModeOP; lp.method = BE; lp.time = 0; lp.h = 0; lp.rh = 0; lp.initJct = false; lp.gmin = o.gmin;
+  lp.srcStepping = false; lp.srcFact = 0;
+  OpState st;
+  for (int64_t c = prog_next(t.prog, queue); c < B; c = prog_next(t.prog, queue)) {
+    thr_bind(t, values, derived, state, work, B, c);
+    init_state(t.prog, t.D, t.Sb);
+    KElem se{};
+    int k = 0;
+    t.prog.each([&](const KElem& e) KS_INLINE_LAMBDA { if (k++ == src) se = e; });
+    const Col S = state_col(t.Sb, se);
+    bool warm = false;
+    int status = KS_STATUS_OK, done = 0, iters = 0;
+    const int n = t.n();
+    for (int p = 0; p < npts && status == KS_STATUS_OK; p++) {
+      S[SV_OVR] = pts[p]; S[SV_OVRON] = 1;  // SetDCOverride, device/source.go:70-73
+      if (warm) { op_state_reset(st, o); st.initJct = false; }
+      else dc_start(t, st, nullptr, c);
+      while (true) {
+        if (deadline_ns && prog_clock(t.prog) - t0 > deadline_ns) { st.status = KS_STATUS_INTERRUPTED; break; }
+        if (o.cancel && (st.total & 7) == 0 && prog_cancelled(t.prog, o.cancel)) { st.status = KS_STATUS_INTERRUPTED; break; }
+        if (st.total >= maxTotal) { st.status = KS_STATUS_NO_CONVERGENCE; break; }
+        const int res = newton_step(t, st, lp);
+        if (res >= 0) dc_advance(t, st, res);
+        if (st.phase == PH_DONE) break;
+      }
+      iters += st.total;
+      status = st.status;
+      if (status != KS_STATUS_OK) break;
+      accept_all(t.prog, t.V, t.D, t.Sb, t.s, 0.0, ModeOP, o.gmin, false);
+      warm = true;
+      done = p + 1;
+      if (out_x) {
+        const int64_t base = ((int64_t)c * npts + p) * n;
+#pragma unroll
+        for (int i = 0; i < n; i++) out_x[base + i] = t.s.xn(i);
+      }
+    }
+    S[SV_OVRON] = 0;  // ClearDCOverride
+    if (out_status) out_status[c] = status;
+    if (out_points) out_points[c] = done;
+    if (out_iters) out_iters[c] = iters;
+  }
+}
+
 }  // namespace ksg

@@ -126,6 +126,42 @@ def test_golden_dc_sweep_points_on_gpu(case):
     assert not gc.compare_sweep(pts, get, sub)
 
 
+@pytest.mark.parametrize("case", DC_CASES, ids=[c["name"] for c in DC_CASES])
+def test_golden_dc_sweep_chained_on_gpu(case):
+    """ks_dc_sweep: the sweep's points in order, each warm-started from the
+    previous one (analysis/dc.go:104-128), against the oracle's chained sweep
+    and the golden table."""
+    ckt = kc.from_dict(case["circuit"])
+    a = case["circuit"]["analyses"][0]
+    pts = gc.sweep_values(a["start"], a["stop"], a["step"])
+    el, v0, _ = ckt.pack()
+    k = ckt.element_index(a["source"])
+    b = analysis.Batch(analysis.Plan(el, ckt.n_nodes, len(v0)), v0[None, :])
+    x, st, npts, it = b.dc_sweep(k, pts, analysis.Options(precision="fp64"))
+    assert st[0] == 0 and npts[0] == len(pts), st
+    ost, ox, _, msg = orc.dc(orc.Packed.of(ckt), k, pts)
+    assert ost == 0, msg
+    _, isv = orc.unknowns(orc.Packed.of(ckt))
+    assert np.all(np.abs(x[0] - ox) <= tol(ox, isv, 1e-6)), np.abs(x[0] - ox).max()
+    want = case["golden"]["independent"]
+    names = [nm for nm in want["names"] if nm.startswith("v(")]
+    if names:
+        def get(nm):
+            i = ckt.node_index(nm[2:-1])
+            return np.zeros(len(pts)) if i == 0 else x[0, :, i - 1]
+        assert not gc.compare_sweep(pts, get, dict(want, names=names))
+
+
+def test_dc_sweep_refusals():
+    ckt = kc.from_dict(DC_CASES[0]["circuit"])
+    el, v0, _ = ckt.pack()
+    b = analysis.Batch(analysis.Plan(el, ckt.n_nodes, len(v0)), v0[None, :])
+    r = [i for i, e in enumerate(ckt.elements) if e.kind == "R"][0]
+    with pytest.raises(Exception) as e:
+        b.dc_sweep(r, [0.0, 1.0])
+    assert "swept source not found" in str(e.value)
+
+
 def test_typed_errors():
     # TestSingularVoltageLoop, analysis/op_test.go:87: two sources in parallel
     b = kc.Builder("loop")

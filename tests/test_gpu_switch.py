@@ -214,3 +214,43 @@ def test_multi_topology_batch_with_switches():
     r = orc.tran(orc.Packed.of(circuits[1]), ospec_, orc.options(reltol=RELTOL))
     assert r[0] == 0
     assert np.allclose(waves[1], r[2], rtol=1e-6, atol=1e-9)
+
+
+def test_hysteresis_loop_as_a_chained_sweep():
+    """A batch of switches with seeded thresholds and hysteresis swept up and back
+    down (ks_dc_sweep): inside the band each point keeps the state the previous
+    point left, so the way down differs from the way up, as in the oracle's
+    chained analysis.DC."""
+    b = kc.Builder("loop")
+    b.voltage_source("V1", "ctl", "0", 0.0)
+    b.voltage_source("V2", "dd", "0", 5.0)
+    b.resistor("R1", "dd", "out", 1e3)
+    b.model("sw", "sw", {"vt": 1.0, "vh": 0.2, "ron": 1.0, "roff": 1e6})
+    b.vswitch("S1", "out", "0", "ctl", "0", "sw")
+    b.resistor("RC", "ctl", "s", 1e3).voltage_source("VS", "s", "0", 0.0)
+    b.model("cs", "csw", {"it": 1e-3, "ih": 2e-4, "ron": 5.0, "roff": 1e6})
+    b.resistor("R2", "dd", "o2", 1e3).iswitch("W1", "o2", "0", "VS", "cs")
+    ckt = b.build()
+    el, v0, _ = ckt.pack()
+    g = np.random.default_rng(9)
+    n = 512
+    vals = np.tile(v0, (n, 1))
+    for name in ("S1", "W1"):
+        col = int(el[ckt.element_index(name)]["param"])
+        vals[:, col] *= g.uniform(0.7, 1.3, n)
+        vals[:, col + 1] *= g.uniform(0.5, 1.5, n)
+    pts = np.concatenate([np.linspace(0, 2, 41), np.linspace(2, 0, 41)[1:]])
+    src = ckt.element_index("V1")
+    bt = analysis.Batch(analysis.Plan(el, ckt.n_nodes, vals.shape[1]), vals)
+    x, st, npts, it = bt.dc_sweep(src, pts, analysis.Options(precision="fp64"))
+    assert np.all(st == 0) and np.all(npts == len(pts))
+    out = ckt.node_index("out") - 1
+    up, down = x[:, :41, out], x[:, 40:, out][:, ::-1]
+    assert np.any(np.abs(up - down) > 1.0)  # the loop is open inside the band
+    pk = orc.Packed(el, ckt.n_nodes, vals[0])
+    for c in range(0, n, 29):
+        pk.values[:] = vals[c]
+        ost, ox, _, msg = orc.dc(pk, src, pts)
+        assert ost == 0, msg
+        assert np.allclose(x[c], ox, rtol=1e-9, atol=1e-12), c
+
