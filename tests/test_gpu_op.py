@@ -156,7 +156,7 @@ def test_dc_sweep_refusals():
     ckt = kc.from_dict(DC_CASES[0]["circuit"])
     el, v0, _ = ckt.pack()
     b = analysis.Batch(analysis.Plan(el, ckt.n_nodes, len(v0)), v0[None, :])
-    r = [i for i, e in enumerate(ckt.elements) if e.kind == "R"][0]
+    r = [i for i, e in enumerate(ckt.elements) if e.kind not in ("V", "I")][0]
     with pytest.raises(Exception) as e:
         b.dc_sweep(r, [0.0, 1.0])
     assert "swept source not found" in str(e.value)
