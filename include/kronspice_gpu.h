@@ -460,14 +460,15 @@ int ks_ac_async(ks_batch* b, const ks_options* opt, const double* x0_dev, const 
                 int32_t n_freq, double* out_x_dev, int32_t* out_status_dev, int32_t* out_iters_dev, void* stream);
 
 /*
- * DC sweep of every circuit of the batch (analysis.DC with one swept source,
- * analysis/dc.go:51-133): element `src` (a V or I source) takes values[0 ..
- * npts-1] in order as its DC value, and each point is an operating point
+ * DC sweep of every circuit of the batch (analysis.DC, analysis/dc.go:51-133):
+ * element `src` (a V or I source) takes values[0 .. npts-1] in order as its DC
+ * value, for each of values2[0 .. npts2-1] of a second, outer source src2 in
+ * turn (src2 < 0: one sweep), and each point is an operating point
  * warm-started from the previous point's solution and device state (no
  * InitJct once a point has converged; a switch's state and the junctions'
  * limiting history carry over), as the reference chains a sweep.  A circuit's
- * sweep stops at its first failing point.
- *   out_x      [n_circ][npts][n_unknowns]   (points after a failure: untouched)
+ * sweep stops at its first failing point.  At most 1,000,000 points.
+ *   out_x      [n_circ][npts2][npts][n_unknowns]   (after a failure: untouched)
  *   out_status [n_circ]  KS_STATUS_OK, or the failing point's status
  *   out_points [n_circ]  points solved
  *   out_iters  [n_circ]  Newton iterations over the sweep
@@ -475,7 +476,8 @@ int ks_ac_async(ks_batch* b, const ks_options* opt, const double* x0_dev, const 
  * check per point).
  */
 int ks_dc_sweep(ks_batch* b, const ks_options* opt, int32_t src, const double* values, int32_t npts,
-                double* out_x, int32_t* out_status, int32_t* out_points, int32_t* out_iters, void* stream);
+                int32_t src2, const double* values2, int32_t npts2, double* out_x, int32_t* out_status,
+                int32_t* out_points, int32_t* out_iters, void* stream);
 
 /* The sweep alone, about operating points the caller already has (device
  * buffers): x_op_dev [n_circ][n] (a ks_op / ks_op_async result; the small-signal

@@ -104,7 +104,8 @@ def load(build_if_missing=False):
     L.ks_ac.argtypes = [P, P, P, P, ctypes.c_int32, P, P, P, P]
     L.ks_ac_async.argtypes = [P, P, P, P, ctypes.c_int32, P, P, P, P]
     L.ks_ac_at.argtypes = [P, P, P, P, P, ctypes.c_int32, P, P, P]
-    L.ks_dc_sweep.argtypes = [P, P, ctypes.c_int32, P, ctypes.c_int32, P, P, P, P, P]
+    L.ks_dc_sweep.argtypes = [P, P, ctypes.c_int32, P, ctypes.c_int32, ctypes.c_int32, P, ctypes.c_int32, P, P, P,
+                              P, P]
     L.ks_torn_create.argtypes = [P, ctypes.c_int32, P, P, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]
     L.ks_torn_destroy.argtypes = [P]
     L.ks_torn_destroy.restype = None

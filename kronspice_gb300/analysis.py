@@ -299,21 +299,26 @@ class Batch:
                "ks_ac")
         return x[..., 0] + 1j * x[..., 1], st, it
 
-    def dc_sweep(self, src, values, opt=None, stream=None):
-        """analysis.DC with one swept source for every circuit (ks_dc_sweep): element
-        `src` takes `values` in order, each point warm-started from the previous
-        one.  (x [n_circ][n_points][n], status [n_circ], points solved [n_circ],
-        Newton iterations [n_circ])."""
+    def dc_sweep(self, src, values, opt=None, src2=None, values2=None, stream=None):
+        """analysis.DC for every circuit (ks_dc_sweep): element `src` takes `values`
+        in order (for each of `values2` of an outer source `src2` in turn), each
+        point warm-started from the previous one.  (x [n_circ][n_points][n], with
+        the inner source stepping fastest, status [n_circ], points solved
+        [n_circ], Newton iterations [n_circ])."""
         o = (opt or Options()).c()
         v = np.ascontiguousarray(values, dtype=np.float64)
         if v.ndim != 1 or len(v) == 0:
             raise ValueError("dc_sweep: values must be a non-empty 1-D array")
-        x = np.zeros((self.n_circ, len(v), self.plan.n))
+        v2 = None if src2 is None else np.ascontiguousarray(values2, dtype=np.float64)
+        total = len(v) * (1 if v2 is None else len(v2))
+        x = np.zeros((self.n_circ, total, self.plan.n))
         st = np.zeros(self.n_circ, dtype=np.int32)
         pts = np.zeros(self.n_circ, dtype=np.int32)
         it = np.zeros(self.n_circ, dtype=np.int32)
-        _check(_lib.load().ks_dc_sweep(self.handle, ctypes.byref(o), int(src), v.ctypes.data, len(v), x.ctypes.data,
-                                       st.ctypes.data, pts.ctypes.data, it.ctypes.data, stream), "ks_dc_sweep")
+        _check(_lib.load().ks_dc_sweep(self.handle, ctypes.byref(o), int(src), v.ctypes.data, len(v),
+                                       -1 if v2 is None else int(src2), None if v2 is None else v2.ctypes.data,
+                                       0 if v2 is None else len(v2), x.ctypes.data, st.ctypes.data, pts.ctypes.data,
+                                       it.ctypes.data, stream), "ks_dc_sweep")
         return x, st, pts, it
 
     def ac_async(self, opt, x0_dev, freqs_dev, n_freq, x_dev, status_dev, iters_dev, stream):

@@ -478,30 +478,41 @@ extern "C" int ks_op_results(ks_batch* b, const ks_options* opt, const double* x
 }
 
 extern "C" int ks_dc_sweep(ks_batch* b, const ks_options* opt, int32_t src, const double* values, int32_t npts,
-                           double* out_x, int32_t* out_status, int32_t* out_points, int32_t* out_iters, void* stream) {
-  if (!b || !values || npts <= 0 || npts > 1000000) { set_error("ks_dc_sweep: bad argument"); return KS_EINVAL; }
+                           int32_t src2, const double* values2, int32_t npts2, double* out_x, int32_t* out_status,
+                           int32_t* out_points, int32_t* out_iters, void* stream) {
+  const bool nested = src2 >= 0;
+  if (!b || !values || npts <= 0 || (nested && (!values2 || npts2 <= 0)) ||
+      (int64_t)npts * (nested ? npts2 : 1) > 1000000) {  // analysis.MaxDCPoints
+    set_error("ks_dc_sweep: bad argument");
+    return KS_EINVAL;
+  }
   const ksh::HostPlan& hp = b->plan->hp;
-  if (src < 0 || src >= hp.n_elem || (hp.src[src].kind != KS_ELEM_V && hp.src[src].kind != KS_ELEM_I)) {
+  auto source = [&](int e) { return e >= 0 && e < hp.n_elem && (hp.src[e].kind == KS_ELEM_V || hp.src[e].kind == KS_ELEM_I); };
+  if (!source(src) || (nested && (!source(src2) || src2 == src))) {
     set_error("analysis: swept source not found");  // analysis.ErrUnknownSource, analysis/dc.go:66-76
     return KS_EINVAL;
   }
   cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
-  const int64_t B = b->B, n = hp.n;
-  const size_t xb = sizeof(double) * (size_t)B * npts * n, pb = sizeof(double) * npts, ib = sizeof(int32_t) * B;
+  const int64_t B = b->B, n = hp.n, total = (int64_t)npts * (nested ? npts2 : 1);
+  const size_t xb = sizeof(double) * (size_t)B * total * n, pb = sizeof(double) * (npts + (nested ? npts2 : 0));
+  const size_t ib = sizeof(int32_t) * B;
   char* d = nullptr;
   if (cudaMalloc(&d, xb + pb + 3 * ib + 64) != cudaSuccess) { set_error("ks_dc_sweep: device allocation failed"); return KS_ENOMEM; }
   double* d_x = reinterpret_cast<double*>(d);
   double* d_pts = reinterpret_cast<double*>(d + xb);
+  double* d_pts2 = nested ? d_pts + npts : nullptr;
   int32_t* d_status = reinterpret_cast<int32_t*>(d + xb + pb);
   int32_t* d_points = d_status + B;
   int32_t* d_iters = d_points + B;
   KOpts o = make_opts(opt);
   o.cancel = b->d_cancel;
   int rc = batch_setup(b, 0.0, 0.0, st);
-  if (!rc && cudaMemcpyAsync(d_pts, values, pb, cudaMemcpyHostToDevice, st) != cudaSuccess) rc = KS_ECUDA;
+  if (!rc && cudaMemcpyAsync(d_pts, values, sizeof(double) * npts, cudaMemcpyHostToDevice, st) != cudaSuccess) rc = KS_ECUDA;
+  if (!rc && nested && cudaMemcpyAsync(d_pts2, values2, sizeof(double) * npts2, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    rc = KS_ECUDA;
   if (!rc) {
-    const int lr = ks_launch_dc_sweep(b->dev, o, src, d_pts, npts, d_x, d_status, d_points, d_iters,
-                                      opt ? opt->deadline_s : 0.0, st);
+    const int lr = ks_launch_dc_sweep(b->dev, o, src, d_pts, npts, nested ? src2 : -1, d_pts2, nested ? npts2 : 0, d_x,
+                                      d_status, d_points, d_iters, opt ? opt->deadline_s : 0.0, st);
     if (lr == -2) { set_error("ks_dc_sweep: system too large for the dense kernels"); rc = KS_EUNSUPPORTED; }
     else if (lr) { set_error(std::string("ks_dc_sweep: kernel launch failed: ") + cudaGetErrorString(cudaGetLastError())); rc = KS_ECUDA; }
   }

@@ -69,8 +69,9 @@ int circuits_per_thread();
 int ks_launch_tran(const KsDeviceBatch& b, const KOpts& o, const ks_tran_spec& spec, int cap, double* out_time,
                    double* out_wave, int32_t* out_npts, int32_t* out_status, int32_t* out_steps, int32_t* out_iters,
                    double deadline_s, void* stream, const KsSpec* kspec);
-int ks_launch_dc_sweep(const KsDeviceBatch& b, const KOpts& o, int src, const double* pts, int npts, double* out_x,
-                       int32_t* out_status, int32_t* out_points, int32_t* out_iters, double deadline_s, void* stream);
+int ks_launch_dc_sweep(const KsDeviceBatch& b, const KOpts& o, int src, const double* pts, int npts, int src2,
+                       const double* pts2, int npts2, double* out_x, int32_t* out_status, int32_t* out_points,
+                       int32_t* out_iters, double deadline_s, void* stream);
 int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, double* out_x, int32_t* out_status,
                  int32_t* out_iters, double deadline_s, void* stream, const KsSpec* kspec);
 // AC sweep after the operating point x_op [B][n] (ks_ac.cu): G / C / b columns in

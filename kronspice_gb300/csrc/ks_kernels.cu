@@ -102,6 +102,7 @@ template <int T>
 __global__ void __launch_bounds__(T) k_dc_sweep(KPlan plan, KOpts o, const double* __restrict__ values,
                                                 const double* __restrict__ derived, double* state, double* work,
                                                 int64_t B, int src, const double* __restrict__ pts, int npts,
+                                                int src2, const double* __restrict__ pts2, int npts2,
                                                 double* out_x, int32_t* out_status, int32_t* out_points,
                                                 int32_t* out_iters, uint64_t deadline_ns, unsigned long long* queue) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -109,8 +110,8 @@ __global__ void __launch_bounds__(T) k_dc_sweep(KPlan plan, KOpts o, const doubl
   smem_layout<T>(t, plan, smem);
   t.o = o;
   __syncthreads();
-  dc_sweep_persistent(t, values, derived, state, work, B, src, pts, npts, out_x, out_status, out_points, out_iters,
-                      deadline_ns, queue);
+  dc_sweep_persistent(t, values, derived, state, work, B, src, pts, npts, src2, pts2, npts2, out_x, out_status,
+                      out_points, out_iters, deadline_ns, queue);
 }
 
 // Blocks of T threads that keep every SM full (persistent grid), capped by the work.
@@ -170,8 +171,9 @@ int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, doubl
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int ks_launch_dc_sweep(const KsDeviceBatch& b, const KOpts& o, int src, const double* pts, int npts, double* out_x,
-                       int32_t* out_status, int32_t* out_points, int32_t* out_iters, double deadline_s, void* stream) {
+int ks_launch_dc_sweep(const KsDeviceBatch& b, const KOpts& o, int src, const double* pts, int npts, int src2,
+                       const double* pts2, int npts2, double* out_x, int32_t* out_status, int32_t* out_points,
+                       int32_t* out_iters, double deadline_s, void* stream) {
   const int n = b.plan.n, ne = b.plan.n_elem;
   if (n > KS_MAX_DENSE) return -2;
   const uint64_t dl = deadline_s > 0 ? (uint64_t)(deadline_s * 1e9) : 0;
@@ -187,8 +189,8 @@ int ks_launch_dc_sweep(const KsDeviceBatch& b, const KOpts& o, int src, const do
   auto go = [&](auto kernel, int threads) {
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     unsigned grid = persistent_grid(kernel, threads, sm, b.B);
-    kernel<<<grid, threads, sm, st>>>(b.plan, o, b.values, b.derived, b.state, b.work, b.B, src, pts, npts, out_x,
-                                      out_status, out_points, out_iters, dl, b.queue);
+    kernel<<<grid, threads, sm, st>>>(b.plan, o, b.values, b.derived, b.state, b.work, b.B, src, pts, npts, src2,
+                                      pts2, npts2, out_x, out_status, out_points, out_iters, dl, b.queue);
   };
   if (T == 64) go(k_dc_sweep<64>, 64);
   else go(k_dc_sweep<32>, 32);

@@ -444,17 +444,19 @@ __device__ __forceinline__ void op_persistent(Thr<SY, P>& t, const double* value
 
 // analysis.DC (analysis/dc.go:51-133) of one circuit after another: the swept
 // source `src` (its .DC override, device/source.go:43-66) takes pts[0..npts-1]
-// in order, and each point is an operating point (dcSolve + Accept at ModeOP)
+// in order (for each value of a second, outer source src2 >= 0 in turn), and
+// each point is an operating point (dcSolve + Accept at ModeOP)
 // warm-started from the previous point's solution and device state, so no
 // InitJct once a point has converged (analysis/newton.go:96) and a switch's
 // state, a junction's limiting history follow the sweep.  The sweep of a circuit
 // stops at its first failing point: out_status[c] is that point's status
 // (KS_STATUS_OK when all converged), out_points[c] the points solved, out_x
-// [B][npts][n] their solutions.
+// [B][npts2][npts][n] their solutions.
 template <class SY, class P>
 __device__ __forceinline__ void dc_sweep_persistent(Thr<SY, P>& t, const double* values, const double* derived,
                                                     double* state, double* work, int64_t B, int src,
-                                                    const double* pts, int npts, double* out_x, int32_t* out_status,
+                                                    const double* pts, int npts, int src2, const double* pts2,
+                                                    int npts2, double* out_x, int32_t* out_status,
                                                     int32_t* out_points, int32_t* out_iters, uint64_t deadline_ns,
                                                     unsigned long long* queue) {
   const uint64_t t0 = deadline_ns ? prog_clock(t.prog) : 0;
@@ -467,15 +469,22 @@ __device__ __forceinline__ void dc_sweep_persistent(Thr<SY, P>& t, const double*
   for (int64_t c = prog_next(t.prog, queue); c < B; c = prog_next(t.prog, queue)) {
     thr_bind(t, values, derived, state, work, B, c);
     init_state(t.prog, t.D, t.Sb);
-    KElem se{};
+    KElem se{}, se2{};
     int k = 0;
-    t.prog.each([&](const KElem& e) KS_INLINE_LAMBDA { if (k++ == src) se = e; });
-    const Col S = state_col(t.Sb, se);
+    t.prog.each([&](const KElem& e) KS_INLINE_LAMBDA {
+      if (k == src) se = e;
+      if (k == src2) se2 = e;
+      k++;
+    });
+    const Col S = state_col(t.Sb, se), S2 = state_col(t.Sb, se2);
     bool warm = false;
     int status = KS_STATUS_OK, done = 0, iters = 0;
-    const int n = t.n();
-    for (int p = 0; p < npts && status == KS_STATUS_OK; p++) {
-      S[SV_OVR] = pts[p]; S[SV_OVRON] = 1;  // SetDCOverride, device/source.go:70-73
+    const int n = t.n(), total = npts * (src2 >= 0 ? npts2 : 1);
+    for (int p = 0; p < total && status == KS_STATUS_OK; p++) {
+      // the inner source steps fastest; the outer one (a second sweep) holds each
+      // of its values through a whole inner sweep (analysis/dc.go:105-111)
+      if (src2 >= 0) { S2[SV_OVR] = pts2[p / npts]; S2[SV_OVRON] = 1; }
+      S[SV_OVR] = pts[p % npts]; S[SV_OVRON] = 1;  // SetDCOverride, device/source.go:70-73
       if (warm) { op_state_reset(st, o); st.initJct = false; }
       else dc_start(t, st, nullptr, c);
       while (true) {
@@ -493,12 +502,13 @@ __device__ __forceinline__ void dc_sweep_persistent(Thr<SY, P>& t, const double*
       warm = true;
       done = p + 1;
       if (out_x) {
-        const int64_t base = ((int64_t)c * npts + p) * n;
+        const int64_t base = ((int64_t)c * total + p) * n;
 #pragma unroll
         for (int i = 0; i < n; i++) out_x[base + i] = t.s.xn(i);
       }
     }
     S[SV_OVRON] = 0;  // ClearDCOverride
+    if (src2 >= 0) S2[SV_OVRON] = 0;
     if (out_status) out_status[c] = status;
     if (out_points) out_points[c] = done;
     if (out_iters) out_iters[c] = iters;

@@ -744,17 +744,23 @@ extern "C" int kso_ac(const ks_topology* t, const double* values, const ks_optio
   return e;
 }
 
-extern "C" int kso_dc(const ks_topology* t, const double* values, const ks_options* o, int src,
-                      const double* vals, int npts, double* x_out, double* i_out, char* err, int errlen) {
+extern "C" int kso_dc2(const ks_topology* t, const double* values, const ks_options* o, int src,
+                       const double* vals, int npts, int src2, const double* vals2, int npts2, double* x_out,
+                       double* i_out, char* err, int errlen) {
   Sim s;
   Opts opt(o);
   if (s.build(t, values, 0, 0, opt.backend)) { copyMsg(s.msg, err, errlen); return KS_STATUS_NOT_RUN; }
-  if (src < 0 || src >= (int)s.devs.size()) { copyMsg("analysis: swept source not found", err, errlen); return KS_STATUS_NOT_RUN; }
-  for (int k = 0; k < npts; k++) {  // analysis/dc.go:104-128: one OP per point, warm-started
-    s.devs[src]->setDCOverride(vals[k]);
+  if (src < 0 || src >= (int)s.devs.size() || src2 >= (int)s.devs.size()) {
+    copyMsg("analysis: swept source not found", err, errlen);
+    return KS_STATUS_NOT_RUN;
+  }
+  const int total = npts * (src2 >= 0 ? npts2 : 1);
+  for (int k = 0; k < total; k++) {  // analysis/dc.go:104-128: one OP per point, warm-started
+    if (src2 >= 0) s.devs[src2]->setDCOverride(vals2[k / npts]);  // the outer sweep, :105-108
+    s.devs[src]->setDCOverride(vals[k % npts]);
     int e = s.op(opt, nullptr);
     if (e) {
-      char buf[64]; snprintf(buf, sizeof buf, "sweep = %g: ", vals[k]);
+      char buf[64]; snprintf(buf, sizeof buf, "sweep = %g: ", vals[k % npts]);
       copyMsg(buf + s.msg, err, errlen);
       return e;
     }
@@ -762,7 +768,13 @@ extern "C" int kso_dc(const ks_topology* t, const double* values, const ks_optio
     if (i_out) for (size_t i = 0; i < s.devs.size(); i++) i_out[(size_t)k * s.devs.size() + i] = s.devs[i]->current(s.x.data());
   }
   s.devs[src]->clearDCOverride();
+  if (src2 >= 0) s.devs[src2]->clearDCOverride();
   return E_OK;
+}
+
+extern "C" int kso_dc(const ks_topology* t, const double* values, const ks_options* o, int src,
+                      const double* vals, int npts, double* x_out, double* i_out, char* err, int errlen) {
+  return kso_dc2(t, values, o, src, vals, npts, -1, nullptr, 0, x_out, i_out, err, errlen);
 }
 
 extern "C" int kso_tran(const ks_topology* t, const double* values, const ks_tran_spec* spec,

@@ -64,6 +64,8 @@ def lib():
         P = ctypes.c_void_p
         L.kso_op.argtypes = [P, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
         L.kso_dc.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, P, P, ctypes.c_char_p, ctypes.c_int]
+        L.kso_dc2.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, P,
+                              ctypes.c_char_p, ctypes.c_int]
         L.kso_tran.argtypes = [P, P, P, P, ctypes.c_int, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
         L.kso_op_results.argtypes = [P, P, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
         L.kso_sparse_order.argtypes = [P, P, P, P, P, P, P]
@@ -209,6 +211,21 @@ def dc(pk, src, vals, opt=None):
     o = opt or options()
     st = lib().kso_dc(pk.tref(), _ptr(pk.values), ctypes.byref(o), src, _ptr(vals), len(vals), _ptr(x),
                       _ptr(cur), err, 512)
+    return st, x, cur, err.value.decode()
+
+
+def dc2(pk, src, vals, src2, vals2, opt=None):
+    """analysis.DC with a second, outer source (the inner one stepping fastest)."""
+    n, _ = unknowns(pk)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    vals2 = np.ascontiguousarray(vals2, dtype=np.float64)
+    total = len(vals) * len(vals2)
+    x = np.zeros((total, n))
+    cur = np.zeros((total, len(pk.elements)))
+    err = ctypes.create_string_buffer(512)
+    o = opt or options()
+    st = lib().kso_dc2(pk.tref(), _ptr(pk.values), ctypes.byref(o), src, _ptr(vals), len(vals), src2, _ptr(vals2),
+                       len(vals2), _ptr(x), _ptr(cur), err, 512)
     return st, x, cur, err.value.decode()
 
 

@@ -152,6 +152,35 @@ def test_golden_dc_sweep_chained_on_gpu(case):
         assert not gc.compare_sweep(pts, get, dict(want, names=names))
 
 
+@pytest.mark.parametrize("name,inner,outer,vals2", [
+    ("bjt_output_dc", "VCE", "IB", [5e-6, 10e-6, 20e-6, 40e-6]),
+    ("mos1_idvd_dc", "VDS", "VGS", [1.0, 1.5, 2.5, 4.0]),
+])
+def test_nested_dc_sweep_on_gpu(name, inner, outer, vals2):
+    """A second, outer swept source (analysis/dc.go:100-111): the family of
+    output characteristics in one chained sweep, against the oracle's."""
+    case = [c for c in DC_CASES if c["name"] == name][0]
+    ckt = kc.from_dict(case["circuit"])
+    a = case["circuit"]["analyses"][0]
+    pts = gc.sweep_values(a["start"], a["stop"], a["step"])
+    el, v0, _ = ckt.pack()
+    k, k2 = ckt.element_index(inner), ckt.element_index(outer)
+    b = analysis.Batch(analysis.Plan(el, ckt.n_nodes, len(v0)), v0[None, :])
+    x, st, npts, it = b.dc_sweep(k, pts, analysis.Options(precision="fp64"), src2=k2, values2=vals2)
+    assert st[0] == 0 and npts[0] == len(pts) * len(vals2), st
+    ost, ox, _, msg = orc.dc2(orc.Packed.of(ckt), k, pts, k2, vals2)
+    assert ost == 0, msg
+    _, isv = orc.unknowns(orc.Packed.of(ckt))
+    assert np.all(np.abs(x[0] - ox) <= tol(ox, isv, 1e-6)), np.abs(x[0] - ox).max()
+    # the last outer value's inner sweep is the single sweep at that value (to
+    # the Newton tolerance: the two start each point from different iterates)
+    v1 = v0.copy()
+    v1[int(el[k2]["param"])] = vals2[-1]
+    ost1, ox1, _, _ = orc.dc(orc.Packed(el, ckt.n_nodes, v1), k, pts)
+    assert ost1 == 0
+    assert np.all(np.abs(x[0, -len(pts):] - ox1) <= tol(ox1, isv, 1e-3))
+
+
 def test_dc_sweep_refusals():
     ckt = kc.from_dict(DC_CASES[0]["circuit"])
     el, v0, _ = ckt.pack()
