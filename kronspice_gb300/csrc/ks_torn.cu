@@ -107,6 +107,11 @@ __global__ void k_tl_init_mos(KPlan plan, const double* derived, double* state, 
   const int e = (int)(t / V), v = (int)(t % V);
   const KElem el = plan.elem[e];
   if (el.kind == KS_ELEM_M) state[(int64_t)(el.state + SM_AVON) * V + v] = derived[(int64_t)(el.derived + DM_VTO) * V + v];
+  if (el.kind == KS_ELEM_S || el.kind == KS_ELEM_W) {  // the ON / OFF initial state, device/switch.go:105-106
+    const double on = derived[(int64_t)(el.derived + DW_INIT) * V + v];
+    state[(int64_t)(el.state + SW_ON) * V + v] = on;
+    state[(int64_t)(el.state + SW_ACC) * V + v] = on;
+  }
 }
 
 // One Load per (element, variant) into J and rhs at the linearization point xo.
@@ -1445,7 +1450,9 @@ int build_plan(ks_torn* T, const ks_topology* topo, const int32_t* torn, int n_t
   std::vector<int32_t> nonlin;
   for (int e = 0; e < hp.n_elem; e++) {
     const int k = hp.elem[e].kind;
-    if (k == KS_ELEM_D || k == KS_ELEM_Q || k == KS_ELEM_M) nonlin.push_back(e);
+    if (k == KS_ELEM_D || k == KS_ELEM_Q || k == KS_ELEM_M || k == KS_ELEM_S || k == KS_ELEM_W ||
+        ((k == KS_ELEM_CN || k == KS_ELEM_LN) && hp.elem[e].level > 0))  // the curved laws
+      nonlin.push_back(e);
   }
   T->n_nonlin = (int)nonlin.size();
   T->h_pieceOf = pieceOf;
@@ -1863,13 +1870,18 @@ extern "C" int ks_torn_create(const ks_topology* topo, int32_t n_variants, const
   std::string err;
   int rc = ksh::plan_layout(topo, &T->hp, &err);
   if (rc) { set_error(err); delete T; return rc; }
-  for (const KElem& e : T->hp.elem)
-    if (e.kind == KS_ELEM_S || e.kind == KS_ELEM_W || e.kind == KS_ELEM_CN || e.kind == KS_ELEM_LN) {
-      // no step limiter, state restart or knot breakpoints in the torn transient
-      set_error("ks_torn_create: switches and nonlinear or time-varying C and L are not supported by the torn engine");
-      delete T;
-      return KS_EUNSUPPORTED;
-    }
+  for (int k = 0; k < T->hp.n_elem; k++) {
+    const KElem& e = T->hp.elem[k];
+    if (e.kind != KS_ELEM_S && e.kind != KS_ELEM_W) continue;
+    // a smooth switch stamps its transconductance on entries the plan (made
+    // without values) does not hold; the abrupt switch stamps its conductance only
+    for (int v = 0; v < n_variants; v++)
+      if (values[(size_t)v * T->hp.n_values + e.param + KS_SW_P_VH] < 0) {
+        set_error("ks_torn_create: smooth switches (negative hysteresis) are not supported by the torn engine");
+        delete T;
+        return KS_EUNSUPPORTED;
+      }
+  }
   T->V = n_variants;
   rc = build_plan(T, topo, torn_elems, n_torn, &err);
   if (rc) { set_error(err); delete T; return rc; }

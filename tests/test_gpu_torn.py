@@ -216,3 +216,33 @@ def test_step_predictor_on_the_power_grid():
         assert r[0] == 0, r[-1]
         xo = r[2]
         assert np.all(np.abs(w6[:, v, :] - xo[:, probes]) <= 1e-6 * np.abs(xo[:, probes]) + 2e-6)
+
+
+@pytest.mark.parametrize("name,cut", [("switch_rc_tran", "R1"), ("nlcap_tran", "R1"), ("varind_tran", "R1"),
+                                      ("nlind_tran", "R1")])
+def test_switches_and_nonlinear_reactive_torn(name, cut):
+    """Switches (abrupt) and the nonlinear / time-varying C and L in the torn
+    engine's fixed-step transient: four seeded variants of a golden netlist torn
+    along a resistor match the oracle's untorn runs."""
+    case = [c for c in json.load(open(os.path.join(HERE, "golden", "reference_cases.json")))["cases"]
+            if c["name"] == name][0]
+    ckt = kc.from_dict(case["circuit"])
+    el, v0, _ = ckt.pack()
+    g = np.random.default_rng(12)
+    vals = np.tile(v0, (4, 1))
+    for k, e in enumerate(ckt.elements):
+        if e.kind == "R":
+            vals[:, int(el[k]["param"])] *= g.uniform(0.8, 1.25, 4)
+    tb = analysis.TornBatch(el, ckt.n_nodes, vals, [ckt.element_index(cut)])
+    nsteps = 400
+    spec = analysis.TranSpec(step=5e-6, stop=nsteps * 5e-6, fixed_step=True, method="be")
+    probes = np.arange(tb.n)
+    wave, x, st, steps, it, stats = tb.tran(spec, analysis.Options(reltol=1e-6), probes=probes)
+    assert np.all(st == 0) and np.all(steps == nsteps), (st, steps)
+    ospec = orc.TranSpec(5e-6, nsteps * 5e-6, 0.0, 0.0, 0, 1, 1, 0, 0.0, 0.0, 0.0)
+    for v in range(len(vals)):
+        r = orc.tran(orc.Packed(el, ckt.n_nodes, vals[v]), ospec, orc.options(reltol=1e-6))
+        assert r[0] == 0, r[-1]
+        scale = np.abs(r[2]).max(axis=0) + 1e-12
+        assert np.all(np.abs(wave[:, v, :] - r[2]) <= 1e-6 * scale), (v, np.abs(wave[:, v, :] - r[2]).max())
+

@@ -145,7 +145,8 @@ def test_switch_validation_on_the_host():
 
 def test_tearing_a_switch():
     """tearTerminals (kron/jacobian.go:136-170): an S switch tears with its
-    control nodes, a W switch is refused; the torn engine takes no switches."""
+    control nodes, a W switch is refused; the torn engine refuses a smooth
+    switch (its transconductance entries are not in the values-free plan)."""
     b = kc.Builder("tear")
     b.voltage_source("V1", "a", "0", 1.0)
     b.resistor("R1", "a", "b", 1e3).resistor("R2", "b", "0", 1e3)
@@ -163,6 +164,7 @@ def test_tearing_a_switch():
     st, pairs, msg = orc.torn_cuts(pk, [c.element_index("W1")])
     assert st != 0 and "branch-current unknown" in msg
     el, vals, _ = c.pack()
+    vals[int(el[c.element_index("S1")]["param"]) + 1] = -0.1  # VH < 0: the smooth switch
     with pytest.raises(RuntimeError) as e:
         analysis.TornBatch(el, c.n_nodes, vals[None, :], [c.element_index("R1")])
-    assert "switches" in str(e.value)
+    assert "smooth switches" in str(e.value)
