@@ -179,27 +179,44 @@ __global__ void k_targets(const double* __restrict__ x, int n, const int32_t* __
 // MSE gradient dY = 2 (Y - T) / rows_valid on the valid block, bf16; loss partials.
 __global__ void k_loss_grad(const float* __restrict__ Y, const float* __restrict__ T, int dout, int dop, int rows_valid,
                             __nv_bfloat16* dY, int rows, float* loss) {
-  int r = blockIdx.x * blockDim.y + threadIdx.y;
-  if (r >= rows) return;
+  const int r = blockIdx.x * blockDim.y + threadIdx.y;
   float l = 0.f;
-  for (int j = threadIdx.x; j < dop; j += blockDim.x) {
-    float g = 0.f;
-    if (r < rows_valid && j < dout) {
-      float e = Y[(size_t)r * dop + j] - T[(size_t)r * dop + j];
-      l += e * e;
-      g = 2.f * e / rows_valid;
+  if (r < rows) {
+    for (int j = threadIdx.x; j < dop; j += blockDim.x) {
+      float g = 0.f;
+      if (r < rows_valid && j < dout) {
+        float e = Y[(size_t)r * dop + j] - T[(size_t)r * dop + j];
+        l += e * e;
+        g = 2.f * e / rows_valid;
+      }
+      dY[(size_t)r * dop + j] = __float2bfloat16(g);
     }
-    dY[(size_t)r * dop + j] = __float2bfloat16(g);
   }
-  if (loss) atomicAdd(loss, l / (rows_valid * (float)dout));
+  // one atomic per block: the squared errors summed over the block's warps
+  // (one per thread serialized on the single loss word)
+  __shared__ float part[32];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
+  if ((tid & 31) == 0) part[tid >> 5] = l;
+  __syncthreads();
+  if (tid == 0 && loss) {
+    float sum = 0.f;
+    for (int w = 0; w < (nthr + 31) / 32; w++) sum += part[w];
+    atomicAdd(loss, sum / (rows_valid * (float)dout));
+  }
 }
 
-// Column sums of dY (bias gradients): db[j] += sum_r dY[r][j].
+// Column sums of dY (bias gradients): db[j] += sum_r dY[r][j], each block a
+// stripe of KS_COLSUM_ROWS rows (independent loads, one atomic per column).
+constexpr int KS_COLSUM_ROWS = 32;
 __global__ void k_colsum(const __nv_bfloat16* __restrict__ dY, int rows, int cols, int ld, float* db) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= cols) return;
+  const int r0 = blockIdx.y * KS_COLSUM_ROWS, r1 = min(rows, r0 + KS_COLSUM_ROWS);
   float s = 0.f;
-  for (int r = blockIdx.y; r < rows; r += gridDim.y) s += __bfloat162float(dY[(size_t)r * ld + j]);
+#pragma unroll 8
+  for (int r = r0; r < r1; r++) s += __bfloat162float(dY[(size_t)r * ld + j]);
   atomicAdd(&db[j], s);
 }
 
@@ -645,7 +662,7 @@ static void mlp_forward(ks_mlp* p, int R, cudaStream_t st) {
 
 // backward from p->dYb; accumulates into p->g (zeroed by the caller)
 static void mlp_backward(ks_mlp* p, int R, cudaStream_t st) {
-  int splits = R / 512 > 1 ? R / 512 : 1;
+  int splits = R / 256 > 1 ? R / 256 : 1;  // K = rows: 256-row chunks fill the SMs at the minibatch sizes
   const __nv_bfloat16* acts[4] = {p->X, p->H[0], p->H[1], p->H[2]};
   const __nv_bfloat16* dout = p->dYb;
   int ldd = p->dop;
@@ -653,7 +670,7 @@ static void mlp_backward(ks_mlp* p, int R, cudaStream_t st) {
     // dW_l[o][i] += sum_r dout[r][o] * act[r][i]:  A = dout^T (stored [R][o]), B = act (stored [R][i])
     gemm<true, true, EPI_ATOMIC_F32>(dout, acts[l], p->g + p->woff[l], nullptr, nullptr, p->out_[l], p->in_[l], R, ldd,
                                      p->ldi[l], p->in_[l], splits, st);
-    dim3 cg((p->out_[l] + 127) / 128, 64);
+    dim3 cg((p->out_[l] + 127) / 128, (R + KS_COLSUM_ROWS - 1) / KS_COLSUM_ROWS);
     k_colsum<<<cg, 128, 0, st>>>(dout, R, p->out_[l], ldd, p->g + p->boff[l]);
     if (l == 0) break;
     // dact[r][i] = sum_o dout[r][o] W[o][i], masked by the ReLU of layer l-1
