@@ -1,0 +1,437 @@
+"""Batched scoring of a population for evolutionary circuit search.
+
+The reference scores a generation on a worker pool, one candidate per
+goroutine (evaluator.one, evo/engine.go:511-612): validate the decoded circuit,
+then run each objective, whose measurements go through a per-candidate cache of
+analyses (Eval.OP / AC / Tran, evo/fitness.go:37-205); the first error becomes a
+penalty class (Penalty, evo/fitness.go:644-681), otherwise the fitness is the
+weighted sum of the objectives' errors.
+
+Here a generation is scored together.  The candidates are validated on the host
+and grouped by topology; the first time any objective asks a candidate for an
+analysis, that analysis runs once for every candidate of the group through the
+engine's batched entry points (ks_op_results, ks_ac, ks_tran_results); each
+candidate's objectives then read its slice of the batched result.  Objectives
+keep the reference's per-candidate form (an Eval with op(), ac(spec), tran(spec)
+that raise the analysis error of that candidate), so a candidate's terms,
+fitness and failure class are what the worker pool computes.
+"""
+from dataclasses import dataclass, field, replace
+import math
+
+import numpy as np
+
+from . import analysis
+
+# Failure classes and their penalty fitness, evo/fitness.go:644-654: a failed
+# candidate scores worse than any successful one with total error below 1e5.
+PENALTY_NO_MEASUREMENT = 1e6
+PENALTY_NO_CONVERGENCE = 2e6
+PENALTY_SINGULAR = 3e6
+PENALTY_INVALID = 4e6
+PENALTY_LEDGER = 5e6
+PENALTY_TIMEOUT = 6e6
+PENALTY_OTHER = 1e7
+
+
+class ErrNoMeasurement(analysis.KronspiceError):
+    """analysis.ErrNoMeasurement: an objective could not take its measurement."""
+
+
+def penalty(err):
+    """Penalty (evo/fitness.go:659-681): (fitness, class) of an evaluation error."""
+    if isinstance(err, analysis.ErrInterrupted):
+        return PENALTY_TIMEOUT, "timeout"
+    if isinstance(err, analysis.ErrLedgerResidual):
+        return PENALTY_LEDGER, "ledger"
+    if isinstance(err, ErrNoMeasurement):
+        return PENALTY_NO_MEASUREMENT, "no-measurement"
+    if isinstance(err, (analysis.ErrNoConvergence, analysis.ErrTimestepTooSmall, analysis.ErrTooManySteps)):
+        return PENALTY_NO_CONVERGENCE, "no-convergence"
+    if isinstance(err, (analysis.ErrSingularMatrix, analysis.ErrNonFinite)):
+        return PENALTY_SINGULAR, "singular"
+    if isinstance(err, analysis.ErrValidation):
+        return PENALTY_INVALID, "invalid"
+    return PENALTY_OTHER, "error"
+
+
+# ---------------------------------------------------------------- results of one candidate
+def _node_value(ckt, x, node):
+    i = ckt.node_index(node)
+    if i < 0:
+        return None
+    return 0.0 if i == 0 else x[..., i - 1]
+
+
+@dataclass
+class OPResult:
+    """The candidate's output.Result: node voltages, element results, ledger."""
+    circuit: object
+    x: np.ndarray
+    elements: np.ndarray  # [n_elem][RES_COLS]
+    ledger: np.ndarray    # [LEDGER_COLS]
+
+    def voltage(self, node):
+        v = _node_value(self.circuit, self.x, node)
+        return None if v is None else float(v)
+
+    def element(self, name):
+        k = self.circuit.element_index(name)
+        if k < 0:
+            return None
+        r = self.elements[k]
+        return {c: float(r[j]) for c, j in analysis.RES.items()}
+
+    @property
+    def model_supplied(self):
+        return float(self.ledger[analysis.LEDGER["model_supplied"]])
+
+
+@dataclass
+class ACResult:
+    """The candidate's output.ACResult: frequencies and complex node voltages."""
+    circuit: object
+    freq: np.ndarray
+    x: np.ndarray  # [n_freq][n] complex
+
+    def node_voltage(self, node):
+        i = self.circuit.node_index(node)
+        if i < 0:
+            return None
+        return np.zeros(len(self.freq), complex) if i == 0 else self.x[:, i - 1]
+
+
+@dataclass
+class Waveforms:
+    """The candidate's output.Waveforms: accepted times, node voltages, per-point ledger."""
+    circuit: object
+    time: np.ndarray
+    x: np.ndarray       # [n_points][n]
+    ledger: np.ndarray  # [n_points][TPOINT_COLS]
+
+    def node_voltage(self, node):
+        i = self.circuit.node_index(node)
+        if i < 0:
+            return None
+        return np.zeros(len(self.time)) if i == 0 else self.x[:, i - 1]
+
+    @property
+    def model_supplied(self):
+        col = self.ledger[:, analysis.TPOINT["model_supplied"]]
+        return float(col.max()) if len(col) else 0.0
+
+
+# ---------------------------------------------------------------- measurements (analysis/measure.go)
+def rel_err(got, want, floor):
+    """relErr, evo/fitness.go:209-211."""
+    return abs(got - want) / max(abs(want), floor)
+
+
+def transfer(r, out, ref):
+    """analysis.Transfer (analysis/measure.go:20-40): V(out)/V(ref) per frequency."""
+    vo = r.node_voltage(out)
+    if vo is None:
+        raise ErrNoMeasurement("analysis: no measurement")
+    if ref in ("0", "gnd", ""):
+        return vo
+    vr = r.node_voltage(ref)
+    if vr is None or np.any(vr == 0):
+        raise ErrNoMeasurement("analysis: no measurement")
+    return vo / vr
+
+
+def db(h):
+    return 20 * math.log10(abs(h))
+
+
+def gain_at(freq, h, f):
+    """analysis.GainAt (analysis/measure.go:44-56): |H| at f, linear in log-frequency and dB."""
+    if len(freq) == 0 or f < freq[0] or f > freq[-1] or f <= 0:
+        raise ErrNoMeasurement("analysis: no measurement")
+    for k in range(1, len(freq)):
+        if f <= freq[k]:
+            d0, d1 = db(h[k - 1]), db(h[k])
+            x = (math.log(f) - math.log(freq[k - 1])) / (math.log(freq[k]) - math.log(freq[k - 1]))
+            return math.pow(10, (d0 + x * (d1 - d0)) / 20)
+    return abs(h[0])
+
+
+def interp(t, y, tq):
+    """output.Interp (output/waveforms.go:87-104)."""
+    n = len(t)
+    if n == 0:
+        return math.nan
+    if tq <= t[0]:
+        return float(y[0])
+    if tq >= t[n - 1]:
+        return float(y[n - 1])
+    k = int(np.searchsorted(t, tq))
+    if t[k] == tq:
+        return float(y[k])
+    return float(y[k - 1] + (y[k] - y[k - 1]) * (tq - t[k - 1]) / (t[k] - t[k - 1]))
+
+
+# ---------------------------------------------------------------- the batched cache
+class _Group:
+    """The candidates of one topology and the analyses run for all of them."""
+
+    def __init__(self, idx, circuits, options, capacity):
+        self.idx = idx
+        self.circuits = [circuits[i] for i in idx]
+        el, v0, _ = self.circuits[0].pack()
+        self.el = el
+        self.vals = np.stack([c.pack()[1] for c in self.circuits])
+        self.plan = analysis.Plan(el, self.circuits[0].n_nodes, self.vals.shape[1])
+        self.options = options
+        self.capacity = capacity
+        self.row = {i: r for r, i in enumerate(idx)}
+        self._batch = None
+        self.cache = {}
+
+    def batch(self):
+        if self._batch is None:
+            self._batch = analysis.Batch(self.plan, self.vals)
+        return self._batch
+
+    def op(self):
+        if "op" not in self.cache:
+            x, st, it, elem, led = self.batch().op_results(self.options)
+            self.cache["op"] = (x, st, elem, led)
+        return self.cache["op"]
+
+    def ac(self, spec):
+        key = ("ac", spec.variation, spec.points, spec.fstart, spec.fstop)
+        if key not in self.cache:
+            freqs = spec.frequencies()
+            x, st, it = self.batch().ac(freqs, self.options)
+            self.cache[key] = (freqs, x, st)
+        return self.cache[key]
+
+    def tran(self, spec):
+        key = ("tran",) + tuple(sorted(vars(spec).items()))
+        if key not in self.cache:
+            # the adaptive transient with evo's step limit (evo/fitness.go:177); the
+            # recording capacity grows until every candidate's points fit
+            sp = replace(spec, fixed_step=False, max_steps=spec.max_steps or 200000)
+            cap = self.capacity
+            while True:
+                wave, tim, elem, led, summ, npts, st, steps, it = self.batch().tran_results(sp, self.options,
+                                                                                         capacity=cap)
+                if int(npts.max()) < cap or cap >= sp.max_steps + 2:
+                    break
+                cap = min(cap * 4, sp.max_steps + 2)
+            self.cache[key] = (wave, tim, led, npts, st)
+        return self.cache[key]
+
+
+class Eval:
+    """The per-candidate context handed to objectives (evo/fitness.go:37-63): its
+    circuit and gene values, and its analyses, each the candidate's slice of the
+    group's batched run (the first request runs it for the whole group)."""
+
+    def __init__(self, circuit, values, group, row):
+        self.circuit, self.values = circuit, values
+        self._g, self._r = group, row
+        self.model_supplied = 0.0
+        self._memo = {}
+
+    def _fail(self, st):
+        err = analysis.status_error(st)
+        if err is not None:
+            raise err
+
+    def op(self):
+        """Eval.OP (evo/fitness.go:96-108)."""
+        x, st, elem, led = self._g.op()
+        self._fail(st[self._r])
+        r = OPResult(self.circuit, x[self._r], elem[self._r], led[self._r])
+        self.model_supplied = max(self.model_supplied, r.model_supplied)
+        return r
+
+    def ac(self, spec):
+        """Eval.AC (evo/fitness.go:111-131)."""
+        freqs, x, st = self._g.ac(spec)
+        self._fail(st[self._r])
+        return ACResult(self.circuit, freqs, x[self._r])
+
+    def tran(self, spec):
+        """Eval.Tran (evo/fitness.go:171-189)."""
+        wave, tim, led, npts, st = self._g.tran(spec)
+        self._fail(st[self._r])
+        k = int(npts[self._r])
+        r = Waveforms(self.circuit, tim[self._r, :k], wave[self._r, :k], led[self._r, :k])
+        self.model_supplied = max(self.model_supplied, r.model_supplied)
+        return r
+
+    def memo(self, key, f):
+        """Eval.Memo (evo/fitness.go:69-79): f once per candidate and key."""
+        if key not in self._memo:
+            try:
+                self._memo[key] = (f(), None)
+            except analysis.KronspiceError as e:
+                self._memo[key] = (None, e)
+        v, err = self._memo[key]
+        if err is not None:
+            raise err
+        return v
+
+
+# ---------------------------------------------------------------- objectives
+@dataclass
+class Objective:
+    """evo.Objective (evo/fitness.go:20-35): eval(Eval) returns a non-negative error."""
+    name: str
+    weight: float
+    eval: object
+    constraint: bool = False
+
+
+def op_voltage(node, target):
+    """OPVoltage (evo/fitness.go:528-540)."""
+    def ev(e):
+        v = e.op().voltage(node)
+        if v is None:
+            raise ErrNoMeasurement("analysis: no measurement")
+        return rel_err(v, target, 1e-3)
+    return Objective("v(%s)" % node, 1.0, ev)
+
+
+def supply_power(*sources):
+    """SupplyPower (evo/fitness.go:312-329)."""
+    def ev(e):
+        r = e.op()
+        p = 0.0
+        for s in sources:
+            el = r.element(s)
+            if el is None:
+                raise ErrNoMeasurement("analysis: no measurement: no element %r" % s)
+            p -= el["power"]
+        return max(0.0, p)
+    return Objective("supply power", 1.0, ev)
+
+
+def model_supplied_limit(pmax):
+    """ModelSuppliedLimit (evo/fitness.go:630-641)."""
+    def ev(e):
+        return max(0.0, e.op().model_supplied - pmax) / max(pmax, 1e-12)
+    return Objective("model-supplied power", 1.0, ev)
+
+
+def gain_at_objective(node, ref, spec, f, target_db):
+    """GainAt (evo/fitness.go:241-259)."""
+    def ev(e):
+        h = transfer(e.ac(spec), node, ref)
+        g = gain_at(e.ac(spec).freq, h, f)
+        if g <= 0:
+            raise ErrNoMeasurement("analysis: no measurement")
+        return abs(20 * math.log10(g) - target_db) / 20
+    return Objective("gain %s at %g Hz" % (node, f), 1.0, ev)
+
+
+def tran_average(node, spec, t_from, t_to, target):
+    """TranAverage (evo/fitness.go:553-583): the mean of V(node) over [from, to]."""
+    def ev(e):
+        wf = e.tran(spec)
+        y = wf.node_voltage(node)
+        if y is None:
+            raise ErrNoMeasurement("analysis: no measurement")
+        t = wf.time
+        area = span = 0.0
+        for k in range(1, len(t)):
+            t0, t1 = t[k - 1], t[k]
+            if t1 <= t_from or t0 >= t_to:
+                continue
+            a, b = max(t0, t_from), min(t1, t_to)
+            area += 0.5 * (interp(t, y, a) + interp(t, y, b)) * (b - a)
+            span += b - a
+        if span <= 0:
+            raise ErrNoMeasurement("analysis: no measurement")
+        return rel_err(area / span, target, 1e-3)
+    return Objective("mean v(%s)" % node, 1.0, ev)
+
+
+def tran_ripple(node, spec, t_from, t_to, vmax):
+    """TranRipple (evo/fitness.go:584-606): a constraint on V(node)'s peak to peak."""
+    def ev(e):
+        wf = e.tran(spec)
+        y = wf.node_voltage(node)
+        if y is None:
+            raise ErrNoMeasurement("analysis: no measurement")
+        w = y[(wf.time >= t_from) & (wf.time <= t_to)]
+        if len(w) < 2 or vmax <= 0:
+            raise ErrNoMeasurement("analysis: no measurement")
+        return max(0.0, float(w.max() - w.min()) - vmax) / vmax
+    return Objective("ripple v(%s)" % node, 1.0, ev)
+
+
+# ---------------------------------------------------------------- the population
+@dataclass
+class Individual:
+    """evo.Individual (evo/engine.go:185-203) without the genome and Pareto fields."""
+    values: list
+    fitness: float = 0.0
+    terms: list = None
+    failure: str = ""
+    error: str = ""
+    model_supplied: float = 0.0
+
+
+def evaluate(circuits, objectives, options=None, values=None, capacity=20000):
+    """Score a population (evaluator.evaluate + one, evo/engine.go:518-612): one
+    Individual per circuit, in order.  `values` are the candidates' gene values
+    (reported back); `capacity` bounds the accepted points a transient records
+    per candidate."""
+    opt = options or analysis.Options()
+    n = len(circuits)
+    out = [Individual(values=list(values[i]) if values is not None else []) for i in range(n)]
+
+    def fail(ind, err):
+        ind.fitness, ind.failure = penalty(err)
+        ind.error = str(err)
+        ind.terms = None
+
+    # Validate (:564-574): a floating node is tolerated when the transient is defined
+    ok, keys = [], {}
+    for i, c in enumerate(circuits):
+        try:
+            err = analysis.validate(c)
+            if isinstance(err, analysis.ErrFloatingNode) and analysis.validate(c, transient=True) is None:
+                err = None
+            key = c.pack()[2]
+        except analysis.KronspiceError as e:
+            err = e
+        except (ValueError, KeyError) as e:  # the circuit does not pack: a bad value or model
+            err = analysis.ErrValidation("circuit: %s" % e)
+        if err is not None:
+            fail(out[i], err)
+            continue
+        ok.append(i)
+        keys.setdefault(key, []).append(i)
+    groups = {}
+    for key, idx in keys.items():
+        # small groups run the generic kernels: no per-topology compilation
+        g_opt = opt if len(idx) >= 256 or opt.kernel != "auto" else replace(opt, kernel="generic")
+        g = _Group(idx, circuits, g_opt, capacity)
+        for i in idx:
+            groups[i] = g
+    for i in ok:
+        g = groups[i]
+        e = Eval(circuits[i], out[i].values, g, g.row[i])
+        ind = out[i]
+        ind.terms = [0.0] * len(objectives)
+        total, failed = 0.0, False
+        for k, ob in enumerate(objectives):  # :591-607
+            try:
+                v = ob.eval(e)
+                if v is None or math.isnan(v) or math.isinf(v) or v < 0:
+                    raise ErrNoMeasurement("analysis: no measurement: objective %r returned %r" % (ob.name, v))
+            except analysis.KronspiceError as err:
+                fail(ind, type(err)("%s: %s" % (ob.name, err)))
+                failed = True
+                break
+            ind.terms[k] = v
+            total += ob.weight * v
+        if not failed:
+            ind.fitness = total
+        ind.model_supplied = e.model_supplied
+    return out
