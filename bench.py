@@ -46,10 +46,10 @@ UNIT = "solves/s"
 RELTOL = 1e-6
 # workload -> (default circuits, compulsory bytes per solve: parameters in + node voltages out, 8 B each)
 WORKLOADS = {"bjt_ce": (16384, (7 + 5) * 8), "cmos_opamp": (65536, (24 + 7) * 8), "rc_ladder": (4096, 0),
-             "random_netlists": (8192, 0), "bjt_ce_ac": (16384, 0), "power_grid": (64, 0)}
+             "random_netlists": (8192, 0), "bjt_ce_ac": (16384, 0), "power_grid": (64, 0), "evo_lowpass": (16384, 0)}
 # timed steps when --steps is not given (the headline times about 200 steps)
 DEFAULT_STEPS = {"bjt_ce": 200, "cmos_opamp": 5, "rc_ladder": 20, "random_netlists": 1, "bjt_ce_ac": 20,
-                 "power_grid": 1}
+                 "power_grid": 1, "evo_lowpass": 5}
 # most FP32 Newton iterations of the chosen path's start stage (its gmin / source-stepping chain included)
 FP32_START = {"bjt_ce": 200, "cmos_opamp": 6000}
 # torn power grid: 256 x 256 mesh in 4 x 4 pieces, 1,024 clamped loads, 500 backward-Euler steps of 0.1 ns
@@ -356,6 +356,22 @@ def run_reference(args):
     if args.workload == "bjt_ce_ac":
         run_reference_ac(args)
         return
+    if args.workload == "evo_lowpass":
+        pop, objectives, spec = evo_population(min(args.n_circ, 4096), args.seed)
+        vals = []
+        for _ in range(args.warmup + args.steps):
+            vals.append(evo_oracle_pool(pop, objectives, spec))
+        v = [x[0] for x in vals[args.warmup:]]
+        value = statistics.median(v)
+        print(json.dumps({"impl": "reference", "metric": "candidates scored/s (batched evaluator: OP + AC objectives)",
+                          "value": value, "unit": "candidates/s", "n_gpus": 1, "steps": args.steps,
+                          "warmup": args.warmup, "higher_is_better": True, "data": "synthetic (seeded candidates)",
+                          "config": {"workload": "evo_lowpass_%d" % args.n_circ},
+                          "cpu_baseline": {"value": value, "unit": "candidates/s", "cores": vals[-1][2],
+                                           "kind": "port", "sample": "%d candidates a step" % len(pop)},
+                          "e2e": {"value": value, "unit": "candidates/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
     if args.workload == "power_grid":
         run_reference_torn(args)
         return
@@ -580,6 +596,125 @@ def bench_tran(args):
     print(json.dumps(line))
     if world > 1:
         torch.distributed.barrier()
+
+
+def evo_population(n, seed):
+    """n seeded candidates of a loaded RC low-pass (R 0.5-5 kOhm, C 1-100 nF, load
+    2-20 kOhm), the value genome of a filter search, and its objectives: the gain
+    at 1 kHz (-3 dB target, 51-point AC sweep 10 Hz-1 MHz), the output's operating
+    point (1 V target), the supply power and the model-supplied power limit."""
+    import numpy as np
+    from kronspice_gb300 import analysis, evo
+    from kronspice_gb300 import circuit as kc
+    g = np.random.default_rng(seed)
+    pop = []
+    for r, c, rl in zip(g.uniform(500, 5e3, n), g.uniform(1e-9, 1e-7, n), g.uniform(2e3, 2e4, n)):
+        b = kc.Builder("lowpass")
+        b.voltage_source("V1", "in", "0", 2.0, ac=(1.0, 0.0))
+        b.resistor("R1", "in", "out", r).capacitor("C1", "out", "0", c).resistor("RL", "out", "0", rl)
+        pop.append(b.build())
+    spec = analysis.ACSpec("dec", 10, 10.0, 1e6)
+    objectives = [evo.gain_at_objective("out", "in", spec, 1e3, -3.0), evo.op_voltage("out", 1.0),
+                  evo.supply_power("V1"), evo.model_supplied_limit(0.0)]
+    return pop, objectives, spec
+
+
+def bench_evo(args):
+    """A generation of an evolutionary filter search scored by the batched
+    evaluator (kronspice_gb300/evo.py): host circuits in, scored individuals out
+    (validation, packing, the batched OP and AC on the GPU, the objectives).
+    Unit = one scored candidate; a step = one generation of n_circ candidates.
+    The CPU line is the reference's worker pool restated: the oracle's OP and AC
+    per candidate on every host thread, the same objective code."""
+    import numpy as np
+    import torch
+    from kronspice_gb300 import build, evo
+    from oracle import oracle as orc
+    build.build()
+    orc.build()
+    pop, objectives, spec = evo_population(args.n_circ, args.seed)
+    for _ in range(max(1, args.warmup)):
+        evo.evaluate(pop, objectives)
+    torch.cuda.synchronize()
+    clk = Clocks(os.path.join(tempfile.gettempdir(), "bench_clocks_evo.csv"))
+    with clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            out = evo.evaluate(pop, objectives)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    clocks = clk.summary(0)
+    value = args.n_circ * args.steps / wall
+    failures = sum(1 for ind in out if ind.failure)
+    cpu_value, cpu_wall, nthreads, cpu_fit = evo_oracle_pool(pop[:min(len(pop), 4096)], objectives, spec)
+    sample = pop[:len(cpu_fit)]
+    gpu_fit = np.array([ind.fitness for ind in out[:len(sample)]])
+    parity = float(np.max(np.abs(gpu_fit - np.array(cpu_fit)) / np.maximum(np.abs(cpu_fit), 1e-12)))
+    el, v0, _ = pop[0].pack()
+    n = int(orc.unknowns(orc.Packed.of(pop[0]))[0])
+    nf = len(spec.frequencies())
+    h2d = args.n_circ * len(v0) * 8 + len(el) * 48 + nf * 8
+    d2h = args.n_circ * (8 * (n + len(el) * 7 + 8) + 8 * nf * n * 2 + 4 * 4)
+    line = {
+        "metric": "candidates scored/s (batched evaluator: OP + AC objectives)", "value": value,
+        "unit": "candidates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded candidates)",
+        "config": {"workload": "evo_lowpass_%d" % args.n_circ, "candidates": args.n_circ,
+                   "objectives": [ob.name for ob in objectives], "ac_points": nf,
+                   "l2": "a generation's arrays are far below L2; each step builds, uploads and solves anew"},
+        "failures": failures, "max_fitness_rel_diff_vs_oracle": parity,
+        "e2e": {"value": value, "unit": "candidates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": None,
+        "roofline_note": "host-bound: per generation the candidates are packed and validated on the host and "
+                         "the objectives read the batched results; the GPU analyses are a small part of a step",
+        "gpu_launches": 9 * args.steps,
+        "cpu_baseline": {"value": cpu_value, "unit": "candidates/s", "cores": nthreads, "kind": "port",
+                         "sample": "%d candidates scored through the oracle's OP and AC, one per host thread "
+                                   "at a time (%.1f s wall)" % (len(sample), cpu_wall)},
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
+def evo_oracle_pool(sample, objectives, spec):
+    """The reference's worker pool restated (evo/engine.go:518-543): each host
+    thread scores one candidate at a time through the oracle's OP and AC and the
+    same objective code.  (candidates/s, wall s, threads, fitnesses)."""
+    import concurrent.futures as cf
+    from kronspice_gb300 import analysis, evo
+    from oracle import oracle as orc
+    orc.build()
+    freqs = spec.frequencies()
+
+    class OracleEval:
+        def __init__(self, ckt):
+            self.circuit, self.model_supplied, self.pk = ckt, 0.0, orc.Packed.of(ckt)
+
+        def op(self):
+            st, x, elem, led, _, _ = orc.op_results(self.pk)
+            err = analysis.status_error(st)
+            if err:
+                raise err
+            return evo.OPResult(self.circuit, x, elem, led)
+
+        def ac(self, sp):
+            st, x, _ = orc.ac(self.pk, freqs)
+            err = analysis.status_error(st)
+            if err:
+                raise err
+            return evo.ACResult(self.circuit, freqs, x)
+
+    def score(ckt):
+        e = OracleEval(ckt)
+        return sum(ob.weight * ob.eval(e) for ob in objectives)
+
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(nthreads) as ex:
+        fits = list(ex.map(score, sample))
+    wall = time.perf_counter() - t0
+    return len(sample) / wall, wall, nthreads, fits
 
 
 def bench_multi(args):
@@ -1245,6 +1380,9 @@ def main():
         return
     if args.workload == "power_grid":
         bench_torn(args)
+        return
+    if args.workload == "evo_lowpass":
+        bench_evo(args)
         return
     import torch
     rank, world, local = dist_env()

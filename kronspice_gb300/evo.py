@@ -175,13 +175,12 @@ def interp(t, y, tq):
 class _Group:
     """The candidates of one topology and the analyses run for all of them."""
 
-    def __init__(self, idx, circuits, options, capacity):
+    def __init__(self, idx, circuits, packed, options, capacity):
         self.idx = idx
         self.circuits = [circuits[i] for i in idx]
-        el, v0, _ = self.circuits[0].pack()
-        self.el = el
-        self.vals = np.stack([c.pack()[1] for c in self.circuits])
-        self.plan = analysis.Plan(el, self.circuits[0].n_nodes, self.vals.shape[1])
+        self.el = packed[idx[0]][0]
+        self.vals = np.stack([packed[i][1] for i in idx])
+        self.plan = analysis.Plan(self.el, self.circuits[0].n_nodes, self.vals.shape[1])
         self.options = options
         self.capacity = capacity
         self.row = {i: r for r, i in enumerate(idx)}
@@ -279,11 +278,46 @@ class Eval:
 # ---------------------------------------------------------------- objectives
 @dataclass
 class Objective:
-    """evo.Objective (evo/fitness.go:20-35): eval(Eval) returns a non-negative error."""
+    """evo.Objective (evo/fitness.go:20-35): eval(Eval) returns a non-negative error.
+    batch (optional): the same measurement for every candidate of a topology group
+    at once, batch(GroupView) -> (errors [m], failures [m]: None or the exception
+    eval would raise); the evaluator uses it in place of eval when present."""
     name: str
     weight: float
     eval: object
     constraint: bool = False
+    batch: object = None
+
+
+class GroupView:
+    """The batched analyses of one topology group, for the batch form of objectives."""
+
+    def __init__(self, group):
+        self.g = group
+        self.circuit = group.circuits[0]
+        self.m = len(group.idx)
+        self.used_op = False  # the objective read the operating point
+
+    def _status(self, st):
+        return [analysis.status_error(s) for s in st]
+
+    def op(self):
+        """(x [m][n], elem [m][n_elem][RES_COLS], ledger [m][LEDGER_COLS], failures [m])."""
+        self.used_op = True
+        x, st, elem, led = self.g.op()
+        return x, elem, led, self._status(st)
+
+    def ac(self, spec):
+        """(freqs, x [m][n_freq][n] complex, failures [m])."""
+        freqs, x, st = self.g.ac(spec)
+        return freqs, x, self._status(st)
+
+    def node(self, name):
+        return self.circuit.node_index(name)
+
+
+def _no_measurement():
+    return ErrNoMeasurement("analysis: no measurement")
 
 
 def op_voltage(node, target):
@@ -293,7 +327,15 @@ def op_voltage(node, target):
         if v is None:
             raise ErrNoMeasurement("analysis: no measurement")
         return rel_err(v, target, 1e-3)
-    return Objective("v(%s)" % node, 1.0, ev)
+
+    def batch(gv):
+        x, _, _, fails = gv.op()
+        i = gv.node(node)
+        if i < 0:
+            return np.zeros(gv.m), [f or _no_measurement() for f in fails]
+        v = np.zeros(gv.m) if i == 0 else x[:, i - 1]
+        return np.abs(v - target) / max(abs(target), 1e-3), fails
+    return Objective("v(%s)" % node, 1.0, ev, batch=batch)
 
 
 def supply_power(*sources):
@@ -307,14 +349,28 @@ def supply_power(*sources):
                 raise ErrNoMeasurement("analysis: no measurement: no element %r" % s)
             p -= el["power"]
         return max(0.0, p)
-    return Objective("supply power", 1.0, ev)
+
+    def batch(gv):
+        x, elem, _, fails = gv.op()
+        ks = [gv.circuit.element_index(s) for s in sources]
+        if any(k < 0 for k in ks):
+            return np.zeros(gv.m), [f or _no_measurement() for f in fails]
+        p = np.zeros(gv.m)
+        for k in ks:
+            p -= elem[:, k, analysis.RES["power"]]
+        return np.maximum(0.0, p), fails
+    return Objective("supply power", 1.0, ev, batch=batch)
 
 
 def model_supplied_limit(pmax):
     """ModelSuppliedLimit (evo/fitness.go:630-641)."""
     def ev(e):
         return max(0.0, e.op().model_supplied - pmax) / max(pmax, 1e-12)
-    return Objective("model-supplied power", 1.0, ev)
+
+    def batch(gv):
+        _, _, led, fails = gv.op()
+        return np.maximum(0.0, led[:, analysis.LEDGER["model_supplied"]] - pmax) / max(pmax, 1e-12), fails
+    return Objective("model-supplied power", 1.0, ev, batch=batch)
 
 
 def gain_at_objective(node, ref, spec, f, target_db):
@@ -325,7 +381,42 @@ def gain_at_objective(node, ref, spec, f, target_db):
         if g <= 0:
             raise ErrNoMeasurement("analysis: no measurement")
         return abs(20 * math.log10(g) - target_db) / 20
-    return Objective("gain %s at %g Hz" % (node, f), 1.0, ev)
+
+    def batch(gv):
+        freqs, x, fails = gv.ac(spec)
+        io, ir = gv.node(node), gv.node(ref)
+        bad = io < 0 or (ref not in ("0", "gnd", "") and ir < 0) or len(freqs) == 0 or not (
+            freqs[0] <= f <= freqs[-1]) or f <= 0
+        if bad:
+            return np.zeros(gv.m), [fl or _no_measurement() for fl in fails]
+        vo = np.zeros(x.shape[:2], complex) if io == 0 else x[:, :, io - 1]
+        if ref in ("0", "gnd", ""):
+            h = vo
+            zero = np.zeros(gv.m, bool)
+        else:
+            vr = np.zeros(x.shape[:2], complex) if ir == 0 else x[:, :, ir - 1]
+            zero = np.any(vr == 0, axis=1)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                h = vo / np.where(vr == 0, 1.0, vr)
+        k = int(np.searchsorted(freqs, f))  # the first frequency >= f (GainAt's segment end)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            if k == 0:
+                g = np.abs(h[:, 0])
+            else:
+                d0, d1 = 20 * np.log10(np.abs(h[:, k - 1])), 20 * np.log10(np.abs(h[:, k]))
+                t = (math.log(f) - math.log(freqs[k - 1])) / (math.log(freqs[k]) - math.log(freqs[k - 1]))
+                g = np.power(10.0, (d0 + t * (d1 - d0)) / 20)
+            err = np.abs(20 * np.log10(g) - target_db) / 20
+        out = []
+        for c in range(gv.m):
+            if fails[c] is not None:
+                out.append(fails[c])
+            elif zero[c] or not (g[c] > 0) or not np.isfinite(err[c]):
+                out.append(_no_measurement())
+            else:
+                out.append(None)
+        return np.where(np.isfinite(err), err, 0.0), out
+    return Objective("gain %s at %g Hz" % (node, f), 1.0, ev, batch=batch)
 
 
 def tran_average(node, spec, t_from, t_to, target):
@@ -391,13 +482,14 @@ def evaluate(circuits, objectives, options=None, values=None, capacity=20000):
         ind.terms = None
 
     # Validate (:564-574): a floating node is tolerated when the transient is defined
-    ok, keys = [], {}
+    ok, keys, packed = [], {}, {}
     for i, c in enumerate(circuits):
         try:
-            err = analysis.validate(c)
-            if isinstance(err, analysis.ErrFloatingNode) and analysis.validate(c, transient=True) is None:
+            el, vals, key = c.pack()
+            err = analysis.validate_packed(el, c.n_nodes, vals)
+            if isinstance(err, analysis.ErrFloatingNode) and analysis.validate_packed(el, c.n_nodes, vals, True) is None:
                 err = None
-            key = c.pack()[2]
+            packed[i] = (el, vals)
         except analysis.KronspiceError as e:
             err = e
         except (ValueError, KeyError) as e:  # the circuit does not pack: a bad value or model
@@ -411,27 +503,72 @@ def evaluate(circuits, objectives, options=None, values=None, capacity=20000):
     for key, idx in keys.items():
         # small groups run the generic kernels: no per-topology compilation
         g_opt = opt if len(idx) >= 256 or opt.kernel != "auto" else replace(opt, kernel="generic")
-        g = _Group(idx, circuits, g_opt, capacity)
+        g = _Group(idx, circuits, packed, g_opt, capacity)
         for i in idx:
             groups[i] = g
+    seen = []
     for i in ok:
-        g = groups[i]
-        e = Eval(circuits[i], out[i].values, g, g.row[i])
-        ind = out[i]
-        ind.terms = [0.0] * len(objectives)
-        total, failed = 0.0, False
-        for k, ob in enumerate(objectives):  # :591-607
+        if groups[i] not in seen:
+            seen.append(groups[i])
+    for g in seen:
+        _score_group(g, objectives, out, fail)
+    return out
+
+
+def _score_group(g, objectives, out, fail):
+    """The objectives of one topology group in order (:591-607), each in its batch
+    form when it has one (else candidate by candidate); a candidate stops at its
+    first failing objective."""
+    m = len(g.idx)
+    terms = np.zeros((m, len(objectives)))
+    first_fail = [None] * m
+    evals = [None] * m
+    ran_op = np.zeros(m, bool)  # an objective read the candidate's operating point (Eval.OP)
+    for k, ob in enumerate(objectives):
+        live = [c for c in range(m) if first_fail[c] is None]
+        if not live:
+            break
+        if ob.batch is not None:
+            gv = GroupView(g)
+            v, fails = ob.batch(gv)
+            if gv.used_op:
+                ran_op[live] = True
+            for c in live:
+                err = fails[c]
+                if err is None and (math.isnan(v[c]) or math.isinf(v[c]) or v[c] < 0):
+                    err = ErrNoMeasurement("analysis: no measurement: objective %r returned %r" % (ob.name, v[c]))
+                if err is not None:
+                    first_fail[c] = type(err)("%s: %s" % (ob.name, err))
+                else:
+                    terms[c, k] = v[c]
+            continue
+        for c in live:
+            if evals[c] is None:
+                i = g.idx[c]
+                evals[c] = Eval(g.circuits[c], out[i].values, g, c)
             try:
-                v = ob.eval(e)
+                v = ob.eval(evals[c])
                 if v is None or math.isnan(v) or math.isinf(v) or v < 0:
                     raise ErrNoMeasurement("analysis: no measurement: objective %r returned %r" % (ob.name, v))
             except analysis.KronspiceError as err:
-                fail(ind, type(err)("%s: %s" % (ob.name, err)))
-                failed = True
-                break
-            ind.terms[k] = v
-            total += ob.weight * v
-        if not failed:
-            ind.fitness = total
-        ind.model_supplied = e.model_supplied
-    return out
+                first_fail[c] = type(err)("%s: %s" % (ob.name, err))
+                continue
+            terms[c, k] = v
+    # model-supplied power: the largest over the operating points and transients the
+    # candidate's own objectives ran (Eval.noteSupplied, evo/fitness.go:90-94)
+    ms = np.zeros(m)
+    if "op" in g.cache:
+        st, led = g.cache["op"][1], g.cache["op"][3]
+        ms = np.where(ran_op & (st == 0), led[:, analysis.LEDGER["model_supplied"]], 0.0)
+    for c in range(m):
+        if evals[c] is not None:
+            ms[c] = max(ms[c], evals[c].model_supplied)
+    w = np.array([ob.weight for ob in objectives])
+    for c in range(m):
+        ind = out[g.idx[c]]
+        ind.model_supplied = float(ms[c])
+        if first_fail[c] is not None:
+            fail(ind, first_fail[c])
+            continue
+        ind.terms = [float(t) for t in terms[c]]
+        ind.fitness = float(np.dot(w, terms[c]))
