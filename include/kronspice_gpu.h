@@ -267,6 +267,17 @@ typedef struct {
                              voltages) and the step control are the reference's,
                              so the start changes how many iterations a step
                              takes.  0: off. */
+  int32_t autotune;       /* ks_op / ks_op_async: > 0 times the operating-point
+                             kernels this batch can run (the per-topology kernel
+                             when the plan has one, the generic kernel; each with
+                             1, 2 or 4 circuits per thread of the persistent grid)
+                             on the first call for the plan, analysis and batch
+                             size (to the power of two), keeps the fastest in the
+                             plan and runs it then and on later calls (the tuning
+                             call synchronizes its stream).  The kernels run the
+                             same algorithm, so the choice changes the time, not
+                             the result beyond the Newton tolerance.  0: the
+                             fixed rules (KS_JIT_MIN_BATCH, KS_CIRCUITS_PER_THREAD). */
 } ks_options;
 
 /* ---- transient request (analysis/tran.go:26-59) ------------------------- */
@@ -668,6 +679,12 @@ int ks_torn_op(ks_torn* t, const ks_options* opt, int32_t reuse, double* out_x, 
 int ks_torn_tran(ks_torn* t, const ks_tran_spec* spec, const ks_options* opt, int32_t reuse, const int32_t* probes,
                  int32_t n_probes, double* out_wave, double* out_x, int32_t* out_status, int32_t* out_steps,
                  int32_t* out_iters, int64_t* stats);
+
+/* The autotuner's choice for operating points of `n_circ` circuits on this plan
+ * (the power-of-two bucket of n_circ): *kernel a KS_KERNEL_* value, *cpt the
+ * circuits per thread of the persistent grid, *ms the winning trial's kernel
+ * time.  KS_EINVAL when no ks_options.autotune call has tuned that bucket. */
+int ks_plan_tuned(const ks_plan* plan, int32_t analysis, int64_t n_circ, int32_t* kernel, int32_t* cpt, double* ms);
 
 /* Predicted starting points x0_dev [n_circ][n] (device memory) for ks_op_async. */
 int ks_mlp_predict(ks_mlp* m, ks_batch* b, double* x0_dev, void* stream);

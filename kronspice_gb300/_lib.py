@@ -24,7 +24,7 @@ class KsOptions(ctypes.Structure):
                 ("deadline_s", ctypes.c_double), ("mixed_passes", ctypes.c_int32),
                 ("fp32_start_iters", ctypes.c_int32), ("start_check", ctypes.c_double),
                 ("ledger_tol", ctypes.c_double), ("skip_energy_check", ctypes.c_int32),
-                ("step_predictor", ctypes.c_int32)]
+                ("step_predictor", ctypes.c_int32), ("autotune", ctypes.c_int32)]
 
 
 class KsTranSpec(ctypes.Structure):
@@ -40,7 +40,7 @@ EXPORTS = ["ks_version", "ks_last_error", "ks_validate", "ks_unknowns", "ks_plan
            "ks_tran", "ks_tran_async", "ks_tran_points", "ks_plan_specialize", "ks_plan_kernel_source",
            "ks_batch_last_kernel", "ks_op_noalloc", "ks_op_noalloc_scratch_bytes", "ks_multi_create",
            "ks_multi_destroy", "ks_multi_info", "ks_multi_op", "ks_multi_op_async", "ks_multi_tran",
-           "ks_multi_tran_async", "ks_sparse_analyze", "ks_ac", "ks_ac_async", "ks_ac_at", "ks_dc_sweep", "ks_torn_create",
+           "ks_multi_tran_async", "ks_sparse_analyze", "ks_ac", "ks_ac_async", "ks_ac_at", "ks_dc_sweep", "ks_plan_tuned", "ks_torn_create",
            "ks_torn_destroy", "ks_torn_plan", "ks_torn_set_stream", "ks_torn_info", "ks_torn_op", "ks_torn_tran",
            "ks_fp64_peak", "ks_batch_cancel_word", "ks_op_results", "ks_op_results_async", "ks_tran_results",
            "ks_tran_results_async", "ks_sparse_pattern"]
@@ -104,6 +104,7 @@ def load(build_if_missing=False):
     L.ks_ac.argtypes = [P, P, P, P, ctypes.c_int32, P, P, P, P]
     L.ks_ac_async.argtypes = [P, P, P, P, ctypes.c_int32, P, P, P, P]
     L.ks_ac_at.argtypes = [P, P, P, P, P, ctypes.c_int32, P, P, P]
+    L.ks_plan_tuned.argtypes = [P, ctypes.c_int32, ctypes.c_int64, P, P, P]
     L.ks_dc_sweep.argtypes = [P, P, ctypes.c_int32, P, ctypes.c_int32, ctypes.c_int32, P, ctypes.c_int32, P, P, P,
                               P, P]
     L.ks_torn_create.argtypes = [P, ctypes.c_int32, P, P, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]

@@ -103,6 +103,7 @@ class Options:
     ledger_tol: float = 0.0     # Options.LedgerTolerance (0: 1e-9)
     skip_energy_check: bool = False  # Options.SkipEnergyCheck
     step_predictor: bool = False     # transients: each step's Newton starts from the extrapolated history
+    autotune: bool = False           # operating points: time the kernels on the first call, keep the fastest
 
     def c(self):
         return _lib.KsOptions(self.reltol, self.abstol, self.vntol, self.gmin, self.itl1, self.itl4,
@@ -110,7 +111,7 @@ class Options:
                               int(self.no_pseudo_transient), PREC[self.precision], KERNEL[self.kernel],
                               self.max_iter_total, self.deadline_s, self.mixed_passes, int(self.fp32_start_iters),
                               float(self.start_check), float(self.ledger_tol), int(self.skip_energy_check),
-                              int(self.step_predictor))
+                              int(self.step_predictor), int(self.autotune))
 
 
 def _check(rc, what):
@@ -147,6 +148,16 @@ class Plan:
         _check(_lib.load().ks_plan_specialize(self.handle, ANALYSIS[analysis], ctypes.byref(k), ctypes.byref(t)),
                "ks_plan_specialize")
         return KERNEL_NAMES[k.value], t.value
+
+    def tuned(self, n_circ, analysis="op"):
+        """The autotuner's choice for n_circ circuits (ks_plan_tuned): (kernel name,
+        circuits per thread, winning trial's ms), or None when not tuned."""
+        k, c, ms = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_double()
+        rc = _lib.load().ks_plan_tuned(self.handle, ANALYSIS[analysis], int(n_circ), ctypes.byref(k), ctypes.byref(c),
+                                       ctypes.byref(ms))
+        if rc != 0:
+            return None
+        return {0: "generic", 1: "specialized-reg", 2: "specialized-smem"}[k.value], c.value, ms.value
 
     def kernel_source(self, analysis="op"):
         L = _lib.load()

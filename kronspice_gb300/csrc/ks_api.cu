@@ -23,6 +23,10 @@ struct ks_plan {
   std::mutex spec_mu;                  // per-topology kernels, per device
   std::map<std::pair<int, int>, KsSpec> spec;           // (device, kind)
   std::map<std::pair<int, int>, std::string> spec_err;  // compile failure (not retried)
+  // the autotuner's choices, per (analysis kind, power-of-two bucket of the batch size)
+  struct Tuned { int backend, cpt, kernel; double ms; };
+  std::mutex tune_mu;
+  std::map<std::pair<int, int>, Tuned> tuned;
   KPlan view() const {
     KPlan p;
     p.n = hp.n; p.n_elem = hp.n_elem; p.n_values = hp.n_values; p.n_derived = hp.n_derived;
@@ -117,6 +121,13 @@ static KOpts make_opts(const ks_options* o) {  // analysis/op.go:91-110
   k.start32 = o && o->fp32_start_iters > 0 ? std::min(o->fp32_start_iters, 100000) : 0;
   k.start_check = o && o->start_check > 0 ? o->start_check : 0.0;
   k.predict = o && o->step_predictor > 0 ? 1 : 0;
+  return k;
+}
+
+// The autotuner's batch-size bucket: floor(log2(B)).
+static int size_bucket(int64_t B) {
+  int k = 0;
+  while (k < 62 && ((int64_t)1 << (k + 1)) <= B) k++;
   return k;
 }
 
@@ -337,6 +348,19 @@ extern "C" int ks_plan_kernel_source(const ks_plan* plan, int32_t analysis, char
 
 extern "C" int ks_batch_last_kernel(const ks_batch* b) { return b ? b->last_kernel : -1; }
 
+extern "C" int ks_plan_tuned(const ks_plan* plan, int32_t analysis, int64_t n_circ, int32_t* kernel, int32_t* cpt,
+                             double* ms) {
+  if (!plan || analysis != KS_ANALYSIS_OP || n_circ <= 0) return KS_EINVAL;
+  ks_plan* p = const_cast<ks_plan*>(plan);
+  std::lock_guard<std::mutex> g(p->tune_mu);
+  auto it = p->tuned.find({ksj::KIND_OP, size_bucket(n_circ)});
+  if (it == p->tuned.end()) return KS_EINVAL;
+  if (kernel) *kernel = it->second.kernel;
+  if (cpt) *cpt = it->second.cpt;
+  if (ms) *ms = it->second.ms;
+  return KS_OK;
+}
+
 extern "C" int ks_batch_cancel_word(ks_batch* b, volatile int32_t** word) {
   if (!b || !word) { set_error("ks_batch_cancel_word: null argument"); return KS_EINVAL; }
   if (!b->h_cancel) {
@@ -382,6 +406,56 @@ static int results_opts(ks_batch* b, const ks_options* opt, const ResOut& r, KOp
   return KS_OK;
 }
 
+// The autotuner's trials for the operating points of batch b: each kernel the
+// batch can run (the per-topology kernel when the plan gets one, the generic
+// kernel) with 1, 2 and 4 circuits per thread of the persistent grid, run twice
+// on the batch's own circuits (outputs into the caller's buffers) and timed by
+// CUDA events on the second run; the fastest wins.
+static int op_autotune(ks_batch* b, const ks_options* opt, const KOpts& base, const double* x0_dev, double* out_x_dev,
+                       int32_t* out_status_dev, int32_t* out_iters_dev, cudaStream_t st, ks_plan::Tuned* best) {
+  ks_options oo = opt ? *opt : ks_options{};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    set_error("ks_op: autotune: event creation failed");
+    return KS_ECUDA;
+  }
+  best->ms = -1;
+  int rc = KS_OK;
+  for (int be : {KS_BACKEND_SPECIALIZED, KS_BACKEND_GENERIC}) {
+    oo.backend = be;
+    const KsSpec* ks = nullptr;
+    if (pick_kernel(b, &oo, ksj::KIND_OP, &ks) != KS_OK || (be == KS_BACKEND_SPECIALIZED && !ks)) continue;
+    for (int cpt : {1, 2, 4}) {
+      KOpts o = base;
+      o.cpt = cpt;
+      float ms = -1;
+      for (int rep = 0; rep < 2 && !rc; rep++) {
+        cudaEventRecord(e0, st);
+        const int lr = ks_launch_op(b->dev, o, x0_dev, out_x_dev, out_status_dev, out_iters_dev,
+                                    opt ? opt->deadline_s : 0.0, st, ks);
+        cudaEventRecord(e1, st);
+        if (lr == -2) { ms = -1; break; }  // too large for this kernel: not a candidate
+        if (lr || cudaEventSynchronize(e1) != cudaSuccess) {
+          set_error(std::string("ks_op: autotune: ") + cudaGetErrorString(cudaGetLastError()));
+          rc = KS_ECUDA;
+          break;
+        }
+        cudaEventElapsedTime(&ms, e0, e1);
+      }
+      if (rc) break;
+      if (ms >= 0 && (best->ms < 0 || ms < best->ms)) {
+        best->backend = be; best->cpt = cpt; best->ms = ms;
+        best->kernel = ks ? (ks->reg ? KS_KERNEL_SPEC_REG : KS_KERNEL_SPEC_SMEM) : KS_KERNEL_GENERIC;
+      }
+    }
+    if (rc) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!rc && best->ms < 0) { set_error("ks_op: system too large for the dense kernels"); rc = KS_EUNSUPPORTED; }
+  return rc;
+}
+
 static int op_async(ks_batch* b, const ks_options* opt, const double* x0_dev, double* out_x_dev,
                     int32_t* out_status_dev, int32_t* out_iters_dev, const ResOut& res, void* stream) {
   if (!b) return KS_EINVAL;
@@ -397,6 +471,26 @@ static int op_async(ks_batch* b, const ks_options* opt, const double* x0_dev, do
     if (res.elem) CK(cudaMemsetAsync(res.elem, 0, sizeof(double) * KS_RES_COLS * ne * b->B, st));
     if (res.ledger) CK(cudaMemsetAsync(res.ledger, 0, sizeof(double) * KS_LEDGER_COLS * b->B, st));
     b->last_kernel = KS_KERNEL_GENERIC;
+  } else if (opt && opt->autotune > 0) {
+    const std::pair<int, int> key{ksj::KIND_OP, size_bucket(b->B)};
+    ks_plan::Tuned t{};
+    bool have = false;
+    {
+      std::lock_guard<std::mutex> g(b->plan->tune_mu);
+      auto it = b->plan->tuned.find(key);
+      if (it != b->plan->tuned.end()) { t = it->second; have = true; }
+    }
+    if (!have) {
+      rc = batch_setup(b, 0.0, 0.0, st);
+      if (!rc) rc = op_autotune(b, opt, o, x0_dev, out_x_dev, out_status_dev, out_iters_dev, st, &t);
+      if (rc) return rc;
+      std::lock_guard<std::mutex> g(b->plan->tune_mu);
+      b->plan->tuned[key] = t;
+    }
+    ks_options oo = *opt;
+    oo.backend = t.backend;
+    rc = pick_kernel(b, &oo, ksj::KIND_OP, &ks);
+    o.cpt = t.cpt;
   } else {
     rc = pick_kernel(b, opt, ksj::KIND_OP, &ks);
   }

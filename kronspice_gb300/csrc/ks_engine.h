@@ -127,6 +127,7 @@ struct KOpts {
   double* res_scratch;     // [n_state][B]: the device-state copy the round-off load runs on
   double ledger_tol;       // relative residual limit (em.DefaultTolerance 1e-9)
   int32_t energy_check;    // 0: Options.SkipEnergyCheck
+  int32_t cpt;             // circuits per thread the persistent grid is sized for (0: KS_CIRCUITS_PER_THREAD)
 };
 
 #ifndef __CUDACC_RTC__

@@ -116,13 +116,14 @@ __global__ void __launch_bounds__(T) k_dc_sweep(KPlan plan, KOpts o, const doubl
 
 // Blocks of T threads that keep every SM full (persistent grid), capped by the work.
 template <typename K>
-static unsigned persistent_grid(K kernel, int T, size_t smem, int64_t B) {
+static unsigned persistent_grid(K kernel, int T, size_t smem, int64_t B, int cpt = 0) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, T, smem);
   if (per < 1) per = 1;
-  int64_t need = (B + (int64_t)T * circuits_per_thread() - 1) / ((int64_t)T * circuits_per_thread());
+  if (cpt <= 0) cpt = circuits_per_thread();
+  int64_t need = (B + (int64_t)T * cpt - 1) / ((int64_t)T * cpt);
   int64_t g = (int64_t)sms * per;
   return (unsigned)(need < g ? need : g);
 }
@@ -143,7 +144,8 @@ int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, doubl
     K32 k32{b.values32, b.derived32, b.state32};
     if (!b.values32 || !b.derived32 || !b.state32) k32 = K32{nullptr, nullptr, nullptr};
     void* args[] = {&ko, &values, &derived, &state, &work, &B, &x0, &out_x, &out_status, &out_iters, &dl, &queue, &k32};
-    int64_t need = (B + (int64_t)kspec->T * circuits_per_thread() - 1) / ((int64_t)kspec->T * circuits_per_thread());
+    const int cpt = o.cpt > 0 ? o.cpt : circuits_per_thread();
+    int64_t need = (B + (int64_t)kspec->T * cpt - 1) / ((int64_t)kspec->T * cpt);
     unsigned grid = (unsigned)(need < kspec->blocks ? need : kspec->blocks);
     std::string err;
     if (ksj::launch(kspec->fn, grid, kspec->T, kspec->smem, stream, args, &err)) { ksh::set_error(err); return -1; }
@@ -162,7 +164,7 @@ int ks_launch_op(const KsDeviceBatch& b, const KOpts& o, const double* x0, doubl
   if (!b.values32 || !b.derived32 || !b.state32) k32 = K32{nullptr, nullptr, nullptr};
   auto go = [&](auto kernel, int threads) {
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    unsigned grid = persistent_grid(kernel, threads, sm, b.B);
+    unsigned grid = persistent_grid(kernel, threads, sm, b.B, o.cpt);
     kernel<<<grid, threads, sm, st>>>(b.plan, o, b.values, b.derived, b.state, b.work, b.B, x0, out_x, out_status,
                                       out_iters, dl, b.queue, k32);
   };

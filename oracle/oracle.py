@@ -43,7 +43,7 @@ class Options(ctypes.Structure):
                 ("deadline_s", ctypes.c_double), ("mixed_passes", ctypes.c_int32),
                 ("fp32_start_iters", ctypes.c_int32), ("start_check", ctypes.c_double),
                 ("ledger_tol", ctypes.c_double), ("skip_energy_check", ctypes.c_int32),
-                ("step_predictor", ctypes.c_int32)]
+                ("step_predictor", ctypes.c_int32), ("autotune", ctypes.c_int32)]
 
 
 class TranSpec(ctypes.Structure):
