@@ -30,8 +30,8 @@ def test_autotune_picks_keeps_and_matches():
     assert np.allclose(x1, x0, rtol=1e-7, atol=1e-10)
     # later calls of the bucket reuse the choice; another bucket is tuned on its own
     b.op(analysis.Options(reltol=1e-6, precision="fp64", autotune=True))
-    assert plan.tuned(16384) == t and plan.tuned(10000) == t  # 10,000 and 16,384 share the 2^13 bucket
-    assert plan.tuned(1000) is None
+    assert plan.tuned(16384) == t and plan.tuned(20000) == t  # 16,384 and 20,000 share the 2^14 bucket
+    assert plan.tuned(10000) is None
     pk = orc.Packed(el, nn, vals[0])
     _, isv = orc.unknowns(pk)
     for c in range(0, 16384, 1021):
