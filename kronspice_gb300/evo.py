@@ -16,7 +16,7 @@ keep the reference's per-candidate form (an Eval with op(), ac(spec), tran(spec)
 that raise the analysis error of that candidate), so a candidate's terms,
 fitness and failure class are what the worker pool computes.
 """
-from dataclasses import dataclass, field, replace
+from dataclasses import dataclass, replace
 import math
 
 import numpy as np
