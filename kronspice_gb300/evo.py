@@ -572,3 +572,38 @@ def _score_group(g, objectives, out, fail):
             continue
         ind.terms = [float(t) for t in terms[c]]
         ind.fitness = float(np.dot(w, terms[c]))
+
+
+def evaluate_values(circuit, values, objectives, options=None, genes=None, capacity=20000):
+    """Score candidates of one topology given as value vectors (the value genome,
+    Eval.Parts = -1): row i of `values` is candidate i's value vector in the
+    layout circuit.pack() gives, so no circuit is built or packed per candidate.
+    Each row is validated as circuit.Validate would the decoded circuit; then the
+    candidates are scored as evaluate scores one topology group."""
+    opt = options or analysis.Options()
+    el, v0, _ = circuit.pack()
+    vals = np.ascontiguousarray(values, dtype=np.float64)
+    if vals.ndim != 2 or vals.shape[1] != len(v0):
+        raise ValueError("evaluate_values: values must be [n_candidates][%d]" % len(v0))
+    n = vals.shape[0]
+    out = [Individual(values=list(genes[i]) if genes is not None else []) for i in range(n)]
+
+    def fail(ind, err):
+        ind.fitness, ind.failure = penalty(err)
+        ind.error = str(err)
+        ind.terms = None
+
+    ok, packed = [], {}
+    for i in range(n):
+        err = analysis.validate_packed(el, circuit.n_nodes, vals[i])
+        if isinstance(err, analysis.ErrFloatingNode) and analysis.validate_packed(el, circuit.n_nodes, vals[i], True) is None:
+            err = None
+        if err is not None:
+            fail(out[i], err)
+            continue
+        ok.append(i)
+        packed[i] = (el, vals[i])
+    if ok:
+        g_opt = opt if len(ok) >= 256 or opt.kernel != "auto" else replace(opt, kernel="generic")
+        _score_group(_Group(ok, [circuit] * n, packed, g_opt, capacity), objectives, out, fail)
+    return out

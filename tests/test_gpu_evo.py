@@ -126,3 +126,22 @@ def test_transient_objectives_match_the_worker_pool():
         fail, terms, fit, ms = oracle_score(ckt, objectives)
         assert ind.failure == fail == "", (k, ind)
         assert np.allclose(ind.terms, terms, rtol=1e-6, atol=1e-9), (k, ind.terms, terms)
+
+
+def test_value_genomes_score_as_circuits():
+    """evaluate_values on the value vectors of one topology scores each candidate
+    exactly as evaluate does on the built circuits (invalid rows included)."""
+    g = np.random.default_rng(5)
+    pop = [lowpass(r, c, rl) for r, c, rl in zip(g.uniform(500, 5e3, 400), g.uniform(1e-9, 1e-7, 400),
+                                                 g.uniform(2e3, 2e4, 400))]
+    pop[7] = lowpass(1e3, -1e-9, 1e4)  # invalid: a negative capacitance
+    spec = analysis.ACSpec("dec", 10, 10.0, 1e6)
+    objectives = [evo.gain_at_objective("out", "in", spec, 1e3, -3.0), evo.op_voltage("out", 1.0),
+                  evo.supply_power("V1")]
+    a = evo.evaluate(pop, objectives)
+    vals = np.stack([c.pack()[1] for c in pop])
+    b = evo.evaluate_values(pop[0], vals, objectives)
+    for x, y in zip(a, b):
+        assert x.failure == y.failure and x.fitness == y.fitness and x.terms == y.terms
+    assert b[7].failure == "invalid"
+
