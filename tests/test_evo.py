@@ -58,3 +58,89 @@ def test_invalid_candidates_are_penalized_without_analysis():
     for ind in out:
         assert ind.failure == "invalid" and ind.fitness == evo.PENALTY_INVALID and ind.terms is None, ind
     assert out[1].values == [2.0]
+
+
+class FakeGroup:
+    """A topology group whose batched analyses are given arrays (no GPU)."""
+
+    def __init__(self, circuit, op, ac):
+        m = len(op[1])
+        self.idx, self.circuits, self.row = list(range(m)), [circuit] * m, {i: i for i in range(m)}
+        self.cache = {"op": op}
+        self._ac = ac
+
+    def op(self):
+        return self.cache["op"]
+
+    def ac(self, spec):
+        self.cache[("ac", spec.variation, spec.points, spec.fstart, spec.fstop)] = self._ac
+        return self._ac
+
+
+def synthetic(m, seed):
+    b = kc.Builder("lp")
+    b.voltage_source("V1", "in", "0", 2.0, ac=(1.0, 0.0))
+    b.resistor("R1", "in", "out", 1e3).capacitor("C1", "out", "0", 1e-8).resistor("RL", "out", "0", 1e4)
+    ckt = b.build()
+    g = np.random.default_rng(seed)
+    n, ne = 3, 4
+    x = g.normal(size=(m, n))
+    st = np.zeros(m, np.int32)
+    elem = g.normal(size=(m, ne, analysis.RES_COLS))
+    led = np.abs(g.normal(size=(m, analysis.LEDGER_COLS)))
+    spec = analysis.ACSpec("dec", 5, 10.0, 1e5)
+    freqs = spec.frequencies()
+    xa = g.normal(size=(m, len(freqs), n)) + 1j * g.normal(size=(m, len(freqs), n))
+    sta = np.zeros(m, np.int32)
+    st[1] = sta[1] = 1                 # singular
+    sta[2] = 3                         # the AC's operating point did not converge
+    xa[3, 4, 0] = 0                    # V(in) = 0 at one frequency: no transfer
+    return ckt, (x, st, elem, led), (freqs, xa, sta), spec
+
+
+def test_batch_forms_match_the_per_candidate_objectives():
+    """Each built-in objective's vectorized form gives, candidate for candidate,
+    the value or the failure class its per-candidate form gives."""
+    ckt, op, ac, spec = synthetic(40, 1)
+    g = FakeGroup(ckt, op, ac)
+    objectives = [evo.gain_at_objective("out", "in", spec, 1e3, -3.0), evo.gain_at_objective("out", "0", spec, 55.0, 6.0),
+                  evo.op_voltage("out", 1.0), evo.supply_power("V1"), evo.model_supplied_limit(0.1),
+                  evo.op_voltage("nowhere", 1.0)]
+    for ob in objectives:
+        v, fails = ob.batch(evo.GroupView(g))
+        for c in range(40):
+            try:
+                want, want_err = ob.eval(evo.Eval(ckt, [], g, c)), None
+            except analysis.KronspiceError as e:
+                want, want_err = None, e
+            if want_err is None and fails[c] is None:
+                assert v[c] == pytest.approx(want, rel=1e-12, abs=1e-300), (ob.name, c)
+            else:
+                assert want_err is not None and fails[c] is not None, (ob.name, c, want_err, fails[c])
+                assert evo.penalty(want_err) == evo.penalty(fails[c]), (ob.name, c)
+
+
+def test_group_scoring_first_failure_and_model_supplied():
+    """_score_group: a candidate stops at its first failing objective (its class
+    that objective's), the others get the weighted sum of their terms, and the
+    model-supplied power counts the operating point only where an objective of
+    the candidate read it."""
+    ckt, op, ac, spec = synthetic(8, 2)
+    g = FakeGroup(ckt, op, ac)
+    objectives = [evo.gain_at_objective("out", "in", spec, 1e3, -3.0), evo.op_voltage("out", 1.0)]
+    objectives[1].weight = 2.0
+    out = [evo.Individual(values=[]) for _ in range(8)]
+
+    def fail(ind, err):
+        ind.fitness, ind.failure = evo.penalty(err)
+        ind.error = str(err)
+        ind.terms = None
+    evo._score_group(g, objectives, out, fail)
+    assert out[1].failure == "singular" and out[2].failure == "no-convergence" and out[3].failure == "no-measurement"
+    assert out[1].error.startswith("gain out at 1000 Hz:")
+    for c in (0, 4, 5, 6, 7):
+        t = out[c].terms
+        assert out[c].failure == "" and out[c].fitness == pytest.approx(t[0] + 2.0 * t[1])
+        assert out[c].model_supplied == pytest.approx(op[3][c, analysis.LEDGER["model_supplied"]])
+    # failed at the AC objective before the operating-point one ran: no model-supplied power
+    assert out[2].model_supplied == 0.0 and out[3].model_supplied == 0.0
