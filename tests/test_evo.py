@@ -144,3 +144,91 @@ def test_group_scoring_first_failure_and_model_supplied():
         assert out[c].model_supplied == pytest.approx(op[3][c, analysis.LEDGER["model_supplied"]])
     # failed at the AC objective before the operating-point one ran: no model-supplied power
     assert out[2].model_supplied == 0.0 and out[3].model_supplied == 0.0
+
+
+class OracleBatch:
+    """analysis.Batch restated over the oracle, circuit by circuit (no GPU): the
+    evaluator's whole host pipeline runs against it."""
+    calls = []
+
+    def __init__(self, plan, vals):
+        from oracle import oracle as orc
+        self.orc, self.plan, self.vals = orc, plan, np.asarray(vals)
+
+    def _pk(self, r):
+        return self.orc.Packed(self.plan.elements, self.plan.n_nodes, self.vals[r])
+
+    def op_results(self, opt=None):
+        OracleBatch.calls.append("op")
+        B, n, ne = len(self.vals), self.plan.n, len(self.plan.elements)
+        x, st, it = np.zeros((B, n)), np.zeros(B, np.int32), np.zeros(B, np.int32)
+        elem, led = np.zeros((B, ne, analysis.RES_COLS)), np.zeros((B, analysis.LEDGER_COLS))
+        for r in range(B):
+            st[r], x[r], elem[r], led[r], it[r], _ = self.orc.op_results(self._pk(r))
+        return x, st, it, elem, led
+
+    def ac(self, freqs, opt=None):
+        OracleBatch.calls.append("ac")
+        B, n = len(self.vals), self.plan.n
+        x, st, it = np.zeros((B, len(freqs), n), complex), np.zeros(B, np.int32), np.zeros(B, np.int32)
+        for r in range(B):
+            st[r], x[r], _ = self.orc.ac(self._pk(r), freqs)
+        return x, st, it
+
+    def tran_results(self, spec, opt=None, capacity=0):
+        OracleBatch.calls.append(("tran", capacity))
+        sp = spec.c()
+        osp = self.orc.TranSpec(sp.step, sp.stop, sp.start, sp.max_step, sp.uic, sp.method, 0, sp.max_steps,
+                                sp.chgtol, sp.trtol, sp.min_step)
+        B, n, ne = len(self.vals), self.plan.n, len(self.plan.elements)
+        wave, tim = np.zeros((B, capacity, n)), np.zeros((B, capacity))
+        led = np.zeros((B, capacity, analysis.TPOINT_COLS))
+        npts, st = np.zeros(B, np.int32), np.zeros(B, np.int32)
+        for r in range(B):
+            out = self.orc.tran_results(self._pk(r), osp)
+            k = min(len(out[1]), capacity)
+            st[r], npts[r] = out[0], k
+            tim[r, :k], wave[r, :k], led[r, :k] = out[1][:k], out[2][:k], out[4][:k]
+        return wave, tim, None, led, None, npts, st, None, None
+
+
+def test_evaluate_against_the_oracle_pipeline(monkeypatch):
+    """evaluate() end to end on the CPU with the oracle standing in for the
+    batched engine: three topologies and invalid candidates in one generation,
+    each analysis run once per group, transient objectives on a recording
+    capacity that has to grow, and per-candidate results equal to scoring each
+    circuit alone."""
+    monkeypatch.setattr(evo.analysis, "Batch", OracleBatch)
+    OracleBatch.calls = []
+    g = np.random.default_rng(6)
+    pop = []
+    for r, c in zip(g.uniform(500, 2e3, 6), g.uniform(1e-8, 1e-7, 6)):
+        b = kc.Builder("rc")
+        b.voltage_source("V1", "in", "0", 0.0, wave="pulse", args=[0, 5, 0, 1e-6, 1e-6, 5e-5, 1e-4], ac=(1.0, 0.0))
+        b.resistor("R1", "in", "out", r).capacitor("C1", "out", "0", c)
+        pop.append(b.build())
+    b = kc.Builder("rl")
+    b.voltage_source("V1", "in", "0", 0.0, wave="pulse", args=[0, 5, 0, 1e-6, 1e-6, 5e-5, 1e-4], ac=(1.0, 0.0))
+    b.resistor("R1", "in", "out", 1e3).inductor("L1", "out", "0", 1e-2)
+    pop.append(b.build())
+    b = kc.Builder("loop")
+    b.voltage_source("V1", "in", "0", 1.0).voltage_source("V2", "in", "0", 2.0).resistor("R1", "in", "out", 1e3)
+    b.resistor("R2", "out", "0", 1e3)
+    pop.append(b.build())
+    b = kc.Builder("rc")
+    b.voltage_source("V1", "in", "0", 0.0).resistor("R1", "in", "out", 1e3).capacitor("C1", "out", "0", -1e-8)
+    pop.append(b.build())  # invalid: a negative capacitance
+    spec = analysis.TranSpec(step=1e-6, stop=4e-4)
+    acs = analysis.ACSpec("dec", 5, 10.0, 1e5)
+    objectives = [evo.gain_at_objective("out", "in", acs, 1e3, -3.0), evo.tran_average("out", spec, 2e-4, 4e-4, 2.5),
+                  evo.supply_power("V1")]
+    out = evo.evaluate(pop, objectives, capacity=64)
+    # one AC and one transient per topology that reached them, the capacity grown from 64
+    assert OracleBatch.calls.count("ac") == 3
+    trans = [c for c in OracleBatch.calls if isinstance(c, tuple)]
+    assert trans[0] == ("tran", 64) and trans[-1][1] > 64
+    assert [ind.failure for ind in out[7:]] == ["singular", "invalid"]
+    assert all(ind.failure == "" for ind in out[:7])
+    for ckt, ind in zip(pop[:7], out[:7]):
+        alone = evo.evaluate([ckt], objectives, capacity=100000)[0]
+        assert ind.terms == pytest.approx(alone.terms, rel=1e-12) and ind.fitness == pytest.approx(alone.fitness)
