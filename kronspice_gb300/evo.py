@@ -38,6 +38,10 @@ class ErrNoMeasurement(analysis.KronspiceError):
     """analysis.ErrNoMeasurement: an objective could not take its measurement."""
 
 
+class ErrUnknownNode(analysis.KronspiceError):
+    """analysis.ErrUnknownNode: a port names a node the circuit does not have."""
+
+
 def penalty(err):
     """Penalty (evo/fitness.go:659-681): (fitness, class) of an evaluation error."""
     if isinstance(err, analysis.ErrInterrupted):
@@ -206,6 +210,45 @@ class _Group:
             self.cache[key] = (freqs, x, st)
         return self.cache[key]
 
+    def port(self, plus, minus):
+        """analysis.OpenShort (analysis/port.go:30-69) for every candidate: Voc from
+        the group's operating points, Isc from the operating points of the same
+        circuits with a 0 V probe source appended from plus to minus (its
+        current, into its + terminal, is what the circuit drives out of plus).
+        (voc [m], isc [m], failures [m])."""
+        key = ("port", plus.lower(), minus.lower())
+        if key in self.cache:
+            return self.cache[key]
+        ckt = self.circuits[0]
+        ip, im = ckt.node_index(plus), ckt.node_index(minus)
+        m = len(self.idx)
+        if ip < 0 or im < 0 or ip == im:
+            err = ErrUnknownNode("analysis: unknown node: %s or %s" % (plus, minus) if ip != im or ip < 0
+                                 else "analysis: unknown node: %s and %s are the same node" % (plus, minus))
+            self.cache[key] = (np.zeros(m), np.zeros(m), [err] * m)
+            return self.cache[key]
+        x, st, _, _ = self.op()
+        vp = np.zeros(m) if ip == 0 else x[:, ip - 1]
+        vm = np.zeros(m) if im == 0 else x[:, im - 1]
+        fails = [None if s == 0 else type(analysis.status_error(s))("open circuit: %s" % analysis.status_error(s))
+                 for s in st]
+        # the short: one more element, a V source with its DC value 0 (value block dc, ac magnitude, ac phase)
+        from .circuit import ELEMENT_DTYPE, KIND, F_HAS_DC
+        el = np.zeros(len(self.el) + 1, dtype=ELEMENT_DTYPE)
+        el[:-1] = self.el
+        el[-1]["kind"], el[-1]["node"], el[-1]["flags"] = KIND["V"], [ip, im, 0, 0], F_HAS_DC
+        el[-1]["param"] = self.vals.shape[1]
+        vals = np.hstack([self.vals, np.zeros((m, 3))])
+        plan = analysis.Plan(el, ckt.n_nodes, vals.shape[1])
+        xs, sts, _, elem, _ = analysis.Batch(plan, vals).op_results(self.options)
+        isc = elem[:, len(self.el), analysis.RES["current"]]
+        for c in range(m):
+            if fails[c] is None and sts[c] != 0:
+                e = analysis.status_error(sts[c])
+                fails[c] = type(e)("short circuit: %s" % e)
+        self.cache[key] = (vp - vm, isc, fails)
+        return self.cache[key]
+
     def tran(self, spec):
         key = ("tran",) + tuple(sorted(vars(spec).items()))
         if key not in self.cache:
@@ -261,6 +304,13 @@ class Eval:
         r = Waveforms(self.circuit, tim[self._r, :k], wave[self._r, :k], led[self._r, :k])
         self.model_supplied = max(self.model_supplied, r.model_supplied)
         return r
+
+    def port(self, plus, minus):
+        """Eval.Port (evo/fitness.go:191-205): (Voc, Isc) between plus and minus."""
+        voc, isc, fails = self._g.port(plus, minus)
+        if fails[self._r] is not None:
+            raise fails[self._r]
+        return float(voc[self._r]), float(isc[self._r])
 
     def memo(self, key, f):
         """Eval.Memo (evo/fitness.go:69-79): f once per candidate and key."""
@@ -360,6 +410,20 @@ def supply_power(*sources):
             p -= elem[:, k, analysis.RES["power"]]
         return np.maximum(0.0, p), fails
     return Objective("supply power", 1.0, ev, batch=batch)
+
+
+def port_voc(plus, minus, target):
+    """PortVoc (evo/fitness.go:608-617): the open-circuit voltage between plus and minus."""
+    def ev(e):
+        return rel_err(e.port(plus, minus)[0], target, 1e-6)
+    return Objective("Voc %s,%s" % (plus, minus), 1.0, ev)
+
+
+def port_isc(plus, minus, target):
+    """PortIsc (evo/fitness.go:619-628): the short-circuit current out of plus."""
+    def ev(e):
+        return rel_err(e.port(plus, minus)[1], target, 1e-12)
+    return Objective("Isc %s,%s" % (plus, minus), 1.0, ev)
 
 
 def model_supplied_limit(pmax):

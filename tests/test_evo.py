@@ -232,3 +232,25 @@ def test_evaluate_against_the_oracle_pipeline(monkeypatch):
     for ckt, ind in zip(pop[:7], out[:7]):
         alone = evo.evaluate([ckt], objectives, capacity=100000)[0]
         assert ind.terms == pytest.approx(alone.terms, rel=1e-12) and ind.fitness == pytest.approx(alone.fitness)
+
+
+def test_port_objectives_against_the_thevenin_values(monkeypatch):
+    """PortVoc / PortIsc over OpenShort (analysis/port.go:30-69): a divider's
+    open-circuit voltage V R2 / (R1 + R2) and short-circuit current V / R1 (out of
+    plus through the probe), the short run as one more batch of the group; a
+    port on one node is an unknown-node error."""
+    monkeypatch.setattr(evo.analysis, "Batch", OracleBatch)
+    g = np.random.default_rng(8)
+    r1, r2 = g.uniform(500, 5e3, 5), g.uniform(500, 5e3, 5)
+    pop = []
+    for a, b_ in zip(r1, r2):
+        b = kc.Builder("div")
+        b.voltage_source("V1", "in", "0", 5.0).resistor("R1", "in", "out", a).resistor("R2", "out", "0", b_)
+        pop.append(b.build())
+    out = evo.evaluate(pop, [evo.port_voc("out", "0", 2.5), evo.port_isc("out", "gnd", 5e-3)])
+    for ind, a, b_ in zip(out, r1, r2):
+        assert ind.failure == "", ind
+        assert ind.terms[0] == pytest.approx(evo.rel_err(5 * b_ / (a + b_), 2.5, 1e-6), rel=1e-9)
+        assert ind.terms[1] == pytest.approx(evo.rel_err(5 / a, 5e-3, 1e-12), rel=1e-9)
+    bad = evo.evaluate(pop[:1], [evo.port_voc("out", "out", 1.0)])[0]
+    assert bad.failure == "error" and "same node" in bad.error
