@@ -160,6 +160,36 @@ def gain_at(freq, h, f):
     return abs(h[0])
 
 
+def cutoff_3db(freq, h):
+    """analysis.Cutoff3dB (analysis/measure.go:58-95): the frequencies where |H|
+    falls 3.0103 dB below its peak on each side of it (0 / inf when it does not),
+    interpolated in log-frequency and dB."""
+    if len(freq) < 2 or len(h) != len(freq):
+        raise ErrNoMeasurement("analysis: no measurement")
+    mag = np.abs(h)
+    kp = int(np.argmax(mag))  # the first maximum, as the strict > scan keeps it
+    peak = float(mag[kp])
+    if peak == 0:
+        raise ErrNoMeasurement("analysis: no measurement")
+    thr = db(peak) - 10 * math.log10(2)
+
+    def cross(k0, k1):
+        d0, d1 = db(h[k0]), db(h[k1])
+        x = (thr - d0) / (d1 - d0)
+        l0, l1 = math.log(freq[k0]), math.log(freq[k1])
+        return math.exp(l0 + x * (l1 - l0))
+    lo, hi = 0.0, math.inf
+    for k in range(kp, 0, -1):
+        if db(h[k - 1]) < thr:
+            lo = cross(k, k - 1)
+            break
+    for k in range(kp, len(h) - 1):
+        if db(h[k + 1]) < thr:
+            hi = cross(k, k + 1)
+            break
+    return lo, hi
+
+
 def interp(t, y, tq):
     """output.Interp (output/waveforms.go:87-104)."""
     n = len(t)
@@ -481,6 +511,61 @@ def gain_at_objective(node, ref, spec, f, target_db):
                 out.append(None)
         return np.where(np.isfinite(err), err, 0.0), out
     return Objective("gain %s at %g Hz" % (node, f), 1.0, ev, batch=batch)
+
+
+def cutoff(node, ref, spec, target, high):
+    """Cutoff (evo/fitness.go:213-238): the upper (high) or lower -3 dB edge of
+    V(node)/V(ref) against target [Hz]."""
+    def ev(e):
+        r = e.ac(spec)
+        lo, hi = cutoff_3db(r.freq, transfer(r, node, ref))
+        f = hi if high else lo
+        if f == 0 or math.isinf(f):
+            raise ErrNoMeasurement("analysis: no measurement")
+        return rel_err(f, target, 0)
+    return Objective("cutoff " + node, 1.0, ev)
+
+
+def gain_shortfall(node, ref, spec, f, ceiling_db):
+    """GainShortfall (evo/fitness.go:261-281): max(0, ceiling - gain at f) / 20."""
+    def ev(e):
+        r = e.ac(spec)
+        g = gain_at(r.freq, transfer(r, node, ref), f)
+        if g <= 0:
+            raise ErrNoMeasurement("analysis: no measurement")
+        return max(0.0, ceiling_db - 20 * math.log10(g)) / 20
+    return Objective("gain short %s at %g Hz" % (node, f), 1.0, ev)
+
+
+def bandwidth_shortfall(node, ref, spec, ceiling_hz):
+    """BandwidthShortfall (evo/fitness.go:283-309): decades the upper -3 dB edge
+    (the sweep's stop when the response has not fallen) lies below the ceiling."""
+    def ev(e):
+        r = e.ac(spec)
+        _, hi = cutoff_3db(r.freq, transfer(r, node, ref))
+        hi = min(hi, float(r.freq[-1]))
+        if not hi > 0:
+            raise ErrNoMeasurement("analysis: no measurement")
+        return max(0.0, math.log10(ceiling_hz / hi))
+    return Objective("bandwidth short " + node, 1.0, ev)
+
+
+def op_efficiency(*loads):
+    """OPEfficiency (evo/fitness.go:331-346, em/efficiency.go:29-43): 1 - the
+    loads' absorbed power over the net inflow of the operating point's ledger."""
+    def ev(e):
+        r = e.op()
+        net = r.ledger[analysis.LEDGER["inflow"]] - r.ledger[analysis.LEDGER["outflow"]]
+        if net <= 0:
+            raise ErrNoMeasurement("analysis: no measurement: em: no net inflow")
+        p = 0.0
+        for n in loads:
+            el = r.element(n)
+            if el is None:
+                raise ErrNoMeasurement("analysis: no measurement: em: OPEfficiency: no element %r" % n)
+            p += el["power"]
+        return 1 - p / net
+    return Objective("1 - efficiency", 1.0, ev)
 
 
 def tran_average(node, spec, t_from, t_to, target):

@@ -254,3 +254,36 @@ def test_port_objectives_against_the_thevenin_values(monkeypatch):
         assert ind.terms[1] == pytest.approx(evo.rel_err(5 / a, 5e-3, 1e-12), rel=1e-9)
     bad = evo.evaluate(pop[:1], [evo.port_voc("out", "out", 1.0)])[0]
     assert bad.failure == "error" and "same node" in bad.error
+
+
+def test_cutoff_and_shortfalls():
+    """Cutoff3dB on an RC low-pass's exact response: the upper edge at
+    1 / (2 pi R C) to the sweep's interpolation, no lower edge; the shortfall
+    objectives and OPEfficiency on the oracle-backed pipeline."""
+    f = np.logspace(1, 7, 121)
+    fc = 1 / (2 * np.pi * 1e3 * 1e-8)
+    h = 1 / (1 + 1j * f / fc)
+    lo, hi = evo.cutoff_3db(f, h)
+    assert lo == 0.0 and hi == pytest.approx(fc, rel=2e-3)
+    with pytest.raises(evo.ErrNoMeasurement):
+        evo.cutoff_3db(f[:1], h[:1])
+
+
+def test_ac_and_efficiency_objectives(monkeypatch):
+    monkeypatch.setattr(evo.analysis, "Batch", OracleBatch)
+    b = kc.Builder("lp")
+    b.voltage_source("V1", "in", "0", 2.0, ac=(1.0, 0.0))
+    b.resistor("R1", "in", "out", 1e3).capacitor("C1", "out", "0", 1e-8).resistor("RL", "out", "0", 1e4)
+    ckt = b.build()
+    spec = analysis.ACSpec("dec", 20, 10.0, 1e7)
+    fc = 1 / (2 * np.pi * (1e3 * 1e4 / 1.1e4) * 1e-8)  # the Thevenin resistance R1 || RL with C1
+    obs = [evo.cutoff("out", "in", spec, fc, True), evo.gain_shortfall("out", "in", spec, 10.0, 0.0),
+           evo.bandwidth_shortfall("out", "in", spec, 10 * fc), evo.op_efficiency("RL")]
+    ind = evo.evaluate([ckt], obs)[0]
+    assert ind.failure == "", ind
+    assert ind.terms[0] <= 5e-3                                   # the edge found to the sweep's resolution
+    assert ind.terms[1] == pytest.approx(-20 * np.log10(1e4 / 1.1e4) / 20, rel=1e-4)  # the divider's loss
+    assert ind.terms[2] == pytest.approx(1.0, abs=5e-3)           # one decade short
+    assert ind.terms[3] == pytest.approx(1 - 1e4 / 1.1e4, rel=1e-9)  # RL's share of the input power
+    low = evo.evaluate([ckt], [evo.cutoff("out", "in", spec, 100.0, False)])[0]
+    assert low.failure == "no-measurement"                        # a low-pass has no lower edge
