@@ -107,11 +107,18 @@ class ACResult:
 
 @dataclass
 class Waveforms:
-    """The candidate's output.Waveforms: accepted times, node voltages, per-point ledger."""
+    """The candidate's output.Waveforms: accepted times, node voltages, per-point
+    ledger and element series."""
     circuit: object
     time: np.ndarray
     x: np.ndarray       # [n_points][n]
     ledger: np.ndarray  # [n_points][TPOINT_COLS]
+    elements: np.ndarray = None  # [n_points][n_elem][2]: current, absorbed power
+
+    def power(self, name):
+        """Waveforms.P of the named element (absorbed power per point), or None."""
+        k = self.circuit.element_index(name)
+        return None if k < 0 or self.elements is None else self.elements[:, k, 1]
 
     def node_voltage(self, node):
         i = self.circuit.node_index(node)
@@ -292,7 +299,7 @@ class _Group:
                 if int(npts.max()) < cap or cap >= sp.max_steps + 2:
                     break
                 cap = min(cap * 4, sp.max_steps + 2)
-            self.cache[key] = (wave, tim, led, npts, st)
+            self.cache[key] = (wave, tim, led, npts, st, elem)
         return self.cache[key]
 
 
@@ -301,9 +308,10 @@ class Eval:
     circuit and gene values, and its analyses, each the candidate's slice of the
     group's batched run (the first request runs it for the whole group)."""
 
-    def __init__(self, circuit, values, group, row):
+    def __init__(self, circuit, values, group, row, parts=-1):
         self.circuit, self.values = circuit, values
         self._g, self._r = group, row
+        self.parts = parts  # evolved parts of a topology genome, -1 for a value genome
         self.model_supplied = 0.0
         self._memo = {}
 
@@ -328,10 +336,11 @@ class Eval:
 
     def tran(self, spec):
         """Eval.Tran (evo/fitness.go:171-189)."""
-        wave, tim, led, npts, st = self._g.tran(spec)
+        wave, tim, led, npts, st, elem = self._g.tran(spec)
         self._fail(st[self._r])
         k = int(npts[self._r])
-        r = Waveforms(self.circuit, tim[self._r, :k], wave[self._r, :k], led[self._r, :k])
+        r = Waveforms(self.circuit, tim[self._r, :k], wave[self._r, :k], led[self._r, :k],
+                      None if elem is None else elem[self._r, :k])
         self.model_supplied = max(self.model_supplied, r.model_supplied)
         return r
 
@@ -568,6 +577,132 @@ def op_efficiency(*loads):
     return Objective("1 - efficiency", 1.0, ev)
 
 
+@dataclass
+class Band:
+    """evo.Band (evo/fitness.go:364-370): between lo and hi [Hz] the gain must
+    lie within [min_db, max_db] (-inf / inf for an open side)."""
+    lo: float
+    hi: float
+    min_db: float
+    max_db: float
+
+
+MASK_VIOLATION_FLOOR = 0.1  # evo.MaskViolationFloor, evo/fitness.go:376
+
+
+def filter_mask(node, ref, spec, bands):
+    """FilterMask (evo/fitness.go:378-449): 0 inside the mask everywhere, else the
+    floor + the fraction of checked points outside + their mean excess in dB/20."""
+    def ev(e):
+        r = e.ac(spec)
+        h = transfer(r, node, ref)
+        fr = r.freq
+        n = bad = 0
+        excess = 0.0
+
+        def check(f, b):
+            nonlocal n, bad, excess
+            lo, hi = fr[0], fr[-1]  # a band edge a rounding error outside the sweep
+            if lo * (1 - 1e-9) < f < lo:
+                f = lo
+            elif hi < f < hi * (1 + 1e-9):
+                f = hi
+            g = gain_at(fr, h, f)
+            d_b = 20 * math.log10(g) if g > 0 else -math.inf
+            n += 1
+            d = 0.0
+            if d_b > b.max_db:
+                d = d_b - b.max_db
+            elif d_b < b.min_db:
+                d = min(b.min_db - d_b, 200.0)  # a dead output counts 200 dB
+            if d > 0:
+                bad += 1
+                excess += d
+        for b in bands:
+            check(b.lo, b)
+            for f in fr:
+                if b.lo < f < b.hi:
+                    check(f, b)
+            check(b.hi, b)
+        return 0.0 if bad == 0 else MASK_VIOLATION_FLOOR + bad / n + excess / 20 / n
+    return Objective("mask " + node, 1.0, ev)
+
+
+def active_bias(vmin, imin, imax):
+    """ActiveBias (evo/fitness.go:451-516): how near the best-biased transistor is
+    to its forward-active region at the operating point (0 inside, at most 1; 1
+    without a transistor)."""
+    def ev(e):
+        r = e.op()
+        c = e.circuit
+        best = 1.0
+        for k, el in enumerate(c.elements):
+            if el.kind not in ("Q", "M"):
+                continue
+            res = r.elements[k]
+            typ = c.models.get(el.model, ("",))[0]
+            sign = -1.0 if typ in ("pnp", "pmos") else 1.0
+            v, i = sign * res[analysis.RES["voltage"]], sign * res[analysis.RES["current"]]
+            d = max(0.0, (vmin - v) / vmin)
+            if i <= 0:
+                d += 1
+            elif i < imin:
+                d += math.log10(imin / i) / 3
+            elif i > imax:
+                d += math.log10(i / imax) / 3
+            if el.kind == "Q":  # nodes: collector, emitter, base
+                vc, ve, vb = (r.voltage(nm) for nm in el.nodes[:3])
+                vbe, vbc = sign * (vb - ve), sign * (vb - vc)
+                d += (max(0.0, 0.4 - vbe) + max(0.0, vbe - 1.0)) / 0.5
+                d += max(0.0, vbc - 0.4) / 0.4
+            best = min(best, d)
+        return min(best, 1.0)
+    return Objective("active bias", 1.0, ev)
+
+
+def part_count():
+    """PartCount (evo/fitness.go:518-526): the evolved parts of a topology genome."""
+    def ev(e):
+        if e.parts < 0:
+            raise ErrNoMeasurement("analysis: no measurement: parts objective needs a topology genome")
+        return float(e.parts)
+    return Objective("parts", 1.0, ev)
+
+
+def _integrate(t, y, t_from, t_to):
+    """em.integrate (em/efficiency.go:83-94): trapezoids over the points, interpolated at the ends."""
+    s_ = 0.0
+    for k in range(1, len(t)):
+        t0, t1 = t[k - 1], t[k]
+        if t1 <= t_from or t0 >= t_to:
+            continue
+        a, b = max(t0, t_from), min(t1, t_to)
+        s_ += 0.5 * (interp(t, y, a) + interp(t, y, b)) * (b - a)
+    return s_
+
+
+def tran_efficiency(spec, t_from, t_to, *loads):
+    """TranEfficiency (evo/fitness.go:347-362, em/efficiency.go:52-80): 1 - the
+    loads' absorbed energy over the net energy the exterior delivered in [from, to]."""
+    def ev(e):
+        wf = e.tran(spec)
+        if not t_to > t_from:
+            raise ErrNoMeasurement("analysis: no measurement: em: TranEfficiency: empty window")
+        load = np.zeros(len(wf.time))
+        for n in loads:
+            p = wf.power(n)
+            if p is None:
+                raise ErrNoMeasurement("analysis: no measurement: em: TranEfficiency: no element %r" % n)
+            load = load + p
+        e_load = _integrate(wf.time, load, t_from, t_to)
+        e_in = (_integrate(wf.time, wf.ledger[:, analysis.TPOINT["inflow"]], t_from, t_to)
+                - _integrate(wf.time, wf.ledger[:, analysis.TPOINT["outflow"]], t_from, t_to))
+        if e_in <= 0:
+            raise ErrNoMeasurement("analysis: no measurement: em: no net inflow")
+        return 1 - e_load / e_in
+    return Objective("1 - efficiency", 1.0, ev)
+
+
 def tran_average(node, spec, t_from, t_to, target):
     """TranAverage (evo/fitness.go:553-583): the mean of V(node) over [from, to]."""
     def ev(e):
@@ -616,11 +751,12 @@ class Individual:
     model_supplied: float = 0.0
 
 
-def evaluate(circuits, objectives, options=None, values=None, capacity=20000):
+def evaluate(circuits, objectives, options=None, values=None, capacity=20000, parts=None):
     """Score a population (evaluator.evaluate + one, evo/engine.go:518-612): one
     Individual per circuit, in order.  `values` are the candidates' gene values
-    (reported back); `capacity` bounds the accepted points a transient records
-    per candidate."""
+    (reported back); `capacity` is the transient recording capacity a group
+    starts from; `parts` the evolved part counts of topology genomes (None: value
+    genomes, Eval.Parts = -1)."""
     opt = options or analysis.Options()
     n = len(circuits)
     out = [Individual(values=list(values[i]) if values is not None else []) for i in range(n)]
@@ -660,11 +796,11 @@ def evaluate(circuits, objectives, options=None, values=None, capacity=20000):
         if groups[i] not in seen:
             seen.append(groups[i])
     for g in seen:
-        _score_group(g, objectives, out, fail)
+        _score_group(g, objectives, out, fail, parts)
     return out
 
 
-def _score_group(g, objectives, out, fail):
+def _score_group(g, objectives, out, fail, parts=None):
     """The objectives of one topology group in order (:591-607), each in its batch
     form when it has one (else candidate by candidate); a candidate stops at its
     first failing objective."""
@@ -694,7 +830,7 @@ def _score_group(g, objectives, out, fail):
         for c in live:
             if evals[c] is None:
                 i = g.idx[c]
-                evals[c] = Eval(g.circuits[c], out[i].values, g, c)
+                evals[c] = Eval(g.circuits[c], out[i].values, g, c, -1 if parts is None else parts[i])
             try:
                 v = ob.eval(evals[c])
                 if v is None or math.isnan(v) or math.isinf(v) or v < 0:

@@ -183,13 +183,14 @@ class OracleBatch:
         B, n, ne = len(self.vals), self.plan.n, len(self.plan.elements)
         wave, tim = np.zeros((B, capacity, n)), np.zeros((B, capacity))
         led = np.zeros((B, capacity, analysis.TPOINT_COLS))
+        elem = np.zeros((B, capacity, ne, 2))
         npts, st = np.zeros(B, np.int32), np.zeros(B, np.int32)
         for r in range(B):
             out = self.orc.tran_results(self._pk(r), osp)
             k = min(len(out[1]), capacity)
             st[r], npts[r] = out[0], k
-            tim[r, :k], wave[r, :k], led[r, :k] = out[1][:k], out[2][:k], out[4][:k]
-        return wave, tim, None, led, None, npts, st, None, None
+            tim[r, :k], wave[r, :k], elem[r, :k], led[r, :k] = out[1][:k], out[2][:k], out[3][:k], out[4][:k]
+        return wave, tim, elem, led, None, npts, st, None, None
 
 
 def test_evaluate_against_the_oracle_pipeline(monkeypatch):
@@ -287,3 +288,39 @@ def test_ac_and_efficiency_objectives(monkeypatch):
     assert ind.terms[3] == pytest.approx(1 - 1e4 / 1.1e4, rel=1e-9)  # RL's share of the input power
     low = evo.evaluate([ckt], [evo.cutoff("out", "in", spec, 100.0, False)])[0]
     assert low.failure == "no-measurement"                        # a low-pass has no lower edge
+
+
+def test_mask_bias_parts_and_transient_efficiency(monkeypatch):
+    """FilterMask, ActiveBias, PartCount and TranEfficiency on the oracle-backed
+    pipeline: a low-pass inside and outside a mask, a BJT stage biased active
+    and one driven into saturation, part counts of topology genomes, and a
+    resistive load's share of a transient's delivered energy."""
+    monkeypatch.setattr(evo.analysis, "Batch", OracleBatch)
+    b = kc.Builder("lp")
+    b.voltage_source("V1", "in", "0", 2.0, ac=(1.0, 0.0))
+    b.resistor("R1", "in", "out", 1e3).capacitor("C1", "out", "0", 1e-8).resistor("RL", "out", "0", 1e4)
+    lp = b.build()
+    spec = analysis.ACSpec("dec", 20, 10.0, 1e7)
+    ok = evo.filter_mask("out", "in", spec, [evo.Band(10.0, 1e3, -3.0, 0.0), evo.Band(1e6, 1e7, -np.inf, -20.0)])
+    tight = evo.filter_mask("out", "in", spec, [evo.Band(10.0, 1e5, -0.1, 0.0)])
+    r = evo.evaluate([lp, lp], [ok, tight, evo.part_count()], parts=[3, 5])
+    assert r[0].terms[0] == 0.0 and r[0].terms[1] > evo.MASK_VIOLATION_FLOOR and r[1].terms[2] == 5.0
+    assert evo.evaluate([lp], [evo.part_count()])[0].failure == "no-measurement"
+
+    def stage(rb):
+        b = kc.Builder("ce")
+        b.voltage_source("VCC", "vcc", "0", 10.0)
+        b.resistor("RB", "vcc", "b", rb).resistor("RC", "vcc", "c", 1e3)
+        b.model("qn", "npn", {"is": 1e-15, "bf": 100})
+        b.bjt("Q1", "c", "b", "0", "qn")
+        return b.build()
+    bias = evo.evaluate([stage(1e6), stage(1e4)], [evo.active_bias(1.0, 1e-4, 1e-1)])
+    assert bias[0].terms[0] == 0.0          # IC about 1 mA, VCE about 9 V: forward active
+    assert bias[1].terms[0] > 0.5           # a base current of 1 mA saturates it
+    b = kc.Builder("rc")
+    b.voltage_source("V1", "in", "0", 0.0, wave="pulse", args=[0, 5, 0, 1e-6, 1e-6, 5e-5, 1e-4])
+    b.resistor("R1", "in", "out", 1e3).resistor("RL", "out", "0", 3e3)
+    spec_t = analysis.TranSpec(step=1e-6, stop=4e-4)
+    eff = evo.evaluate([b.build()], [evo.tran_efficiency(spec_t, 1e-4, 4e-4, "RL")])[0]
+    assert eff.terms[0] == pytest.approx(1 - 3e3 / 4e3, rel=1e-6)  # the load's share of a resistive divider
+
