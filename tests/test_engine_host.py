@@ -208,3 +208,11 @@ def test_validation_of_controlled_and_mutual():
     b.voltage_source("V1", "a", "0", 1).inductor("L1", "a", "b", 1e-3).resistor("R1", "b", "0", 1)
     b.inductor("L2", "c", "0", 1e-3).resistor("R2", "c", "0", 1).mutual("K1", "L1", "L2", 1.5)
     assert analysis.validate(b.build()) is not None
+
+
+def test_untuned_plan_reports_no_choice(lib):
+    """ks_plan_tuned on a plan no autotune call has run for: KS_EINVAL, None in Python."""
+    from kronspice_gb300 import workloads
+    el, nn, vals = workloads.bjt_ce_batch(4, seed=0)
+    plan = analysis.Plan(el, nn, vals.shape[1])
+    assert plan.tuned(4) is None and plan.tuned(1 << 20) is None
