@@ -237,7 +237,7 @@ int validate(const ks_topology* t, const double* v, bool transient, std::string*
         if (!validate_wave(e, p + KS_SRC_P_ARGS, err)) return KS_EVALIDATE;
         break;
       case KS_ELEM_D: case KS_ELEM_Q: case KS_ELEM_M: {
-        int np = e.kind == KS_ELEM_D ? KS_D_NP : e.kind == KS_ELEM_Q ? KS_Q_NP : KS_M_NP;
+        const int np = e.kind == KS_ELEM_D ? (int)KS_D_NP : e.kind == KS_ELEM_Q ? (int)KS_Q_NP : (int)KS_M_NP;
         for (int i = 0; i < np; i++) if (!finite(p[i])) { *err = "circuit: bad model: parameter is not finite"; return KS_EVALIDATE; }
         if (e.kind == KS_ELEM_M) {  // validateMOSInstance, circuit/circuit.go:845-862
           for (int i = KS_M_P_L; i <= KS_M_P_MULT; i++) {
