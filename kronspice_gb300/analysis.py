@@ -458,6 +458,27 @@ def torn_plan(elements, n_nodes, n_values, torn):
     return piece, rows[:nr.value].copy(), mp.value, mb.value
 
 
+def sparse_lu_pattern(elements, n_nodes, values, step=0.0):
+    """The L + U slots of the host's fixed pivot sequence (ks_sparse_analyze): an
+    [n][n] bool matrix in step coordinates (row i: the row pivoting at step i,
+    column k: the column eliminated at step k), fill included."""
+    L = _lib.load()
+    el = np.ascontiguousarray(elements, dtype=ELEMENT_DTYPE)
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    topo = _lib.KsTopology(int(n_nodes), len(el), len(v), 0, el.ctypes.data)
+    n, slots = ctypes.c_int32(), ctypes.c_int64()
+    _check(L.ks_sparse_analyze(ctypes.byref(topo), v.ctypes.data, float(step), ctypes.byref(n), ctypes.byref(slots),
+                               None, None, None, None, None), "ks_sparse_analyze")
+    rowptr = np.zeros(n.value + 1, dtype=np.int32)
+    cols = np.zeros(slots.value, dtype=np.int32)
+    _check(L.ks_sparse_analyze(ctypes.byref(topo), v.ctypes.data, float(step), None, None, None, None, None,
+                               rowptr.ctypes.data, cols.ctypes.data), "ks_sparse_analyze")
+    out = np.zeros((n.value, n.value), dtype=bool)
+    for i in range(n.value):
+        out[i, cols[rowptr[i]:rowptr[i + 1]]] = True
+    return out
+
+
 def sparse_analysis(elements, n_nodes, values, step=0.0):
     """The host's sparse analysis of one circuit (ks_sparse_analyze, ks_sparse_pattern):
     (column order [n], pivot rows [n], pattern [n][n] bool); step > 0: the

@@ -744,6 +744,52 @@ extern "C" int kso_ac(const ks_topology* t, const double* values, const ks_optio
   return e;
 }
 
+// The left-looking LU's reach sets (solver/sparse.go:301-352: the depth-first
+// search of Gilbert & Peierls from the rows of A(:, q[k]), pivotal rows leading on
+// to the rows of their L column) for a fixed pivot sequence: prow[k] pivots at
+// step k.  A is n x n row-major (A rows, A columns); out[i * n + k] = 1 when the
+// row pivoting at step i is in the reach of step k (U above the diagonal, L
+// below).  Returns the first step whose pivot row is outside its reach, or -1.
+extern "C" int kso_reach_pattern(int n, const uint8_t* A, const int32_t* q, const int32_t* prow, uint8_t* out) {
+  std::vector<int> pinv(n, -1), mark(n, -1), stack(n), pstack(n);
+  for (int k = 0; k < n; k++) pinv[prow[k]] = k;
+  std::vector<std::vector<int>> lcol(n);  // rows of L(:, j): its reach's rows pivoting after j
+  std::fill(out, out + (size_t)n * n, 0);
+  int bad = -1;
+  for (int k = 0; k < n; k++) {
+    std::vector<int> reach;
+    for (int r = 0; r < n; r++) {
+      if (!A[(size_t)r * n + q[k]] || mark[r] == k) continue;
+      int head = 0;  // non-recursive DFS from r, as reach does
+      stack[0] = r;
+      while (head >= 0) {
+        const int v = stack[head];
+        const int j = pinv[v] < k ? pinv[v] : -1;  // pivotal before step k
+        if (mark[v] != k) { mark[v] = k; pstack[head] = 0; }
+        bool done = true;
+        if (j >= 0) {
+          for (int& p = pstack[head]; p < (int)lcol[j].size(); ) {
+            const int w = lcol[j][p++];
+            if (mark[w] == k) continue;
+            stack[++head] = w;
+            done = false;
+            break;
+          }
+        }
+        if (done) { head--; reach.push_back(v); }
+      }
+    }
+    bool has_pivot = false;
+    for (int v : reach) {
+      out[(size_t)pinv[v] * n + k] = 1;
+      if (pinv[v] > k) lcol[k].push_back(v);
+      has_pivot = has_pivot || v == prow[k];
+    }
+    if (!has_pivot && bad < 0) bad = k;
+  }
+  return bad;
+}
+
 extern "C" int kso_dc2(const ks_topology* t, const double* values, const ks_options* o, int src,
                        const double* vals, int npts, int src2, const double* vals2, int npts2, double* x_out,
                        double* i_out, char* err, int errlen) {

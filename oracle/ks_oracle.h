@@ -30,6 +30,7 @@ int kso_op(const ks_topology* t, const double* values, const ks_options* o, cons
 /* AC small-signal sweep (analysis/ac.go): x_out [nf][n] complex, interleaved re/im. */
 int kso_ac(const ks_topology* t, const double* values, const ks_options* o, const double* freqs, int nf,
            double* x_out, char* err, int errlen);
+int kso_reach_pattern(int n, const uint8_t* A, const int32_t* q, const int32_t* prow, uint8_t* out);
 int kso_dc2(const ks_topology* t, const double* values, const ks_options* o, int src, const double* vals,
             int npts, int src2, const double* vals2, int npts2, double* x_out, double* i_out, char* err, int errlen);
 int kso_dc(const ks_topology* t, const double* values, const ks_options* o, int src,

@@ -64,6 +64,7 @@ def lib():
         P = ctypes.c_void_p
         L.kso_op.argtypes = [P, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
         L.kso_dc.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, P, P, ctypes.c_char_p, ctypes.c_int]
+        L.kso_reach_pattern.argtypes = [ctypes.c_int, P, P, P, P]
         L.kso_dc2.argtypes = [P, P, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, P,
                               ctypes.c_char_p, ctypes.c_int]
         L.kso_tran.argtypes = [P, P, P, P, ctypes.c_int, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
@@ -212,6 +213,19 @@ def dc(pk, src, vals, opt=None):
     st = lib().kso_dc(pk.tref(), _ptr(pk.values), ctypes.byref(o), src, _ptr(vals), len(vals), _ptr(x),
                       _ptr(cur), err, 512)
     return st, x, cur, err.value.decode()
+
+
+def reach_pattern(A, q, prow):
+    """The reference's Gilbert-Peierls reach sets for a fixed pivot sequence:
+    (pattern [n][n] bool in step coordinates, first step whose pivot row is
+    outside its reach or -1)."""
+    A = np.ascontiguousarray(A, dtype=np.uint8)
+    n = A.shape[0]
+    q = np.ascontiguousarray(q, dtype=np.int32)
+    prow = np.ascontiguousarray(prow, dtype=np.int32)
+    out = np.zeros((n, n), dtype=np.uint8)
+    bad = lib().kso_reach_pattern(n, _ptr(A), _ptr(q), _ptr(prow), _ptr(out))
+    return out.astype(bool), bad
 
 
 def dc2(pk, src, vals, src2, vals2, opt=None):

@@ -122,3 +122,37 @@ def test_only_cutoff_inverters_differ():
         if not np.array_equal(q, oorder):
             differ.append(case["name"])
     assert sorted(differ) == ["mos1_cmos_vtc", "mos1_inv_tran"], differ
+
+
+def lu_and_reach(ckt, step=0.0):
+    el, vals, _ = ckt.pack()
+    q, prow, epat = analysis.sparse_analysis(el, ckt.n_nodes, vals, step=step)
+    lu = analysis.sparse_lu_pattern(el, ckt.n_nodes, vals, step=step)
+    reach, bad = orc.reach_pattern(epat, q, prow)
+    return lu, reach, bad
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_lu_pattern_is_the_reach_of_the_pivot_sequence(case):
+    """The engine's L + U slots (row-wise symbolic elimination on its fixed pivot
+    sequence) are the reference's Gilbert-Peierls reach sets (solver/sparse.go:
+    301-352) for the same pattern, column order and pivot rows, entry for entry,
+    at the operating point and, for the transient netlists, at their step."""
+    ckt = kc.from_dict(case["circuit"])
+    lu, reach, bad = lu_and_reach(ckt)
+    assert bad == -1 and np.array_equal(lu, reach)
+    for a in case["circuit"]["analyses"]:
+        if a["kind"] == "tran":
+            lu, reach, bad = lu_and_reach(ckt, a["step"])
+            assert bad == -1 and np.array_equal(lu, reach)
+
+
+def test_lu_patterns_of_random_netlists_are_their_reach():
+    fill = 0
+    for ckt in workloads.random_netlists(120, seed=9, nodes=(10, 200)):
+        lu, reach, bad = lu_and_reach(ckt)
+        assert bad == -1 and np.array_equal(lu, reach)
+        el, vals, _ = ckt.pack()
+        q, prow, epat = analysis.sparse_analysis(el, ckt.n_nodes, vals)
+        fill += int(lu.sum()) - int(epat[np.ix_(prow, q)].sum())
+    assert fill > 1000  # the factors' fill is part of what is compared
