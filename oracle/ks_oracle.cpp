@@ -843,7 +843,8 @@ extern "C" int kso_tran(const ks_topology* t, const double* values, const ks_tra
 // The sparse backend's column order after an analysis (solver/sparse.go:154-187:
 // minimumDegree of the pattern every load of the run stamped) and that pattern.
 extern "C" int kso_sparse_order(const ks_topology* t, const double* values, const ks_tran_spec* spec,
-                                const ks_options* o, int32_t* n_out, int32_t* order, uint8_t* pattern) {
+                                const ks_options* o, int32_t* n_out, int32_t* order, uint8_t* pattern,
+                                int32_t* pivots) {
   Sim s;
   ks_options oo = o ? *o : ks_options{};
   oo.backend = KS_BACKEND_SPARSE;
@@ -861,6 +862,9 @@ extern "C" int kso_sparse_order(const ks_topology* t, const double* values, cons
   if (!sp) return KS_STATUS_NOT_RUN;
   if (n_out) *n_out = s.n;
   if (order) for (int k = 0; k < s.n; k++) order[k] = sp->q[k];
+  // the pivot rows of the run's last factorization, as A rows (the factor holds
+  // rows in the column order's symmetric permutation)
+  if (pivots) for (int k = 0; k < s.n; k++) pivots[k] = sp->valid ? sp->q[sp->prow[k]] : -1;
   if (pattern) {
     std::fill(pattern, pattern + (size_t)s.n * s.n, 0);
     for (size_t k = 0; k < sp->ri.size(); k++) pattern[(size_t)sp->ri[k] * s.n + sp->ci[k]] = 1;

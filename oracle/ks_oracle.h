@@ -91,7 +91,8 @@ int kso_torn_plan(const ks_topology* t, const double* values, const int32_t* pai
  * n x n bytes); returns the analysis's status.  kso_min_degree: minimumDegree
  * (solver/sparse.go:412-452) of a given pattern. */
 int kso_sparse_order(const ks_topology* t, const double* values, const ks_tran_spec* spec, const ks_options* o,
-                     int32_t* n, int32_t* order, uint8_t* pattern);
+                     int32_t* n, int32_t* order, uint8_t* pattern,
+                     int32_t* pivots);
 void kso_min_degree(int n, const uint8_t* pattern, int32_t* order);
 
 /* Unknown count and layout of one circuit (device Setup), for the tests. */

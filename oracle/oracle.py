@@ -69,7 +69,7 @@ def lib():
                               ctypes.c_char_p, ctypes.c_int]
         L.kso_tran.argtypes = [P, P, P, P, ctypes.c_int, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
         L.kso_op_results.argtypes = [P, P, P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
-        L.kso_sparse_order.argtypes = [P, P, P, P, P, P, P]
+        L.kso_sparse_order.argtypes = [P, P, P, P, P, P, P, P]
         L.kso_min_degree.argtypes = [ctypes.c_int, P, P]
         L.kso_min_degree.restype = None
         L.kso_tran_results.argtypes = [P, P, P, P, ctypes.c_int, P, P, P, P, P, P, P, P, ctypes.c_char_p,
@@ -183,15 +183,19 @@ def tran_results(pk, spec, opt=None, capacity=200000):
             err.value.decode())
 
 
-def sparse_order(pk, spec=None, opt=None):
+def sparse_order(pk, spec=None, opt=None, pivots=False):
     """The sparse backend's column order after an operating point (or a transient
-    when spec is given) and the pattern it ordered: (status, order [n], pattern [n][n] bool)."""
+    when spec is given) and the pattern it ordered: (status, order [n], pattern [n][n] bool)
+    and, with pivots, the A rows its last factorization pivoted on per step."""
     n, _ = unknowns(pk)
     order = np.zeros(n, dtype=np.int32)
     pat = np.zeros((n, n), dtype=np.uint8)
+    piv = np.zeros(n, dtype=np.int32)
     o = opt or options()
     st = lib().kso_sparse_order(pk.tref(), _ptr(pk.values), None if spec is None else ctypes.byref(spec),
-                                ctypes.byref(o), None, _ptr(order), _ptr(pat))
+                                ctypes.byref(o), None, _ptr(order), _ptr(pat), _ptr(piv) if pivots else None)
+    if pivots:
+        return st, order, pat.astype(bool), piv
     return st, order, pat.astype(bool)
 
 

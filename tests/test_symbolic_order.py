@@ -156,3 +156,24 @@ def test_lu_patterns_of_random_netlists_are_their_reach():
         q, prow, epat = analysis.sparse_analysis(el, ckt.n_nodes, vals)
         fill += int(lu.sum()) - int(epat[np.ix_(prow, q)].sum())
     assert fill > 1000  # the factors' fill is part of what is compared
+
+
+def test_pivot_rows_of_the_golden_operating_points():
+    """The engine's pivot rows (chosen once, on a representative matrix) are the
+    ones the reference's last factorization of the operating point pivoted on
+    (threshold partial pivoting with the diagonal preferred, solver/sparse.go:
+    256-281) on every golden netlist whose column order is the reference's.  On
+    circuits whose junctions or companions change which entry dominates a column,
+    they may differ: a fixed pivot failing its run-time threshold hands the solve
+    to partial pivoting, so results do not depend on it."""
+    compared = 0
+    for case in CASES:
+        ckt = kc.from_dict(case["circuit"])
+        el, vals, _ = ckt.pack()
+        st, order, _, piv = orc.sparse_order(orc.Packed(el, ckt.n_nodes, vals), None, None, pivots=True)
+        q, prow, _ = analysis.sparse_analysis(el, ckt.n_nodes, vals)
+        if st != 0 or not np.array_equal(order, q):
+            continue
+        assert np.array_equal(piv, prow), case["name"]
+        compared += 1
+    assert compared >= 40
