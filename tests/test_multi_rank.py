@@ -72,3 +72,39 @@ def test_two_ranks_share_the_work_and_time_the_slowest(tmp_path):
     # the whole job's rate as the bench reports it: every rank's units over the slowest time
     value = world * B / res[0][1]
     assert value <= world * B / min(mine)
+
+
+def rank_dies(rank, world, port, out_dir):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    import datetime
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=5))
+    if rank == 1:
+        os._exit(3)  # leaves between steps, with nothing in flight
+    t0 = time.perf_counter()
+    try:
+        dist.barrier()
+        outcome = "returned"
+    except RuntimeError as e:
+        outcome = "error: " + str(e).splitlines()[0][:200]
+    with open(os.path.join(out_dir, "rank0.txt"), "w") as f:
+        f.write("%s\n%.3f\n" % (outcome, time.perf_counter() - t0))
+
+
+def test_a_rank_that_leaves_ends_the_others_collective_with_an_error(tmp_path):
+    """A rank that exits between steps: the surviving rank's next collective ends
+    with an error within the process group's timeout instead of waiting for ever."""
+    ctx = mp.get_context("spawn")
+    port = free_port()
+    procs = [ctx.Process(target=rank_dies, args=(r, 2, port, str(tmp_path))) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+    for p in procs:
+        if p.is_alive():
+            p.kill()
+            pytest.fail("a rank did not finish")
+    assert procs[1].exitcode == 3
+    outcome, secs = open(os.path.join(tmp_path, "rank0.txt")).read().split("\n")[:2]
+    assert outcome.startswith("error"), outcome
+    assert float(secs) < 60
