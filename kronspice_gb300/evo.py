@@ -775,6 +775,8 @@ def evaluate(circuits, objectives, options=None, values=None, capacity=20000, pa
             if isinstance(err, analysis.ErrFloatingNode) and analysis.validate_packed(el, c.n_nodes, vals, True) is None:
                 err = None
             packed[i] = (el, vals)
+            # the names too: a group's objectives read node and element names once for all its rows
+            key = (key, tuple(c.node_names), tuple(e.name.lower() for e in c.elements))
         except analysis.KronspiceError as e:
             err = e
         except (ValueError, KeyError) as e:  # the circuit does not pack: a bad value or model

@@ -324,3 +324,18 @@ def test_mask_bias_parts_and_transient_efficiency(monkeypatch):
     eff = evo.evaluate([b.build()], [evo.tran_efficiency(spec_t, 1e-4, 4e-4, "RL")])[0]
     assert eff.terms[0] == pytest.approx(1 - 3e3 / 4e3, rel=1e-6)  # the load's share of a resistive divider
 
+
+
+def test_same_structure_different_names_are_not_grouped(monkeypatch):
+    """Two candidates whose topologies match index for index but whose nodes are
+    named differently are scored apart: each reads its own names."""
+    monkeypatch.setattr(evo.analysis, "Batch", OracleBatch)
+    a = kc.Builder("a")
+    a.voltage_source("V1", "in", "0", 2.0).resistor("R1", "in", "out", 1e3).resistor("R2", "out", "0", 1e3)
+    b = kc.Builder("b")
+    b.voltage_source("V1", "x", "0", 2.0).resistor("R1", "x", "y", 1e3).resistor("R2", "y", "0", 1e3)
+    ca, cb = a.build(), b.build()
+    assert ca.pack()[2] == cb.pack()[2]  # the same topology key
+    out = evo.evaluate([ca, cb], [evo.op_voltage("out", 1.0)])
+    assert out[0].failure == "" and out[0].terms[0] == pytest.approx(0.0, abs=1e-12)
+    assert out[1].failure == "no-measurement"
