@@ -320,6 +320,8 @@ class Batch:
         v = np.ascontiguousarray(values, dtype=np.float64)
         if v.ndim != 1 or len(v) == 0:
             raise ValueError("dc_sweep: values must be a non-empty 1-D array")
+        if src2 is not None and (values2 is None or len(values2) == 0):
+            raise ValueError("dc_sweep: an outer source needs a non-empty values2")
         v2 = None if src2 is None else np.ascontiguousarray(values2, dtype=np.float64)
         total = len(v) * (1 if v2 is None else len(v2))
         x = np.zeros((self.n_circ, total, self.plan.n))
