@@ -365,7 +365,9 @@ def run_reference(args):
         value = statistics.median(v)
         print(json.dumps({"impl": "reference", "metric": "candidates scored/s (batched evaluator: OP + AC objectives)",
                           "value": value, "unit": "candidates/s", "n_gpus": 1, "steps": args.steps,
-                          "warmup": args.warmup, "higher_is_better": True, "data": "synthetic (seeded candidates)",
+                          "warmup": args.warmup, "ms_per_step": len(pop) / value * 1e3, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic (seeded candidates)",
                           "config": {"workload": "evo_lowpass_%d" % args.n_circ},
                           "cpu_baseline": {"value": value, "unit": "candidates/s", "cores": vals[-1][2],
                                            "kind": "port", "sample": "%d candidates a step" % len(pop)},
